@@ -1,0 +1,390 @@
+"""Benchmark: events/s of the fused phase-space kernel on GB300.
+
+Default workload (one GPU): e+e- -> t tbar -> b l nu bbar q q' at sqrt(s) = 1 TeV, plain
+FP64, 1e7 events per step, 14 Philox4x32-10 x per event resident in HBM.  A step is one
+forward generation of all events (one kernel launch).  x (1.12 GB) and the outputs
+(2.1 GB) are far larger than L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+For N > 1 (torchrun) every rank generates its own event range on its own GPU (replicas,
+no collective on the data path); value is the events of all ranks / the slowest rank's
+time.  --impl reference times the reference CPU path on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "events/s on 1 GB300: FP32-mixed batched vs plain FP64 at stated momentum error"
+SEED = 1234
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def workload(name: str):
+    from gpu_phs_gb300 import processes as P
+    if name == "tt":
+        return P.tt(), 10_000_000
+    if name == "ww":
+        return P.ww(), 1_000_000
+    if name == "precision":
+        return P.precision(), 1 << 24
+    raise ValueError(name)
+
+
+def bytes_per_event(proc) -> int:
+    """Algorithmic HBM bytes per event: x row read + momenta, factor, volume, ok written."""
+    return 8 * proc.n_x + 32 * proc.n_out + 8 + 8 + 1
+
+
+def flops_per_event(proc) -> float:
+    """FP64 operations of the minimal algorithm per event, one convention for all
+    workloads: add/sub/mul/div/sqrt = 1, FMA = 2, each transcendental call = 1.  It
+    undercounts library math (tan, exp, sincos expand to tens of operations), so the
+    FP64-pipe fraction is also measured directly with ncu."""
+    from gpu_phs_gb300.processes import MAP_NO, MAP_SCHANNEL, MAP_STEP_E, MAP_STEP_H
+    R = (1 << proc.n_out) - 1
+    d1, d2, hc, mid = proc.d1[0], proc.d2[0], proc.has_children[0], proc.map_ids[0]
+    msq_cost = {MAP_NO: 5, MAP_SCHANNEL: 11, MAP_STEP_E: 12, MAP_STEP_H: 12}
+    total = 0.0
+
+    def internal(code):
+        return hc[code - 1] != 0
+
+    def walk(code, root):
+        nonlocal total
+        k = (d1[code - 1], d2[code - 1])
+        if not root:
+            total += msq_cost.get(int(mid[code - 1]), 7) + 1       # mapping + sqrt(msq)
+        total += 12                                                  # Kallen, p_decay, factor
+        total += 21                                                  # bg, gamma, sincos, ct, L1
+        if not root:
+            total += 80 if any(internal(c) for c in k) else 40       # L0 * L1 (structured)
+        for c in k:
+            if internal(c):
+                walk(c, False)
+            else:
+                total += 15                                          # E and L * (E,0,0,p)
+
+    walk(R, True)
+    return total
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-i", str(self.device), "-lms", "200"], stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        self.tmp.flush()
+        self.tmp.seek(0)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.tmp.read().splitlines():
+            f = [t.strip() for t in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.tmp.name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_reference_rate(proc, sqrts, seconds: float, max_events: int, prefer_ref: bool = True):
+    """Events/s of the reference CPU path (oracle/_ref if it loads here, else the C
+    restatement) on all host threads, on the first events of the same Philox stream."""
+    from gpu_phs_gb300.philox import uniform_x
+    from oracle import oracle
+    threads = os.cpu_count() or 1
+    kind = "port"
+    gen = None
+    if prefer_ref and oracle.ref_available():
+        try:
+            gen = oracle.RefCPU(proc, sqrts)
+            kind = "reference"
+        except OSError:
+            gen = None
+    if gen is None:
+        gen = oracle.Oracle(proc, sqrts)
+    n = 65536
+    x = uniform_x(SEED, n, proc.n_x)
+    t = time.perf_counter()
+    gen.generate(x, threads=threads)
+    rate = n / (time.perf_counter() - t)
+    n = int(min(max_events, max(4096, rate * seconds / 4)))
+    x = uniform_x(SEED, n, proc.n_x)
+    done, t0 = 0, time.perf_counter()
+    while True:
+        gen.generate(x, threads=threads)
+        done += n
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return done / el, kind, threads, n, gen, x
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    proc, _ = workload(args.config)
+    from gpu_phs_gb300.philox import uniform_x
+    from oracle import oracle
+    threads = os.cpu_count() or 1
+    kind = "port"
+    gen = None
+    if oracle.ref_available():
+        try:
+            gen = oracle.RefCPU(proc, proc.sqrts)
+            kind = "reference"
+        except OSError:
+            gen = None
+    if gen is None:
+        gen = oracle.Oracle(proc, proc.sqrts)
+    # size each step so that warmup + steps stay within about a minute
+    n = 65536
+    x = uniform_x(SEED, n, proc.n_x)
+    t = time.perf_counter()
+    gen.generate(x, threads=threads)
+    rate = n / (time.perf_counter() - t)
+    n = int(min(1 << 21, max(4096, rate * 60.0 / max(1, args.steps + args.warmup))))
+    x = uniform_x(SEED, n, proc.n_x)
+    for _ in range(args.warmup):
+        gen.generate(x, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        gen.generate(x, threads=threads)
+    el = time.perf_counter() - t0
+    value = n * args.steps / el
+    sample = f"{n} events of the {proc.name} workload per step (first events of the Philox stream)"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "events/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (Philox4x32-10 x)",
+        "config": {"workload": proc.name, "n_events_per_step": n, "n_x": proc.n_x,
+                   "n_out": proc.n_out, "sqrts_gev": proc.sqrts,
+                   "path": "reference phs_cpu.cpp set_msq_cpu + set_angles_cpu" if kind == "reference"
+                   else "C restatement of phs_cpu.cpp (oracle/phs_oracle.c)"},
+        "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+
+    from gpu_phs_gb300 import _lib
+    from gpu_phs_gb300.api import PhaseSpace, philox_fill
+
+    proc, n = workload(args.config)
+    if args.events:
+        n = args.events
+    ps = PhaseSpace(proc, proc.sqrts / 2, proc.sqrts / 2)
+    x = torch.empty((n, proc.n_x), dtype=torch.float64, device="cuda")
+    philox_fill(x, n, proc.n_x, SEED, first_event=rank * n)
+    out = ps.alloc(n)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        ps.generate(x, out=out)
+    torch.cuda.synchronize()
+    ok_frac = out.ok.double().mean().item()
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    with Clocks(dev) as clk:
+        t_all0 = torch.cuda.Event(enable_timing=True)
+        t_all1 = torch.cuda.Event(enable_timing=True)
+        t_all0.record(stream)
+        for k in range(args.steps):
+            starts[k].record(stream)
+            ps.generate(x, out=out)
+            ends[k].record(stream)
+        t_all1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    total_ms = t_all0.elapsed_time(t_all1)
+    kern_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_per_step = t.item() / args.steps
+    value = world * n / (ms_per_step * 1e-3)
+    clocks = clk.summary()
+
+    # roofline of the forward kernel (one launch per step)
+    hbm_peak, peak_kind = peaks()
+    launch_ms = statistics.mean(kern_ms)
+    bpe = bytes_per_event(proc)
+    achieved_gbs = bpe * n / (launch_ms * 1e-3) / 1e9
+    fpe = flops_per_event(proc)
+    lib = _lib.load()
+    import ctypes as C
+    g64 = C.c_double()
+    _lib.check(lib.phs_measure_fma_peak(1, C.byref(g64)))
+    fp64_peak = g64.value
+    fp64_achieved = fpe * n / (launch_ms * 1e-3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        with open(prof) as fh:
+            tj = json.load(fh)
+        per_ev = tj.get(proc.name, {}).get("dram_bytes_per_event")
+        if per_ev:
+            traffic = per_ev * n
+
+    # end to end through the host-pointer C entry point (pinned buffers)
+    e2e = None
+    if not args.no_e2e:
+        xh = torch.empty((n, proc.n_x), dtype=torch.float64).pin_memory()
+        xh.copy_(x.cpu())
+        outh = type(out)(torch.empty((n, proc.n_out, 4), dtype=torch.float64).pin_memory(),
+                         torch.empty(n, dtype=torch.float64).pin_memory(),
+                         torch.empty(n, dtype=torch.float64).pin_memory(),
+                         torch.empty(n, dtype=torch.uint8).pin_memory())
+        e2e_steps = max(1, min(args.steps, 10))
+        for _ in range(max(1, min(args.warmup, 3))):
+            ps.generate_host(xh, out=outh)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            ps.generate_host(xh, out=outh)
+        el = time.perf_counter() - t0
+        te = torch.tensor([el], device="cuda", dtype=torch.float64)
+        if world > 1:
+            dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        e2e = {"value": world * n * e2e_steps / te.item(), "unit": "events/s",
+               "h2d_bytes_per_step": n * proc.n_x * 8,
+               "d2h_bytes_per_step": n * (32 * proc.n_out + 8 + 8 + 1),
+               "path": "phs_generate_host (C ABI), pinned host buffers, 1 Mi-event chunks on 2 streams",
+               "steps": e2e_steps}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, kind, threads, sample_n, _, _ = cpu_reference_rate(proc, proc.sqrts, args.cpu_seconds,
+                                                                  1 << 21)
+        cpu = {"value": rate, "unit": "events/s", "cores": threads, "kind": kind,
+               "sample": f"{sample_n} events of the same workload, repeated for "
+                         f"{args.cpu_seconds:.0f} s on all host threads"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (Philox4x32-10 x, seed 1234, in HBM)",
+            "config": {"workload": proc.name, "variant": "plain FP64, fused persistent kernel",
+                       "n_events_per_gpu": n, "n_x": proc.n_x, "n_out": proc.n_out,
+                       "sqrts_gev": proc.sqrts, "parallelism": f"replicas x{world}",
+                       "l2": "inputs (x 1.12 GB) and outputs larger than L2; no flush"},
+            "ok_fraction": ok_frac,
+            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved_gbs / hbm_peak, "traffic": traffic,
+                         "peak_kind": peak_kind, "bytes_per_event": bpe,
+                         "kernel_ms": launch_ms,
+                         "fp64": {"achieved_gflops": fp64_achieved, "peak_gflops": fp64_peak,
+                                  "frac": fp64_achieved / fp64_peak, "flops_per_event": fpe,
+                                  "peak_kind": "measured (phs_measure_fma_peak, DFMA chains)"}},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": args.steps,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", choices=["tt", "ww", "precision"], default="tt")
+    ap.add_argument("--events", type=int, default=0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,197 @@
+"""Python front end of libgpuphs, over its C ABI (include/gpu_phs.h).
+
+PyTorch supplies device memory and streams only; every computation runs in the CUDA
+library.  ``PhaseSpace`` mirrors the reference's generate call gen_phs_from_x_gpu
+(phs.cu:1333) for one process, ``Batch`` runs many processes in one launch.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from ._lib import check, load
+from .processes import Process
+
+
+def _ptr(t) -> Optional[int]:
+    if t is None:
+        return None
+    if isinstance(t, np.ndarray):
+        return t.ctypes.data
+    return t.data_ptr()
+
+
+def _stream(stream) -> Optional[int]:
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+@dataclass
+class Events:
+    p: "object"       # [n, n_out, 4] float64
+    factor: "object"  # [n] float64
+    volume: "object"  # [n] float64
+    ok: "object"      # [n] uint8
+
+
+class PhaseSpace:
+    """One process on the current CUDA device."""
+
+    def __init__(self, proc: Process, E1: Optional[float] = None, E2: Optional[float] = None):
+        lib = load()
+        self.proc = proc
+        self._keep = [np.ascontiguousarray(a, dt) for a, dt in (
+            (proc.d1, np.int32), (proc.d2, np.int32), (proc.has_children, np.int32),
+            (proc.friends, np.int32), (proc.map_ids, np.int32), (proc.map_masses, np.float64),
+            (proc.map_widths, np.float64), (proc.flv_masses, np.float64),
+            (proc.flv_widths, np.float64))]
+        h = C.c_void_p()
+        check(lib.phs_process_create(C.byref(h), proc.n_in, proc.n_out, proc.n_channels,
+                                     proc.n_x, *[_ptr(a) for a in self._keep]))
+        self.h = h
+        if E1 is not None:
+            self.set_beams(E1, E2 if E2 is not None else E1)
+
+    def set_beams(self, E1: float, E2: float) -> None:
+        check(load().phs_process_set_beams(self.h, float(E1), float(E2)))
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            load().phs_process_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        v = [C.c_int() for _ in range(5)]
+        check(load().phs_process_info(self.h, *[C.byref(i) for i in v]))
+        return dict(zip(("n_in", "n_out", "n_channels", "n_x", "stack_depth"), [i.value for i in v]))
+
+    def alloc(self, n: int, device="cuda") -> Events:
+        import torch
+        return Events(torch.empty((n, self.proc.n_out, 4), dtype=torch.float64, device=device),
+                      torch.empty(n, dtype=torch.float64, device=device),
+                      torch.empty(n, dtype=torch.float64, device=device),
+                      torch.empty(n, dtype=torch.uint8, device=device))
+
+    @staticmethod
+    def _counts(counts, n_channels: int, n: int) -> Optional[np.ndarray]:
+        if counts is None:
+            if n_channels != 1:
+                raise ValueError("counts are required for a multi-channel process")
+            return None
+        c = np.ascontiguousarray(counts, np.int64)
+        if c.shape != (n_channels,):
+            raise ValueError(f"counts must have shape ({n_channels},)")
+        return c
+
+    def generate(self, x, counts=None, out: Optional[Events] = None, stream=None) -> Events:
+        """x: CUDA float64 [n, n_x]; events grouped by channel with ``counts`` per channel."""
+        n = int(x.shape[0])
+        if x.dtype.itemsize != 8 or not x.is_cuda or not x.is_contiguous():
+            raise ValueError("x must be a contiguous CUDA float64 tensor")
+        if x.dim() != 2 or x.shape[1] != self.proc.n_x:
+            raise ValueError(f"x must be [n, {self.proc.n_x}]")
+        out = out or self.alloc(n, x.device)
+        c = self._counts(counts, self.proc.n_channels, n)
+        check(load().phs_generate_device(self.h, n, _ptr(c), _ptr(x), _ptr(out.p),
+                                         _ptr(out.factor), _ptr(out.volume), _ptr(out.ok),
+                                         _stream(stream)))
+        return out
+
+    def generate_beams(self, x, E1, E2, counts=None, out: Optional[Events] = None,
+                       stream=None) -> Events:
+        """Per-event beam energies E1[n], E2[n] (CUDA float64)."""
+        n = int(x.shape[0])
+        out = out or self.alloc(n, x.device)
+        c = self._counts(counts, self.proc.n_channels, n)
+        check(load().phs_generate_beams_device(self.h, n, _ptr(c), _ptr(E1), _ptr(E2), _ptr(x),
+                                               _ptr(out.p), _ptr(out.factor), _ptr(out.volume),
+                                               _ptr(out.ok), _stream(stream)))
+        return out
+
+    def generate_host(self, x, counts=None, out: Optional[Events] = None) -> Events:
+        """Host (ideally pinned) tensors or arrays in and out; synchronous."""
+        import torch
+        n = int(x.shape[0])
+        if out is None:
+            out = Events(torch.empty((n, self.proc.n_out, 4), dtype=torch.float64),
+                         torch.empty(n, dtype=torch.float64), torch.empty(n, dtype=torch.float64),
+                         torch.empty(n, dtype=torch.uint8))
+        c = self._counts(counts, self.proc.n_channels, n)
+        check(load().phs_generate_host(self.h, n, _ptr(c), _ptr(x), _ptr(out.p), _ptr(out.factor),
+                                       _ptr(out.volume), _ptr(out.ok)))
+        return out
+
+
+class Batch:
+    """Many processes (uneven n_out, n_x and counts) in one persistent launch."""
+
+    def __init__(self, spaces: Sequence[PhaseSpace]):
+        self.spaces = list(spaces)
+        arr = (C.c_void_p * len(self.spaces))(*[s.h.value for s in self.spaces])
+        h = C.c_void_p()
+        check(load().phs_batch_create(C.byref(h), len(self.spaces), C.cast(arr, C.c_void_p)))
+        self.h = h
+        self.n_outs: List[int] = []
+        self.n_xs: List[int] = []
+        for s in self.spaces:
+            self.n_outs += [s.proc.n_out] * s.proc.n_channels
+            self.n_xs += [s.proc.n_x] * s.proc.n_channels
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            load().phs_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def n_channels(self) -> int:
+        return len(self.n_outs)
+
+    def offsets(self, counts):
+        c = np.ascontiguousarray(counts, np.int64)
+        xo = np.zeros(self.n_channels + 1, np.int64)
+        po = np.zeros(self.n_channels + 1, np.int64)
+        check(load().phs_batch_offsets(self.h, _ptr(c), _ptr(xo), _ptr(po)))
+        return xo, po
+
+    def generate(self, x, counts, p=None, factor=None, volume=None, ok=None, stream=None):
+        """x: flat CUDA float64 of all channels' x rows; returns flat p and per-event arrays."""
+        import torch
+        c = np.ascontiguousarray(counts, np.int64)
+        n = int(c.sum())
+        xo, po = self.offsets(c)
+        dev = x.device
+        p = p if p is not None else torch.empty(int(po[-1]), dtype=torch.float64, device=dev)
+        factor = factor if factor is not None else torch.empty(n, dtype=torch.float64, device=dev)
+        volume = volume if volume is not None else torch.empty(n, dtype=torch.float64, device=dev)
+        ok = ok if ok is not None else torch.empty(n, dtype=torch.uint8, device=dev)
+        check(load().phs_batch_generate_device(self.h, _ptr(c), _ptr(x), _ptr(p), _ptr(factor),
+                                               _ptr(volume), _ptr(ok), _stream(stream)))
+        return p, factor, volume, ok
+
+
+def philox_fill(x, n_events: int, n_x: int, seed: int, first_event: int = 0, stream=None):
+    """Fills CUDA float64 x[n_events * n_x] with the Philox stream (gpu_phs_gb300/philox.py)."""
+    check(load().phs_philox_fill(_ptr(x), n_events, n_x, seed, first_event, _stream(stream)))
+    return x
+
+
+def philox_x(n_events: int, n_x: int, seed: int, first_event: int = 0, device="cuda"):
+    import torch
+    x = torch.empty((n_events, n_x), dtype=torch.float64, device=device)
+    return philox_fill(x, n_events, n_x, seed, first_event)

@@ -1,0 +1,79 @@
+"""Builds libgpuphs.so in-tree (gpu_phs_gb300/libgpuphs.so) for sm_103a.
+
+Device code is compiled by nvcc for exactly one target
+(-gencode arch=compute_103a,code=sm_103a); host code by g++ with -ffp-contract=off so
+that the mapping constants equal the reference CPU path's on every host (x86-64 and
+aarch64).  Translation units compile in parallel.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libgpuphs.so")
+ROOT = os.path.dirname(HERE)
+
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+CU_SOURCES = ["phs_kernels.cu"]
+CPP_SOURCES = ["phs_compile.cpp", "phs_api.cpp"]
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build step failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return r.stdout + r.stderr
+
+
+def _stale(out: str, deps) -> bool:
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(verbose: bool = False, force: bool = False) -> str:
+    """Compile and link; returns the library path.  Raises RuntimeError on failure."""
+    os.makedirs(BUILD, exist_ok=True)
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    headers.append(os.path.join(ROOT, "include", "gpu_phs.h"))
+    inc = ["-I", os.path.join(ROOT, "include"), "-I", CSRC, "-I", os.path.join(CUDA_HOME, "include")]
+    jobs, objs = [], []
+    for src in CU_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src + ".o")
+        objs.append(o)
+        if force or _stale(o, [s] + headers):
+            jobs.append([NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                         "-Xptxas", "-v", *inc, "-c", s, "-o", o])
+    for src in CPP_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src + ".o")
+        objs.append(o)
+        if force or _stale(o, [s] + headers):
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
+                         "-Wall", "-Wno-unused-function", *inc, "-c", s, "-o", o])
+    with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        logs = list(ex.map(_run, jobs))
+    if verbose:
+        for lg in logs:
+            sys.stdout.write(lg)
+    if force or jobs or _stale(LIB, objs):
+        tmp = LIB + ".tmp"
+        _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart",
+              "-Xlinker", "-rpath", "-Xlinker", os.path.join(CUDA_HOME, "lib64")])
+        shutil.move(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv, force="-f" in sys.argv))

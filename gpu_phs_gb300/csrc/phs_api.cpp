@@ -1,0 +1,906 @@
+// phs_api.cpp -- the C ABI of libgpuphs (include/gpu_phs.h): handle API, batches, the
+// chunk-pipelined host path, and the Whizard binding (whizard_gpu_phs.cpp:12-249).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gpu_phs.h"
+#include "phs_device.h"
+#include "phs_host.h"
+
+// ---------------------------------------------------------------------------- errors
+static thread_local std::string g_err;
+
+static int fail(int code, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CUDA_TRY(call)                                                                    \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(PHS_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));          \
+  } while (0)
+
+extern "C" const char *phs_last_error(void) { return g_err.c_str(); }
+extern "C" const char *phs_version(void) { return "gpu_phs_gb300 0.1 (sm_103a, fp64 fused)"; }
+
+// ------------------------------------------------------------------- device buffers
+namespace {
+
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t cap = 0;
+  int reserve(size_t bytes) {
+    if (bytes <= cap) return PHS_OK;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&ptr, bytes);
+    if (e != cudaSuccess) {
+      ptr = nullptr;
+      return fail(PHS_ERR_ALLOC, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    cap = bytes;
+    return PHS_OK;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+  }
+  template <class T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+// Segment list of one launch, built from per-channel event counts.
+struct Segments {
+  std::vector<PhsSegment> host;
+  DevBuf dev;
+  std::vector<PhsSegment> uploaded;  // content of dev
+  int64_t n_tiles = 0;
+  int64_t n_events = 0;
+};
+
+struct ChanLayout {  // per launched channel: shape of its x and p rows
+  int n_out;
+  int x_stride;
+};
+
+int build_segments(Segments &S, const int64_t *counts, int n_channels,
+                   const std::vector<ChanLayout> &lay, int64_t ev0, int64_t x0, int64_t p0,
+                   bool whizard_cols) {
+  S.host.clear();
+  int64_t ev = ev0, x = x0, p = p0, tile = 0;
+  for (int c = 0; c < n_channels; c++) {
+    const int64_t n = counts[c];
+    if (n < 0) return fail(PHS_ERR_INVALID_ARG, "channel %d has a negative event count", c);
+    if (n == 0) continue;
+    PhsSegment g;
+    memset(&g, 0, sizeof g);
+    g.channel = c;
+    g.n_out = lay[c].n_out;
+    g.ev_begin = ev;
+    g.ev_count = n;
+    g.x_base = x;
+    g.p_base = p;
+    g.tile_begin = tile;
+    g.x_stride = lay[c].x_stride;
+    g.factor_col = whizard_cols ? c : 0;
+    S.host.push_back(g);
+    tile += (n + 31) / 32;
+    ev += n;
+    x += n * lay[c].x_stride;
+    p += n * 4 * lay[c].n_out;
+  }
+  S.n_tiles = tile;
+  S.n_events = ev - ev0;
+  return PHS_OK;
+}
+
+// Fills the launch's segment fields; uploads the table when it does not fit the params.
+int attach_segments(Segments &S, PhsLaunch &a, cudaStream_t stream) {
+  a.n_segments = (int32_t)S.host.size();
+  a.n_tiles = S.n_tiles;
+  a.segments = nullptr;
+  if (S.host.size() <= PHS_INLINE_SEGS) {
+    std::copy(S.host.begin(), S.host.end(), a.seg_inline);
+    return PHS_OK;
+  }
+  const size_t bytes = S.host.size() * sizeof(PhsSegment);
+  bool same = S.uploaded.size() == S.host.size() &&
+              memcmp(S.uploaded.data(), S.host.data(), bytes) == 0;
+  if (!same) {
+    int rc = S.dev.reserve(bytes);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(S.dev.ptr, S.host.data(), bytes, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    S.uploaded = S.host;
+  }
+  a.segments = S.dev.as<PhsSegment>();
+  return PHS_OK;
+}
+
+int sm_count(int device) {
+  static int cached[64] = {0};
+  if (device >= 0 && device < 64 && cached[device]) return cached[device];
+  int n = 0;
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device);
+  if (n <= 0) n = 1;
+  if (device >= 0 && device < 64) cached[device] = n;
+  return n;
+}
+
+int grid_for(int64_t n_tiles, int device, int stack_depth, bool per_event) {
+  const int warps_per_block = PHS_FWD_BLOCK / 32;
+  int64_t want = (n_tiles + warps_per_block - 1) / warps_per_block;
+  int64_t cap = (int64_t)sm_count(device) * phs_forward_blocks_per_sm(stack_depth, per_event);
+  return (int)std::max<int64_t>(1, std::min(want, cap));
+}
+
+// Restores the caller's current device on scope exit.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+}  // namespace
+
+// -------------------------------------------------------------------------- process
+struct phs_process {
+  phs::Process p;
+  int device = 0;
+  bool beams = false;
+  double E1 = 0, E2 = 0;
+  std::vector<PhsChannel> prog;
+  std::vector<ChanLayout> lay;
+  int stack_depth = 0;
+  DevBuf d_prog;
+  Segments segs;
+  // host-path pipeline
+  static const int kStreams = 2;
+  cudaStream_t streams[kStreams] = {nullptr, nullptr};
+  DevBuf bx[kStreams], bp[kStreams], bf[kStreams], bv[kStreams], bo[kStreams];
+  Segments pseg[kStreams];
+  int64_t chunk = 0;
+};
+
+static int check_proc(phs_process_t h) {
+  if (!h) return fail(PHS_ERR_INVALID_ARG, "null process handle");
+  return PHS_OK;
+}
+
+extern "C" int phs_process_create(phs_process_t *out, int n_in, int n_out, int n_channels, int n_x,
+                                  const int *d1, const int *d2, const int *hc, const int *friends,
+                                  const int *map_ids, const double *map_m, const double *map_w,
+                                  const double *flv_m, const double *flv_w) {
+  if (!out) return fail(PHS_ERR_INVALID_ARG, "null output handle pointer");
+  *out = nullptr;
+  if (!d1 || !d2 || !hc || !map_ids || !map_m || !map_w || !flv_m)
+    return fail(PHS_ERR_INVALID_ARG, "null table pointer");
+  phs::Process P;
+  P.n_in = n_in;
+  P.n_out = n_out;
+  P.n_channels = n_channels;
+  P.n_x = n_x;
+  std::string err;
+  int rc = phs::validate_process(P, err);
+  if (rc) return fail(rc, "%s", err.c_str());
+  P.n_prt = (1 << (n_in + n_out)) - 1;
+  P.n_prt_out = (1 << n_out) - 1;
+  const size_t nt = (size_t)n_channels * P.n_prt, nm = (size_t)n_channels * P.n_prt_out;
+  P.d1.assign(d1, d1 + nt);
+  P.d2.assign(d2, d2 + nt);
+  P.has_children.assign(hc, hc + nt);
+  P.friends = friends ? std::vector<int>(friends, friends + nt) : std::vector<int>(nt, 0);
+  P.map_id.assign(map_ids, map_ids + nm);
+  P.map_m.assign(map_m, map_m + nm);
+  P.map_w.assign(map_w, map_w + nm);
+  P.flv_m.assign(flv_m, flv_m + n_in + n_out);
+  P.flv_w = flv_w ? std::vector<double>(flv_w, flv_w + n_in + n_out)
+                  : std::vector<double>(n_in + n_out, 0.0);
+  // structural validation at a nominal sqrt(s) (constants are recompiled by set_beams)
+  for (int c = 0; c < n_channels; c++) {
+    PhsChannel tmp;
+    phs::ChannelInfo info;
+    double m_tot = 0;
+    for (int k = 0; k < n_out; k++) m_tot += P.flv_m[n_in + k];
+    rc = phs::compile_channel(P, c, 2 * m_tot + 1000.0, tmp, info, err);
+    if (rc) return fail(rc, "%s", err.c_str());
+  }
+  phs_process *h = new phs_process;
+  h->p = std::move(P);
+  cudaGetDevice(&h->device);
+  *out = h;
+  return PHS_OK;
+}
+
+extern "C" int phs_process_destroy(phs_process_t h) {
+  if (!h) return PHS_OK;
+  DeviceGuard g(h->device);
+  for (int s = 0; s < phs_process::kStreams; s++) {
+    if (h->streams[s]) cudaStreamDestroy(h->streams[s]);
+    h->bx[s].release(); h->bp[s].release(); h->bf[s].release(); h->bv[s].release();
+    h->bo[s].release(); h->pseg[s].dev.release();
+  }
+  h->d_prog.release();
+  h->segs.dev.release();
+  delete h;
+  return PHS_OK;
+}
+
+extern "C" int phs_process_set_beams(phs_process_t h, double E1, double E2) {
+  if (int rc = check_proc(h)) return rc;
+  if (!(E1 > 0) || !(E2 > 0) || !isfinite(E1) || !isfinite(E2))
+    return fail(PHS_ERR_INVALID_ARG, "beam energies must be positive and finite");
+  if (h->beams && h->E1 == E1 && h->E2 == E2) return PHS_OK;
+  DeviceGuard g(h->device);
+  const phs::Process &P = h->p;
+  const double sqrts = 2 * sqrt(E1 * E2);
+  double m_tot = 0;
+  for (int k = 0; k < P.n_out; k++) m_tot += P.flv_m[P.n_in + k];
+  if (!(sqrts > m_tot))
+    return fail(PHS_ERR_INVALID_ARG, "sqrt(s) = %g is below the final-state mass sum %g", sqrts,
+                m_tot);
+  std::vector<PhsChannel> prog(P.n_channels);
+  int depth = 0;
+  std::string err;
+  const double bg = (E1 - E2) / (2 * sqrt(E1 * E2));
+  for (int c = 0; c < P.n_channels; c++) {
+    phs::ChannelInfo info;
+    int rc = phs::compile_channel(P, c, sqrts, prog[c], info, err);
+    if (rc) return fail(rc, "%s", err.c_str());
+    prog[c].sqrts = sqrts;
+    prog[c].lab = E1 != E2;
+    prog[c].lab_bg = bg;
+    prog[c].lab_gamma = sqrt(1 + bg * bg);
+    depth = std::max(depth, info.stack_depth);
+  }
+  int rc = h->d_prog.reserve(prog.size() * sizeof(PhsChannel));
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpy(h->d_prog.ptr, prog.data(), prog.size() * sizeof(PhsChannel),
+                      cudaMemcpyHostToDevice));
+  h->prog = std::move(prog);
+  h->lay.assign(P.n_channels, ChanLayout{P.n_out, P.n_x});
+  h->stack_depth = depth;
+  h->E1 = E1;
+  h->E2 = E2;
+  h->beams = true;
+  return PHS_OK;
+}
+
+extern "C" int phs_process_info(phs_process_t h, int *n_in, int *n_out, int *n_channels, int *n_x,
+                                int *depth) {
+  if (int rc = check_proc(h)) return rc;
+  if (n_in) *n_in = h->p.n_in;
+  if (n_out) *n_out = h->p.n_out;
+  if (n_channels) *n_channels = h->p.n_channels;
+  if (n_x) *n_x = h->p.n_x;
+  if (depth) {
+    int d = 0;
+    for (int c = 0; c < h->p.n_channels; c++) {
+      PhsChannel tmp;
+      phs::ChannelInfo info;
+      std::string err;
+      if (phs::compile_channel(h->p, c, 1e4, tmp, info, err) == 0) d = std::max(d, info.stack_depth);
+    }
+    *depth = d;
+  }
+  return PHS_OK;
+}
+
+static int check_counts(const int64_t *counts, int n_channels, int64_t n_events) {
+  if (n_events < 0) return fail(PHS_ERR_INVALID_ARG, "n_events < 0");
+  if (!counts) {
+    if (n_channels != 1)
+      return fail(PHS_ERR_INVALID_ARG, "channel_counts is required for %d channels", n_channels);
+    return PHS_OK;
+  }
+  int64_t sum = 0;
+  for (int c = 0; c < n_channels; c++) {
+    if (counts[c] < 0) return fail(PHS_ERR_INVALID_ARG, "channel %d has a negative count", c);
+    sum += counts[c];
+  }
+  if (sum != n_events)
+    return fail(PHS_ERR_INVALID_ARG, "channel counts sum to %lld, not n_events = %lld",
+                (long long)sum, (long long)n_events);
+  return PHS_OK;
+}
+
+static int launch_process(phs_process_t h, Segments &S, int64_t n_events, const int64_t *counts,
+                          int64_t ev0, const double *x, double *p, double *f, double *v,
+                          uint8_t *ok, const double *E1, const double *E2, int64_t fstride,
+                          bool whizard_cols, cudaStream_t stream) {
+  int64_t one = n_events;
+  const int64_t *cnt = counts ? counts : &one;
+  int rc = build_segments(S, cnt, h->p.n_channels, h->lay, ev0, 0, 0, whizard_cols);
+  if (rc) return rc;
+  PhsLaunch a;
+  memset(&a, 0, sizeof a);
+  a.channels = h->d_prog.as<PhsChannel>();
+  a.stack_depth = h->stack_depth;
+  a.x = x;
+  a.p = p;
+  a.factor = f;
+  a.volume = v;
+  a.ok = ok;
+  a.factor_stride = fstride;
+  a.E1 = E1;
+  a.E2 = E2;
+  // segment events are numbered from ev0 within this launch's output arrays
+  for (auto &g : S.host) g.ev_begin -= ev0;
+  if ((rc = attach_segments(S, a, stream))) return rc;
+  if (a.n_tiles == 0) return PHS_OK;
+  const int grid = grid_for(a.n_tiles, h->device, h->stack_depth, E1 != nullptr);
+  CUDA_TRY(phs_launch_forward_f64(a, grid, stream));
+  return PHS_OK;
+}
+
+static int check_ptrs(int64_t n, const void *x, const void *p, const void *f, const void *v,
+                      const void *o) {
+  if (n > 0 && (!x || !p || !f || !v || !o)) return fail(PHS_ERR_INVALID_ARG, "null data pointer");
+  if (((uintptr_t)p & 15) != 0) return fail(PHS_ERR_INVALID_ARG, "p must be 16-byte aligned");
+  return PHS_OK;
+}
+
+extern "C" int phs_generate_device(phs_process_t h, int64_t n_events, const int64_t *counts,
+                                   const double *x, double *p, double *f, double *v, uint8_t *ok,
+                                   void *stream) {
+  if (int rc = check_proc(h)) return rc;
+  if (!h->beams) return fail(PHS_ERR_STATE, "phs_process_set_beams has not been called");
+  if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
+  if (int rc = check_ptrs(n_events, x, p, f, v, ok)) return rc;
+  DeviceGuard g(h->device);
+  return launch_process(h, h->segs, n_events, counts, 0, x, p, f, v, ok, nullptr, nullptr, 1,
+                        false, (cudaStream_t)stream);
+}
+
+extern "C" int phs_generate_beams_device(phs_process_t h, int64_t n_events, const int64_t *counts,
+                                         const double *E1, const double *E2, const double *x,
+                                         double *p, double *f, double *v, uint8_t *ok,
+                                         void *stream) {
+  if (int rc = check_proc(h)) return rc;
+  if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
+  if (int rc = check_ptrs(n_events, x, p, f, v, ok)) return rc;
+  if (n_events > 0 && (!E1 || !E2)) return fail(PHS_ERR_INVALID_ARG, "null beam energy pointer");
+  DeviceGuard g(h->device);
+  if (!h->beams) {
+    // programs need compiling once; per-event constants replace the uniform ones
+    double m_tot = 0;
+    for (int k = 0; k < h->p.n_out; k++) m_tot += h->p.flv_m[h->p.n_in + k];
+    int rc = phs_process_set_beams(h, m_tot + 500.0, m_tot + 500.0);
+    if (rc) return rc;
+  }
+  return launch_process(h, h->segs, n_events, counts, 0, x, p, f, v, ok, E1, E2, 1, false,
+                        (cudaStream_t)stream);
+}
+
+// Host path: chunks alternate between two streams; each stream's buffers are reused only
+// after its previous chunk's copies back have been ordered before the next copy in.
+extern "C" int phs_generate_host(phs_process_t h, int64_t n_events, const int64_t *counts,
+                                 const double *x, double *p, double *f, double *v, uint8_t *ok) {
+  if (int rc = check_proc(h)) return rc;
+  if (!h->beams) return fail(PHS_ERR_STATE, "phs_process_set_beams has not been called");
+  if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
+  if (n_events > 0 && (!x || !p || !f || !v || !ok)) return fail(PHS_ERR_INVALID_ARG, "null data pointer");
+  if (n_events == 0) return PHS_OK;
+  DeviceGuard g(h->device);
+  const int n_out = h->p.n_out, n_x = h->p.n_x, nch = h->p.n_channels;
+  const int64_t chunk = std::min<int64_t>(n_events, 1 << 20);
+  for (int s = 0; s < phs_process::kStreams; s++) {
+    if (!h->streams[s]) CUDA_TRY(cudaStreamCreateWithFlags(&h->streams[s], cudaStreamNonBlocking));
+    int rc;
+    if ((rc = h->bx[s].reserve(chunk * n_x * sizeof(double)))) return rc;
+    if ((rc = h->bp[s].reserve(chunk * 4 * n_out * sizeof(double)))) return rc;
+    if ((rc = h->bf[s].reserve(chunk * sizeof(double)))) return rc;
+    if ((rc = h->bv[s].reserve(chunk * sizeof(double)))) return rc;
+    if ((rc = h->bo[s].reserve(chunk))) return rc;
+  }
+  std::vector<int64_t> cnt(nch, 0), prefix(nch + 1, 0);
+  if (counts) std::copy(counts, counts + nch, cnt.begin()); else cnt[0] = n_events;
+  for (int c = 0; c < nch; c++) prefix[c + 1] = prefix[c] + cnt[c];
+  int k = 0;
+  for (int64_t e0 = 0; e0 < n_events; e0 += chunk, k++) {
+    const int s = k % phs_process::kStreams;
+    cudaStream_t st = h->streams[s];
+    const int64_t n = std::min(chunk, n_events - e0);
+    // this chunk's per-channel counts
+    std::vector<int64_t> cc(nch, 0);
+    for (int c = 0; c < nch; c++) {
+      int64_t lo = std::max(prefix[c], e0), hi = std::min(prefix[c + 1], e0 + n);
+      cc[c] = hi > lo ? hi - lo : 0;
+    }
+    CUDA_TRY(cudaMemcpyAsync(h->bx[s].ptr, x + e0 * n_x, n * n_x * sizeof(double),
+                             cudaMemcpyHostToDevice, st));
+    int rc = launch_process(h, h->pseg[s], n, cc.data(), 0, h->bx[s].as<double>(),
+                            h->bp[s].as<double>(), h->bf[s].as<double>(), h->bv[s].as<double>(),
+                            h->bo[s].as<uint8_t>(), nullptr, nullptr, 1, false, st);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(p + e0 * 4 * n_out, h->bp[s].ptr, n * 4 * n_out * sizeof(double),
+                             cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(f + e0, h->bf[s].ptr, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(v + e0, h->bv[s].ptr, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(ok + e0, h->bo[s].ptr, n, cudaMemcpyDeviceToHost, st));
+  }
+  for (int s = 0; s < phs_process::kStreams; s++) CUDA_TRY(cudaStreamSynchronize(h->streams[s]));
+  return PHS_OK;
+}
+
+// ---------------------------------------------------------------------------- batches
+struct phs_batch {
+  int device = 0;
+  std::vector<PhsChannel> prog;
+  std::vector<ChanLayout> lay;
+  int stack_depth = 0;
+  DevBuf d_prog;
+  Segments segs;
+};
+
+extern "C" int phs_batch_create(phs_batch_t *out, int n_procs, const phs_process_t *procs) {
+  if (!out) return fail(PHS_ERR_INVALID_ARG, "null output handle pointer");
+  *out = nullptr;
+  if (n_procs < 1 || !procs) return fail(PHS_ERR_INVALID_ARG, "no processes");
+  phs_batch *b = new phs_batch;
+  cudaGetDevice(&b->device);
+  for (int i = 0; i < n_procs; i++) {
+    phs_process_t h = procs[i];
+    if (!h || !h->beams) {
+      delete b;
+      return fail(PHS_ERR_STATE, "process %d is null or has no beams set", i);
+    }
+    b->prog.insert(b->prog.end(), h->prog.begin(), h->prog.end());
+    b->lay.insert(b->lay.end(), h->lay.begin(), h->lay.end());
+    b->stack_depth = std::max(b->stack_depth, h->stack_depth);
+  }
+  DeviceGuard g(b->device);
+  int rc = b->d_prog.reserve(b->prog.size() * sizeof(PhsChannel));
+  if (rc) { delete b; return rc; }
+  cudaError_t e = cudaMemcpy(b->d_prog.ptr, b->prog.data(), b->prog.size() * sizeof(PhsChannel),
+                             cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    b->d_prog.release();
+    delete b;
+    return fail(PHS_ERR_CUDA, "cudaMemcpy of batch programs failed: %s", cudaGetErrorString(e));
+  }
+  *out = b;
+  return PHS_OK;
+}
+
+extern "C" int phs_batch_destroy(phs_batch_t b) {
+  if (!b) return PHS_OK;
+  DeviceGuard g(b->device);
+  b->d_prog.release();
+  b->segs.dev.release();
+  delete b;
+  return PHS_OK;
+}
+
+extern "C" int phs_batch_info(phs_batch_t b, int *n_channels, int64_t *x_stride_sum, int *max_n_out) {
+  if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
+  if (n_channels) *n_channels = (int)b->prog.size();
+  int64_t xs = 0;
+  int mo = 0;
+  for (auto &l : b->lay) { xs += l.x_stride; mo = std::max(mo, l.n_out); }
+  if (x_stride_sum) *x_stride_sum = xs;
+  if (max_n_out) *max_n_out = mo;
+  return PHS_OK;
+}
+
+extern "C" int phs_batch_offsets(phs_batch_t b, const int64_t *counts, int64_t *xo, int64_t *po) {
+  if (!b || !counts || !xo || !po) return fail(PHS_ERR_INVALID_ARG, "null argument");
+  const int n = (int)b->prog.size();
+  xo[0] = po[0] = 0;
+  for (int c = 0; c < n; c++) {
+    xo[c + 1] = xo[c] + counts[c] * b->lay[c].x_stride;
+    po[c + 1] = po[c] + counts[c] * 4 * b->lay[c].n_out;
+  }
+  return PHS_OK;
+}
+
+extern "C" int phs_batch_generate_device(phs_batch_t b, const int64_t *counts, const double *x,
+                                         double *p, double *f, double *v, uint8_t *ok,
+                                         void *stream) {
+  if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
+  if (!counts) return fail(PHS_ERR_INVALID_ARG, "null counts");
+  const int n = (int)b->prog.size();
+  int64_t n_events = 0;
+  for (int c = 0; c < n; c++) n_events += counts[c] > 0 ? counts[c] : 0;
+  if (int rc = check_counts(counts, n, n_events)) return rc;
+  if (int rc = check_ptrs(n_events, x, p, f, v, ok)) return rc;
+  DeviceGuard g(b->device);
+  int rc = build_segments(b->segs, counts, n, b->lay, 0, 0, 0, false);
+  if (rc) return rc;
+  PhsLaunch a;
+  memset(&a, 0, sizeof a);
+  a.channels = b->d_prog.as<PhsChannel>();
+  a.stack_depth = b->stack_depth;
+  a.x = x;
+  a.p = p;
+  a.factor = f;
+  a.volume = v;
+  a.ok = ok;
+  a.factor_stride = 1;
+  if ((rc = attach_segments(b->segs, a, (cudaStream_t)stream))) return rc;
+  if (a.n_tiles == 0) return PHS_OK;
+  const int grid = grid_for(a.n_tiles, b->device, b->stack_depth, false);
+  CUDA_TRY(phs_launch_forward_f64(a, grid, (cudaStream_t)stream));
+  return PHS_OK;
+}
+
+// ---------------------------------------------------------------------- random numbers
+extern "C" int phs_philox_fill(double *x, int64_t n_events, int n_x, uint64_t seed,
+                               int64_t first_event, void *stream) {
+  if (n_events < 0 || n_x < 1 || first_event < 0) return fail(PHS_ERR_INVALID_ARG, "bad sizes");
+  if (n_events > 0 && !x) return fail(PHS_ERR_INVALID_ARG, "null x");
+  CUDA_TRY(phs_launch_philox(x, n_events, n_x, seed, first_event, (cudaStream_t)stream));
+  return PHS_OK;
+}
+
+// --------------------------------------------------------------- peak measurement
+extern "C" int phs_measure_fma_peak(int fp64, double *gflops) {
+  if (!gflops) return fail(PHS_ERR_INVALID_ARG, "null output");
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  const int blocks = sm_count(dev) * 8, threads = 256, iters = fp64 ? 4096 : 65536;
+  DevBuf out;
+  if (int rc = out.reserve((size_t)blocks * threads * 8)) return rc;
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; rep++) {
+    CUDA_TRY(cudaEventRecord(e0, nullptr));
+    CUDA_TRY(phs_launch_fma_rate(out.ptr, fp64, blocks, threads, iters, nullptr));
+    CUDA_TRY(cudaEventRecord(e1, nullptr));
+    CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0) best = std::min(best, ms);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  out.release();
+  *gflops = 16.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e9;
+  return PHS_OK;
+}
+
+// -------------------------------------------------------------------- Whizard binding
+// Process-global state, as in the reference (global_phs.cpp, whizard_gpu_phs.cpp:10): one
+// process per library instance, driven by Whizard's single host thread.
+namespace {
+struct Whizard {
+  std::mutex mu;
+  int n_channels = 0, n_trees = 0, n_groves = 0, n_x = 0, n_in = 0, n_out = 0;
+  int n_prt = 0, n_prt_out = 0;
+  bool structure = false, flavors = false, mappings = false, trees = false;
+  std::vector<double> flv_m, flv_w;
+  std::vector<int> map_id, d1, d2, hc, fr;
+  std::vector<double> map_m, map_w;
+  std::vector<int64_t> counts;  // from init_channel_ids
+  int64_t batch_size = 0;
+  phs_process_t proc = nullptr;
+  DevBuf dx, dp, df, dv, dok;
+  int64_t last_events = 0;
+  int msq_threads = 0, cb_threads = 0, ab_threads = 0;
+};
+Whizard W;
+
+void whizard_log(int rc) {
+  if (rc) fprintf(stderr, "gpu_phs: %s\n", g_err.c_str());
+}
+
+void whizard_release_device() {
+  W.dx.release(); W.dp.release(); W.df.release(); W.dv.release(); W.dok.release();
+  W.last_events = 0;
+}
+}  // namespace
+
+extern "C" void c_whizard_set_particle_structure(int *n_channels, int *n_trees, int *n_groves,
+                                                 int *n_x, int *n_in, int *n_out) {
+  std::lock_guard<std::mutex> lk(W.mu);
+  if (!n_channels || !n_trees || !n_groves || !n_x || !n_in || !n_out) {
+    whizard_log(fail(PHS_ERR_INVALID_ARG, "c_whizard_set_particle_structure: null argument"));
+    return;
+  }
+  if (*n_out < 2 || *n_out > PHS_MAX_OUT || *n_in < 1 || *n_in > 2 || *n_channels < 1) {
+    whizard_log(fail(PHS_ERR_UNSUPPORTED, "c_whizard_set_particle_structure: n_in=%d n_out=%d "
+                     "n_channels=%d not supported", *n_in, *n_out, *n_channels));
+    return;
+  }
+  W.n_channels = *n_channels;
+  W.n_trees = *n_trees;
+  W.n_groves = *n_groves;
+  W.n_x = *n_x;
+  W.n_in = *n_in;
+  W.n_out = *n_out;
+  W.n_prt = (1 << (W.n_in + W.n_out)) - 1;
+  W.n_prt_out = (1 << W.n_out) - 1;
+  W.flv_m.assign(W.n_in + W.n_out, 0.0);
+  W.flv_w.assign(W.n_in + W.n_out, 0.0);
+  W.structure = true;
+  W.flavors = W.mappings = W.trees = false;
+}
+
+extern "C" void c_whizard_set_flavors(double *masses, double *widths) {
+  std::lock_guard<std::mutex> lk(W.mu);
+  if (!W.structure || !masses || !widths) {
+    whizard_log(fail(PHS_ERR_STATE, "c_whizard_set_flavors: no particle structure or null input"));
+    return;
+  }
+  std::copy(masses, masses + W.n_in + W.n_out, W.flv_m.begin());
+  std::copy(widths, widths + W.n_in + W.n_out, W.flv_w.begin());
+  W.flavors = true;
+}
+
+extern "C" void c_whizard_init_mappings(void) {
+  std::lock_guard<std::mutex> lk(W.mu);
+  if (!W.structure) { whizard_log(fail(PHS_ERR_STATE, "c_whizard_init_mappings: no particle structure")); return; }
+  const size_t n = (size_t)W.n_channels * W.n_prt_out;
+  W.map_id.assign(n, 0);
+  W.map_m.assign(n, 0.0);
+  W.map_w.assign(n, 0.0);
+  W.mappings = true;
+}
+
+extern "C" void c_whizard_fill_mapping(int *channel, int *map_ids, double *masses, double *widths) {
+  std::lock_guard<std::mutex> lk(W.mu);
+  if (!W.mappings || !channel || !map_ids || !masses || !widths || *channel < 1 ||
+      *channel > W.n_channels) {
+    whizard_log(fail(PHS_ERR_INVALID_ARG, "c_whizard_fill_mapping: bad channel or state"));
+    return;
+  }
+  const size_t o = (size_t)(*channel - 1) * W.n_prt_out;
+  std::copy(map_ids, map_ids + W.n_prt_out, W.map_id.begin() + o);
+  std::copy(masses, masses + W.n_prt_out, W.map_m.begin() + o);
+  std::copy(widths, widths + W.n_prt_out, W.map_w.begin() + o);
+}
+
+extern "C" void c_whizard_init_tree_structures(void) {
+  std::lock_guard<std::mutex> lk(W.mu);
+  if (!W.structure) { whizard_log(fail(PHS_ERR_STATE, "c_whizard_init_tree_structures: no particle structure")); return; }
+  const size_t n = (size_t)W.n_channels * W.n_prt;
+  W.d1.assign(n, 0);
+  W.d2.assign(n, 0);
+  W.hc.assign(n, 0);
+  W.fr.assign(n, 0);
+  W.trees = true;
+}
+
+extern "C" void c_whizard_fill_tree_structure(int *channel, int *d1, int *d2, int *hc, int *friends) {
+  std::lock_guard<std::mutex> lk(W.mu);
+  if (!W.trees || !channel || !d1 || !d2 || !hc || !friends || *channel < 1 ||
+      *channel > W.n_channels) {
+    whizard_log(fail(PHS_ERR_INVALID_ARG, "c_whizard_fill_tree_structure: bad channel or state"));
+    return;
+  }
+  const size_t o = (size_t)(*channel - 1) * W.n_prt;
+  std::copy(d1, d1 + W.n_prt, W.d1.begin() + o);
+  std::copy(d2, d2 + W.n_prt, W.d2.begin() + o);
+  std::copy(hc, hc + W.n_prt, W.hc.begin() + o);
+  std::copy(friends, friends + W.n_prt, W.fr.begin() + o);
+}
+
+// channel_limits[c] is the cumulative number of events up to and including channel c; events
+// are grouped by channel (whizard_gpu_phs.cpp:89-98).  Empty channels anywhere are allowed.
+extern "C" void c_whizard_init_channel_ids(int *batch_size, int *n_channels, int *channel_limits) {
+  std::lock_guard<std::mutex> lk(W.mu);
+  if (!batch_size || !n_channels || !channel_limits || *n_channels < 1 || *batch_size < 0) {
+    whizard_log(fail(PHS_ERR_INVALID_ARG, "c_whizard_init_channel_ids: bad arguments"));
+    return;
+  }
+  W.counts.assign(*n_channels, 0);
+  int64_t prev = 0;
+  for (int c = 0; c < *n_channels; c++) {
+    int64_t lim = std::min<int64_t>(channel_limits[c], *batch_size);
+    W.counts[c] = std::max<int64_t>(0, lim - prev);
+    prev = std::max(prev, lim);
+  }
+  W.batch_size = *batch_size;
+}
+
+extern "C" void c_whizard_set_threads(int *msq_threads, int *cb_threads, int *ab_threads) {
+  std::lock_guard<std::mutex> lk(W.mu);
+  W.msq_threads = msq_threads ? *msq_threads : 0;
+  W.cb_threads = cb_threads ? *cb_threads : 0;
+  W.ab_threads = ab_threads ? *ab_threads : 0;
+}
+
+extern "C" void c_whizard_init_gpu_phs(void) {
+  std::lock_guard<std::mutex> lk(W.mu);
+  if (!W.structure || !W.flavors || !W.mappings || !W.trees) {
+    whizard_log(fail(PHS_ERR_STATE, "c_whizard_init_gpu_phs: structure, flavors, mappings and "
+                     "trees must be set first"));
+    return;
+  }
+  if (W.proc) { phs_process_destroy(W.proc); W.proc = nullptr; }
+  whizard_log(phs_process_create(&W.proc, W.n_in, W.n_out, W.n_channels, W.n_x, W.d1.data(),
+                                 W.d2.data(), W.hc.data(), W.fr.data(), W.map_id.data(),
+                                 W.map_m.data(), W.map_w.data(), W.flv_m.data(), W.flv_w.data()));
+}
+
+extern "C" void c_whizard_finalize_gpu_phs(void) {
+  std::lock_guard<std::mutex> lk(W.mu);
+  if (W.proc) phs_process_destroy(W.proc);
+  W.proc = nullptr;
+  whizard_release_device();
+  W.map_id.clear(); W.map_m.clear(); W.map_w.clear();
+  W.d1.clear(); W.d2.clear(); W.hc.clear(); W.fr.clear();
+  W.flv_m.clear(); W.flv_w.clear();
+  W.counts.clear();
+  W.structure = W.flavors = W.mappings = W.trees = false;
+}
+
+extern "C" void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in,
+                                             bool *requires_boost_to_lab, int *n_events_p,
+                                             int *n_channels_p, int *n_x_p, double *x,
+                                             double *factors, double *volumes, bool *oks,
+                                             double *p, double *x_out) {
+  (void)requires_boost_to_lab;  // stored but unused by the reference (phs.cu:1559)
+  std::lock_guard<std::mutex> lk(W.mu);
+  int rc = PHS_OK;
+  do {
+    if (!W.proc) { rc = fail(PHS_ERR_STATE, "c_whizard_gen_phs_from_x_gpu: init_gpu_phs not done"); break; }
+    if (!n_events_p || !n_channels_p || !n_x_p || !E1_in || !E2_in) {
+      rc = fail(PHS_ERR_INVALID_ARG, "c_whizard_gen_phs_from_x_gpu: null argument");
+      break;
+    }
+    const int64_t n = *n_events_p;
+    const int nch = *n_channels_p, n_x = *n_x_p, n_out = W.n_out;
+    if (nch != W.n_channels || n_x != W.n_x) {
+      rc = fail(PHS_ERR_INVALID_ARG, "n_channels/n_x differ from the particle structure");
+      break;
+    }
+    if (n == 0) break;
+    if (!x || !factors || !volumes || !oks || !p) { rc = fail(PHS_ERR_INVALID_ARG, "null data pointer"); break; }
+    std::vector<int64_t> counts = W.counts;
+    int64_t sum = 0;
+    for (auto c : counts) sum += c;
+    if (counts.size() != (size_t)nch || sum != n) {
+      rc = fail(PHS_ERR_INVALID_ARG, "channel ids from c_whizard_init_channel_ids cover %lld "
+                "events, not %lld", (long long)sum, (long long)n);
+      break;
+    }
+    bool uniform = true;
+    for (int64_t i = 1; i < n && uniform; i++) uniform = E1_in[i] == E1_in[0] && E2_in[i] == E2_in[0];
+    DeviceGuard g(W.proc->device);
+    if ((rc = W.dx.reserve(n * n_x * sizeof(double)))) break;
+    if ((rc = W.dp.reserve(n * 4 * n_out * sizeof(double)))) break;
+    if ((rc = W.df.reserve(n * sizeof(double) * (uniform ? 1 : 3)))) break;
+    if ((rc = W.dv.reserve(n * sizeof(double)))) break;
+    if ((rc = W.dok.reserve(n))) break;
+    cudaError_t e = cudaMemcpy(W.dx.ptr, x, n * n_x * sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy of x: %s", cudaGetErrorString(e)); break; }
+    double *df = W.df.as<double>();
+    if (uniform) {
+      if ((rc = phs_process_set_beams(W.proc, E1_in[0], E2_in[0]))) break;
+      rc = phs_generate_device(W.proc, n, counts.data(), W.dx.as<double>(), W.dp.as<double>(), df,
+                               W.dv.as<double>(), W.dok.as<uint8_t>(), nullptr);
+    } else {
+      double *dE1 = df + n, *dE2 = df + 2 * n;
+      cudaMemcpy(dE1, E1_in, n * sizeof(double), cudaMemcpyHostToDevice);
+      cudaMemcpy(dE2, E2_in, n * sizeof(double), cudaMemcpyHostToDevice);
+      rc = phs_generate_beams_device(W.proc, n, counts.data(), dE1, dE2, W.dx.as<double>(),
+                                     W.dp.as<double>(), df, W.dv.as<double>(),
+                                     W.dok.as<uint8_t>(), nullptr);
+    }
+    if (rc) break;
+    std::vector<double> fh(n);
+    e = cudaMemcpy(p, W.dp.ptr, n * 4 * n_out * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(fh.data(), df, n * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(volumes, W.dv.ptr, n * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(oks, W.dok.ptr, n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e)); break; }
+    // factors[n_channels * i + c] and x_out[n_x * n * c + n_x * i + k] (phs.cu:1580-1585):
+    // the event's own channel is filled; the other channels' entries need the inverse
+    // mapping, which this build does not provide yet, and are set to 0.
+    memset(factors, 0, (size_t)n * nch * sizeof(double));
+    if (x_out) memset(x_out, 0, (size_t)n * nch * n_x * sizeof(double));
+    int64_t i = 0;
+    for (int c = 0; c < nch; c++) {
+      for (int64_t k = 0; k < counts[c]; k++, i++) {
+        factors[(size_t)nch * i + c] = fh[i];
+        if (x_out) memcpy(x_out + (size_t)n_x * n * c + (size_t)n_x * i, x + (size_t)n_x * i,
+                          n_x * sizeof(double));
+      }
+    }
+    W.last_events = n;
+  } while (0);
+  whizard_log(rc);
+}
+
+extern "C" void c_whizard_get_momentum_device_pointer(double *p) { (void)p; }
+
+extern "C" double *phs_whizard_momentum_device_pointer(void) {
+  std::lock_guard<std::mutex> lk(W.mu);
+  return W.last_events ? W.dp.as<double>() : nullptr;
+}
+
+extern "C" void c_whizard_reset_generator(void) {
+  std::lock_guard<std::mutex> lk(W.mu);
+  // phs.cu:1303-1308: drops the flavors and the retained device buffers
+  std::fill(W.flv_m.begin(), W.flv_m.end(), 0.0);
+  std::fill(W.flv_w.begin(), W.flv_w.end(), 0.0);
+  W.flavors = false;
+  whizard_release_device();
+}
+
+extern "C" void c_whizard_show_module(void) {
+  std::lock_guard<std::mutex> lk(W.mu);
+  printf("n_channels: %d\n", W.n_channels);
+  printf("n_ext_in: %d\n", W.n_in);
+  printf("n_ext_out: %d\n", W.n_out);
+  printf("n_ext_tot: %d\n", W.n_in + W.n_out);
+  printf("n_prt: %d\n", W.n_prt);
+  printf("n_prt_out: %d\n", W.n_prt_out);
+  printf("n_x: %d\n", W.n_x);
+  printf("root_branch: %d\n", W.n_prt_out - 1);
+  printf("n_branches: %d\n", 2 * W.n_out - 1);
+  printf("\nMappings: \n");
+  if (!W.mappings) {
+    printf(" MAPPINGS NOT SET UP!\n");
+    return;
+  }
+  for (int c = 0; c < W.n_channels; c++) {
+    printf(" c: %d\n ids: ", c);
+    for (int i = 0; i < W.n_prt_out; i++) printf("%d ", W.map_id[(size_t)c * W.n_prt_out + i]);
+    printf("\n masses: ");
+    for (int i = 0; i < W.n_prt_out; i++) printf("%lf ", W.map_m[(size_t)c * W.n_prt_out + i]);
+    printf("\n widths: ");
+    for (int i = 0; i < W.n_prt_out; i++) printf("%lf ", W.map_w[(size_t)c * W.n_prt_out + i]);
+    printf("\n");
+  }
+  if (W.trees) {
+    printf("Children: \n");
+    for (int c = 0; c < W.n_channels; c++) {
+      for (auto *t : {&W.d1, &W.d2, &W.hc}) {
+        for (int i = 0; i < W.n_prt; i++) printf("%d ", (*t)[(size_t)c * W.n_prt + i]);
+        printf("\n");
+      }
+    }
+    printf("Friends: \n");
+    for (int c = 0; c < W.n_channels; c++) {
+      printf("channel %d: ", c);
+      for (int i = 0; i < W.n_prt; i++) printf("%d ", W.fr[(size_t)c * W.n_prt + i]);
+      printf("\n");
+    }
+  }
+  if (W.proc && W.proc->beams) {
+    printf("Visit programs (sqrt(s) = %g): \n", W.proc->prog[0].sqrts);
+    for (int c = 0; c < W.n_channels; c++) {
+      const PhsChannel &ch = W.proc->prog[c];
+      printf("  channel %d: %d visits, volume %.17g\n", c, ch.n_visits, ch.volume);
+      for (int v = 0; v < ch.n_visits; v++) {
+        const PhsVisit &V = ch.visit[v];
+        printf("    visit %d: x_phi %d x_ct %d ct_class %d carry %d push %d children", v, V.x_phi,
+               V.x_ct, V.ct_class, V.carry, V.push);
+        for (int j = 0; j < 2; j++) {
+          const PhsChild &C = V.child[j];
+          if (C.internal) printf(" [map %d x %d]", C.map_id, C.x_msq);
+          else printf(" [leaf %d]", C.out_index);
+        }
+        printf("\n");
+      }
+    }
+  }
+  printf("END OF MODULE\n");
+}

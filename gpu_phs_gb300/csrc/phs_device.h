@@ -1,0 +1,43 @@
+// phs_device.h -- launch interface of the device kernels (host side of phs_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "phs_program.h"
+
+#define PHS_INLINE_SEGS 64
+
+// One forward launch over a list of segments (runs of events of one channel).
+struct PhsLaunch {
+  const PhsChannel *channels;  // device, per channel
+  const PhsSegment *segments;  // device table, used when n_segments > PHS_INLINE_SEGS
+  PhsSegment seg_inline[PHS_INLINE_SEGS];  // sorted by tile_begin
+  int32_t n_segments;
+  int32_t stack_depth;         // max push depth over the launched channels
+  int64_t n_tiles;             // total 32-event warp tiles
+  const double *x;
+  double *p;
+  double *factor;
+  double *volume;
+  uint8_t *ok;
+  int64_t factor_stride;       // factor index = event * factor_stride + segment.factor_col
+  const double *E1;            // per-event beams (both non-null) or null
+  const double *E2;
+};
+
+// Block size and resident blocks per SM of the forward kernel.
+#define PHS_FWD_BLOCK 128
+
+cudaError_t phs_launch_forward_f64(const PhsLaunch &a, int n_blocks, cudaStream_t stream);
+int phs_forward_blocks_per_sm(int stack_depth, bool per_event);
+size_t phs_forward_smem_bytes(int stack_depth);
+
+// Philox4x32-10 uniform doubles for events [first_event, first_event + n_events) of the
+// stream `seed`, row length n_x (the layout is documented in gpu_phs_gb300/philox.py).
+cudaError_t phs_launch_philox(double *x, int64_t n_events, int32_t n_x, uint64_t seed,
+                              int64_t first_event, cudaStream_t stream);
+
+// FMA-throughput probe (8 independent chains per thread, `iters` rounds): 16 * iters flops
+// per thread.  Used to measure the FP64 and FP32 peaks the roofline is quoted against.
+cudaError_t phs_launch_fma_rate(void *out, int fp64, int blocks, int threads, int iters,
+                                cudaStream_t stream);

@@ -1,0 +1,98 @@
+// phs_program.h -- the compiled form of one channel tree, shared by host and device.
+//
+// The host tree compiler (phs_compile.cpp) turns a Whizard channel (daughter codes,
+// mapping ids, masses, widths) into a flat "visit program" that the fused kernel walks
+// once per event, top-down, with no recursion and no per-branch arrays:
+//
+//   * one visit per internal branch (n_out - 1 visits, the root first);
+//   * a visit of branch b receives b's frame matrix L0 (its parent's boost), b's msq,
+//     mass and decay momentum, maps its internal children's msq from x, evaluates the
+//     Kallen function and the kinematic ok test at b, builds b's rotation+boost L1,
+//     forms L0*L1, and writes the momenta of its leaf children;
+//   * the next visit continues with an internal child ("carry"), and a second internal
+//     child is pushed on a per-thread stack of depth <= PHS_STACK_DEPTH (the smaller
+//     subtree is carried first, so the depth is <= 2 for n_out <= 15).
+//
+// x indices are static: the reference consumes x in a fixed order (msq x's of the
+// non-root internal branches in post-order, then phi and cos(theta) per internal branch
+// in pre-order; phs_cpu.cpp:174-234, 283-345), so the visit order is free.
+#pragma once
+#include <stdint.h>
+
+#define PHS_MAX_OUT 12
+#define PHS_MAX_VISITS (PHS_MAX_OUT - 1)
+#define PHS_STACK_DEPTH 2
+
+// Mapping ids (phs.h:8-17).
+enum {
+  PHS_MAP_NO = 0, PHS_MAP_SCHANNEL = 1, PHS_MAP_TCHANNEL = 2, PHS_MAP_UCHANNEL = 3,
+  PHS_MAP_RADIATION = 4, PHS_MAP_COLLINEAR = 5, PHS_MAP_INFRARED = 6,
+  PHS_MAP_STEP_E = 11, PHS_MAP_STEP_H = 12
+};
+
+// cos(theta) mapping classes (phs_cpu.cpp:112-146).
+enum { PHS_CT_UNIFORM = 0, PHS_CT_COLLINEAR = 1 };
+
+// One daughter of a visited branch.
+struct PhsChild {
+  int32_t internal;   // 0: outgoing particle (leaf); 1: internal branch
+  int32_t out_index;  // leaf: output particle index j (Whizard code 2^j)
+  int32_t map_id;     // internal: msq mapping id
+  int32_t x_msq;      // internal: index of its msq x within the event's x row
+  double msq_leaf;    // leaf: m^2 (flv mass squared, phs_cpu.cpp:541-547)
+  double m_leaf;      // leaf: sqrt(m^2), correctly rounded
+  double m, w;        // internal: mapping mass and width
+  double a0, a1, a2;  // internal: msq mapping constants at the handle's sqrt(s)
+  double msq_min, msq_max;  // internal: m_min^2, m_max^2 at the handle's sqrt(s)
+  double m_max;       // internal: sqrt(s) - m_tot + m_min (the ok test's upper bound)
+  double m_min;       // internal: sum of leaf masses below it (phs.cu:61-78)
+};
+
+struct PhsVisit {
+  PhsChild child[2];  // child[0] = daughters1 (+p_decay), child[1] = daughters2 (-p_decay)
+  int32_t x_phi;      // index of the phi x
+  int32_t x_ct;       // index of the cos(theta) x
+  int32_t ct_class;   // PHS_CT_UNIFORM or PHS_CT_COLLINEAR
+  int32_t map_id;     // the visited branch's own mapping id (selects the ct mapping)
+  int32_t carry;      // child continued by the next visit (0/1), -1: next visit pops
+  int32_t push;       // child pushed on the stack after this visit (0/1), -1: none
+  double b0, b1;      // collinear cos(theta) constants at the handle's sqrt(s)
+  double m;           // the visited branch's mapping mass (per-event b0 = m^2/s)
+  double self_m_min;  // the visited branch's m_min (per-event m_max)
+  double self_m_max;  // the visited branch's ok-test bound at the handle's sqrt(s)
+  int32_t self_root;  // 1 for the root visit
+  int32_t both_leaves;  // 1 when neither child is internal (only L columns 0,3 needed)
+};
+
+struct PhsChannel {
+  int32_t n_out;
+  int32_t n_visits;
+  int32_t n_x_used;   // 3 n_out - 4
+  int32_t n_vol;      // entries of the volume program
+  double m_tot;       // sum of all outgoing masses
+  double volume;      // channel volume at the handle's sqrt(s) (phs_cpu.cpp:194-213)
+  double sqrts;       // uniform beams: sqrt(s) = 2 sqrt(E1 E2) the constants were made for
+  double lab_bg;      // uniform beams: longitudinal lab boost (E1-E2)/(2 sqrt(E1 E2))
+  double lab_gamma;   //   and its gamma (phs.cu:1286-1301)
+  int32_t lab;        //   1 when E1 != E2
+  int32_t pad0;
+  PhsVisit visit[PHS_MAX_VISITS];
+  // Volume program for per-event sqrt(s): post-order internal branches; for entry i,
+  // vol_child[i][j] >= 0 is the entry index of an internal child, -1 a leaf (volume 1).
+  int8_t vol_child[PHS_MAX_VISITS][2];
+  int8_t vol_is_root[PHS_MAX_VISITS];
+  int8_t pad[5];
+};
+
+// A contiguous run of events of one channel within a launch.
+struct PhsSegment {
+  int32_t channel;      // index into the launch's channel table
+  int32_t n_out;
+  int64_t ev_begin;     // global index of the first event (factor/volume/ok index)
+  int64_t ev_count;
+  int64_t x_base;       // element offset of the first event's x row
+  int64_t p_base;       // element offset of the first event's momenta
+  int64_t tile_begin;   // first warp tile of this segment (prefix sum)
+  int32_t x_stride;     // x row length (>= n_x_used)
+  int32_t factor_col;   // column added to the factor index (whizard: own channel)
+};

@@ -1,0 +1,186 @@
+/*
+ * gpu_phs.h -- C ABI of libgpuphs, the GB300 (sm_103a) phase-space generator.
+ *
+ * Two layers, both plain C (pointers and sizes, no C++ or framework types):
+ *
+ *  1. The Whizard binding: the same 14 symbols, signatures and by-reference argument
+ *     conventions as the reference's C-ABI (whizard_gpu_phs.cpp:12-249), so the reference's
+ *     Fortran module gpu_phs_whizard_interface.f90 links against this library unchanged.
+ *     These keep the reference's void returns; failures are logged to stderr and kept for
+ *     phs_last_error().
+ *
+ *  2. A handle API (phs_*) with status codes, device-pointer and host-pointer entry points,
+ *     per-event beams, and multi-process batches.  The Whizard binding is built on it.
+ *
+ * Data layouts (identical to the reference, phs.cu:1564-1602):
+ *   x        [n_events][n_x]            doubles in [0,1), event-major
+ *   p        [n_events][n_out][4]       (E, px, py, pz) of the outgoing particles, particle j
+ *                                       is the leaf with Whizard code 2^j
+ *   factors  [n_events]                 phase-space Jacobian of the event's channel
+ *   volumes  [n_events]
+ *   oks      [n_events]                 1 byte each (C bool)
+ * Events are grouped by channel: channel_counts[c] consecutive events belong to channel c.
+ * For ok = 0 events, p and factor are 0 and volume is the channel volume.
+ *
+ * Tree tables (as whizard_gpu_phs.cpp:57-87 and the .ref files, file_input.cpp:183-250):
+ *   daughters1/daughters2/has_children/friends  [n_channels][2^(n_in+n_out)-1], indexed by
+ *       Whizard code - 1, holding daughter codes (0 = none)
+ *   map_ids/map_masses/map_widths               [n_channels][2^n_out-1], by code - 1
+ *   flv_masses/flv_widths                       [n_in + n_out], incoming first
+ */
+#ifndef GPU_PHS_H
+#define GPU_PHS_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------- status codes */
+#define PHS_OK 0
+#define PHS_ERR_INVALID_ARG (-1) /* null pointer, bad size, counts not summing to n_events */
+#define PHS_ERR_TREE (-2)        /* daughters do not form a binary tree over the outgoing codes */
+#define PHS_ERR_MAPPING (-3)     /* mapping id without an implementation (e.g. 99 ONSHELL) */
+#define PHS_ERR_CUDA (-4)        /* a CUDA runtime call failed (message has the CUDA error) */
+#define PHS_ERR_STATE (-5)       /* call out of order (e.g. generate before beams are set) */
+#define PHS_ERR_ALLOC (-6)       /* device or host allocation failed */
+#define PHS_ERR_UNSUPPORTED (-7) /* n_out above PHS_MAX_OUT_API or feature not built */
+
+#define PHS_MAX_OUT_API 12
+
+typedef struct phs_process *phs_process_t;
+typedef struct phs_batch *phs_batch_t;
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char *phs_last_error(void);
+const char *phs_version(void);
+
+/* ------------------------------------------------------------------ handle API: process */
+
+/* Validates and stores a process.  Replaces the reference's global set-up sequence
+ * c_whizard_set_particle_structure / set_flavors / init_mappings / fill_mapping /
+ * init_tree_structures / fill_tree_structure / init_gpu_phs (whizard_gpu_phs.cpp:12-108,
+ * init_phs_gpu phs.cu:327-509).  friends and flv_widths may be NULL.  The device is the
+ * current CUDA device at creation; all later calls on the handle must use it. */
+int phs_process_create(phs_process_t *out, int n_in, int n_out, int n_channels, int n_x,
+                       const int *daughters1, const int *daughters2, const int *has_children,
+                       const int *friends, const int *map_ids, const double *map_masses,
+                       const double *map_widths, const double *flv_masses,
+                       const double *flv_widths);
+int phs_process_destroy(phs_process_t proc);
+
+/* Uniform beam energies for all events: sqrt(s) = 2 sqrt(E1 E2) (phs.cu:1313-1317).  Compiles
+ * the channel programs with the mapping constants at this sqrt(s) (init_mapping_constants_cpu,
+ * phs_cpu.cpp:452-531) and uploads them.  E1 != E2 adds the longitudinal lab boost
+ * (phs.cu:1286-1301). */
+int phs_process_set_beams(phs_process_t proc, double E1, double E2);
+
+/* Sizes: any pointer may be NULL. */
+int phs_process_info(phs_process_t proc, int *n_in, int *n_out, int *n_channels, int *n_x,
+                     int *max_stack_depth);
+
+/* Forward generation on device pointers, stream-ordered on `stream` (a cudaStream_t, NULL =
+ * legacy default stream).  Up to 64 channels with events travel in the kernel parameters;
+ * beyond that a per-handle device table is (re)uploaded when the counts change.  Replaces
+ * gen_phs_from_x_gpu (phs.cu:1333-1636) without its host copies and repack. */
+int phs_generate_device(phs_process_t proc, int64_t n_events, const int64_t *channel_counts,
+                        const double *x, double *p, double *factors, double *volumes,
+                        uint8_t *oks, void *stream);
+
+/* As phs_generate_device with per-event beam energies E1[n_events], E2[n_events] (device):
+ * mapping constants are evaluated per event and the lab boost applied where E1 != E2, as the
+ * reference GPU path does per event (mappings_gpu.hpp:23-99, phs.cu:1286-1301). */
+int phs_generate_beams_device(phs_process_t proc, int64_t n_events, const int64_t *channel_counts,
+                              const double *E1, const double *E2, const double *x, double *p,
+                              double *factors, double *volumes, uint8_t *oks, void *stream);
+
+/* Host pointers in and out (pinned memory is fastest); copies run chunk-pipelined with the
+ * kernel.  Synchronous. */
+int phs_generate_host(phs_process_t proc, int64_t n_events, const int64_t *channel_counts,
+                      const double *x, double *p, double *factors, double *volumes,
+                      uint8_t *oks);
+
+/* -------------------------------------------------------------------- handle API: batches */
+
+/* Many processes (uneven n_out and n_x) generated in one persistent launch.  Batch channel k
+ * enumerates the channels of procs[0], then procs[1], ...  Every process must have beams. */
+int phs_batch_create(phs_batch_t *out, int n_procs, const phs_process_t *procs);
+int phs_batch_destroy(phs_batch_t batch);
+int phs_batch_info(phs_batch_t batch, int *n_channels, int64_t *x_stride_sum, int *max_n_out);
+
+/* Events grouped by batch channel, counts[n_channels]; channel k's events read x rows of that
+ * process's n_x and write p rows of 4 n_out, blocks concatenated in channel order. */
+int phs_batch_generate_device(phs_batch_t batch, const int64_t *counts, const double *x,
+                              double *p, double *factors, double *volumes, uint8_t *oks,
+                              void *stream);
+
+/* Offsets of channel k's first x element and first p element for the given counts
+ * (x_offsets/p_offsets [n_channels + 1], host). */
+int phs_batch_offsets(phs_batch_t batch, const int64_t *counts, int64_t *x_offsets,
+                      int64_t *p_offsets);
+
+/* ---------------------------------------------------------------------- random numbers */
+
+/* Philox4x32-10 uniform doubles in [0,1) for events [first_event, first_event + n_events) of
+ * stream `seed`, rows of n_x, into device memory x (layout in gpu_phs_gb300/philox.py).
+ * Replaces the host sampler rng_generate (rng.cpp:69-108) for benchmark inputs. */
+int phs_philox_fill(double *x, int64_t n_events, int n_x, uint64_t seed, int64_t first_event,
+                    void *stream);
+
+/* ---------------------------------------------------------------------- measurement */
+
+/* Measured FMA throughput of the current device in GFLOP/s (an FMA counts 2), FP64 when
+ * fp64 != 0 else FP32: the pipe peaks the forward kernel's roofline is quoted against.  No
+ * counterpart in the reference, which records only host wall-clock (monitoring.h:32-40). */
+int phs_measure_fma_peak(int fp64, double *gflops);
+
+/* ------------------------------------------------- Whizard binding (whizard_gpu_phs.cpp) */
+
+/* whizard_gpu_phs.cpp:12 */
+void c_whizard_set_particle_structure(int *n_channels, int *n_trees, int *n_groves, int *n_x,
+                                      int *n_in, int *n_out);
+/* whizard_gpu_phs.cpp:35 -- masses/widths [n_in + n_out] */
+void c_whizard_set_flavors(double *masses, double *widths);
+/* whizard_gpu_phs.cpp:42 */
+void c_whizard_init_mappings(void);
+/* whizard_gpu_phs.cpp:57 -- channel is 1-based; arrays [2^n_out - 1] */
+void c_whizard_fill_mapping(int *channel, int *map_ids, double *masses, double *widths);
+/* whizard_gpu_phs.cpp:66 */
+void c_whizard_init_tree_structures(void);
+/* whizard_gpu_phs.cpp:79 -- channel is 1-based; arrays [2^(n_in+n_out) - 1] */
+void c_whizard_fill_tree_structure(int *channel, int *daughters1, int *daughters2,
+                                   int *has_children, int *friends);
+/* whizard_gpu_phs.cpp:89 -- channel_limits[n_channels]: cumulative event counts */
+void c_whizard_init_channel_ids(int *batch_size, int *n_channels, int *channel_limits);
+/* whizard_gpu_phs.cpp:100 -- accepted for compatibility; launch shapes come from the
+ * occupancy calculator instead */
+void c_whizard_set_threads(int *msq_threads, int *cb_threads, int *ab_threads);
+/* whizard_gpu_phs.cpp:106 -- validates and stores the trees */
+void c_whizard_init_gpu_phs(void);
+/* whizard_gpu_phs.cpp:110 */
+void c_whizard_finalize_gpu_phs(void);
+/* whizard_gpu_phs.cpp:114 -- host arrays; factors [n_events][n_channels], x_out
+ * [n_channels][n_events][n_x] (phs.cu:1580-1585) */
+void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in, bool *requires_boost_to_lab,
+                                  int *n_events, int *n_channels, int *n_x, double *x,
+                                  double *factors, double *volumes, bool *oks, double *p,
+                                  double *x_out);
+/* whizard_gpu_phs.cpp:124 -- a no-op in the reference (its argument is passed by value) */
+void c_whizard_get_momentum_device_pointer(double *p);
+/* whizard_gpu_phs.cpp:128 */
+void c_whizard_reset_generator(void);
+/* whizard_gpu_phs.cpp:132 */
+void c_whizard_show_module(void);
+
+/* Device buffer holding the momenta of the last c_whizard_gen_phs_from_x_gpu call,
+ * [n_events][n_out][4], valid until the next generate/reset/finalize; NULL if none.
+ * Replaces get_momentum_device_pointer (phs.cu:1638-1640, transfer_to_whizard.h:1). */
+double *phs_whizard_momentum_device_pointer(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

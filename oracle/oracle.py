@@ -1,0 +1,175 @@
+"""ctypes front end for the CPU checkers.  TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
+module.  Two checkers, both built by oracle/Makefile:
+
+* ``Oracle``    -- the C restatement in phs_oracle.c (_build/libphsoracle.so).
+* ``RefCPU``    -- the reference's own phs_cpu.cpp driven by ref_harness.cpp
+                   (_ref/libphsref.so); present only where the reference sources
+                   were available to compile it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libphsoracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libphsref.so")
+REF_SRC = "/root/reference"
+
+_pd = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_pi = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_pu8 = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+
+
+def build(ref: bool = True) -> None:
+    """Compile the restatement, and the reference harness when the reference sources exist."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    if ref and os.path.isdir(REF_SRC):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+
+
+def _load(path: str) -> C.CDLL:
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is not built; run `make -C oracle`")
+    return C.CDLL(path)
+
+
+def _tables(proc):
+    return (np.ascontiguousarray(proc.d1, np.int32), np.ascontiguousarray(proc.d2, np.int32),
+            np.ascontiguousarray(proc.has_children, np.int32),
+            np.ascontiguousarray(proc.map_ids, np.int32),
+            np.ascontiguousarray(proc.map_masses, np.float64),
+            np.ascontiguousarray(proc.map_widths, np.float64))
+
+
+class Result:
+    def __init__(self, n: int, n_out: int):
+        self.p = np.zeros((n, n_out, 4))
+        self.factor = np.zeros(n)
+        self.volume = np.zeros(n)
+        self.ok = np.zeros(n, np.uint8)
+
+
+class Oracle:
+    """The C restatement of the reference CPU path for one process."""
+
+    _lib: Optional[C.CDLL] = None
+
+    @classmethod
+    def lib(cls) -> C.CDLL:
+        if cls._lib is None:
+            L = _load(ORACLE_SO)
+            L.oracle_create.restype = C.c_void_p
+            L.oracle_create.argtypes = [C.c_int, C.c_int, C.c_int, _pi, _pi, _pi, _pi, _pd, _pd, _pd]
+            L.oracle_destroy.argtypes = [C.c_void_p]
+            L.oracle_set_sqrts.argtypes = [C.c_void_p, C.c_double]
+            L.oracle_get_constants.argtypes = [C.c_void_p, C.c_int, _pd, _pd]
+            L.oracle_mass_sum.restype = C.c_double
+            L.oracle_mass_sum.argtypes = [C.c_void_p, C.c_int, C.c_int]
+            L.oracle_generate.argtypes = [C.c_void_p, C.c_long, C.c_int, _pd, C.c_void_p,
+                                          _pd, _pd, _pd, _pu8, C.c_int]
+            L.oracle_generate_beams.argtypes = [C.c_void_p, C.c_long, C.c_int, _pd, C.c_void_p,
+                                                _pd, _pd, _pd, _pd, _pd, _pu8, C.c_int]
+            cls._lib = L
+        return cls._lib
+
+    def __init__(self, proc, sqrts: float):
+        L = self.lib()
+        self.proc = proc
+        t = _tables(proc)
+        self.h = L.oracle_create(proc.n_in, proc.n_out, proc.n_channels, *t,
+                                 np.ascontiguousarray(proc.flv_masses, np.float64))
+        if not self.h:
+            raise ValueError("oracle rejected the process tables")
+        L.oracle_set_sqrts(self.h, float(sqrts))
+        self.sqrts = float(sqrts)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib().oracle_destroy(self.h)
+            self.h = None
+
+    def constants(self, channel: int):
+        n = 1 << self.proc.n_out
+        a = np.zeros(3 * n)
+        b = np.zeros(3 * n)
+        self.lib().oracle_get_constants(self.h, channel, a, b)
+        return a.reshape(n, 3), b.reshape(n, 3)
+
+    def mass_sum(self, channel: int, code: int) -> float:
+        return self.lib().oracle_mass_sum(self.h, channel, code)
+
+    def generate(self, x: np.ndarray, channels: Optional[np.ndarray] = None,
+                 threads: int = 0, E1: Optional[np.ndarray] = None,
+                 E2: Optional[np.ndarray] = None) -> Result:
+        x = np.ascontiguousarray(x, np.float64)
+        n, n_x = x.shape
+        r = Result(n, self.proc.n_out)
+        chp = None
+        if channels is not None:
+            channels = np.ascontiguousarray(channels, np.int32)
+            chp = channels.ctypes.data_as(C.c_void_p)
+        threads = threads or os.cpu_count() or 1
+        if E1 is None:
+            self.lib().oracle_generate(self.h, n, n_x, x.reshape(-1), chp, r.p.reshape(-1),
+                                       r.factor, r.volume, r.ok, threads)
+        else:
+            E1 = np.ascontiguousarray(np.broadcast_to(E1, (n,)), np.float64)
+            E2 = np.ascontiguousarray(np.broadcast_to(E2, (n,)), np.float64)
+            self.lib().oracle_generate_beams(self.h, n, n_x, x.reshape(-1), chp, E1, E2,
+                                             r.p.reshape(-1), r.factor, r.volume, r.ok, threads)
+        return r
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+class RefCPU:
+    """The reference's own phs_cpu.cpp (process-global state: one process at a time)."""
+
+    _lib: Optional[C.CDLL] = None
+
+    @classmethod
+    def lib(cls) -> C.CDLL:
+        if cls._lib is None:
+            L = _load(REF_SO)
+            L.ref_setup.restype = C.c_int
+            L.ref_setup.argtypes = [C.c_int, C.c_int, C.c_int, _pi, _pi, _pi, _pi, _pd, _pd,
+                                    _pd, _pd, C.c_double]
+            L.ref_generate.restype = C.c_int
+            L.ref_generate.argtypes = [C.c_long, C.c_int, _pd, C.c_void_p, C.c_double, _pd, _pd,
+                                       _pd, _pu8, C.c_int]
+            L.ref_teardown.argtypes = []
+            cls._lib = L
+        return cls._lib
+
+    def __init__(self, proc, sqrts: float):
+        self.proc = proc
+        self.sqrts = float(sqrts)
+        t = _tables(proc)
+        self.lib().ref_setup(proc.n_in, proc.n_out, proc.n_channels, *t,
+                             np.ascontiguousarray(proc.flv_masses, np.float64),
+                             np.ascontiguousarray(proc.flv_widths, np.float64), self.sqrts)
+
+    def generate(self, x: np.ndarray, channels: Optional[np.ndarray] = None,
+                 threads: int = 0) -> Result:
+        x = np.ascontiguousarray(x, np.float64)
+        n, n_x = x.shape
+        r = Result(n, self.proc.n_out)
+        chp = None
+        if channels is not None:
+            channels = np.ascontiguousarray(channels, np.int32)
+            chp = channels.ctypes.data_as(C.c_void_p)
+        threads = threads or os.cpu_count() or 1
+        rc = self.lib().ref_generate(n, n_x, x.reshape(-1), chp, self.sqrts, r.p.reshape(-1),
+                                     r.factor, r.volume, r.ok, threads)
+        if rc != 0:
+            raise RuntimeError("reference harness not set up")
+        return r

@@ -1,0 +1,135 @@
+"""The CPU oracle (oracle/phs_oracle.c) pinned against the reference's golden vectors
+(the Whizard sample files) and against outputs of the reference's own phs_cpu.cpp."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import REFCPU_FIXTURES, golden, load_process, momentum_rel_err
+from gpu_phs_gb300 import processes as P
+from gpu_phs_gb300.philox import philox4x32_10, uniform_x
+from oracle import oracle
+
+
+def test_philox_known_answers():
+    # Random123 kat_vectors for philox4x32_10
+    cases = [([0, 0, 0, 0], [0, 0], [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]),
+             ([0xffffffff] * 4, [0xffffffff] * 2, [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]),
+             ([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0],
+              [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1])]
+    for ctr, key, want in cases:
+        got = philox4x32_10(np.array([ctr], np.uint32), np.array(key, np.uint32))[0]
+        assert [int(v) for v in got] == want
+
+
+def test_philox_stream_windows():
+    a = uniform_x(5, 40, 7)
+    assert np.array_equal(a[13:29], uniform_x(5, 16, 7, first_event=13))
+    assert a.min() >= 0 and a.max() < 1
+
+
+@pytest.mark.parametrize("name", ["ttH", "bwbw"])
+def test_oracle_vs_whizard_golden(name):
+    z = golden(f"whizard_{name}")
+    proc = load_process(z)
+    friendless = z["hasfriends"][z["channel"]] == 0
+    r = oracle.Oracle(proc, 1000.0).generate(z["x"], z["channel"])
+    assert np.array_equal(r.ok, z["ok"].astype(np.uint8))
+    # x is printed with 9 decimals, which limits momentum agreement to ~1e-4 GeV
+    dp = np.abs(r.p - z["p_out"])[friendless]
+    assert dp.max() < 1e-3
+    assert np.allclose(r.volume, z["volume"], rtol=1e-14, atol=0)
+    # factors are printed with 4-7 decimals
+    f, g = r.factor[friendless], z["factor"][friendless]
+    dec = 4 if name == "ttH" else 7
+    assert np.all(np.abs(f - g) <= 2e-3 * np.abs(g) + 0.5 * 10.0 ** -dec)
+
+
+@pytest.mark.parametrize("name", REFCPU_FIXTURES)
+def test_oracle_bitexact_vs_reference_fixture(name):
+    z = golden(f"refcpu_{name}")
+    proc = load_process(z)
+    x = uniform_x(int(z["seed"][0]), len(z["ok"]), proc.n_x)
+    assert x.sum() == z["x_checksum"][0]
+    r = oracle.Oracle(proc, float(z["sqrts"][0])).generate(x, z["channel"])
+    assert np.array_equal(r.ok, z["ok"])
+    ok = r.ok == 1
+    assert np.array_equal(r.p[ok], z["p"][ok])
+    assert np.array_equal(r.factor[ok], z["factor"][ok])
+    assert np.array_equal(r.volume[ok], z["volume"][ok])
+    assert np.all(r.p[~ok] == 0) and np.all(r.factor[~ok] == 0)
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference CPU path not built here")
+@pytest.mark.parametrize("builder", [P.ww, P.tt, P.precision])
+def test_oracle_bitexact_vs_live_reference(builder):
+    proc = builder()
+    x = uniform_x(77, 20000, proc.n_x)
+    r = oracle.Oracle(proc, proc.sqrts).generate(x)
+    q = oracle.RefCPU(proc, proc.sqrts).generate(x)
+    assert np.array_equal(r.ok, q.ok)
+    ok = r.ok == 1
+    assert np.array_equal(r.p[ok], q.p[ok])
+    assert np.array_equal(r.factor[ok], q.factor[ok])
+    assert np.array_equal(r.volume[ok], q.volume[ok])
+
+
+def test_oracle_invariants_tt():
+    proc = P.tt()
+    x = uniform_x(3, 5000, proc.n_x)
+    r = oracle.Oracle(proc, 1000.0).generate(x)
+    ok = r.ok == 1
+    assert 0.9 < ok.mean() < 1.0          # some events fall outside the kinematic limits
+    tot = r.p[ok].sum(axis=1)
+    assert np.allclose(tot[:, 0], 1000.0, rtol=1e-12)
+    assert np.abs(tot[:, 1:]).max() < 1e-9
+    m2 = r.p[ok, :, 0] ** 2 - (r.p[ok, :, 1:] ** 2).sum(-1)
+    masses = proc.flv_masses[2:] ** 2
+    assert np.abs(m2 - masses).max() < 1e-6
+
+
+def test_oracle_beams_uniform_matches_scalar():
+    proc = P.ww()
+    x = uniform_x(9, 1000, proc.n_x)
+    o = oracle.Oracle(proc, 500.0)
+    a = o.generate(x)
+    b = o.generate(x, E1=np.full(1000, 250.0), E2=np.full(1000, 250.0))
+    assert np.array_equal(a.ok, b.ok)
+    assert np.array_equal(a.p, b.p)
+    assert np.array_equal(a.factor, b.factor)
+
+
+def test_oracle_lab_boost_conserves_beam_momentum():
+    proc = P.ww()
+    x = uniform_x(10, 2000, proc.n_x)
+    E1, E2 = 300.0, 200.0
+    r = oracle.Oracle(proc, 500.0).generate(x, E1=np.full(2000, E1), E2=np.full(2000, E2))
+    ok = r.ok == 1
+    tot = r.p[ok].sum(axis=1)
+    assert np.allclose(tot[:, 0], E1 + E2, rtol=1e-12)
+    assert np.allclose(tot[:, 3], E1 - E2, atol=1e-9)
+
+
+def test_oracle_rejects_bad_trees():
+    proc = P.ww()
+    bad = proc.subset([0])
+    bad.d1 = bad.d1.copy()
+    bad.d1[0, 2] = 1
+    bad.d2 = bad.d2.copy()
+    bad.d2[0, 2] = 4            # code 3 -> (1, 4): does not OR to 3
+    with pytest.raises(ValueError):
+        oracle.Oracle(bad, 500.0)
+    bad = proc.subset([0])
+    bad.map_ids = bad.map_ids.copy()
+    bad.map_ids[0, 2] = 99      # ONSHELL has no implementation
+    with pytest.raises(ValueError):
+        oracle.Oracle(bad, 500.0)
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/samples"), reason="reference samples absent")
+def test_ref_reader_matches_fixture():
+    from gpu_phs_gb300.refformat import read_ref
+    proc, fr, ev = read_ref("/root/reference/samples/ttH.ref")
+    z = golden("whizard_ttH")
+    assert np.array_equal(proc.d1, z["d1"]) and np.array_equal(proc.map_ids, z["map_ids"])
+    assert len(ev.ok) == 999 and ev.x.shape == (999, 5)
