@@ -89,20 +89,21 @@ __device__ __forceinline__ void map_msq(int t, double x, double s, double m, dou
   }
 }
 
-// cos(theta) from x (phs_cpu.cpp:112-146).
+// cos(theta) from x (phs_cpu.cpp:112-146).  The collinear branch keeps the reference's
+// rounding: sin(theta) = sqrt(1 - ct^2) is ill-conditioned as |ct| -> 1.
 __device__ __forceinline__ void map_ct(int ct_class, double x, double b0, double b1, double &ct,
                                        double &st, double &f) {
   if (ct_class == PHS_CT_COLLINEAR) {
     double tmp;
     if (x < 0.5) {
-      tmp = b0 * exp(2.0 * x * b1);
-      ct = tmp - b0 - 1.0;
+      tmp = dmul(b0, exp(dmul(dmul(2.0, x), b1)));
+      ct = dsub(dsub(tmp, b0), 1.0);
     } else {
-      tmp = b0 * exp(2.0 * (1.0 - x) * b1);
-      ct = -(tmp - b0) + 1.0;
+      tmp = dmul(b0, exp(dmul(dmul(2.0, dsub(1.0, x)), b1)));
+      ct = dadd(-dsub(tmp, b0), 1.0);
     }
     if (ct >= -1.0 && ct <= 1.0) {
-      st = sqrt(1.0 - ct * ct);
+      st = sqrt(dsub(1.0, dmul(ct, ct)));
       f = tmp * b1;
     } else {
       ct = 1.0;
@@ -315,24 +316,25 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK)
       }
 
       // next frame: push one internal child, carry the other (or pop)
+      // (selects instead of indexing keep the child values in registers)
       if (V.push >= 0) {
-        const int j = V.push;
+        const bool j0 = V.push == 0;
 #pragma unroll
         for (int i = 0; i < 16; i++) stack_store(smem, sp, i, Ln[i]);
-        stack_store(smem, sp, 16, cmsq[j]);
-        stack_store(smem, sp, 17, cm[j]);
-        stack_store(smem, sp, 18, j == 0 ? pc : -pc);
-        stack_store(smem, sp, 19, cmax[j]);
+        stack_store(smem, sp, 16, j0 ? cmsq[0] : cmsq[1]);
+        stack_store(smem, sp, 17, j0 ? cm[0] : cm[1]);
+        stack_store(smem, sp, 18, j0 ? pc : -pc);
+        stack_store(smem, sp, 19, j0 ? cmax[0] : cmax[1]);
         sp++;
       }
       if (V.carry >= 0) {
-        const int j = V.carry;
+        const bool j0 = V.carry == 0;
 #pragma unroll
         for (int i = 0; i < 16; i++) L[i] = Ln[i];
-        msq_b = cmsq[j];
-        m_b = cm[j];
-        p_b = j == 0 ? pc : -pc;
-        mmax_b = cmax[j];
+        msq_b = j0 ? cmsq[0] : cmsq[1];
+        m_b = j0 ? cm[0] : cm[1];
+        p_b = j0 ? pc : -pc;
+        mmax_b = j0 ? cmax[0] : cmax[1];
       } else if (sp > 0) {
         sp--;
 #pragma unroll
