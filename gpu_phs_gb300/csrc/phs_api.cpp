@@ -547,6 +547,73 @@ extern "C" int phs_batch_generate_device(phs_batch_t b, const int64_t *counts, c
   return PHS_OK;
 }
 
+// ------------------------------------------------------- generation without allocation
+// For callers that cannot allocate device memory: the channel programs are compiled here
+// on the host at the given beams, and the programs and the segment table go into the
+// library's file-scope device scratch array (phs_kernels.cu) instead of buffers from
+// cudaMalloc.  Nothing on this path calls cudaMalloc, cudaFree or an allocating library
+// routine.  At most PHS_NOALLOC_MAX_CHANNELS channels.  The first call on a device
+// resolves the scratch array's address (make it before any stream capture).  Calls that
+// overlap on the GPU share the scratch array and race.
+extern "C" int phs_generate_device_noalloc(phs_process_t h, double E1, double E2,
+                                           int64_t n_events, const int64_t *counts,
+                                           const double *x, double *p, double *f, double *v,
+                                           uint8_t *ok, void *stream) {
+  if (int rc = check_proc(h)) return rc;
+  if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
+  if (int rc = check_ptrs(n_events, x, p, f, v, ok)) return rc;
+  if (!(E1 > 0) || !(E2 > 0) || !isfinite(E1) || !isfinite(E2))
+    return fail(PHS_ERR_INVALID_ARG, "beam energies must be positive and finite");
+  const phs::Process &P = h->p;
+  if (P.n_channels > PHS_NOALLOC_MAX_CHANNELS)
+    return fail(PHS_ERR_UNSUPPORTED, "phs_generate_device_noalloc takes at most %d channels "
+                "(its static device scratch holds %zu bytes); this process has %d",
+                PHS_NOALLOC_MAX_CHANNELS, phs_noalloc_scratch_bytes(), P.n_channels);
+  const double sqrts = 2 * sqrt(E1 * E2);
+  double m_tot = 0;
+  for (int k = 0; k < P.n_out; k++) m_tot += P.flv_m[P.n_in + k];
+  if (!(sqrts > m_tot))
+    return fail(PHS_ERR_INVALID_ARG, "sqrt(s) = %g is below the final-state mass sum %g", sqrts,
+                m_tot);
+  DeviceGuard g(h->device);
+  std::vector<PhsChannel> prog(P.n_channels);
+  int depth = 0;
+  std::string err;
+  const double bg = (E1 - E2) / (2 * sqrt(E1 * E2));
+  for (int c = 0; c < P.n_channels; c++) {
+    phs::ChannelInfo info;
+    int rc = phs::compile_channel(P, c, sqrts, prog[c], info, err);
+    if (rc) return fail(rc, "%s", err.c_str());
+    prog[c].sqrts = sqrts;
+    prog[c].lab = E1 != E2;
+    prog[c].lab_bg = bg;
+    prog[c].lab_gamma = sqrt(1 + bg * bg);
+    depth = std::max(depth, info.stack_depth);
+  }
+  std::vector<ChanLayout> lay(P.n_channels, ChanLayout{P.n_out, P.n_x});
+  int64_t one = n_events;
+  Segments S;
+  int rc = build_segments(S, counts ? counts : &one, P.n_channels, lay, 0, 0, 0, false);
+  if (rc) return rc;
+  PhsLaunch a;
+  memset(&a, 0, sizeof a);
+  a.stack_depth = depth;
+  a.n_tiles = S.n_tiles;
+  a.x = x;
+  a.p = p;
+  a.factor = f;
+  a.volume = v;
+  a.ok = ok;
+  a.factor_stride = 1;
+  if (S.host.size() <= PHS_INLINE_SEGS) std::copy(S.host.begin(), S.host.end(), a.seg_inline);
+  const int grid = a.n_tiles > 0 ? grid_for(a.n_tiles, h->device, depth, false) : 1;
+  cudaError_t e = phs_launch_forward_f64_noalloc(a, prog.data(), P.n_channels, S.host.data(),
+                                                 (int)S.host.size(), grid, (cudaStream_t)stream);
+  if (e != cudaSuccess)
+    return fail(PHS_ERR_CUDA, "phs_generate_device_noalloc: %s", cudaGetErrorString(e));
+  return PHS_OK;
+}
+
 // ---------------------------------------------------------------------- random numbers
 extern "C" int phs_philox_fill(double *x, int64_t n_events, int n_x, uint64_t seed,
                                int64_t first_event, void *stream) {

@@ -41,3 +41,13 @@ cudaError_t phs_launch_philox(double *x, int64_t n_events, int32_t n_x, uint64_t
 // per thread.  Used to measure the FP64 and FP32 peaks the roofline is quoted against.
 cudaError_t phs_launch_fma_rate(void *out, int fp64, int blocks, int threads, int iters,
                                 cudaStream_t stream);
+
+// Forward launch whose channel programs and segment table are copied into a file-scope
+// device array of phs_kernels.cu (no device allocation; see there).  At most
+// PHS_NOALLOC_MAX_CHANNELS channels and as many segments; returns cudaErrorInvalidValue
+// beyond that.  The first call on a device resolves the array's device address.
+#define PHS_NOALLOC_MAX_CHANNELS 256
+cudaError_t phs_launch_forward_f64_noalloc(PhsLaunch a, const PhsChannel *channels,
+                                           int n_channels, const PhsSegment *segments,
+                                           int n_segments, int n_blocks, cudaStream_t stream);
+size_t phs_noalloc_scratch_bytes();

@@ -458,3 +458,63 @@ cudaError_t phs_launch_philox(double *x, int64_t n_events, int32_t n_x, uint64_t
   phs_philox_kernel<<<grid, 256, 0, stream>>>(x, first_event * n_x, n, seed);
   return cudaGetLastError();
 }
+
+// ------------------------------------------------------------------------------------
+// Forward generation without device allocation.
+//
+// For callers that must not allocate device memory: code running inside a host that
+// owns the device heap through its own allocator, sandboxes or plugins denied cudaMalloc,
+// and drivers that would otherwise synchronise the device inside their hot loop.  The
+// channel programs and the segment table, which the regular entry points keep in buffers
+// the library allocates, live here in one file-scope device array instead.  Every GPU
+// that loads the library holds this array (sizeof(PhsNoAllocScratch), about 0.8 MB) until
+// the process exits.  All calls share it and it keeps the last call's contents; each call
+// overwrites everything it reads, so nothing needs clearing, but calls that overlap on
+// the GPU (different streams or host threads) race on it.
+struct PhsNoAllocScratch {
+  PhsChannel channels[PHS_NOALLOC_MAX_CHANNELS];
+  PhsSegment segments[PHS_NOALLOC_MAX_CHANNELS];
+};
+
+static __device__ __align__(256) unsigned char phs_noalloc_scratch[sizeof(PhsNoAllocScratch)];
+
+// Device address of the scratch array per device (filled at set-up; in host code the
+// array's name only stands in for the symbol and is never a device address).
+static void *g_noalloc_addr[256];
+
+size_t phs_noalloc_scratch_bytes() { return sizeof(PhsNoAllocScratch); }
+
+cudaError_t phs_launch_forward_f64_noalloc(PhsLaunch a, const PhsChannel *channels,
+                                           int n_channels, const PhsSegment *segments,
+                                           int n_segments, int n_blocks, cudaStream_t stream) {
+  if (n_channels > PHS_NOALLOC_MAX_CHANNELS || n_segments > PHS_NOALLOC_MAX_CHANNELS)
+    return cudaErrorInvalidValue;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
+  if (!g_noalloc_addr[dev]) {
+    // set-up, once per device, with that device current
+    void *ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, phs_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_addr[dev] = ptr;
+  }
+  PhsNoAllocScratch *s = static_cast<PhsNoAllocScratch *>(g_noalloc_addr[dev]);
+  // pageable host sources: each copy has read its source when the call returns
+  e = cudaMemcpyAsync(s->channels, channels, (size_t)n_channels * sizeof(PhsChannel),
+                      cudaMemcpyHostToDevice, stream);
+  if (e != cudaSuccess) return e;
+  if (n_segments > 0) {
+    e = cudaMemcpyAsync(s->segments, segments, (size_t)n_segments * sizeof(PhsSegment),
+                        cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return e;
+  }
+  a.channels = s->channels;
+  a.segments = s->segments;
+  a.n_segments = n_segments;
+  if (a.n_tiles <= 0) return cudaSuccess;
+  const size_t smem = phs_forward_smem_bytes(a.stack_depth);
+  phs_forward_f64_kernel<false><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+  return cudaGetLastError();
+}

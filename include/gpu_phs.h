@@ -97,6 +97,18 @@ int phs_generate_beams_device(phs_process_t proc, int64_t n_events, const int64_
                               const double *E1, const double *E2, const double *x, double *p,
                               double *factors, double *volumes, uint8_t *oks, void *stream);
 
+/* As phs_generate_device, for callers that cannot allocate device memory (a host that owns
+ * the device heap through its own allocator, a sandbox or plug-in host that denies
+ * cudaMalloc, or a loop that must not synchronise the device): takes the beam energies
+ * itself and needs no phs_process_set_beams.  It allocates nothing: the channel programs
+ * and event segments go into one static device array of the library, so the process may
+ * have at most 256 channels (PHS_ERR_UNSUPPORTED beyond).  The first call on a device
+ * resolves that array's address; make it before any stream capture.  All calls share the
+ * array, so calls that overlap on the GPU race.  No counterpart in the reference. */
+int phs_generate_device_noalloc(phs_process_t proc, double E1, double E2, int64_t n_events,
+                                const int64_t *channel_counts, const double *x, double *p,
+                                double *factors, double *volumes, uint8_t *oks, void *stream);
+
 /* Host pointers in and out (pinned memory is fastest); copies run chunk-pipelined with the
  * kernel.  Synchronous. */
 int phs_generate_host(phs_process_t proc, int64_t n_events, const int64_t *channel_counts,
