@@ -38,6 +38,10 @@ class Events:
     ok: "object"      # [n] uint8
 
 
+PRECISION_F64 = 0     # IEEE FP64 throughout
+PRECISION_F32X2 = 1   # float-float pairs on the FP32 pipe, FP64 next to kinematic limits
+
+
 class PhaseSpace:
     """One process on the current CUDA device."""
 
@@ -58,6 +62,10 @@ class PhaseSpace:
 
     def set_beams(self, E1: float, E2: float) -> None:
         check(load().phs_process_set_beams(self.h, float(E1), float(E2)))
+
+    def set_precision(self, precision: int) -> None:
+        """PRECISION_F64 (default) or PRECISION_F32X2 for the uniform-beam generate calls."""
+        check(load().phs_process_set_precision(self.h, int(precision)))
 
     def close(self) -> None:
         if getattr(self, "h", None):
@@ -161,6 +169,9 @@ class Batch:
     @property
     def n_channels(self) -> int:
         return len(self.n_outs)
+
+    def set_precision(self, precision: int) -> None:
+        check(load().phs_batch_set_precision(self.h, int(precision)))
 
     def offsets(self, counts):
         c = np.ascontiguousarray(counts, np.int64)

@@ -150,6 +150,53 @@ int grid_for(int64_t n_tiles, int device, int stack_depth, bool per_event) {
   return (int)std::max<int64_t>(1, std::min(want, cap));
 }
 
+int grid_for_ff(int64_t n_tiles, int device, int stack_depth, int variant) {
+  const int warps_per_block = PHS_FWD_BLOCK / 32;
+  int64_t want = (n_tiles + warps_per_block - 1) / warps_per_block;
+  int64_t cap = (int64_t)sm_count(device) * phs_forward_ff_blocks_per_sm(stack_depth, variant);
+  return (int)std::max<int64_t>(1, std::min(want, cap));
+}
+
+// FP32-pair launch with autotuning.  The kernel comes in PHS_FF_VARIANTS register budgets
+// (resident blocks per SM); they compute identical bits.  The first launch of at least
+// kTuneEvents events, outside stream capture, runs every variant twice on the real data,
+// times them with CUDA events on the launch stream and keeps the fastest in `variant`.
+const int64_t kTuneEvents = 1 << 18;
+
+int launch_ff_tuned(int &variant, const PhsLaunch &a, int device, int depth, int64_t n_events,
+                    cudaStream_t st) {
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(st, &cap);
+  if (variant < 0 && n_events >= kTuneEvents && cap == cudaStreamCaptureStatusNone) {
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    float best[PHS_FF_VARIANTS];
+    for (int v = 0; v < PHS_FF_VARIANTS; v++) best[v] = 1e30f;
+    for (int rep = 0; rep < 2; rep++) {
+      for (int v = 0; v < PHS_FF_VARIANTS; v++) {
+        CUDA_TRY(cudaEventRecord(e0, st));
+        CUDA_TRY(phs_launch_forward_ff(a, grid_for_ff(a.n_tiles, device, depth, v), v, st));
+        CUDA_TRY(cudaEventRecord(e1, st));
+        CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        best[v] = std::min(best[v], ms);
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int bv = 0;
+    for (int v = 1; v < PHS_FF_VARIANTS; v++)
+      if (best[v] < best[bv]) bv = v;
+    variant = bv;
+    return PHS_OK;  // the timed launches already wrote the outputs
+  }
+  const int v = variant < 0 ? 0 : variant;
+  CUDA_TRY(phs_launch_forward_ff(a, grid_for_ff(a.n_tiles, device, depth, v), v, st));
+  return PHS_OK;
+}
+
 // Restores the caller's current device on scope exit.
 struct DeviceGuard {
   int prev = -1;
@@ -172,10 +219,13 @@ struct phs_process {
   int device = 0;
   bool beams = false;
   double E1 = 0, E2 = 0;
+  int precision = PHS_PRECISION_F64;
+  int ff_variant = -1;  // autotuned FP32-pair kernel variant (-1: not tuned yet)
   std::vector<PhsChannel> prog;
+  std::vector<PhsChannelFF> prog_ff;
   std::vector<ChanLayout> lay;
   int stack_depth = 0;
-  DevBuf d_prog;
+  DevBuf d_prog, d_prog_ff;
   Segments segs;
   // host-path pipeline
   static const int kStreams = 2;
@@ -244,6 +294,7 @@ extern "C" int phs_process_destroy(phs_process_t h) {
     h->bo[s].release(); h->pseg[s].dev.release();
   }
   h->d_prog.release();
+  h->d_prog_ff.release();
   h->segs.dev.release();
   delete h;
   return PHS_OK;
@@ -276,16 +327,36 @@ extern "C" int phs_process_set_beams(phs_process_t h, double E1, double E2) {
     prog[c].lab_gamma = sqrt(1 + bg * bg);
     depth = std::max(depth, info.stack_depth);
   }
+  std::vector<PhsChannelFF> prog_ff(prog.size());
+  for (size_t c = 0; c < prog.size(); c++) phs::channel_to_ff(prog[c], prog_ff[c]);
   int rc = h->d_prog.reserve(prog.size() * sizeof(PhsChannel));
   if (rc) return rc;
+  if ((rc = h->d_prog_ff.reserve(prog_ff.size() * sizeof(PhsChannelFF)))) return rc;
   CUDA_TRY(cudaMemcpy(h->d_prog.ptr, prog.data(), prog.size() * sizeof(PhsChannel),
                       cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(h->d_prog_ff.ptr, prog_ff.data(), prog_ff.size() * sizeof(PhsChannelFF),
+                      cudaMemcpyHostToDevice));
   h->prog = std::move(prog);
+  h->prog_ff = std::move(prog_ff);
   h->lay.assign(P.n_channels, ChanLayout{P.n_out, P.n_x});
   h->stack_depth = depth;
   h->E1 = E1;
   h->E2 = E2;
   h->beams = true;
+  return PHS_OK;
+}
+
+extern "C" int phs_process_set_precision(phs_process_t h, int precision) {
+  if (int rc = check_proc(h)) return rc;
+  if (precision != PHS_PRECISION_F64 && precision != PHS_PRECISION_F32X2)
+    return fail(PHS_ERR_INVALID_ARG, "unknown precision mode %d", precision);
+  h->precision = precision;
+  return PHS_OK;
+}
+
+extern "C" int phs_process_tuning(phs_process_t h, int *ff_variant) {
+  if (int rc = check_proc(h)) return rc;
+  if (ff_variant) *ff_variant = h->ff_variant;
   return PHS_OK;
 }
 
@@ -338,6 +409,7 @@ static int launch_process(phs_process_t h, Segments &S, int64_t n_events, const 
   PhsLaunch a;
   memset(&a, 0, sizeof a);
   a.channels = h->d_prog.as<PhsChannel>();
+  a.channels_ff = h->d_prog_ff.as<PhsChannelFF>();
   a.stack_depth = h->stack_depth;
   a.x = x;
   a.p = p;
@@ -351,6 +423,8 @@ static int launch_process(phs_process_t h, Segments &S, int64_t n_events, const 
   for (auto &g : S.host) g.ev_begin -= ev0;
   if ((rc = attach_segments(S, a, stream))) return rc;
   if (a.n_tiles == 0) return PHS_OK;
+  if (h->precision == PHS_PRECISION_F32X2 && E1 == nullptr)
+    return launch_ff_tuned(h->ff_variant, a, h->device, h->stack_depth, n_events, stream);
   const int grid = grid_for(a.n_tiles, h->device, h->stack_depth, E1 != nullptr);
   CUDA_TRY(phs_launch_forward_f64(a, grid, stream));
   return PHS_OK;
@@ -449,10 +523,13 @@ extern "C" int phs_generate_host(phs_process_t h, int64_t n_events, const int64_
 // ---------------------------------------------------------------------------- batches
 struct phs_batch {
   int device = 0;
+  int precision = PHS_PRECISION_F64;
+  int ff_variant = -1;
   std::vector<PhsChannel> prog;
+  std::vector<PhsChannelFF> prog_ff;
   std::vector<ChanLayout> lay;
   int stack_depth = 0;
-  DevBuf d_prog;
+  DevBuf d_prog, d_prog_ff;
   Segments segs;
 };
 
@@ -469,16 +546,23 @@ extern "C" int phs_batch_create(phs_batch_t *out, int n_procs, const phs_process
       return fail(PHS_ERR_STATE, "process %d is null or has no beams set", i);
     }
     b->prog.insert(b->prog.end(), h->prog.begin(), h->prog.end());
+    b->prog_ff.insert(b->prog_ff.end(), h->prog_ff.begin(), h->prog_ff.end());
     b->lay.insert(b->lay.end(), h->lay.begin(), h->lay.end());
     b->stack_depth = std::max(b->stack_depth, h->stack_depth);
   }
   DeviceGuard g(b->device);
   int rc = b->d_prog.reserve(b->prog.size() * sizeof(PhsChannel));
   if (rc) { delete b; return rc; }
+  rc = b->d_prog_ff.reserve(b->prog_ff.size() * sizeof(PhsChannelFF));
+  if (rc) { b->d_prog.release(); delete b; return rc; }
   cudaError_t e = cudaMemcpy(b->d_prog.ptr, b->prog.data(), b->prog.size() * sizeof(PhsChannel),
                              cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_prog_ff.ptr, b->prog_ff.data(), b->prog_ff.size() * sizeof(PhsChannelFF),
+                   cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     b->d_prog.release();
+    b->d_prog_ff.release();
     delete b;
     return fail(PHS_ERR_CUDA, "cudaMemcpy of batch programs failed: %s", cudaGetErrorString(e));
   }
@@ -490,6 +574,7 @@ extern "C" int phs_batch_destroy(phs_batch_t b) {
   if (!b) return PHS_OK;
   DeviceGuard g(b->device);
   b->d_prog.release();
+  b->d_prog_ff.release();
   b->segs.dev.release();
   delete b;
   return PHS_OK;
@@ -533,6 +618,7 @@ extern "C" int phs_batch_generate_device(phs_batch_t b, const int64_t *counts, c
   PhsLaunch a;
   memset(&a, 0, sizeof a);
   a.channels = b->d_prog.as<PhsChannel>();
+  a.channels_ff = b->d_prog_ff.as<PhsChannelFF>();
   a.stack_depth = b->stack_depth;
   a.x = x;
   a.p = p;
@@ -542,8 +628,19 @@ extern "C" int phs_batch_generate_device(phs_batch_t b, const int64_t *counts, c
   a.factor_stride = 1;
   if ((rc = attach_segments(b->segs, a, (cudaStream_t)stream))) return rc;
   if (a.n_tiles == 0) return PHS_OK;
+  if (b->precision == PHS_PRECISION_F32X2)
+    return launch_ff_tuned(b->ff_variant, a, b->device, b->stack_depth, n_events,
+                           (cudaStream_t)stream);
   const int grid = grid_for(a.n_tiles, b->device, b->stack_depth, false);
   CUDA_TRY(phs_launch_forward_f64(a, grid, (cudaStream_t)stream));
+  return PHS_OK;
+}
+
+extern "C" int phs_batch_set_precision(phs_batch_t b, int precision) {
+  if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
+  if (precision != PHS_PRECISION_F64 && precision != PHS_PRECISION_F32X2)
+    return fail(PHS_ERR_INVALID_ARG, "unknown precision mode %d", precision);
+  b->precision = precision;
   return PHS_OK;
 }
 

@@ -283,4 +283,68 @@ int compile_channel(const Process &p, int c, double sqrts, PhsChannel &out, Chan
   return PHS_OK;
 }
 
+static PhsFF split(double d) {
+  PhsFF r;
+  r.hi = (float)d;
+  r.lo = (float)(d - (double)r.hi);
+  return r;
+}
+
+static PhsFF split_ld(long double d) {
+  PhsFF r;
+  r.hi = (float)d;
+  r.lo = (float)(d - (long double)r.hi);
+  return r;
+}
+
+void channel_to_ff(const PhsChannel &in, PhsChannelFF &out) {
+  memset(&out, 0, sizeof(out));
+  out.n_out = in.n_out;
+  out.n_visits = in.n_visits;
+  out.lab = in.lab;
+  out.sqrts = split(in.sqrts);
+  out.s = split(in.sqrts * in.sqrts);
+  out.lab_bg = split(in.lab_bg);
+  out.lab_gamma = split(in.lab_gamma);
+  out.volume = in.volume;
+  for (int v = 0; v < in.n_visits; v++) {
+    const PhsVisit &V = in.visit[v];
+    PhsVisitFF &F = out.visit[v];
+    for (int j = 0; j < 2; j++) {
+      const PhsChild &C = V.child[j];
+      PhsChildFF &G = F.child[j];
+      G.internal = C.internal;
+      G.out_index = C.out_index;
+      G.map_id = C.map_id;
+      G.x_msq = C.x_msq;
+      G.msq_leaf = split(C.msq_leaf);
+      G.m_leaf = split(C.m_leaf);
+      G.m2 = split(C.m * C.m);
+      G.mw = split(C.m * C.w);
+      G.a0 = split(C.a0);
+      G.a1 = split(C.map_id == PHS_MAP_SCHANNEL ? C.a1 - C.a0 : C.a1);
+      G.a2 = split(C.map_id == PHS_MAP_NO ? (C.msq_max - C.msq_min) / (in.sqrts * in.sqrts) : C.a2);
+      G.msq_min = split(C.msq_min);
+      G.msq_max = split(C.msq_max);
+      G.m_max = split(C.m_max);
+      if (C.map_id == PHS_MAP_SCHANNEL) {
+        const long double half_pi = 1.57079632679489661923132169163975144L;
+        G.u0 = split_ld(half_pi + (long double)C.a0);
+        G.u1 = split_ld(half_pi - (long double)C.a1);
+      }
+      if (C.internal && (C.map_id == PHS_MAP_STEP_E || C.map_id == PHS_MAP_STEP_H)) out.exact_only = 1;
+    }
+    F.x_phi = V.x_phi;
+    F.x_ct = V.x_ct;
+    F.ct_class = V.ct_class;
+    F.carry = V.carry;
+    F.push = V.push;
+    F.self_root = V.self_root;
+    F.both_leaves = V.both_leaves;
+    F.b0 = split(V.b0);
+    F.b1 = split(V.b1);
+    F.self_m_max = split(V.self_m_max);
+  }
+}
+
 }  // namespace phs

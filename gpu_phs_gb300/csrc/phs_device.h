@@ -10,6 +10,7 @@
 // One forward launch over a list of segments (runs of events of one channel).
 struct PhsLaunch {
   const PhsChannel *channels;  // device, per channel
+  const PhsChannelFF *channels_ff;  // device, float-float copies (FP32-pair kernel only)
   const PhsSegment *segments;  // device table, used when n_segments > PHS_INLINE_SEGS
   PhsSegment seg_inline[PHS_INLINE_SEGS];  // sorted by tile_begin
   int32_t n_segments;
@@ -51,3 +52,12 @@ cudaError_t phs_launch_forward_f64_noalloc(PhsLaunch a, const PhsChannel *channe
                                            int n_channels, const PhsSegment *segments,
                                            int n_segments, int n_blocks, cudaStream_t stream);
 size_t phs_noalloc_scratch_bytes();
+
+// Forward launch on the FP32 pipe (float-float arithmetic), FP64 only for events within
+// 1e-5 of a kinematic limit, which are recomputed exactly (phs_kernels_ff.cu).  Needs
+// a.channels and a.channels_ff; uniform beams only.
+// variant: 0 = registers for 3 resident blocks per SM, 1 = for 4 (PHS_FF_VARIANTS).
+#define PHS_FF_VARIANTS 2
+cudaError_t phs_launch_forward_ff(const PhsLaunch &a, int n_blocks, int variant, cudaStream_t stream);
+int phs_forward_ff_blocks_per_sm(int stack_depth, int variant);
+size_t phs_forward_ff_smem_bytes(int stack_depth);

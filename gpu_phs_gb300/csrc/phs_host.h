@@ -31,6 +31,9 @@ struct ChannelInfo {
 int compile_channel(const Process &p, int c, double sqrts, PhsChannel &out, ChannelInfo &info,
                     std::string &err);
 
+// Float-float copy of a compiled channel (same visit order and x indices).
+void channel_to_ff(const PhsChannel &in, PhsChannelFF &out);
+
 // Validates the sizes and tables of a whole process (no sqrt(s) needed).
 int validate_process(const Process &p, std::string &err);
 

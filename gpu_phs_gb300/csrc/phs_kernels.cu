@@ -5,182 +5,16 @@
 // thread walks its event's visit program top-down (phs_program.h) with the running 4x4
 // boost in registers and at most two saved frames on a per-thread shared-memory stack.
 //
-// Arithmetic follows the reference CPU path (phs_cpu.cpp), whose expression order it keeps
-// with explicit round-to-nearest intrinsics wherever a value feeds the kinematic ok test
-// (msq mappings, the Kallen function and the mass sums), so ok flags match the reference
-// bit for bit whenever the transcendental functions agree; factors and boosts use FMA.
+// The per-event arithmetic is in phs_event_f64.cuh.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
 
 #include "phs_device.h"
+#include "phs_event_f64.cuh"
 #include "phs_program.h"
 
-#define PHS_PI 3.14159265358979323846
-#define PHS_TWOPI2 39.47841760435743447534
-#define PHS_TWOPI5 9792.62991312900650440772
-#define PHS_STATE 20  // doubles per saved frame: L[16], msq, m, p, m_max
-
 namespace {
-
-__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
-
-// msq from x (phs_cpu.cpp:12-61), same expression order, no contraction.
-__device__ __forceinline__ void map_msq(int t, double x, double s, double m, double w,
-                                        double msq_min, double msq_max, double a0, double a1,
-                                        double a2, double &msq, double &f) {
-  switch (t) {
-    case PHS_MAP_NO:
-      msq = dadd(dmul(dsub(1.0, x), msq_min), dmul(x, msq_max));
-      f = (msq_max - msq_min) / s;
-      break;
-    case PHS_MAP_SCHANNEL: {
-      double z = dadd(dmul(dsub(1.0, x), a0), dmul(x, a1));
-      if (-PHS_PI / 2 < z && z < PHS_PI / 2) {
-        double tz = tan(z);
-        msq = dmul(m, dadd(m, dmul(w, tz)));
-        f = a2 * (1.0 + tz * tz);
-      } else {
-        msq = 0.0;
-        f = 0.0;
-      }
-      break;
-    }
-    case PHS_MAP_COLLINEAR:
-    case PHS_MAP_INFRARED:
-    case PHS_MAP_RADIATION: {
-      double msq1 = dmul(a0, exp(dmul(x, a1)));
-      msq = dadd(dsub(msq1, a0), msq_min);
-      f = a2 * msq1;
-      break;
-    }
-    case PHS_MAP_TCHANNEL:
-    case PHS_MAP_UCHANNEL: {
-      double msq1;
-      if (x < 0.5) {
-        msq1 = dmul(a0, exp(dmul(x, a1)));
-        msq = dadd(dsub(msq1, a0), msq_min);
-      } else {
-        msq1 = dmul(a0, exp(dmul(dsub(1.0, x), a1)));
-        msq = dadd(-dsub(msq1, a0), msq_max);
-      }
-      f = a2 * msq1;
-      break;
-    }
-    case PHS_MAP_STEP_H: {
-      double am = dsub(a0, x);
-      double z = dadd(dsub(a1 / am, a1 / a0), dmul(a2, x));
-      msq = dadd(dmul(z, msq_max), dmul(dsub(1.0, z), msq_min));
-      f = (a1 / (am * am) + a2) * (msq_max - msq_min) / s;
-      break;
-    }
-    case PHS_MAP_STEP_E: {
-      double tmp = dmul(exp(dmul(-x, a0) / a2), dadd(1.0, a1));
-      double z = dmul(-a2, log(dsub(tmp, a1)));
-      msq = dadd(dmul(z, msq_max), dmul(dsub(1.0, z), msq_min));
-      f = a0 / (1.0 - a1 / tmp) * (msq_max - msq_min) / s;
-      break;
-    }
-    default:
-      msq = 0.0;
-      f = 0.0;
-  }
-}
-
-// cos(theta) from x (phs_cpu.cpp:112-146).  The collinear branch keeps the reference's
-// rounding: sin(theta) = sqrt(1 - ct^2) is ill-conditioned as |ct| -> 1.
-__device__ __forceinline__ void map_ct(int ct_class, double x, double b0, double b1, double &ct,
-                                       double &st, double &f) {
-  if (ct_class == PHS_CT_COLLINEAR) {
-    double tmp;
-    if (x < 0.5) {
-      tmp = dmul(b0, exp(dmul(dmul(2.0, x), b1)));
-      ct = dsub(dsub(tmp, b0), 1.0);
-    } else {
-      tmp = dmul(b0, exp(dmul(dmul(2.0, dsub(1.0, x)), b1)));
-      ct = dadd(-dsub(tmp, b0), 1.0);
-    }
-    if (ct >= -1.0 && ct <= 1.0) {
-      st = sqrt(dsub(1.0, dmul(ct, ct)));
-      f = tmp * b1;
-    } else {
-      ct = 1.0;
-      st = 0.0;
-      f = 0.0;
-    }
-  } else {
-    double tmp = 2.0 * (1.0 - x);
-    ct = 1.0 - tmp;
-    st = sqrt(tmp * (2.0 - tmp));
-    f = 1.0;
-  }
-}
-
-// Mapping constants at one sqrt(s) (phs_cpu.cpp:452-531), for the per-event-beam path.
-__device__ void child_constants(const PhsChild &C, double sqrts, double m_tot, double &a0,
-                                double &a1, double &a2, double &msq_min, double &msq_max,
-                                double &m_max) {
-  double m = C.m, w = C.w, m_min = C.m_min;
-  m_max = dadd(dsub(sqrts, m_tot), m_min);
-  msq_min = dmul(m_min, m_min);
-  msq_max = dmul(m_max, m_max);
-  double s = dmul(sqrts, sqrts);
-  a0 = a1 = a2 = 0.0;
-  switch (C.map_id) {
-    case PHS_MAP_NO:
-      a1 = msq_max - msq_min;
-      a2 = a1 / s;
-      break;
-    case PHS_MAP_SCHANNEL: {
-      double msq0 = dmul(m, m), mw = dmul(m, w);
-      a0 = atan(dsub(msq_min, msq0) / mw);
-      a1 = atan(dsub(msq_max, msq0) / mw);
-      a2 = dmul(dsub(a1, a0), mw) / s;
-      break;
-    }
-    case PHS_MAP_RADIATION:
-    case PHS_MAP_COLLINEAR:
-    case PHS_MAP_INFRARED: {
-      double msq0 = C.map_id == PHS_MAP_RADIATION ? dmul(w, w) : dmul(m, m);
-      a0 = msq0;
-      a1 = log(dadd(dsub(msq_max, msq_min) / msq0, 1.0));
-      a2 = a1 / s;
-      break;
-    }
-    case PHS_MAP_TCHANNEL:
-    case PHS_MAP_UCHANNEL: {
-      double msq0 = dmul(m, m);
-      a0 = msq0;
-      a1 = dmul(2.0, log(dadd(dsub(msq_max, msq_min) / dmul(2.0, msq0), 1.0)));
-      a2 = a1 / s;
-      break;
-    }
-    case PHS_MAP_STEP_E: {
-      double r = dmul(dmul(2.0, m), w) / dsub(msq_max, msq_min);
-      a2 = r > 0.01 ? r : 0.01;
-      a1 = exp(-(dsub(dmul(m, m), msq_min)) / dsub(msq_max, msq_min) / a2);
-      a0 = dsub(1.0, dmul(a2, log(dadd(1.0, dmul(a1, exp(1.0 / a2))) / dadd(1.0, a1))));
-      break;
-    }
-    case PHS_MAP_STEP_H: {
-      a2 = dsub(dmul(m, m), msq_min) / dsub(msq_max, msq_min);
-      double q = dmul(dmul(2.0, m), w) / dsub(msq_max, msq_min);
-      double r = dmul(q, q) / a2;
-      a1 = r > 0.000001 ? r : 0.000001;
-      a0 = dadd(1.0, sqrt(dadd(1.0, dmul(4.0, a1) / dsub(1.0, a2)))) / 2.0;
-      break;
-    }
-  }
-}
-
-__device__ __forceinline__ void stack_store(double *smem, int depth, int k, double v) {
-  smem[(depth * PHS_STATE + k) * PHS_FWD_BLOCK + threadIdx.x] = v;
-}
-__device__ __forceinline__ double stack_load(const double *smem, int depth, int k) {
-  return smem[(depth * PHS_STATE + k) * PHS_FWD_BLOCK + threadIdx.x];
-}
 
 template <bool PER_EVENT>
 __global__ void __launch_bounds__(PHS_FWD_BLOCK)
@@ -201,171 +35,7 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK)
     const PhsSegment seg = segs[lo];
     const int64_t local = (tile - seg.tile_begin) * 32 + lane;
     if (local >= seg.ev_count) continue;
-    const PhsChannel &ch = a.channels[seg.channel];
-    const int64_t ev = seg.ev_begin + local;
-    const double *xe = a.x + seg.x_base + local * seg.x_stride;
-    double *out = a.p + seg.p_base + local * 4 * (int64_t)ch.n_out;
-
-    double sqrts = ch.sqrts;
-    double lab_bg = ch.lab_bg, lab_ga = ch.lab_gamma;
-    bool lab = ch.lab != 0;
-    if (PER_EVENT) {
-      double E1 = a.E1[ev], E2 = a.E2[ev];
-      double r = sqrt(dmul(E1, E2));
-      sqrts = dmul(2.0, r);
-      lab = E1 != E2;
-      lab_bg = dsub(E1, E2) / dmul(2.0, r);
-      lab_ga = sqrt(1.0 + lab_bg * lab_bg);
-    }
-    const double s = dmul(sqrts, sqrts);
-
-    // frame of the visited branch; the root's parent frame is the lab boost (or 1)
-    double L[16];
-#pragma unroll
-    for (int i = 0; i < 16; i++) L[i] = 0.0;
-    L[0] = lab ? lab_ga : 1.0;
-    L[5] = 1.0;
-    L[10] = 1.0;
-    L[15] = L[0];
-    L[3] = lab ? lab_bg : 0.0;
-    L[12] = L[3];
-    double msq_b = s, m_b = sqrts, p_b = 0.0, mmax_b = sqrts;
-    double factor = 1.0;
-    bool ok = true;
-    int sp = 0;
-
-    const int n_visits = ch.n_visits;
-    for (int v = 0; v < n_visits; v++) {
-      const PhsVisit &V = ch.visit[v];
-      double cmsq[2], cm[2], cmax[2];
-#pragma unroll
-      for (int j = 0; j < 2; j++) {
-        const PhsChild &C = V.child[j];
-        if (!C.internal) {
-          cmsq[j] = C.msq_leaf;
-          cm[j] = C.m_leaf;
-          cmax[j] = 0.0;
-        } else {
-          double a0 = C.a0, a1 = C.a1, a2 = C.a2, mn = C.msq_min, mx = C.msq_max;
-          cmax[j] = C.m_max;
-          if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, a0, a1, a2, mn, mx, cmax[j]);
-          double f;
-          map_msq(C.map_id, xe[C.x_msq], s, C.m, C.w, mn, mx, a0, a1, a2, cmsq[j], f);
-          factor *= f;
-          cm[j] = sqrt(cmsq[j]);
-        }
-      }
-      // Kallen function and kinematic test at the visited branch (phs_cpu.cpp:218-233)
-      double d = dsub(dsub(msq_b, cmsq[0]), cmsq[1]);
-      double lda = dsub(dmul(d, d), dmul(dmul(4.0, cmsq[0]), cmsq[1]));
-      ok = ok && (lda > 0.0) && (m_b > dadd(cm[0], cm[1])) && (m_b <= mmax_b);
-      double sl = sqrt(lda);
-      double pc = sl / (2.0 * m_b);
-      factor *= sl / msq_b;
-
-      // rotation + boost of the visited branch (phs_cpu.cpp:299-330)
-      double bg = m_b > 0.0 ? p_b / m_b : 0.0;
-      double ga = sqrt(1.0 + bg * bg);
-      double sphi, cphi;
-      sincospi(2.0 * xe[V.x_phi], &sphi, &cphi);
-      double b0 = V.b0, b1 = V.b1;
-      if (PER_EVENT && V.ct_class == PHS_CT_COLLINEAR) {
-        b0 = dmul(V.m, V.m) / s;
-        b1 = log(dadd(b0, 1.0) / b0);
-      }
-      double ct, st, fct;
-      map_ct(V.ct_class, xe[V.x_ct], b0, b1, ct, st, fct);
-      factor *= fct;
-      const double e01 = -bg * st, e03 = bg * ct, e11 = ct * cphi, e12 = -sphi, e13 = st * cphi;
-      const double e21 = ct * sphi, e22 = cphi, e23 = st * sphi, e31 = -ga * st, e33 = ga * ct;
-
-      double Ln[16];
-      if (V.self_root && !lab) {
-        // parent frame is the identity: L0 * L1 = L1
-        Ln[0] = ga;  Ln[1] = e01; Ln[2] = 0.0;  Ln[3] = e03;
-        Ln[4] = 0.0; Ln[5] = e11; Ln[6] = e12;  Ln[7] = e13;
-        Ln[8] = 0.0; Ln[9] = e21; Ln[10] = e22; Ln[11] = e23;
-        Ln[12] = bg; Ln[13] = e31; Ln[14] = 0.0; Ln[15] = e33;
-      } else {
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-          const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
-          Ln[4 * r + 0] = l0 * ga + l3 * bg;
-          Ln[4 * r + 3] = l0 * e03 + l1 * e13 + l2 * e23 + l3 * e33;
-          if (!V.both_leaves) {
-            Ln[4 * r + 1] = l0 * e01 + l1 * e11 + l2 * e21 + l3 * e31;
-            Ln[4 * r + 2] = l1 * e12 + l2 * e22;
-          } else {
-            Ln[4 * r + 1] = 0.0;
-            Ln[4 * r + 2] = 0.0;
-          }
-        }
-      }
-
-      // leaf momenta: L_new * (E, 0, 0, +-p) (phs_cpu.cpp:286-291)
-#pragma unroll
-      for (int j = 0; j < 2; j++) {
-        const PhsChild &C = V.child[j];
-        if (!C.internal) {
-          double pj = j == 0 ? pc : -pc;
-          double E = sqrt(cmsq[j] + pj * pj);
-          double2 *o = reinterpret_cast<double2 *>(out + 4 * C.out_index);
-          o[0] = make_double2(Ln[0] * E + Ln[3] * pj, Ln[4] * E + Ln[7] * pj);
-          o[1] = make_double2(Ln[8] * E + Ln[11] * pj, Ln[12] * E + Ln[15] * pj);
-        }
-      }
-
-      // next frame: push one internal child, carry the other (or pop)
-      // (selects instead of indexing keep the child values in registers)
-      if (V.push >= 0) {
-        const bool j0 = V.push == 0;
-#pragma unroll
-        for (int i = 0; i < 16; i++) stack_store(smem, sp, i, Ln[i]);
-        stack_store(smem, sp, 16, j0 ? cmsq[0] : cmsq[1]);
-        stack_store(smem, sp, 17, j0 ? cm[0] : cm[1]);
-        stack_store(smem, sp, 18, j0 ? pc : -pc);
-        stack_store(smem, sp, 19, j0 ? cmax[0] : cmax[1]);
-        sp++;
-      }
-      if (V.carry >= 0) {
-        const bool j0 = V.carry == 0;
-#pragma unroll
-        for (int i = 0; i < 16; i++) L[i] = Ln[i];
-        msq_b = j0 ? cmsq[0] : cmsq[1];
-        m_b = j0 ? cm[0] : cm[1];
-        p_b = j0 ? pc : -pc;
-        mmax_b = j0 ? cmax[0] : cmax[1];
-      } else if (sp > 0) {
-        sp--;
-#pragma unroll
-        for (int i = 0; i < 16; i++) L[i] = stack_load(smem, sp, i);
-        msq_b = stack_load(smem, sp, 16);
-        m_b = stack_load(smem, sp, 17);
-        p_b = stack_load(smem, sp, 18);
-        mmax_b = stack_load(smem, sp, 19);
-      }
-    }
-
-    double volume = ch.volume;
-    if (PER_EVENT) {
-      // phs_cpu.cpp:194-213, bottom-up in post-order with the reference's operation order
-      double vol[PHS_MAX_VISITS];
-      const double c_int = 4 * PHS_TWOPI2, c_root = 4 * PHS_TWOPI5;
-      for (int i = 0; i < ch.n_vol; i++) {
-        int k1 = ch.vol_child[i][0], k2 = ch.vol_child[i][1];
-        double v1 = k1 >= 0 ? vol[k1] : 1.0, v2 = k2 >= 0 ? vol[k2] : 1.0;
-        vol[i] = ch.vol_is_root[i] ? dmul(v1, v2) / c_root
-                                   : dmul(dmul(dmul(v1, v2), sqrts), sqrts) / c_int;
-      }
-      volume = vol[ch.n_vol - 1];
-    }
-    a.volume[ev] = volume;
-    a.factor[ev * a.factor_stride + seg.factor_col] = ok ? factor : 0.0;
-    a.ok[ev] = ok ? 1 : 0;
-    if (!ok) {
-      double2 *o = reinterpret_cast<double2 *>(out);
-      for (int i = 0; i < 2 * ch.n_out; i++) o[i] = make_double2(0.0, 0.0);
-    }
+    phs_event_f64<PER_EVENT>(a, seg, local, smem);
   }
 }
 

@@ -1,0 +1,367 @@
+// phs_kernels_ff.cu -- forward phase-space kernel on the FP32 pipe (float-float pairs).
+//
+// Same walk as the FP64 kernel (visit programs, persistent grid, warp tiles of one
+// channel), with every mapping, angle, boost and momentum in float-float arithmetic
+// (phs_ff.h).  GB300 issues 64x more FP32 than FP64 operations per cycle, and a pair of
+// floats carries ~48 bits, so momenta stay within ~1e-10 of the FP64 path.
+//
+// ok flags stay bit-exact with the reference: the kinematic test at every branch is
+// decided in float-float only when the margins |m - m1 - m2| and |m_max - m| exceed
+// 1e-5 of the mass (and msq is not within 1e-10 s of zero).  Otherwise -- and for channels
+// with STEP mappings, which have no float-float form -- the event is recomputed with the
+// exact FP64 path (phs_event_f64.cuh), which also keeps p_decay near threshold in FP64.
+// The Kallen function is evaluated in factored form, (m-m1-m2)(m+m1+m2)(m-m1+m2)(m+m1-m2),
+// which keeps its relative accuracy close to threshold.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "phs_device.h"
+#include "phs_event_f64.cuh"
+#include "phs_ff.h"
+#include "phs_program.h"
+
+#define PHS_FF_STATE 40   // floats per saved frame: L[16], msq, m, p, m_max as pairs
+#define PHS_FF_MARGIN 1e-5f     // kinematic margins decided in float-float
+#define PHS_FF_MSQ_ZERO 1e-10f  // |msq| below this fraction of s takes the exact path
+
+namespace {
+
+__device__ __forceinline__ ff ld(const PhsFF &c) { return ff_make(c.hi, c.lo); }
+__device__ __forceinline__ ff ffsel(bool c, ff a, ff b) { return c ? a : b; }
+
+// A float-float frame value sits at the same 8-byte slot a double of the FP64 stack
+// (phs_event_f64.cuh) takes: slot (depth * 20 + k) * block + thread.  The two stacks share
+// shared memory, and with identical slots every byte belongs to one thread in both layouts,
+// so a thread on the exact path never touches another thread's float-float frames.
+__device__ __forceinline__ void fstack_store(float *st, int depth, int k, ff v) {
+  reinterpret_cast<float2 *>(st)[(depth * (PHS_FF_STATE / 2) + k) * PHS_FWD_BLOCK + threadIdx.x] =
+      make_float2(v.hi, v.lo);
+}
+__device__ __forceinline__ ff fstack_load(const float *st, int depth, int k) {
+  const float2 t =
+      reinterpret_cast<const float2 *>(st)[(depth * (PHS_FF_STATE / 2) + k) * PHS_FWD_BLOCK + threadIdx.x];
+  return ff_make(t.x, t.y);
+}
+
+__device__ __forceinline__ bool near_zero(ff v, float scale) {
+  return fabsf(v.hi) <= PHS_FF_MARGIN * scale;
+}
+__device__ __forceinline__ bool msq_near_zero(ff v, float s) {
+  return fabsf(v.hi) <= PHS_FF_MSQ_ZERO * s;
+}
+
+// msq from x in float-float; returns false when the event must take the exact path.
+// x arrives as a float-float pair truncated from the double, so x < 0.5 is decided on its
+// high part exactly as the reference decides it on the double.
+__device__ __forceinline__ bool map_msq_ff(const PhsChildFF &C, double xd, const FFTables &T,
+                                           ff &msq, ff &f) {
+  const ff x = ff_from_double_int(xd);
+  switch (C.map_id) {
+    case PHS_MAP_NO:
+      msq = ff_add(ld(C.msq_min), ff_mul(x, ff_sub(ld(C.msq_max), ld(C.msq_min))));
+      f = ld(C.a2);
+      return true;
+    case PHS_MAP_SCHANNEL: {
+      // z = (1-x) a0 + x a1; next to +-pi/2, tan z = -+cot(pi/2 -+ z) with pi/2 -+ z formed
+      // from the host's pi/2 - a1 and pi/2 + a0, so its relative accuracy holds there
+      ff z = ff_add(ld(C.a0), ff_mul(x, ld(C.a1)));   // a1 holds a1 - a0
+      if (!(fabsf(z.hi) < 1.5707962f)) return false;   // the reference's |z| < pi/2 test
+      ff t;
+      if (z.hi > 0.78539816f) {
+        t = ff_cot(ff_add(ld(C.u1), ff_mul(ff_one_minus_double_int(xd), ld(C.a1))), T);
+      } else if (z.hi < -0.78539816f) {
+        t = ff_neg(ff_cot(ff_add(ld(C.u0), ff_mul(x, ld(C.a1))), T));
+      } else {
+        t = ff_tan(z, T);
+      }
+      msq = ff_add(ld(C.m2), ff_mul(ld(C.mw), t));
+      f = ff_mul(ld(C.a2), ff_add_f(ff_sqr(t), 1.0f));
+      return true;
+    }
+    case PHS_MAP_COLLINEAR:
+    case PHS_MAP_INFRARED:
+    case PHS_MAP_RADIATION: {
+      ff msq1 = ff_mul(ld(C.a0), ff_exp(ff_mul(x, ld(C.a1)), T));
+      msq = ff_add(ff_sub(msq1, ld(C.a0)), ld(C.msq_min));
+      f = ff_mul(ld(C.a2), msq1);
+      return true;
+    }
+    case PHS_MAP_TCHANNEL:
+    case PHS_MAP_UCHANNEL: {
+      ff msq1;
+      if (x.hi < 0.5f) {
+        msq1 = ff_mul(ld(C.a0), ff_exp(ff_mul(x, ld(C.a1)), T));
+        msq = ff_add(ff_sub(msq1, ld(C.a0)), ld(C.msq_min));
+      } else {
+        msq1 = ff_mul(ld(C.a0), ff_exp(ff_mul(ff_one_minus_double_int(xd), ld(C.a1)), T));
+        msq = ff_add(ff_sub(ld(C.a0), msq1), ld(C.msq_max));
+      }
+      f = ff_mul(ld(C.a2), msq1);
+      return true;
+    }
+  }
+  return false;
+}
+
+__device__ __forceinline__ ff ldx(const double *xe, int i) { return ff_from_double_int(xe[i]); }
+__device__ __forceinline__ ff ff_twice(ff a) { return ff_make(f_add(a.hi, a.hi), f_add(a.lo, a.lo)); }
+__device__ __forceinline__ ff ff_half(ff a) { return ff_make(f_mul(a.hi, 0.5f), f_mul(a.lo, 0.5f)); }
+
+// One event in float-float.  Returns false if it must be recomputed on the exact path
+// (outputs written so far are then overwritten).
+__device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegment &seg,
+                                             int64_t local, const FFTables &T, float *fst) {
+  const PhsChannelFF &ch = a.channels_ff[seg.channel];
+  if (ch.exact_only) return false;
+  const int64_t ev = seg.ev_begin + local;
+  const double *xe = a.x + seg.x_base + local * seg.x_stride;
+  double *out = a.p + seg.p_base + local * 4 * (int64_t)ch.n_out;
+  const ff zero = ff_from_float(0.0f), one = ff_from_float(1.0f);
+  const float s_scale = ch.s.hi;
+
+  // the frame of the visited branch, updated in place row by row
+  ff L[16];
+#pragma unroll
+  for (int i = 0; i < 16; i++) L[i] = zero;
+  const bool lab = ch.lab != 0;
+  L[0] = lab ? ld(ch.lab_gamma) : one;
+  L[5] = one;
+  L[10] = one;
+  L[15] = L[0];
+  L[3] = lab ? ld(ch.lab_bg) : zero;
+  L[12] = L[3];
+  ff msq_b = ld(ch.s), m_b = ld(ch.sqrts), p_b = zero, mmax_b = ld(ch.sqrts);
+  ff factor = one;
+  bool ok = true;
+  int sp = 0;
+
+  const int n_visits = ch.n_visits;
+  for (int v = 0; v < n_visits; v++) {
+    const PhsVisitFF &V = ch.visit[v];
+    ff cmsq[2], cm[2], cmax[2];
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const PhsChildFF &C = V.child[j];
+      if (!C.internal) {
+        cmsq[j] = ld(C.msq_leaf);
+        cm[j] = ld(C.m_leaf);
+        cmax[j] = zero;
+      } else {
+        ff f;
+        if (!map_msq_ff(C, xe[C.x_msq], T, cmsq[j], f)) return false;
+        factor = ff_mul(factor, f);
+        if (msq_near_zero(cmsq[j], s_scale)) return false;
+        if (cmsq[j].hi < 0.0f) {  // the reference takes sqrt of a negative: not ok
+          ok = false;
+          cmsq[j] = zero;
+        }
+        cm[j] = ff_sqrt_fast(cmsq[j]);
+        cmax[j] = ld(C.m_max);
+      }
+    }
+    // kinematic test at the visited branch, decided here only away from its limits
+    const ff msum = ff_add(cm[0], cm[1]);
+    const ff dlo = ff_sub(m_b, msum);
+    if (near_zero(dlo, m_b.hi)) return false;
+    ok = ok && dlo.hi > 0.0f;
+    if (!V.self_root) {
+      const ff dhi = ff_sub(mmax_b, m_b);
+      if (near_zero(dhi, mmax_b.hi)) return false;
+      ok = ok && dhi.hi > 0.0f;
+    }
+    // Kallen function, factored; one reciprocal of m serves p_decay, the factor and bg
+    const ff mdiff = ff_sub(cm[0], cm[1]);
+    ff lda = ff_mul(ff_mul(dlo, ff_add(m_b, msum)),
+                    ff_mul(ff_sub(m_b, mdiff), ff_add(m_b, mdiff)));
+    if (!(lda.hi > 0.0f)) lda = zero;
+    const ff sl = ff_sqrt_fast(lda);
+    const ff rm = m_b.hi > 0.0f ? ff_recip_fast(m_b) : zero;
+    const ff slrm = ff_mul(sl, rm);
+    const ff pc = ff_half(slrm);                       // sqrt(lambda) / (2 m)
+    factor = ff_mul(factor, ff_mul(slrm, rm));         // sqrt(lambda) / m^2
+
+    // rotation + boost of the visited branch
+    const ff bg = ff_mul(p_b, rm);
+    const ff ga = ff_sqrt_fast(ff_add_f(ff_sqr(bg), 1.0f));
+    ff sphi, cphi;
+    ff_sincos2pi(ldx(xe, V.x_phi), T, sphi, cphi);
+    const double xctd = xe[V.x_ct];
+    const ff xct = ff_from_double_int(xctd);
+    ff ct, st, fct;
+    if (V.ct_class == PHS_CT_COLLINEAR) {
+      const ff b0 = ld(V.b0), b1 = ld(V.b1);
+      ff tmp;
+      if (xct.hi < 0.5f) {
+        tmp = ff_mul(b0, ff_exp(ff_mul(ff_twice(xct), b1), T));
+        ct = ff_add_f(ff_sub(tmp, b0), -1.0f);
+      } else {
+        tmp = ff_mul(b0, ff_exp(ff_mul(ff_twice(ff_one_minus_double_int(xctd)), b1), T));
+        ct = ff_add_f(ff_sub(b0, tmp), 1.0f);
+      }
+      if (ct.hi >= -1.0f && ct.hi <= 1.0f) {
+        // 1 - ct^2 = (1 - ct)(1 + ct), each factor without cancellation
+        st = ff_sqrt_fast(ff_mul(ff_sub(one, ct), ff_add_f(ct, 1.0f)));
+        fct = ff_mul(tmp, b1);
+      } else {
+        ct = one;
+        st = zero;
+        fct = zero;
+      }
+    } else {
+      // tmp = 2(1 - x), ct = 1 - tmp, st = sqrt(tmp (2 - tmp)) = 2 sqrt((1-x) x)
+      const ff u = ff_one_minus_double_int(xctd);
+      ct = ff_sub(xct, u);
+      st = ff_twice(ff_sqrt_fast(ff_mul(u, xct)));
+      fct = one;
+    }
+    factor = ff_mul(factor, fct);
+    const ff e01 = ff_neg(ff_mul(bg, st)), e03 = ff_mul(bg, ct), e11 = ff_mul(ct, cphi);
+    const ff e12 = ff_neg(sphi), e13 = ff_mul(st, cphi), e21 = ff_mul(ct, sphi), e22 = cphi;
+    const ff e23 = ff_mul(st, sphi), e31 = ff_neg(ff_mul(ga, st)), e33 = ff_mul(ga, ct);
+
+    if (V.self_root && !lab) {
+      L[0] = ga;   L[1] = e01;  L[2] = zero;  L[3] = e03;
+      L[4] = zero; L[5] = e11;  L[6] = e12;   L[7] = e13;
+      L[8] = zero; L[9] = e21;  L[10] = e22;  L[11] = e23;
+      L[12] = bg;  L[13] = e31; L[14] = zero; L[15] = e33;
+    } else {
+      // row r of L L1 depends on row r of L only: update in place
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        const ff l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
+        L[4 * r + 0] = ff_dot2(l0, ga, l3, bg);
+        L[4 * r + 3] = ff_dot4(l0, e03, l1, e13, l2, e23, l3, e33);
+        if (!V.both_leaves) {
+          L[4 * r + 1] = ff_dot4(l0, e01, l1, e11, l2, e21, l3, e31);
+          L[4 * r + 2] = ff_dot2(l1, e12, l2, e22);
+        }
+      }
+    }
+
+    // leaf momenta L_new (E, 0, 0, +-p)
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const PhsChildFF &C = V.child[j];
+      if (!C.internal) {
+        const ff pj = j == 0 ? pc : ff_neg(pc);
+        const ff E = ff_sqrt_fast(ff_add(cmsq[j], ff_sqr(pj)));
+        double2 *o = reinterpret_cast<double2 *>(out + 4 * C.out_index);
+        // to double on the (otherwise idle) FP64 pipe: two exact widenings and one add
+        o[0] = make_double2(ff_to_double(ff_dot2(L[0], E, L[3], pj)),
+                            ff_to_double(ff_dot2(L[4], E, L[7], pj)));
+        o[1] = make_double2(ff_to_double(ff_dot2(L[8], E, L[11], pj)),
+                            ff_to_double(ff_dot2(L[12], E, L[15], pj)));
+      }
+    }
+
+    if (V.push >= 0) {
+      const bool j0 = V.push == 0;
+#pragma unroll
+      for (int i = 0; i < 16; i++) fstack_store(fst, sp, i, L[i]);
+      fstack_store(fst, sp, 16, ffsel(j0, cmsq[0], cmsq[1]));
+      fstack_store(fst, sp, 17, ffsel(j0, cm[0], cm[1]));
+      fstack_store(fst, sp, 18, j0 ? pc : ff_neg(pc));
+      fstack_store(fst, sp, 19, ffsel(j0, cmax[0], cmax[1]));
+      sp++;
+    }
+    if (V.carry >= 0) {
+      const bool j0 = V.carry == 0;
+      msq_b = ffsel(j0, cmsq[0], cmsq[1]);
+      m_b = ffsel(j0, cm[0], cm[1]);
+      p_b = j0 ? pc : ff_neg(pc);
+      mmax_b = ffsel(j0, cmax[0], cmax[1]);
+    } else if (sp > 0) {
+      sp--;
+#pragma unroll
+      for (int i = 0; i < 16; i++) L[i] = fstack_load(fst, sp, i);
+      msq_b = fstack_load(fst, sp, 16);
+      m_b = fstack_load(fst, sp, 17);
+      p_b = fstack_load(fst, sp, 18);
+      mmax_b = fstack_load(fst, sp, 19);
+    }
+  }
+
+  a.volume[ev] = ch.volume;
+  a.factor[ev * a.factor_stride + seg.factor_col] = ok ? ff_to_double(factor) : 0.0;
+  a.ok[ev] = ok ? 1 : 0;
+  if (!ok) {
+    double2 *o = reinterpret_cast<double2 *>(out);
+    for (int i = 0; i < 2 * ch.n_out; i++) o[i] = make_double2(0.0, 0.0);
+  }
+  return true;
+}
+
+// MIN_BLOCKS: resident blocks per SM the register allocation targets (the autotuner in
+// phs_api.cpp picks the faster instantiation per process).
+template <int MIN_BLOCKS>
+__global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
+    phs_forward_ff_kernel(const __grid_constant__ PhsLaunch a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  FFTables &T = *reinterpret_cast<FFTables *>(smem_raw);
+  // the float-float frame stack and the FP64 one share memory slot for slot (fstack_store):
+  // a thread uses one at a time, and no slot of one thread overlaps another thread's
+  float *fst = reinterpret_cast<float *>(smem_raw + sizeof(FFTables));
+  double *dst = reinterpret_cast<double *>(smem_raw + sizeof(FFTables));
+
+  // reduction tables, exact at multiples of pi/2
+  if (threadIdx.x < 64) {
+    const int k = threadIdx.x;
+    double sv, cv;
+    sincospi(k / 32.0, &sv, &cv);
+    if (k % 16 == 0) {
+      sv = k == 16 ? 1.0 : (k == 48 ? -1.0 : 0.0);
+      cv = k == 0 ? 1.0 : (k == 32 ? -1.0 : 0.0);
+    }
+    const float sh = (float)sv, chh = (float)cv;
+    T.trig[k] = make_float4(sh, (float)(sv - (double)sh), chh, (float)(cv - (double)chh));
+  } else if (threadIdx.x < 96) {
+    const int j = threadIdx.x - 64;
+    const double v = exp2(j / 32.0);
+    const float h = (float)v;
+    T.exp2[j] = make_float2(h, (float)(v - (double)h));
+  }
+  __syncthreads();
+
+  const int lane = threadIdx.x & 31;
+  const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t tile = warp0; tile < a.n_tiles; tile += n_warps) {
+    const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
+    int lo = 0, hi = a.n_segments - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (segs[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+    }
+    const PhsSegment seg = segs[lo];
+    const int64_t local = (tile - seg.tile_begin) * 32 + lane;
+    if (local >= seg.ev_count) continue;
+    if (!phs_event_ff(a, seg, local, T, fst)) phs_event_f64<false>(a, seg, local, dst);
+  }
+}
+
+}  // namespace
+
+size_t phs_forward_ff_smem_bytes(int stack_depth) {
+  return sizeof(FFTables) + (size_t)stack_depth * PHS_FF_STATE * PHS_FWD_BLOCK * sizeof(float);
+}
+
+int phs_forward_ff_blocks_per_sm(int stack_depth, int variant) {
+  int n = 0;
+  const size_t smem = phs_forward_ff_smem_bytes(stack_depth);
+  if (variant == 1)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phs_forward_ff_kernel<4>, PHS_FWD_BLOCK, smem);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phs_forward_ff_kernel<3>, PHS_FWD_BLOCK, smem);
+  return n > 0 ? n : 1;
+}
+
+cudaError_t phs_launch_forward_ff(const PhsLaunch &a, int n_blocks, int variant, cudaStream_t stream) {
+  if (a.n_tiles <= 0) return cudaSuccess;
+  const size_t smem = phs_forward_ff_smem_bytes(a.stack_depth);
+  if (variant == 1)
+    phs_forward_ff_kernel<4><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+  else
+    phs_forward_ff_kernel<3><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+  return cudaGetLastError();
+}

@@ -96,3 +96,34 @@ struct PhsSegment {
   int32_t x_stride;     // x row length (>= n_x_used)
   int32_t factor_col;   // column added to the factor index (whizard: own channel)
 };
+
+// ------------------------------------------------------------------------------------
+// Float-float form of a channel program, for the FP32-pipe kernel: every constant is a
+// pair of floats hi + lo (about 48 bits).  Built on the host from PhsChannel.
+struct PhsFF {
+  float hi, lo;
+};
+
+struct PhsChildFF {
+  int32_t internal, out_index, map_id, x_msq;
+  PhsFF msq_leaf, m_leaf;
+  PhsFF m2, mw;       // Breit-Wigner: m^2 and m*w
+  PhsFF a0, a1, a2;   // mapping constants; Breit-Wigner keeps a1 - a0 in a1
+  PhsFF msq_min, msq_max, m_max;
+  PhsFF u0, u1;       // Breit-Wigner: pi/2 + a0 and pi/2 - a1 (z near -+pi/2 as cot)
+};
+
+struct PhsVisitFF {
+  PhsChildFF child[2];
+  int32_t x_phi, x_ct, ct_class, carry, push, self_root, both_leaves, pad;
+  PhsFF b0, b1, self_m_max;
+};
+
+struct PhsChannelFF {
+  int32_t n_out, n_visits;
+  int32_t exact_only;  // 1: a mapping without a float-float form (STEP_E/STEP_H): FP64 path
+  int32_t lab;
+  PhsFF sqrts, s, lab_bg, lab_gamma;
+  double volume;
+  PhsVisitFF visit[PHS_MAX_VISITS];
+};

@@ -51,6 +51,12 @@ extern "C" {
 
 #define PHS_MAX_OUT_API 12
 
+/* Arithmetic of the forward kernel (phs_process_set_precision / phs_batch_set_precision). */
+#define PHS_PRECISION_F64 0   /* IEEE FP64 throughout (default) */
+#define PHS_PRECISION_F32X2 1 /* float-float pairs on the FP32 pipe (~48 bits); events within
+                                 1e-5 of a kinematic limit are recomputed in FP64, so ok flags
+                                 stay bit-exact */
+
 typedef struct phs_process *phs_process_t;
 typedef struct phs_batch *phs_batch_t;
 
@@ -77,6 +83,16 @@ int phs_process_destroy(phs_process_t proc);
  * phs_cpu.cpp:452-531) and uploads them.  E1 != E2 adds the longitudinal lab boost
  * (phs.cu:1286-1301). */
 int phs_process_set_beams(phs_process_t proc, double E1, double E2);
+
+/* Arithmetic of the uniform-beam generate calls (phs_generate_device/_host and batches built
+ * afterwards keep their own setting): PHS_PRECISION_F64 or PHS_PRECISION_F32X2.  Per-event
+ * beams always use FP64.  No counterpart in the reference (FP64 only). */
+int phs_process_set_precision(phs_process_t proc, int precision);
+
+/* The FP32-pair kernel's autotuned variant (register budget for 3 or 4 resident blocks per
+ * SM: 0 or 1), or -1 before the first launch of at least 2^18 events has timed them.  The
+ * variants compute identical bits.  Tuning needs that first launch outside stream capture. */
+int phs_process_tuning(phs_process_t proc, int *ff_variant);
 
 /* Sizes: any pointer may be NULL. */
 int phs_process_info(phs_process_t proc, int *n_in, int *n_out, int *n_channels, int *n_x,
@@ -128,6 +144,9 @@ int phs_batch_info(phs_batch_t batch, int *n_channels, int64_t *x_stride_sum, in
 int phs_batch_generate_device(phs_batch_t batch, const int64_t *counts, const double *x,
                               double *p, double *factors, double *volumes, uint8_t *oks,
                               void *stream);
+
+/* Arithmetic of the batch's launches (PHS_PRECISION_F64 or PHS_PRECISION_F32X2). */
+int phs_batch_set_precision(phs_batch_t batch, int precision);
 
 /* Offsets of channel k's first x element and first p element for the given counts
  * (x_offsets/p_offsets [n_channels + 1], host). */
