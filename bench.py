@@ -140,6 +140,121 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def _time_calls(torch, fn, steps: int, warmup: int, stream) -> float:
+    """Mean ms per call from CUDA events on `stream` after `warmup` untimed calls."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def _errors(torch, ref, got, sqrts):
+    """FP32-pair outputs against the FP64 kernel's on the same x (the FP64 kernel equals the
+    CPU oracle to 1e-12; tests/test_gpu_parity.py)."""
+    ok_mism = int((ref.ok != got.ok).sum().item())
+    sel = ref.ok.bool() & got.ok.bool()
+    a, b = ref.p[sel], got.p[sel]
+    d = (b - a).abs().amax(-1)
+    floored = d / a[..., 0].abs().clamp(min=1e-3 * sqrts)
+    unfloored = d / a[..., 0].abs().clamp(min=1e-300)
+    fr = (got.factor[sel] - ref.factor[sel]).abs() / ref.factor[sel].abs()
+    return {"ok_mismatches": ok_mism,
+            "momentum_max_rel": floored.max().item(),
+            "momentum_rms_rel": floored.pow(2).mean().sqrt().item(),
+            "momentum_max_rel_unfloored": unfloored.max().item(),
+            "factor_max_rel": fr.max().item(),
+            "factor_rms_rel": fr.pow(2).mean().sqrt().item(),
+            "definition": "per particle max_mu |dp^mu| / max(E, 1e-3 sqrt(s)); unfloored: / E"}
+
+
+def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64):
+    """FP32-pair arithmetic on the tt workload, the 13 TeV configuration and the batched
+    64-channel workload (CUDA-graph replay), each beside FP64 on the same x."""
+    import ctypes as C
+    from gpu_phs_gb300 import _lib
+    from gpu_phs_gb300 import processes as P
+    from gpu_phs_gb300.api import (PRECISION_F32X2, Batch, PhaseSpace, batch_graph, philox_fill)
+    stream = torch.cuda.current_stream()
+    steps = max(3, min(steps, 20))
+    res = {}
+
+    proc = P.tt()
+    n = x_tt.shape[0]
+    ps = PhaseSpace(proc, proc.sqrts / 2, proc.sqrts / 2)
+    ps.set_precision(PRECISION_F32X2)
+    o = ps.alloc(n)
+    ms = _time_calls(torch, lambda: ps.generate(x_tt, out=o), steps, warmup, stream)
+    v = C.c_int()
+    _lib.load().phs_process_tuning(ps.h, C.byref(v))
+    res["fp32_mixed_tt"] = {"value": n / ms * 1e3, "unit": "events/s", "ms_per_step": ms,
+                            "speedup_vs_fp64": ms_tt64 / ms, "n_events": n,
+                            "autotuned_variant": v.value,
+                            "error_vs_fp64": _errors(torch, out_tt, o, proc.sqrts)}
+    del o
+
+    proc = P.precision()
+    n = 1 << 24
+    x = torch.empty((n, proc.n_x), dtype=torch.float64, device="cuda")
+    philox_fill(x, n, proc.n_x, SEED)
+    outs, t = {}, {}
+    for prec in (0, 1):
+        ps = PhaseSpace(proc, proc.sqrts / 2, proc.sqrts / 2)
+        ps.set_precision(prec)
+        outs[prec] = ps.alloc(n)
+        t[prec] = _time_calls(torch, lambda: ps.generate(x, out=outs[prec]), steps, warmup, stream)
+    res["precision_13TeV"] = {"workload": proc.name, "n_events": n, "n_x": proc.n_x,
+                              "fp64_events_per_s": n / t[0] * 1e3,
+                              "fp32_mixed_events_per_s": n / t[1] * 1e3,
+                              "speedup": t[0] / t[1],
+                              "ok_fraction": outs[0].ok.double().mean().item(),
+                              "error_vs_fp64": _errors(torch, outs[0], outs[1], proc.sqrts)}
+    del outs, x
+
+    procs, counts = P.batched(seed=2024, n_channels=64, total_events=1 << 24)
+    spaces = [PhaseSpace(p, 500.0, 500.0) for p in procs]
+    n = int(counts.sum())
+    bres, bufs = {}, {}
+    for prec in (0, 1):
+        batch = Batch(spaces)
+        batch.set_precision(prec)
+        xo, po = batch.offsets(counts)
+        if prec == 0:
+            xb = torch.empty(int(xo[-1]), dtype=torch.float64, device="cuda")
+            philox_fill(xb, int(xo[-1]), 1, SEED)
+        bufs[prec] = (torch.empty(int(po[-1]), dtype=torch.float64, device="cuda"),
+                      torch.empty(n, dtype=torch.float64, device="cuda"),
+                      torch.empty(n, dtype=torch.float64, device="cuda"),
+                      torch.empty(n, dtype=torch.uint8, device="cuda"))
+        g = batch_graph(batch, xb, counts, *bufs[prec])
+        bres[prec] = _time_calls(torch, lambda: g.launch(), steps, warmup, stream)
+        del g
+    # ok flags of the FP64 batch against per-channel plain runs
+    per_channel_mism = 0
+    e = 0
+    for i, (sp, c) in enumerate(zip(spaces, counts)):
+        c = int(c)
+        ev = sp.generate(xb[xo[i]:xo[i + 1]].view(c, sp.proc.n_x))
+        per_channel_mism += int((ev.ok != bufs[0][3][e:e + c]).sum().item())
+        e += c
+    res["batched_64ch"] = {"n_channels": 64, "n_events": n, "n_out_range": [3, 8],
+                           "counts": "power law, exponent 1.5, seed 2024",
+                           "launch": "one persistent kernel per step, replayed from a CUDA graph",
+                           "fp64_events_per_s": n / bres[0] * 1e3,
+                           "fp32_mixed_events_per_s": n / bres[1] * 1e3,
+                           "speedup": bres[0] / bres[1],
+                           "ok_fraction": bufs[0][3].double().mean().item(),
+                           "ok_mismatches_fp32_mixed_vs_fp64": int((bufs[0][3] != bufs[1][3]).sum().item()),
+                           "ok_mismatches_vs_per_channel_runs": per_channel_mism}
+    return res
+
+
 def cpu_reference_rate(proc, sqrts, seconds: float, max_events: int, prefer_ref: bool = True):
     """Events/s of the reference CPU path (oracle/_ref if it loads here, else the C
     restatement) on all host threads, on the first events of the same Philox stream."""
@@ -330,6 +445,11 @@ def run_ours(args):
                "path": "phs_generate_host (C ABI), pinned host buffers, 1 Mi-event chunks on 2 streams",
                "steps": e2e_steps}
 
+    variants = None
+    if not args.no_variants and world == 1:
+        variants = measure_variants(torch, args.steps, args.warmup, x, out, ms_per_step)
+        variants["fp32_mixed_over_fp64_batched"] = variants["batched_64ch"]["speedup"]
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         rate, kind, threads, sample_n, _, _ = cpu_reference_rate(proc, proc.sqrts, args.cpu_seconds,
@@ -358,6 +478,7 @@ def run_ours(args):
                                   "peak_kind": "measured (phs_measure_fma_peak, DFMA chains)"}},
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "variants": variants,
             "gpu_launches": args.steps,
             "clocks": clocks,
         }
@@ -376,6 +497,7 @@ def main():
     ap.add_argument("--events", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -38,6 +38,10 @@ _SIGS = {
     "phs_batch_generate_device": (I, [P, P, P, P, P, P, P, P]),
     "phs_batch_offsets": (I, [P, P, P, P]),
     "phs_philox_fill": (I, [P, I64, I, C.c_uint64, I64, P]),
+    "phs_batch_graph_create": (I, [C.POINTER(P), P, P, P, P, P, P, P]),
+    "phs_process_graph_create": (I, [C.POINTER(P), P, I64, P, P, P, P, P, P]),
+    "phs_graph_launch": (I, [P, P]),
+    "phs_graph_destroy": (I, [P]),
     "phs_whizard_momentum_device_pointer": (P, []),
     "phs_measure_fma_peak": (I, [I, P]),
     "c_whizard_set_particle_structure": (None, [P] * 6),

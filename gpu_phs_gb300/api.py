@@ -196,6 +196,48 @@ class Batch:
         return p, factor, volume, ok
 
 
+class Graph:
+    """A captured generate call (fixed pointers and counts); launch() replays it."""
+
+    def __init__(self, handle):
+        self.h = handle
+
+    def launch(self, stream=None) -> None:
+        check(load().phs_graph_launch(self.h, _stream(stream)))
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            load().phs_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_graph(batch: "Batch", x, counts, p, factor, volume, ok) -> Graph:
+    c = np.ascontiguousarray(counts, np.int64)
+    h = C.c_void_p()
+    check(load().phs_batch_graph_create(C.byref(h), batch.h, _ptr(c), _ptr(x), _ptr(p),
+                                        _ptr(factor), _ptr(volume), _ptr(ok)))
+    g = Graph(h)
+    g._keep = (batch, x, c, p, factor, volume, ok)
+    return g
+
+
+def process_graph(ps: PhaseSpace, x, out: Events, counts=None) -> Graph:
+    n = int(x.shape[0])
+    c = ps._counts(counts, ps.proc.n_channels, n)
+    h = C.c_void_p()
+    check(load().phs_process_graph_create(C.byref(h), ps.h, n, _ptr(c), _ptr(x), _ptr(out.p),
+                                          _ptr(out.factor), _ptr(out.volume), _ptr(out.ok)))
+    g = Graph(h)
+    g._keep = (ps, x, c, out)
+    return g
+
+
 def philox_fill(x, n_events: int, n_x: int, seed: int, first_event: int = 0, stream=None):
     """Fills CUDA float64 x[n_events * n_x] with the Philox stream (gpu_phs_gb300/philox.py)."""
     check(load().phs_philox_fill(_ptr(x), n_events, n_x, seed, first_event, _stream(stream)))

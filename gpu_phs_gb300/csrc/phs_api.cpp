@@ -711,6 +711,91 @@ extern "C" int phs_generate_device_noalloc(phs_process_t h, double E1, double E2
   return PHS_OK;
 }
 
+// ----------------------------------------------------------------------- CUDA graphs
+// A graph holds one generate call with fixed pointers and counts.  Creation runs the call
+// once on a private stream (segment table upload, FP32-pair autotuning: everything that
+// may synchronize), then captures it; launching replays the kernel with no host work.
+struct phs_graph {
+  int device = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+template <class Call>
+static int capture_graph(phs_graph_t *out, int device, Call call) {
+  if (!out) return fail(PHS_ERR_INVALID_ARG, "null output handle pointer");
+  *out = nullptr;
+  DeviceGuard g(device);
+  cudaStream_t st;
+  CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  int rc = call(st);
+  if (rc == PHS_OK) {
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = fail(PHS_ERR_CUDA, "warm-up run: %s", cudaGetErrorString(e));
+  }
+  phs_graph *G = nullptr;
+  if (rc == PHS_OK) {
+    G = new phs_graph;
+    G->device = device;
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      rc = call(st);
+      cudaError_t e2 = cudaStreamEndCapture(st, &G->graph);
+      if (rc == PHS_OK && e2 != cudaSuccess)
+        rc = fail(PHS_ERR_CUDA, "stream capture: %s", cudaGetErrorString(e2));
+    } else {
+      rc = fail(PHS_ERR_CUDA, "cudaStreamBeginCapture: %s", cudaGetErrorString(e));
+    }
+    if (rc == PHS_OK) {
+      e = cudaGraphInstantiate(&G->exec, G->graph, 0);
+      if (e != cudaSuccess) rc = fail(PHS_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+    }
+    if (rc != PHS_OK) {
+      if (G->exec) cudaGraphExecDestroy(G->exec);
+      if (G->graph) cudaGraphDestroy(G->graph);
+      delete G;
+      G = nullptr;
+    }
+  }
+  cudaStreamDestroy(st);
+  *out = G;
+  return rc;
+}
+
+extern "C" int phs_batch_graph_create(phs_graph_t *out, phs_batch_t b, const int64_t *counts,
+                                      const double *x, double *p, double *f, double *v,
+                                      uint8_t *ok) {
+  if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
+  return capture_graph(out, b->device, [&](cudaStream_t st) {
+    return phs_batch_generate_device(b, counts, x, p, f, v, ok, st);
+  });
+}
+
+extern "C" int phs_process_graph_create(phs_graph_t *out, phs_process_t h, int64_t n_events,
+                                        const int64_t *counts, const double *x, double *p,
+                                        double *f, double *v, uint8_t *ok) {
+  if (int rc = check_proc(h)) return rc;
+  return capture_graph(out, h->device, [&](cudaStream_t st) {
+    return phs_generate_device(h, n_events, counts, x, p, f, v, ok, st);
+  });
+}
+
+extern "C" int phs_graph_launch(phs_graph_t G, void *stream) {
+  if (!G) return fail(PHS_ERR_INVALID_ARG, "null graph handle");
+  DeviceGuard g(G->device);
+  CUDA_TRY(cudaGraphLaunch(G->exec, (cudaStream_t)stream));
+  return PHS_OK;
+}
+
+extern "C" int phs_graph_destroy(phs_graph_t G) {
+  if (!G) return PHS_OK;
+  DeviceGuard g(G->device);
+  if (G->exec) cudaGraphExecDestroy(G->exec);
+  if (G->graph) cudaGraphDestroy(G->graph);
+  delete G;
+  return PHS_OK;
+}
+
 // ---------------------------------------------------------------------- random numbers
 extern "C" int phs_philox_fill(double *x, int64_t n_events, int n_x, uint64_t seed,
                                int64_t first_event, void *stream) {

@@ -153,6 +153,23 @@ int phs_batch_set_precision(phs_batch_t batch, int precision);
 int phs_batch_offsets(phs_batch_t batch, const int64_t *counts, int64_t *x_offsets,
                       int64_t *p_offsets);
 
+/* ----------------------------------------------------------------------- CUDA graphs */
+
+typedef struct phs_graph *phs_graph_t;
+
+/* One generate call with fixed pointers and counts as a CUDA graph.  Creation runs the call
+ * once (uploads, FP32-pair autotuning), then captures it on a private stream; launching
+ * replays the single persistent kernel with no host work.  The reference launches
+ * 3 + 2(n_out - 1) kernels with a device synchronization after each (phs.cu:1427-1560). */
+int phs_batch_graph_create(phs_graph_t *out, phs_batch_t batch, const int64_t *counts,
+                           const double *x, double *p, double *factors, double *volumes,
+                           uint8_t *oks);
+int phs_process_graph_create(phs_graph_t *out, phs_process_t proc, int64_t n_events,
+                             const int64_t *channel_counts, const double *x, double *p,
+                             double *factors, double *volumes, uint8_t *oks);
+int phs_graph_launch(phs_graph_t graph, void *stream);
+int phs_graph_destroy(phs_graph_t graph);
+
 /* ---------------------------------------------------------------------- random numbers */
 
 /* Philox4x32-10 uniform doubles in [0,1) for events [first_event, first_event + n_events) of

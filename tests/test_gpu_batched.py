@@ -1,0 +1,71 @@
+"""The batched workload: 64 channel trees with 3-8 outgoing particles and power-law event
+counts in one persistent launch, replayed from a CUDA graph.  ok flags must equal those of
+per-channel plain runs bit for bit, in FP64 and in FP32-pair arithmetic."""
+import numpy as np
+import pytest
+
+from gpu_phs_gb300 import processes as P
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def test_batched_graph_matches_direct_and_per_channel(torch):
+    from gpu_phs_gb300.api import Batch, PhaseSpace, batch_graph, philox_fill
+    procs, counts = P.batched(seed=2024, n_channels=64, total_events=1 << 20)
+    spaces = [PhaseSpace(p, 500.0, 500.0) for p in procs]
+    results = {}
+    for prec in (0, 1):
+        batch = Batch(spaces)
+        batch.set_precision(prec)
+        xo, po = batch.offsets(counts)
+        x = torch.empty(int(xo[-1]), dtype=torch.float64, device="cuda")
+        philox_fill(x, int(xo[-1]), 1, seed=5)
+        n = int(counts.sum())
+        direct = batch.generate(x, counts)
+        bufs = (torch.empty(int(po[-1]), dtype=torch.float64, device="cuda"),
+                torch.empty(n, dtype=torch.float64, device="cuda"),
+                torch.empty(n, dtype=torch.float64, device="cuda"),
+                torch.empty(n, dtype=torch.uint8, device="cuda"))
+        g = batch_graph(batch, x, counts, *bufs)
+        for t in bufs:
+            t.zero_()
+        g.launch()
+        g.launch()
+        torch.cuda.synchronize()
+        for a, b in zip(direct, bufs):
+            assert torch.equal(a, b)
+        results[prec] = (x, xo, po, direct)
+    # FP32 pairs decide ok exactly as FP64 does
+    assert torch.equal(results[0][3][3], results[1][3][3])
+    # ... and FP64 batched equals per-channel plain runs
+    x, xo, po, (p, f, v, ok) = results[0]
+    e = 0
+    for i, (ps, c) in enumerate(zip(spaces, counts)):
+        c = int(c)
+        ev = ps.generate(x[xo[i]:xo[i + 1]].view(c, ps.proc.n_x))
+        assert torch.equal(ev.ok, ok[e:e + c])
+        assert torch.equal(ev.p.reshape(-1), p[po[i]:po[i + 1]])
+        e += c
+    assert 0.01 < ok.double().mean().item() < 1.0
+
+
+def test_process_graph_replay(torch):
+    from gpu_phs_gb300.api import PhaseSpace, philox_x, process_graph
+    proc = P.tt()
+    ps = PhaseSpace(proc, 500.0, 500.0)
+    x = philox_x(300_000, proc.n_x, seed=8)
+    ref = ps.generate(x)
+    out = ps.alloc(300_000)
+    g = process_graph(ps, x, out)
+    out.p.zero_()
+    g.launch()
+    torch.cuda.synchronize()
+    assert torch.equal(out.p, ref.p) and torch.equal(out.ok, ref.ok)
