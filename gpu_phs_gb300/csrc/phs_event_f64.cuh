@@ -16,7 +16,7 @@
 #define PHS_PI 3.14159265358979323846
 #define PHS_TWOPI2 39.47841760435743447534
 #define PHS_TWOPI5 9792.62991312900650440772
-#define PHS_STATE 20  // doubles per saved frame: L[16], msq, m, p, m_max
+#define PHS_STATE 21  // doubles per saved frame: L[16], msq, m, p, m_max, E
 
 namespace {
 
@@ -213,7 +213,7 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
   L[15] = L[0];
   L[3] = lab ? lab_bg : 0.0;
   L[12] = L[3];
-  double msq_b = s, m_b = sqrts, p_b = 0.0, mmax_b = sqrts;
+  double msq_b = s, m_b = sqrts, p_b = 0.0, mmax_b = sqrts, E_b = sqrts;
   double factor = 1.0;
   bool ok = true;
   int sp = 0;
@@ -243,13 +243,20 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
     double d = dsub(dsub(msq_b, cmsq[0]), cmsq[1]);
     double lda = dsub(dmul(d, d), dmul(dmul(4.0, cmsq[0]), cmsq[1]));
     ok = ok && (lda > 0.0) && (m_b > dadd(cm[0], cm[1])) && (m_b <= mmax_b);
-    double sl = sqrt(lda);
-    double pc = sl / (2.0 * m_b);
-    factor *= sl / msq_b;
+    // one reciprocal of m serves p_decay = sqrt(lda)/(2m), sqrt(lda)/m^2, bg, gamma and the
+    // daughters' energies E = (m^2 + m_j^2 - m_k^2)/(2m) (the two-body energy, equal to the
+    // reference's sqrt(m_j^2 + p^2))
+    const double sl = sqrt(lda);
+    const double rm = m_b > 0.0 ? __drcp_rn(m_b) : 0.0;
+    const double hm = 0.5 * rm;
+    const double pc = sl * hm;
+    factor *= (sl * rm) * rm;
+    const double ce0 = (msq_b + cmsq[0] - cmsq[1]) * hm;
+    const double ce1 = (msq_b + cmsq[1] - cmsq[0]) * hm;
 
     // rotation + boost of the visited branch (phs_cpu.cpp:299-330)
-    double bg = m_b > 0.0 ? p_b / m_b : 0.0;
-    double ga = sqrt(1.0 + bg * bg);
+    const double bg = p_b * rm;
+    const double ga = V.self_root ? 1.0 : E_b * rm;
     double sphi, cphi;
     sincospi(2.0 * xe[V.x_phi], &sphi, &cphi);
     double b0 = V.b0, b1 = V.b1;
@@ -292,7 +299,7 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
       const PhsChild &C = V.child[j];
       if (!C.internal) {
         double pj = j == 0 ? pc : -pc;
-        double E = sqrt(cmsq[j] + pj * pj);
+        const double E = j == 0 ? ce0 : ce1;
         double2 *o = reinterpret_cast<double2 *>(out + 4 * C.out_index);
         o[0] = make_double2(Ln[0] * E + Ln[3] * pj, Ln[4] * E + Ln[7] * pj);
         o[1] = make_double2(Ln[8] * E + Ln[11] * pj, Ln[12] * E + Ln[15] * pj);
@@ -309,6 +316,7 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
       stack_store(smem, sp, 17, j0 ? cm[0] : cm[1]);
       stack_store(smem, sp, 18, j0 ? pc : -pc);
       stack_store(smem, sp, 19, j0 ? cmax[0] : cmax[1]);
+      stack_store(smem, sp, 20, j0 ? ce0 : ce1);
       sp++;
     }
     if (V.carry >= 0) {
@@ -319,6 +327,7 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
       m_b = j0 ? cm[0] : cm[1];
       p_b = j0 ? pc : -pc;
       mmax_b = j0 ? cmax[0] : cmax[1];
+      E_b = j0 ? ce0 : ce1;
     } else if (sp > 0) {
       sp--;
 #pragma unroll
@@ -327,6 +336,7 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
       m_b = stack_load(smem, sp, 17);
       p_b = stack_load(smem, sp, 18);
       mmax_b = stack_load(smem, sp, 19);
+      E_b = stack_load(smem, sp, 20);
     }
   }
 

@@ -30,10 +30,10 @@ namespace {
 __device__ __forceinline__ ff ld(const PhsFF &c) { return ff_make(c.hi, c.lo); }
 __device__ __forceinline__ ff ffsel(bool c, ff a, ff b) { return c ? a : b; }
 
-// A float-float frame value sits at the same 8-byte slot a double of the FP64 stack
-// (phs_event_f64.cuh) takes: slot (depth * 20 + k) * block + thread.  The two stacks share
-// shared memory, and with identical slots every byte belongs to one thread in both layouts,
-// so a thread on the exact path never touches another thread's float-float frames.
+// A float-float frame value takes one 8-byte slot, (depth * 20 + k) * block + thread, as a
+// double of the FP64 stack (phs_event_f64.cuh) does at (depth * 21 + k) * block + thread.
+// The two stacks share shared memory; in both layouts every slot of thread t has an index
+// = t (mod block), so a thread on the exact path never touches another thread's frames.
 __device__ __forceinline__ void fstack_store(float *st, int depth, int k, ff v) {
   reinterpret_cast<float2 *>(st)[(depth * (PHS_FF_STATE / 2) + k) * PHS_FWD_BLOCK + threadIdx.x] =
       make_float2(v.hi, v.lo);
@@ -299,8 +299,8 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
     phs_forward_ff_kernel(const __grid_constant__ PhsLaunch a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FFTables &T = *reinterpret_cast<FFTables *>(smem_raw);
-  // the float-float frame stack and the FP64 one share memory slot for slot (fstack_store):
-  // a thread uses one at a time, and no slot of one thread overlaps another thread's
+  // the float-float frame stack and the FP64 one share memory (fstack_store): a thread
+  // uses one at a time, and no slot of one thread overlaps another thread's
   float *fst = reinterpret_cast<float *>(smem_raw + sizeof(FFTables));
   double *dst = reinterpret_cast<double *>(smem_raw + sizeof(FFTables));
 
@@ -342,8 +342,11 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
 
 }  // namespace
 
+// The frame region holds either stack: PHS_STATE 8-byte slots per frame and thread (the
+// FP64 frames are the larger ones).
+static_assert(PHS_STATE * 2 >= PHS_FF_STATE, "FP64 frame must be at least the float-float frame");
 size_t phs_forward_ff_smem_bytes(int stack_depth) {
-  return sizeof(FFTables) + (size_t)stack_depth * PHS_FF_STATE * PHS_FWD_BLOCK * sizeof(float);
+  return sizeof(FFTables) + (size_t)stack_depth * PHS_STATE * PHS_FWD_BLOCK * sizeof(double);
 }
 
 int phs_forward_ff_blocks_per_sm(int stack_depth, int variant) {
