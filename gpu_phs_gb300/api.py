@@ -126,6 +126,21 @@ class PhaseSpace:
                                                _ptr(out.ok), _stream(stream)))
         return out
 
+    def vjp(self, x, pbar, jbar=None, counts=None, stream=None):
+        """Reverse-mode derivatives (FP64): for cotangents pbar [n, n_out, 4] of the momenta
+        and jbar [n] of log(factor), returns xbar [n, n_x] and thbar [n, n_out - 2, 2]
+        (d/dm, d/dGamma of the Breit-Wigner branch at each msq x index)."""
+        import torch
+        n = int(x.shape[0])
+        xbar = torch.empty_like(x)
+        thbar = torch.empty((n, max(1, self.proc.n_out - 2), 2), dtype=torch.float64, device=x.device)
+        c = self._counts(counts, self.proc.n_channels, n)
+        pbar = pbar.contiguous()
+        jbar = jbar.contiguous() if jbar is not None else None
+        check(load().phs_adjoint_device(self.h, n, _ptr(c), _ptr(x), _ptr(pbar), _ptr(jbar),
+                                        _ptr(xbar), _ptr(thbar), _stream(stream)))
+        return xbar, thbar
+
     def generate_host(self, x, counts=None, out: Optional[Events] = None) -> Events:
         """Host (ideally pinned) tensors or arrays in and out; synchronous."""
         import torch

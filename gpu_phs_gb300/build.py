@@ -23,7 +23,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["phs_kernels.cu", "phs_kernels_ff.cu"]
+CU_SOURCES = ["phs_kernels.cu", "phs_kernels_ff.cu", "phs_adjoint.cu"]
 CPP_SOURCES = ["phs_compile.cpp", "phs_api.cpp"]
 
 

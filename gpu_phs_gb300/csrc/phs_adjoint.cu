@@ -1,0 +1,491 @@
+// phs_adjoint.cu -- reverse-mode derivatives of the forward map (FP64).
+//
+// For cotangents pbar (of the momenta) and jbar (of the log-Jacobian log(factor)), one
+// thread per event computes
+//     xbar[k]      = sum pbar . dp/dx_k + jbar dlogJ/dx_k                 (every x)
+//     thbar[b][0/1] = the same for d/dm and d/dGamma of Breit-Wigner branch b
+// (b = the branch's msq x index).  Two passes per event:
+//   1. the forward walk of phs_event_f64.cuh recomputed, keeping only the state each visit
+//      starts from (msq, m, p, E of the visited branch) and the frame current before each
+//      pop -- no per-branch matrices;
+//   2. the visits in reverse.  The frame of a visit's parent is recovered from the visit's
+//      own frame with the inverse rotation+boost, L_pre = L_post eta L1^T eta, so the boost
+//      chain is recomputed backwards.  Adjoints of frames and states travel up the tree
+//      with a stack that mirrors the forward one.
+// Uniform beams only.  Events with ok = 0 get zero derivatives.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "phs_device.h"
+#include "phs_event_f64.cuh"
+#include "phs_program.h"
+
+#define PHS_ADJ_BLOCK 64
+#define PHS_ADJ_STATE 4    // per visit: msq, m, p, E of the visited branch
+#define PHS_ADJ_ANG 7      // per visit: cos phi, sin phi, ct, st, dct/dx, dst/dx, dlog fct/dx
+#define PHS_ADJ_DER 6      // per visited branch: dmsq/dx, dlog f/dx, dmsq/dm, dmsq/dw, dlogf/dm, dlogf/dw
+#define PHS_ADJ_FRAME 20   // adjoint stack entry: Lbar[16], msqbar, mbar, pbar, Ebar
+
+namespace {
+
+struct AdjLayout {
+  int state0, ang0, der0, pop0, stack0;  // offsets (in slots) of the per-thread regions
+};
+
+__device__ __forceinline__ double &slot(double *sm, int i) {
+  return sm[i * PHS_ADJ_BLOCK + threadIdx.x];
+}
+
+// msq mapping derivatives at x: dmsq/dx, dlog f/dx, and for Breit-Wigner branches the
+// derivatives in the mass and the width (through the atan bounds a0, a1 as well).
+__device__ void map_derivs(const PhsChild &C, const PhsAdjChild &A, double x, double &dmsq_dx,
+                           double &dlf_dx, double &dmsq_dm, double &dmsq_dw, double &dlf_dm,
+                           double &dlf_dw) {
+  dmsq_dm = dmsq_dw = dlf_dm = dlf_dw = 0.0;
+  switch (C.map_id) {
+    case PHS_MAP_NO:
+      dmsq_dx = C.msq_max - C.msq_min;
+      dlf_dx = 0.0;
+      break;
+    case PHS_MAP_SCHANNEL: {
+      const double da = C.a1 - C.a0;
+      const double z = (1.0 - x) * C.a0 + x * C.a1;
+      const double t = tan(z), u = 1.0 + t * t, mw = C.m * C.w;
+      dmsq_dx = mw * u * da;
+      dlf_dx = 2.0 * t * da;
+      const double dz_dm = (1.0 - x) * A.da0_dm + x * A.da1_dm;
+      const double dz_dw = (1.0 - x) * A.da0_dw + x * A.da1_dw;
+      dmsq_dm = 2.0 * C.m + C.w * t + mw * u * dz_dm;
+      dmsq_dw = C.m * t + mw * u * dz_dw;
+      dlf_dm = (A.da1_dm - A.da0_dm) / da + 1.0 / C.m + 2.0 * t * dz_dm;
+      dlf_dw = (A.da1_dw - A.da0_dw) / da + 1.0 / C.w + 2.0 * t * dz_dw;
+      break;
+    }
+    case PHS_MAP_COLLINEAR:
+    case PHS_MAP_INFRARED:
+    case PHS_MAP_RADIATION:
+      dmsq_dx = C.a1 * C.a0 * exp(x * C.a1);
+      dlf_dx = C.a1;
+      break;
+    case PHS_MAP_TCHANNEL:
+    case PHS_MAP_UCHANNEL:
+      if (x < 0.5) {
+        dmsq_dx = C.a1 * C.a0 * exp(x * C.a1);
+        dlf_dx = C.a1;
+      } else {
+        dmsq_dx = C.a1 * C.a0 * exp((1.0 - x) * C.a1);
+        dlf_dx = -C.a1;
+      }
+      break;
+    case PHS_MAP_STEP_H: {
+      const double q = C.a0 - x, g = C.a1 / (q * q) + C.a2;
+      dmsq_dx = (C.msq_max - C.msq_min) * g;
+      dlf_dx = 2.0 * C.a1 / (q * q * q) / g;
+      break;
+    }
+    case PHS_MAP_STEP_E: {
+      const double tmp = exp(-x * C.a0 / C.a2) * (1.0 + C.a1);
+      dmsq_dx = C.a0 * tmp / (tmp - C.a1) * (C.msq_max - C.msq_min);
+      dlf_dx = C.a0 * C.a1 / (C.a2 * (tmp - C.a1));
+      break;
+    }
+    default:
+      dmsq_dx = dlf_dx = 0.0;
+  }
+}
+
+// cos(theta) mapping with derivatives in x.
+__device__ __forceinline__ void ct_derivs(int ct_class, double x, double b0, double b1, double ct,
+                                          double st, double &dct, double &dst, double &dlf) {
+  if (ct_class == PHS_CT_COLLINEAR) {
+    const double tmp = x < 0.5 ? b0 * exp(2.0 * x * b1) : b0 * exp(2.0 * (1.0 - x) * b1);
+    if (st > 0.0) {
+      dct = 2.0 * b1 * tmp;
+      dst = -ct / st * dct;
+      dlf = x < 0.5 ? 2.0 * b1 : -2.0 * b1;
+    } else {
+      dct = dst = dlf = 0.0;  // outside the mapped range: constant
+    }
+  } else {
+    dct = 2.0;
+    dst = st > 0.0 ? -2.0 * ct / st : 0.0;
+    dlf = 0.0;
+  }
+}
+
+__global__ void __launch_bounds__(PHS_ADJ_BLOCK)
+    phs_adjoint_kernel(const __grid_constant__ PhsLaunch a, const PhsAdjChannel *__restrict__ adj,
+                       const double *__restrict__ pbar, const double *__restrict__ jbar,
+                       double *__restrict__ xbar, double *__restrict__ thbar, int th_stride,
+                       AdjLayout lay) {
+  extern __shared__ double sm[];
+  const int lane = threadIdx.x & 31;
+  const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+
+  for (int64_t tile = warp0; tile < a.n_tiles; tile += n_warps) {
+    const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
+    int lo = 0, hi = a.n_segments - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (segs[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+    }
+    const PhsSegment seg = segs[lo];
+    const int64_t local = (tile - seg.tile_begin) * 32 + lane;
+    if (local >= seg.ev_count) continue;
+    const PhsChannel &ch = a.channels[seg.channel];
+    const PhsAdjChannel &ad = adj[seg.channel];
+    const int64_t ev = seg.ev_begin + local;
+    const double *xe = a.x + seg.x_base + local * seg.x_stride;
+    double *xb = xbar + seg.x_base + local * seg.x_stride;
+    double *tb = thbar + ev * th_stride;
+    const double *pb = pbar + seg.p_base + local * 4 * (int64_t)ch.n_out;
+    const double jb = jbar ? jbar[ev] : 0.0;
+    for (int k = 0; k < seg.x_stride; k++) xb[k] = 0.0;
+    for (int k = 0; k < th_stride; k++) tb[k] = 0.0;
+
+    const double sqrts = ch.sqrts, s = dmul(sqrts, sqrts);
+    const bool lab = ch.lab != 0;
+    const int n_visits = ch.n_visits;
+
+    // ---------------------------------------------------------------- 1. forward walk
+    double L[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) L[i] = 0.0;
+    L[0] = lab ? ch.lab_gamma : 1.0;
+    L[5] = 1.0;
+    L[10] = 1.0;
+    L[15] = L[0];
+    L[3] = lab ? ch.lab_bg : 0.0;
+    L[12] = L[3];
+    double msq_b = s, m_b = sqrts, p_b = 0.0, mmax_b = sqrts, E_b = sqrts;
+    bool ok = true;
+    int sp = 0, np = 0;
+    for (int v = 0; v < n_visits; v++) {
+      const PhsVisit &V = ch.visit[v];
+      slot(sm, lay.state0 + 4 * v + 0) = msq_b;
+      slot(sm, lay.state0 + 4 * v + 1) = m_b;
+      slot(sm, lay.state0 + 4 * v + 2) = p_b;
+      slot(sm, lay.state0 + 4 * v + 3) = E_b;
+      double cmsq[2], cm[2], cmax[2];
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        const PhsChild &C = V.child[j];
+        if (!C.internal) {
+          cmsq[j] = C.msq_leaf;
+          cm[j] = C.m_leaf;
+          cmax[j] = 0.0;
+        } else {
+          double f;
+          const double xm = xe[C.x_msq];
+          map_msq(C.map_id, xm, s, C.m, C.w, C.msq_min, C.msq_max, C.a0, C.a1, C.a2, cmsq[j], f);
+          cm[j] = sqrt(cmsq[j]);
+          cmax[j] = C.m_max;
+          double dd[6];
+          map_derivs(C, ad.visit[v].child[j], xm, dd[0], dd[1], dd[2], dd[3], dd[4], dd[5]);
+          const int cv = ad.visit[v].child_visit[j];
+#pragma unroll
+          for (int k = 0; k < 6; k++) slot(sm, lay.der0 + PHS_ADJ_DER * cv + k) = dd[k];
+        }
+      }
+      const double d = dsub(dsub(msq_b, cmsq[0]), cmsq[1]);
+      const double lda = dsub(dmul(d, d), dmul(dmul(4.0, cmsq[0]), cmsq[1]));
+      ok = ok && (lda > 0.0) && (m_b > dadd(cm[0], cm[1])) && (m_b <= mmax_b);
+      const double sl = sqrt(lda);
+      const double rm = m_b > 0.0 ? __drcp_rn(m_b) : 0.0;
+      const double hm = 0.5 * rm;
+      const double pc = sl * hm;
+      const double ce0 = (msq_b + cmsq[0] - cmsq[1]) * hm;
+      const double ce1 = (msq_b + cmsq[1] - cmsq[0]) * hm;
+      const double bg = p_b * rm;
+      const double ga = V.self_root ? 1.0 : E_b * rm;
+      double sphi, cphi, ct, st, fct;
+      sincospi(2.0 * xe[V.x_phi], &sphi, &cphi);
+      map_ct(V.ct_class, xe[V.x_ct], V.b0, V.b1, ct, st, fct);
+      {
+        double dct, dst, dlf;
+        ct_derivs(V.ct_class, xe[V.x_ct], V.b0, V.b1, ct, st, dct, dst, dlf);
+        const int b = lay.ang0 + PHS_ADJ_ANG * v;
+        slot(sm, b + 0) = cphi;
+        slot(sm, b + 1) = sphi;
+        slot(sm, b + 2) = ct;
+        slot(sm, b + 3) = st;
+        slot(sm, b + 4) = dct;
+        slot(sm, b + 5) = dst;
+        slot(sm, b + 6) = dlf;
+      }
+      const double e01 = -bg * st, e03 = bg * ct, e11 = ct * cphi, e12 = -sphi, e13 = st * cphi;
+      const double e21 = ct * sphi, e22 = cphi, e23 = st * sphi, e31 = -ga * st, e33 = ga * ct;
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
+        L[4 * r + 0] = l0 * ga + l3 * bg;
+        L[4 * r + 1] = l0 * e01 + l1 * e11 + l2 * e21 + l3 * e31;
+        L[4 * r + 2] = l1 * e12 + l2 * e22;
+        L[4 * r + 3] = l0 * e03 + l1 * e13 + l2 * e23 + l3 * e33;
+      }
+      if (V.push >= 0) {
+        const bool j0 = V.push == 0;
+        const int base = lay.stack0 + PHS_STATE * sp;
+#pragma unroll
+        for (int i = 0; i < 16; i++) slot(sm, base + i) = L[i];
+        slot(sm, base + 16) = j0 ? cmsq[0] : cmsq[1];
+        slot(sm, base + 17) = j0 ? cm[0] : cm[1];
+        slot(sm, base + 18) = j0 ? pc : -pc;
+        slot(sm, base + 19) = j0 ? cmax[0] : cmax[1];
+        slot(sm, base + 20) = j0 ? ce0 : ce1;
+        sp++;
+      }
+      if (V.carry >= 0) {
+        const bool j0 = V.carry == 0;
+        msq_b = j0 ? cmsq[0] : cmsq[1];
+        m_b = j0 ? cm[0] : cm[1];
+        p_b = j0 ? pc : -pc;
+        mmax_b = j0 ? cmax[0] : cmax[1];
+        E_b = j0 ? ce0 : ce1;
+      } else if (sp > 0) {
+        // the frame the reverse walk resumes with after this pop
+#pragma unroll
+        for (int i = 0; i < 16; i++) slot(sm, lay.pop0 + 16 * np + i) = L[i];
+        np++;
+        sp--;
+        const int base = lay.stack0 + PHS_STATE * sp;
+#pragma unroll
+        for (int i = 0; i < 16; i++) L[i] = slot(sm, base + i);
+        msq_b = slot(sm, base + 16);
+        m_b = slot(sm, base + 17);
+        p_b = slot(sm, base + 18);
+        mmax_b = slot(sm, base + 19);
+        E_b = slot(sm, base + 20);
+      }
+    }
+    if (!ok) continue;  // zero derivatives
+
+    // ---------------------------------------------------------------- 2. reverse walk
+    // L holds the frame after the last visit; Lb the adjoint of the current visit's frame
+    double Lb[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) Lb[i] = 0.0;
+    double sb_msq = 0.0, sb_m = 0.0, sb_p = 0.0, sb_E = 0.0;  // carried child's state adjoint
+    int asp = 0;
+    for (int v = n_visits - 1; v >= 0; v--) {
+      const PhsVisit &V = ch.visit[v];
+      const PhsAdjVisit &A = ad.visit[v];
+      const double msq_v = slot(sm, lay.state0 + 4 * v + 0);
+      const double m_v = slot(sm, lay.state0 + 4 * v + 1);
+      const double p_v = slot(sm, lay.state0 + 4 * v + 2);
+      const double E_v = slot(sm, lay.state0 + 4 * v + 3);
+      double cmsq[2], cm[2];
+      double c_msqb[2] = {0.0, 0.0}, c_mb[2] = {0.0, 0.0}, c_pb[2] = {0.0, 0.0}, c_Eb[2] = {0.0, 0.0};
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        const PhsChild &C = V.child[j];
+        if (!C.internal) {
+          cmsq[j] = C.msq_leaf;
+          cm[j] = C.m_leaf;
+        } else {
+          cmsq[j] = slot(sm, lay.state0 + 4 * A.child_visit[j] + 0);
+          cm[j] = slot(sm, lay.state0 + 4 * A.child_visit[j] + 1);
+        }
+      }
+      if (V.carry >= 0) {
+        const int j = V.carry;
+        c_msqb[j] = sb_msq; c_mb[j] = sb_m; c_pb[j] = sb_p; c_Eb[j] = sb_E;
+      }
+      if (V.push >= 0) {
+        asp--;
+        const int base = lay.stack0 + PHS_ADJ_FRAME * asp;
+#pragma unroll
+        for (int i = 0; i < 16; i++) Lb[i] += slot(sm, base + i);
+        const int j = V.push;
+        c_msqb[j] = slot(sm, base + 16);
+        c_mb[j] = slot(sm, base + 17);
+        c_pb[j] = slot(sm, base + 18);
+        c_Eb[j] = slot(sm, base + 19);
+      }
+      // local quantities of the visit, recomputed
+      const double d = msq_v - cmsq[0] - cmsq[1];
+      const double lda = d * d - 4.0 * cmsq[0] * cmsq[1];
+      const double sl = sqrt(lda);
+      const double rm = __drcp_rn(m_v), hm = 0.5 * rm;
+      const double pc = sl * hm;
+      const double A0 = msq_v + cmsq[0] - cmsq[1], A1 = msq_v + cmsq[1] - cmsq[0];
+      const double ce0 = A0 * hm, ce1 = A1 * hm;
+      const double bg = p_v * rm;
+      const double ga = V.self_root ? 1.0 : E_v * rm;
+      const int ab = lay.ang0 + PHS_ADJ_ANG * v;
+      const double cphi = slot(sm, ab + 0), sphi = slot(sm, ab + 1);
+      const double ct = slot(sm, ab + 2), st = slot(sm, ab + 3);
+      double L1[16] = {ga,  -bg * st, 0.0,   bg * ct,
+                       0.0, ct * cphi, -sphi, st * cphi,
+                       0.0, ct * sphi, cphi,  st * sphi,
+                       bg,  -ga * st, 0.0,   ga * ct};
+      // leaf children: P_j = L (ce_j, 0, 0, +-pc)
+      double pcb = 0.0, ceb[2] = {0.0, 0.0};
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        const PhsChild &C = V.child[j];
+        if (!C.internal) {
+          const double sj = j == 0 ? 1.0 : -1.0;
+          const double ce = j == 0 ? ce0 : ce1;
+          const double *P = pb + 4 * C.out_index;
+          double v0 = 0.0, v3 = 0.0;
+#pragma unroll
+          for (int r = 0; r < 4; r++) {
+            Lb[4 * r + 0] += P[r] * ce;
+            Lb[4 * r + 3] += P[r] * sj * pc;
+            v0 += L[4 * r + 0] * P[r];
+            v3 += L[4 * r + 3] * P[r];
+          }
+          ceb[j] += v0;
+          pcb += sj * v3;
+        } else {
+          ceb[j] += c_Eb[j];
+          pcb += (j == 0 ? 1.0 : -1.0) * c_pb[j];
+        }
+      }
+      // parent frame L_pre = L eta L1^T eta; adjoints L1bar = L_pre^T Lb, Lpre_bar = Lb L1^T.
+      // L1 has zeros at (0,2), (1,0), (2,0), (3,2), and only its other 12 entries carry
+      // adjoints; the loops skip the zero terms (the compiler folds the constant ones).
+      const double eta[4] = {1.0, -1.0, -1.0, -1.0};
+      double Lp[16], Lpb[16], L1b[16];
+#pragma unroll
+      for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          double acc = 0.0, accb = 0.0;
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            if ((c == 0 && k == 2) || (c == 1 && k == 0) || (c == 2 && k == 0) || (c == 3 && k == 2))
+              continue;
+            acc += L[4 * r + k] * (eta[k] * eta[c]) * L1[4 * c + k];
+            accb += Lb[4 * r + k] * L1[4 * c + k];
+          }
+          Lp[4 * r + c] = acc;
+          Lpb[4 * r + c] = accb;
+        }
+#pragma unroll
+      for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          if ((r == 0 && c == 2) || (r == 1 && c == 0) || (r == 2 && c == 0) || (r == 3 && c == 2)) {
+            L1b[4 * r + c] = 0.0;
+            continue;
+          }
+          double acc = 0.0;
+#pragma unroll
+          for (int k = 0; k < 4; k++) acc += Lp[4 * k + r] * Lb[4 * k + c];
+          L1b[4 * r + c] = acc;
+        }
+      const double gab = L1b[0] - L1b[13] * st + L1b[15] * ct;
+      const double bgb = -L1b[1] * st + L1b[3] * ct + L1b[12];
+      const double ctb = L1b[3] * bg + L1b[5] * cphi + L1b[9] * sphi + L1b[15] * ga;
+      const double stb = -L1b[1] * bg + L1b[7] * cphi + L1b[11] * sphi - L1b[13] * ga;
+      const double cpb = L1b[5] * ct + L1b[7] * st + L1b[10];
+      const double spb = -L1b[6] + L1b[9] * ct + L1b[11] * st;
+      xb[V.x_phi] = 2.0 * PHS_PI * (-sphi * cpb + cphi * spb);
+      xb[V.x_ct] = ctb * slot(sm, ab + 4) + stb * slot(sm, ab + 5) + jb * slot(sm, ab + 6);
+      // bg = p rm, gamma = E rm
+      double vb_p = 0.0, vb_E = 0.0, rmb = 0.0;
+      if (!V.self_root) {
+        vb_p = bgb * rm;
+        vb_E = gab * rm;
+        rmb = bgb * p_v + gab * E_v;
+      }
+      // p_decay, daughter energies, log-Jacobian term log(sl) - 2 log(m)
+      const double slb = pcb * hm + jb / sl;
+      const double hmb = pcb * sl + ceb[0] * A0 + ceb[1] * A1;
+      double vb_msq = (ceb[0] + ceb[1]) * hm;
+      double cmsqb[2] = {(ceb[0] - ceb[1]) * hm, (ceb[1] - ceb[0]) * hm};
+      rmb += 0.5 * hmb + 2.0 * jb * m_v;
+      const double vb_m = -rmb * rm * rm;
+      const double ldab = slb / (2.0 * sl);
+      const double db = 2.0 * d * ldab;
+      vb_msq += db;
+      cmsqb[0] += -4.0 * cmsq[1] * ldab - db;
+      cmsqb[1] += -4.0 * cmsq[0] * ldab - db;
+      // internal children: their msq is complete now; map it to x and the mapping parameters
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        const PhsChild &C = V.child[j];
+        if (!C.internal) continue;
+        const double msqb = cmsqb[j] + c_msqb[j] + c_mb[j] / (2.0 * cm[j]);
+        const int db = lay.der0 + PHS_ADJ_DER * A.child_visit[j];
+        xb[C.x_msq] = msqb * slot(sm, db + 0) + jb * slot(sm, db + 1);
+        if (C.map_id == PHS_MAP_SCHANNEL && 2 * C.x_msq + 1 < th_stride) {
+          tb[2 * C.x_msq] = msqb * slot(sm, db + 2) + jb * slot(sm, db + 4);
+          tb[2 * C.x_msq + 1] = msqb * slot(sm, db + 3) + jb * slot(sm, db + 5);
+        }
+      }
+      // on to the previous visit
+      if (v > 0) {
+        if (A.entered_by_pop) {
+          const int base = lay.stack0 + PHS_ADJ_FRAME * asp;
+#pragma unroll
+          for (int i = 0; i < 16; i++) slot(sm, base + i) = Lpb[i];
+          slot(sm, base + 16) = vb_msq;
+          slot(sm, base + 17) = vb_m;
+          slot(sm, base + 18) = vb_p;
+          slot(sm, base + 19) = vb_E;
+          asp++;
+#pragma unroll
+          for (int i = 0; i < 16; i++) {
+            L[i] = slot(sm, lay.pop0 + 16 * A.pop_slot + i);
+            Lb[i] = 0.0;
+          }
+          sb_msq = sb_m = sb_p = sb_E = 0.0;
+        } else {
+#pragma unroll
+          for (int i = 0; i < 16; i++) {
+            L[i] = Lp[i];
+            Lb[i] = Lpb[i];
+          }
+          sb_msq = vb_msq; sb_m = vb_m; sb_p = vb_p; sb_E = vb_E;
+        }
+      }
+    }
+  }
+}
+
+}  // namespace
+
+void phs_adjoint_sizes(int max_visits, int max_pops, int stack_depth, int *state0, int *ang0,
+                       int *der0, int *pop0, int *stack0, size_t *smem) {
+  *state0 = 0;
+  *ang0 = PHS_ADJ_STATE * max_visits;
+  *der0 = *ang0 + PHS_ADJ_ANG * max_visits;
+  *pop0 = *der0 + PHS_ADJ_DER * max_visits;
+  *stack0 = *pop0 + 16 * max_pops;
+  const int slots = *stack0 + PHS_STATE * (stack_depth > 0 ? stack_depth : 0);
+  *smem = (size_t)slots * PHS_ADJ_BLOCK * sizeof(double);
+}
+
+cudaError_t phs_launch_adjoint(const PhsLaunch &a, const PhsAdjChannel *adj, const double *pbar,
+                               const double *jbar, double *xbar, double *thbar, int th_stride,
+                               int max_visits, int max_pops, int n_blocks, cudaStream_t stream) {
+  if (a.n_tiles <= 0) return cudaSuccess;
+  AdjLayout lay;
+  size_t smem;
+  phs_adjoint_sizes(max_visits, max_pops, a.stack_depth, &lay.state0, &lay.ang0, &lay.der0,
+                    &lay.pop0, &lay.stack0, &smem);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(phs_adjoint_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  phs_adjoint_kernel<<<n_blocks, PHS_ADJ_BLOCK, smem, stream>>>(a, adj, pbar, jbar, xbar, thbar,
+                                                                th_stride, lay);
+  return cudaGetLastError();
+}
+
+int phs_adjoint_blocks_per_sm(int max_visits, int max_pops, int stack_depth) {
+  int s0, a0, d0, p0, k0;
+  size_t smem;
+  phs_adjoint_sizes(max_visits, max_pops, stack_depth, &s0, &a0, &d0, &p0, &k0, &smem);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(phs_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phs_adjoint_kernel, PHS_ADJ_BLOCK, smem);
+  return n > 0 ? n : 1;
+}

@@ -223,9 +223,10 @@ struct phs_process {
   int ff_variant = -1;  // autotuned FP32-pair kernel variant (-1: not tuned yet)
   std::vector<PhsChannel> prog;
   std::vector<PhsChannelFF> prog_ff;
+  std::vector<PhsAdjChannel> prog_adj;
   std::vector<ChanLayout> lay;
-  int stack_depth = 0;
-  DevBuf d_prog, d_prog_ff;
+  int stack_depth = 0, max_visits = 0, max_pops = 0;
+  DevBuf d_prog, d_prog_ff, d_prog_adj;
   Segments segs;
   // host-path pipeline
   static const int kStreams = 2;
@@ -295,6 +296,7 @@ extern "C" int phs_process_destroy(phs_process_t h) {
   }
   h->d_prog.release();
   h->d_prog_ff.release();
+  h->d_prog_adj.release();
   h->segs.dev.release();
   delete h;
   return PHS_OK;
@@ -328,16 +330,29 @@ extern "C" int phs_process_set_beams(phs_process_t h, double E1, double E2) {
     depth = std::max(depth, info.stack_depth);
   }
   std::vector<PhsChannelFF> prog_ff(prog.size());
-  for (size_t c = 0; c < prog.size(); c++) phs::channel_to_ff(prog[c], prog_ff[c]);
+  std::vector<PhsAdjChannel> prog_adj(prog.size());
+  int max_visits = 0, max_pops = 0;
+  for (size_t c = 0; c < prog.size(); c++) {
+    phs::channel_to_ff(prog[c], prog_ff[c]);
+    phs::channel_adjoint(prog[c], prog_adj[c]);
+    max_visits = std::max(max_visits, (int)prog[c].n_visits);
+    max_pops = std::max(max_pops, (int)prog_adj[c].n_pops);
+  }
   int rc = h->d_prog.reserve(prog.size() * sizeof(PhsChannel));
   if (rc) return rc;
   if ((rc = h->d_prog_ff.reserve(prog_ff.size() * sizeof(PhsChannelFF)))) return rc;
+  if ((rc = h->d_prog_adj.reserve(prog_adj.size() * sizeof(PhsAdjChannel)))) return rc;
+  CUDA_TRY(cudaMemcpy(h->d_prog_adj.ptr, prog_adj.data(), prog_adj.size() * sizeof(PhsAdjChannel),
+                      cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(h->d_prog.ptr, prog.data(), prog.size() * sizeof(PhsChannel),
                       cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(h->d_prog_ff.ptr, prog_ff.data(), prog_ff.size() * sizeof(PhsChannelFF),
                       cudaMemcpyHostToDevice));
   h->prog = std::move(prog);
   h->prog_ff = std::move(prog_ff);
+  h->prog_adj = std::move(prog_adj);
+  h->max_visits = max_visits;
+  h->max_pops = max_pops;
   h->lay.assign(P.n_channels, ChanLayout{P.n_out, P.n_x});
   h->stack_depth = depth;
   h->E1 = E1;
@@ -467,6 +482,35 @@ extern "C" int phs_generate_beams_device(phs_process_t h, int64_t n_events, cons
   }
   return launch_process(h, h->segs, n_events, counts, 0, x, p, f, v, ok, E1, E2, 1, false,
                         (cudaStream_t)stream);
+}
+
+// Reverse-mode derivatives for cotangents pbar (momenta) and jbar (log-Jacobian).
+extern "C" int phs_adjoint_device(phs_process_t h, int64_t n_events, const int64_t *counts,
+                                  const double *x, const double *pbar, const double *jbar,
+                                  double *xbar, double *thbar, void *stream) {
+  if (int rc = check_proc(h)) return rc;
+  if (!h->beams) return fail(PHS_ERR_STATE, "phs_process_set_beams has not been called");
+  if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
+  if (n_events > 0 && (!x || !pbar || !xbar || !thbar))
+    return fail(PHS_ERR_INVALID_ARG, "null data pointer");
+  DeviceGuard g(h->device);
+  int64_t one = n_events;
+  int rc = build_segments(h->segs, counts ? counts : &one, h->p.n_channels, h->lay, 0, 0, 0, false);
+  if (rc) return rc;
+  PhsLaunch a;
+  memset(&a, 0, sizeof a);
+  a.channels = h->d_prog.as<PhsChannel>();
+  a.stack_depth = h->stack_depth;
+  a.x = x;
+  if ((rc = attach_segments(h->segs, a, (cudaStream_t)stream))) return rc;
+  if (a.n_tiles == 0) return PHS_OK;
+  const int per_sm = phs_adjoint_blocks_per_sm(h->max_visits, h->max_pops, h->stack_depth);
+  const int64_t want = (a.n_tiles + PHS_ADJ_BLOCK_HOST / 32 - 1) / (PHS_ADJ_BLOCK_HOST / 32);
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sm_count(h->device) * per_sm));
+  CUDA_TRY(phs_launch_adjoint(a, h->d_prog_adj.as<PhsAdjChannel>(), pbar, jbar, xbar, thbar,
+                              2 * std::max(1, h->p.n_out - 2), h->max_visits, h->max_pops, grid,
+                              (cudaStream_t)stream));
+  return PHS_OK;
 }
 
 // Host path: chunks alternate between two streams; each stream's buffers are reused only

@@ -347,4 +347,39 @@ void channel_to_ff(const PhsChannel &in, PhsChannelFF &out) {
   }
 }
 
+// Which visit holds each internal child, and where a pop enters a visit: the adjoint walks
+// the visits backwards and, at a visit entered by a pop, resumes with the frame that the
+// forward walk saved just before the pop.
+void channel_adjoint(const PhsChannel &in, PhsAdjChannel &out) {
+  memset(&out, 0, sizeof(out));
+  std::vector<std::pair<int, int>> pushed;  // (visit, child) awaiting their visit
+  int pops = 0;
+  for (int v = 0; v < in.n_visits; v++) {
+    const PhsVisit &V = in.visit[v];
+    PhsAdjVisit &A = out.visit[v];
+    A.child_visit[0] = A.child_visit[1] = -1;
+    for (int j = 0; j < 2; j++) {
+      const PhsChild &C = V.child[j];
+      if (C.internal && C.map_id == PHS_MAP_SCHANNEL) {
+        const double m2 = C.m * C.m, mw = C.m * C.w;
+        const double u0 = (C.msq_min - m2) / mw, u1 = (C.msq_max - m2) / mw;
+        A.child[j].da0_dm = -(C.msq_min + m2) / (m2 * C.w) / (1 + u0 * u0);
+        A.child[j].da1_dm = -(C.msq_max + m2) / (m2 * C.w) / (1 + u1 * u1);
+        A.child[j].da0_dw = -u0 / (C.w * (1 + u0 * u0));
+        A.child[j].da1_dw = -u1 / (C.w * (1 + u1 * u1));
+      }
+    }
+    if (V.carry >= 0) A.child_visit[V.carry] = v + 1;
+    if (V.push >= 0) pushed.push_back({v, V.push});
+    if (V.carry < 0 && v + 1 < in.n_visits) {
+      const auto vj = pushed.back();
+      pushed.pop_back();
+      out.visit[vj.first].child_visit[vj.second] = v + 1;
+      out.visit[v + 1].entered_by_pop = 1;
+      out.visit[v + 1].pop_slot = pops++;
+    }
+  }
+  out.n_pops = pops;
+}
+
 }  // namespace phs

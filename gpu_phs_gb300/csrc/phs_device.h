@@ -61,3 +61,13 @@ size_t phs_noalloc_scratch_bytes();
 cudaError_t phs_launch_forward_ff(const PhsLaunch &a, int n_blocks, int variant, cudaStream_t stream);
 int phs_forward_ff_blocks_per_sm(int stack_depth, int variant);
 size_t phs_forward_ff_smem_bytes(int stack_depth);
+
+// Reverse-mode derivatives (phs_adjoint.cu): xbar [event][x stride] and thbar
+// [event][th_stride] (d/dm, d/dGamma per Breit-Wigner branch, at 2 * its msq x index).
+cudaError_t phs_launch_adjoint(const PhsLaunch &a, const PhsAdjChannel *adj, const double *pbar,
+                               const double *jbar, double *xbar, double *thbar, int th_stride,
+                               int max_visits, int max_pops, int n_blocks, cudaStream_t stream);
+int phs_adjoint_blocks_per_sm(int max_visits, int max_pops, int stack_depth);
+void phs_adjoint_sizes(int max_visits, int max_pops, int stack_depth, int *state0, int *ang0,
+                       int *der0, int *pop0, int *stack0, size_t *smem);
+#define PHS_ADJ_BLOCK_HOST 64

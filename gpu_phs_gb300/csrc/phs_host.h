@@ -34,6 +34,9 @@ int compile_channel(const Process &p, int c, double sqrts, PhsChannel &out, Chan
 // Float-float copy of a compiled channel (same visit order and x indices).
 void channel_to_ff(const PhsChannel &in, PhsChannelFF &out);
 
+// Reverse-walk tables of a compiled channel for the adjoint kernel.
+void channel_adjoint(const PhsChannel &in, PhsAdjChannel &out);
+
 // Validates the sizes and tables of a whole process (no sqrt(s) needed).
 int validate_process(const Process &p, std::string &err);
 

@@ -127,3 +127,22 @@ struct PhsChannelFF {
   double volume;
   PhsVisitFF visit[PHS_MAX_VISITS];
 };
+
+// ------------------------------------------------------------------------------------
+// Reverse-walk tables of a channel, for the adjoint kernel (phs_adjoint.cu).
+struct PhsAdjChild {
+  double da0_dm, da0_dw, da1_dm, da1_dw;  // Breit-Wigner: derivatives of the atan bounds
+};
+
+struct PhsAdjVisit {
+  int32_t child_visit[2];  // visit index where an internal child is the visited branch, -1: leaf
+  int32_t entered_by_pop;  // 1: this visit follows a pop (its predecessor ends a subtree)
+  int32_t pop_slot;        // frame slot holding the predecessor's frame (entered_by_pop)
+  PhsAdjChild child[2];
+};
+
+struct PhsAdjChannel {
+  int32_t n_pops;
+  int32_t pad;
+  PhsAdjVisit visit[PHS_MAX_VISITS];
+};

@@ -125,6 +125,18 @@ int phs_generate_device_noalloc(phs_process_t proc, double E1, double E2, int64_
                                 const int64_t *channel_counts, const double *x, double *p,
                                 double *factors, double *volumes, uint8_t *oks, void *stream);
 
+/* Reverse-mode derivatives (FP64, uniform beams) of the forward map on device pointers.
+ * Given cotangents pbar [n_events][n_out][4] of the momenta and jbar [n_events] of the
+ * log-Jacobian log(factor) (jbar may be NULL), writes
+ *   xbar  [n_events][n_x]            sum pbar . dp/dx + jbar dlog(factor)/dx
+ *   thbar [n_events][n_out - 2][2]   the same for d/dm and d/dGamma of the Breit-Wigner
+ *                                    branch whose msq x index is the middle index (0 else).
+ * ok = 0 events get zeros.  The boost chain is recomputed backwards from the last frame;
+ * no per-branch matrices are stored.  No counterpart in the reference (forward only). */
+int phs_adjoint_device(phs_process_t proc, int64_t n_events, const int64_t *channel_counts,
+                       const double *x, const double *pbar, const double *jbar, double *xbar,
+                       double *thbar, void *stream);
+
 /* Host pointers in and out (pinned memory is fastest); copies run chunk-pipelined with the
  * kernel.  Synchronous. */
 int phs_generate_host(phs_process_t proc, int64_t n_events, const int64_t *channel_counts,
