@@ -252,6 +252,32 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64):
                            "ok_fraction": bufs[0][3].double().mean().item(),
                            "ok_mismatches_fp32_mixed_vs_fp64": int((bufs[0][3] != bufs[1][3]).sum().item()),
                            "ok_mismatches_vs_per_channel_runs": per_channel_mism}
+    del bufs, xb, spaces
+
+    # adjoint: forward + reverse on 1e6 tt events with random cotangents
+    proc = P.tt()
+    n = 1_000_000
+    ps = PhaseSpace(proc, proc.sqrts / 2, proc.sqrts / 2)
+    x = torch.empty((n, proc.n_x), dtype=torch.float64, device="cuda")
+    philox_fill(x, n, proc.n_x, SEED)
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    pbar = torch.randn((n, proc.n_out, 4), dtype=torch.float64, device="cuda", generator=g)
+    jbar = torch.randn(n, dtype=torch.float64, device="cuda", generator=g)
+    o = ps.alloc(n)
+    t_fwd = _time_calls(torch, lambda: ps.generate(x, out=o), steps, warmup, stream)
+    torch.cuda.reset_peak_memory_stats()
+    base = torch.cuda.memory_allocated()
+    t_adj = _time_calls(torch, lambda: ps.vjp(x, pbar, jbar), steps, warmup, stream)
+    n_internal = proc.n_out - 1
+    res["adjoint_tt"] = {
+        "n_events": n, "n_x": proc.n_x,
+        "forward_ms": t_fwd, "adjoint_ms": t_adj, "adjoint_over_forward": t_adj / t_fwd,
+        "fwd_plus_bwd_events_per_s": n / (t_fwd + t_adj) * 1e3,
+        "outputs": "d(momenta, log factor)/dx and d/d(m, Gamma) of every Breit-Wigner branch",
+        "peak_hbm_bytes_per_event": (torch.cuda.max_memory_allocated() - base) / n,
+        "output_bytes_per_event": 8 * proc.n_x + 16 * (proc.n_out - 2),
+        "stored_matrix_checkpoint_bytes_per_event": 16 * 8 * n_internal,
+        "scratch": "per-visit state in shared memory; the boost chain is recomputed in reverse"}
     return res
 
 

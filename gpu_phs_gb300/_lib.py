@@ -32,6 +32,7 @@ _SIGS = {
     "phs_generate_beams_device": (I, [P, I64, P, P, P, P, P, P, P, P, P]),
     "phs_generate_host": (I, [P, I64, P, P, P, P, P, P]),
     "phs_adjoint_device": (I, [P, I64, P, P, P, P, P, P, P]),
+    "phs_inverse_device": (I, [P, I64, P, P, P, P, P, P, P, P, P, P]),
     "phs_generate_device_noalloc": (I, [P, D, D, I64, P, P, P, P, P, P, P]),
     "phs_batch_create": (I, [C.POINTER(P), I, P]),
     "phs_batch_destroy": (I, [P]),

@@ -141,6 +141,25 @@ class PhaseSpace:
                                         _ptr(xbar), _ptr(thbar), _stream(stream)))
         return xbar, thbar
 
+    def inverse(self, p, counts=None, ok=None, x=None, factor=None, E1=None, E2=None,
+                stream=None):
+        """All-channel factors [n, n_channels] and x [n_channels, n, n_x] of events with lab
+        momenta p [n, n_out, 4] (CUDA float64), events grouped by generating channel.  With
+        x (and factor) the generating channel's row is copied from them, as the reference
+        does; without, it is inverted like the others (a round trip of the forward map)."""
+        import torch
+        n = int(p.shape[0])
+        if p.dtype != torch.float64 or not p.is_cuda or not p.is_contiguous():
+            raise ValueError("p must be a contiguous CUDA float64 tensor")
+        nch = self.proc.n_channels
+        fac = torch.empty((n, nch), dtype=torch.float64, device=p.device)
+        xo = torch.empty((nch, n, self.proc.n_x), dtype=torch.float64, device=p.device)
+        c = self._counts(counts, nch, n)
+        check(load().phs_inverse_device(self.h, n, _ptr(c), _ptr(E1), _ptr(E2), _ptr(p), _ptr(ok),
+                                        _ptr(x), _ptr(factor), _ptr(fac), _ptr(xo),
+                                        _stream(stream)))
+        return fac, xo
+
     def generate_host(self, x, counts=None, out: Optional[Events] = None) -> Events:
         """Host (ideally pinned) tensors or arrays in and out; synchronous."""
         import torch

@@ -23,7 +23,11 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["phs_kernels.cu", "phs_kernels_ff.cu", "phs_adjoint.cu"]
+CU_SOURCES = ["phs_kernels.cu", "phs_kernels_ff.cu", "phs_adjoint.cu", "phs_inverse.cu"]
+# The inverse map mirrors the operation order of the reference's algorithm (as the oracle
+# restates it) without contraction: its results then differ from the oracle's only by the
+# ulps of the transcendental functions, although x(p) is ill-conditioned near the poles.
+CU_FLAGS = {"phs_inverse.cu": ["-fmad=false"]}
 CPP_SOURCES = ["phs_compile.cpp", "phs_api.cpp"]
 
 
@@ -44,7 +48,7 @@ def _stale(out: str, deps) -> bool:
 def build(verbose: bool = False, force: bool = False) -> str:
     """Compile and link; returns the library path.  Raises RuntimeError on failure."""
     os.makedirs(BUILD, exist_ok=True)
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "gpu_phs.h"))
     inc = ["-I", os.path.join(ROOT, "include"), "-I", CSRC, "-I", os.path.join(CUDA_HOME, "include")]
     jobs, objs = [], []
@@ -54,7 +58,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         objs.append(o)
         if force or _stale(o, [s] + headers):
             jobs.append([NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                         "-Xptxas", "-v", *inc, "-c", s, "-o", o])
+                         "-Xptxas", "-v", *CU_FLAGS.get(src, []), *inc, "-c", s, "-o", o])
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD, src + ".o")

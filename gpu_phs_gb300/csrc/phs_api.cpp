@@ -226,7 +226,10 @@ struct phs_process {
   std::vector<PhsAdjChannel> prog_adj;
   std::vector<ChanLayout> lay;
   int stack_depth = 0, max_visits = 0, max_pops = 0;
+  bool has_friends = false;
   DevBuf d_prog, d_prog_ff, d_prog_adj;
+  DevBuf d_ch_begin;                  // inverse map: first event per generating channel
+  std::vector<int64_t> ch_begin_up;   // content of d_ch_begin
   Segments segs;
   // host-path pipeline
   static const int kStreams = 2;
@@ -297,6 +300,7 @@ extern "C" int phs_process_destroy(phs_process_t h) {
   h->d_prog.release();
   h->d_prog_ff.release();
   h->d_prog_adj.release();
+  h->d_ch_begin.release();
   h->segs.dev.release();
   delete h;
   return PHS_OK;
@@ -354,6 +358,9 @@ extern "C" int phs_process_set_beams(phs_process_t h, double E1, double E2) {
   h->max_visits = max_visits;
   h->max_pops = max_pops;
   h->lay.assign(P.n_channels, ChanLayout{P.n_out, P.n_x});
+  h->has_friends = false;
+  for (const auto &ch : h->prog)
+    for (int v = 0; v < ch.n_visits; v++) h->has_friends |= ch.visit[v].friend_sign != 0;
   h->stack_depth = depth;
   h->E1 = E1;
   h->E2 = E2;
@@ -493,6 +500,8 @@ extern "C" int phs_adjoint_device(phs_process_t h, int64_t n_events, const int64
   if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
   if (n_events > 0 && (!x || !pbar || !xbar || !thbar))
     return fail(PHS_ERR_INVALID_ARG, "null data pointer");
+  if (h->has_friends)
+    return fail(PHS_ERR_UNSUPPORTED, "the adjoint does not cover friend (beam-axis) boosts");
   DeviceGuard g(h->device);
   int64_t one = n_events;
   int rc = build_segments(h->segs, counts ? counts : &one, h->p.n_channels, h->lay, 0, 0, 0, false);
@@ -510,6 +519,64 @@ extern "C" int phs_adjoint_device(phs_process_t h, int64_t n_events, const int64
   CUDA_TRY(phs_launch_adjoint(a, h->d_prog_adj.as<PhsAdjChannel>(), pbar, jbar, xbar, thbar,
                               2 * std::max(1, h->p.n_out - 2), h->max_visits, h->max_pops, grid,
                               (cudaStream_t)stream));
+  return PHS_OK;
+}
+
+// Inverse map: all-channel factors and x of generated events.
+extern "C" int phs_inverse_device(phs_process_t h, int64_t n_events, const int64_t *counts,
+                                  const double *E1, const double *E2, const double *p,
+                                  const uint8_t *ok, const double *x_own,
+                                  const double *factor_own, double *all_factors, double *x_out,
+                                  void *stream) {
+  if (int rc = check_proc(h)) return rc;
+  if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
+  if (n_events > 0 && (!p || !all_factors || !x_out))
+    return fail(PHS_ERR_INVALID_ARG, "null data pointer");
+  if ((E1 == nullptr) != (E2 == nullptr))
+    return fail(PHS_ERR_INVALID_ARG, "give both beam energy arrays or neither");
+  if (((uintptr_t)p & 15) != 0) return fail(PHS_ERR_INVALID_ARG, "p must be 16-byte aligned");
+  DeviceGuard g(h->device);
+  if (!h->beams) {
+    if (!E1) return fail(PHS_ERR_STATE, "phs_process_set_beams has not been called");
+    double m_tot = 0;
+    for (int k = 0; k < h->p.n_out; k++) m_tot += h->p.flv_m[h->p.n_in + k];
+    int rc = phs_process_set_beams(h, m_tot + 500.0, m_tot + 500.0);
+    if (rc) return rc;
+  }
+  if (n_events == 0) return PHS_OK;
+  const int nch = h->p.n_channels;
+  std::vector<int64_t> begin(nch, 0);
+  for (int c = 1; c < nch; c++) begin[c] = begin[c - 1] + (counts ? counts[c - 1] : n_events);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (begin != h->ch_begin_up) {
+    int rc = h->d_ch_begin.reserve(nch * sizeof(int64_t));
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(h->d_ch_begin.ptr, begin.data(), nch * sizeof(int64_t),
+                             cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    h->ch_begin_up = begin;
+  }
+  PhsInvLaunch a;
+  memset(&a, 0, sizeof a);
+  a.channels = h->d_prog.as<PhsChannel>();
+  a.ch_begin = h->d_ch_begin.as<int64_t>();
+  a.p = p;
+  a.ok = ok;
+  a.E1 = E1;
+  a.E2 = E2;
+  a.x_own = x_own;
+  a.factor_own = factor_own;
+  a.all_factors = all_factors;
+  a.x_out = x_out;
+  a.n_events = n_events;
+  a.n_channels = nch;
+  a.n_out = h->p.n_out;
+  a.n_x = h->p.n_x;
+  a.stack_depth = h->stack_depth;
+  const int64_t tiles = (n_events + PHS_INV_BLOCK - 1) / PHS_INV_BLOCK;
+  const int64_t cap = (int64_t)sm_count(h->device) *
+                      phs_inverse_blocks_per_sm(a.n_out, a.stack_depth, E1 != nullptr);
+  CUDA_TRY(phs_launch_inverse(a, (int)std::max<int64_t>(1, std::min(tiles, cap)), st));
   return PHS_OK;
 }
 
@@ -893,6 +960,7 @@ struct Whizard {
   int64_t batch_size = 0;
   phs_process_t proc = nullptr;
   DevBuf dx, dp, df, dv, dok;
+  DevBuf dfa, dxo;  // all-channel factors and x of the inverse map
   int64_t last_events = 0;
   int msq_threads = 0, cb_threads = 0, ab_threads = 0;
 };
@@ -904,6 +972,7 @@ void whizard_log(int rc) {
 
 void whizard_release_device() {
   W.dx.release(); W.dp.release(); W.df.release(); W.dv.release(); W.dok.release();
+  W.dfa.release(); W.dxo.release();
   W.last_events = 0;
 }
 }  // namespace
@@ -1050,6 +1119,7 @@ extern "C" void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in,
                                              double *p, double *x_out) {
   (void)requires_boost_to_lab;  // stored but unused by the reference (phs.cu:1559)
   std::lock_guard<std::mutex> lk(W.mu);
+  g_err.clear();  // the call returns nothing: phs_last_error() reports this call alone
   int rc = PHS_OK;
   do {
     if (!W.proc) { rc = fail(PHS_ERR_STATE, "c_whizard_gen_phs_from_x_gpu: init_gpu_phs not done"); break; }
@@ -1097,25 +1167,24 @@ extern "C" void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in,
                                      W.dok.as<uint8_t>(), nullptr);
     }
     if (rc) break;
-    std::vector<double> fh(n);
+    // the inverse map fills factors[n_channels * i + c] and x_out[n_x * n * c + n_x * i + k]
+    // for every channel (do_inverse_mapping is forced on, whizard_gpu_phs.cpp:118;
+    // layouts phs.cu:1580-1585); the generating channel keeps its own x and factor
+    if ((rc = W.dfa.reserve((size_t)n * nch * sizeof(double)))) break;
+    if ((rc = W.dxo.reserve((size_t)n * nch * n_x * sizeof(double)))) break;
+    rc = phs_inverse_device(W.proc, n, counts.data(), uniform ? nullptr : df + n,
+                            uniform ? nullptr : df + 2 * n, W.dp.as<double>(),
+                            W.dok.as<uint8_t>(), W.dx.as<double>(), df, W.dfa.as<double>(),
+                            W.dxo.as<double>(), nullptr);
+    if (rc) break;
     e = cudaMemcpy(p, W.dp.ptr, n * 4 * n_out * sizeof(double), cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(fh.data(), df, n * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(factors, W.dfa.ptr, (size_t)n * nch * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && x_out)
+      e = cudaMemcpy(x_out, W.dxo.ptr, (size_t)n * nch * n_x * sizeof(double), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(volumes, W.dv.ptr, n * sizeof(double), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(oks, W.dok.ptr, n, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e)); break; }
-    // factors[n_channels * i + c] and x_out[n_x * n * c + n_x * i + k] (phs.cu:1580-1585):
-    // the event's own channel is filled; the other channels' entries need the inverse
-    // mapping, which this build does not provide yet, and are set to 0.
-    memset(factors, 0, (size_t)n * nch * sizeof(double));
-    if (x_out) memset(x_out, 0, (size_t)n * nch * n_x * sizeof(double));
-    int64_t i = 0;
-    for (int c = 0; c < nch; c++) {
-      for (int64_t k = 0; k < counts[c]; k++, i++) {
-        factors[(size_t)nch * i + c] = fh[i];
-        if (x_out) memcpy(x_out + (size_t)n_x * n * c + (size_t)n_x * i, x + (size_t)n_x * i,
-                          n_x * sizeof(double));
-      }
-    }
     W.last_events = n;
   } while (0);
   whizard_log(rc);

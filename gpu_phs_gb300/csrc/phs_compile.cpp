@@ -234,6 +234,14 @@ int compile_channel(const Process &p, int c, double sqrts, PhsChannel &out, Chan
     V.self_m_min = m_min;
     V.self_m_max = m_max;
     V.self_root = cur == R;
+    // friends (extract_boost_origins, phs.cu:268-292): code 2^n_out pairs the branch with
+    // the beam along -z, 2^(n_out+1) with the beam along +z; anything else is no friend
+    const int fr = p.friends[ix(cur)];
+    V.friend_sign = fr == (1 << p.n_out) ? -1 : fr == (1 << (p.n_out + 1)) ? 1 : 0;
+    if (V.friend_sign && cur == R) {
+      err = where + "the root branch cannot have a friend (its decay axis is the beam axis)";
+      return PHS_ERR_TREE;
+    }
     const bool i0 = internal(kid(cur, 0)), i1 = internal(kid(cur, 1));
     V.both_leaves = !i0 && !i1;
     V.push = V.carry = -1;
@@ -280,6 +288,35 @@ int compile_channel(const Process &p, int c, double sqrts, PhsChannel &out, Chan
   };
   vpost(R);
   out.n_vol = ne;
+  // momentum slots for the inverse map: leaves by output index, internals after them
+  auto slot_of = [&](int code) -> int {
+    if (internal(code)) return p.n_out + entry[code];
+    int ld2 = 0, bb = code;
+    while (bb > 1) { bb /= 2; ld2++; }
+    return ld2;
+  };
+  for (int code = 1; code <= R; code++) {
+    if (!internal(code) || entry[code] < 0) continue;
+    out.comb[entry[code]][0] = (int8_t)slot_of(kid(code, 0));
+    out.comb[entry[code]][1] = (int8_t)slot_of(kid(code, 1));
+  }
+  {
+    // visits in program order: the code of each visited branch
+    std::vector<int> st2;
+    int cur2 = R;
+    for (int v2 = 0; v2 < out.n_visits; v2++) {
+      PhsVisit &V = out.visit[v2];
+      V.slot[0] = (int8_t)slot_of(kid(cur2, 0));
+      V.slot[1] = (int8_t)slot_of(kid(cur2, 1));
+      if (V.push >= 0) st2.push_back(kid(cur2, V.push));
+      if (V.carry >= 0) {
+        cur2 = kid(cur2, V.carry);
+      } else if (!st2.empty()) {
+        cur2 = st2.back();
+        st2.pop_back();
+      }
+    }
+  }
   return PHS_OK;
 }
 
@@ -334,6 +371,7 @@ void channel_to_ff(const PhsChannel &in, PhsChannelFF &out) {
       }
       if (C.internal && (C.map_id == PHS_MAP_STEP_E || C.map_id == PHS_MAP_STEP_H)) out.exact_only = 1;
     }
+    if (V.friend_sign) out.exact_only = 1;
     F.x_phi = V.x_phi;
     F.x_ct = V.x_ct;
     F.ct_class = V.ct_class;

@@ -71,3 +71,23 @@ int phs_adjoint_blocks_per_sm(int max_visits, int max_pops, int stack_depth);
 void phs_adjoint_sizes(int max_visits, int max_pops, int stack_depth, int *state0, int *ang0,
                        int *der0, int *pop0, int *stack0, size_t *smem);
 #define PHS_ADJ_BLOCK_HOST 64
+
+// Inverse map (phs_inverse.cu): for every event and every channel, the x row and factor
+// that channel assigns to the event's momenta.
+#define PHS_INV_BLOCK 128
+struct PhsInvLaunch {
+  const PhsChannel *channels;  // device, per channel (uniform-beam constants)
+  const int64_t *ch_begin;     // device, [n_channels]: first event of each generating channel
+  const double *p;             // [n][n_out][4] lab momenta
+  const uint8_t *ok;           // [n] or null (all valid)
+  const double *E1, *E2;       // per-event beams, or null (the programs' beams)
+  const double *x_own;         // [n][n_x]: the generating channel's x (copied), or null
+  const double *factor_own;    // [n]: the generating channel's factor, or null
+  double *all_factors;         // [n][n_channels]
+  double *x_out;               // [n_channels][n][n_x]
+  int64_t n_events;
+  int32_t n_channels, n_out, n_x, stack_depth;
+};
+cudaError_t phs_launch_inverse(const PhsInvLaunch &a, int n_blocks, cudaStream_t stream);
+int phs_inverse_blocks_per_sm(int n_out, int stack_depth, bool per_event);
+size_t phs_inverse_smem_bytes(int n_out, int stack_depth);

@@ -116,6 +116,32 @@ __device__ __forceinline__ void map_ct(int ct_class, double x, double b0, double
   }
 }
 
+// Rotation taking the z axis onto the direction of (bx, by, bz) about the axis z x b
+// (Rodrigues), row-major 3x3: the friend boost's rotation (phs.cu:753-781 restated; the
+// reference's matrix equals this one whenever by = 0, which holds for friends on the root's
+// daughters, the only ones Whizard's trees carry).  The symmetric part is written as
+// cos + (1 - cos) k k^T with k k^T from the transverse components, as the reference does:
+// the form cos + sin^2/(1 + cos) turns rounding of the normalisation into errors of order
+// eps/(1 + cos) as the axis approaches -z.  An axis exactly along -z (where the reference
+// divides 0 by 0) gives the rotation by pi about x.
+__device__ __forceinline__ void rot_z_onto(double bx, double by, double bz, double R[9]) {
+  const double n = sqrt(bx * bx + by * by + bz * bz);
+  bx /= n;
+  by /= n;
+  bz /= n;
+  const double t = bx * bx + by * by;
+  double r00 = 1.0, r01 = 0.0, r11 = bz;
+  if (t > 0.0) {
+    const double w = (1.0 - bz) / t;
+    r00 = bz + w * (by * by);
+    r01 = -w * (bx * by);
+    r11 = bz + w * (bx * bx);
+  }
+  R[0] = r00; R[1] = r01; R[2] = bx;
+  R[3] = r01; R[4] = r11; R[5] = by;
+  R[6] = -bx; R[7] = -by; R[8] = bz;
+}
+
 // Mapping constants at one sqrt(s) (phs_cpu.cpp:452-531), for the per-event-beam path.
 __device__ void child_constants(const PhsChild &C, double sqrts, double m_tot, double &a0,
                                 double &a1, double &a2, double &msq_min, double &msq_max,
@@ -271,7 +297,35 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
     const double e21 = ct * sphi, e22 = cphi, e23 = st * sphi, e31 = -ga * st, e33 = ga * ct;
 
     double Ln[16];
-    if (V.self_root && !lab) {
+    if (V.friend_sign != 0) {
+      // friend boost (phs.cu:853-910): the decay angles are measured from the friend
+      // beam's direction in the branch's rest frame, B_z(-bg) L^-1 (1, 0, 0, ff) (only
+      // its direction matters, so the lab boost inside L needs no special case);
+      // L1 = B_z(bg) diag(1, R_f R(theta, phi)).  Uniform per channel: no divergence.
+      const double ff = V.friend_sign;
+      const double u0 = L[0] - ff * L[12];
+      double Rf[9];
+      rot_z_onto(-(L[1] - ff * L[13]), -(L[2] - ff * L[14]),
+                 -bg * u0 - ga * (L[3] - ff * L[15]), Rf);
+      const double A[9] = {e11, e12, e13, e21, e22, e23, -st, 0.0, ct};
+      double Q[9];
+#pragma unroll
+      for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+          Q[3 * r + c] = Rf[3 * r] * A[c] + Rf[3 * r + 1] * A[3 + c] + Rf[3 * r + 2] * A[6 + c];
+      const double E1r[4] = {ga, bg * Q[6], bg * Q[7], bg * Q[8]};
+      const double E2r[4] = {0.0, Q[0], Q[1], Q[2]};
+      const double E3r[4] = {0.0, Q[3], Q[4], Q[5]};
+      const double E4r[4] = {bg, ga * Q[6], ga * Q[7], ga * Q[8]};
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
+#pragma unroll
+        for (int c = 0; c < 4; c++)
+          Ln[4 * r + c] = l0 * E1r[c] + l1 * E2r[c] + l2 * E3r[c] + l3 * E4r[c];
+      }
+    } else if (V.self_root && !lab) {
       // parent frame is the identity: L0 * L1 = L1
       Ln[0] = ga;  Ln[1] = e01; Ln[2] = 0.0;  Ln[3] = e03;
       Ln[4] = 0.0; Ln[5] = e11; Ln[6] = e12;  Ln[7] = e13;

@@ -1,0 +1,376 @@
+// phs_inverse.cu -- the inverse map: momenta of generated events -> x and factor of every
+// channel (the reference's do_inverse_mapping pass of gen_phs_from_x_gpu, phs.cu:1499-1554,
+// with _combine_particles 1262-1283, _apply_msq_inv 626-675, the boost inversion 924-1244
+// and the inverse mappings of mappings_gpu.hpp:15-219).
+//
+// The reference runs this as a host loop over channels, each iteration a chain of
+// event-parallel kernels (combine, msq, one launch per boost level, with and without
+// friends) that round-trip msq, p_decay, phi/ct/st and a 4x4 matrix per boost through HBM.
+// Here one persistent kernel does all of it: a block takes 128 consecutive events, stages
+// their CM-frame momenta in shared memory once, and every thread then walks the visit
+// program (phs_program.h) of each channel in turn for its event, with the running frame in
+// registers and the channel's branch momenta in its shared-memory column.  Per (event,
+// channel) the only HBM traffic is the x row and the factor written.
+//
+// At a visit of branch b, with Gp and (theta, phi) the frame and angles of b's parent:
+//   G   = [R_f^-1] B_z(-bg_b) R_y(-theta) R_z(-phi) Gp   b's rest frame, z along its flight
+//                                                         (or friend) axis
+//   msq of both daughters from their summed momenta; inverse msq maps of internal ones
+//   Kallen function at b -> daughters' decay momentum; factor *= sqrt(lambda)/msq_b
+//   q   = G p(daughter 1) -> phi = atan2(q_y, q_x), cos(theta) = q_z/|q| -> x, inverse ct map
+//   (G, theta, phi) handed to the internal daughters (carry / stack)
+// The friend rotation R_f is the exact rotation onto the friend beam's direction; the
+// reference's differs from it only away from the root's daughters (phs.cu:1183-1244).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "phs_device.h"
+#include "phs_event_f64.cuh"
+#include "phs_program.h"
+
+#define PHS_INV_STATE 23  // doubles per saved frame: G[16], ct, st, cos phi, sin phi, msq, p_decay, m
+
+namespace {
+
+// mappings_gpu.hpp:15-172 (mapping_x_from_msq_*), constants as in phs_cpu.cpp:452-531.
+__device__ __forceinline__ void map_msq_inverse(int t, double msq, double s, double m, double w,
+                                                double msq_min, double msq_max, double a0,
+                                                double a1, double a2, double &x, double &f) {
+  switch (t) {
+    case PHS_MAP_NO:
+      x = (msq - msq_min) / (msq_max - msq_min);
+      f = (msq_max - msq_min) / s;
+      break;
+    case PHS_MAP_SCHANNEL: {
+      const double z = (msq - m * m) / (m * w);
+      x = (atan(z) - a0) / (a1 - a0);
+      f = a2 * (1.0 + z * z);
+      break;
+    }
+    case PHS_MAP_COLLINEAR:
+    case PHS_MAP_INFRARED:
+    case PHS_MAP_RADIATION: {
+      const double z = msq - msq_min + a0;
+      x = log(z / a0) / a1;
+      f = a2 * z;
+      break;
+    }
+    case PHS_MAP_TCHANNEL:
+    case PHS_MAP_UCHANNEL: {
+      double z;
+      if (msq < (msq_max + msq_min) / 2) {
+        z = msq - msq_min + a0;
+        x = log(z / a0) / a1;
+      } else {
+        z = msq_max - msq + a0;
+        x = 1.0 - log(z / a0) / a1;
+      }
+      f = a2 * z;
+      break;
+    }
+    case PHS_MAP_STEP_E: {
+      const double z1 = (msq - msq_min) / (msq_max - msq_min);
+      const double z2 = 1.0 + a1 * exp(z1 / a2);
+      x = (z1 - a2 * log(z2 / (1.0 + a1))) / a0;
+      f = a0 * z2 * (msq_max - msq_min) / s;
+      break;
+    }
+    case PHS_MAP_STEP_H: {
+      const double z1 = (msq - msq_min) / (msq_max - msq_min);
+      const double z3 = a0 - z1 / a2;
+      x = ((a0 + z1 / a2 + z1) - sqrt(z3 * z3 + 2.0 * z1 * (a0 + z1 / a2) + z1 * z1)) / 2.0;
+      f = (a1 / (a0 - x) / (a0 - x) + a2) * (msq_max - msq_min) / s;
+      break;
+    }
+    default:
+      x = 0.0;
+      f = 0.0;
+  }
+}
+
+// mappings_gpu.hpp:184-219 (mapping_x_from_ct_*).
+__device__ __forceinline__ void map_ct_inverse(int ct_class, double ct, double b0, double b1,
+                                               double &x, double &f) {
+  if (ct_class == PHS_CT_COLLINEAR) {
+    double ct1;
+    if (ct < 0.0) {
+      ct1 = ct + b0 + 1.0;
+      x = log(ct1 / b0) / (2.0 * b1);
+    } else {
+      ct1 = -ct + b0 + 1.0;
+      x = 1.0 - log(ct1 / b0) / (2.0 * b1);
+    }
+    f = ct1 * b1;
+  } else {
+    x = (ct + 1.0) / 2.0;
+    f = 1.0;
+  }
+}
+
+__device__ __forceinline__ void inv_store(double *stk, int depth, int k, double v) {
+  stk[(depth * PHS_INV_STATE + k) * PHS_INV_BLOCK + threadIdx.x] = v;
+}
+__device__ __forceinline__ double inv_load(const double *stk, int depth, int k) {
+  return stk[(depth * PHS_INV_STATE + k) * PHS_INV_BLOCK + threadIdx.x];
+}
+
+// One (event, channel): writes the channel's x entries of xr and returns its factor.
+// pm: this thread's momentum slots, component (4 j + mu) at pm[(4 j + mu) * PHS_INV_BLOCK]:
+// the CM momenta in slots 0..n_out-1, the channel's internal branches after them.
+// The arithmetic keeps the reference's operation order (this file is compiled without
+// contraction): x(p) is ill-conditioned near the poles of each decay (cos(theta) -> +-1,
+// where 1 - cos^2 cancels) and for soft daughters of fast branches, and there any other
+// rounding order moves the result by far more than the input's own rounding does.
+template <bool PER_EVENT>
+__device__ double inverse_event(const PhsChannel &ch, double *pm, double sqrts, double *xr,
+                                double *stk) {
+  const double s = sqrts * sqrts;
+  // internal momenta as sums of their daughters in post-order (_combine_particles,
+  // phs.cu:1262-1283)
+  for (int i = 0; i < ch.n_vol; i++) {
+    const int a = ch.comb[i][0], b = ch.comb[i][1], o = ch.n_out + i;
+#pragma unroll
+    for (int mu = 0; mu < 4; mu++)
+      pm[(4 * o + mu) * PHS_INV_BLOCK] = pm[(4 * a + mu) * PHS_INV_BLOCK] + pm[(4 * b + mu) * PHS_INV_BLOCK];
+  }
+  // carried state of the visited branch: its parent's frame Gp and angles, its msq, decay
+  // momentum and mass
+  double Gp[16];
+  double ct0 = 1.0, st0 = 0.0, cp0 = 1.0, sp0 = 0.0;
+  double msq_b = s, pd_b = 0.0, m_b = sqrts;
+  double factor = 1.0;
+  int sp = 0;
+  const int n_visits = ch.n_visits;
+  for (int v = 0; v < n_visits; v++) {
+    const PhsVisit &V = ch.visit[v];
+    // the branch's frame G: CM momenta -> its rest frame, z along its flight (or friend)
+    // axis.  The root's is the identity; else L_r3_r2_b3(-bg, gamma, ct0, -st0, cp0, -sp0)
+    // times the parent's (phs.cu:1114-1125)
+    double G[16];
+    if (V.self_root) {
+#pragma unroll
+      for (int i = 0; i < 16; i++) G[i] = (i % 5 == 0) ? 1.0 : 0.0;
+    } else {
+      const double bg = m_b > 0.0 ? pd_b / m_b : 0.0;
+      const double ga = sqrt(1.0 + bg * bg);
+      const double t01 = -bg * st0 * cp0, t02 = -bg * st0 * sp0, t03 = -bg * ct0;
+      const double t11 = ct0 * cp0, t12 = ct0 * sp0;
+      const double t31 = ga * st0 * cp0, t32 = ga * st0 * sp0, t33 = ga * ct0;
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const double g0 = Gp[c], g1 = Gp[4 + c], g2 = Gp[8 + c], g3 = Gp[12 + c];
+        G[c] = ga * g0 + t01 * g1 + t02 * g2 + t03 * g3;
+        G[4 + c] = t11 * g1 + t12 * g2 + (-st0) * g3;
+        G[8 + c] = (-sp0) * g1 + cp0 * g2;
+        G[12 + c] = (-bg) * g0 + t31 * g1 + t32 * g2 + t33 * g3;
+      }
+      if (V.friend_sign != 0) {
+        // rotate the friend beam's direction G (1, 0, 0, ff) onto z (phs.cu:1183-1206);
+        // uniform per channel
+        const double ff = V.friend_sign;
+        double Rf[9];
+        rot_z_onto(G[4] + ff * G[7], G[8] + ff * G[11], G[12] + ff * G[15], Rf);
+        double Gn[12];
+#pragma unroll
+        for (int r = 0; r < 3; r++)
+#pragma unroll
+          for (int c = 0; c < 4; c++)
+            Gn[4 * r + c] = Rf[r] * G[4 + c] + Rf[3 + r] * G[8 + c] + Rf[6 + r] * G[12 + c];
+#pragma unroll
+        for (int i = 0; i < 12; i++) G[4 + i] = Gn[i];
+      }
+    }
+
+    // daughters' momenta and invariant masses
+    double q0[4], q1[4];
+#pragma unroll
+    for (int mu = 0; mu < 4; mu++) {
+      q0[mu] = pm[(4 * V.slot[0] + mu) * PHS_INV_BLOCK];
+      q1[mu] = pm[(4 * V.slot[1] + mu) * PHS_INV_BLOCK];
+    }
+    double cmsq[2];
+    cmsq[0] = q0[0] * q0[0] - q0[1] * q0[1] - q0[2] * q0[2] - q0[3] * q0[3];
+    cmsq[1] = q1[0] * q1[0] - q1[1] * q1[1] - q1[2] * q1[2] - q1[3] * q1[3];
+
+    // inverse msq maps of the internal daughters
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const PhsChild &C = V.child[j];
+      if (C.internal) {
+        double a0 = C.a0, a1 = C.a1, a2 = C.a2, mn = C.msq_min, mx = C.msq_max, mmax;
+        if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, a0, a1, a2, mn, mx, mmax);
+        double x, f;
+        map_msq_inverse(C.map_id, cmsq[j], s, C.m, C.w, mn, mx, a0, a1, a2, x, f);
+        xr[C.x_msq] = x;
+        factor *= f;
+      }
+    }
+
+    // Kallen function at the visited branch
+    const double d = msq_b - cmsq[0] - cmsq[1];
+    const double sl = sqrt(d * d - 4.0 * cmsq[0] * cmsq[1]);
+    const double pd = sl / (2.0 * m_b);
+    factor *= sl / msq_b;
+
+    // angles of daughter 1 in the branch's frame (azimuthal_angle, polar_angle_ct,
+    // phs.cu:913-922)
+    const double qx = G[4] * q0[0] + G[5] * q0[1] + G[6] * q0[2] + G[7] * q0[3];
+    const double qy = G[8] * q0[0] + G[9] * q0[1] + G[10] * q0[2] + G[11] * q0[3];
+    const double qz = G[12] * q0[0] + G[13] * q0[1] + G[14] * q0[2] + G[15] * q0[3];
+    double phi = atan2(qy, qx);
+    if (phi < 0.0) phi += 2.0 * PHS_PI;
+    xr[V.x_phi] = phi / (2.0 * PHS_PI);
+    const double ct = qz / sqrt(qx * qx + qy * qy + qz * qz);
+    const double st = sqrt(1.0 - ct * ct);
+    double b0 = V.b0, b1 = V.b1;
+    if (PER_EVENT && V.ct_class == PHS_CT_COLLINEAR) {
+      b0 = V.m * V.m / s;
+      b1 = log((b0 + 1.0) / b0);
+    }
+    {
+      double x, f;
+      map_ct_inverse(V.ct_class, ct, b0, b1, x, f);
+      xr[V.x_ct] = x;
+      factor *= f;
+    }
+    if (V.both_leaves) {
+      if (sp > 0) {
+        sp--;
+#pragma unroll
+        for (int i = 0; i < 16; i++) Gp[i] = inv_load(stk, sp, i);
+        ct0 = inv_load(stk, sp, 16);
+        st0 = inv_load(stk, sp, 17);
+        cp0 = inv_load(stk, sp, 18);
+        sp0 = inv_load(stk, sp, 19);
+        msq_b = inv_load(stk, sp, 20);
+        pd_b = inv_load(stk, sp, 21);
+        m_b = inv_load(stk, sp, 22);
+      }
+      continue;
+    }
+    double sph, cph;
+    sincos(phi, &sph, &cph);
+    if (V.push >= 0) {
+      const bool j0 = V.push == 0;
+#pragma unroll
+      for (int i = 0; i < 16; i++) inv_store(stk, sp, i, G[i]);
+      inv_store(stk, sp, 16, ct);
+      inv_store(stk, sp, 17, st);
+      inv_store(stk, sp, 18, cph);
+      inv_store(stk, sp, 19, sph);
+      const double mq = j0 ? cmsq[0] : cmsq[1];
+      inv_store(stk, sp, 20, mq);
+      inv_store(stk, sp, 21, j0 ? pd : -pd);
+      inv_store(stk, sp, 22, sqrt(mq));
+      sp++;
+    }
+    if (V.carry >= 0) {
+      const bool j0 = V.carry == 0;
+#pragma unroll
+      for (int i = 0; i < 16; i++) Gp[i] = G[i];
+      ct0 = ct;
+      st0 = st;
+      cp0 = cph;
+      sp0 = sph;
+      msq_b = j0 ? cmsq[0] : cmsq[1];
+      pd_b = j0 ? pd : -pd;
+      m_b = sqrt(msq_b);
+    }
+  }
+  return factor;
+}
+
+template <bool PER_EVENT>
+__global__ void __launch_bounds__(PHS_INV_BLOCK)
+    phs_inverse_kernel(const __grid_constant__ PhsInvLaunch a) {
+  extern __shared__ double sm[];
+  double *pm = sm;                                                  // [4 (2 n_out - 1)][block]
+  double *stk = sm + (size_t)4 * (2 * a.n_out - 1) * PHS_INV_BLOCK;  // frame stack
+  const int tid = threadIdx.x;
+  const int64_t n_tiles = (a.n_events + PHS_INV_BLOCK - 1) / PHS_INV_BLOCK;
+  const PhsChannel &ch0 = a.channels[0];
+
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const int64_t ev = tile * PHS_INV_BLOCK + tid;
+    if (ev >= a.n_events) continue;
+    // the generating channel: the last c with ch_begin[c] <= ev
+    int lo = 0, hi = a.n_channels - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (a.ch_begin[mid] <= ev) lo = mid; else hi = mid - 1;
+    }
+    const int own = lo;
+    const bool ok = a.ok ? a.ok[ev] != 0 : true;
+    double sqrts = ch0.sqrts, lab_bg = ch0.lab ? ch0.lab_bg : 0.0;
+    double lab_ga = ch0.lab ? ch0.lab_gamma : 1.0;
+    if (PER_EVENT) {
+      const double E1 = a.E1[ev], E2 = a.E2[ev], r = sqrt(E1 * E2);
+      sqrts = 2.0 * r;
+      lab_bg = (E1 - E2) / (2.0 * r);
+      lab_ga = sqrt(1.0 + lab_bg * lab_bg);
+    }
+    // this event's momenta, lab -> CM (the inverse of phs.cu:1286-1301)
+    const double2 *pe = reinterpret_cast<const double2 *>(a.p + ev * 4 * (int64_t)a.n_out);
+    for (int k = 0; k < a.n_out; k++) {
+      const double2 e_x = pe[2 * k], y_z = pe[2 * k + 1];
+      pm[(4 * k + 0) * PHS_INV_BLOCK + tid] = dsub(dmul(lab_ga, e_x.x), dmul(lab_bg, y_z.y));
+      pm[(4 * k + 1) * PHS_INV_BLOCK + tid] = e_x.y;
+      pm[(4 * k + 2) * PHS_INV_BLOCK + tid] = y_z.x;
+      pm[(4 * k + 3) * PHS_INV_BLOCK + tid] = dadd(dmul(-lab_bg, e_x.x), dmul(lab_ga, y_z.y));
+    }
+    const double *xo = a.x_own ? a.x_own + ev * a.n_x : nullptr;
+    for (int c = 0; c < a.n_channels; c++) {
+      double *xr = a.x_out + ((int64_t)c * a.n_events + ev) * a.n_x;
+      double *fo = a.all_factors + ev * a.n_channels + c;
+      const PhsChannel &ch = a.channels[c];
+      if (c == own && xo) {
+        // the generating channel keeps its own x and factor (_move_x/_move_factors)
+        for (int k = 0; k < a.n_x; k++) xr[k] = xo[k];
+        *fo = a.factor_own ? a.factor_own[ev] : 0.0;
+        continue;
+      }
+      for (int k = ch.n_x_used; k < a.n_x; k++) xr[k] = xo ? xo[k] : 0.0;
+      if (!ok) {
+        for (int k = 0; k < ch.n_x_used; k++) xr[k] = 0.0;
+        *fo = 0.0;
+        continue;
+      }
+      *fo = inverse_event<PER_EVENT>(ch, pm + tid, sqrts, xr, stk);
+    }
+  }
+}
+
+}  // namespace
+
+size_t phs_inverse_smem_bytes(int n_out, int stack_depth) {
+  return ((size_t)4 * (2 * n_out - 1) + (size_t)PHS_INV_STATE * stack_depth) * PHS_INV_BLOCK *
+         sizeof(double);
+}
+
+int phs_inverse_blocks_per_sm(int n_out, int stack_depth, bool per_event) {
+  int n = 0;
+  const size_t smem = phs_inverse_smem_bytes(n_out, stack_depth);
+  if (per_event)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phs_inverse_kernel<true>, PHS_INV_BLOCK, smem);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phs_inverse_kernel<false>, PHS_INV_BLOCK, smem);
+  return n > 0 ? n : 1;
+}
+
+cudaError_t phs_launch_inverse(const PhsInvLaunch &a, int n_blocks, cudaStream_t stream) {
+  if (a.n_events <= 0) return cudaSuccess;
+  const size_t smem = phs_inverse_smem_bytes(a.n_out, a.stack_depth);
+  const bool per_event = a.E1 && a.E2;
+  if (smem > 48 * 1024) {
+    cudaError_t e = per_event
+        ? cudaFuncSetAttribute(phs_inverse_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+        : cudaFuncSetAttribute(phs_inverse_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  if (per_event)
+    phs_inverse_kernel<true><<<n_blocks, PHS_INV_BLOCK, smem, stream>>>(a);
+  else
+    phs_inverse_kernel<false><<<n_blocks, PHS_INV_BLOCK, smem, stream>>>(a);
+  return cudaGetLastError();
+}

@@ -17,7 +17,7 @@
 namespace {
 
 template <bool PER_EVENT>
-__global__ void __launch_bounds__(PHS_FWD_BLOCK)
+__global__ void __launch_bounds__(PHS_FWD_BLOCK, 4)
     phs_forward_f64_kernel(const __grid_constant__ PhsLaunch a) {
   extern __shared__ double smem[];
   const int lane = threadIdx.x & 31;

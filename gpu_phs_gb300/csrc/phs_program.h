@@ -13,6 +13,9 @@
 //     child is pushed on a per-thread stack of depth <= PHS_STACK_DEPTH (the smaller
 //     subtree is carried first, so the depth is <= 2 for n_out <= 15).
 //
+// The inverse map (phs_inverse.cu) walks the same program: at each visit it recovers the
+// visited branch's angles and its children's msq x from the event's momenta.
+//
 // x indices are static: the reference consumes x in a fixed order (msq x's of the
 // non-root internal branches in post-order, then phi and cos(theta) per internal branch
 // in pre-order; phs_cpu.cpp:174-234, 283-345), so the visit order is free.
@@ -62,6 +65,10 @@ struct PhsVisit {
   double self_m_max;  // the visited branch's ok-test bound at the handle's sqrt(s)
   int32_t self_root;  // 1 for the root visit
   int32_t both_leaves;  // 1 when neither child is internal (only L columns 0,3 needed)
+  int32_t friend_sign;  // 0, or the beam (+1: along +z, -1: along -z) that the visited
+                        // branch's decay angles are measured from (phs.cu:853-910)
+  int8_t slot[2];       // inverse map: momentum slot of each child (see PhsChannel::comb)
+  int8_t pad1[2];
 };
 
 struct PhsChannel {
@@ -81,7 +88,11 @@ struct PhsChannel {
   // vol_child[i][j] >= 0 is the entry index of an internal child, -1 a leaf (volume 1).
   int8_t vol_child[PHS_MAX_VISITS][2];
   int8_t vol_is_root[PHS_MAX_VISITS];
-  int8_t pad[5];
+  // Momentum sums of the inverse map (_combine_particles, phs.cu:1262-1283): slots
+  // 0..n_out-1 hold the outgoing momenta, slot n_out + i the i-th internal branch in
+  // post-order (the volume program's order), = slot comb[i][0] + slot comb[i][1].
+  int8_t comb[PHS_MAX_VISITS][2];
+  int8_t pad[1];
 };
 
 // A contiguous run of events of one channel within a launch.
@@ -121,7 +132,7 @@ struct PhsVisitFF {
 
 struct PhsChannelFF {
   int32_t n_out, n_visits;
-  int32_t exact_only;  // 1: a mapping without a float-float form (STEP_E/STEP_H): FP64 path
+  int32_t exact_only;  // 1: STEP_E/STEP_H mappings or a friend boost: FP64 path
   int32_t lab;
   PhsFF sqrts, s, lab_bg, lab_gamma;
   double volume;

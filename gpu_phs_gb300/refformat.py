@@ -33,6 +33,28 @@ class RefEvents:
     all_factors: np.ndarray  # float64 [n, n_channels]
 
 
+def friends_from_trees(n_out: int, d1, d2, has_children, flags) -> np.ndarray:
+    """Friend table [n_trees, N_PRT] (Whizard code of the paired incoming particle, 0 =
+    none) from the trees of a .ref file, which store only a per-tree ``hasfriends`` flag.
+
+    In a flagged tree, a daughter k of the root is paired with the incoming particle
+    ``in`` (code 2^n_out or 2^(n_out+1)) when the tree lists the branch k|in: the
+    t-channel line that connects k to that beam.  This reproduces the momenta of
+    Whizard's own events in samples/bwbw.ref for all 16 flagged trees; unflagged trees
+    list such branches too but carry no friend."""
+    root = (1 << n_out) - 1
+    out = np.zeros_like(np.asarray(d1, np.int32))
+    for t in range(out.shape[0]):
+        if not flags[t]:
+            continue
+        for k in (int(d1[t][root - 1]), int(d2[t][root - 1])):
+            for inc in (1 << n_out, 1 << (n_out + 1)):
+                code = k | inc
+                if code <= out.shape[1] and has_children[t][code - 1]:
+                    out[t][k - 1] = inc
+    return out
+
+
 def _values(line: str, conv=float) -> List:
     parts = line.split()
     return [conv(v) for v in parts[1:]]
@@ -66,7 +88,8 @@ def read_ref(path: str):
     flv_m = np.array(_values(lines[pos])[: n_in + n_out])
     flv_w = np.array(_values(lines[pos + 1])[: n_in + n_out])
     pos += 2
-    proc = Process(n_in, n_out, d1, d2, hc, np.zeros_like(d1), mid, mm, mw, flv_m, flv_w,
+    fr = friends_from_trees(n_out, d1, d2, hc, friends_flag)
+    proc = Process(n_in, n_out, d1, d2, hc, fr, mid, mm, mw, flv_m, flv_w,
                    n_x=n_x, name=path.rsplit("/", 1)[-1], sqrts=0.0)
     n_lines = 5 + n_in + n_out
     body = [ln for ln in lines[pos:] if ln.strip()]

@@ -137,6 +137,24 @@ int phs_adjoint_device(phs_process_t proc, int64_t n_events, const int64_t *chan
                        const double *x, const double *pbar, const double *jbar, double *xbar,
                        double *thbar, void *stream);
 
+/* Inverse map on device pointers: for events grouped by generating channel
+ * (channel_counts), with lab momenta p [n_events][n_out][4] (16-byte aligned), writes for
+ * EVERY channel c the x row and factor that channel assigns to the same momenta:
+ *   all_factors [n_events][n_channels]        (factors[n_channels * i + c], phs.cu:1580-1583)
+ *   x_out       [n_channels][n_events][n_x]   (x_out[n_x * n_events * c + n_x * i + k], :1585)
+ * Replaces the do_inverse_mapping pass of gen_phs_from_x_gpu (phs.cu:1499-1554 with
+ * _apply_msq_inv 626-675, the boost inversion 924-1244 and mappings_gpu.hpp:15-219).
+ * E1/E2 (device, both or neither): per-event beams; NULL uses the handle's beams.  oks may
+ * be NULL (all events valid); events with ok = 0 get factor 0 and x 0 in the other channels.
+ * x_own [n_events][n_x] and factor_own [n_events] (may be NULL): the generating channel's
+ * row is copied from them, as the reference does (_move_x, _move_factors phs.cu:203-232);
+ * with x_own NULL it is inverted like the others.  x entries past 3 n_out - 4 are copied
+ * from x_own (0 without).  FP64. */
+int phs_inverse_device(phs_process_t proc, int64_t n_events, const int64_t *channel_counts,
+                       const double *E1, const double *E2, const double *p, const uint8_t *oks,
+                       const double *x_own, const double *factor_own, double *all_factors,
+                       double *x_out, void *stream);
+
 /* Host pointers in and out (pinned memory is fastest); copies run chunk-pipelined with the
  * kernel.  Synchronous. */
 int phs_generate_host(phs_process_t proc, int64_t n_events, const int64_t *channel_counts,

@@ -76,6 +76,12 @@ class Oracle:
                                           _pd, _pd, _pd, _pu8, C.c_int]
             L.oracle_generate_beams.argtypes = [C.c_void_p, C.c_long, C.c_int, _pd, C.c_void_p,
                                                 _pd, _pd, _pd, _pd, _pd, _pu8, C.c_int]
+            L.oracle_set_friends.restype = C.c_int
+            L.oracle_set_friends.argtypes = [C.c_void_p, _pi]
+            L.oracle_inverse.restype = C.c_int
+            L.oracle_inverse.argtypes = [C.c_void_p, C.c_long, C.c_int, _pd, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, _pd, _pd, C.c_int]
             cls._lib = L
         return cls._lib
 
@@ -87,6 +93,9 @@ class Oracle:
                                  np.ascontiguousarray(proc.flv_masses, np.float64))
         if not self.h:
             raise ValueError("oracle rejected the process tables")
+        fr = np.ascontiguousarray(proc.friends, np.int32)
+        if fr.any() and L.oracle_set_friends(self.h, fr) != 0:
+            raise ValueError("oracle rejected the friend table")
         L.oracle_set_sqrts(self.h, float(sqrts))
         self.sqrts = float(sqrts)
 
@@ -125,6 +134,38 @@ class Oracle:
             self.lib().oracle_generate_beams(self.h, n, n_x, x.reshape(-1), chp, E1, E2,
                                              r.p.reshape(-1), r.factor, r.volume, r.ok, threads)
         return r
+
+    def inverse(self, p: np.ndarray, channels: Optional[np.ndarray] = None,
+                ok: Optional[np.ndarray] = None, x_own: Optional[np.ndarray] = None,
+                factor_own: Optional[np.ndarray] = None, n_x: Optional[int] = None,
+                E1: Optional[np.ndarray] = None, E2: Optional[np.ndarray] = None,
+                threads: int = 0):
+        """All-channel factors [n, n_channels] and x [n_channels, n, n_x] of events with
+        lab momenta p [n, n_out, 4] (phs.cu:1499-1554).  With x_own/factor_own the
+        generating channel's row is copied, otherwise inverted like the others."""
+        p = np.ascontiguousarray(p, np.float64)
+        n = p.shape[0]
+        n_x = n_x or (x_own.shape[1] if x_own is not None else self.proc.n_x)
+        keep = []
+
+        def vp(a, dt):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dt)
+            keep.append(a)
+            return a.ctypes.data_as(C.c_void_p)
+
+        if E1 is not None:
+            E1 = np.broadcast_to(E1, (n,))
+            E2 = np.broadcast_to(E2, (n,))
+        fac = np.zeros((n, self.proc.n_channels))
+        xo = np.zeros((self.proc.n_channels, n, n_x))
+        threads = threads or os.cpu_count() or 1
+        self.lib().oracle_inverse(self.h, n, n_x, p.reshape(-1), vp(channels, np.int32),
+                                  vp(ok, np.uint8), vp(E1, np.float64), vp(E2, np.float64),
+                                  vp(x_own, np.float64), vp(factor_own, np.float64),
+                                  fac.reshape(-1), xo.reshape(-1), threads)
+        return fac, xo
 
 
 def ref_available() -> bool:

@@ -20,6 +20,24 @@
  *   mass sums               phs.cu:61-78
  *   lab-frame boost         phs.cu:1286-1301 (the CPU path has none; used only
  *                           when the two beam energies differ)
+ *   friend (beam-axis) boost  phs.cu:853-910 (GPU only; restated exactly, below)
+ *   inverse mapping         phs.cu:626-675 (_apply_msq_inv), 924-1244 (boost
+ *                           inversion), 1262-1283 (_combine_particles), inverse
+ *                           maps mappings_gpu.hpp:15-219 (GPU only)
+ *
+ * Friend boosts and the inverse have no CPU implementation in the reference; they are
+ * pinned against Whizard's own golden events (samples/bwbw.ref momenta and
+ * all_factors).  Where the reference's GPU formulas are not the exact Lorentz
+ * algebra, this file uses the exact algebra, which is what the golden events follow:
+ *   - friend axis: the reference's z component carries -bg*L0[3][0]*pf where the
+ *     inverse boost gives +bg*L0[3][0]*pf (phs.cu:890); equal when L0 has no boost;
+ *   - rotation onto the axis: L_rot_to_2nd (phs.cu:753-781) flips the sign of the
+ *     (y,z) and (z,y) elements of the Rodrigues rotation; equal when the axis has no
+ *     y component;
+ *   - inverse with a friend: the branch's frame is stored as L0*L_friend
+ *     (phs.cu:1237-1244) where the chain needs L_friend*L0; equal when the branch
+ *     has no internal daughter.
+ * Whizard trees carry friends only on the root's daughters, where all three agree.
  *
  * Differences from the reference, all on events the reference leaves undefined:
  *   - ok=false events get momenta 0 and factor 0 (the reference CPU returns
@@ -58,6 +76,7 @@ typedef struct {
   double *m, *w, *mass_sum;
   double *a, *b;          /* [(c*stride + code)*3 + i] */
   double *flv_masses;     /* n_in + n_out */
+  int *friend_sign;       /* [c*stride + code]: 0, or the beam direction +-1 of a friend */
   double sqrts;           /* sqrts the constants were computed for */
 } oracle_t;
 
@@ -247,6 +266,25 @@ typedef struct {
   int ok;
 } ev_t;
 
+/* Rotation taking the z axis onto the direction of (bx, by, bz) about the axis z x b
+ * (Rodrigues), as a 3x3 matrix, with the symmetric part cos + (1 - cos) k k^T formed from
+ * the transverse components as L_rot_to_2nd (phs.cu:753-781) does (stable as the axis
+ * nears -z).  An axis exactly along -z gives the rotation by pi about x. */
+static void rot_z_onto(double bx, double by, double bz, double R[3][3]) {
+  double n = sqrt(bx * bx + by * by + bz * bz);
+  bx /= n; by /= n; bz /= n;
+  double t = bx * bx + by * by, r00 = 1, r01 = 0, r11 = bz;
+  if (t > 0) {
+    double w = (1 - bz) / t;
+    r00 = bz + w * (by * by);
+    r01 = -w * (bx * by);
+    r11 = bz + w * (bx * bx);
+  }
+  R[0][0] = r00; R[0][1] = r01; R[0][2] = bx;
+  R[1][0] = r01; R[1][1] = r11; R[1][2] = by;
+  R[2][0] = -bx; R[2][1] = -by; R[2][2] = bz;
+}
+
 /* phs_cpu.cpp:174-234 */
 static void set_msq(ev_t *e, int code, double *factor, double *volume) {
   const oracle_t *o = e->o;
@@ -316,6 +354,28 @@ static void set_angles(ev_t *e, int code, double *factor, double L0[4][4]) {
       {0, ct * cp, -sp, st * cp},
       {0, ct * sp, cp, st * sp},
       {bg, -gamma * st, 0, gamma * ct}};
+  int ff = o->friend_sign ? o->friend_sign[i] : 0;
+  if (ff) {
+    /* phs.cu:853-910: the decay angles are measured from the friend beam's direction in
+     * the branch's rest frame, B_z(-bg) L0^-1 (1, 0, 0, ff) (only its direction matters) */
+    double u0 = L0[0][0] - ff * L0[3][0];
+    double ax = -(L0[0][1] - ff * L0[3][1]);
+    double ay = -(L0[0][2] - ff * L0[3][2]);
+    double az = -bg * u0 - gamma * (L0[0][3] - ff * L0[3][3]);
+    double Rf[3][3], Q[3][3];
+    double A[3][3] = {{ct * cp, -sp, st * cp}, {ct * sp, cp, st * sp}, {-st, 0, ct}};
+    rot_z_onto(ax, ay, az, Rf);
+    for (int r = 0; r < 3; r++)
+      for (int s = 0; s < 3; s++) Q[r][s] = Rf[r][0] * A[0][s] + Rf[r][1] * A[1][s] + Rf[r][2] * A[2][s];
+    /* L1 = B_z(bg) diag(1, Q) */
+    L1[0][0] = gamma; L1[1][0] = 0; L1[2][0] = 0; L1[3][0] = bg;
+    for (int s = 0; s < 3; s++) {
+      L1[0][s + 1] = bg * Q[2][s];
+      L1[1][s + 1] = Q[0][s];
+      L1[2][s + 1] = Q[1][s];
+      L1[3][s + 1] = gamma * Q[2][s];
+    }
+  }
   double Ln[4][4];
   memset(Ln, 0, sizeof Ln);
   for (int r = 0; r < 4; r++)
@@ -340,6 +400,7 @@ void oracle_destroy(oracle_t *o) {
   if (!o) return;
   free(o->k1); free(o->k2); free(o->has_ch); free(o->map_id);
   free(o->m); free(o->w); free(o->mass_sum); free(o->a); free(o->b); free(o->flv_masses);
+  free(o->friend_sign);
   free(o);
 }
 
@@ -524,4 +585,318 @@ int oracle_generate_beams(const oracle_t *o, long n_events, int n_x, const doubl
                           double *factors, double *volumes, unsigned char *oks, int n_threads) {
   job_t j = {o, 0, 0, n_x, x, channels, E1, E2, p, factors, volumes, oks};
   return run_threads(&j, n_events, n_threads);
+}
+
+/* friends: [n_channels][2^(n_in+n_out)-1] by code-1, the Whizard code of the incoming
+ * particle a branch is paired with (0 = none), as c_whizard_fill_tree_structure takes it
+ * (whizard_gpu_phs.cpp:79-87).  As extract_boost_origins (phs.cu:268-292) reads it, code
+ * 2^n_out selects the beam along -z and 2^(n_out+1) the beam along +z; other values and
+ * leaves are ignored.  A friend on the root is rejected (-1): the reference divides by
+ * zero there (phs.cu:753-765 with both axes along z). */
+int oracle_set_friends(oracle_t *o, const int *friends) {
+  int n_prt = (1 << (o->n_in + o->n_out)) - 1;
+  size_t nt = (size_t)o->n_channels * o->stride;
+  if (!o->friend_sign) o->friend_sign = calloc(nt, sizeof(int));
+  for (int c = 0; c < o->n_channels; c++)
+    for (int code = 1; code <= o->n_codes; code++) {
+      int i = c * o->stride + code, f = friends[c * n_prt + code - 1];
+      int sgn = f == (1 << o->n_out) ? -1 : f == (1 << (o->n_out + 1)) ? 1 : 0;
+      if (!o->has_ch[i]) sgn = 0;
+      if (sgn && code == o->n_codes) return -1;
+      o->friend_sign[i] = sgn;
+    }
+  return 0;
+}
+
+/* ---------------------------------------------------------------------------------- */
+/* Inverse mapping: momenta -> (x, factor) of a channel.                                */
+
+/* mappings_gpu.hpp:15-172 (mapping_x_from_msq_*), with the constants of
+ * init_mapping_constants_cpu. */
+static void msq_to_x(int t, double msq, double s, double m, double w, double msq_min,
+                     double msq_max, const double *a, double *x, double *factor) {
+  double z, z1, z2, z3;
+  switch (t) {
+    case OR_MAP_NO:
+      *x = (msq - msq_min) / (msq_max - msq_min);
+      *factor = (msq_max - msq_min) / s;
+      break;
+    case OR_MAP_SCHANNEL:
+      z = (msq - m * m) / (m * w);
+      *x = (atan(z) - a[0]) / (a[1] - a[0]);
+      *factor = a[2] * (1 + z * z);
+      break;
+    case OR_MAP_COLLINEAR:
+    case OR_MAP_INFRARED:
+    case OR_MAP_RADIATION:
+      z = msq - msq_min + a[0];
+      *x = log(z / a[0]) / a[1];
+      *factor = a[2] * z;
+      break;
+    case OR_MAP_TCHANNEL:
+    case OR_MAP_UCHANNEL:
+      if (msq < (msq_max + msq_min) / 2) {
+        z = msq - msq_min + a[0];
+        *x = log(z / a[0]) / a[1];
+      } else {
+        z = msq_max - msq + a[0];
+        *x = 1 - log(z / a[0]) / a[1];
+      }
+      *factor = a[2] * z;
+      break;
+    case OR_MAP_STEP_E:
+      z1 = (msq - msq_min) / (msq_max - msq_min);
+      z2 = 1 + a[1] * exp(z1 / a[2]);
+      *x = (z1 - a[2] * log(z2 / (1 + a[1]))) / a[0];
+      *factor = a[0] * z2 * (msq_max - msq_min) / s;
+      break;
+    case OR_MAP_STEP_H:
+      z1 = (msq - msq_min) / (msq_max - msq_min);
+      z3 = a[0] - z1 / a[2];
+      *x = ((a[0] + z1 / a[2] + z1) - sqrt(z3 * z3 + 2 * z1 * (a[0] + z1 / a[2]) + z1 * z1)) / 2;
+      *factor = (a[1] / (a[0] - *x) / (a[0] - *x) + a[2]) * (msq_max - msq_min) / s;
+      break;
+    default:
+      *x = 0;
+      *factor = 0;
+  }
+}
+
+/* mappings_gpu.hpp:184-219 (mapping_x_from_ct_*) */
+static void ct_to_x(int t, double ct, const double *b, double *x, double *factor) {
+  double ct1;
+  switch (t) {
+    case OR_MAP_COLLINEAR:
+    case OR_MAP_TCHANNEL:
+    case OR_MAP_UCHANNEL:
+      if (ct < 0) {
+        ct1 = ct + b[0] + 1;
+        *x = log(ct1 / b[0]) / (2 * b[1]);
+      } else {
+        ct1 = -ct + b[0] + 1;
+        *x = 1 - log(ct1 / b[0]) / (2 * b[1]);
+      }
+      *factor = ct1 * b[1];
+      break;
+    default:
+      *x = (ct + 1) / 2;
+      *factor = 1;
+  }
+}
+
+typedef struct {
+  const oracle_t *o;
+  int c;
+  const double *a, *b;
+  double sqrts;
+  double *x;            /* output row */
+  int id_x;
+  double *msq, *pd;     /* [code] */
+  double (*p)[4];       /* [code][4], CM frame */
+  double factor;
+} inv_t;
+
+static void matvec4(const double M[4][4], const double v[4], double out[4]) {
+  for (int r = 0; r < 4; r++) {
+    out[r] = 0;
+    for (int k = 0; k < 4; k++) out[r] += M[r][k] * v[k];
+  }
+}
+
+/* _combine_particles (phs.cu:1262-1283): internal momenta as sums of their daughters in
+ * post-order, and msq of every branch from its momentum. */
+static void inv_combine(inv_t *e, int code) {
+  const oracle_t *o = e->o;
+  int i = e->c * o->stride + code;
+  if (o->has_ch[i]) {
+    int k1 = o->k1[i], k2 = o->k2[i];
+    inv_combine(e, k1);
+    inv_combine(e, k2);
+    for (int r = 0; r < 4; r++) e->p[code][r] = e->p[k1][r] + e->p[k2][r];
+  }
+  double *q = e->p[code];
+  e->msq[code] = q[0] * q[0] - q[1] * q[1] - q[2] * q[2] - q[3] * q[3];
+}
+
+/* _apply_msq_inv (phs.cu:626-675): post-order; returns the subtree's factor. */
+static double inv_msq(inv_t *e, int code) {
+  const oracle_t *o = e->o;
+  int i = e->c * o->stride + code;
+  int k1 = o->k1[i], k2 = o->k2[i];
+  double f1 = o->has_ch[e->c * o->stride + k1] ? inv_msq(e, k1) : 1;
+  double f2 = o->has_ch[e->c * o->stride + k2] ? inv_msq(e, k2) : 1;
+  double f;
+  if (code == o->n_codes) {
+    e->msq[code] = e->sqrts * e->sqrts;
+    f = f1 * f2;
+  } else {
+    double m_tot = o->mass_sum[e->c * o->stride + o->n_codes];
+    double m_min = o->mass_sum[i], m_max = e->sqrts - m_tot + m_min;
+    msq_to_x(o->map_id[i], e->msq[code], e->sqrts * e->sqrts, o->m[i], o->w[i], m_min * m_min,
+             m_max * m_max, e->a + 3 * code, &e->x[e->id_x], &f);
+    e->id_x++;
+    f *= f1 * f2;
+  }
+  double msq0 = e->msq[code], msq1 = e->msq[k1], msq2 = e->msq[k2];
+  double m0 = sqrt(msq0);
+  double lda = (msq0 - msq1 - msq2) * (msq0 - msq1 - msq2) - 4 * msq1 * msq2;
+  e->pd[k1] = sqrt(lda) / (2 * m0);
+  e->pd[k2] = -sqrt(lda) / (2 * m0);
+  return f * (sqrt(lda) / msq0);
+}
+
+/* The boost inversion (phs.cu:924-1244), pre-order.  G takes CM momenta into the
+ * branch's rest frame with z along the branch's flight direction (or its friend axis). */
+static void inv_angles(inv_t *e, int code, double G[4][4]) {
+  const oracle_t *o = e->o;
+  int i = e->c * o->stride + code;
+  int k1 = o->k1[i], k2 = o->k2[i];
+  double q[4];
+  matvec4((const double(*)[4])G, e->p[k1], q);
+  /* azimuthal_angle, polar_angle_ct (phs.cu:913-922) */
+  double phi = atan2(q[2], q[1]);
+  if (phi < 0) phi += OR_TWOPI;
+  e->x[e->id_x++] = phi / OR_TWOPI;
+  double dn = sqrt(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  double ct = q[3] / dn, st = sqrt(1 - ct * ct), f;
+  ct_to_x(o->map_id[i], ct, e->b + 3 * code, &e->x[e->id_x++], &f);
+  e->factor *= f;
+  double cp = cos(phi), sp = sin(phi);
+  int kids[2] = {k1, k2};
+  for (int j = 0; j < 2; j++) {
+    int kc = kids[j], ki = e->c * o->stride + kc;
+    if (!o->has_ch[ki]) continue;
+    double m = sqrt(e->msq[kc]);
+    double bg = m > 0 ? e->pd[kc] / m : 0;
+    double gamma = sqrt(1 + bg * bg);
+    /* L_r3_r2_b3(-bg, gamma, ct, -st, cp, -sp) = B_z(-bg) R_y(-theta) R_z(-phi) */
+    double T[4][4] = {
+        {gamma, -bg * st * cp, -bg * st * sp, -bg * ct},
+        {0, ct * cp, ct * sp, -st},
+        {0, -sp, cp, 0},
+        {-bg, gamma * st * cp, gamma * st * sp, gamma * ct}};
+    double H[4][4];
+    for (int r = 0; r < 4; r++)
+      for (int s = 0; s < 4; s++) {
+        H[r][s] = 0;
+        for (int k = 0; k < 4; k++) H[r][s] += T[r][k] * G[k][s];
+      }
+    int ff = o->friend_sign ? o->friend_sign[ki] : 0;
+    if (ff) {
+      /* rotate the friend beam's direction H (1, 0, 0, ff) onto z (phs.cu:1183-1206) */
+      double Rf[3][3], Hn[4][4];
+      rot_z_onto(H[1][0] + ff * H[1][3], H[2][0] + ff * H[2][3], H[3][0] + ff * H[3][3], Rf);
+      for (int s = 0; s < 4; s++) {
+        Hn[0][s] = H[0][s];
+        for (int r = 0; r < 3; r++)
+          Hn[r + 1][s] = Rf[0][r] * H[1][s] + Rf[1][r] * H[2][s] + Rf[2][r] * H[3][s];
+      }
+      memcpy(H, Hn, sizeof H);
+    }
+    inv_angles(e, kc, H);
+  }
+}
+
+typedef struct {
+  const oracle_t *o;
+  long lo, hi;
+  int n_x;
+  const double *p;
+  const int *channels;
+  const unsigned char *oks;
+  const double *E1, *E2;
+  const double *x_own, *factor_own;
+  double *all_factors, *x_out;
+  long n_events;
+} inv_job_t;
+
+static void *run_inv_job(void *arg) {
+  inv_job_t *j = (inv_job_t *)arg;
+  const oracle_t *o = j->o;
+  int nc = o->n_codes, n_ch = o->n_channels;
+  double *msq = malloc((nc + 1) * sizeof(double)), *pd = malloc((nc + 1) * sizeof(double));
+  double(*pp)[4] = malloc((nc + 1) * sizeof(double[4]));
+  double *a_ev = malloc((size_t)o->stride * 3 * sizeof(double));
+  double *b_ev = malloc((size_t)o->stride * 3 * sizeof(double));
+  for (long ev = j->lo; ev < j->hi; ev++) {
+    int own = j->channels ? j->channels[ev] : 0;
+    int ok = j->oks ? j->oks[ev] != 0 : 1;
+    double sqrts = o->sqrts, bg_lab = 0, ga_lab = 1;
+    if (j->E1) {
+      double E1 = j->E1[ev], E2 = j->E2[ev];
+      sqrts = 2 * sqrt(E1 * E2);
+      bg_lab = (E1 - E2) / (2 * sqrt(E1 * E2));
+      ga_lab = sqrt(1 + bg_lab * bg_lab);
+    }
+    for (int c = 0; c < n_ch; c++) {
+      double *xr = j->x_out + ((size_t)c * j->n_events + ev) * j->n_x;
+      double *fo = j->all_factors + (size_t)ev * n_ch + c;
+      if (c == own && j->x_own) {
+        memcpy(xr, j->x_own + (size_t)ev * j->n_x, j->n_x * sizeof(double));
+        *fo = j->factor_own ? j->factor_own[ev] : 0;
+        continue;
+      }
+      if (j->x_own) memcpy(xr, j->x_own + (size_t)ev * j->n_x, j->n_x * sizeof(double));
+      else memset(xr, 0, j->n_x * sizeof(double));
+      if (!ok) {
+        memset(xr, 0, (size_t)(3 * o->n_out - 4) * sizeof(double));
+        *fo = 0;
+        continue;
+      }
+      inv_t e;
+      e.o = o; e.c = c; e.sqrts = sqrts; e.x = xr; e.id_x = 0;
+      e.msq = msq; e.pd = pd; e.p = pp; e.factor = 1;
+      if (j->E1) {
+        constants_for(o, c, sqrts, a_ev, b_ev);
+        e.a = a_ev; e.b = b_ev;
+      } else {
+        e.a = o->a + (size_t)c * o->stride * 3;
+        e.b = o->b + (size_t)c * o->stride * 3;
+      }
+      memset(pd, 0, (nc + 1) * sizeof(double));
+      for (int k = 0; k < o->n_out; k++) {
+        const double *q = j->p + ((size_t)ev * o->n_out + k) * 4;
+        double *t = pp[1 << k];
+        t[0] = ga_lab * q[0] - bg_lab * q[3];  /* lab -> CM (phs.cu:1286-1301 inverted) */
+        t[1] = q[1];
+        t[2] = q[2];
+        t[3] = -bg_lab * q[0] + ga_lab * q[3];
+      }
+      inv_combine(&e, nc);
+      double fmsq = inv_msq(&e, nc);
+      double G[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
+      inv_angles(&e, nc, G);
+      *fo = fmsq * e.factor;
+    }
+  }
+  free(msq); free(pd); free(pp); free(a_ev); free(b_ev);
+  return NULL;
+}
+
+/* All-channel factors and x of generated events (gen_phs_from_x_gpu with
+ * do_inverse_mapping, phs.cu:1499-1554).  p: [n][n_out][4] lab momenta; channels: the
+ * generating channel per event (NULL: 0); oks (NULL: all 1); E1/E2 per event (NULL:
+ * uniform beams at the oracle's sqrts).  Outputs all_factors [n][n_channels] and
+ * x_out [n_channels][n][n_x].  For the generating channel the row is x_own and the
+ * factor factor_own (copies, as the reference's _move_x/_move_factors) when x_own is
+ * given, else the inverse itself.  Events with ok = 0 get factor 0 and x 0 for the
+ * other channels. */
+int oracle_inverse(const oracle_t *o, long n_events, int n_x, const double *p,
+                   const int *channels, const unsigned char *oks, const double *E1,
+                   const double *E2, const double *x_own, const double *factor_own,
+                   double *all_factors, double *x_out, int n_threads) {
+  if (n_threads < 1) n_threads = 1;
+  if (n_threads > 512) n_threads = 512;
+  if (n_events < n_threads) n_threads = n_events > 0 ? (int)n_events : 1;
+  pthread_t th[512];
+  inv_job_t jobs[512];
+  for (int t = 0; t < n_threads; t++) {
+    inv_job_t jb = {o, n_events * t / n_threads, n_events * (t + 1) / n_threads, n_x, p,
+                    channels, oks, E1, E2, x_own, factor_own, all_factors, x_out, n_events};
+    jobs[t] = jb;
+  }
+  for (int t = 1; t < n_threads; t++) pthread_create(&th[t], NULL, run_inv_job, &jobs[t]);
+  run_inv_job(&jobs[0]);
+  for (int t = 1; t < n_threads; t++) pthread_join(th[t], NULL);
+  return 0;
 }

@@ -5,9 +5,12 @@ Two kinds of fixture, each a compressed .npz:
 
 * ``whizard_<name>.npz`` -- a subset of the reference's own Whizard sample files
   (samples/ttH.ref, samples/bwbw.ref): the process tables, the per-channel
-  ``hasfriends`` flag, and per event the channel, x (9 printed decimals), the
-  outgoing momenta, volume, ok and the event's own-channel factor (4 printed
-  digits).  These are the golden vectors the reference's test.sh checks against.
+  ``hasfriends`` flag with the friend table derived from it
+  (gpu_phs_gb300.refformat.friends_from_trees), and per event the channel, x (9
+  printed decimals), the outgoing momenta, volume, ok, the event's own-channel
+  factor and the factors of all channels (``all_factors``, Whizard's inverse
+  mapping; printed to a fixed number of decimals).  These are the golden vectors the
+  reference's test.sh checks against.
 * ``refcpu_<name>.npz`` -- outputs of the reference's own phs_cpu.cpp (compiled
   from the reference sources by ``make -C oracle ref``) on seeded Philox x for
   the benchmark processes: the process tables, the Philox seed, sqrt(s) and the
@@ -57,7 +60,7 @@ def whizard_fixture(name: str, per_channel: int) -> None:
         "hasfriends": friends_flag,
         "channel": ev.channel[keep], "x": ev.x[keep], "p_out": ev.p_out[keep],
         "p_in": ev.p_in[keep], "volume": ev.volume[keep], "ok": ev.ok[keep],
-        "factor": own[keep],
+        "factor": own[keep], "all_factors": ev.all_factors[keep],
     }
     path = os.path.join(HERE, f"whizard_{name}.npz")
     np.savez_compressed(path, **out)

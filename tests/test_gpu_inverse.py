@@ -1,0 +1,252 @@
+"""Parity of the CUDA inverse map (phs_inverse_device) with the oracle's inverse and with
+Whizard's all_factors, its round trip through the forward map, and the Whizard ABI's
+all-channel outputs.
+
+Bar (FP64).  The kernel keeps the oracle's (the reference's) operation order and is
+compiled without contraction, so the two differ only through the ulps of the
+transcendental functions (CUDA's vs glibc's atan2, sin, cos, log, atan).  The reference's
+algorithm amplifies such ulps on some elements: near the poles of a decay (1 - cos(theta)
+cancels in the collinear map), for light combinations (msq = E^2 - |p|^2 cancels), and
+through boosts of rounded rotations (a one-ulp change of one sin(phi) in the reference's
+own arithmetic moves a factor by 6e-11 on one of these events).  So:
+  * element-wise: |d factor| <= 1e-9 |factor| and |d x| <= 1e-9, each plus 64 times the
+    oracle's own change under one-ulp perturbations of its input momenta;
+  * in distribution: median relative factor difference below 1e-14, 99th percentile
+    below 1e-12;
+  * against the truth: on the generating channel (whose x and factor are known), the GPU's
+    round-trip error is at most that of the oracle (x4, plus 1e-15)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import counts_of, golden, load_process
+from gpu_phs_gb300 import processes as P
+from gpu_phs_gb300.philox import uniform_x
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def assert_inverse_parity(o, fac, xo, p, ch, ok, x_own=None, factor_own=None, E1=None, E2=None):
+    """GPU (fac, xo) against the oracle's inverse of the same momenta p."""
+    kw = dict(x_own=x_own, factor_own=factor_own, n_x=xo.shape[2], E1=E1, E2=E2)
+    rf, rx = o.inverse(p, ch, ok, **kw)
+    rng = np.random.default_rng(1)
+    sf = np.zeros_like(rf)
+    sx = np.zeros_like(rx)
+    for _ in range(2):
+        pp = p * (1 + rng.choice([-1.0, 1.0], p.shape) * 2.0 ** -52)
+        pf, px = o.inverse(pp, ch, ok, **kw)
+        sf = np.maximum(sf, np.abs(pf - rf))
+        sx = np.maximum(sx, np.abs(px - rx))
+    df = np.abs(fac - rf)
+    dx = np.abs(xo - rx)
+    bf = 1e-9 * np.abs(rf) + 64 * sf
+    bx = 1e-9 + 64 * sx
+    assert np.all(df <= bf), f"factor: {np.max(df / (bf + 1e-300)):.3g} x the bound"
+    assert np.all(dx <= bx), f"x: {np.max(dx / bx):.3g} x the bound"
+    live = np.broadcast_to(np.asarray(ok, bool)[:, None], fac.shape) & (rf != 0)
+    rel = (df / np.maximum(np.abs(rf), 1e-300))[live]
+    assert np.median(rel) < 1e-14 and np.quantile(rel, 0.99) < 1e-12
+    return rf, rx
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def gpu_forward_inverse(torch, proc, x, counts, E=(500.0, 500.0), own=True, Eev=None):
+    from gpu_phs_gb300.api import PhaseSpace
+    ps = PhaseSpace(proc, *E)
+    xd = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    if Eev is None:
+        ev = ps.generate(xd, counts)
+        E1 = E2 = None
+    else:
+        E1 = torch.from_numpy(Eev[0]).cuda()
+        E2 = torch.from_numpy(Eev[1]).cuda()
+        ev = ps.generate_beams(xd, E1, E2, counts)
+    fac, xo = ps.inverse(ev.p, counts, ev.ok, xd if own else None, ev.factor if own else None,
+                         E1, E2)
+    torch.cuda.synchronize()
+    return (ev.p.cpu().numpy(), ev.factor.cpu().numpy(), ev.ok.cpu().numpy(),
+            fac.cpu().numpy(), xo.cpu().numpy())
+
+
+@pytest.mark.parametrize("name", ["ttH", "bwbw"])
+def test_inverse_vs_oracle_and_whizard(torch, name):
+    z = golden(f"whizard_{name}")
+    proc = load_process(z)
+    counts = counts_of(z["channel"], proc.n_channels)
+    p, f, ok, fac, xo = gpu_forward_inverse(torch, proc, z["x"], counts)
+    o = oracle.Oracle(proc, 1000.0)
+    assert_inverse_parity(o, fac, xo, p, z["channel"], ok, x_own=z["x"], factor_own=f)
+    n = len(z["channel"])
+    assert np.array_equal(xo[z["channel"], np.arange(n)], z["x"])
+    g = z["all_factors"]
+    dec = 4 if name == "ttH" else 7
+    assert np.all(np.abs(fac - g) <= 0.5 * 10.0 ** -dec + 2e-3 * np.abs(g))
+
+
+@pytest.mark.parametrize("builder", [P.ww, P.tt, P.precision])
+def test_round_trip(torch, builder):
+    proc = builder()
+    n = 100_003
+    x = uniform_x(404, n, proc.n_x)
+    p, f, ok, fac, xo = gpu_forward_inverse(torch, proc, x, None, E=(proc.sqrts / 2,) * 2,
+                                            own=False)
+    okb = ok == 1
+    nu = 3 * proc.n_out - 4
+    dx = np.abs(xo[0][okb, :nu] - x[okb, :nu])
+    assert np.median(dx) < 1e-13 and dx.max() < 1e-6
+    rel = np.abs(fac[okb, 0] / f[okb] - 1)
+    assert np.median(rel) < 1e-11 and rel.max() < 1e-5
+    assert np.all(fac[~okb] == 0) and np.all(xo[0][~okb, :nu] == 0)
+    # against the oracle's inverse of the same momenta
+    sl = slice(0, 20000)
+    assert_inverse_parity(oracle.Oracle(proc, proc.sqrts), fac[sl], xo[:, sl], p[sl], None,
+                          ok[sl])
+
+
+@pytest.mark.parametrize("builder", [P.tt, P.precision])
+def test_round_trip_at_least_as_accurate_as_oracle(torch, builder):
+    """Against the known truth (the generating channel's x and forward factor): the GPU's
+    inverse errs no more than the oracle's."""
+    proc = builder()
+    n = 50_000
+    x = uniform_x(505, n, proc.n_x)
+    p, f, ok, fac, xo = gpu_forward_inverse(torch, proc, x, None, E=(proc.sqrts / 2,) * 2,
+                                            own=False)
+    okb = ok == 1
+    nu = 3 * proc.n_out - 4
+    rf, rx = oracle.Oracle(proc, proc.sqrts).inverse(p, None, ok, n_x=proc.n_x)
+    err_gpu = np.abs(xo[0][okb, :nu] - x[okb, :nu])
+    err_ora = np.abs(rx[0][okb, :nu] - x[okb, :nu])
+    assert err_gpu.max() <= 4 * err_ora.max() + 1e-15
+    assert np.quantile(err_gpu, 0.999) <= 4 * np.quantile(err_ora, 0.999) + 1e-15
+    ferr_gpu = np.abs(fac[okb, 0] / f[okb] - 1)
+    ferr_ora = np.abs(rf[okb, 0] / f[okb] - 1)
+    assert ferr_gpu.max() <= 4 * ferr_ora.max() + 1e-15
+    assert np.quantile(ferr_gpu, 0.999) <= 4 * np.quantile(ferr_ora, 0.999) + 1e-15
+
+
+def test_round_trip_random_trees_and_lab_frame(torch):
+    rng = np.random.default_rng(12)
+    for n_out in range(3, 9):
+        proc = P.random_process(rng, n_out, 5, 1000.0, name=f"inv{n_out}")
+        n = 20000
+        counts = np.full(proc.n_channels, n // proc.n_channels, np.int64)
+        counts[0] += n - counts.sum()
+        x = uniform_x(50 + n_out, n, proc.n_x)
+        E1 = np.full(n, 600.0)
+        E2 = np.linspace(300.0, 700.0, n)
+        p, f, ok, fac, xo = gpu_forward_inverse(torch, proc, x, counts, own=False, Eev=(E1, E2))
+        ch = np.repeat(np.arange(proc.n_channels), counts)
+        okb = ok == 1
+        nu = 3 * n_out - 4
+        own = xo[ch, np.arange(n)]
+        assert np.median(np.abs(own[okb, :nu] - x[okb, :nu])) < 1e-12
+        ownf = fac[np.arange(n), ch]
+        assert np.median(np.abs(ownf[okb] / f[okb] - 1)) < 1e-11
+        assert_inverse_parity(oracle.Oracle(proc, 1000.0), fac, xo, p, ch.astype(np.int32), ok,
+                              E1=E1, E2=E2)
+
+
+def test_full_size_bwbw(torch):
+    """2^21 events over the 61 bwbw channels (1.28e8 channel inversions): the generating
+    channel's round trip for every event and the oracle on a slice."""
+    from gpu_phs_gb300.api import PhaseSpace, philox_x
+    z = golden("whizard_bwbw")
+    proc = load_process(z)
+    n = 1 << 21
+    counts = np.full(proc.n_channels, n // proc.n_channels, np.int64)
+    counts[: n - counts.sum()] += 1
+    ps = PhaseSpace(proc, 500.0, 500.0)
+    x = philox_x(n, proc.n_x, seed=77)
+    ev = ps.generate(x, counts)
+    fac, xo = ps.inverse(ev.p, counts, ev.ok)
+    ch = torch.repeat_interleave(torch.arange(proc.n_channels, device="cuda"),
+                                 torch.from_numpy(counts).cuda())
+    idx = torch.arange(n, device="cuda")
+    okb = ev.ok.bool()
+    own_x = xo[ch, idx][okb]
+    dx = (own_x - x[okb]).abs()
+    assert dx.median().item() < 1e-12
+    own_f = fac[idx, ch][okb]
+    assert ((own_f / ev.factor[okb] - 1).abs().median().item()) < 1e-11
+    assert torch.isfinite(fac[okb]).all().item()
+    sl = slice(1_000_000, 1_004_000)
+    assert_inverse_parity(oracle.Oracle(proc, 1000.0), fac[sl].cpu().numpy(),
+                          xo[:, sl].cpu().numpy(), ev.p[sl].cpu().numpy(),
+                          ch[sl].cpu().numpy().astype(np.int32), ev.ok[sl].cpu().numpy())
+
+
+def test_whizard_abi_all_channels(torch):
+    from gpu_phs_gb300 import _lib
+    lib = _lib.load()
+    z = golden("whizard_bwbw")
+    proc = load_process(z)
+    ip = lambda v: C.byref(C.c_int(v))
+    nch, n_x = proc.n_channels, proc.n_x
+    lib.c_whizard_set_particle_structure(ip(nch), ip(nch), ip(nch), ip(n_x), ip(2), ip(proc.n_out))
+    fm = np.ascontiguousarray(proc.flv_masses)
+    fw = np.ascontiguousarray(proc.flv_widths)
+    lib.c_whizard_set_flavors(fm.ctypes.data, fw.ctypes.data)
+    lib.c_whizard_init_mappings()
+    keep = []
+    for c in range(nch):
+        a = [np.ascontiguousarray(proc.map_ids[c], np.int32), np.ascontiguousarray(proc.map_masses[c]),
+             np.ascontiguousarray(proc.map_widths[c])]
+        keep += a
+        lib.c_whizard_fill_mapping(ip(c + 1), *[t.ctypes.data for t in a])
+    lib.c_whizard_init_tree_structures()
+    for c in range(nch):
+        a = [np.ascontiguousarray(t[c], np.int32) for t in (proc.d1, proc.d2, proc.has_children, proc.friends)]
+        keep += a
+        lib.c_whizard_fill_tree_structure(ip(c + 1), *[t.ctypes.data for t in a])
+    lib.c_whizard_set_threads(ip(512), ip(512), ip(512))
+    lib.c_whizard_init_gpu_phs()
+    counts = counts_of(z["channel"], nch)
+    n = int(counts.sum())
+    limits = np.ascontiguousarray(np.cumsum(counts), np.int32)
+    lib.c_whizard_init_channel_ids(ip(n), ip(nch), limits.ctypes.data)
+    x = np.ascontiguousarray(z["x"])
+    E1 = np.full(n, 500.0)
+    E2 = np.full(n, 500.0)
+    factors = np.zeros(n * nch)
+    volumes = np.zeros(n)
+    oks = np.zeros(n, np.uint8)
+    p = np.zeros(n * proc.n_out * 4)
+    x_out = np.zeros(n * n_x * nch)
+    flag = C.c_bool(False)
+    lib.c_whizard_gen_phs_from_x_gpu(E1.ctypes.data, E2.ctypes.data, C.byref(flag), ip(n), ip(nch),
+                                     ip(n_x), x.ctypes.data, factors.ctypes.data,
+                                     volumes.ctypes.data, oks.ctypes.data, p.ctypes.data,
+                                     x_out.ctypes.data)
+    assert lib.phs_last_error().decode() == ""
+    o = oracle.Oracle(proc, 1000.0)
+    fac = factors.reshape(n, nch)
+    own = fac[np.arange(n), z["channel"]]
+    assert_inverse_parity(o, fac, x_out.reshape(nch, n, n_x), p.reshape(n, proc.n_out, 4),
+                          z["channel"], oks, x_own=x, factor_own=own)
+    g = z["all_factors"]
+    assert np.all(np.abs(fac - g) <= 0.5e-7 + 2e-3 * np.abs(g))
+    lib.c_whizard_reset_generator()
+    lib.c_whizard_finalize_gpu_phs()
+
+
+def test_adjoint_rejects_friend_channels(torch):
+    from gpu_phs_gb300.api import PhaseSpace
+    z = golden("whizard_bwbw")
+    proc = load_process(z)
+    ps = PhaseSpace(proc, 500.0, 500.0)
+    x = torch.from_numpy(np.ascontiguousarray(z["x"])).cuda()
+    counts = counts_of(z["channel"], proc.n_channels)
+    pbar = torch.zeros((x.shape[0], proc.n_out, 4), dtype=torch.float64, device="cuda")
+    with pytest.raises(Exception, match="friend"):
+        ps.vjp(x, pbar, None, counts)

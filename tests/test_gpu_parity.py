@@ -4,6 +4,9 @@ fixtures and the Whizard golden vectors.
 Bar: ok flags bit-exact; momenta within 1e-12 of max(particle energy, 1e-3 sqrt(s))
 (conftest.momentum_rel_err), factors within 1e-12 relative (FP64; the transcendental
 functions of CUDA and glibc may differ by an ulp); volumes within 1e-15 relative.
+Channels with a friend (beam-axis) boost: momenta within 1e-10, because the rotation onto
+the friend axis divides by 1 + cos(angle of the axis to z) (Rodrigues), so two FP64
+evaluations in different operation order drift apart as that axis nears -z.
 """
 import ctypes as C
 
@@ -18,6 +21,7 @@ from oracle import oracle
 pytestmark = pytest.mark.gpu
 
 MOM_TOL = 1e-12
+MOM_TOL_FRIEND = 1e-10
 FAC_TOL = 1e-12
 
 
@@ -41,14 +45,19 @@ def run_gpu(torch, proc, x, sqrts, counts=None, E=None):
     return out
 
 
-def assert_parity(got, ref_p, ref_f, ref_v, ref_ok, vol_all=False, sqrts=1000.0):
+def assert_parity(got, ref_p, ref_f, ref_v, ref_ok, vol_all=False, sqrts=1000.0, friend=None):
+    """friend: per-event mask of events generated by a channel with a friend boost."""
     p, f, v, ok = got
     mism = int(np.count_nonzero(ok != ref_ok))
     assert mism == 0, f"{mism} ok-flag mismatches"
     sel = ref_ok == 1
     if sel.any():
-        err = momentum_rel_err(p[sel], ref_p[sel], sqrts).max()
-        assert err <= MOM_TOL, f"momentum error {err:.3e}"
+        tol = np.full(len(ok), MOM_TOL)
+        if friend is not None:
+            tol[friend] = MOM_TOL_FRIEND
+        err = momentum_rel_err(p[sel], ref_p[sel], sqrts).max(axis=-1)
+        worst = (err / tol[sel]).max()
+        assert worst <= 1.0, f"momentum error {worst:.3e} x the tolerance"
         ferr = (np.abs(f[sel] - ref_f[sel]) / np.abs(ref_f[sel])).max()
         assert ferr <= FAC_TOL, f"factor error {ferr:.3e}"
     vs = slice(None) if vol_all else sel
@@ -91,12 +100,13 @@ def test_forward_vs_whizard_golden(torch, name):
     proc = load_process(z)
     counts = counts_of(z["channel"], proc.n_channels)
     p, f, v, ok = run_gpu(torch, proc, z["x"], 1000.0, counts)
-    friendless = z["hasfriends"][z["channel"]] == 0
     assert np.array_equal(ok, z["ok"].astype(np.uint8))
-    assert np.abs(p - z["p_out"])[friendless].max() < 1e-3
+    # all channels, the 16 friend-boost trees of bwbw included
+    assert np.abs(p - z["p_out"]).max() < 1e-3
     assert np.allclose(v, z["volume"], rtol=1e-14, atol=0)
     r = oracle.Oracle(proc, 1000.0).generate(z["x"], z["channel"])
-    assert_parity((p, f, v, ok), r.p, r.factor, r.volume, r.ok)
+    assert_parity((p, f, v, ok), r.p, r.factor, r.volume, r.ok,
+                  friend=z["hasfriends"][z["channel"]] == 1)
 
 
 @pytest.mark.parametrize("n", [0, 1, 31, 32, 33, 1025])
@@ -122,7 +132,7 @@ def test_multichannel_uneven_counts(torch):
     x = uniform_x(6, n, proc.n_x)
     r = oracle.Oracle(proc, 1000.0).generate(x, channels)
     got = run_gpu(torch, proc, x, 1000.0, counts)
-    assert_parity(got, r.p, r.factor, r.volume, r.ok)
+    assert_parity(got, r.p, r.factor, r.volume, r.ok, friend=z["hasfriends"][channels] == 1)
 
 
 def test_many_channels_device_segment_table(torch):
@@ -253,7 +263,8 @@ def test_whizard_binding_end_to_end(torch):
     assert lib.phs_whizard_momentum_device_pointer()
     r = oracle.Oracle(proc, 1000.0).generate(x, z["channel"])
     own = factors.reshape(n, nch)[np.arange(n), z["channel"]]
-    assert_parity((p.reshape(n, proc.n_out, 4), own, volumes, oks), r.p, r.factor, r.volume, r.ok)
+    assert_parity((p.reshape(n, proc.n_out, 4), own, volumes, oks), r.p, r.factor, r.volume, r.ok,
+                  friend=z["hasfriends"][z["channel"]] == 1)
     xo = x_out.reshape(nch, n, n_x)
     assert np.array_equal(xo[z["channel"], np.arange(n)], x)
     lib.c_whizard_reset_generator()

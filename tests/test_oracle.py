@@ -32,17 +32,30 @@ def test_philox_stream_windows():
 def test_oracle_vs_whizard_golden(name):
     z = golden(f"whizard_{name}")
     proc = load_process(z)
-    friendless = z["hasfriends"][z["channel"]] == 0
     r = oracle.Oracle(proc, 1000.0).generate(z["x"], z["channel"])
     assert np.array_equal(r.ok, z["ok"].astype(np.uint8))
-    # x is printed with 9 decimals, which limits momentum agreement to ~1e-4 GeV
-    dp = np.abs(r.p - z["p_out"])[friendless]
+    # x is printed with 9 decimals, which limits momentum agreement to ~1e-4 GeV; the
+    # friend-boost channels of bwbw (16 of 61) are included
+    dp = np.abs(r.p - z["p_out"])
     assert dp.max() < 1e-3
     assert np.allclose(r.volume, z["volume"], rtol=1e-14, atol=0)
-    # factors are printed with 4-7 decimals
-    f, g = r.factor[friendless], z["factor"][friendless]
+    # factors are printed with a fixed number of decimals (4 for ttH, 7 for bwbw)
+    f, g = r.factor, z["factor"]
     dec = 4 if name == "ttH" else 7
     assert np.all(np.abs(f - g) <= 2e-3 * np.abs(g) + 0.5 * 10.0 ** -dec)
+
+
+def test_friend_channels_need_the_friend_boost():
+    """Without the friend table the flagged bwbw trees miss Whizard's momenta by far: the
+    golden events pin the friend boost itself, not just the friend-free channels."""
+    z = golden("whizard_bwbw")
+    proc = load_process(z)
+    assert proc.friends.any()
+    flagged = z["hasfriends"][z["channel"]] == 1
+    assert flagged.sum() == 149
+    proc.friends = np.zeros_like(proc.friends)
+    r = oracle.Oracle(proc, 1000.0).generate(z["x"], z["channel"])
+    assert np.abs(r.p - z["p_out"])[flagged].max() > 10.0
 
 
 @pytest.mark.parametrize("name", REFCPU_FIXTURES)
