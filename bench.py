@@ -278,7 +278,50 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64):
         "output_bytes_per_event": 8 * proc.n_x + 16 * (proc.n_out - 2),
         "stored_matrix_checkpoint_bytes_per_event": 16 * 8 * n_internal,
         "scratch": "per-visit state in shared memory; the boost chain is recomputed in reverse"}
+    del x, pbar, jbar, o
+
+    # inverse map: Whizard's bwbw process (61 channels, 16 with friend boosts), every
+    # event inverted in every channel, as the Whizard ABI does
+    proc = whizard_process("bwbw")
+    n = 1 << 20
+    counts = np.full(proc.n_channels, n // proc.n_channels, np.int64)
+    counts[: n - int(counts.sum())] += 1
+    ps = PhaseSpace(proc, 500.0, 500.0)
+    x = torch.empty((n, proc.n_x), dtype=torch.float64, device="cuda")
+    philox_fill(x, n, proc.n_x, SEED)
+    ev = ps.generate(x, counts)
+    fac = torch.empty((n, proc.n_channels), dtype=torch.float64, device="cuda")
+    xo = torch.empty((proc.n_channels, n, proc.n_x), dtype=torch.float64, device="cuda")
+    lib = _lib.load()
+
+    def inv():
+        _lib.check(lib.phs_inverse_device(ps.h, n, counts.ctypes.data, None, None,
+                                          ev.p.data_ptr(), ev.ok.data_ptr(), x.data_ptr(),
+                                          ev.factor.data_ptr(), fac.data_ptr(), xo.data_ptr(),
+                                          stream.cuda_stream))
+
+    t_inv = _time_calls(torch, inv, steps, warmup, stream)
+    pairs = n * proc.n_channels
+    wbytes = pairs * 8 * (proc.n_x + 1)
+    rbytes = n * (32 * proc.n_out + 1 + 8 * proc.n_x + 8)
+    res["inverse_bwbw_61ch"] = {
+        "n_events": n, "n_channels": proc.n_channels, "ms_per_step": t_inv,
+        "events_per_s": n / t_inv * 1e3, "channel_inversions_per_s": pairs / t_inv * 1e3,
+        "hbm_gbs": (wbytes + rbytes) / t_inv * 1e-6,
+        "algorithmic_bytes_per_step": wbytes + rbytes,
+        "ok_fraction": ev.ok.double().mean().item(),
+        "launch": "one persistent kernel: 128 events per block, every channel per event"}
     return res
+
+
+def whizard_process(name: str):
+    """A Whizard process from the sample-file fixtures committed under tests/golden."""
+    z = np.load(os.path.join(ROOT, "tests", "golden", f"whizard_{name}.npz"))
+    from gpu_phs_gb300.processes import Process
+    meta = z["meta"]
+    return Process(int(meta[0]), int(meta[1]), z["d1"], z["d2"], z["has_children"], z["friends"],
+                   z["map_ids"], z["map_masses"], z["map_widths"], z["flv_masses"],
+                   z["flv_widths"], n_x=int(meta[2]), name=f"whizard_{name}", sqrts=1000.0)
 
 
 def cpu_reference_rate(proc, sqrts, seconds: float, max_events: int, prefer_ref: bool = True):
