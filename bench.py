@@ -192,48 +192,61 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64):
     o = ps.alloc(n)
     ms = _time_calls(torch, lambda: ps.generate(x_tt, out=o), steps, warmup, stream)
     v = C.c_int()
-    _lib.load().phs_process_tuning(ps.h, C.byref(v))
+    _lib.load().phs_process_tuning(ps.h, C.byref(v), None)
     res["fp32_mixed_tt"] = {"value": n / ms * 1e3, "unit": "events/s", "ms_per_step": ms,
                             "speedup_vs_fp64": ms_tt64 / ms, "n_events": n,
                             "autotuned_variant": v.value,
                             "error_vs_fp64": _errors(torch, out_tt, o, proc.sqrts)}
     del o
 
+    # Three FP64/FP32 forms per workload: FP64 one pass (the plain kernel, every event
+    # walked in full), FP64 autotuned (one pass or compacting: test every event first, walk
+    # only those that pass), and FP32 pair autotuned (register budgets x one pass /
+    # compacting with an FP32 first pass).  All three produce identical ok flags.
+    forms = (("fp64_one_pass", 0, 0), ("fp64", 0, -1), ("fp32_mixed", 1, -1))
+
     proc = P.precision()
     n = 1 << 24
     x = torch.empty((n, proc.n_x), dtype=torch.float64, device="cuda")
     philox_fill(x, n, proc.n_x, SEED)
-    outs, t = {}, {}
-    for prec in (0, 1):
+    outs, t, tuned = {}, {}, {}
+    for name, prec, f64v in forms:
         ps = PhaseSpace(proc, proc.sqrts / 2, proc.sqrts / 2)
         ps.set_precision(prec)
-        outs[prec] = ps.alloc(n)
-        t[prec] = _time_calls(torch, lambda: ps.generate(x, out=outs[prec]), steps, warmup, stream)
-    res["precision_13TeV"] = {"workload": proc.name, "n_events": n, "n_x": proc.n_x,
-                              "fp64_events_per_s": n / t[0] * 1e3,
-                              "fp32_mixed_events_per_s": n / t[1] * 1e3,
-                              "speedup": t[0] / t[1],
-                              "ok_fraction": outs[0].ok.double().mean().item(),
-                              "error_vs_fp64": _errors(torch, outs[0], outs[1], proc.sqrts)}
+        ps.set_variants(-1, f64v)
+        outs[name] = ps.alloc(n)
+        t[name] = _time_calls(torch, lambda: ps.generate(x, out=outs[name]), steps, warmup, stream)
+        tuned[name] = ps.tuning()[prec == 0]
+    res["precision_13TeV"] = {
+        "workload": proc.name, "n_events": n, "n_x": proc.n_x,
+        **{f"{k}_events_per_s": n / t[k] * 1e3 for k, _, _ in forms},
+        "kernel_variants": tuned,
+        "speedup": t["fp64"] / t["fp32_mixed"],
+        "speedup_vs_fp64_one_pass": t["fp64_one_pass"] / t["fp32_mixed"],
+        "ok_fraction": outs["fp64"].ok.double().mean().item(),
+        "ok_mismatches_fp64_forms": int((outs["fp64"].ok != outs["fp64_one_pass"].ok).sum().item()),
+        "error_vs_fp64": _errors(torch, outs["fp64"], outs["fp32_mixed"], proc.sqrts)}
     del outs, x
 
     procs, counts = P.batched(seed=2024, n_channels=64, total_events=1 << 24)
     spaces = [PhaseSpace(p, 500.0, 500.0) for p in procs]
     n = int(counts.sum())
-    bres, bufs = {}, {}
-    for prec in (0, 1):
+    bres, bufs, tuned = {}, {}, {}
+    for name, prec, f64v in forms:
         batch = Batch(spaces)
         batch.set_precision(prec)
+        batch.set_variants(-1, f64v)
         xo, po = batch.offsets(counts)
-        if prec == 0:
+        if name == "fp64_one_pass":
             xb = torch.empty(int(xo[-1]), dtype=torch.float64, device="cuda")
             philox_fill(xb, int(xo[-1]), 1, SEED)
-        bufs[prec] = (torch.empty(int(po[-1]), dtype=torch.float64, device="cuda"),
+        bufs[name] = (torch.empty(int(po[-1]), dtype=torch.float64, device="cuda"),
                       torch.empty(n, dtype=torch.float64, device="cuda"),
                       torch.empty(n, dtype=torch.float64, device="cuda"),
                       torch.empty(n, dtype=torch.uint8, device="cuda"))
-        g = batch_graph(batch, xb, counts, *bufs[prec])
-        bres[prec] = _time_calls(torch, lambda: g.launch(), steps, warmup, stream)
+        g = batch_graph(batch, xb, counts, *bufs[name])   # tunes on its untimed first run
+        bres[name] = _time_calls(torch, lambda: g.launch(), steps, warmup, stream)
+        tuned[name] = batch.tuning()[prec == 0]
         del g
     # ok flags of the FP64 batch against per-channel plain runs
     per_channel_mism = 0
@@ -241,17 +254,28 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64):
     for i, (sp, c) in enumerate(zip(spaces, counts)):
         c = int(c)
         ev = sp.generate(xb[xo[i]:xo[i + 1]].view(c, sp.proc.n_x))
-        per_channel_mism += int((ev.ok != bufs[0][3][e:e + c]).sum().item())
+        per_channel_mism += int((ev.ok != bufs["fp64"][3][e:e + c]).sum().item())
         e += c
-    res["batched_64ch"] = {"n_channels": 64, "n_events": n, "n_out_range": [3, 8],
-                           "counts": "power law, exponent 1.5, seed 2024",
-                           "launch": "one persistent kernel per step, replayed from a CUDA graph",
-                           "fp64_events_per_s": n / bres[0] * 1e3,
-                           "fp32_mixed_events_per_s": n / bres[1] * 1e3,
-                           "speedup": bres[0] / bres[1],
-                           "ok_fraction": bufs[0][3].double().mean().item(),
-                           "ok_mismatches_fp32_mixed_vs_fp64": int((bufs[0][3] != bufs[1][3]).sum().item()),
-                           "ok_mismatches_vs_per_channel_runs": per_channel_mism}
+    ok64 = bufs["fp64"][3]
+    res["batched_64ch"] = {
+        "n_channels": 64, "n_events": n, "n_out_range": [3, 8],
+        "counts": "power law, exponent 1.5, seed 2024",
+        "launch": "one persistent kernel per step, replayed from a CUDA graph",
+        **{f"{k}_events_per_s": n / bres[k] * 1e3 for k, _, _ in forms},
+        "kernel_variants": tuned,
+        "speedup": bres["fp64"] / bres["fp32_mixed"],
+        "speedup_vs_fp64_one_pass": bres["fp64_one_pass"] / bres["fp32_mixed"],
+        "ok_fraction": ok64.double().mean().item(),
+        "ok_mismatches_fp32_mixed_vs_fp64": int((ok64 != bufs["fp32_mixed"][3]).sum().item()),
+        "ok_mismatches_fp64_forms": int((ok64 != bufs["fp64_one_pass"][3]).sum().item()),
+        "ok_mismatches_vs_per_channel_runs": per_channel_mism}
+    # momentum / factor error of the FP32-pair batch against FP64 (ok events)
+    sel = ok64.bool()
+    pf, p6 = bufs["fp32_mixed"][0], bufs["fp64"][0]
+    dp = (pf - p6).abs().max().item()
+    res["batched_64ch"]["max_abs_momentum_diff_gev"] = dp
+    res["batched_64ch"]["factor_max_rel"] = (
+        (bufs["fp32_mixed"][1][sel] / bufs["fp64"][1][sel] - 1).abs().max().item())
     del bufs, xb, spaces
 
     # adjoint: forward + reverse on 1e6 tt events with random cotangents
@@ -518,6 +542,8 @@ def run_ours(args):
     if not args.no_variants and world == 1:
         variants = measure_variants(torch, args.steps, args.warmup, x, out, ms_per_step)
         variants["fp32_mixed_over_fp64_batched"] = variants["batched_64ch"]["speedup"]
+        variants["fp32_mixed_over_fp64_one_pass_batched"] = (
+            variants["batched_64ch"]["speedup_vs_fp64_one_pass"])
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -26,7 +26,10 @@ _SIGS = {
     "phs_process_set_beams": (I, [P, D, D]),
     "phs_process_info": (I, [P, P, P, P, P, P]),
     "phs_process_set_precision": (I, [P, I]),
-    "phs_process_tuning": (I, [P, P]),
+    "phs_process_tuning": (I, [P, P, P]),
+    "phs_process_set_variants": (I, [P, I, I]),
+    "phs_batch_tuning": (I, [P, P, P]),
+    "phs_batch_set_variants": (I, [P, I, I]),
     "phs_batch_set_precision": (I, [P, I]),
     "phs_generate_device": (I, [P, I64, P, P, P, P, P, P, P]),
     "phs_generate_beams_device": (I, [P, I64, P, P, P, P, P, P, P, P, P]),

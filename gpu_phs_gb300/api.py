@@ -67,6 +67,16 @@ class PhaseSpace:
         """PRECISION_F64 (default) or PRECISION_F32X2 for the uniform-beam generate calls."""
         check(load().phs_process_set_precision(self.h, int(precision)))
 
+    def tuning(self):
+        """(ff_variant, f64_variant) the autotuner chose (-1: not tuned yet)."""
+        f, d = C.c_int(), C.c_int()
+        check(load().phs_process_tuning(self.h, C.byref(f), C.byref(d)))
+        return f.value, d.value
+
+    def set_variants(self, ff_variant: int = -1, f64_variant: int = -1) -> None:
+        """Pins the kernel variants (-1: autotune)."""
+        check(load().phs_process_set_variants(self.h, int(ff_variant), int(f64_variant)))
+
     def close(self) -> None:
         if getattr(self, "h", None):
             load().phs_process_destroy(self.h)
@@ -206,6 +216,14 @@ class Batch:
 
     def set_precision(self, precision: int) -> None:
         check(load().phs_batch_set_precision(self.h, int(precision)))
+
+    def tuning(self):
+        f, d = C.c_int(), C.c_int()
+        check(load().phs_batch_tuning(self.h, C.byref(f), C.byref(d)))
+        return f.value, d.value
+
+    def set_variants(self, ff_variant: int = -1, f64_variant: int = -1) -> None:
+        check(load().phs_batch_set_variants(self.h, int(ff_variant), int(f64_variant)))
 
     def offsets(self, counts):
         c = np.ascontiguousarray(counts, np.int64)

@@ -70,8 +70,15 @@ struct Segments {
   std::vector<PhsSegment> host;
   DevBuf dev;
   std::vector<PhsSegment> uploaded;  // content of dev
+  DevBuf work;                       // chunk counter of the compacting kernels
   int64_t n_tiles = 0;
+  int64_t n_chunks = 0;
   int64_t n_events = 0;
+  void release() {
+    dev.release();
+    work.release();
+    uploaded.clear();
+  }
 };
 
 struct ChanLayout {  // per launched channel: shape of its x and p rows
@@ -83,7 +90,7 @@ int build_segments(Segments &S, const int64_t *counts, int n_channels,
                    const std::vector<ChanLayout> &lay, int64_t ev0, int64_t x0, int64_t p0,
                    bool whizard_cols) {
   S.host.clear();
-  int64_t ev = ev0, x = x0, p = p0, tile = 0;
+  int64_t ev = ev0, x = x0, p = p0, tile = 0, chunk = 0;
   for (int c = 0; c < n_channels; c++) {
     const int64_t n = counts[c];
     if (n < 0) return fail(PHS_ERR_INVALID_ARG, "channel %d has a negative event count", c);
@@ -99,13 +106,17 @@ int build_segments(Segments &S, const int64_t *counts, int n_channels,
     g.tile_begin = tile;
     g.x_stride = lay[c].x_stride;
     g.factor_col = whizard_cols ? c : 0;
+    g.chunk_begin = chunk;
     S.host.push_back(g);
-    tile += (n + 31) / 32;
+    const int64_t tiles = (n + 31) / 32;
+    tile += tiles;
+    chunk += (tiles + PHS_CHUNK_TILES - 1) / PHS_CHUNK_TILES;
     ev += n;
     x += n * lay[c].x_stride;
     p += n * 4 * lay[c].n_out;
   }
   S.n_tiles = tile;
+  S.n_chunks = chunk;
   S.n_events = ev - ev0;
   return PHS_OK;
 }
@@ -114,7 +125,10 @@ int build_segments(Segments &S, const int64_t *counts, int n_channels,
 int attach_segments(Segments &S, PhsLaunch &a, cudaStream_t stream) {
   a.n_segments = (int32_t)S.host.size();
   a.n_tiles = S.n_tiles;
+  a.n_chunks = S.n_chunks;
   a.segments = nullptr;
+  if (int rc = S.work.reserve(sizeof(unsigned long long))) return rc;
+  a.work = S.work.as<unsigned long long>();
   if (S.host.size() <= PHS_INLINE_SEGS) {
     std::copy(S.host.begin(), S.host.end(), a.seg_inline);
     return PHS_OK;
@@ -143,10 +157,11 @@ int sm_count(int device) {
   return n;
 }
 
-int grid_for(int64_t n_tiles, int device, int stack_depth, bool per_event) {
+int grid_for(int64_t n_tiles, int device, int stack_depth, bool per_event, int variant) {
   const int warps_per_block = PHS_FWD_BLOCK / 32;
   int64_t want = (n_tiles + warps_per_block - 1) / warps_per_block;
-  int64_t cap = (int64_t)sm_count(device) * phs_forward_blocks_per_sm(stack_depth, per_event);
+  int64_t cap =
+      (int64_t)sm_count(device) * phs_forward_blocks_per_sm(stack_depth, per_event, variant);
   return (int)std::max<int64_t>(1, std::min(want, cap));
 }
 
@@ -157,26 +172,28 @@ int grid_for_ff(int64_t n_tiles, int device, int stack_depth, int variant) {
   return (int)std::max<int64_t>(1, std::min(want, cap));
 }
 
-// FP32-pair launch with autotuning.  The kernel comes in PHS_FF_VARIANTS register budgets
-// (resident blocks per SM); they compute identical bits.  The first launch of at least
-// kTuneEvents events, outside stream capture, runs every variant twice on the real data,
-// times them with CUDA events on the launch stream and keeps the fastest in `variant`.
+// Launch with autotuning.  A kernel comes in n_variants forms that compute identical bits
+// (register budgets, one- or two-pass); which is fastest depends on the trees and on how
+// many events pass the kinematic test.  The first launch of at least kTuneEvents events,
+// outside stream capture, runs every variant twice on the real data, times them with
+// CUDA events on the launch stream and keeps the fastest in `variant`; later launches use
+// it.  launch(v) enqueues variant v.
 const int64_t kTuneEvents = 1 << 18;
 
-int launch_ff_tuned(int &variant, const PhsLaunch &a, int device, int depth, int64_t n_events,
-                    cudaStream_t st) {
+template <class Launch>
+int launch_tuned(int &variant, int n_variants, int64_t n_events, cudaStream_t st, Launch launch) {
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   cudaStreamIsCapturing(st, &cap);
   if (variant < 0 && n_events >= kTuneEvents && cap == cudaStreamCaptureStatusNone) {
     cudaEvent_t e0, e1;
     CUDA_TRY(cudaEventCreate(&e0));
     CUDA_TRY(cudaEventCreate(&e1));
-    float best[PHS_FF_VARIANTS];
-    for (int v = 0; v < PHS_FF_VARIANTS; v++) best[v] = 1e30f;
+    float best[8];
+    for (int v = 0; v < n_variants; v++) best[v] = 1e30f;
     for (int rep = 0; rep < 2; rep++) {
-      for (int v = 0; v < PHS_FF_VARIANTS; v++) {
+      for (int v = 0; v < n_variants; v++) {
         CUDA_TRY(cudaEventRecord(e0, st));
-        CUDA_TRY(phs_launch_forward_ff(a, grid_for_ff(a.n_tiles, device, depth, v), v, st));
+        CUDA_TRY(launch(v));
         CUDA_TRY(cudaEventRecord(e1, st));
         CUDA_TRY(cudaEventSynchronize(e1));
         float ms = 0;
@@ -187,14 +204,36 @@ int launch_ff_tuned(int &variant, const PhsLaunch &a, int device, int depth, int
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     int bv = 0;
-    for (int v = 1; v < PHS_FF_VARIANTS; v++)
+    for (int v = 1; v < n_variants; v++)
       if (best[v] < best[bv]) bv = v;
     variant = bv;
     return PHS_OK;  // the timed launches already wrote the outputs
   }
-  const int v = variant < 0 ? 0 : variant;
-  CUDA_TRY(phs_launch_forward_ff(a, grid_for_ff(a.n_tiles, device, depth, v), v, st));
+  CUDA_TRY(launch(variant < 0 ? 0 : variant));
   return PHS_OK;
+}
+
+int launch_ff_tuned(int &variant, const PhsLaunch &a, int device, int depth, int64_t n_events,
+                    cudaStream_t st) {
+  return launch_tuned(variant, PHS_FF_VARIANTS, n_events, st, [&](int v) {
+    if (a.work) {
+      cudaError_t e = cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), st);
+      if (e != cudaSuccess) return e;
+    }
+    return phs_launch_forward_ff(a, grid_for_ff(a.n_tiles, device, depth, v), v, st);
+  });
+}
+
+int launch_f64_tuned(int &variant, const PhsLaunch &a, int device, int depth, int64_t n_events,
+                     cudaStream_t st) {
+  const bool per_event = a.E1 != nullptr;
+  return launch_tuned(variant, PHS_F64_VARIANTS, n_events, st, [&](int v) {
+    if (a.work) {
+      cudaError_t e = cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), st);
+      if (e != cudaSuccess) return e;
+    }
+    return phs_launch_forward_f64(a, grid_for(a.n_tiles, device, depth, per_event, v), v, st);
+  });
 }
 
 // Restores the caller's current device on scope exit.
@@ -221,6 +260,7 @@ struct phs_process {
   double E1 = 0, E2 = 0;
   int precision = PHS_PRECISION_F64;
   int ff_variant = -1;  // autotuned FP32-pair kernel variant (-1: not tuned yet)
+  int f64_variant[2] = {-1, -1};  // autotuned FP64 variant: uniform, per-event beams
   std::vector<PhsChannel> prog;
   std::vector<PhsChannelFF> prog_ff;
   std::vector<PhsAdjChannel> prog_adj;
@@ -295,13 +335,13 @@ extern "C" int phs_process_destroy(phs_process_t h) {
   for (int s = 0; s < phs_process::kStreams; s++) {
     if (h->streams[s]) cudaStreamDestroy(h->streams[s]);
     h->bx[s].release(); h->bp[s].release(); h->bf[s].release(); h->bv[s].release();
-    h->bo[s].release(); h->pseg[s].dev.release();
+    h->bo[s].release(); h->pseg[s].release();
   }
   h->d_prog.release();
   h->d_prog_ff.release();
   h->d_prog_adj.release();
   h->d_ch_begin.release();
-  h->segs.dev.release();
+  h->segs.release();
   delete h;
   return PHS_OK;
 }
@@ -376,9 +416,28 @@ extern "C" int phs_process_set_precision(phs_process_t h, int precision) {
   return PHS_OK;
 }
 
-extern "C" int phs_process_tuning(phs_process_t h, int *ff_variant) {
+extern "C" int phs_process_tuning(phs_process_t h, int *ff_variant, int *f64_variant) {
   if (int rc = check_proc(h)) return rc;
   if (ff_variant) *ff_variant = h->ff_variant;
+  if (f64_variant) *f64_variant = h->f64_variant[0];
+  return PHS_OK;
+}
+
+static int check_variants(int ff_variant, int f64_variant) {
+  if (ff_variant < -1 || ff_variant >= PHS_FF_VARIANTS)
+    return fail(PHS_ERR_INVALID_ARG, "FP32-pair variant %d is not in [-1, %d)", ff_variant,
+                PHS_FF_VARIANTS);
+  if (f64_variant < -1 || f64_variant >= PHS_F64_VARIANTS)
+    return fail(PHS_ERR_INVALID_ARG, "FP64 variant %d is not in [-1, %d)", f64_variant,
+                PHS_F64_VARIANTS);
+  return PHS_OK;
+}
+
+extern "C" int phs_process_set_variants(phs_process_t h, int ff_variant, int f64_variant) {
+  if (int rc = check_proc(h)) return rc;
+  if (int rc = check_variants(ff_variant, f64_variant)) return rc;
+  h->ff_variant = ff_variant;
+  h->f64_variant[0] = h->f64_variant[1] = f64_variant;
   return PHS_OK;
 }
 
@@ -447,9 +506,8 @@ static int launch_process(phs_process_t h, Segments &S, int64_t n_events, const 
   if (a.n_tiles == 0) return PHS_OK;
   if (h->precision == PHS_PRECISION_F32X2 && E1 == nullptr)
     return launch_ff_tuned(h->ff_variant, a, h->device, h->stack_depth, n_events, stream);
-  const int grid = grid_for(a.n_tiles, h->device, h->stack_depth, E1 != nullptr);
-  CUDA_TRY(phs_launch_forward_f64(a, grid, stream));
-  return PHS_OK;
+  return launch_f64_tuned(h->f64_variant[E1 != nullptr], a, h->device, h->stack_depth, n_events,
+                          stream);
 }
 
 static int check_ptrs(int64_t n, const void *x, const void *p, const void *f, const void *v,
@@ -636,6 +694,7 @@ struct phs_batch {
   int device = 0;
   int precision = PHS_PRECISION_F64;
   int ff_variant = -1;
+  int f64_variant = -1;
   std::vector<PhsChannel> prog;
   std::vector<PhsChannelFF> prog_ff;
   std::vector<ChanLayout> lay;
@@ -686,7 +745,7 @@ extern "C" int phs_batch_destroy(phs_batch_t b) {
   DeviceGuard g(b->device);
   b->d_prog.release();
   b->d_prog_ff.release();
-  b->segs.dev.release();
+  b->segs.release();
   delete b;
   return PHS_OK;
 }
@@ -742,8 +801,22 @@ extern "C" int phs_batch_generate_device(phs_batch_t b, const int64_t *counts, c
   if (b->precision == PHS_PRECISION_F32X2)
     return launch_ff_tuned(b->ff_variant, a, b->device, b->stack_depth, n_events,
                            (cudaStream_t)stream);
-  const int grid = grid_for(a.n_tiles, b->device, b->stack_depth, false);
-  CUDA_TRY(phs_launch_forward_f64(a, grid, (cudaStream_t)stream));
+  return launch_f64_tuned(b->f64_variant, a, b->device, b->stack_depth, n_events,
+                          (cudaStream_t)stream);
+}
+
+extern "C" int phs_batch_set_variants(phs_batch_t b, int ff_variant, int f64_variant) {
+  if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
+  if (int rc = check_variants(ff_variant, f64_variant)) return rc;
+  b->ff_variant = ff_variant;
+  b->f64_variant = f64_variant;
+  return PHS_OK;
+}
+
+extern "C" int phs_batch_tuning(phs_batch_t b, int *ff_variant, int *f64_variant) {
+  if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
+  if (ff_variant) *ff_variant = b->ff_variant;
+  if (f64_variant) *f64_variant = b->f64_variant;
   return PHS_OK;
 }
 
@@ -814,7 +887,7 @@ extern "C" int phs_generate_device_noalloc(phs_process_t h, double E1, double E2
   a.ok = ok;
   a.factor_stride = 1;
   if (S.host.size() <= PHS_INLINE_SEGS) std::copy(S.host.begin(), S.host.end(), a.seg_inline);
-  const int grid = a.n_tiles > 0 ? grid_for(a.n_tiles, h->device, depth, false) : 1;
+  const int grid = a.n_tiles > 0 ? grid_for(a.n_tiles, h->device, depth, false, 0) : 1;
   cudaError_t e = phs_launch_forward_f64_noalloc(a, prog.data(), P.n_channels, S.host.data(),
                                                  (int)S.host.size(), grid, (cudaStream_t)stream);
   if (e != cudaSuccess)

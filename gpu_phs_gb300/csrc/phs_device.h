@@ -16,6 +16,7 @@ struct PhsLaunch {
   int32_t n_segments;
   int32_t stack_depth;         // max push depth over the launched channels
   int64_t n_tiles;             // total 32-event warp tiles
+  int64_t n_chunks;            // total work chunks (PhsSegment::chunk_begin)
   const double *x;
   double *p;
   double *factor;
@@ -24,13 +25,20 @@ struct PhsLaunch {
   int64_t factor_stride;       // factor index = event * factor_stride + segment.factor_col
   const double *E1;            // per-event beams (both non-null) or null
   const double *E2;
+  unsigned long long *work;    // compacting kernels: chunk counter, zeroed before the
+                               // launch (warps claim chunks dynamically); null: static
 };
 
 // Block size and resident blocks per SM of the forward kernel.
 #define PHS_FWD_BLOCK 128
 
-cudaError_t phs_launch_forward_f64(const PhsLaunch &a, int n_blocks, cudaStream_t stream);
-int phs_forward_blocks_per_sm(int stack_depth, bool per_event);
+// variant 0: one pass per event; 1 and 2: compacting (pass A tests every event and writes
+// the failures, pass B computes the passing events densely) with registers for 4 or 3
+// resident blocks per SM.  PHS_F64_VARIANTS of them.
+#define PHS_F64_VARIANTS 3
+cudaError_t phs_launch_forward_f64(const PhsLaunch &a, int n_blocks, int variant,
+                                   cudaStream_t stream);
+int phs_forward_blocks_per_sm(int stack_depth, bool per_event, int variant);
 size_t phs_forward_smem_bytes(int stack_depth);
 
 // Philox4x32-10 uniform doubles for events [first_event, first_event + n_events) of the
@@ -56,8 +64,9 @@ size_t phs_noalloc_scratch_bytes();
 // Forward launch on the FP32 pipe (float-float arithmetic), FP64 only for events within
 // 1e-5 of a kinematic limit, which are recomputed exactly (phs_kernels_ff.cu).  Needs
 // a.channels and a.channels_ff; uniform beams only.
-// variant: 0 = registers for 3 resident blocks per SM, 1 = for 4 (PHS_FF_VARIANTS).
-#define PHS_FF_VARIANTS 2
+// variant bit 0: registers for 4 (1) or 3 (0) resident blocks per SM; bit 1: the
+// compacting two-pass form (PHS_FF_VARIANTS in all).
+#define PHS_FF_VARIANTS 4
 cudaError_t phs_launch_forward_ff(const PhsLaunch &a, int n_blocks, int variant, cudaStream_t stream);
 int phs_forward_ff_blocks_per_sm(int stack_depth, int variant);
 size_t phs_forward_ff_smem_bytes(int stack_depth);

@@ -416,4 +416,182 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
   }
 }
 
+
+// Pass A of the compacting kernels: the kinematic test of one event alone -- the msq
+// mappings of its internal branches and the Kallen / mass tests of phs_event_f64 in the
+// same arithmetic, so the flag is the same bit -- without angles or boosts.  An event that
+// fails gets its outputs here (momenta 0, factor 0, ok 0, the channel volume); one that
+// passes gets them from phs_event_f64 in pass B.  Returns ok.  smem: the event's frame
+// stack (only the msq, m and m_max slots are used).
+template <bool PER_EVENT>
+__device__ __forceinline__ bool phs_ok_f64(const PhsLaunch &a, const PhsSegment &seg,
+                                           int64_t local, double *smem) {
+  const PhsChannel &ch = a.channels[seg.channel];
+  const int64_t ev = seg.ev_begin + local;
+  const double *xe = a.x + seg.x_base + local * seg.x_stride;
+  double sqrts = ch.sqrts;
+  if (PER_EVENT) sqrts = dmul(2.0, sqrt(dmul(a.E1[ev], a.E2[ev])));
+  const double s = dmul(sqrts, sqrts);
+  double msq_b = s, m_b = sqrts, mmax_b = sqrts;
+  bool ok = true;
+  int sp = 0;
+  const int n_visits = ch.n_visits;
+  for (int v = 0; v < n_visits; v++) {
+    const PhsVisit &V = ch.visit[v];
+    double cmsq[2], cm[2], cmax[2];
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const PhsChild &C = V.child[j];
+      if (!C.internal) {
+        cmsq[j] = C.msq_leaf;
+        cm[j] = C.m_leaf;
+        cmax[j] = 0.0;
+      } else {
+        double a0 = C.a0, a1 = C.a1, a2 = C.a2, mn = C.msq_min, mx = C.msq_max;
+        cmax[j] = C.m_max;
+        if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, a0, a1, a2, mn, mx, cmax[j]);
+        double f;
+        map_msq(C.map_id, xe[C.x_msq], s, C.m, C.w, mn, mx, a0, a1, a2, cmsq[j], f);
+        cm[j] = sqrt(cmsq[j]);
+      }
+    }
+    const double d = dsub(dsub(msq_b, cmsq[0]), cmsq[1]);
+    const double lda = dsub(dmul(d, d), dmul(dmul(4.0, cmsq[0]), cmsq[1]));
+    ok = ok && (lda > 0.0) && (m_b > dadd(cm[0], cm[1])) && (m_b <= mmax_b);
+    if (V.push >= 0) {
+      const bool j0 = V.push == 0;
+      stack_store(smem, sp, 16, j0 ? cmsq[0] : cmsq[1]);
+      stack_store(smem, sp, 17, j0 ? cm[0] : cm[1]);
+      stack_store(smem, sp, 19, j0 ? cmax[0] : cmax[1]);
+      sp++;
+    }
+    if (V.carry >= 0) {
+      const bool j0 = V.carry == 0;
+      msq_b = j0 ? cmsq[0] : cmsq[1];
+      m_b = j0 ? cm[0] : cm[1];
+      mmax_b = j0 ? cmax[0] : cmax[1];
+    } else if (sp > 0) {
+      sp--;
+      msq_b = stack_load(smem, sp, 16);
+      m_b = stack_load(smem, sp, 17);
+      mmax_b = stack_load(smem, sp, 19);
+    }
+  }
+  if (!ok) {
+    double volume = ch.volume;
+    if (PER_EVENT) {
+      double vol[PHS_MAX_VISITS];
+      const double c_int = 4 * PHS_TWOPI2, c_root = 4 * PHS_TWOPI5;
+      for (int i = 0; i < ch.n_vol; i++) {
+        int k1 = ch.vol_child[i][0], k2 = ch.vol_child[i][1];
+        double v1 = k1 >= 0 ? vol[k1] : 1.0, v2 = k2 >= 0 ? vol[k2] : 1.0;
+        vol[i] = ch.vol_is_root[i] ? dmul(v1, v2) / c_root
+                                   : dmul(dmul(dmul(v1, v2), sqrts), sqrts) / c_int;
+      }
+      volume = vol[ch.n_vol - 1];
+    }
+    a.volume[ev] = volume;
+    a.factor[ev * a.factor_stride + seg.factor_col] = 0.0;
+    a.ok[ev] = 0;
+    double2 *o = reinterpret_cast<double2 *>(a.p + seg.p_base + local * 4 * (int64_t)ch.n_out);
+    for (int i = 0; i < 2 * ch.n_out; i++) o[i] = make_double2(0.0, 0.0);
+  }
+  return ok;
+}
+
+// The persistent loop of the compacting kernels.  Each warp runs pass A on its 32-event
+// tiles (`pass_a(seg, local)` tests an event, writes it if it fails, and returns whether it
+// passed) and appends the passing events to its queue in shared memory (q: 64 slots);
+// pass B (`pass_b(seg, local)`, the full event) drains the queue 32 events at a time with
+// every lane busy.  The queue holds events of one segment only, so the visit program stays
+// warp-uniform: a tile of another segment first drains it.  Pass A and pass B have one
+// call site each, which keeps the (large) event code once in the kernel.
+//
+// Work is claimed in chunks of CHUNK consecutive tiles of one segment: CHUNK = 1 (single
+// tiles), or PHS_CHUNK_TILES (PhsSegment::chunk_begin; a segment's last chunk may be
+// shorter), whichever was measured faster for the kernel.  With a.work set, a warp claims
+// its next chunk from that counter when it finishes one (events of different channels and
+// kinematics cost very different amounts, and static shares leave SMs idle at the end);
+// without, chunks are strided over the grid.
+template <int CHUNK, class PassA, class PassB>
+__device__ __forceinline__ void compacting_loop(const PhsLaunch &a, int64_t *q, PassA pass_a,
+                                                PassB pass_b) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
+  int64_t claimed = 0;
+  auto next_chunk = [&]() -> int64_t {
+    if (a.work) {
+      unsigned long long c = 0;
+      if (lane == 0) c = atomicAdd(a.work, 1ull);
+      return (int64_t)__shfl_sync(0xffffffffu, c, 0);
+    }
+    return warp0 + (claimed++) * n_warps;
+  };
+  int qn = 0, qseg = 0;  // warp-uniform: queue length and its segment
+  int cseg = 0;          // segment of the current chunk
+  int64_t tile = 0, tile_end = 0;
+  bool done = false;
+  static_assert(CHUNK == 1 || CHUNK == PHS_CHUNK_TILES, "chunks of 1 or PHS_CHUNK_TILES tiles");
+  auto claim = [&]() {
+    const int64_t c = next_chunk();
+    done = c >= (CHUNK == 1 ? a.n_tiles : a.n_chunks);
+    if (done) return;
+    int lo = 0, hi = a.n_segments - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if ((CHUNK == 1 ? segs[mid].tile_begin : segs[mid].chunk_begin) <= c) lo = mid; else hi = mid - 1;
+    }
+    cseg = lo;
+    if (CHUNK == 1) {
+      tile = c;
+      tile_end = c + 1;
+      return;
+    }
+    const int64_t seg_tiles = (segs[lo].ev_count + 31) / 32;
+    tile = segs[lo].tile_begin + (c - segs[lo].chunk_begin) * CHUNK;
+    const int64_t end = tile + CHUNK, seg_end = segs[lo].tile_begin + seg_tiles;
+    tile_end = end < seg_end ? end : seg_end;
+  };
+  claim();
+  for (;;) {
+    bool passed = false;
+    int64_t local = 0;
+    if (!done) {
+      local = (tile - segs[cseg].tile_begin) * 32 + lane;
+      if (local < segs[cseg].ev_count) passed = pass_a(segs[cseg], local);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, passed);
+    // stage 0: drain the queue (end of the work, or a new segment); 1: append; 2: drain
+    // full warps
+    int stage = (done || (m != 0 && qn > 0 && qseg != cseg)) ? 0 : 1;
+    for (;;) {
+      int take;
+      if (stage == 0) {
+        if (qn == 0) { stage = 1; continue; }
+        take = qn < 32 ? qn : 32;
+      } else if (stage == 1) {
+        if (m != 0) {
+          if (passed) q[qn + __popc(m & ((1u << lane) - 1u))] = local;
+          qn += __popc(m);
+          qseg = cseg;
+        }
+        stage = 2;
+        continue;
+      } else {
+        if (qn < 32) break;
+        take = 32;
+      }
+      __syncwarp();
+      const int64_t l = lane < take ? q[qn - take + lane] : -1;
+      __syncwarp();
+      qn -= take;
+      if (l >= 0) pass_b(segs[qseg], l);
+    }
+    if (done) break;
+    if (++tile == tile_end) claim();
+  }
+}
+
 }  // namespace

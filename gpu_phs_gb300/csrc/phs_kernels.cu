@@ -16,26 +16,38 @@
 
 namespace {
 
-template <bool PER_EVENT>
-__global__ void __launch_bounds__(PHS_FWD_BLOCK, 4)
+// COMPACT: events whose kinematic test fails need no angles or boosts.  Where many fail
+// (low ok fractions: multi-channel batches, hard cuts), pass A tests each event, writes
+// the failures, and queues the rest per warp; pass B runs them densely.  Where nearly all
+// pass, the plain loop avoids the second msq evaluation; the launcher times both.
+template <bool PER_EVENT, bool COMPACT, int MIN_BLOCKS>
+__global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
     phs_forward_f64_kernel(const __grid_constant__ PhsLaunch a) {
   extern __shared__ double smem[];
   const int lane = threadIdx.x & 31;
   const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-
-  for (int64_t tile = warp0; tile < a.n_tiles; tile += n_warps) {
-    // the segment holding this tile (warp-uniform binary search on tile_begin)
-    const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
-    int lo = 0, hi = a.n_segments - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (segs[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+  if constexpr (COMPACT) {
+    int64_t *q = reinterpret_cast<int64_t *>(smem + (size_t)a.stack_depth * PHS_STATE * PHS_FWD_BLOCK) +
+                 (threadIdx.x >> 5) * 64;
+    compacting_loop<PHS_CHUNK_TILES>(
+        a, q,
+        [&](const PhsSegment &sg, int64_t loc) { return phs_ok_f64<PER_EVENT>(a, sg, loc, smem); },
+        [&](const PhsSegment &sg, int64_t loc) { phs_event_f64<PER_EVENT>(a, sg, loc, smem); });
+  } else {
+    for (int64_t tile = warp0; tile < a.n_tiles; tile += n_warps) {
+      // the segment holding this tile (warp-uniform binary search on tile_begin)
+      const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
+      int lo = 0, hi = a.n_segments - 1;
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (segs[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+      }
+      const PhsSegment seg = segs[lo];
+      const int64_t local = (tile - seg.tile_begin) * 32 + lane;
+      if (local >= seg.ev_count) continue;
+      phs_event_f64<PER_EVENT>(a, seg, local, smem);
     }
-    const PhsSegment seg = segs[lo];
-    const int64_t local = (tile - seg.tile_begin) * 32 + lane;
-    if (local >= seg.ev_count) continue;
-    phs_event_f64<PER_EVENT>(a, seg, local, smem);
   }
 }
 
@@ -96,26 +108,53 @@ cudaError_t phs_launch_fma_rate(void *out, int fp64, int blocks, int threads, in
 }
 
 size_t phs_forward_smem_bytes(int stack_depth) {
-  return (size_t)stack_depth * PHS_STATE * PHS_FWD_BLOCK * sizeof(double);
+  // frame stack, then the compacting variant's per-warp queues (64 events per warp)
+  return (size_t)stack_depth * PHS_STATE * PHS_FWD_BLOCK * sizeof(double) +
+         (size_t)(PHS_FWD_BLOCK / 32) * 64 * sizeof(int64_t);
 }
 
-int phs_forward_blocks_per_sm(int stack_depth, bool per_event) {
+// variant 0: one pass, registers for 4 resident blocks per SM; 1: compacting, 4 blocks;
+// 2: compacting, 3 blocks (no spills).
+template <bool PER_EVENT>
+static const void *f64_kernel(int variant) {
+  switch (variant) {
+    case 1: return (const void *)phs_forward_f64_kernel<PER_EVENT, true, 4>;
+    case 2: return (const void *)phs_forward_f64_kernel<PER_EVENT, true, 3>;
+    default: return (const void *)phs_forward_f64_kernel<PER_EVENT, false, 4>;
+  }
+}
+
+int phs_forward_blocks_per_sm(int stack_depth, bool per_event, int variant) {
   int n = 0;
-  size_t smem = phs_forward_smem_bytes(stack_depth);
-  if (per_event)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phs_forward_f64_kernel<true>, PHS_FWD_BLOCK, smem);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phs_forward_f64_kernel<false>, PHS_FWD_BLOCK, smem);
+  const size_t smem = phs_forward_smem_bytes(stack_depth);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &n, per_event ? f64_kernel<true>(variant) : f64_kernel<false>(variant), PHS_FWD_BLOCK, smem);
   return n > 0 ? n : 1;
 }
 
-cudaError_t phs_launch_forward_f64(const PhsLaunch &a, int n_blocks, cudaStream_t stream) {
+template <bool PER_EVENT>
+static void launch_f64(const PhsLaunch &a, int n_blocks, int variant, size_t smem,
+                       cudaStream_t stream) {
+  switch (variant) {
+    case 1:
+      phs_forward_f64_kernel<PER_EVENT, true, 4><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+      break;
+    case 2:
+      phs_forward_f64_kernel<PER_EVENT, true, 3><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+      break;
+    default:
+      phs_forward_f64_kernel<PER_EVENT, false, 4><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+  }
+}
+
+cudaError_t phs_launch_forward_f64(const PhsLaunch &a, int n_blocks, int variant,
+                                   cudaStream_t stream) {
   if (a.n_tiles <= 0) return cudaSuccess;
-  size_t smem = phs_forward_smem_bytes(a.stack_depth);
+  const size_t smem = phs_forward_smem_bytes(a.stack_depth);
   if (a.E1 && a.E2)
-    phs_forward_f64_kernel<true><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+    launch_f64<true>(a, n_blocks, variant, smem, stream);
   else
-    phs_forward_f64_kernel<false><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+    launch_f64<false>(a, n_blocks, variant, smem, stream);
   return cudaGetLastError();
 }
 
@@ -185,6 +224,6 @@ cudaError_t phs_launch_forward_f64_noalloc(PhsLaunch a, const PhsChannel *channe
   a.n_segments = n_segments;
   if (a.n_tiles <= 0) return cudaSuccess;
   const size_t smem = phs_forward_smem_bytes(a.stack_depth);
-  phs_forward_f64_kernel<false><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+  phs_forward_f64_kernel<false, false, 4><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
   return cudaGetLastError();
 }

@@ -292,9 +292,120 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
   return true;
 }
 
-// MIN_BLOCKS: resident blocks per SM the register allocation targets (the autotuner in
-// phs_api.cpp picks the faster instantiation per process).
-template <int MIN_BLOCKS>
+// Pass A of the compacting variant, in plain FP32 with error bounds.  It only ever decides
+// that an event FAILS.  Each internal msq is evaluated in FP32 together with a bound on its
+// absolute error, 64 FP32 epsilons times the magnitudes of the terms it is made of (the
+// Breit-Wigner tails through the same cot reformulation as the float-float path, whose
+// tan error grows with 1 + tan^2; the exponential mappings through expm1f, whose error
+// grows with the exponent): the reference's FP64 msq, and the exact one, lie inside
+// [msq - e, msq + e].  Masses are then intervals, and a test fails here only if it fails
+// for every value in them (with a further 1e-6 relative slack for the FP64 roundings of
+// the reference's own sums and bounds), so such an event fails the reference's test too.
+// Its outputs are written here.  Every other event goes to pass B, whose float-float /
+// FP64 walk decides its flag exactly.  Returns false for a failed event.
+#define PHS_F32_EPS_BOUND (64.0f * 5.9604645e-8f)
+__device__ __forceinline__ float msq_f32(const PhsChildFF &C, double xd, float &e) {
+  const float x = (float)xd, k = PHS_F32_EPS_BOUND;
+  switch (C.map_id) {
+    case PHS_MAP_NO:
+      e = k * (fabsf(C.msq_min.hi) + fabsf(C.msq_max.hi));
+      return C.msq_min.hi + x * (C.msq_max.hi - C.msq_min.hi);
+    case PHS_MAP_SCHANNEL: {
+      const float z = C.a0.hi + x * C.a1.hi;  // a1 holds a1 - a0
+      float t;
+      if (z > 0.78539816f)
+        t = 1.0f / tanf(C.u1.hi + (float)(1.0 - xd) * C.a1.hi);
+      else if (z < -0.78539816f)
+        t = -1.0f / tanf(C.u0.hi + x * C.a1.hi);
+      else
+        t = tanf(z);
+      e = k * (fabsf(C.m2.hi) + fabsf(C.mw.hi) * (1.0f + t * t));
+      return C.m2.hi + C.mw.hi * t;
+    }
+    case PHS_MAP_COLLINEAR:
+    case PHS_MAP_INFRARED:
+    case PHS_MAP_RADIATION: {
+      const float y = x * C.a1.hi, em = expm1f(y);
+      e = k * (fabsf(C.msq_min.hi) + fabsf(C.a0.hi) * (em + 1.0f) * (1.0f + fabsf(y)));
+      return C.a0.hi * em + C.msq_min.hi;
+    }
+    case PHS_MAP_TCHANNEL:
+    case PHS_MAP_UCHANNEL: {
+      const bool lower = xd < 0.5;
+      const float y = (lower ? x : (float)(1.0 - xd)) * C.a1.hi, em = expm1f(y);
+      e = k * (fabsf(lower ? C.msq_min.hi : C.msq_max.hi) +
+               fabsf(C.a0.hi) * (em + 1.0f) * (1.0f + fabsf(y)));
+      return lower ? C.a0.hi * em + C.msq_min.hi : C.msq_max.hi - C.a0.hi * em;
+    }
+  }
+  e = INFINITY;
+  return 0.0f;
+}
+
+__device__ __forceinline__ bool phs_ok_f32(const PhsLaunch &a, const PhsSegment &seg,
+                                           int64_t local, float *fst) {
+  const PhsChannelFF &ch = a.channels_ff[seg.channel];
+  if (ch.exact_only) return true;
+  const double *xe = a.x + seg.x_base + local * seg.x_stride;
+  const float up = 1.0f + 1e-6f, dn = 1.0f - 1e-6f;
+  float mlo_b = ch.sqrts.hi * dn, mhi_b = ch.sqrts.hi * up, mmax_b = ch.sqrts.hi;
+  bool fails = false;
+  int sp = 0;
+  const int n_visits = ch.n_visits;
+  for (int v = 0; v < n_visits && !fails; v++) {
+    const PhsVisitFF &V = ch.visit[v];
+    float lo[2], hi[2], cmax[2];
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const PhsChildFF &C = V.child[j];
+      if (!C.internal) {
+        lo[j] = C.m_leaf.hi * dn;
+        hi[j] = C.m_leaf.hi * up;
+        cmax[j] = 0.0f;
+      } else {
+        float e;
+        const float msq = msq_f32(C, xe[C.x_msq], e);
+        fails = fails || msq + e < 0.0f;                // negative for certain: not ok
+        lo[j] = sqrtf(fmaxf(msq - e, 0.0f)) * dn;       // NaN bounds decide nothing
+        hi[j] = sqrtf(fmaxf(msq + e, 0.0f)) * up;
+        cmax[j] = C.m_max.hi;
+      }
+    }
+    fails = fails || mhi_b < (lo[0] + lo[1]) * dn;     // below threshold for certain
+    if (!V.self_root) fails = fails || mlo_b > mmax_b * up;  // above the bound for certain
+    if (V.push >= 0) {
+      const bool j0 = V.push == 0;
+      fstack_store(fst, sp, 17, ff_make(j0 ? lo[0] : lo[1], j0 ? hi[0] : hi[1]));
+      fstack_store(fst, sp, 19, ff_make(j0 ? cmax[0] : cmax[1], 0.0f));
+      sp++;
+    }
+    if (V.carry >= 0) {
+      const bool j0 = V.carry == 0;
+      mlo_b = j0 ? lo[0] : lo[1];
+      mhi_b = j0 ? hi[0] : hi[1];
+      mmax_b = j0 ? cmax[0] : cmax[1];
+    } else if (sp > 0) {
+      sp--;
+      const ff t = fstack_load(fst, sp, 17);
+      mlo_b = t.hi;
+      mhi_b = t.lo;
+      mmax_b = fstack_load(fst, sp, 19).hi;
+    }
+  }
+  if (!fails) return true;
+  const int64_t ev = seg.ev_begin + local;
+  a.volume[ev] = ch.volume;
+  a.factor[ev * a.factor_stride + seg.factor_col] = 0.0;
+  a.ok[ev] = 0;
+  double2 *o = reinterpret_cast<double2 *>(a.p + seg.p_base + local * 4 * (int64_t)ch.n_out);
+  for (int i = 0; i < 2 * ch.n_out; i++) o[i] = make_double2(0.0, 0.0);
+  return false;
+}
+
+// MIN_BLOCKS: resident blocks per SM the register allocation targets; COMPACT: the
+// two-pass form of phs_kernels.cu (pass A, here in FP32, settles the events that clearly
+// fail; pass B computes the rest densely).  The autotuner in phs_api.cpp picks the faster instantiation per process.
+template <int MIN_BLOCKS, bool COMPACT>
 __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
     phs_forward_ff_kernel(const __grid_constant__ PhsLaunch a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -326,17 +437,29 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
   const int lane = threadIdx.x & 31;
   const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t tile = warp0; tile < a.n_tiles; tile += n_warps) {
-    const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
-    int lo = 0, hi = a.n_segments - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (segs[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+  if constexpr (COMPACT) {
+    int64_t *q = reinterpret_cast<int64_t *>(smem_raw + sizeof(FFTables) +
+                                             (size_t)a.stack_depth * PHS_STATE * PHS_FWD_BLOCK * sizeof(double)) +
+                 (threadIdx.x >> 5) * 64;
+    compacting_loop<1>(
+        a, q,
+        [&](const PhsSegment &sg, int64_t loc) { return phs_ok_f32(a, sg, loc, fst); },
+        [&](const PhsSegment &sg, int64_t loc) {
+          if (!phs_event_ff(a, sg, loc, T, fst)) phs_event_f64<false>(a, sg, loc, dst);
+        });
+  } else {
+    for (int64_t tile = warp0; tile < a.n_tiles; tile += n_warps) {
+      const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
+      int lo = 0, hi = a.n_segments - 1;
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (segs[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+      }
+      const PhsSegment seg = segs[lo];
+      const int64_t local = (tile - seg.tile_begin) * 32 + lane;
+      if (local >= seg.ev_count) continue;
+      if (!phs_event_ff(a, seg, local, T, fst)) phs_event_f64<false>(a, seg, local, dst);
     }
-    const PhsSegment seg = segs[lo];
-    const int64_t local = (tile - seg.tile_begin) * 32 + lane;
-    if (local >= seg.ev_count) continue;
-    if (!phs_event_ff(a, seg, local, T, fst)) phs_event_f64<false>(a, seg, local, dst);
   }
 }
 
@@ -346,25 +469,35 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
 // FP64 frames are the larger ones).
 static_assert(PHS_STATE * 2 >= PHS_FF_STATE, "FP64 frame must be at least the float-float frame");
 size_t phs_forward_ff_smem_bytes(int stack_depth) {
-  return sizeof(FFTables) + (size_t)stack_depth * PHS_STATE * PHS_FWD_BLOCK * sizeof(double);
+  return sizeof(FFTables) + (size_t)stack_depth * PHS_STATE * PHS_FWD_BLOCK * sizeof(double) +
+         (size_t)(PHS_FWD_BLOCK / 32) * 64 * sizeof(int64_t);
+}
+
+// variant bit 0: register budget for 4 (1) or 3 (0) resident blocks; bit 1: compacting.
+static const void *ff_kernel(int variant) {
+  switch (variant) {
+    case 1: return (const void *)phs_forward_ff_kernel<4, false>;
+    case 2: return (const void *)phs_forward_ff_kernel<3, true>;
+    case 3: return (const void *)phs_forward_ff_kernel<4, true>;
+    default: return (const void *)phs_forward_ff_kernel<3, false>;
+  }
 }
 
 int phs_forward_ff_blocks_per_sm(int stack_depth, int variant) {
   int n = 0;
-  const size_t smem = phs_forward_ff_smem_bytes(stack_depth);
-  if (variant == 1)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phs_forward_ff_kernel<4>, PHS_FWD_BLOCK, smem);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phs_forward_ff_kernel<3>, PHS_FWD_BLOCK, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ff_kernel(variant), PHS_FWD_BLOCK,
+                                                phs_forward_ff_smem_bytes(stack_depth));
   return n > 0 ? n : 1;
 }
 
 cudaError_t phs_launch_forward_ff(const PhsLaunch &a, int n_blocks, int variant, cudaStream_t stream) {
   if (a.n_tiles <= 0) return cudaSuccess;
   const size_t smem = phs_forward_ff_smem_bytes(a.stack_depth);
-  if (variant == 1)
-    phs_forward_ff_kernel<4><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
-  else
-    phs_forward_ff_kernel<3><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+  switch (variant) {
+    case 1: phs_forward_ff_kernel<4, false><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a); break;
+    case 2: phs_forward_ff_kernel<3, true><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a); break;
+    case 3: phs_forward_ff_kernel<4, true><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a); break;
+    default: phs_forward_ff_kernel<3, false><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+  }
   return cudaGetLastError();
 }

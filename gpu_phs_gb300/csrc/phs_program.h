@@ -106,7 +106,11 @@ struct PhsSegment {
   int64_t tile_begin;   // first warp tile of this segment (prefix sum)
   int32_t x_stride;     // x row length (>= n_x_used)
   int32_t factor_col;   // column added to the factor index (whizard: own channel)
+  int64_t chunk_begin;  // first work chunk of this segment for the compacting FP64 kernel:
+                        // chunks of PHS_CHUNK_TILES tiles never cross a segment boundary
 };
+
+#define PHS_CHUNK_TILES 8
 
 // ------------------------------------------------------------------------------------
 // Float-float form of a channel program, for the FP32-pipe kernel: every constant is a

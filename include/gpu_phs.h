@@ -89,10 +89,19 @@ int phs_process_set_beams(phs_process_t proc, double E1, double E2);
  * beams always use FP64.  No counterpart in the reference (FP64 only). */
 int phs_process_set_precision(phs_process_t proc, int precision);
 
-/* The FP32-pair kernel's autotuned variant (register budget for 3 or 4 resident blocks per
- * SM: 0 or 1), or -1 before the first launch of at least 2^18 events has timed them.  The
- * variants compute identical bits.  Tuning needs that first launch outside stream capture. */
-int phs_process_tuning(phs_process_t proc, int *ff_variant);
+/* The autotuned kernel variants of the handle's uniform-beam launches, or -1 before the
+ * first launch of at least 2^18 events (outside stream capture) has timed them.  FP32 pair
+ * (ff_variant): bit 0 register budget for 4 (1) or 3 (0) resident blocks per SM, bit 1 the
+ * compacting two-pass form.  FP64 (f64_variant): 0 one pass, 1 and 2 compacting (registers
+ * for 4 or 3 resident blocks).  The compacting
+ * form tests every event first and computes only the passing ones, densely; it wins where
+ * many events fail the kinematic test.  Variants compute identical bits.  Either pointer
+ * may be NULL. */
+int phs_process_tuning(phs_process_t proc, int *ff_variant, int *f64_variant);
+
+/* Pins the kernel variants (values as phs_process_tuning reports; -1 re-enables tuning), for
+ * reproducible timings or to skip the tuning launches. */
+int phs_process_set_variants(phs_process_t proc, int ff_variant, int f64_variant);
 
 /* Sizes: any pointer may be NULL. */
 int phs_process_info(phs_process_t proc, int *n_in, int *n_out, int *n_channels, int *n_x,
@@ -174,6 +183,10 @@ int phs_batch_info(phs_batch_t batch, int *n_channels, int64_t *x_stride_sum, in
 int phs_batch_generate_device(phs_batch_t batch, const int64_t *counts, const double *x,
                               double *p, double *factors, double *volumes, uint8_t *oks,
                               void *stream);
+
+/* Kernel variants of the batch's launches, tuned and pinned as for a process. */
+int phs_batch_tuning(phs_batch_t batch, int *ff_variant, int *f64_variant);
+int phs_batch_set_variants(phs_batch_t batch, int ff_variant, int f64_variant);
 
 /* Arithmetic of the batch's launches (PHS_PRECISION_F64 or PHS_PRECISION_F32X2). */
 int phs_batch_set_precision(phs_batch_t batch, int precision);

@@ -69,3 +69,58 @@ def test_process_graph_replay(torch):
     g.launch()
     torch.cuda.synchronize()
     assert torch.equal(out.p, ref.p) and torch.equal(out.ok, ref.ok)
+
+
+def _gen_batch(torch, spaces, counts, x, prec, ff_v=-1, f64_v=-1):
+    from gpu_phs_gb300.api import Batch
+    batch = Batch(spaces)
+    batch.set_precision(prec)
+    batch.set_variants(ff_v, f64_v)
+    out = batch.generate(x, counts)
+    torch.cuda.synchronize()
+    return [t.clone() for t in out]
+
+
+@pytest.mark.parametrize("prec,n_var", [(0, 3), (1, 4)])
+def test_kernel_variants_identical_bits(torch, prec, n_var):
+    """Every kernel variant (register budgets, one-pass or compacting) computes the same
+    bits: the compacting form's pass B runs the same event code, and its pass A writes the
+    outputs of failing events exactly as the one-pass form does."""
+    from gpu_phs_gb300.api import Batch, PhaseSpace, philox_fill
+    procs, counts = P.batched(seed=2024, n_channels=64, total_events=1 << 19)
+    spaces = [PhaseSpace(p, 500.0, 500.0) for p in procs]
+    xo, _ = Batch(spaces).offsets(counts)
+    x = torch.empty(int(xo[-1]), dtype=torch.float64, device="cuda")
+    philox_fill(x, int(xo[-1]), 1, seed=6)
+    kw = (lambda v: dict(ff_v=v)) if prec else (lambda v: dict(f64_v=v))
+    ref = _gen_batch(torch, spaces, counts, x, prec, **kw(0))
+    assert 0.1 < ref[3].double().mean().item() < 0.5   # many events fail: compaction matters
+    for v in range(1, n_var):
+        got = _gen_batch(torch, spaces, counts, x, prec, **kw(v))
+        for a, b in zip(ref, got):
+            assert torch.equal(a, b), f"variant {v} differs from variant 0"
+
+
+@pytest.mark.parametrize("f64_v", [1, 2])
+def test_compacting_fp64_vs_oracle_low_ok_fraction(torch, f64_v):
+    """The 13 TeV configuration (about 4% of events pass) through a compacting variant,
+    against the oracle."""
+    from conftest import momentum_rel_err
+    from gpu_phs_gb300.api import PhaseSpace
+    from gpu_phs_gb300.philox import uniform_x
+    from oracle import oracle
+    proc = P.precision()
+    n = 100_000
+    x = uniform_x(77, n, proc.n_x)
+    ps = PhaseSpace(proc, proc.sqrts / 2, proc.sqrts / 2)
+    ps.set_variants(-1, f64_v)
+    ev = ps.generate(torch.from_numpy(x).cuda())
+    p, f, v, ok = (t.cpu().numpy() for t in (ev.p, ev.factor, ev.volume, ev.ok))
+    r = oracle.Oracle(proc, proc.sqrts).generate(x)
+    assert np.array_equal(ok, r.ok)
+    sel = r.ok == 1
+    assert 0.01 < sel.mean() < 0.1
+    assert momentum_rel_err(p[sel], r.p[sel], proc.sqrts).max() <= 1e-12
+    assert (np.abs(f[sel] / r.factor[sel] - 1)).max() <= 1e-12
+    assert np.all(p[~sel] == 0) and np.all(f[~sel] == 0)
+    assert np.allclose(v, r.volume, rtol=1e-15, atol=0)
