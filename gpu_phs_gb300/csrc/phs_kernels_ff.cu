@@ -311,14 +311,14 @@ __device__ __forceinline__ float msq_f32(const PhsChildFF &C, double xd, float &
       e = k * (fabsf(C.msq_min.hi) + fabsf(C.msq_max.hi));
       return C.msq_min.hi + x * (C.msq_max.hi - C.msq_min.hi);
     case PHS_MAP_SCHANNEL: {
+      // one tanf per lane, on z or on pi/2 -+ z (selected, not branched: lanes of a warp
+      // take different sides)
       const float z = C.a0.hi + x * C.a1.hi;  // a1 holds a1 - a0
-      float t;
-      if (z > 0.78539816f)
-        t = 1.0f / tanf(C.u1.hi + (float)(1.0 - xd) * C.a1.hi);
-      else if (z < -0.78539816f)
-        t = -1.0f / tanf(C.u0.hi + x * C.a1.hi);
-      else
-        t = tanf(z);
+      const bool hi_side = z > 0.78539816f, lo_side = z < -0.78539816f;
+      const float w = hi_side ? C.u1.hi + (float)(1.0 - xd) * C.a1.hi
+                              : (lo_side ? C.u0.hi + x * C.a1.hi : z);
+      const float tw = tanf(w);
+      const float t = hi_side ? 1.0f / tw : (lo_side ? -1.0f / tw : tw);
       e = k * (fabsf(C.m2.hi) + fabsf(C.mw.hi) * (1.0f + t * t));
       return C.m2.hi + C.mw.hi * t;
     }
