@@ -582,6 +582,62 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+PROFILE_CASES = ("f64_tt", "f64_batched", "ff_batched", "inverse_bwbw", "adjoint_tt")
+
+
+def run_case(name: str) -> None:
+    """Small workloads for ncu captures of one kernel each (a few hundred MB on the device,
+    inputs still larger than L2): two launches of the kernel, the second is the one to
+    capture (ncu -k <kernel> -s 1 -c 1)."""
+    import torch
+    from gpu_phs_gb300 import processes as P
+    from gpu_phs_gb300.api import Batch, PhaseSpace, philox_fill, philox_x
+    if name == "f64_tt":              # 2^21 tt events, FP64 one pass
+        proc = P.tt()
+        n = 1 << 21
+        ps = PhaseSpace(proc, 500.0, 500.0)
+        ps.set_variants(-1, 0)
+        x = philox_x(n, proc.n_x, SEED)
+        o = ps.alloc(n)
+        for _ in range(2):
+            ps.generate(x, out=o)
+    elif name in ("f64_batched", "ff_batched"):   # 2^22 batched events, compacting
+        procs, counts = P.batched(seed=2024, n_channels=64, total_events=1 << 22)
+        b = Batch([PhaseSpace(p, 500.0, 500.0) for p in procs])
+        if name == "ff_batched":
+            b.set_precision(1)
+            b.set_variants(3, -1)
+        else:
+            b.set_variants(-1, 2)
+        xo, _ = b.offsets(counts)
+        x = torch.empty(int(xo[-1]), dtype=torch.float64, device="cuda")
+        philox_fill(x, int(xo[-1]), 1, SEED)
+        for _ in range(2):
+            b.generate(x, counts)
+    elif name == "inverse_bwbw":      # 2^17 bwbw events x 61 channels
+        proc = whizard_process("bwbw")
+        n = 1 << 17
+        counts = np.full(proc.n_channels, n // proc.n_channels, np.int64)
+        counts[: n - int(counts.sum())] += 1
+        ps = PhaseSpace(proc, 500.0, 500.0)
+        ps.set_variants(-1, 0)
+        x = philox_x(n, proc.n_x, SEED)
+        ev = ps.generate(x, counts)
+        for _ in range(2):
+            ps.inverse(ev.p, counts, ev.ok, x, ev.factor)
+    elif name == "adjoint_tt":        # 2^20 tt events
+        proc = P.tt()
+        n = 1 << 20
+        ps = PhaseSpace(proc, 500.0, 500.0)
+        x = philox_x(n, proc.n_x, SEED)
+        g = torch.Generator(device="cuda").manual_seed(SEED)
+        pbar = torch.randn((n, proc.n_out, 4), dtype=torch.float64, device="cuda", generator=g)
+        jbar = torch.randn(n, dtype=torch.float64, device="cuda", generator=g)
+        for _ in range(2):
+            ps.vjp(x, pbar, jbar)
+    torch.cuda.synchronize()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -594,7 +650,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--case", choices=PROFILE_CASES, default=None,
+                    help="run one small profiling workload instead of the benchmark")
     args = ap.parse_args()
+    if args.case:
+        run_case(args.case)
+        return
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
