@@ -448,13 +448,16 @@ def run_ours(args):
 
     from gpu_phs_gb300 import _lib
     from gpu_phs_gb300.api import PhaseSpace, philox_fill
+    from gpu_phs_gb300.replicas import event_window, max_over_ranks
 
     proc, n = workload(args.config)
     if args.events:
         n = args.events
     ps = PhaseSpace(proc, proc.sqrts / 2, proc.sqrts / 2)
     x = torch.empty((n, proc.n_x), dtype=torch.float64, device="cuda")
-    philox_fill(x, n, proc.n_x, SEED, first_event=rank * n)
+    # weak scaling: n events per rank, rank r's window of one Philox stream
+    first, _ = event_window(rank, world, n * world)
+    philox_fill(x, n, proc.n_x, SEED, first_event=first)
     out = ps.alloc(n)
     stream = torch.cuda.current_stream()
 
@@ -484,10 +487,7 @@ def run_ours(args):
     barrier()
     total_ms = t_all0.elapsed_time(t_all1)
     kern_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_per_step = t.item() / args.steps
+    ms_per_step = max_over_ranks(total_ms) / args.steps
     value = world * n / (ms_per_step * 1e-3)
     clocks = clk.summary()
 
@@ -503,14 +503,14 @@ def run_ours(args):
     _lib.check(lib.phs_measure_fma_peak(1, C.byref(g64)))
     fp64_peak = g64.value
     fp64_achieved = fpe * n / (launch_ms * 1e-3) / 1e9
-    traffic = None
+    traffic, pipe_pct = None, None
     prof = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(prof):
         with open(prof) as fh:
-            tj = json.load(fh)
-        per_ev = tj.get(proc.name, {}).get("dram_bytes_per_event")
-        if per_ev:
-            traffic = per_ev * n
+            tj = json.load(fh).get(proc.name, {})
+        if tj.get("dram_bytes_per_event"):
+            traffic = tj["dram_bytes_per_event"] * n
+        pipe_pct = tj.get("fp64_pipe_pct_of_peak")
 
     # end to end through the host-pointer C entry point (pinned buffers)
     e2e = None
@@ -528,11 +528,8 @@ def run_ours(args):
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
             ps.generate_host(xh, out=outh)
-        el = time.perf_counter() - t0
-        te = torch.tensor([el], device="cuda", dtype=torch.float64)
-        if world > 1:
-            dist.all_reduce(te, op=dist.ReduceOp.MAX)
-        e2e = {"value": world * n * e2e_steps / te.item(), "unit": "events/s",
+        el = max_over_ranks(time.perf_counter() - t0)
+        e2e = {"value": world * n * e2e_steps / el, "unit": "events/s",
                "h2d_bytes_per_step": n * proc.n_x * 8,
                "d2h_bytes_per_step": n * (32 * proc.n_out + 8 + 8 + 1),
                "path": "phs_generate_host (C ABI), pinned host buffers, 1 Mi-event chunks on 2 streams",
@@ -570,7 +567,12 @@ def run_ours(args):
                          "kernel_ms": launch_ms,
                          "fp64": {"achieved_gflops": fp64_achieved, "peak_gflops": fp64_peak,
                                   "frac": fp64_achieved / fp64_peak, "flops_per_event": fpe,
-                                  "peak_kind": "measured (phs_measure_fma_peak, DFMA chains)"}},
+                                  "peak_kind": "measured (phs_measure_fma_peak, DFMA chains)",
+                                  "pipe_utilization_ncu": pipe_pct / 100 if pipe_pct else None,
+                                  "note": "the binding roof: frac counts each transcendental "
+                                          "as one operation; ncu's FP64-pipe utilisation "
+                                          "(profiles/fwd_f64_tt_ncu.md) counts the "
+                                          "instructions the library math expands into"}},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "variants": variants,
