@@ -71,12 +71,15 @@ struct Segments {
   DevBuf dev;
   std::vector<PhsSegment> uploaded;  // content of dev
   DevBuf work;                       // chunk counter of the compacting kernels
+  DevBuf exact_n, exact_q;           // FP32-pair launches: the exact-path queue
   int64_t n_tiles = 0;
   int64_t n_chunks = 0;
   int64_t n_events = 0;
   void release() {
     dev.release();
     work.release();
+    exact_n.release();
+    exact_q.release();
     uploaded.clear();
   }
 };
@@ -213,14 +216,23 @@ int launch_tuned(int &variant, int n_variants, int64_t n_events, cudaStream_t st
   return PHS_OK;
 }
 
-int launch_ff_tuned(int &variant, const PhsLaunch &a, int device, int depth, int64_t n_events,
-                    cudaStream_t st) {
+// FP32-pair launch: the float-float kernel, then the exact FP64 path over the events it
+// queued (a handful of blocks: they are about 0.1 % of the events, or all events of a
+// channel without a float-float form).
+int launch_ff_tuned(int &variant, Segments &S, PhsLaunch a, int device, int depth,
+                    int64_t n_events, cudaStream_t st) {
+  if (int rc = S.exact_n.reserve(sizeof(unsigned long long))) return rc;
+  if (int rc = S.exact_q.reserve((size_t)std::max<int64_t>(n_events, 1) * sizeof(uint64_t)))
+    return rc;
+  a.exact_count = S.exact_n.as<unsigned long long>();
+  a.exact_queue = S.exact_q.as<uint64_t>();
+  const int exact_grid = sm_count(device) * 2;
   return launch_tuned(variant, PHS_FF_VARIANTS, n_events, st, [&](int v) {
-    if (a.work) {
-      cudaError_t e = cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), st);
-      if (e != cudaSuccess) return e;
-    }
-    return phs_launch_forward_ff(a, grid_for_ff(a.n_tiles, device, depth, v), v, st);
+    cudaError_t e = cudaMemsetAsync(a.exact_count, 0, sizeof(unsigned long long), st);
+    if (e == cudaSuccess && a.work) e = cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), st);
+    if (e == cudaSuccess) e = phs_launch_forward_ff(a, grid_for_ff(a.n_tiles, device, depth, v), v, st);
+    if (e == cudaSuccess) e = phs_launch_forward_exact(a, exact_grid, st);
+    return e;
   });
 }
 
@@ -505,7 +517,7 @@ static int launch_process(phs_process_t h, Segments &S, int64_t n_events, const 
   if ((rc = attach_segments(S, a, stream))) return rc;
   if (a.n_tiles == 0) return PHS_OK;
   if (h->precision == PHS_PRECISION_F32X2 && E1 == nullptr)
-    return launch_ff_tuned(h->ff_variant, a, h->device, h->stack_depth, n_events, stream);
+    return launch_ff_tuned(h->ff_variant, S, a, h->device, h->stack_depth, n_events, stream);
   return launch_f64_tuned(h->f64_variant[E1 != nullptr], a, h->device, h->stack_depth, n_events,
                           stream);
 }
@@ -799,7 +811,7 @@ extern "C" int phs_batch_generate_device(phs_batch_t b, const int64_t *counts, c
   if ((rc = attach_segments(b->segs, a, (cudaStream_t)stream))) return rc;
   if (a.n_tiles == 0) return PHS_OK;
   if (b->precision == PHS_PRECISION_F32X2)
-    return launch_ff_tuned(b->ff_variant, a, b->device, b->stack_depth, n_events,
+    return launch_ff_tuned(b->ff_variant, b->segs, a, b->device, b->stack_depth, n_events,
                            (cudaStream_t)stream);
   return launch_f64_tuned(b->f64_variant, a, b->device, b->stack_depth, n_events,
                           (cudaStream_t)stream);

@@ -27,6 +27,8 @@ struct PhsLaunch {
   const double *E2;
   unsigned long long *work;    // compacting kernels: chunk counter, zeroed before the
                                // launch (warps claim chunks dynamically); null: static
+  unsigned long long *exact_count;  // FP32-pair launches: events queued for the exact
+  uint64_t *exact_queue;            //   FP64 path (segment << 40 | local), zeroed before
 };
 
 // Block size and resident blocks per SM of the forward kernel.
@@ -62,14 +64,17 @@ cudaError_t phs_launch_forward_f64_noalloc(PhsLaunch a, const PhsChannel *channe
 size_t phs_noalloc_scratch_bytes();
 
 // Forward launch on the FP32 pipe (float-float arithmetic), FP64 only for events within
-// 1e-5 of a kinematic limit, which are recomputed exactly (phs_kernels_ff.cu).  Needs
-// a.channels and a.channels_ff; uniform beams only.
+// 1e-5 of a kinematic limit, which it queues for phs_launch_forward_exact (phs_kernels_ff.cu).
+// Needs a.channels, a.channels_ff, a.exact_count (zeroed) and a.exact_queue (n events);
+// uniform beams only.
 // variant bit 0: registers for 4 (1) or 3 (0) resident blocks per SM; bit 1: the
 // compacting two-pass form (PHS_FF_VARIANTS in all).
 #define PHS_FF_VARIANTS 4
 cudaError_t phs_launch_forward_ff(const PhsLaunch &a, int n_blocks, int variant, cudaStream_t stream);
 int phs_forward_ff_blocks_per_sm(int stack_depth, int variant);
 size_t phs_forward_ff_smem_bytes(int stack_depth);
+// The exact FP64 path over the events an FP32-pair launch queued (a.exact_queue).
+cudaError_t phs_launch_forward_exact(const PhsLaunch &a, int n_blocks, cudaStream_t stream);
 
 // Reverse-mode derivatives (phs_adjoint.cu): xbar [event][x stride] and thbar
 // [event][th_stride] (d/dm, d/dGamma per Breit-Wigner branch, at 2 * its msq x index).

@@ -502,7 +502,7 @@ __device__ __forceinline__ bool phs_ok_f64(const PhsLaunch &a, const PhsSegment 
 // The persistent loop of the compacting kernels.  Each warp runs pass A on its 32-event
 // tiles (`pass_a(seg, local)` tests an event, writes it if it fails, and returns whether it
 // passed) and appends the passing events to its queue in shared memory (q: 64 slots);
-// pass B (`pass_b(seg, local)`, the full event) drains the queue 32 events at a time with
+// pass B (`pass_b(seg_index, seg, local)`, the full event) drains the queue 32 events at a time with
 // every lane busy.  The queue holds events of one segment only, so the visit program stays
 // warp-uniform: a tile of another segment first drains it.  Pass A and pass B have one
 // call site each, which keeps the (large) event code once in the kernel.
@@ -587,7 +587,7 @@ __device__ __forceinline__ void compacting_loop(const PhsLaunch &a, int64_t *q, 
       const int64_t l = lane < take ? q[qn - take + lane] : -1;
       __syncwarp();
       qn -= take;
-      if (l >= 0) pass_b(segs[qseg], l);
+      if (l >= 0) pass_b(qseg, segs[qseg], l);
     }
     if (done) break;
     if (++tile == tile_end) claim();

@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
     compacting_loop<PHS_CHUNK_TILES>(
         a, q,
         [&](const PhsSegment &sg, int64_t loc) { return phs_ok_f64<PER_EVENT>(a, sg, loc, smem); },
-        [&](const PhsSegment &sg, int64_t loc) { phs_event_f64<PER_EVENT>(a, sg, loc, smem); });
+        [&](int, const PhsSegment &sg, int64_t loc) { phs_event_f64<PER_EVENT>(a, sg, loc, smem); });
   } else {
     for (int64_t tile = warp0; tile < a.n_tiles; tile += n_warps) {
       // the segment holding this tile (warp-uniform binary search on tile_begin)
@@ -48,6 +48,25 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
       if (local >= seg.ev_count) continue;
       phs_event_f64<PER_EVENT>(a, seg, local, smem);
     }
+  }
+}
+
+// The exact FP64 path for the events the FP32-pair kernel queued (a.exact_queue: segment
+// index << 40 | event within the segment; *a.exact_count entries).  Those are events within
+// 1e-5 of a kinematic limit, and all events of channels whose mappings or boosts have no
+// float-float form; keeping their FP64 code out of the FP32-pair kernel keeps that
+// kernel's body small.  A grid-stride loop: the count is read on the device, so the launch
+// can sit in a CUDA graph behind the FP32-pair launch.
+__global__ void __launch_bounds__(PHS_FWD_BLOCK, 4)
+    phs_forward_exact_kernel(const __grid_constant__ PhsLaunch a) {
+  extern __shared__ double smem[];
+  const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
+  const int64_t n = (int64_t)*a.exact_count;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t e = a.exact_queue[i];
+    const PhsSegment seg = segs[e >> 40];
+    phs_event_f64<false>(a, seg, (int64_t)(e & ((1ull << 40) - 1)), smem);
   }
 }
 
@@ -155,6 +174,13 @@ cudaError_t phs_launch_forward_f64(const PhsLaunch &a, int n_blocks, int variant
     launch_f64<true>(a, n_blocks, variant, smem, stream);
   else
     launch_f64<false>(a, n_blocks, variant, smem, stream);
+  return cudaGetLastError();
+}
+
+cudaError_t phs_launch_forward_exact(const PhsLaunch &a, int n_blocks, cudaStream_t stream) {
+  if (a.n_tiles <= 0) return cudaSuccess;
+  phs_forward_exact_kernel<<<n_blocks, PHS_FWD_BLOCK, phs_forward_smem_bytes(a.stack_depth),
+                             stream>>>(a);
   return cudaGetLastError();
 }
 

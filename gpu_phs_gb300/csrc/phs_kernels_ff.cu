@@ -30,10 +30,7 @@ namespace {
 __device__ __forceinline__ ff ld(const PhsFF &c) { return ff_make(c.hi, c.lo); }
 __device__ __forceinline__ ff ffsel(bool c, ff a, ff b) { return c ? a : b; }
 
-// A float-float frame value takes one 8-byte slot, (depth * 20 + k) * block + thread, as a
-// double of the FP64 stack (phs_event_f64.cuh) does at (depth * 21 + k) * block + thread.
-// The two stacks share shared memory; in both layouts every slot of thread t has an index
-// = t (mod block), so a thread on the exact path never touches another thread's frames.
+// A float-float frame value takes one 8-byte slot, (depth * 20 + k) * block + thread.
 __device__ __forceinline__ void fstack_store(float *st, int depth, int k, ff v) {
   reinterpret_cast<float2 *>(st)[(depth * (PHS_FF_STATE / 2) + k) * PHS_FWD_BLOCK + threadIdx.x] =
       make_float2(v.hi, v.lo);
@@ -413,7 +410,11 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
   // the float-float frame stack and the FP64 one share memory (fstack_store): a thread
   // uses one at a time, and no slot of one thread overlaps another thread's
   float *fst = reinterpret_cast<float *>(smem_raw + sizeof(FFTables));
-  double *dst = reinterpret_cast<double *>(smem_raw + sizeof(FFTables));
+  // events the float-float walk cannot decide go to the exact FP64 launch behind this one
+  auto to_exact = [&](int si, int64_t loc) {
+    const unsigned long long slot = atomicAdd(a.exact_count, 1ull);
+    a.exact_queue[slot] = ((uint64_t)si << 40) | (uint64_t)loc;
+  };
 
   // reduction tables, exact at multiples of pi/2
   if (threadIdx.x < 64) {
@@ -439,13 +440,13 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   if constexpr (COMPACT) {
     int64_t *q = reinterpret_cast<int64_t *>(smem_raw + sizeof(FFTables) +
-                                             (size_t)a.stack_depth * PHS_STATE * PHS_FWD_BLOCK * sizeof(double)) +
+                                             (size_t)a.stack_depth * (PHS_FF_STATE / 2) * PHS_FWD_BLOCK * sizeof(float2)) +
                  (threadIdx.x >> 5) * 64;
     compacting_loop<1>(
         a, q,
         [&](const PhsSegment &sg, int64_t loc) { return phs_ok_f32(a, sg, loc, fst); },
-        [&](const PhsSegment &sg, int64_t loc) {
-          if (!phs_event_ff(a, sg, loc, T, fst)) phs_event_f64<false>(a, sg, loc, dst);
+        [&](int si, const PhsSegment &sg, int64_t loc) {
+          if (!phs_event_ff(a, sg, loc, T, fst)) to_exact(si, loc);
         });
   } else {
     for (int64_t tile = warp0; tile < a.n_tiles; tile += n_warps) {
@@ -458,18 +459,15 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
       const PhsSegment seg = segs[lo];
       const int64_t local = (tile - seg.tile_begin) * 32 + lane;
       if (local >= seg.ev_count) continue;
-      if (!phs_event_ff(a, seg, local, T, fst)) phs_event_f64<false>(a, seg, local, dst);
+      if (!phs_event_ff(a, seg, local, T, fst)) to_exact(lo, local);
     }
   }
 }
 
 }  // namespace
 
-// The frame region holds either stack: PHS_STATE 8-byte slots per frame and thread (the
-// FP64 frames are the larger ones).
-static_assert(PHS_STATE * 2 >= PHS_FF_STATE, "FP64 frame must be at least the float-float frame");
 size_t phs_forward_ff_smem_bytes(int stack_depth) {
-  return sizeof(FFTables) + (size_t)stack_depth * PHS_STATE * PHS_FWD_BLOCK * sizeof(double) +
+  return sizeof(FFTables) + (size_t)stack_depth * (PHS_FF_STATE / 2) * PHS_FWD_BLOCK * sizeof(float2) +
          (size_t)(PHS_FWD_BLOCK / 32) * 64 * sizeof(int64_t);
 }
 
