@@ -36,6 +36,11 @@ _SIGS = {
     "phs_generate_host": (I, [P, I64, P, P, P, P, P, P]),
     "phs_adjoint_device": (I, [P, I64, P, P, P, P, P, P, P]),
     "phs_inverse_device": (I, [P, I64, P, P, P, P, P, P, P, P, P, P]),
+    "phs_grid_create": (I, [C.POINTER(P), I, I]),
+    "phs_grid_destroy": (I, [P]),
+    "phs_grid_sample_device": (I, [P, I64, P, C.c_uint64, I64, P, P]),
+    "phs_grid_update_device": (I, [P, I64, P, P, P, P]),
+    "phs_grid_weights": (I, [P, P]),
     "phs_generate_device_noalloc": (I, [P, D, D, I64, P, P, P, P, P, P, P]),
     "phs_batch_create": (I, [C.POINTER(P), I, P]),
     "phs_batch_destroy": (I, [P]),

@@ -290,6 +290,75 @@ def process_graph(ps: PhaseSpace, x, out: Events, counts=None) -> Graph:
     return g
 
 
+GRID_BINS = 10
+
+
+class Grid:
+    """Per-channel x grid of the warm-up (rng.cpp): weights [n_channels, n_x, 10] on the
+    device, uniform at first."""
+
+    def __init__(self, n_channels: int, n_x: int):
+        h = C.c_void_p()
+        check(load().phs_grid_create(C.byref(h), int(n_channels), int(n_x)))
+        self.h, self.n_channels, self.n_x = h, int(n_channels), int(n_x)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            load().phs_grid_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _counts(self, counts, n):
+        if counts is None:
+            if self.n_channels != 1:
+                raise ValueError("counts are required for a multi-channel grid")
+            return None
+        return np.ascontiguousarray(counts, np.int64)
+
+    def sample(self, n_events: int, counts=None, seed: int = 0, first_event: int = 0,
+               out=None, stream=None):
+        """x [n_events, n_x] (CUDA float64) drawn from each channel's grid."""
+        import torch
+        x = out if out is not None else torch.empty((n_events, self.n_x), dtype=torch.float64,
+                                                    device="cuda")
+        c = self._counts(counts, n_events)
+        check(load().phs_grid_sample_device(self.h, int(n_events), _ptr(c), int(seed),
+                                            int(first_event), _ptr(x), _stream(stream)))
+        return x
+
+    def update(self, x, ok, counts=None, stream=None) -> None:
+        """Weights from the ok events' x (rng.cpp:34-67)."""
+        c = self._counts(counts, int(x.shape[0]))
+        check(load().phs_grid_update_device(self.h, int(x.shape[0]), _ptr(c), _ptr(x), _ptr(ok),
+                                            _stream(stream)))
+
+    def weights(self) -> np.ndarray:
+        w = np.zeros((self.n_channels, self.n_x, GRID_BINS))
+        check(load().phs_grid_weights(self.h, w.ctypes.data))
+        return w
+
+
+def precondition(ps: "PhaseSpace", grid: Grid, n_trials: int, n_per_channel: int,
+                 seed: int = 0):
+    """The reference's grid warm-up (main.cpp:145-157): n_trials rounds of sampling
+    n_per_channel events per channel, generating them, and updating the grid from their
+    ok flags.  Returns the ok fraction of each round."""
+    counts = np.full(ps.proc.n_channels, int(n_per_channel), np.int64)
+    n = int(counts.sum())
+    fractions = []
+    for t in range(int(n_trials)):
+        x = grid.sample(n, counts, seed=seed, first_event=t * n)
+        ev = ps.generate(x, counts)
+        grid.update(x, ev.ok, counts)
+        fractions.append(ev.ok.double().mean().item())
+    return fractions
+
+
 def philox_fill(x, n_events: int, n_x: int, seed: int, first_event: int = 0, stream=None):
     """Fills CUDA float64 x[n_events * n_x] with the Philox stream (gpu_phs_gb300/philox.py)."""
     check(load().phs_philox_fill(_ptr(x), n_events, n_x, seed, first_event, _stream(stream)))

@@ -23,7 +23,8 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["phs_kernels.cu", "phs_kernels_ff.cu", "phs_adjoint.cu", "phs_inverse.cu"]
+CU_SOURCES = ["phs_kernels.cu", "phs_kernels_ff.cu", "phs_adjoint.cu", "phs_inverse.cu",
+              "phs_grid.cu"]
 # The inverse map mirrors the operation order of the reference's algorithm (as the oracle
 # restates it) without contraction: its results then differ from the oracle's only by the
 # ulps of the transcendental functions, although x(p) is ill-conditioned near the poles.

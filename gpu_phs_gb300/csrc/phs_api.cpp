@@ -1351,3 +1351,97 @@ extern "C" void c_whizard_show_module(void) {
   }
   printf("END OF MODULE\n");
 }
+
+// -------------------------------------------------------------------------- x grids
+struct phs_grid {
+  int device = 0;
+  int n_channels = 0, n_x = 0;
+  DevBuf weights, bins, n_ok, ch_begin;
+  std::vector<int64_t> ch_begin_up;
+};
+
+extern "C" int phs_grid_create(phs_grid_t *out, int n_channels, int n_x) {
+  if (!out) return fail(PHS_ERR_INVALID_ARG, "null output handle pointer");
+  *out = nullptr;
+  if (n_channels < 1 || n_x < 1) return fail(PHS_ERR_INVALID_ARG, "n_channels and n_x must be >= 1");
+  phs_grid *g = new phs_grid;
+  cudaGetDevice(&g->device);
+  g->n_channels = n_channels;
+  g->n_x = n_x;
+  const size_t nb = (size_t)n_channels * n_x * PHS_GRID_BINS;
+  int rc = g->weights.reserve(nb * sizeof(double));
+  if (!rc) rc = g->bins.reserve(nb * sizeof(unsigned long long));
+  if (!rc) rc = g->n_ok.reserve(n_channels * sizeof(unsigned long long));
+  if (rc) { delete g; return rc; }
+  std::vector<double> w(nb, 1.0 / PHS_GRID_BINS);   // rng.cpp:19-29: uniform start
+  cudaError_t e = cudaMemcpy(g->weights.ptr, w.data(), nb * sizeof(double), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    delete g;
+    return fail(PHS_ERR_CUDA, "grid upload: %s", cudaGetErrorString(e));
+  }
+  *out = g;
+  return PHS_OK;
+}
+
+extern "C" int phs_grid_destroy(phs_grid_t g) {
+  if (!g) return PHS_OK;
+  DeviceGuard dg(g->device);
+  g->weights.release();
+  g->bins.release();
+  g->n_ok.release();
+  g->ch_begin.release();
+  delete g;
+  return PHS_OK;
+}
+
+static int grid_channels(phs_grid_t g, int64_t n_events, const int64_t *counts, cudaStream_t st) {
+  if (int rc = check_counts(counts, g->n_channels, n_events)) return rc;
+  std::vector<int64_t> begin(g->n_channels, 0);
+  for (int c = 1; c < g->n_channels; c++) begin[c] = begin[c - 1] + (counts ? counts[c - 1] : n_events);
+  if (begin != g->ch_begin_up) {
+    if (int rc = g->ch_begin.reserve(g->n_channels * sizeof(int64_t))) return rc;
+    CUDA_TRY(cudaMemcpyAsync(g->ch_begin.ptr, begin.data(), g->n_channels * sizeof(int64_t),
+                             cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    g->ch_begin_up = begin;
+  }
+  return PHS_OK;
+}
+
+extern "C" int phs_grid_sample_device(phs_grid_t g, int64_t n_events, const int64_t *counts,
+                                      uint64_t seed, int64_t first_event, double *x,
+                                      void *stream) {
+  if (!g) return fail(PHS_ERR_INVALID_ARG, "null grid handle");
+  if (n_events > 0 && !x) return fail(PHS_ERR_INVALID_ARG, "null x");
+  DeviceGuard dg(g->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (int rc = grid_channels(g, n_events, counts, st)) return rc;
+  if (n_events == 0) return PHS_OK;
+  CUDA_TRY(phs_launch_philox(x, n_events, g->n_x, seed, first_event, st));
+  CUDA_TRY(phs_launch_grid_sample(x, n_events, g->n_x, g->ch_begin.as<int64_t>(), g->n_channels,
+                                  g->weights.as<double>(), sm_count(g->device), st));
+  return PHS_OK;
+}
+
+extern "C" int phs_grid_update_device(phs_grid_t g, int64_t n_events, const int64_t *counts,
+                                      const double *x, const uint8_t *oks, void *stream) {
+  if (!g) return fail(PHS_ERR_INVALID_ARG, "null grid handle");
+  if (n_events > 0 && (!x || !oks)) return fail(PHS_ERR_INVALID_ARG, "null data pointer");
+  DeviceGuard dg(g->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (int rc = grid_channels(g, n_events, counts, st)) return rc;
+  CUDA_TRY(phs_launch_grid_update(x, oks, n_events, g->n_x, g->ch_begin.as<int64_t>(),
+                                  g->n_channels, g->bins.as<unsigned long long>(),
+                                  g->n_ok.as<unsigned long long>(), g->weights.as<double>(),
+                                  sm_count(g->device), st));
+  return PHS_OK;
+}
+
+extern "C" int phs_grid_weights(phs_grid_t g, double *weights) {
+  if (!g || !weights) return fail(PHS_ERR_INVALID_ARG, "null argument");
+  DeviceGuard dg(g->device);
+  CUDA_TRY(cudaMemcpy(weights, g->weights.ptr,
+                      (size_t)g->n_channels * g->n_x * PHS_GRID_BINS * sizeof(double),
+                      cudaMemcpyDeviceToHost));
+  return PHS_OK;
+}

@@ -105,3 +105,14 @@ struct PhsInvLaunch {
 cudaError_t phs_launch_inverse(const PhsInvLaunch &a, int n_blocks, cudaStream_t stream);
 int phs_inverse_blocks_per_sm(int n_out, int stack_depth, bool per_event);
 size_t phs_inverse_smem_bytes(int n_out, int stack_depth);
+
+// Per-channel x grid of the warm-up (phs_grid.cu): weights [n_channels][n_x][PHS_GRID_BINS].
+#define PHS_GRID_BINS 10
+// x holds the Philox uniforms on entry and the grid-distributed x on return.
+cudaError_t phs_launch_grid_sample(double *x, int64_t n_events, int n_x, const int64_t *ch_begin,
+                                   int n_channels, const double *weights, int sm_count,
+                                   cudaStream_t stream);
+cudaError_t phs_launch_grid_update(const double *x, const uint8_t *ok, int64_t n_events, int n_x,
+                                   const int64_t *ch_begin, int n_channels,
+                                   unsigned long long *bins, unsigned long long *n_ok,
+                                   double *weights, int sm_count, cudaStream_t stream);

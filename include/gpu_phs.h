@@ -271,6 +271,32 @@ void c_whizard_show_module(void);
  * Replaces get_momentum_device_pointer (phs.cu:1638-1640, transfer_to_whizard.h:1). */
 double *phs_whizard_momentum_device_pointer(void);
 
+/* ---------------------------------------------------------------- x grids (warm-up) */
+
+/* The per-channel x grid of the reference's warm-up (rng.cpp, main.cpp:145-157): per channel
+ * and x dimension, 10 equal-width bins on [0, 1) with weights, starting uniform
+ * (init_rng, rng.cpp:19-30).  Replaces the host sampler with device kernels. */
+typedef struct phs_grid *phs_grid_t;
+int phs_grid_create(phs_grid_t *out, int n_channels, int n_x);
+int phs_grid_destroy(phs_grid_t grid);
+
+/* x [n_events][n_x] (device) for events grouped by channel (channel_counts), drawn from each
+ * channel's piecewise-constant density (rng_generate, rng.cpp:69-90): the Philox stream of
+ * phs_philox_fill (seed, first_event) mapped through the inverse distribution function.
+ * The reference draws from std::default_random_engine instead; the distribution is the
+ * same. */
+int phs_grid_sample_device(phs_grid_t grid, int64_t n_events, const int64_t *channel_counts,
+                           uint64_t seed, int64_t first_event, double *x, void *stream);
+
+/* Sets each weight to the fraction of the channel's ok events (oks, 1 byte each) whose x
+ * falls into the bin (update_weights, rng.cpp:34-67).  A channel without ok events keeps its
+ * weights (the reference divides by zero there). */
+int phs_grid_update_device(phs_grid_t grid, int64_t n_events, const int64_t *channel_counts,
+                           const double *x, const uint8_t *oks, void *stream);
+
+/* Copies the weights, [n_channels][n_x][10] doubles, to host memory. */
+int phs_grid_weights(phs_grid_t grid, double *weights);
+
 #ifdef __cplusplus
 }
 #endif

@@ -214,3 +214,49 @@ class RefCPU:
         if rc != 0:
             raise RuntimeError("reference harness not set up")
         return r
+
+
+# --------------------------------------------------------------------------- x grids
+GRID_BINS = 10
+
+
+def grid_update(weights, x, counts, ok):
+    """update_weights (rng.cpp:34-67) restated: per channel and dimension, the fraction of
+    the channel's ok events whose x falls into each of the 10 bins.  Channels without ok
+    events keep their weights (the reference divides by zero there)."""
+    w = np.array(weights, dtype=np.float64, copy=True)
+    ch = np.repeat(np.arange(len(counts)), counts)
+    ok = np.asarray(ok).astype(bool)
+    for c in range(len(counts)):
+        sel = (ch == c) & ok
+        n_ok = int(sel.sum())
+        if n_ok == 0:
+            continue
+        b = np.clip((x[sel] * GRID_BINS).astype(np.int64), 0, GRID_BINS - 1)
+        for d in range(x.shape[1]):
+            cnt = np.bincount(b[:, d], minlength=GRID_BINS).astype(np.float64)
+            w[c, d] = cnt / n_ok
+    return w
+
+
+def grid_sample(weights, u, counts):
+    """The inverse distribution function of the piecewise-constant density (the device
+    sampler's formula): bin b with C[b] <= u among bins of positive weight, x = (b + (u -
+    C[b]) / w[b]) / 10, the offset kept inside [0, 1)."""
+    ch = np.repeat(np.arange(len(counts)), counts)
+    x = np.empty_like(u)
+    for i in range(u.shape[0]):
+        for d in range(u.shape[1]):
+            w = weights[ch[i], d]
+            c, b = 0.0, 0
+            for k in range(GRID_BINS):
+                if w[k] > 0.0 and c <= u[i, d]:
+                    b = k
+                c += w[k]
+            cb = 0.0
+            for k in range(b):
+                cb += w[k]
+            t = (u[i, d] - cb) / w[b]
+            t = 0.0 if t < 0.0 else (np.nextafter(1.0, 0.0) if t >= 1.0 else t)
+            x[i, d] = (b + t) / GRID_BINS
+    return x
