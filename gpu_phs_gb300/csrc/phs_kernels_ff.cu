@@ -8,8 +8,9 @@
 // ok flags stay bit-exact with the reference: the kinematic test at every branch is
 // decided in float-float only when the margins |m - m1 - m2| and |m_max - m| exceed
 // 1e-5 of the mass (and msq is not within 1e-10 s of zero).  Otherwise -- and for channels
-// with STEP mappings, which have no float-float form -- the event is recomputed with the
-// exact FP64 path (phs_event_f64.cuh), which also keeps p_decay near threshold in FP64.
+// with STEP mappings or friend boosts, which have no float-float form -- the event is
+// queued for the exact FP64 path (phs_event_f64.cuh, launched behind this kernel by
+// phs_launch_forward_exact), which also keeps p_decay near threshold in FP64.
 // The Kallen function is evaluated in factored form, (m-m1-m2)(m+m1+m2)(m-m1+m2)(m+m1-m2),
 // which keeps its relative accuracy close to threshold.
 #include <cuda_runtime.h>
@@ -17,7 +18,7 @@
 #include <stdint.h>
 
 #include "phs_device.h"
-#include "phs_event_f64.cuh"
+#include "phs_event_f64.cuh"  // the compacting loop and rot_z_onto
 #include "phs_ff.h"
 #include "phs_program.h"
 
