@@ -532,7 +532,7 @@ def run_ours(args):
         e2e = {"value": world * n * e2e_steps / el, "unit": "events/s",
                "h2d_bytes_per_step": n * proc.n_x * 8,
                "d2h_bytes_per_step": n * (32 * proc.n_out + 8 + 8 + 1),
-               "path": "phs_generate_host (C ABI), pinned host buffers, 1 Mi-event chunks on 2 streams",
+               "path": "phs_generate_host (C ABI), pinned host buffers, 512 Ki-event chunks on 3 streams",
                "steps": e2e_steps}
 
     variants = None
