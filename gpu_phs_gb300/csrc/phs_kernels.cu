@@ -16,6 +16,12 @@
 
 namespace {
 
+// The sin/cos table sits after the frame stack and the queues (phs_forward_smem_bytes).
+__device__ __forceinline__ double2 *phs_trig_table(double *smem, int stack_depth) {
+  return reinterpret_cast<double2 *>(smem + (size_t)stack_depth * PHS_STATE * PHS_FWD_BLOCK +
+                                     (size_t)(PHS_FWD_BLOCK / 32) * 64);
+}
+
 // COMPACT: events whose kinematic test fails need no angles or boosts.  Where many fail
 // (low ok fractions: multi-channel batches, hard cuts), pass A tests each event, writes
 // the failures, and queues the rest per warp; pass B runs them densely.  Where nearly all
@@ -27,13 +33,16 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
   const int lane = threadIdx.x & 31;
   const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  double2 *trig = phs_trig_table(smem, a.stack_depth);
+  fill_trig_table(trig);
+  __syncthreads();
   if constexpr (COMPACT) {
     int64_t *q = reinterpret_cast<int64_t *>(smem + (size_t)a.stack_depth * PHS_STATE * PHS_FWD_BLOCK) +
                  (threadIdx.x >> 5) * 64;
     compacting_loop<PHS_CHUNK_TILES>(
         a, q,
         [&](const PhsSegment &sg, int64_t loc) { return phs_ok_f64<PER_EVENT>(a, sg, loc, smem); },
-        [&](int, const PhsSegment &sg, int64_t loc) { phs_event_f64<PER_EVENT>(a, sg, loc, smem); });
+        [&](int, const PhsSegment &sg, int64_t loc) { phs_event_f64<PER_EVENT>(a, sg, loc, smem, trig); });
   } else {
     for (int64_t tile = warp0; tile < a.n_tiles; tile += n_warps) {
       // the segment holding this tile (warp-uniform binary search on tile_begin)
@@ -46,7 +55,7 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
       const PhsSegment seg = segs[lo];
       const int64_t local = (tile - seg.tile_begin) * 32 + lane;
       if (local >= seg.ev_count) continue;
-      phs_event_f64<PER_EVENT>(a, seg, local, smem);
+      phs_event_f64<PER_EVENT>(a, seg, local, smem, trig);
     }
   }
 }
@@ -60,13 +69,16 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
 __global__ void __launch_bounds__(PHS_FWD_BLOCK, 4)
     phs_forward_exact_kernel(const __grid_constant__ PhsLaunch a) {
   extern __shared__ double smem[];
+  double2 *trig = phs_trig_table(smem, a.stack_depth);
+  fill_trig_table(trig);
+  __syncthreads();
   const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
   const int64_t n = (int64_t)*a.exact_count;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const uint64_t e = a.exact_queue[i];
     const PhsSegment seg = segs[e >> 40];
-    phs_event_f64<false>(a, seg, (int64_t)(e & ((1ull << 40) - 1)), smem);
+    phs_event_f64<false>(a, seg, (int64_t)(e & ((1ull << 40) - 1)), smem, trig);
   }
 }
 
@@ -127,9 +139,10 @@ cudaError_t phs_launch_fma_rate(void *out, int fp64, int blocks, int threads, in
 }
 
 size_t phs_forward_smem_bytes(int stack_depth) {
-  // frame stack, then the compacting variant's per-warp queues (64 events per warp)
+  // frame stack, the compacting variant's per-warp queues (64 events per warp), the
+  // sin/cos table
   return (size_t)stack_depth * PHS_STATE * PHS_FWD_BLOCK * sizeof(double) +
-         (size_t)(PHS_FWD_BLOCK / 32) * 64 * sizeof(int64_t);
+         (size_t)(PHS_FWD_BLOCK / 32) * 64 * sizeof(int64_t) + 64 * sizeof(double2);
 }
 
 // variant 0: one pass, registers for 4 resident blocks per SM; 1: compacting, 4 blocks;
