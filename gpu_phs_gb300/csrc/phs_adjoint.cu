@@ -31,6 +31,7 @@ namespace {
 
 struct AdjLayout {
   int state0, ang0, der0, pop0, stack0;  // offsets (in slots) of the per-thread regions
+  int trig0;                             // the block's sin/cos table (2 slots)
 };
 
 __device__ __forceinline__ double &slot(double *sm, int i) {
@@ -123,6 +124,9 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
   const int lane = threadIdx.x & 31;
   const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  double2 *trig = reinterpret_cast<double2 *>(sm + (size_t)lay.trig0 * PHS_ADJ_BLOCK);
+  fill_trig_table(trig);
+  __syncthreads();
 
   for (int64_t tile = warp0; tile < a.n_tiles; tile += n_warps) {
     const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
@@ -201,7 +205,7 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
       const double bg = p_b * rm;
       const double ga = V.self_root ? 1.0 : E_b * rm;
       double sphi, cphi, ct, st, fct;
-      sincospi(2.0 * xe[V.x_phi], &sphi, &cphi);
+      sincos2pi_tab(xe[V.x_phi], trig, sphi, cphi);
       map_ct(V.ct_class, xe[V.x_ct], V.b0, V.b1, ct, st, fct);
       {
         double dct, dst, dlf;
@@ -451,13 +455,14 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
 }  // namespace
 
 void phs_adjoint_sizes(int max_visits, int max_pops, int stack_depth, int *state0, int *ang0,
-                       int *der0, int *pop0, int *stack0, size_t *smem) {
+                       int *der0, int *pop0, int *stack0, int *trig0, size_t *smem) {
   *state0 = 0;
   *ang0 = PHS_ADJ_STATE * max_visits;
   *der0 = *ang0 + PHS_ADJ_ANG * max_visits;
   *pop0 = *der0 + PHS_ADJ_DER * max_visits;
   *stack0 = *pop0 + 16 * max_pops;
-  const int slots = *stack0 + PHS_STATE * (stack_depth > 0 ? stack_depth : 0);
+  *trig0 = *stack0 + PHS_STATE * (stack_depth > 0 ? stack_depth : 0);
+  const int slots = *trig0 + (int)(64 * sizeof(double2) / (PHS_ADJ_BLOCK * sizeof(double)));
   *smem = (size_t)slots * PHS_ADJ_BLOCK * sizeof(double);
 }
 
@@ -468,7 +473,7 @@ cudaError_t phs_launch_adjoint(const PhsLaunch &a, const PhsAdjChannel *adj, con
   AdjLayout lay;
   size_t smem;
   phs_adjoint_sizes(max_visits, max_pops, a.stack_depth, &lay.state0, &lay.ang0, &lay.der0,
-                    &lay.pop0, &lay.stack0, &smem);
+                    &lay.pop0, &lay.stack0, &lay.trig0, &smem);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(phs_adjoint_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -480,9 +485,9 @@ cudaError_t phs_launch_adjoint(const PhsLaunch &a, const PhsAdjChannel *adj, con
 }
 
 int phs_adjoint_blocks_per_sm(int max_visits, int max_pops, int stack_depth) {
-  int s0, a0, d0, p0, k0;
+  int s0, a0, d0, p0, k0, t0;
   size_t smem;
-  phs_adjoint_sizes(max_visits, max_pops, stack_depth, &s0, &a0, &d0, &p0, &k0, &smem);
+  phs_adjoint_sizes(max_visits, max_pops, stack_depth, &s0, &a0, &d0, &p0, &k0, &t0, &smem);
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(phs_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int n = 0;
