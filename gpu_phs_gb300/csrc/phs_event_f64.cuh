@@ -56,14 +56,10 @@ __device__ __forceinline__ void map_msq(int t, double x, double s, double m, dou
     }
     case PHS_MAP_TCHANNEL:
     case PHS_MAP_UCHANNEL: {
-      double msq1;
-      if (x < 0.5) {
-        msq1 = dmul(a0, exp(dmul(x, a1)));
-        msq = dadd(dsub(msq1, a0), msq_min);
-      } else {
-        msq1 = dmul(a0, exp(dmul(dsub(1.0, x), a1)));
-        msq = dadd(-dsub(msq1, a0), msq_max);
-      }
+      // one exponential per lane: the side of x = 0.5 selects its argument and the sum
+      const bool lower = x < 0.5;
+      const double msq1 = dmul(a0, exp(dmul(lower ? x : dsub(1.0, x), a1)));
+      msq = lower ? dadd(dsub(msq1, a0), msq_min) : dadd(-dsub(msq1, a0), msq_max);
       f = a2 * msq1;
       break;
     }
@@ -92,14 +88,9 @@ __device__ __forceinline__ void map_msq(int t, double x, double s, double m, dou
 __device__ __forceinline__ void map_ct(int ct_class, double x, double b0, double b1, double &ct,
                                        double &st, double &f) {
   if (ct_class == PHS_CT_COLLINEAR) {
-    double tmp;
-    if (x < 0.5) {
-      tmp = dmul(b0, exp(dmul(dmul(2.0, x), b1)));
-      ct = dsub(dsub(tmp, b0), 1.0);
-    } else {
-      tmp = dmul(b0, exp(dmul(dmul(2.0, dsub(1.0, x)), b1)));
-      ct = dadd(-dsub(tmp, b0), 1.0);
-    }
+    const bool lower = x < 0.5;
+    const double tmp = dmul(b0, exp(dmul(dmul(2.0, lower ? x : dsub(1.0, x)), b1)));
+    ct = lower ? dsub(dsub(tmp, b0), 1.0) : dadd(-dsub(tmp, b0), 1.0);
     if (ct >= -1.0 && ct <= 1.0) {
       st = sqrt(dsub(1.0, dmul(ct, ct)));
       f = tmp * b1;

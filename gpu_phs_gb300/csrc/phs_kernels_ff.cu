@@ -62,17 +62,18 @@ __device__ __forceinline__ bool map_msq_ff(const PhsChildFF &C, double xd, const
       return true;
     case PHS_MAP_SCHANNEL: {
       // z = (1-x) a0 + x a1; next to +-pi/2, tan z = -+cot(pi/2 -+ z) with pi/2 -+ z formed
-      // from the host's pi/2 - a1 and pi/2 + a0, so its relative accuracy holds there
+      // from the host's pi/2 - a1 and pi/2 + a0, so its relative accuracy holds there.
+      // Lanes of a warp fall on different sides: the argument and the quotient are
+      // selected, and every lane runs one sincos and one division.
       ff z = ff_add(ld(C.a0), ff_mul(x, ld(C.a1)));   // a1 holds a1 - a0
       if (!(fabsf(z.hi) < 1.5707962f)) return false;   // the reference's |z| < pi/2 test
-      ff t;
-      if (z.hi > 0.78539816f) {
-        t = ff_cot(ff_add(ld(C.u1), ff_mul(ff_one_minus_double_int(xd), ld(C.a1))), T);
-      } else if (z.hi < -0.78539816f) {
-        t = ff_neg(ff_cot(ff_add(ld(C.u0), ff_mul(x, ld(C.a1))), T));
-      } else {
-        t = ff_tan(z, T);
-      }
+      const bool hs = z.hi > 0.78539816f, ls = z.hi < -0.78539816f, cot = hs || ls;
+      ff w = z;
+      if (cot) w = ff_add(hs ? ld(C.u1) : ld(C.u0), ff_mul(hs ? ff_one_minus_double_int(xd) : x, ld(C.a1)));
+      ff sw, cw;
+      ff_sincos(w, T, sw, cw);
+      ff t = ff_div_fast(cot ? cw : sw, cot ? sw : cw);
+      if (ls) t = ff_neg(t);
       msq = ff_add(ld(C.m2), ff_mul(ld(C.mw), t));
       f = ff_mul(ld(C.a2), ff_add_f(ff_sqr(t), 1.0f));
       return true;
@@ -87,14 +88,11 @@ __device__ __forceinline__ bool map_msq_ff(const PhsChildFF &C, double xd, const
     }
     case PHS_MAP_TCHANNEL:
     case PHS_MAP_UCHANNEL: {
-      ff msq1;
-      if (x.hi < 0.5f) {
-        msq1 = ff_mul(ld(C.a0), ff_exp(ff_mul(x, ld(C.a1)), T));
-        msq = ff_add(ff_sub(msq1, ld(C.a0)), ld(C.msq_min));
-      } else {
-        msq1 = ff_mul(ld(C.a0), ff_exp(ff_mul(ff_one_minus_double_int(xd), ld(C.a1)), T));
-        msq = ff_add(ff_sub(ld(C.a0), msq1), ld(C.msq_max));
-      }
+      // one exponential per lane: the side of x = 0.5 selects its argument and the sum
+      const bool lower = x.hi < 0.5f;
+      const ff msq1 = ff_mul(ld(C.a0), ff_exp(ff_mul(lower ? x : ff_one_minus_double_int(xd), ld(C.a1)), T));
+      msq = lower ? ff_add(ff_sub(msq1, ld(C.a0)), ld(C.msq_min))
+                  : ff_add(ff_sub(ld(C.a0), msq1), ld(C.msq_max));
       f = ff_mul(ld(C.a2), msq1);
       return true;
     }
@@ -189,14 +187,9 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
     ff ct, st, fct;
     if (V.ct_class == PHS_CT_COLLINEAR) {
       const ff b0 = ld(V.b0), b1 = ld(V.b1);
-      ff tmp;
-      if (xct.hi < 0.5f) {
-        tmp = ff_mul(b0, ff_exp(ff_mul(ff_twice(xct), b1), T));
-        ct = ff_add_f(ff_sub(tmp, b0), -1.0f);
-      } else {
-        tmp = ff_mul(b0, ff_exp(ff_mul(ff_twice(ff_one_minus_double_int(xctd)), b1), T));
-        ct = ff_add_f(ff_sub(b0, tmp), 1.0f);
-      }
+      const bool lower = xct.hi < 0.5f;
+      const ff tmp = ff_mul(b0, ff_exp(ff_mul(ff_twice(lower ? xct : ff_one_minus_double_int(xctd)), b1), T));
+      ct = lower ? ff_add_f(ff_sub(tmp, b0), -1.0f) : ff_add_f(ff_sub(b0, tmp), 1.0f);
       if (ct.hi >= -1.0f && ct.hi <= 1.0f) {
         // 1 - ct^2 = (1 - ct)(1 + ct), each factor without cancellation
         st = ff_sqrt_fast(ff_mul(ff_sub(one, ct), ff_add_f(ct, 1.0f)));
