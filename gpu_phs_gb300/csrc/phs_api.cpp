@@ -72,6 +72,7 @@ struct Segments {
   std::vector<PhsSegment> uploaded;  // content of dev
   DevBuf work;                       // chunk counter of the compacting kernels
   DevBuf exact_n, exact_q;           // FP32-pair launches: the exact-path queue
+  DevBuf pass_n, pass_t, pass_q;     // FP32-pair split form: pre-test survivors per segment
   int64_t n_tiles = 0;
   int64_t n_chunks = 0;
   int64_t n_events = 0;
@@ -80,6 +81,9 @@ struct Segments {
     work.release();
     exact_n.release();
     exact_q.release();
+    pass_n.release();
+    pass_t.release();
+    pass_q.release();
     uploaded.clear();
   }
 };
@@ -224,12 +228,22 @@ int launch_ff_tuned(int &variant, Segments &S, PhsLaunch a, int device, int dept
   if (int rc = S.exact_n.reserve(sizeof(unsigned long long))) return rc;
   if (int rc = S.exact_q.reserve((size_t)std::max<int64_t>(n_events, 1) * sizeof(uint64_t)))
     return rc;
+  const size_t n_seg = (size_t)std::max(a.n_segments, 1);
+  if (int rc = S.pass_n.reserve(n_seg * sizeof(unsigned int))) return rc;
+  if (int rc = S.pass_t.reserve((n_seg + 1) * sizeof(int64_t))) return rc;
+  if (int rc = S.pass_q.reserve((size_t)std::max<int64_t>(a.n_tiles, 1) * 32 * sizeof(int32_t)))
+    return rc;
   a.exact_count = S.exact_n.as<unsigned long long>();
   a.exact_queue = S.exact_q.as<uint64_t>();
+  a.pass_count = S.pass_n.as<unsigned int>();
+  a.pass_tile = S.pass_t.as<int64_t>();
+  a.pass_queue = S.pass_q.as<int32_t>();
   const int exact_grid = sm_count(device) * 2;
   return launch_tuned(variant, PHS_FF_VARIANTS, n_events, st, [&](int v) {
     cudaError_t e = cudaMemsetAsync(a.exact_count, 0, sizeof(unsigned long long), st);
     if (e == cudaSuccess && a.work) e = cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), st);
+    if (e == cudaSuccess && v >= 4)
+      e = cudaMemsetAsync(a.pass_count, 0, (size_t)a.n_segments * sizeof(unsigned int), st);
     if (e == cudaSuccess) e = phs_launch_forward_ff(a, grid_for_ff(a.n_tiles, device, depth, v), v, st);
     if (e == cudaSuccess) e = phs_launch_forward_exact(a, exact_grid, st);
     return e;

@@ -29,6 +29,12 @@ struct PhsLaunch {
                                // launch (warps claim chunks dynamically); null: static
   unsigned long long *exact_count;  // FP32-pair launches: events queued for the exact
   uint64_t *exact_queue;            //   FP64 path (segment << 40 | local), zeroed before
+  // FP32-pair split form: per segment, the events that passed the pre-test (count, zeroed
+  // before the launch), the walk's dense claim numbering ([n_segments + 1]) and their local
+  // indices (segment s from tile_begin * 32 on; n_tiles * 32 entries).
+  unsigned int *pass_count;
+  int64_t *pass_tile;
+  int32_t *pass_queue;
 };
 
 // Block size and resident blocks per SM of the forward kernel.
@@ -68,8 +74,10 @@ size_t phs_noalloc_scratch_bytes();
 // Needs a.channels, a.channels_ff, a.exact_count (zeroed) and a.exact_queue (n events);
 // uniform beams only.
 // variant bit 0: registers for 4 (1) or 3 (0) resident blocks per SM; bit 1: the
-// compacting two-pass form (PHS_FF_VARIANTS in all).
-#define PHS_FF_VARIANTS 4
+// compacting two-pass form; variants 4 and 5 (bit 0 as before): the split form, the FP32
+// pre-test as a kernel of its own, then the float-float walk over the events it passed
+// (needs a.pass_count zeroed, a.pass_tile, a.pass_queue).  PHS_FF_VARIANTS in all.
+#define PHS_FF_VARIANTS 6
 cudaError_t phs_launch_forward_ff(const PhsLaunch &a, int n_blocks, int variant, cudaStream_t stream);
 int phs_forward_ff_blocks_per_sm(int stack_depth, int variant);
 size_t phs_forward_ff_smem_bytes(int stack_depth);

@@ -25,6 +25,7 @@
 #define PHS_FF_STATE 40   // floats per saved frame: L[16], msq, m, p, m_max as pairs
 #define PHS_FF_MARGIN 1e-5f     // kinematic margins decided in float-float
 #define PHS_FF_MSQ_ZERO 1e-10f  // |msq| below this fraction of s takes the exact path
+#define PHS_FF_TEST_MIN_BLOCKS 8  // resident blocks per SM of the stand-alone pre-test kernel
 
 namespace {
 
@@ -80,19 +81,15 @@ __device__ __forceinline__ bool map_msq_ff(const PhsChildFF &C, double xd, const
     }
     case PHS_MAP_COLLINEAR:
     case PHS_MAP_INFRARED:
-    case PHS_MAP_RADIATION: {
-      ff msq1 = ff_mul(ld(C.a0), ff_exp(ff_mul(x, ld(C.a1)), T));
-      msq = ff_add(ff_sub(msq1, ld(C.a0)), ld(C.msq_min));
-      f = ff_mul(ld(C.a2), msq1);
-      return true;
-    }
+    case PHS_MAP_RADIATION:
     case PHS_MAP_TCHANNEL:
     case PHS_MAP_UCHANNEL: {
-      // one exponential per lane: the side of x = 0.5 selects its argument and the sum
-      const bool lower = x.hi < 0.5f;
-      const ff msq1 = ff_mul(ld(C.a0), ff_exp(ff_mul(lower ? x : ff_one_minus_double_int(xd), ld(C.a1)), T));
-      msq = lower ? ff_add(ff_sub(msq1, ld(C.a0)), ld(C.msq_min))
-                  : ff_add(ff_sub(ld(C.a0), msq1), ld(C.msq_max));
+      // one exponential for all five: the t/u-channel maps take x >= 0.5 from the other
+      // end, with the argument and the sum selected per lane
+      const bool upper = (C.map_id == PHS_MAP_TCHANNEL || C.map_id == PHS_MAP_UCHANNEL) && !(x.hi < 0.5f);
+      const ff msq1 = ff_mul(ld(C.a0), ff_exp(ff_mul(upper ? ff_one_minus_double_int(xd) : x, ld(C.a1)), T));
+      msq = upper ? ff_add(ff_sub(ld(C.a0), msq1), ld(C.msq_max))
+                  : ff_add(ff_sub(msq1, ld(C.a0)), ld(C.msq_min));
       f = ff_mul(ld(C.a2), msq1);
       return true;
     }
@@ -315,26 +312,82 @@ __device__ __forceinline__ float msq_f32(const PhsChildFF &C, double xd, float &
     }
     case PHS_MAP_COLLINEAR:
     case PHS_MAP_INFRARED:
-    case PHS_MAP_RADIATION: {
-      const float y = x * C.a1.hi, em = expm1f(y);
-      e = k * (fabsf(C.msq_min.hi) + fabsf(C.a0.hi) * (em + 1.0f) * (1.0f + fabsf(y)));
-      return C.a0.hi * em + C.msq_min.hi;
-    }
+    case PHS_MAP_RADIATION:
     case PHS_MAP_TCHANNEL:
     case PHS_MAP_UCHANNEL: {
-      const bool lower = xd < 0.5;
-      const float y = (lower ? x : (float)(1.0 - xd)) * C.a1.hi, em = expm1f(y);
-      e = k * (fabsf(lower ? C.msq_min.hi : C.msq_max.hi) +
+      const bool upper = (C.map_id == PHS_MAP_TCHANNEL || C.map_id == PHS_MAP_UCHANNEL) && !(xd < 0.5);
+      const float y = (upper ? (float)(1.0 - xd) : x) * C.a1.hi, em = expm1f(y);
+      e = k * (fabsf(upper ? C.msq_max.hi : C.msq_min.hi) +
                fabsf(C.a0.hi) * (em + 1.0f) * (1.0f + fabsf(y)));
-      return lower ? C.a0.hi * em + C.msq_min.hi : C.msq_max.hi - C.a0.hi * em;
+      return upper ? C.msq_max.hi - C.a0.hi * em : C.a0.hi * em + C.msq_min.hi;
     }
   }
   e = INFINITY;
   return 0.0f;
 }
 
+// The reduction tables of the float-float functions, built per block in shared memory,
+// exact at multiples of pi/2 (threads 0..95; the caller synchronises).
+__device__ __forceinline__ void fill_ff_tables(FFTables &T) {
+  if (threadIdx.x < 64) {
+    const int k = threadIdx.x;
+    double sv, cv;
+    sincospi(k / 32.0, &sv, &cv);
+    if (k % 16 == 0) {
+      sv = k == 16 ? 1.0 : (k == 48 ? -1.0 : 0.0);
+      cv = k == 0 ? 1.0 : (k == 32 ? -1.0 : 0.0);
+    }
+    const float sh = (float)sv, chh = (float)cv;
+    T.trig[k] = make_float4(sh, (float)(sv - (double)sh), chh, (float)(cv - (double)chh));
+  } else if (threadIdx.x < 96) {
+    const int j = threadIdx.x - 64;
+    const double v = exp2(j / 32.0);
+    const float h = (float)v;
+    T.exp2[j] = make_float2(h, (float)(v - (double)h));
+  }
+}
+
+// Saved mass intervals of the pre-test: in shared memory inside the fused kernel (slots of
+// the float-float frame stack, which that kernel owns anyway), in registers in the
+// stand-alone test kernel (the depth is at most PHS_STACK_DEPTH).
+struct SmemBounds {
+  float *fst;
+  __device__ __forceinline__ void push(int sp, float lo, float hi, float mx) {
+    fstack_store(fst, sp, 17, ff_make(lo, hi));
+    fstack_store(fst, sp, 19, ff_make(mx, 0.0f));
+  }
+  __device__ __forceinline__ void pop(int sp, float &lo, float &hi, float &mx) {
+    const ff t = fstack_load(fst, sp, 17);
+    lo = t.hi;
+    hi = t.lo;
+    mx = fstack_load(fst, sp, 19).hi;
+  }
+};
+struct RegBounds {
+  float lo_[PHS_STACK_DEPTH], hi_[PHS_STACK_DEPTH], mx_[PHS_STACK_DEPTH];
+  __device__ __forceinline__ void push(int sp, float lo, float hi, float mx) {
+#pragma unroll
+    for (int i = 0; i < PHS_STACK_DEPTH; i++)
+      if (i == sp) {
+        lo_[i] = lo;
+        hi_[i] = hi;
+        mx_[i] = mx;
+      }
+  }
+  __device__ __forceinline__ void pop(int sp, float &lo, float &hi, float &mx) {
+#pragma unroll
+    for (int i = 0; i < PHS_STACK_DEPTH; i++)
+      if (i == sp) {
+        lo = lo_[i];
+        hi = hi_[i];
+        mx = mx_[i];
+      }
+  }
+};
+
+template <class Bounds>
 __device__ __forceinline__ bool phs_ok_f32(const PhsLaunch &a, const PhsSegment &seg,
-                                           int64_t local, float *fst) {
+                                           int64_t local, Bounds &stack) {
   const PhsChannelFF &ch = a.channels_ff[seg.channel];
   if (ch.exact_only) return true;
   const double *xe = a.x + seg.x_base + local * seg.x_stride;
@@ -366,8 +419,7 @@ __device__ __forceinline__ bool phs_ok_f32(const PhsLaunch &a, const PhsSegment 
     if (!V.self_root) fails = fails || mlo_b > mmax_b * up;  // above the bound for certain
     if (V.push >= 0) {
       const bool j0 = V.push == 0;
-      fstack_store(fst, sp, 17, ff_make(j0 ? lo[0] : lo[1], j0 ? hi[0] : hi[1]));
-      fstack_store(fst, sp, 19, ff_make(j0 ? cmax[0] : cmax[1], 0.0f));
+      stack.push(sp, j0 ? lo[0] : lo[1], j0 ? hi[0] : hi[1], j0 ? cmax[0] : cmax[1]);
       sp++;
     }
     if (V.carry >= 0) {
@@ -377,10 +429,7 @@ __device__ __forceinline__ bool phs_ok_f32(const PhsLaunch &a, const PhsSegment 
       mmax_b = j0 ? cmax[0] : cmax[1];
     } else if (sp > 0) {
       sp--;
-      const ff t = fstack_load(fst, sp, 17);
-      mlo_b = t.hi;
-      mhi_b = t.lo;
-      mmax_b = fstack_load(fst, sp, 19).hi;
+      stack.pop(sp, mlo_b, mhi_b, mmax_b);
     }
   }
   if (!fails) return true;
@@ -410,23 +459,7 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
     a.exact_queue[slot] = ((uint64_t)si << 40) | (uint64_t)loc;
   };
 
-  // reduction tables, exact at multiples of pi/2
-  if (threadIdx.x < 64) {
-    const int k = threadIdx.x;
-    double sv, cv;
-    sincospi(k / 32.0, &sv, &cv);
-    if (k % 16 == 0) {
-      sv = k == 16 ? 1.0 : (k == 48 ? -1.0 : 0.0);
-      cv = k == 0 ? 1.0 : (k == 32 ? -1.0 : 0.0);
-    }
-    const float sh = (float)sv, chh = (float)cv;
-    T.trig[k] = make_float4(sh, (float)(sv - (double)sh), chh, (float)(cv - (double)chh));
-  } else if (threadIdx.x < 96) {
-    const int j = threadIdx.x - 64;
-    const double v = exp2(j / 32.0);
-    const float h = (float)v;
-    T.exp2[j] = make_float2(h, (float)(v - (double)h));
-  }
+  fill_ff_tables(T);
   __syncthreads();
 
   const int lane = threadIdx.x & 31;
@@ -438,7 +471,10 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
                  (threadIdx.x >> 5) * 64;
     compacting_loop<1>(
         a, q,
-        [&](const PhsSegment &sg, int64_t loc) { return phs_ok_f32(a, sg, loc, fst); },
+        [&](const PhsSegment &sg, int64_t loc) {
+          SmemBounds st{fst};
+          return phs_ok_f32(a, sg, loc, st);
+        },
         [&](int si, const PhsSegment &sg, int64_t loc) {
           if (!phs_event_ff(a, sg, loc, T, fst)) to_exact(si, loc);
         });
@@ -458,6 +494,102 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
   }
 }
 
+// Split form, kernel 1 of 3: the FP32 pre-test alone, at the occupancy its few registers
+// allow (the fused kernel runs it at the float-float walk's).  Events that fail for certain
+// get their outputs here; the others are appended to their segment's queue (local event
+// indices from tile_begin * 32 on, in any order) for the walk kernel.
+__global__ void __launch_bounds__(PHS_FWD_BLOCK, PHS_FF_TEST_MIN_BLOCKS)
+    phs_ff_test_kernel(const __grid_constant__ PhsLaunch a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
+  for (int64_t tile = warp0; tile < a.n_tiles; tile += n_warps) {
+    int lo = 0, hi = a.n_segments - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (segs[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+    }
+    const PhsSegment &seg = segs[lo];
+    const int64_t local = (tile - seg.tile_begin) * 32 + lane;
+    RegBounds st;
+    const bool pass = local < seg.ev_count && phs_ok_f32(a, seg, local, st);
+    const unsigned m = __ballot_sync(0xffffffffu, pass);
+    if (m == 0) continue;
+    unsigned base = 0;
+    if (lane == 0) base = atomicAdd(a.pass_count + lo, (unsigned)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    // base + rank < ev_count: at most ev_count events of the segment pass
+    if (pass) a.pass_queue[seg.tile_begin * 32 + base + __popc(m & ((1u << lane) - 1u))] = (int32_t)local;
+  }
+}
+
+// Kernel 2 of 3 (one block): pass_tile[s] = sum over the segments before s of
+// ceil(pass_count / 32), the dense numbering of the walk's warp tiles; pass_tile[n] is
+// their total.
+__global__ void __launch_bounds__(1024) phs_ff_pass_scan_kernel(const __grid_constant__ PhsLaunch a) {
+  __shared__ int64_t warp_sum[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int64_t carry = 0;
+  for (int base = 0; base < a.n_segments; base += blockDim.x) {
+    const int s = base + threadIdx.x;
+    const int64_t v = s < a.n_segments ? ((int64_t)a.pass_count[s] + 31) / 32 : 0;
+    int64_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    if (lane == 31) warp_sum[wid] = inc;
+    __syncthreads();
+    int64_t before = 0, total = 0;
+    for (int w = 0; w < nw; w++) {
+      if (w < wid) before += warp_sum[w];
+      total += warp_sum[w];
+    }
+    if (s < a.n_segments) a.pass_tile[s] = carry + before + inc - v;
+    carry += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) a.pass_tile[a.n_segments] = carry;
+}
+
+// Kernel 3 of 3: the float-float walk over the queued events, 32 of one segment per warp
+// claim (a.work counts the claims, zeroed before the launch), so every warp runs one
+// channel's program with all lanes busy except at a segment's last claim.
+template <int MIN_BLOCKS>
+__global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
+    phs_ff_walk_kernel(const __grid_constant__ PhsLaunch a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  FFTables &T = *reinterpret_cast<FFTables *>(smem_raw);
+  float *fst = reinterpret_cast<float *>(smem_raw + sizeof(FFTables));
+  fill_ff_tables(T);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
+  const int64_t n_claims = a.pass_tile[a.n_segments];
+  for (;;) {
+    unsigned long long c = 0;
+    if (lane == 0) c = atomicAdd(a.work, 1ull);
+    const int64_t t = (int64_t)__shfl_sync(0xffffffffu, c, 0);
+    if (t >= n_claims) break;
+    // the last segment whose first claim is <= t (empty segments share the next one's)
+    int lo = 0, hi = a.n_segments - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (a.pass_tile[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    const PhsSegment &seg = segs[lo];
+    const int64_t idx = (t - a.pass_tile[lo]) * 32 + lane;
+    if (idx >= (int64_t)a.pass_count[lo]) continue;
+    const int64_t local = a.pass_queue[seg.tile_begin * 32 + idx];
+    if (!phs_event_ff(a, seg, local, T, fst)) {
+      const unsigned long long slot = atomicAdd(a.exact_count, 1ull);
+      a.exact_queue[slot] = ((uint64_t)lo << 40) | (uint64_t)local;
+    }
+  }
+}
+
 }  // namespace
 
 size_t phs_forward_ff_smem_bytes(int stack_depth) {
@@ -465,25 +597,50 @@ size_t phs_forward_ff_smem_bytes(int stack_depth) {
          (size_t)(PHS_FWD_BLOCK / 32) * 64 * sizeof(int64_t);
 }
 
-// variant bit 0: register budget for 4 (1) or 3 (0) resident blocks; bit 1: compacting.
+// variant bit 0: register budget for 4 (1) or 3 (0) resident blocks; bit 1: compacting
+// (fused pre-test); variants 4 and 5: the split form (pre-test kernel, scan, walk kernel).
+static size_t ff_walk_smem_bytes(int stack_depth) {
+  return sizeof(FFTables) + (size_t)stack_depth * (PHS_FF_STATE / 2) * PHS_FWD_BLOCK * sizeof(float2);
+}
+
 static const void *ff_kernel(int variant) {
   switch (variant) {
     case 1: return (const void *)phs_forward_ff_kernel<4, false>;
     case 2: return (const void *)phs_forward_ff_kernel<3, true>;
     case 3: return (const void *)phs_forward_ff_kernel<4, true>;
+    case 4: return (const void *)phs_ff_walk_kernel<3>;
+    case 5: return (const void *)phs_ff_walk_kernel<4>;
     default: return (const void *)phs_forward_ff_kernel<3, false>;
   }
 }
 
 int phs_forward_ff_blocks_per_sm(int stack_depth, int variant) {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ff_kernel(variant), PHS_FWD_BLOCK,
-                                                phs_forward_ff_smem_bytes(stack_depth));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &n, ff_kernel(variant), PHS_FWD_BLOCK,
+      variant >= 4 ? ff_walk_smem_bytes(stack_depth) : phs_forward_ff_smem_bytes(stack_depth));
   return n > 0 ? n : 1;
 }
 
 cudaError_t phs_launch_forward_ff(const PhsLaunch &a, int n_blocks, int variant, cudaStream_t stream) {
   if (a.n_tiles <= 0) return cudaSuccess;
+  if (variant >= 4) {
+    // a.pass_count and a.work are zeroed by the caller
+    int dev = 0, sms = 1, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, phs_ff_test_kernel, PHS_FWD_BLOCK, 0);
+    const int64_t want = (a.n_tiles + PHS_FWD_BLOCK / 32 - 1) / (PHS_FWD_BLOCK / 32);
+    const int64_t cap = (int64_t)(sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+    phs_ff_test_kernel<<<(int)(want < cap ? want : cap), PHS_FWD_BLOCK, 0, stream>>>(a);
+    phs_ff_pass_scan_kernel<<<1, 1024, 0, stream>>>(a);
+    const size_t smem = ff_walk_smem_bytes(a.stack_depth);
+    if (variant == 5)
+      phs_ff_walk_kernel<4><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+    else
+      phs_ff_walk_kernel<3><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+    return cudaGetLastError();
+  }
   const size_t smem = phs_forward_ff_smem_bytes(a.stack_depth);
   switch (variant) {
     case 1: phs_forward_ff_kernel<4, false><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a); break;

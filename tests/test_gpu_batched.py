@@ -81,11 +81,12 @@ def _gen_batch(torch, spaces, counts, x, prec, ff_v=-1, f64_v=-1):
     return [t.clone() for t in out]
 
 
-@pytest.mark.parametrize("prec,n_var", [(0, 3), (1, 4)])
+@pytest.mark.parametrize("prec,n_var", [(0, 3), (1, 6)])
 def test_kernel_variants_identical_bits(torch, prec, n_var):
-    """Every kernel variant (register budgets, one-pass or compacting) computes the same
-    bits: the compacting form's pass B runs the same event code, and its pass A writes the
-    outputs of failing events exactly as the one-pass form does."""
+    """Every kernel variant (register budgets, one-pass, compacting or split) computes the
+    same bits: the compacting and split forms run the same event code on the events that
+    pass their pre-test, and the pre-test writes the outputs of failing events exactly as
+    the one-pass form does."""
     from gpu_phs_gb300.api import Batch, PhaseSpace, philox_fill
     procs, counts = P.batched(seed=2024, n_channels=64, total_events=1 << 19)
     spaces = [PhaseSpace(p, 500.0, 500.0) for p in procs]
@@ -124,3 +125,22 @@ def test_compacting_fp64_vs_oracle_low_ok_fraction(torch, f64_v):
     assert (np.abs(f[sel] / r.factor[sel] - 1)).max() <= 1e-12
     assert np.all(p[~sel] == 0) and np.all(f[~sel] == 0)
     assert np.allclose(v, r.volume, rtol=1e-15, atol=0)
+
+
+def test_split_form_many_segments_and_empty_channels(torch):
+    """The FP32-pair split form with more segments than the launch parameters hold inline
+    (a device segment table) and with empty channels between full ones (the scan gives
+    them no claims): identical bits to the one-pass form."""
+    from gpu_phs_gb300.api import Batch, PhaseSpace, philox_fill
+    procs, counts = P.batched(seed=11, n_channels=100, total_events=1 << 18)
+    counts = counts.copy()
+    counts[[0, 7, 50, 99]] = 0
+    spaces = [PhaseSpace(p, 500.0, 500.0) for p in procs]
+    xo, _ = Batch(spaces).offsets(counts)
+    x = torch.empty(int(xo[-1]), dtype=torch.float64, device="cuda")
+    philox_fill(x, int(xo[-1]), 1, seed=12)
+    ref = _gen_batch(torch, spaces, counts, x, 1, ff_v=0)
+    for v in (4, 5):
+        got = _gen_batch(torch, spaces, counts, x, 1, ff_v=v)
+        for a, b in zip(ref, got):
+            assert torch.equal(a, b), f"variant {v} differs from variant 0"
