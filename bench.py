@@ -603,12 +603,12 @@ def run_case(name: str) -> None:
         o = ps.alloc(n)
         for _ in range(2):
             ps.generate(x, out=o)
-    elif name in ("f64_batched", "ff_batched"):   # 2^22 batched events, compacting
+    elif name in ("f64_batched", "ff_batched"):   # 2^22 batched events, compacting / split
         procs, counts = P.batched(seed=2024, n_channels=64, total_events=1 << 22)
         b = Batch([PhaseSpace(p, 500.0, 500.0) for p in procs])
         if name == "ff_batched":
             b.set_precision(1)
-            b.set_variants(3, -1)
+            b.set_variants(5, -1)
         else:
             b.set_variants(-1, 2)
         xo, _ = b.offsets(counts)

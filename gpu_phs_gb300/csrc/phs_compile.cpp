@@ -382,6 +382,33 @@ void channel_to_ff(const PhsChannel &in, PhsChannelFF &out) {
     F.b0 = split(V.b0);
     F.b1 = split(V.b1);
     F.self_m_max = split(V.self_m_max);
+    PhsTestVisit &P = out.test[v];
+    for (int j = 0; j < 2; j++) {
+      const PhsChildFF &G = F.child[j];
+      PhsTestChild &Q = P.child[j];
+      switch (G.map_id) {
+        case PHS_MAP_NO:
+          Q.c[0] = G.msq_min.hi;
+          Q.c[1] = G.msq_max.hi;
+          break;
+        case PHS_MAP_SCHANNEL:
+          Q.c[0] = G.a0.hi;
+          Q.c[1] = G.a1.hi;
+          Q.c[2] = G.u0.hi;
+          Q.c[3] = G.u1.hi;
+          Q.c[4] = G.m2.hi;
+          Q.c[5] = G.mw.hi;
+          break;
+        default:
+          Q.c[0] = G.a0.hi;
+          Q.c[1] = G.a1.hi;
+          Q.c[2] = G.msq_min.hi;
+          Q.c[3] = G.msq_max.hi;
+      }
+      Q.m = G.internal ? G.m_max.hi : G.m_leaf.hi;
+      Q.code = (G.internal ? 1 : 0) | (G.map_id & 127) << 1 | (G.x_msq & 255) << 8;
+    }
+    P.child[0].code |= (V.push + 1) << 16 | (V.carry + 1) << 18 | (V.self_root ? 1 : 0) << 20;
   }
 }
 

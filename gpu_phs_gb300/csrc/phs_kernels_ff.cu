@@ -292,34 +292,34 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
 // Its outputs are written here.  Every other event goes to pass B, whose float-float /
 // FP64 walk decides its flag exactly.  Returns false for a failed event.
 #define PHS_F32_EPS_BOUND (64.0f * 5.9604645e-8f)
-__device__ __forceinline__ float msq_f32(const PhsChildFF &C, double xd, float &e) {
+// c0..c5: the packed constants of PhsTestChild.
+__device__ __forceinline__ float msq_f32(int map_id, float4 c, float c4, float c5, double xd,
+                                         float &e) {
   const float x = (float)xd, k = PHS_F32_EPS_BOUND;
-  switch (C.map_id) {
+  switch (map_id) {
     case PHS_MAP_NO:
-      e = k * (fabsf(C.msq_min.hi) + fabsf(C.msq_max.hi));
-      return C.msq_min.hi + x * (C.msq_max.hi - C.msq_min.hi);
+      e = k * (fabsf(c.x) + fabsf(c.y));
+      return c.x + x * (c.y - c.x);
     case PHS_MAP_SCHANNEL: {
       // one tanf per lane, on z or on pi/2 -+ z (selected, not branched: lanes of a warp
       // take different sides)
-      const float z = C.a0.hi + x * C.a1.hi;  // a1 holds a1 - a0
+      const float z = c.x + x * c.y;  // c.y holds a1 - a0
       const bool hi_side = z > 0.78539816f, lo_side = z < -0.78539816f;
-      const float w = hi_side ? C.u1.hi + (float)(1.0 - xd) * C.a1.hi
-                              : (lo_side ? C.u0.hi + x * C.a1.hi : z);
+      const float w = hi_side ? c.w + (float)(1.0 - xd) * c.y : (lo_side ? c.z + x * c.y : z);
       const float tw = tanf(w);
       const float t = hi_side ? 1.0f / tw : (lo_side ? -1.0f / tw : tw);
-      e = k * (fabsf(C.m2.hi) + fabsf(C.mw.hi) * (1.0f + t * t));
-      return C.m2.hi + C.mw.hi * t;
+      e = k * (fabsf(c4) + fabsf(c5) * (1.0f + t * t));
+      return c4 + c5 * t;
     }
     case PHS_MAP_COLLINEAR:
     case PHS_MAP_INFRARED:
     case PHS_MAP_RADIATION:
     case PHS_MAP_TCHANNEL:
     case PHS_MAP_UCHANNEL: {
-      const bool upper = (C.map_id == PHS_MAP_TCHANNEL || C.map_id == PHS_MAP_UCHANNEL) && !(xd < 0.5);
-      const float y = (upper ? (float)(1.0 - xd) : x) * C.a1.hi, em = expm1f(y);
-      e = k * (fabsf(upper ? C.msq_max.hi : C.msq_min.hi) +
-               fabsf(C.a0.hi) * (em + 1.0f) * (1.0f + fabsf(y)));
-      return upper ? C.msq_max.hi - C.a0.hi * em : C.a0.hi * em + C.msq_min.hi;
+      const bool upper = (map_id == PHS_MAP_TCHANNEL || map_id == PHS_MAP_UCHANNEL) && !(xd < 0.5);
+      const float y = (upper ? (float)(1.0 - xd) : x) * c.y, em = expm1f(y);
+      e = k * (fabsf(upper ? c.w : c.z) + fabsf(c.x) * (em + 1.0f) * (1.0f + fabsf(y)));
+      return upper ? c.w - c.x * em : c.x * em + c.z;
     }
   }
   e = INFINITY;
@@ -397,33 +397,37 @@ __device__ __forceinline__ bool phs_ok_f32(const PhsLaunch &a, const PhsSegment 
   int sp = 0;
   const int n_visits = ch.n_visits;
   for (int v = 0; v < n_visits && !fails; v++) {
-    const PhsVisitFF &V = ch.visit[v];
+    // the visit in four independent 16-byte loads
+    const float4 *q = reinterpret_cast<const float4 *>(ch.test + v);
+    const float4 A[2] = {__ldg(q), __ldg(q + 2)}, B[2] = {__ldg(q + 1), __ldg(q + 3)};
+    const int code0 = __float_as_int(B[0].w);
     float lo[2], hi[2], cmax[2];
 #pragma unroll
     for (int j = 0; j < 2; j++) {
-      const PhsChildFF &C = V.child[j];
-      if (!C.internal) {
-        lo[j] = C.m_leaf.hi * dn;
-        hi[j] = C.m_leaf.hi * up;
+      const int code = __float_as_int(B[j].w);
+      if (!(code & 1)) {
+        lo[j] = B[j].z * dn;
+        hi[j] = B[j].z * up;
         cmax[j] = 0.0f;
       } else {
         float e;
-        const float msq = msq_f32(C, xe[C.x_msq], e);
+        const float msq = msq_f32((code >> 1) & 127, A[j], B[j].x, B[j].y, xe[(code >> 8) & 255], e);
         fails = fails || msq + e < 0.0f;                // negative for certain: not ok
         lo[j] = sqrtf(fmaxf(msq - e, 0.0f)) * dn;       // NaN bounds decide nothing
         hi[j] = sqrtf(fmaxf(msq + e, 0.0f)) * up;
-        cmax[j] = C.m_max.hi;
+        cmax[j] = B[j].z;
       }
     }
     fails = fails || mhi_b < (lo[0] + lo[1]) * dn;     // below threshold for certain
-    if (!V.self_root) fails = fails || mlo_b > mmax_b * up;  // above the bound for certain
-    if (V.push >= 0) {
-      const bool j0 = V.push == 0;
+    const int push = ((code0 >> 16) & 3) - 1, carry = ((code0 >> 18) & 3) - 1;
+    if (!((code0 >> 20) & 1)) fails = fails || mlo_b > mmax_b * up;  // above the bound for certain
+    if (push >= 0) {
+      const bool j0 = push == 0;
       stack.push(sp, j0 ? lo[0] : lo[1], j0 ? hi[0] : hi[1], j0 ? cmax[0] : cmax[1]);
       sp++;
     }
-    if (V.carry >= 0) {
-      const bool j0 = V.carry == 0;
+    if (carry >= 0) {
+      const bool j0 = carry == 0;
       mlo_b = j0 ? lo[0] : lo[1];
       mhi_b = j0 ? hi[0] : hi[1];
       mmax_b = j0 ? cmax[0] : cmax[1];
@@ -432,14 +436,41 @@ __device__ __forceinline__ bool phs_ok_f32(const PhsLaunch &a, const PhsSegment 
       stack.pop(sp, mlo_b, mhi_b, mmax_b);
     }
   }
-  if (!fails) return true;
+  return !fails;
+}
+
+// The outputs of an event that fails the kinematic test (as the walk writes them).
+__device__ __forceinline__ void write_failed_event(const PhsLaunch &a, const PhsSegment &seg,
+                                                   int64_t local) {
   const int64_t ev = seg.ev_begin + local;
-  a.volume[ev] = ch.volume;
+  a.volume[ev] = a.channels_ff[seg.channel].volume;
   a.factor[ev * a.factor_stride + seg.factor_col] = 0.0;
   a.ok[ev] = 0;
-  double2 *o = reinterpret_cast<double2 *>(a.p + seg.p_base + local * 4 * (int64_t)ch.n_out);
-  for (int i = 0; i < 2 * ch.n_out; i++) o[i] = make_double2(0.0, 0.0);
-  return false;
+  double2 *o = reinterpret_cast<double2 *>(a.p + seg.p_base + local * 4 * (int64_t)seg.n_out);
+  for (int i = 0; i < 2 * seg.n_out; i++) o[i] = make_double2(0.0, 0.0);
+}
+
+// The same for the events of a warp tile (first event local0) whose lanes are set in
+// `failed`, with the momentum rows written by the whole warp (the tile's rows are
+// contiguous): 512 bytes per store instruction.
+__device__ __forceinline__ void write_failed_tile(const PhsLaunch &a, const PhsSegment &seg,
+                                                  int64_t local0, unsigned failed) {
+  const int lane = threadIdx.x & 31;
+  if (failed >> lane & 1) {
+    const int64_t ev = seg.ev_begin + local0 + lane;
+    a.volume[ev] = a.channels_ff[seg.channel].volume;
+    a.factor[ev * a.factor_stride + seg.factor_col] = 0.0;
+    a.ok[ev] = 0;
+  }
+  const int row = 2 * seg.n_out;  // double2 per event
+  const float inv_row = 1.0f / (float)row;
+  double2 *o = reinterpret_cast<double2 *>(a.p + seg.p_base + local0 * 4 * (int64_t)seg.n_out);
+  for (int i = lane; i < 32 * row; i += 32) {
+    // event of entry i: the quotient is at least 0.5 / row from an integer, far above the
+    // rounding of the product (i < 32 * 2 * PHS_MAX_OUT)
+    const int e = __float2int_rz(((float)i + 0.5f) * inv_row);
+    if (failed >> e & 1) o[i] = make_double2(0.0, 0.0);
+  }
 }
 
 // MIN_BLOCKS: resident blocks per SM the register allocation targets; COMPACT: the
@@ -473,7 +504,9 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
         a, q,
         [&](const PhsSegment &sg, int64_t loc) {
           SmemBounds st{fst};
-          return phs_ok_f32(a, sg, loc, st);
+          if (phs_ok_f32(a, sg, loc, st)) return true;
+          write_failed_event(a, sg, loc);
+          return false;
         },
         [&](int si, const PhsSegment &sg, int64_t loc) {
           if (!phs_event_ff(a, sg, loc, T, fst)) to_exact(si, loc);
@@ -495,32 +528,50 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
 }
 
 // Split form, kernel 1 of 3: the FP32 pre-test alone, at the occupancy its few registers
-// allow (the fused kernel runs it at the float-float walk's).  Events that fail for certain
-// get their outputs here; the others are appended to their segment's queue (local event
-// indices from tile_begin * 32 on, in any order) for the walk kernel.
+// allow (the fused kernel runs it at the float-float walk's).  A warp takes a chunk of
+// PHS_CHUNK_TILES tiles of one segment; events that fail for certain get their outputs
+// here, the others are gathered in shared memory and appended to their segment's queue
+// (local event indices from tile_begin * 32 on, in any order) with one atomic per chunk.
 __global__ void __launch_bounds__(PHS_FWD_BLOCK, PHS_FF_TEST_MIN_BLOCKS)
     phs_ff_test_kernel(const __grid_constant__ PhsLaunch a) {
+  __shared__ int32_t gathered[PHS_FWD_BLOCK / 32][PHS_CHUNK_TILES * 32];
   const int lane = threadIdx.x & 31;
+  int32_t *buf = gathered[threadIdx.x >> 5];
   const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
-  for (int64_t tile = warp0; tile < a.n_tiles; tile += n_warps) {
+  for (int64_t chunk = warp0; chunk < a.n_chunks; chunk += n_warps) {
     int lo = 0, hi = a.n_segments - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if (segs[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+      if (segs[mid].chunk_begin <= chunk) lo = mid; else hi = mid - 1;
     }
     const PhsSegment &seg = segs[lo];
-    const int64_t local = (tile - seg.tile_begin) * 32 + lane;
-    RegBounds st;
-    const bool pass = local < seg.ev_count && phs_ok_f32(a, seg, local, st);
-    const unsigned m = __ballot_sync(0xffffffffu, pass);
-    if (m == 0) continue;
-    unsigned base = 0;
-    if (lane == 0) base = atomicAdd(a.pass_count + lo, (unsigned)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    // base + rank < ev_count: at most ev_count events of the segment pass
-    if (pass) a.pass_queue[seg.tile_begin * 32 + base + __popc(m & ((1u << lane) - 1u))] = (int32_t)local;
+    const int64_t t0 = (chunk - seg.chunk_begin) * PHS_CHUNK_TILES;
+    const int64_t seg_tiles = (seg.ev_count + 31) / 32;
+    const int n_t = (int)(seg_tiles - t0 < PHS_CHUNK_TILES ? seg_tiles - t0 : PHS_CHUNK_TILES);
+    int n_pass = 0;
+    for (int t = 0; t < n_t; t++) {
+      const int64_t local0 = (t0 + t) * 32, local = local0 + lane;
+      const bool valid = local < seg.ev_count;
+      RegBounds st;
+      const bool pass = valid && phs_ok_f32(a, seg, local, st);
+      const unsigned m = __ballot_sync(0xffffffffu, pass);
+      const unsigned failed = __ballot_sync(0xffffffffu, valid && !pass);
+      if (pass) buf[n_pass + __popc(m & ((1u << lane) - 1u))] = (int32_t)local;
+      n_pass += __popc(m);
+      if (failed) write_failed_tile(a, seg, local0, failed);
+    }
+    __syncwarp();
+    if (n_pass > 0) {
+      unsigned base = 0;
+      if (lane == 0) base = atomicAdd(a.pass_count + lo, (unsigned)n_pass);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      // base + n_pass <= ev_count: at most ev_count events of the segment pass
+      int32_t *dst = a.pass_queue + seg.tile_begin * 32 + base;
+      for (int i = lane; i < n_pass; i += 32) dst[i] = buf[i];
+    }
+    __syncwarp();
   }
 }
 

@@ -134,6 +134,19 @@ struct PhsVisitFF {
   PhsFF b0, b1, self_m_max;
 };
 
+// The FP32 pre-test's view of a visit (high parts only), four 16-byte loads.  Per child
+// c[0..5] by mapping: none {msq_min, msq_max}; Breit-Wigner {a0, a1 - a0, pi/2 + a0,
+// pi/2 - a1, m^2, m w}; exponential {a0, a1, msq_min, msq_max}; m = m_max (internal) or
+// the leaf mass; code = internal | map_id << 1 | x_msq << 8, and child 0's code also holds
+// push + 1 (bits 16-17), carry + 1 (bits 18-19) and self_root (bit 20).
+struct PhsTestChild {
+  float c[6];
+  float m;
+  int32_t code;
+};
+struct alignas(16) PhsTestVisit {
+  PhsTestChild child[2];
+};
 struct PhsChannelFF {
   int32_t n_out, n_visits;
   int32_t exact_only;  // 1: STEP_E/STEP_H mappings or a friend boost: FP64 path
@@ -141,6 +154,7 @@ struct PhsChannelFF {
   PhsFF sqrts, s, lab_bg, lab_gamma;
   double volume;
   PhsVisitFF visit[PHS_MAX_VISITS];
+  PhsTestVisit test[PHS_MAX_VISITS];
 };
 
 // ------------------------------------------------------------------------------------
