@@ -223,21 +223,28 @@ int launch_tuned(int &variant, int n_variants, int64_t n_events, cudaStream_t st
 // FP32-pair launch: the float-float kernel, then the exact FP64 path over the events it
 // queued (a handful of blocks: they are about 0.1 % of the events, or all events of a
 // channel without a float-float form).
-int launch_ff_tuned(int &variant, Segments &S, PhsLaunch a, int device, int depth,
-                    int64_t n_events, cudaStream_t st) {
-  if (int rc = S.exact_n.reserve(sizeof(unsigned long long))) return rc;
-  if (int rc = S.exact_q.reserve((size_t)std::max<int64_t>(n_events, 1) * sizeof(uint64_t)))
-    return rc;
+// Scratch of the split forms: pre-test survivors per segment, their claim numbering and
+// their indices (n_tiles * 32 entries).
+int attach_pass_buffers(Segments &S, PhsLaunch &a) {
   const size_t n_seg = (size_t)std::max(a.n_segments, 1);
   if (int rc = S.pass_n.reserve(n_seg * sizeof(unsigned int))) return rc;
   if (int rc = S.pass_t.reserve((n_seg + 1) * sizeof(int64_t))) return rc;
   if (int rc = S.pass_q.reserve((size_t)std::max<int64_t>(a.n_tiles, 1) * 32 * sizeof(int32_t)))
     return rc;
-  a.exact_count = S.exact_n.as<unsigned long long>();
-  a.exact_queue = S.exact_q.as<uint64_t>();
   a.pass_count = S.pass_n.as<unsigned int>();
   a.pass_tile = S.pass_t.as<int64_t>();
   a.pass_queue = S.pass_q.as<int32_t>();
+  return PHS_OK;
+}
+
+int launch_ff_tuned(int &variant, Segments &S, PhsLaunch a, int device, int depth,
+                    int64_t n_events, cudaStream_t st) {
+  if (int rc = S.exact_n.reserve(sizeof(unsigned long long))) return rc;
+  if (int rc = S.exact_q.reserve((size_t)std::max<int64_t>(n_events, 1) * sizeof(uint64_t)))
+    return rc;
+  if (int rc = attach_pass_buffers(S, a)) return rc;
+  a.exact_count = S.exact_n.as<unsigned long long>();
+  a.exact_queue = S.exact_q.as<uint64_t>();
   const int exact_grid = sm_count(device) * 2;
   return launch_tuned(variant, PHS_FF_VARIANTS, n_events, st, [&](int v) {
     cudaError_t e = cudaMemsetAsync(a.exact_count, 0, sizeof(unsigned long long), st);
@@ -250,14 +257,20 @@ int launch_ff_tuned(int &variant, Segments &S, PhsLaunch a, int device, int dept
   });
 }
 
-int launch_f64_tuned(int &variant, const PhsLaunch &a, int device, int depth, int64_t n_events,
-                     cudaStream_t st) {
+int launch_f64_tuned(int &variant, Segments &S, PhsLaunch a, int device, int depth,
+                     int64_t n_events, cudaStream_t st) {
   const bool per_event = a.E1 != nullptr;
-  return launch_tuned(variant, PHS_F64_VARIANTS, n_events, st, [&](int v) {
-    if (a.work) {
-      cudaError_t e = cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), st);
-      if (e != cudaSuccess) return e;
-    }
+  if (!per_event)
+    if (int rc = attach_pass_buffers(S, a)) return rc;
+  const int n_variants = per_event ? PHS_F64_VARIANTS_PER_EVENT : PHS_F64_VARIANTS;
+  return launch_tuned(variant, n_variants, n_events, st, [&](int v) {
+    // per-event beams have no pre-test: a pinned split form runs as the compacting one
+    if (per_event && v >= PHS_F64_VARIANTS_PER_EVENT) v -= 2;
+    cudaError_t e = cudaSuccess;
+    if (a.work) e = cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), st);
+    if (e == cudaSuccess && v >= PHS_F64_VARIANTS_PER_EVENT)
+      e = cudaMemsetAsync(a.pass_count, 0, (size_t)a.n_segments * sizeof(unsigned int), st);
+    if (e != cudaSuccess) return e;
     return phs_launch_forward_f64(a, grid_for(a.n_tiles, device, depth, per_event, v), v, st);
   });
 }
@@ -532,7 +545,7 @@ static int launch_process(phs_process_t h, Segments &S, int64_t n_events, const 
   if (a.n_tiles == 0) return PHS_OK;
   if (h->precision == PHS_PRECISION_F32X2 && E1 == nullptr)
     return launch_ff_tuned(h->ff_variant, S, a, h->device, h->stack_depth, n_events, stream);
-  return launch_f64_tuned(h->f64_variant[E1 != nullptr], a, h->device, h->stack_depth, n_events,
+  return launch_f64_tuned(h->f64_variant[E1 != nullptr], S, a, h->device, h->stack_depth, n_events,
                           stream);
 }
 
@@ -828,7 +841,7 @@ extern "C" int phs_batch_generate_device(phs_batch_t b, const int64_t *counts, c
   if (b->precision == PHS_PRECISION_F32X2)
     return launch_ff_tuned(b->ff_variant, b->segs, a, b->device, b->stack_depth, n_events,
                            (cudaStream_t)stream);
-  return launch_f64_tuned(b->f64_variant, a, b->device, b->stack_depth, n_events,
+  return launch_f64_tuned(b->f64_variant, b->segs, a, b->device, b->stack_depth, n_events,
                           (cudaStream_t)stream);
 }
 

@@ -42,8 +42,12 @@ struct PhsLaunch {
 
 // variant 0: one pass per event; 1 and 2: compacting (pass A tests every event and writes
 // the failures, pass B computes the passing events densely) with registers for 4 or 3
-// resident blocks per SM.  PHS_F64_VARIANTS of them.
-#define PHS_F64_VARIANTS 3
+// resident blocks per SM; 3 and 4: split (the FP32 pre-test of phs_launch_pretest, then
+// the FP64 walk over its survivors; uniform beams only, needs the a.pass_* buffers and
+// a.work zeroed), 4 or 3 blocks.  PHS_F64_VARIANTS of them; the first
+// PHS_F64_VARIANTS_PER_EVENT serve per-event beams.
+#define PHS_F64_VARIANTS 5
+#define PHS_F64_VARIANTS_PER_EVENT 3
 cudaError_t phs_launch_forward_f64(const PhsLaunch &a, int n_blocks, int variant,
                                    cudaStream_t stream);
 int phs_forward_blocks_per_sm(int stack_depth, bool per_event, int variant);
@@ -81,6 +85,11 @@ size_t phs_noalloc_scratch_bytes();
 cudaError_t phs_launch_forward_ff(const PhsLaunch &a, int n_blocks, int variant, cudaStream_t stream);
 int phs_forward_ff_blocks_per_sm(int stack_depth, int variant);
 size_t phs_forward_ff_smem_bytes(int stack_depth);
+// The FP32 pre-test of the split forms (phs_kernels_ff.cu): writes the outputs of the
+// events whose kinematic test fails for certain, and queues the others per segment in
+// a.pass_queue / a.pass_count (zeroed before) with the dense claim numbering a.pass_tile.
+// Uniform beams only (it reads the float-float programs' constants).
+cudaError_t phs_launch_pretest(const PhsLaunch &a, cudaStream_t stream);
 // The exact FP64 path over the events an FP32-pair launch queued (a.exact_queue).
 cudaError_t phs_launch_forward_exact(const PhsLaunch &a, int n_blocks, cudaStream_t stream);
 

@@ -82,6 +82,39 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, 4)
   }
 }
 
+// Split form of the FP64 kernel: after the FP32 pre-test (phs_launch_pretest, which writes
+// the outputs of the events that fail for certain and queues the others per segment), the
+// FP64 walk over the queued events, 32 of one segment per warp claim (a.work counts the
+// claims, zeroed before the launch).  The pre-test only settles failures that the FP64
+// test makes too, so the outputs are the one-pass kernel's bits.  Uniform beams only.
+template <int MIN_BLOCKS>
+__global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
+    phs_f64_walk_kernel(const __grid_constant__ PhsLaunch a) {
+  extern __shared__ double smem[];
+  const int lane = threadIdx.x & 31;
+  double2 *trig = phs_trig_table(smem, a.stack_depth);
+  fill_trig_table(trig);
+  __syncthreads();
+  const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
+  const int64_t n_claims = a.pass_tile[a.n_segments];
+  for (;;) {
+    unsigned long long c = 0;
+    if (lane == 0) c = atomicAdd(a.work, 1ull);
+    const int64_t t = (int64_t)__shfl_sync(0xffffffffu, c, 0);
+    if (t >= n_claims) break;
+    // the last segment whose first claim is <= t (empty segments share the next one's)
+    int lo = 0, hi = a.n_segments - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (a.pass_tile[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    const PhsSegment seg = segs[lo];
+    const int64_t idx = (t - a.pass_tile[lo]) * 32 + lane;
+    if (idx >= (int64_t)a.pass_count[lo]) continue;
+    phs_event_f64<false>(a, seg, a.pass_queue[seg.tile_begin * 32 + idx], smem, trig);
+  }
+}
+
 // Philox4x32-10 (Salmon et al., SC'11); layout documented in gpu_phs_gb300/philox.py.
 __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
 #pragma unroll
@@ -146,12 +179,15 @@ size_t phs_forward_smem_bytes(int stack_depth) {
 }
 
 // variant 0: one pass, registers for 4 resident blocks per SM; 1: compacting, 4 blocks;
-// 2: compacting, 3 blocks (no spills).
+// 2: compacting, 3 blocks (no spills); 3 and 4: split (FP32 pre-test, then the walk over
+// its survivors) with 4 or 3 blocks, uniform beams only.
 template <bool PER_EVENT>
 static const void *f64_kernel(int variant) {
   switch (variant) {
     case 1: return (const void *)phs_forward_f64_kernel<PER_EVENT, true, 4>;
     case 2: return (const void *)phs_forward_f64_kernel<PER_EVENT, true, 3>;
+    case 3: return (const void *)phs_f64_walk_kernel<4>;
+    case 4: return (const void *)phs_f64_walk_kernel<3>;
     default: return (const void *)phs_forward_f64_kernel<PER_EVENT, false, 4>;
   }
 }
@@ -183,6 +219,16 @@ cudaError_t phs_launch_forward_f64(const PhsLaunch &a, int n_blocks, int variant
                                    cudaStream_t stream) {
   if (a.n_tiles <= 0) return cudaSuccess;
   const size_t smem = phs_forward_smem_bytes(a.stack_depth);
+  if (variant >= 3) {
+    if (a.E1 || a.E2) return cudaErrorInvalidValue;  // the pre-test needs uniform beams
+    cudaError_t e = phs_launch_pretest(a, stream);
+    if (e != cudaSuccess) return e;
+    if (variant == 3)
+      phs_f64_walk_kernel<4><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+    else
+      phs_f64_walk_kernel<3><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+    return cudaGetLastError();
+  }
   if (a.E1 && a.E2)
     launch_f64<true>(a, n_blocks, variant, smem, stream);
   else

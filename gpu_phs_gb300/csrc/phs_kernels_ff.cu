@@ -648,6 +648,19 @@ size_t phs_forward_ff_smem_bytes(int stack_depth) {
          (size_t)(PHS_FWD_BLOCK / 32) * 64 * sizeof(int64_t);
 }
 
+cudaError_t phs_launch_pretest(const PhsLaunch &a, cudaStream_t stream) {
+  if (a.n_tiles <= 0) return cudaSuccess;
+  int dev = 0, sms = 1, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, phs_ff_test_kernel, PHS_FWD_BLOCK, 0);
+  const int64_t want = (a.n_chunks + PHS_FWD_BLOCK / 32 - 1) / (PHS_FWD_BLOCK / 32);
+  const int64_t cap = (int64_t)(sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+  phs_ff_test_kernel<<<(int)(want < cap ? want : cap), PHS_FWD_BLOCK, 0, stream>>>(a);
+  phs_ff_pass_scan_kernel<<<1, 1024, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
 // variant bit 0: register budget for 4 (1) or 3 (0) resident blocks; bit 1: compacting
 // (fused pre-test); variants 4 and 5: the split form (pre-test kernel, scan, walk kernel).
 static size_t ff_walk_smem_bytes(int stack_depth) {
@@ -676,15 +689,8 @@ int phs_forward_ff_blocks_per_sm(int stack_depth, int variant) {
 cudaError_t phs_launch_forward_ff(const PhsLaunch &a, int n_blocks, int variant, cudaStream_t stream) {
   if (a.n_tiles <= 0) return cudaSuccess;
   if (variant >= 4) {
-    // a.pass_count and a.work are zeroed by the caller
-    int dev = 0, sms = 1, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, phs_ff_test_kernel, PHS_FWD_BLOCK, 0);
-    const int64_t want = (a.n_tiles + PHS_FWD_BLOCK / 32 - 1) / (PHS_FWD_BLOCK / 32);
-    const int64_t cap = (int64_t)(sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
-    phs_ff_test_kernel<<<(int)(want < cap ? want : cap), PHS_FWD_BLOCK, 0, stream>>>(a);
-    phs_ff_pass_scan_kernel<<<1, 1024, 0, stream>>>(a);
+    cudaError_t e = phs_launch_pretest(a, stream);
+    if (e != cudaSuccess) return e;
     const size_t smem = ff_walk_smem_bytes(a.stack_depth);
     if (variant == 5)
       phs_ff_walk_kernel<4><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);

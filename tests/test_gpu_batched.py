@@ -81,7 +81,7 @@ def _gen_batch(torch, spaces, counts, x, prec, ff_v=-1, f64_v=-1):
     return [t.clone() for t in out]
 
 
-@pytest.mark.parametrize("prec,n_var", [(0, 3), (1, 6)])
+@pytest.mark.parametrize("prec,n_var", [(0, 5), (1, 6)])
 def test_kernel_variants_identical_bits(torch, prec, n_var):
     """Every kernel variant (register budgets, one-pass, compacting or split) computes the
     same bits: the compacting and split forms run the same event code on the events that
@@ -102,10 +102,10 @@ def test_kernel_variants_identical_bits(torch, prec, n_var):
             assert torch.equal(a, b), f"variant {v} differs from variant 0"
 
 
-@pytest.mark.parametrize("f64_v", [1, 2])
+@pytest.mark.parametrize("f64_v", [1, 2, 3, 4])
 def test_compacting_fp64_vs_oracle_low_ok_fraction(torch, f64_v):
-    """The 13 TeV configuration (about 4% of events pass) through a compacting variant,
-    against the oracle."""
+    """The 13 TeV configuration (about 4% of events pass) through a compacting or split
+    variant, against the oracle."""
     from conftest import momentum_rel_err
     from gpu_phs_gb300.api import PhaseSpace
     from gpu_phs_gb300.philox import uniform_x
@@ -144,3 +144,25 @@ def test_split_form_many_segments_and_empty_channels(torch):
         got = _gen_batch(torch, spaces, counts, x, 1, ff_v=v)
         for a, b in zip(ref, got):
             assert torch.equal(a, b), f"variant {v} differs from variant 0"
+
+
+def test_per_event_beams_with_a_split_variant_pinned(torch):
+    """The FP32 pre-test needs uniform beams: with per-event beams a pinned split variant
+    runs as the compacting one, with the same bits as the one-pass kernel."""
+    from gpu_phs_gb300.api import PhaseSpace, philox_x
+    proc = P.tt()
+    n = 100_000
+    x = philox_x(n, proc.n_x, seed=31)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    E1 = 300 + 400 * torch.rand(n, generator=g, device="cuda", dtype=torch.float64)
+    E2 = 300 + 400 * torch.rand(n, generator=g, device="cuda", dtype=torch.float64)
+    outs = []
+    for v in (0, 3, 4):
+        ps = PhaseSpace(proc)
+        ps.set_variants(-1, v)
+        ev = ps.generate_beams(x, E1, E2)
+        torch.cuda.synchronize()
+        outs.append((ev.p.clone(), ev.factor.clone(), ev.volume.clone(), ev.ok.clone()))
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            assert torch.equal(a, b)
