@@ -199,11 +199,14 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64):
                             "error_vs_fp64": _errors(torch, out_tt, o, proc.sqrts)}
     del o
 
-    # Three FP64/FP32 forms per workload: FP64 one pass (the plain kernel, every event
-    # walked in full), FP64 autotuned (one pass or compacting: test every event first, walk
-    # only those that pass), and FP32 pair autotuned (register budgets x one pass /
-    # compacting with an FP32 first pass).  All three produce identical ok flags.
-    forms = (("fp64_one_pass", 0, 0), ("fp64", 0, -1), ("fp32_mixed", 1, -1))
+    # Four forms per workload, three of them FP64 with identical output bits: FP64 one pass
+    # (the plain kernel, every event walked in full), FP64 compacting (an FP64 pass tests
+    # every event first, only those that pass are walked), FP64 autotuned over all FP64
+    # variants (including the split form: an FP32 pre-test with error bounds settles only
+    # the events that fail for certain, the FP64 walk computes the rest), and the FP32 pair
+    # form autotuned (register budgets x one pass / compacting / split).
+    forms = (("fp64_one_pass", 0, 0), ("fp64_compacting", 0, 2), ("fp64", 0, -1),
+             ("fp32_mixed", 1, -1))
 
     proc = P.precision()
     n = 1 << 24
@@ -223,8 +226,11 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64):
         "kernel_variants": tuned,
         "speedup": t["fp64"] / t["fp32_mixed"],
         "speedup_vs_fp64_one_pass": t["fp64_one_pass"] / t["fp32_mixed"],
+        "speedup_vs_fp64_compacting": t["fp64_compacting"] / t["fp32_mixed"],
         "ok_fraction": outs["fp64"].ok.double().mean().item(),
-        "ok_mismatches_fp64_forms": int((outs["fp64"].ok != outs["fp64_one_pass"].ok).sum().item()),
+        "fp64_forms_identical_bits": all(
+            torch.equal(getattr(outs["fp64"], f), getattr(outs[k], f))
+            for k in ("fp64_one_pass", "fp64_compacting") for f in ("p", "factor", "volume", "ok")),
         "error_vs_fp64": _errors(torch, outs["fp64"], outs["fp32_mixed"], proc.sqrts)}
     del outs, x
 
@@ -265,9 +271,12 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64):
         "kernel_variants": tuned,
         "speedup": bres["fp64"] / bres["fp32_mixed"],
         "speedup_vs_fp64_one_pass": bres["fp64_one_pass"] / bres["fp32_mixed"],
+        "speedup_vs_fp64_compacting": bres["fp64_compacting"] / bres["fp32_mixed"],
         "ok_fraction": ok64.double().mean().item(),
         "ok_mismatches_fp32_mixed_vs_fp64": int((ok64 != bufs["fp32_mixed"][3]).sum().item()),
-        "ok_mismatches_fp64_forms": int((ok64 != bufs["fp64_one_pass"][3]).sum().item()),
+        "fp64_forms_identical_bits": all(
+            torch.equal(a, b) for k in ("fp64_one_pass", "fp64_compacting")
+            for a, b in zip(bufs["fp64"], bufs[k])),
         "ok_mismatches_vs_per_channel_runs": per_channel_mism}
     # momentum / factor error of the FP32-pair batch against FP64 (ok events)
     sel = ok64.bool()
@@ -541,6 +550,8 @@ def run_ours(args):
         variants["fp32_mixed_over_fp64_batched"] = variants["batched_64ch"]["speedup"]
         variants["fp32_mixed_over_fp64_one_pass_batched"] = (
             variants["batched_64ch"]["speedup_vs_fp64_one_pass"])
+        variants["fp32_mixed_over_fp64_compacting_batched"] = (
+            variants["batched_64ch"]["speedup_vs_fp64_compacting"])
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -71,7 +71,7 @@ struct Segments {
   DevBuf dev;
   std::vector<PhsSegment> uploaded;  // content of dev
   DevBuf work;                       // chunk counter of the compacting kernels
-  DevBuf exact_n, exact_q;           // FP32-pair launches: the exact-path queue
+  DevBuf exact_n, exact_q, exact_t;  // FP32-pair launches: the exact-path queues
   DevBuf pass_n, pass_t, pass_q;     // FP32-pair split form: pre-test survivors per segment
   int64_t n_tiles = 0;
   int64_t n_chunks = 0;
@@ -81,6 +81,7 @@ struct Segments {
     work.release();
     exact_n.release();
     exact_q.release();
+    exact_t.release();
     pass_n.release();
     pass_t.release();
     pass_q.release();
@@ -134,7 +135,7 @@ int attach_segments(Segments &S, PhsLaunch &a, cudaStream_t stream) {
   a.n_tiles = S.n_tiles;
   a.n_chunks = S.n_chunks;
   a.segments = nullptr;
-  if (int rc = S.work.reserve(sizeof(unsigned long long))) return rc;
+  if (int rc = S.work.reserve(2 * sizeof(unsigned long long))) return rc;
   a.work = S.work.as<unsigned long long>();
   if (S.host.size() <= PHS_INLINE_SEGS) {
     std::copy(S.host.begin(), S.host.end(), a.seg_inline);
@@ -239,16 +240,20 @@ int attach_pass_buffers(Segments &S, PhsLaunch &a) {
 
 int launch_ff_tuned(int &variant, Segments &S, PhsLaunch a, int device, int depth,
                     int64_t n_events, cudaStream_t st) {
-  if (int rc = S.exact_n.reserve(sizeof(unsigned long long))) return rc;
-  if (int rc = S.exact_q.reserve((size_t)std::max<int64_t>(n_events, 1) * sizeof(uint64_t)))
+  const size_t n_seg = (size_t)std::max(a.n_segments, 1);
+  if (int rc = S.exact_n.reserve(n_seg * sizeof(unsigned int))) return rc;
+  if (int rc = S.exact_t.reserve((n_seg + 1) * sizeof(int64_t))) return rc;
+  if (int rc = S.exact_q.reserve((size_t)std::max<int64_t>(a.n_tiles, 1) * 32 * sizeof(int32_t)))
     return rc;
   if (int rc = attach_pass_buffers(S, a)) return rc;
-  a.exact_count = S.exact_n.as<unsigned long long>();
-  a.exact_queue = S.exact_q.as<uint64_t>();
-  const int exact_grid = sm_count(device) * 2;
+  a.exact_work = a.work + 1;  // attach_segments reserved two counters
+  a.exact_count = S.exact_n.as<unsigned int>();
+  a.exact_queue = S.exact_q.as<int32_t>();
+  a.exact_tile = S.exact_t.as<int64_t>();
+  const int exact_grid = sm_count(device) * 4;
   return launch_tuned(variant, PHS_FF_VARIANTS, n_events, st, [&](int v) {
-    cudaError_t e = cudaMemsetAsync(a.exact_count, 0, sizeof(unsigned long long), st);
-    if (e == cudaSuccess && a.work) e = cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), st);
+    cudaError_t e = cudaMemsetAsync(a.exact_count, 0, (size_t)a.n_segments * sizeof(unsigned int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a.work, 0, 2 * sizeof(unsigned long long), st);
     if (e == cudaSuccess && v >= 4)
       e = cudaMemsetAsync(a.pass_count, 0, (size_t)a.n_segments * sizeof(unsigned int), st);
     if (e == cudaSuccess) e = phs_launch_forward_ff(a, grid_for_ff(a.n_tiles, device, depth, v), v, st);

@@ -27,8 +27,14 @@ struct PhsLaunch {
   const double *E2;
   unsigned long long *work;    // compacting kernels: chunk counter, zeroed before the
                                // launch (warps claim chunks dynamically); null: static
-  unsigned long long *exact_count;  // FP32-pair launches: events queued for the exact
-  uint64_t *exact_queue;            //   FP64 path (segment << 40 | local), zeroed before
+  // FP32-pair launches: the events queued for the exact FP64 path, per segment as the
+  // pre-test survivors are (count zeroed before the launch; local indices from
+  // tile_begin * 32 on; the dense claim numbering [n_segments + 1]; the exact launch's
+  // claim counter, zeroed before the launch)
+  unsigned int *exact_count;
+  int32_t *exact_queue;
+  int64_t *exact_tile;
+  unsigned long long *exact_work;
   // FP32-pair split form: per segment, the events that passed the pre-test (count, zeroed
   // before the launch), the walk's dense claim numbering ([n_segments + 1]) and their local
   // indices (segment s from tile_begin * 32 on; n_tiles * 32 entries).
@@ -75,7 +81,7 @@ size_t phs_noalloc_scratch_bytes();
 
 // Forward launch on the FP32 pipe (float-float arithmetic), FP64 only for events within
 // 1e-5 of a kinematic limit, which it queues for phs_launch_forward_exact (phs_kernels_ff.cu).
-// Needs a.channels, a.channels_ff, a.exact_count (zeroed) and a.exact_queue (n events);
+// Needs a.channels, a.channels_ff and the a.exact_* buffers (count and work zeroed);
 // uniform beams only.
 // variant bit 0: registers for 4 (1) or 3 (0) resident blocks per SM; bit 1: the
 // compacting two-pass form; variants 4 and 5 (bit 0 as before): the split form, the FP32
@@ -90,7 +96,12 @@ size_t phs_forward_ff_smem_bytes(int stack_depth);
 // a.pass_queue / a.pass_count (zeroed before) with the dense claim numbering a.pass_tile.
 // Uniform beams only (it reads the float-float programs' constants).
 cudaError_t phs_launch_pretest(const PhsLaunch &a, cudaStream_t stream);
-// The exact FP64 path over the events an FP32-pair launch queued (a.exact_queue).
+// Dense claim numbering of per-segment queues: tile[s] = sum over the segments before s of
+// ceil(count / 32), tile[n] their total (one block).
+cudaError_t phs_launch_count_scan(const unsigned int *count, int64_t *tile, int n,
+                                  cudaStream_t stream);
+// The exact FP64 path over the events an FP32-pair launch queued (a.exact_queue): the scan
+// of their counts, then the FP64 walk, 32 events of one segment per warp claim.
 cudaError_t phs_launch_forward_exact(const PhsLaunch &a, int n_blocks, cudaStream_t stream);
 
 // Reverse-mode derivatives (phs_adjoint.cu): xbar [event][x stride] and thbar

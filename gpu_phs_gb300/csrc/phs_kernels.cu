@@ -60,25 +60,36 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
   }
 }
 
-// The exact FP64 path for the events the FP32-pair kernel queued (a.exact_queue: segment
-// index << 40 | event within the segment; *a.exact_count entries).  Those are events within
-// 1e-5 of a kinematic limit, and all events of channels whose mappings or boosts have no
-// float-float form; keeping their FP64 code out of the FP32-pair kernel keeps that
-// kernel's body small.  A grid-stride loop: the count is read on the device, so the launch
-// can sit in a CUDA graph behind the FP32-pair launch.
+// The exact FP64 path for the events the FP32-pair kernel queued, per segment
+// (a.exact_queue from tile_begin * 32 on, a.exact_count entries, claims numbered by
+// a.exact_tile).  Those are events within 1e-5 of a kinematic limit, and all events of
+// channels whose mappings or boosts have no float-float form; keeping their FP64 code out
+// of the FP32-pair kernel keeps that kernel's body small.  Warps claim 32 events of one
+// segment (a.exact_work counts the claims), so each runs one channel's program; the counts
+// are read on the device, so the launch can sit in a CUDA graph behind the FP32-pair one.
 __global__ void __launch_bounds__(PHS_FWD_BLOCK, 4)
     phs_forward_exact_kernel(const __grid_constant__ PhsLaunch a) {
   extern __shared__ double smem[];
+  const int lane = threadIdx.x & 31;
   double2 *trig = phs_trig_table(smem, a.stack_depth);
   fill_trig_table(trig);
   __syncthreads();
   const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
-  const int64_t n = (int64_t)*a.exact_count;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const uint64_t e = a.exact_queue[i];
-    const PhsSegment seg = segs[e >> 40];
-    phs_event_f64<false>(a, seg, (int64_t)(e & ((1ull << 40) - 1)), smem, trig);
+  const int64_t n_claims = a.exact_tile[a.n_segments];
+  for (;;) {
+    unsigned long long c = 0;
+    if (lane == 0) c = atomicAdd(a.exact_work, 1ull);
+    const int64_t t = (int64_t)__shfl_sync(0xffffffffu, c, 0);
+    if (t >= n_claims) break;
+    int lo = 0, hi = a.n_segments - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (a.exact_tile[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    const PhsSegment seg = segs[lo];
+    const int64_t idx = (t - a.exact_tile[lo]) * 32 + lane;
+    if (idx >= (int64_t)a.exact_count[lo]) continue;
+    phs_event_f64<false>(a, seg, a.exact_queue[seg.tile_begin * 32 + idx], smem, trig);
   }
 }
 
@@ -238,6 +249,8 @@ cudaError_t phs_launch_forward_f64(const PhsLaunch &a, int n_blocks, int variant
 
 cudaError_t phs_launch_forward_exact(const PhsLaunch &a, int n_blocks, cudaStream_t stream) {
   if (a.n_tiles <= 0) return cudaSuccess;
+  cudaError_t e = phs_launch_count_scan(a.exact_count, a.exact_tile, a.n_segments, stream);
+  if (e != cudaSuccess) return e;
   phs_forward_exact_kernel<<<n_blocks, PHS_FWD_BLOCK, phs_forward_smem_bytes(a.stack_depth),
                              stream>>>(a);
   return cudaGetLastError();

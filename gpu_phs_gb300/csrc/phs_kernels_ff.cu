@@ -326,6 +326,14 @@ __device__ __forceinline__ float msq_f32(int map_id, float4 c, float c4, float c
   return 0.0f;
 }
 
+// Queues event `local` of segment si for the exact FP64 launch (each event at most once,
+// so the slot stays below the segment's event count).
+__device__ __forceinline__ void queue_exact(const PhsLaunch &a, int si, int64_t local) {
+  const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
+  const unsigned slot = atomicAdd(a.exact_count + si, 1u);
+  a.exact_queue[segs[si].tile_begin * 32 + slot] = (int32_t)local;
+}
+
 // The reduction tables of the float-float functions, built per block in shared memory,
 // exact at multiples of pi/2 (threads 0..95; the caller synchronises).
 __device__ __forceinline__ void fill_ff_tables(FFTables &T) {
@@ -485,10 +493,7 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
   // uses one at a time, and no slot of one thread overlaps another thread's
   float *fst = reinterpret_cast<float *>(smem_raw + sizeof(FFTables));
   // events the float-float walk cannot decide go to the exact FP64 launch behind this one
-  auto to_exact = [&](int si, int64_t loc) {
-    const unsigned long long slot = atomicAdd(a.exact_count, 1ull);
-    a.exact_queue[slot] = ((uint64_t)si << 40) | (uint64_t)loc;
-  };
+  auto to_exact = [&](int si, int64_t loc) { queue_exact(a, si, loc); };
 
   fill_ff_tables(T);
   __syncthreads();
@@ -575,16 +580,17 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, PHS_FF_TEST_MIN_BLOCKS)
   }
 }
 
-// Kernel 2 of 3 (one block): pass_tile[s] = sum over the segments before s of
-// ceil(pass_count / 32), the dense numbering of the walk's warp tiles; pass_tile[n] is
-// their total.
-__global__ void __launch_bounds__(1024) phs_ff_pass_scan_kernel(const __grid_constant__ PhsLaunch a) {
+// Kernel 2 of 3 (one block): tile[s] = sum over the segments before s of
+// ceil(count / 32), the dense numbering of the next kernel's warp claims; tile[n] is their
+// total.  Also serves the exact path's queues.
+__global__ void __launch_bounds__(1024)
+    phs_count_scan_kernel(const unsigned int *count, int64_t *tile, int n) {
   __shared__ int64_t warp_sum[32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   int64_t carry = 0;
-  for (int base = 0; base < a.n_segments; base += blockDim.x) {
+  for (int base = 0; base < n; base += blockDim.x) {
     const int s = base + threadIdx.x;
-    const int64_t v = s < a.n_segments ? ((int64_t)a.pass_count[s] + 31) / 32 : 0;
+    const int64_t v = s < n ? ((int64_t)count[s] + 31) / 32 : 0;
     int64_t inc = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -598,11 +604,11 @@ __global__ void __launch_bounds__(1024) phs_ff_pass_scan_kernel(const __grid_con
       if (w < wid) before += warp_sum[w];
       total += warp_sum[w];
     }
-    if (s < a.n_segments) a.pass_tile[s] = carry + before + inc - v;
+    if (s < n) tile[s] = carry + before + inc - v;
     carry += total;
     __syncthreads();
   }
-  if (threadIdx.x == 0) a.pass_tile[a.n_segments] = carry;
+  if (threadIdx.x == 0) tile[n] = carry;
 }
 
 // Kernel 3 of 3: the float-float walk over the queued events, 32 of one segment per warp
@@ -635,8 +641,7 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
     if (idx >= (int64_t)a.pass_count[lo]) continue;
     const int64_t local = a.pass_queue[seg.tile_begin * 32 + idx];
     if (!phs_event_ff(a, seg, local, T, fst)) {
-      const unsigned long long slot = atomicAdd(a.exact_count, 1ull);
-      a.exact_queue[slot] = ((uint64_t)lo << 40) | (uint64_t)local;
+      queue_exact(a, lo, local);
     }
   }
 }
@@ -657,7 +662,13 @@ cudaError_t phs_launch_pretest(const PhsLaunch &a, cudaStream_t stream) {
   const int64_t want = (a.n_chunks + PHS_FWD_BLOCK / 32 - 1) / (PHS_FWD_BLOCK / 32);
   const int64_t cap = (int64_t)(sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
   phs_ff_test_kernel<<<(int)(want < cap ? want : cap), PHS_FWD_BLOCK, 0, stream>>>(a);
-  phs_ff_pass_scan_kernel<<<1, 1024, 0, stream>>>(a);
+  phs_count_scan_kernel<<<1, 1024, 0, stream>>>(a.pass_count, a.pass_tile, a.n_segments);
+  return cudaGetLastError();
+}
+
+cudaError_t phs_launch_count_scan(const unsigned int *count, int64_t *tile, int n,
+                                  cudaStream_t stream) {
+  phs_count_scan_kernel<<<1, 1024, 0, stream>>>(count, tile, n);
   return cudaGetLastError();
 }
 

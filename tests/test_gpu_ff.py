@@ -24,10 +24,16 @@ def torch():
     return torch
 
 
-def run(torch, proc, x, sqrts, counts=None, precision=1):
+# FP32-pair kernel variants: one pass, fused compacting, split (pre-test kernel + walk)
+FF_FORMS = [0, 3, 5]
+
+
+def run(torch, proc, x, sqrts, counts=None, precision=1, variant=-1):
     from gpu_phs_gb300.api import PhaseSpace
     ps = PhaseSpace(proc, sqrts / 2, sqrts / 2)
     ps.set_precision(precision)
+    if precision == 1:
+        ps.set_variants(variant, -1)
     ev = ps.generate(torch.from_numpy(np.ascontiguousarray(x)).cuda(), counts)
     torch.cuda.synchronize()
     return ev.p.cpu().numpy(), ev.factor.cpu().numpy(), ev.volume.cpu().numpy(), ev.ok.cpu().numpy()
@@ -64,15 +70,19 @@ def test_ff_vs_reference_fixture(torch, name):
     check(got, z["p"], z["factor"], z["volume"], z["ok"], sq)
 
 
-def test_ff_whizard_golden_bwbw(torch):
+@pytest.mark.parametrize("variant", FF_FORMS)
+def test_ff_whizard_golden_bwbw(torch, variant):
+    """Whizard's 61 bwbw channels, 16 of them with friend boosts (exact path only)."""
     z = golden("whizard_bwbw")
     proc = load_process(z)
     counts = counts_of(z["channel"], proc.n_channels)
     r = oracle.Oracle(proc, 1000.0).generate(z["x"], z["channel"])
-    check(run(torch, proc, z["x"], 1000.0, counts), r.p, r.factor, r.volume, r.ok, 1000.0)
+    check(run(torch, proc, z["x"], 1000.0, counts, variant=variant), r.p, r.factor, r.volume,
+          r.ok, 1000.0)
 
 
-def test_ff_fallback_at_kinematic_limits(torch):
+@pytest.mark.parametrize("variant", FF_FORMS)
+def test_ff_fallback_at_kinematic_limits(torch, variant):
     """x = 0 on an unmapped branch gives msq = msq_min exactly: m = m1 + m2, a tie the
     reference decides as not ok.  Those events must take the exact path."""
     rng = np.random.default_rng(5)
@@ -83,7 +93,7 @@ def test_ff_fallback_at_kinematic_limits(torch):
     x[::3, :proc.n_out - 2] = 0.0                            # msq at the lower limit
     x[1::7, :proc.n_out - 2] = 1.0 - 2.0 ** -53              # msq just below the upper limit
     r = oracle.Oracle(proc, 1000.0).generate(x)
-    check(run(torch, proc, x, 1000.0), r.p, r.factor, r.volume, r.ok, 1000.0)
+    check(run(torch, proc, x, 1000.0, variant=variant), r.p, r.factor, r.volume, r.ok, 1000.0)
     f64 = run(torch, proc, x, 1000.0, precision=0)
     assert np.array_equal(f64[3], r.ok)
 
@@ -129,7 +139,8 @@ def test_ff_batch(torch):
         e += c
 
 
-def test_ff_exact_path_beside_ff_warps(torch):
+@pytest.mark.parametrize("variant", FF_FORMS)
+def test_ff_exact_path_beside_ff_warps(torch, variant):
     """Channels alternate between trees the float-float path handles and trees with a STEP
     mapping (exact path only), so blocks run both paths at once; the paths share the
     frame stack memory and must not disturb each other."""
@@ -143,7 +154,8 @@ def test_ff_exact_path_beside_ff_warps(torch):
     channels = np.repeat(np.arange(n_ch), counts).astype(np.int32)
     x = uniform_x(91, int(counts.sum()), proc.n_x)
     r = oracle.Oracle(proc, 1000.0).generate(x, channels)
-    check(run(torch, proc, x, 1000.0, counts), r.p, r.factor, r.volume, r.ok, 1000.0)
+    check(run(torch, proc, x, 1000.0, counts, variant=variant), r.p, r.factor, r.volume, r.ok,
+          1000.0)
 
 
 def test_ff_matches_f64_kernel_tt_full_size(torch):
