@@ -174,7 +174,7 @@ def _errors(torch, ref, got, sqrts):
             "definition": "per particle max_mu |dp^mu| / max(E, 1e-3 sqrt(s)); unfloored: / E"}
 
 
-def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64):
+def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64, pin=(-1, -1)):
     """FP32-pair arithmetic on the tt workload, the 13 TeV configuration and the batched
     64-channel workload (CUDA-graph replay), each beside FP64 on the same x."""
     import ctypes as C
@@ -205,18 +205,21 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64):
     # variants (including the split form: an FP32 pre-test with error bounds settles only
     # the events that fail for certain, the FP64 walk computes the rest), and the FP32 pair
     # form autotuned (register budgets x one pass / compacting / split).
-    forms = (("fp64_one_pass", 0, 0), ("fp64_compacting", 0, 2), ("fp64", 0, -1),
-             ("fp32_mixed", 1, -1))
+    # (name, precision, kernel variant of that precision).  pin: the (FP32 pair, FP64)
+    # variants of the autotuned forms (-1: the autotuner picks; a profiler distorts its
+    # timings, so a profiled run pins what the plain run picked)
+    forms = (("fp64_one_pass", 0, 0), ("fp64_compacting", 0, 2), ("fp64", 0, pin[1]),
+             ("fp32_mixed", 1, pin[0]))
 
     proc = P.precision()
     n = 1 << 24
     x = torch.empty((n, proc.n_x), dtype=torch.float64, device="cuda")
     philox_fill(x, n, proc.n_x, SEED)
     outs, t, tuned = {}, {}, {}
-    for name, prec, f64v in forms:
+    for name, prec, var in forms:
         ps = PhaseSpace(proc, proc.sqrts / 2, proc.sqrts / 2)
         ps.set_precision(prec)
-        ps.set_variants(-1, f64v)
+        ps.set_variants(var if prec else -1, -1 if prec else var)
         outs[name] = ps.alloc(n)
         t[name] = _time_calls(torch, lambda: ps.generate(x, out=outs[name]), steps, warmup, stream)
         tuned[name] = ps.tuning()[prec == 0]
@@ -238,10 +241,10 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64):
     spaces = [PhaseSpace(p, 500.0, 500.0) for p in procs]
     n = int(counts.sum())
     bres, bufs, tuned = {}, {}, {}
-    for name, prec, f64v in forms:
+    for name, prec, var in forms:
         batch = Batch(spaces)
         batch.set_precision(prec)
-        batch.set_variants(-1, f64v)
+        batch.set_variants(var if prec else -1, -1 if prec else var)
         xo, po = batch.offsets(counts)
         if name == "fp64_one_pass":
             xb = torch.empty(int(xo[-1]), dtype=torch.float64, device="cuda")
@@ -546,7 +549,8 @@ def run_ours(args):
 
     variants = None
     if not args.no_variants and world == 1:
-        variants = measure_variants(torch, args.steps, args.warmup, x, out, ms_per_step)
+        variants = measure_variants(torch, args.steps, args.warmup, x, out, ms_per_step,
+                                    tuple(int(v) for v in args.pin.split(",")))
         variants["fp32_mixed_over_fp64_batched"] = variants["batched_64ch"]["speedup"]
         variants["fp32_mixed_over_fp64_one_pass_batched"] = (
             variants["batched_64ch"]["speedup_vs_fp64_one_pass"])
@@ -595,7 +599,8 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-PROFILE_CASES = ("f64_tt", "f64_batched", "ff_batched", "inverse_bwbw", "adjoint_tt")
+PROFILE_CASES = ("f64_tt", "f64_batched", "f64_split_batched", "ff_batched", "inverse_bwbw",
+                 "adjoint_tt")
 
 
 def run_case(name: str) -> None:
@@ -614,13 +619,15 @@ def run_case(name: str) -> None:
         o = ps.alloc(n)
         for _ in range(2):
             ps.generate(x, out=o)
-    elif name in ("f64_batched", "ff_batched"):   # 2^22 batched events, compacting / split
+    elif name in ("f64_batched", "f64_split_batched", "ff_batched"):   # 2^22 batched events
         procs, counts = P.batched(seed=2024, n_channels=64, total_events=1 << 22)
         b = Batch([PhaseSpace(p, 500.0, 500.0) for p in procs])
-        if name == "ff_batched":
+        if name == "ff_batched":          # split: FP32 pre-test, float-float walk
             b.set_precision(1)
             b.set_variants(5, -1)
-        else:
+        elif name == "f64_split_batched":  # split: FP32 pre-test, FP64 walk
+            b.set_variants(-1, 4)
+        else:                              # compacting, FP64 pre-test
             b.set_variants(-1, 2)
         xo, _ = b.offsets(counts)
         x = torch.empty(int(xo[-1]), dtype=torch.float64, device="cuda")
@@ -663,6 +670,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--pin", default="-1,-1",
+                    help="FP32-pair,FP64 kernel variants of the autotuned forms in the "
+                         "13 TeV and batched measurements (-1: autotune); for profiled runs")
     ap.add_argument("--case", choices=PROFILE_CASES, default=None,
                     help="run one small profiling workload instead of the benchmark")
     args = ap.parse_args()
