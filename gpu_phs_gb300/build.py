@@ -50,7 +50,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
     """Compile and link; returns the library path.  Raises RuntimeError on failure."""
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    headers.append(os.path.join(ROOT, "include", "gpu_phs.h"))
+    inc_dir = os.path.join(ROOT, "include")
+    headers += [os.path.join(inc_dir, f) for f in os.listdir(inc_dir) if f.endswith(".h")]
     inc = ["-I", os.path.join(ROOT, "include"), "-I", CSRC, "-I", os.path.join(CUDA_HOME, "include")]
     jobs, objs = [], []
     for src in CU_SOURCES:

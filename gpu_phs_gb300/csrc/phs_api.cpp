@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/gpu_phs.h"
+#include "../../include/gpu_phs_transfer.h"
 #include "phs_device.h"
 #include "phs_host.h"
 
@@ -1079,6 +1080,10 @@ struct Whizard {
   phs_process_t proc = nullptr;
   DevBuf dx, dp, df, dv, dok;
   DevBuf dfa, dxo;  // all-channel factors and x of the inverse map
+  DevBuf dsparse, din;  // device handoff in the reference's layouts, built on request
+  bool sparse_ok = false, in_ok = false, last_uniform = true;
+  double last_e1 = 0, last_e2 = 0;
+  std::vector<uint32_t> internal;  // bit code: an internal branch of some channel
   int64_t last_events = 0;
   int msq_threads = 0, cb_threads = 0, ab_threads = 0;
 };
@@ -1091,6 +1096,8 @@ void whizard_log(int rc) {
 void whizard_release_device() {
   W.dx.release(); W.dp.release(); W.df.release(); W.dv.release(); W.dok.release();
   W.dfa.release(); W.dxo.release();
+  W.dsparse.release(); W.din.release();
+  W.sparse_ok = W.in_ok = false;
   W.last_events = 0;
 }
 }  // namespace
@@ -1213,6 +1220,11 @@ extern "C" void c_whizard_init_gpu_phs(void) {
     return;
   }
   if (W.proc) { phs_process_destroy(W.proc); W.proc = nullptr; }
+  // codes of internal branches over all channels, for the sparse momentum handoff
+  W.internal.assign((1 << PHS_SPARSE_MAX_OUT) / 32, 0u);
+  for (int c = 0; c < W.n_channels && W.n_out <= PHS_SPARSE_MAX_OUT; c++)
+    for (int code = 1; code < (1 << W.n_out); code++)
+      if (W.hc[(size_t)c * W.n_prt + code - 1]) W.internal[code >> 5] |= 1u << (code & 31);
   whizard_log(phs_process_create(&W.proc, W.n_in, W.n_out, W.n_channels, W.n_x, W.d1.data(),
                                  W.d2.data(), W.hc.data(), W.fr.data(), W.map_id.data(),
                                  W.map_m.data(), W.map_w.data(), W.flv_m.data(), W.flv_w.data()));
@@ -1304,6 +1316,10 @@ extern "C" void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in,
     if (e == cudaSuccess) e = cudaMemcpy(oks, W.dok.ptr, n, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e)); break; }
     W.last_events = n;
+    W.sparse_ok = W.in_ok = false;  // the handoff buffers are rebuilt on request
+    W.last_uniform = uniform;
+    W.last_e1 = E1_in[0];
+    W.last_e2 = E2_in[0];
   } while (0);
   whizard_log(rc);
 }
@@ -1313,6 +1329,70 @@ extern "C" void c_whizard_get_momentum_device_pointer(double *p) { (void)p; }
 extern "C" double *phs_whizard_momentum_device_pointer(void) {
   std::lock_guard<std::mutex> lk(W.mu);
   return W.last_events ? W.dp.as<double>() : nullptr;
+}
+
+// The device handoff of the reference's transfer_to_whizard.h (C++ linkage, as there):
+// the last c_whizard_gen_phs_from_x_gpu call's momenta in the sparse Whizard layout, its
+// beam energies [E1...; E2...] and its ok flags, in device memory the library owns until
+// the next call, c_whizard_reset_generator or c_whizard_finalize_gpu_phs.  Null before the
+// first call or on error (phs_last_error).
+double *get_momentum_device_pointer() {
+  std::lock_guard<std::mutex> lk(W.mu);
+  if (!W.last_events || !W.proc) return nullptr;
+  if (W.sparse_ok) return W.dsparse.as<double>();
+  if (W.n_out > PHS_SPARSE_MAX_OUT) {
+    whizard_log(fail(PHS_ERR_UNSUPPORTED, "sparse momentum layout: n_out > %d", PHS_SPARSE_MAX_OUT));
+    return nullptr;
+  }
+  DeviceGuard g(W.proc->device);
+  const int64_t n = W.last_events;
+  int rc = W.dsparse.reserve((size_t)n * W.n_prt * 4 * sizeof(double));
+  if (rc) { whizard_log(rc); return nullptr; }
+  PhsSparseLaunch a;
+  memset(&a, 0, sizeof a);
+  a.p = W.dp.as<double>();
+  a.E1 = W.last_uniform ? nullptr : W.df.as<double>() + n;
+  a.E2 = W.last_uniform ? nullptr : W.df.as<double>() + 2 * n;
+  a.e1 = W.last_e1;
+  a.e2 = W.last_e2;
+  a.out = W.dsparse.as<double>();
+  a.n_events = n;
+  a.n_out = W.n_out;
+  a.n_prt = W.n_prt;
+  std::copy(W.internal.begin(), W.internal.end(), a.internal);
+  cudaError_t e = phs_launch_whizard_sparse(a, nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    whizard_log(fail(PHS_ERR_CUDA, "sparse momentum layout: %s", cudaGetErrorString(e)));
+    return nullptr;
+  }
+  W.sparse_ok = true;
+  return W.dsparse.as<double>();
+}
+
+double *get_in_momentum_device_pointer() {
+  std::lock_guard<std::mutex> lk(W.mu);
+  if (!W.last_events || !W.proc) return nullptr;
+  const int64_t n = W.last_events;
+  if (!W.last_uniform) return W.df.as<double>() + n;  // [E1; E2] as the per-event launch read them
+  if (W.in_ok) return W.din.as<double>();
+  DeviceGuard g(W.proc->device);
+  int rc = W.din.reserve((size_t)2 * n * sizeof(double));
+  if (rc) { whizard_log(rc); return nullptr; }
+  std::vector<double> h((size_t)2 * n, W.last_e1);
+  std::fill(h.begin() + n, h.end(), W.last_e2);
+  cudaError_t e = cudaMemcpy(W.din.ptr, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    whizard_log(fail(PHS_ERR_CUDA, "beam energies: %s", cudaGetErrorString(e)));
+    return nullptr;
+  }
+  W.in_ok = true;
+  return W.din.as<double>();
+}
+
+bool *get_ok_device_pointer() {
+  std::lock_guard<std::mutex> lk(W.mu);
+  return W.last_events ? reinterpret_cast<bool *>(W.dok.ptr) : nullptr;
 }
 
 extern "C" void c_whizard_reset_generator(void) {

@@ -69,6 +69,24 @@ cudaError_t phs_launch_philox(double *x, int64_t n_events, int32_t n_x, uint64_t
 cudaError_t phs_launch_fma_rate(void *out, int fp64, int blocks, int threads, int iters,
                                 cudaStream_t stream);
 
+// Whizard's sparse momentum layout (phs.cu:1364-1373): out[event][n_prt][4], slot code - 1
+// for every Whizard code up to n_prt = 2^(n_in + n_out) - 1.  Outgoing particles (codes
+// 2^k) hold their lab momenta; every code that is an internal branch of some channel
+// (bit code of `internal`) holds the sum of its particles' momenta in the centre-of-mass
+// frame, as the reference's buffer ends up after its inverse-map loop (phs.cu:1262-1283;
+// its lab boost touches the outgoing codes only, phs.cu:1286-1301); every other slot is 0.
+#define PHS_SPARSE_MAX_OUT 12
+struct PhsSparseLaunch {
+  const double *p;         // [event][n_out][4] lab momenta
+  const double *E1, *E2;   // per-event beams, or null: e1, e2 for every event
+  double e1, e2;
+  double *out;
+  int64_t n_events;
+  int32_t n_out, n_prt;
+  uint32_t internal[(1 << PHS_SPARSE_MAX_OUT) / 32];
+};
+cudaError_t phs_launch_whizard_sparse(const PhsSparseLaunch &a, cudaStream_t stream);
+
 // Forward launch whose channel programs and segment table are copied into a file-scope
 // device array of phs_kernels.cu (no device allocation; see there).  At most
 // PHS_NOALLOC_MAX_CHANNELS channels and as many segments; returns cudaErrorInvalidValue

@@ -126,6 +126,42 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
   }
 }
 
+// Whizard's sparse momentum buffer from the dense one (layout in phs_device.h): one thread
+// per 32-byte slot, consecutive threads on consecutive slots.
+__global__ void phs_whizard_sparse_kernel(const __grid_constant__ PhsSparseLaunch a) {
+  const int64_t total = a.n_events * a.n_prt;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ev = i / a.n_prt;
+    const int code = (int)(i - ev * a.n_prt) + 1;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    const double *pe = a.p + ev * 4 * a.n_out;
+    if (code < (1 << a.n_out)) {
+      if ((code & (code - 1)) == 0) {
+        const int k = __ffs(code) - 1;
+#pragma unroll
+        for (int mu = 0; mu < 4; mu++) v[mu] = pe[4 * k + mu];
+      } else if (a.internal[code >> 5] >> (code & 31) & 1u) {
+        // back to the centre-of-mass frame: the inverse of the lab boost
+        // p0 = gamma p0* + bg p3*, p3 = bg p0* + gamma p3* (phs.cu:1286-1301)
+        const double e1 = a.E1 ? a.E1[ev] : a.e1, e2 = a.E2 ? a.E2[ev] : a.e2;
+        const double bg = (e1 - e2) / (2.0 * sqrt(e1 * e2)), ga = sqrt(1.0 + bg * bg);
+        for (int k = 0; k < a.n_out; k++) {
+          if (!(code >> k & 1)) continue;
+          const double *q = pe + 4 * k;
+          v[0] += ga * q[0] - bg * q[3];
+          v[1] += q[1];
+          v[2] += q[2];
+          v[3] += ga * q[3] - bg * q[0];
+        }
+      }
+    }
+    double2 *o = reinterpret_cast<double2 *>(a.out + 4 * i);
+    o[0] = make_double2(v[0], v[1]);
+    o[1] = make_double2(v[2], v[3]);
+  }
+}
+
 // Philox4x32-10 (Salmon et al., SC'11); layout documented in gpu_phs_gb300/philox.py.
 __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
 #pragma unroll
@@ -253,6 +289,14 @@ cudaError_t phs_launch_forward_exact(const PhsLaunch &a, int n_blocks, cudaStrea
   if (e != cudaSuccess) return e;
   phs_forward_exact_kernel<<<n_blocks, PHS_FWD_BLOCK, phs_forward_smem_bytes(a.stack_depth),
                              stream>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t phs_launch_whizard_sparse(const PhsSparseLaunch &a, cudaStream_t stream) {
+  const int64_t total = a.n_events * a.n_prt;
+  if (total <= 0) return cudaSuccess;
+  const int64_t blocks = (total + 255) / 256;
+  phs_whizard_sparse_kernel<<<(int)(blocks < 152 * 32 ? blocks : 152 * 32), 256, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

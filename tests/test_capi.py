@@ -39,6 +39,24 @@ def test_exports_every_declared_symbol(lib):
         assert getattr(lib, s) is not None
 
 
+def test_exports_the_device_handoff_with_cpp_linkage(lib):
+    """include/gpu_phs_transfer.h declares the reference's transfer_to_whizard.h functions
+    with C++ linkage: the library exports them under their Itanium-mangled names."""
+    import re
+    hdr = os.path.join(os.path.dirname(_lib.HEADER), "gpu_phs_transfer.h")
+    text = re.sub(r"/\*.*?\*/", "", open(hdr).read(), flags=re.S)
+    names = re.findall(r"\b(get_\w+_device_pointer)\s*\(\s*\)", text)
+    assert sorted(names) == ["get_in_momentum_device_pointer", "get_momentum_device_pointer",
+                             "get_ok_device_pointer"]
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+    for nm in names:
+        mangled = f"_Z{len(nm)}{nm}v"
+        assert mangled in exported, mangled
+        assert getattr(lib, mangled) is not None
+
+
 def _create(lib, proc, **over):
     t = dict(d1=proc.d1, d2=proc.d2, hc=proc.has_children, fr=proc.friends, mid=proc.map_ids,
              mm=proc.map_masses, mw=proc.map_widths, fm=proc.flv_masses, fw=proc.flv_widths)

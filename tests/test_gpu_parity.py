@@ -271,6 +271,101 @@ def test_whizard_binding_end_to_end(torch):
     lib.c_whizard_finalize_gpu_phs()
 
 
+class _DeviceArray:
+    """A device pointer the library returned, seen by torch (CUDA array interface)."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr,
+                                         "data": (ptr, False), "version": 3, "strides": None}
+
+
+@pytest.mark.parametrize("beams", [(500.0, 500.0), (600.0, 420.0)])
+def test_whizard_device_handoff(torch, beams):
+    """The reference's transfer_to_whizard.h functions after a Whizard call: momenta in the
+    sparse [event][2^(n_in+n_out)-1][4] layout (outgoing codes in the lab frame, internal
+    codes of any channel as centre-of-mass sums, all else 0), the beams [E1; E2] and the ok
+    flags, all in device memory."""
+    from gpu_phs_gb300 import _lib
+    lib = _lib.load()
+    z = golden("whizard_ttH")
+    proc = load_process(z)
+    ip = lambda v: C.byref(C.c_int(v))
+    nch, n_x, n_out = proc.n_channels, proc.n_x, proc.n_out
+    lib.c_whizard_set_particle_structure(ip(nch), ip(nch), ip(nch), ip(n_x), ip(2), ip(n_out))
+    fm = np.ascontiguousarray(proc.flv_masses)
+    fw = np.ascontiguousarray(proc.flv_widths)
+    lib.c_whizard_set_flavors(fm.ctypes.data, fw.ctypes.data)
+    lib.c_whizard_init_mappings()
+    keep = []
+    for c in range(nch):
+        a = [np.ascontiguousarray(proc.map_ids[c], np.int32), np.ascontiguousarray(proc.map_masses[c]),
+             np.ascontiguousarray(proc.map_widths[c])]
+        keep += a
+        lib.c_whizard_fill_mapping(ip(c + 1), *[t.ctypes.data for t in a])
+    lib.c_whizard_init_tree_structures()
+    for c in range(nch):
+        a = [np.ascontiguousarray(t[c], np.int32) for t in (proc.d1, proc.d2, proc.has_children, proc.friends)]
+        keep += a
+        lib.c_whizard_fill_tree_structure(ip(c + 1), *[t.ctypes.data for t in a])
+    lib.c_whizard_init_gpu_phs()
+    counts = counts_of(z["channel"], nch)
+    n = int(counts.sum())
+    limits = np.ascontiguousarray(np.cumsum(counts), np.int32)
+    lib.c_whizard_init_channel_ids(ip(n), ip(nch), limits.ctypes.data)
+    x = np.ascontiguousarray(z["x"])
+    E1, E2 = np.full(n, beams[0]), np.full(n, beams[1])
+    factors, volumes = np.zeros(n * nch), np.zeros(n)
+    oks = np.zeros(n, np.uint8)
+    p = np.zeros(n * n_out * 4)
+    x_out = np.zeros(n * n_x * nch)
+    lib.c_whizard_gen_phs_from_x_gpu(E1.ctypes.data, E2.ctypes.data, C.byref(C.c_bool(False)), ip(n),
+                                     ip(nch), ip(n_x), x.ctypes.data, factors.ctypes.data,
+                                     volumes.ctypes.data, oks.ctypes.data, p.ctypes.data,
+                                     x_out.ctypes.data)
+    assert lib.phs_last_error().decode() == ""
+    getters = {}
+    for name, res in (("get_momentum_device_pointer", C.c_void_p),
+                      ("get_in_momentum_device_pointer", C.c_void_p),
+                      ("get_ok_device_pointer", C.c_void_p)):
+        f = getattr(lib, f"_Z{len(name)}{name}v")
+        f.restype = res
+        getters[name] = f
+    n_prt = 2 ** (2 + n_out) - 1
+    sp = torch.as_tensor(_DeviceArray(getters["get_momentum_device_pointer"](), (n, n_prt, 4), "<f8"),
+                         device="cuda").cpu().numpy()
+    pin = torch.as_tensor(_DeviceArray(getters["get_in_momentum_device_pointer"](), (2 * n,), "<f8"),
+                          device="cuda").cpu().numpy()
+    okd = torch.as_tensor(_DeviceArray(getters["get_ok_device_pointer"](), (n,), "|u1"),
+                          device="cuda").cpu().numpy()
+    assert np.array_equal(pin, np.concatenate([E1, E2]))
+    assert np.array_equal(okd, oks)
+    pl = p.reshape(n, n_out, 4)
+    # centre-of-mass frame: the inverse of the lab boost along z
+    bg = (E1 - E2) / (2 * np.sqrt(E1 * E2))
+    ga = np.sqrt(1 + bg * bg)
+    pcm = pl.copy()
+    pcm[..., 0] = ga[:, None] * pl[..., 0] - bg[:, None] * pl[..., 3]
+    pcm[..., 3] = ga[:, None] * pl[..., 3] - bg[:, None] * pl[..., 0]
+    internal = {code for c in range(nch) for code in range(1, 2 ** n_out)
+                if proc.has_children[c][code - 1]}
+    assert (2 ** n_out - 1) in internal
+    sqrts = 2 * np.sqrt(beams[0] * beams[1])
+    for code in range(1, n_prt + 1):
+        slot = sp[:, code - 1]
+        if code < 2 ** n_out and code & (code - 1) == 0:
+            assert np.array_equal(slot, pl[:, code.bit_length() - 1])
+        elif code in internal:
+            want = sum(pcm[:, k] for k in range(n_out) if code >> k & 1)
+            assert np.abs(slot - want).max() <= 1e-12 * sqrts
+        else:
+            assert not slot.any(), code
+    root = sp[oks == 1, 2 ** n_out - 2]
+    assert np.abs(root - np.array([sqrts, 0, 0, 0])).max() <= 1e-9
+    lib.c_whizard_reset_generator()
+    assert not getters["get_momentum_device_pointer"]()
+    lib.c_whizard_finalize_gpu_phs()
+
+
 def test_full_size_invariants_tt(torch):
     """1e7 tt events: the sizes the benchmark runs, checked through properties that do not
     need the oracle: momentum conservation, on-shell masses, a stable ok fraction."""
