@@ -58,14 +58,11 @@ __device__ __forceinline__ void map_msq_inverse(int t, double msq, double s, dou
     }
     case PHS_MAP_TCHANNEL:
     case PHS_MAP_UCHANNEL: {
-      double z;
-      if (msq < (msq_max + msq_min) / 2) {
-        z = msq - msq_min + a0;
-        x = log(z / a0) / a1;
-      } else {
-        z = msq_max - msq + a0;
-        x = 1.0 - log(z / a0) / a1;
-      }
+      // one logarithm per lane: the side of the midpoint selects its argument
+      const bool lower = msq < (msq_max + msq_min) / 2;
+      const double z = lower ? msq - msq_min + a0 : msq_max - msq + a0;
+      const double lx = log(z / a0) / a1;
+      x = lower ? lx : 1.0 - lx;
       f = a2 * z;
       break;
     }
@@ -93,14 +90,11 @@ __device__ __forceinline__ void map_msq_inverse(int t, double msq, double s, dou
 __device__ __forceinline__ void map_ct_inverse(int ct_class, double ct, double b0, double b1,
                                                double &x, double &f) {
   if (ct_class == PHS_CT_COLLINEAR) {
-    double ct1;
-    if (ct < 0.0) {
-      ct1 = ct + b0 + 1.0;
-      x = log(ct1 / b0) / (2.0 * b1);
-    } else {
-      ct1 = -ct + b0 + 1.0;
-      x = 1.0 - log(ct1 / b0) / (2.0 * b1);
-    }
+    // one logarithm per lane, as for the msq maps
+    const bool lower = ct < 0.0;
+    const double ct1 = lower ? ct + b0 + 1.0 : -ct + b0 + 1.0;
+    const double lx = log(ct1 / b0) / (2.0 * b1);
+    x = lower ? lx : 1.0 - lx;
     f = ct1 * b1;
   } else {
     x = (ct + 1.0) / 2.0;
