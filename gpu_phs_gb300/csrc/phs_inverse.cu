@@ -285,53 +285,91 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
   const int64_t n_tiles = (a.n_events + PHS_INV_BLOCK - 1) / PHS_INV_BLOCK;
   const PhsChannel &ch0 = a.channels[0];
 
+  __shared__ int64_t dense_ev[PHS_INV_BLOCK];  // the tile's ok events, packed
+  __shared__ int dense_own[PHS_INV_BLOCK];
+  __shared__ int warp_ok[PHS_INV_BLOCK / 32];
+  const int lane = tid & 31, wid = tid >> 5;
+
   for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    // 1. per event: the outputs that need no arithmetic (the generating channel's own x and
+    // factor, x padding beyond a channel's n_x_used, zeros for ok = false events)
     const int64_t ev = tile * PHS_INV_BLOCK + tid;
-    if (ev >= a.n_events) continue;
-    // the generating channel: the last c with ch_begin[c] <= ev
-    int lo = 0, hi = a.n_channels - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (a.ch_begin[mid] <= ev) lo = mid; else hi = mid - 1;
-    }
-    const int own = lo;
-    const bool ok = a.ok ? a.ok[ev] != 0 : true;
-    double sqrts = ch0.sqrts, lab_bg = ch0.lab ? ch0.lab_bg : 0.0;
-    double lab_ga = ch0.lab ? ch0.lab_gamma : 1.0;
-    if (PER_EVENT) {
-      const double E1 = a.E1[ev], E2 = a.E2[ev], r = sqrt(E1 * E2);
-      sqrts = 2.0 * r;
-      lab_bg = (E1 - E2) / (2.0 * r);
-      lab_ga = sqrt(1.0 + lab_bg * lab_bg);
-    }
-    // this event's momenta, lab -> CM (the inverse of phs.cu:1286-1301)
-    const double2 *pe = reinterpret_cast<const double2 *>(a.p + ev * 4 * (int64_t)a.n_out);
-    for (int k = 0; k < a.n_out; k++) {
-      const double2 e_x = pe[2 * k], y_z = pe[2 * k + 1];
-      pm[(4 * k + 0) * PHS_INV_BLOCK + tid] = dsub(dmul(lab_ga, e_x.x), dmul(lab_bg, y_z.y));
-      pm[(4 * k + 1) * PHS_INV_BLOCK + tid] = e_x.y;
-      pm[(4 * k + 2) * PHS_INV_BLOCK + tid] = y_z.x;
-      pm[(4 * k + 3) * PHS_INV_BLOCK + tid] = dadd(dmul(-lab_bg, e_x.x), dmul(lab_ga, y_z.y));
-    }
-    const double *xo = a.x_own ? a.x_own + ev * a.n_x : nullptr;
-    for (int c = 0; c < a.n_channels; c++) {
-      double *xr = a.x_out + ((int64_t)c * a.n_events + ev) * a.n_x;
-      double *fo = a.all_factors + ev * a.n_channels + c;
-      const PhsChannel &ch = a.channels[c];
-      if (c == own && xo) {
-        // the generating channel keeps its own x and factor (_move_x/_move_factors)
-        for (int k = 0; k < a.n_x; k++) xr[k] = xo[k];
-        *fo = a.factor_own ? a.factor_own[ev] : 0.0;
-        continue;
+    const bool valid = ev < a.n_events;
+    int own = 0;
+    bool ok = false;
+    if (valid) {
+      // the generating channel: the last c with ch_begin[c] <= ev
+      int lo = 0, hi = a.n_channels - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a.ch_begin[mid] <= ev) lo = mid; else hi = mid - 1;
       }
-      for (int k = ch.n_x_used; k < a.n_x; k++) xr[k] = xo ? xo[k] : 0.0;
-      if (!ok) {
-        for (int k = 0; k < ch.n_x_used; k++) xr[k] = 0.0;
-        *fo = 0.0;
-        continue;
+      own = lo;
+      ok = a.ok ? a.ok[ev] != 0 : true;
+      const double *xo = a.x_own ? a.x_own + ev * a.n_x : nullptr;
+      for (int c = 0; c < a.n_channels; c++) {
+        double *xr = a.x_out + ((int64_t)c * a.n_events + ev) * a.n_x;
+        double *fo = a.all_factors + ev * a.n_channels + c;
+        if (c == own && xo) {
+          // the generating channel keeps its own x and factor (_move_x/_move_factors)
+          for (int k = 0; k < a.n_x; k++) xr[k] = xo[k];
+          *fo = a.factor_own ? a.factor_own[ev] : 0.0;
+          continue;
+        }
+        const int n_used = a.channels[c].n_x_used;
+        for (int k = n_used; k < a.n_x; k++) xr[k] = xo ? xo[k] : 0.0;
+        if (!ok) {
+          for (int k = 0; k < n_used; k++) xr[k] = 0.0;
+          *fo = 0.0;
+        }
       }
-      *fo = inverse_event<PER_EVENT>(ch, pm + tid, sqrts, xr, stk);
     }
+    // 2. pack the ok events: thread d takes the d-th, so the inversions run in full warps
+    // (an FP64 instruction costs the pipe the same whatever the number of active lanes)
+    const unsigned m = __ballot_sync(0xffffffffu, ok);
+    if (lane == 0) warp_ok[wid] = __popc(m);
+    __syncthreads();
+    int before = 0, n_ok = 0;
+    for (int w = 0; w < PHS_INV_BLOCK / 32; w++) {
+      if (w < wid) before += warp_ok[w];
+      n_ok += warp_ok[w];
+    }
+    if (ok) {
+      const int d = before + __popc(m & ((1u << lane) - 1u));
+      dense_ev[d] = ev;
+      dense_own[d] = own;
+    }
+    __syncthreads();
+    // 3. every other channel of the d-th ok event
+    if (tid < n_ok) {
+      const int64_t e = dense_ev[tid];
+      const int own_e = dense_own[tid];
+      double sqrts = ch0.sqrts, lab_bg = ch0.lab ? ch0.lab_bg : 0.0;
+      double lab_ga = ch0.lab ? ch0.lab_gamma : 1.0;
+      if (PER_EVENT) {
+        const double E1 = a.E1[e], E2 = a.E2[e], r = sqrt(E1 * E2);
+        sqrts = 2.0 * r;
+        lab_bg = (E1 - E2) / (2.0 * r);
+        lab_ga = sqrt(1.0 + lab_bg * lab_bg);
+      }
+      // this event's momenta, lab -> CM (the inverse of phs.cu:1286-1301)
+      const double2 *pe = reinterpret_cast<const double2 *>(a.p + e * 4 * (int64_t)a.n_out);
+      for (int k = 0; k < a.n_out; k++) {
+        const double2 e_x = pe[2 * k], y_z = pe[2 * k + 1];
+        pm[(4 * k + 0) * PHS_INV_BLOCK + tid] = dsub(dmul(lab_ga, e_x.x), dmul(lab_bg, y_z.y));
+        pm[(4 * k + 1) * PHS_INV_BLOCK + tid] = e_x.y;
+        pm[(4 * k + 2) * PHS_INV_BLOCK + tid] = y_z.x;
+        pm[(4 * k + 3) * PHS_INV_BLOCK + tid] = dadd(dmul(-lab_bg, e_x.x), dmul(lab_ga, y_z.y));
+      }
+      const bool has_own = a.x_own != nullptr;
+      for (int c = 0; c < a.n_channels; c++) {
+        if (c == own_e && has_own) continue;
+        double *xr = a.x_out + ((int64_t)c * a.n_events + e) * a.n_x;
+        a.all_factors[e * a.n_channels + c] =
+            inverse_event<PER_EVENT>(a.channels[c], pm + tid, sqrts, xr, stk);
+      }
+    }
+    __syncthreads();  // dense_ev is refilled by the next tile
   }
 }
 
