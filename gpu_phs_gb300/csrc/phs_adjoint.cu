@@ -39,10 +39,11 @@ __device__ __forceinline__ double &slot(double *sm, int i) {
 }
 
 // msq mapping derivatives at x: dmsq/dx, dlog f/dx, and for Breit-Wigner branches the
-// derivatives in the mass and the width (through the atan bounds a0, a1 as well).
-__device__ void map_derivs(const PhsChild &C, const PhsAdjChild &A, double x, double &dmsq_dx,
-                           double &dlf_dx, double &dmsq_dm, double &dmsq_dw, double &dlf_dm,
-                           double &dlf_dw) {
+// derivatives in the mass and the width (through the atan bounds a0, a1 as well).  aux is
+// the forward map's transcendental term (map_msq): tan z, a0 exp(.), or exp(.)(1 + a1).
+__device__ void map_derivs(const PhsChild &C, const PhsAdjChild &A, double x, double aux,
+                           double &dmsq_dx, double &dlf_dx, double &dmsq_dm, double &dmsq_dw,
+                           double &dlf_dm, double &dlf_dw) {
   dmsq_dm = dmsq_dw = dlf_dm = dlf_dw = 0.0;
   switch (C.map_id) {
     case PHS_MAP_NO:
@@ -51,8 +52,7 @@ __device__ void map_derivs(const PhsChild &C, const PhsAdjChild &A, double x, do
       break;
     case PHS_MAP_SCHANNEL: {
       const double da = C.a1 - C.a0;
-      const double z = (1.0 - x) * C.a0 + x * C.a1;
-      const double t = tan(z), u = 1.0 + t * t, mw = C.m * C.w;
+      const double t = aux, u = 1.0 + t * t, mw = C.m * C.w;
       dmsq_dx = mw * u * da;
       dlf_dx = 2.0 * t * da;
       const double dz_dm = (1.0 - x) * A.da0_dm + x * A.da1_dm;
@@ -66,18 +66,13 @@ __device__ void map_derivs(const PhsChild &C, const PhsAdjChild &A, double x, do
     case PHS_MAP_COLLINEAR:
     case PHS_MAP_INFRARED:
     case PHS_MAP_RADIATION:
-      dmsq_dx = C.a1 * C.a0 * exp(x * C.a1);
+      dmsq_dx = C.a1 * aux;
       dlf_dx = C.a1;
       break;
     case PHS_MAP_TCHANNEL:
     case PHS_MAP_UCHANNEL:
-      if (x < 0.5) {
-        dmsq_dx = C.a1 * C.a0 * exp(x * C.a1);
-        dlf_dx = C.a1;
-      } else {
-        dmsq_dx = C.a1 * C.a0 * exp((1.0 - x) * C.a1);
-        dlf_dx = -C.a1;
-      }
+      dmsq_dx = C.a1 * aux;
+      dlf_dx = x < 0.5 ? C.a1 : -C.a1;
       break;
     case PHS_MAP_STEP_H: {
       const double q = C.a0 - x, g = C.a1 / (q * q) + C.a2;
@@ -86,7 +81,7 @@ __device__ void map_derivs(const PhsChild &C, const PhsAdjChild &A, double x, do
       break;
     }
     case PHS_MAP_STEP_E: {
-      const double tmp = exp(-x * C.a0 / C.a2) * (1.0 + C.a1);
+      const double tmp = aux;
       dmsq_dx = C.a0 * tmp / (tmp - C.a1) * (C.msq_max - C.msq_min);
       dlf_dx = C.a0 * C.a1 / (C.a2 * (tmp - C.a1));
       break;
@@ -181,13 +176,14 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
           cm[j] = C.m_leaf;
           cmax[j] = 0.0;
         } else {
-          double f;
+          double f, aux;
           const double xm = xe[C.x_msq];
-          map_msq(C.map_id, xm, s, C.m, C.w, C.msq_min, C.msq_max, C.a0, C.a1, C.a2, cmsq[j], f);
+          map_msq(C.map_id, xm, s, C.m, C.w, C.msq_min, C.msq_max, C.a0, C.a1, C.a2, cmsq[j], f,
+                  aux);
           cm[j] = sqrt(cmsq[j]);
           cmax[j] = C.m_max;
           double dd[6];
-          map_derivs(C, ad.visit[v].child[j], xm, dd[0], dd[1], dd[2], dd[3], dd[4], dd[5]);
+          map_derivs(C, ad.visit[v].child[j], xm, aux, dd[0], dd[1], dd[2], dd[3], dd[4], dd[5]);
           const int cv = ad.visit[v].child_visit[j];
 #pragma unroll
           for (int k = 0; k < 6; k++) slot(sm, lay.der0 + PHS_ADJ_DER * cv + k) = dd[k];

@@ -25,10 +25,14 @@ __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a,
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 
-// msq from x (phs_cpu.cpp:12-61), same expression order, no contraction.
+// msq from x (phs_cpu.cpp:12-61), same expression order, no contraction.  aux receives the
+// mapping's transcendental term for the adjoint's derivatives: tan z (Breit-Wigner), the
+// exponential term a0 exp(.) (collinear, infrared, radiation, t/u channel), exp(.)(1 + a1)
+// (STEP_E); 0 otherwise.
 __device__ __forceinline__ void map_msq(int t, double x, double s, double m, double w,
                                         double msq_min, double msq_max, double a0, double a1,
-                                        double a2, double &msq, double &f) {
+                                        double a2, double &msq, double &f, double &aux) {
+  aux = 0.0;
   switch (t) {
     case PHS_MAP_NO:
       msq = dadd(dmul(dsub(1.0, x), msq_min), dmul(x, msq_max));
@@ -40,6 +44,7 @@ __device__ __forceinline__ void map_msq(int t, double x, double s, double m, dou
         double tz = tan(z);
         msq = dmul(m, dadd(m, dmul(w, tz)));
         f = a2 * (1.0 + tz * tz);
+        aux = tz;
       } else {
         msq = 0.0;
         f = 0.0;
@@ -52,6 +57,7 @@ __device__ __forceinline__ void map_msq(int t, double x, double s, double m, dou
       double msq1 = dmul(a0, exp(dmul(x, a1)));
       msq = dadd(dsub(msq1, a0), msq_min);
       f = a2 * msq1;
+      aux = msq1;
       break;
     }
     case PHS_MAP_TCHANNEL:
@@ -61,6 +67,7 @@ __device__ __forceinline__ void map_msq(int t, double x, double s, double m, dou
       const double msq1 = dmul(a0, exp(dmul(lower ? x : dsub(1.0, x), a1)));
       msq = lower ? dadd(dsub(msq1, a0), msq_min) : dadd(-dsub(msq1, a0), msq_max);
       f = a2 * msq1;
+      aux = msq1;
       break;
     }
     case PHS_MAP_STEP_H: {
@@ -75,12 +82,20 @@ __device__ __forceinline__ void map_msq(int t, double x, double s, double m, dou
       double z = dmul(-a2, log(dsub(tmp, a1)));
       msq = dadd(dmul(z, msq_max), dmul(dsub(1.0, z), msq_min));
       f = a0 / (1.0 - a1 / tmp) * (msq_max - msq_min) / s;
+      aux = tmp;
       break;
     }
     default:
       msq = 0.0;
       f = 0.0;
   }
+}
+
+__device__ __forceinline__ void map_msq(int t, double x, double s, double m, double w,
+                                        double msq_min, double msq_max, double a0, double a1,
+                                        double a2, double &msq, double &f) {
+  double aux;
+  map_msq(t, x, s, m, w, msq_min, msq_max, a0, a1, a2, msq, f, aux);
 }
 
 // cos(theta) from x (phs_cpu.cpp:112-146).  The collinear branch keeps the reference's
