@@ -22,7 +22,7 @@
 #include "phs_program.h"
 
 #define PHS_ADJ_BLOCK 64
-#define PHS_ADJ_STATE 4    // per visit: msq, m, p, E of the visited branch
+#define PHS_ADJ_STATE 6    // per visit: msq, m, p, E of the visited branch, sqrt(lambda), 1/m
 #define PHS_ADJ_ANG 7      // per visit: cos phi, sin phi, ct, st, dct/dx, dst/dx, dlog fct/dx
 #define PHS_ADJ_DER 6      // per visited branch: dmsq/dx, dlog f/dx, dmsq/dm, dmsq/dw, dlogf/dm, dlogf/dw
 #define PHS_ADJ_FRAME 20   // adjoint stack entry: Lbar[16], msqbar, mbar, pbar, Ebar
@@ -163,10 +163,10 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
     int sp = 0, np = 0;
     for (int v = 0; v < n_visits; v++) {
       const PhsVisit &V = ch.visit[v];
-      slot(sm, lay.state0 + 4 * v + 0) = msq_b;
-      slot(sm, lay.state0 + 4 * v + 1) = m_b;
-      slot(sm, lay.state0 + 4 * v + 2) = p_b;
-      slot(sm, lay.state0 + 4 * v + 3) = E_b;
+      slot(sm, lay.state0 + PHS_ADJ_STATE * v + 0) = msq_b;
+      slot(sm, lay.state0 + PHS_ADJ_STATE * v + 1) = m_b;
+      slot(sm, lay.state0 + PHS_ADJ_STATE * v + 2) = p_b;
+      slot(sm, lay.state0 + PHS_ADJ_STATE * v + 3) = E_b;
       double cmsq[2], cm[2], cmax[2];
 #pragma unroll
       for (int j = 0; j < 2; j++) {
@@ -194,6 +194,8 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
       ok = ok && (lda > 0.0) && (m_b > dadd(cm[0], cm[1])) && (m_b <= mmax_b);
       const double sl = sqrt(lda);
       const double rm = m_b > 0.0 ? __drcp_rn(m_b) : 0.0;
+      slot(sm, lay.state0 + PHS_ADJ_STATE * v + 4) = sl;
+      slot(sm, lay.state0 + PHS_ADJ_STATE * v + 5) = rm;
       const double hm = 0.5 * rm;
       const double pc = sl * hm;
       const double ce0 = (msq_b + cmsq[0] - cmsq[1]) * hm;
@@ -272,10 +274,10 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
     for (int v = n_visits - 1; v >= 0; v--) {
       const PhsVisit &V = ch.visit[v];
       const PhsAdjVisit &A = ad.visit[v];
-      const double msq_v = slot(sm, lay.state0 + 4 * v + 0);
-      const double m_v = slot(sm, lay.state0 + 4 * v + 1);
-      const double p_v = slot(sm, lay.state0 + 4 * v + 2);
-      const double E_v = slot(sm, lay.state0 + 4 * v + 3);
+      const double msq_v = slot(sm, lay.state0 + PHS_ADJ_STATE * v + 0);
+      const double m_v = slot(sm, lay.state0 + PHS_ADJ_STATE * v + 1);
+      const double p_v = slot(sm, lay.state0 + PHS_ADJ_STATE * v + 2);
+      const double E_v = slot(sm, lay.state0 + PHS_ADJ_STATE * v + 3);
       double cmsq[2], cm[2];
       double c_msqb[2] = {0.0, 0.0}, c_mb[2] = {0.0, 0.0}, c_pb[2] = {0.0, 0.0}, c_Eb[2] = {0.0, 0.0};
 #pragma unroll
@@ -285,8 +287,8 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
           cmsq[j] = C.msq_leaf;
           cm[j] = C.m_leaf;
         } else {
-          cmsq[j] = slot(sm, lay.state0 + 4 * A.child_visit[j] + 0);
-          cm[j] = slot(sm, lay.state0 + 4 * A.child_visit[j] + 1);
+          cmsq[j] = slot(sm, lay.state0 + PHS_ADJ_STATE * A.child_visit[j] + 0);
+          cm[j] = slot(sm, lay.state0 + PHS_ADJ_STATE * A.child_visit[j] + 1);
         }
       }
       if (V.carry >= 0) {
@@ -304,11 +306,11 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
         c_pb[j] = slot(sm, base + 18);
         c_Eb[j] = slot(sm, base + 19);
       }
-      // local quantities of the visit, recomputed
+      // local quantities of the visit (the square root and the reciprocal as the forward
+      // pass left them)
       const double d = msq_v - cmsq[0] - cmsq[1];
-      const double lda = d * d - 4.0 * cmsq[0] * cmsq[1];
-      const double sl = sqrt(lda);
-      const double rm = __drcp_rn(m_v), hm = 0.5 * rm;
+      const double sl = slot(sm, lay.state0 + PHS_ADJ_STATE * v + 4);
+      const double rm = slot(sm, lay.state0 + PHS_ADJ_STATE * v + 5), hm = 0.5 * rm;
       const double pc = sl * hm;
       const double A0 = msq_v + cmsq[0] - cmsq[1], A1 = msq_v + cmsq[1] - cmsq[0];
       const double ce0 = A0 * hm, ce1 = A1 * hm;
