@@ -59,8 +59,8 @@ __device__ void map_derivs(const PhsChild &C, const PhsAdjChild &A, double x, do
       const double dz_dw = (1.0 - x) * A.da0_dw + x * A.da1_dw;
       dmsq_dm = 2.0 * C.m + C.w * t + mw * u * dz_dm;
       dmsq_dw = C.m * t + mw * u * dz_dw;
-      dlf_dm = (A.da1_dm - A.da0_dm) / da + 1.0 / C.m + 2.0 * t * dz_dm;
-      dlf_dw = (A.da1_dw - A.da0_dw) / da + 1.0 / C.w + 2.0 * t * dz_dw;
+      dlf_dm = A.dlf_dm0 + 2.0 * t * dz_dm;
+      dlf_dw = A.dlf_dw0 + 2.0 * t * dz_dw;
       break;
     }
     case PHS_MAP_COLLINEAR:

@@ -432,6 +432,9 @@ void channel_adjoint(const PhsChannel &in, PhsAdjChannel &out) {
         A.child[j].da1_dm = -(C.msq_max + m2) / (m2 * C.w) / (1 + u1 * u1);
         A.child[j].da0_dw = -u0 / (C.w * (1 + u0 * u0));
         A.child[j].da1_dw = -u1 / (C.w * (1 + u1 * u1));
+        const double da = C.a1 - C.a0;
+        A.child[j].dlf_dm0 = (A.child[j].da1_dm - A.child[j].da0_dm) / da + 1.0 / C.m;
+        A.child[j].dlf_dw0 = (A.child[j].da1_dw - A.child[j].da0_dw) / da + 1.0 / C.w;
       }
     }
     if (V.carry >= 0) A.child_visit[V.carry] = v + 1;

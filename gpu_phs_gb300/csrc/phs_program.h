@@ -161,6 +161,8 @@ struct PhsChannelFF {
 // Reverse-walk tables of a channel, for the adjoint kernel (phs_adjoint.cu).
 struct PhsAdjChild {
   double da0_dm, da0_dw, da1_dm, da1_dw;  // Breit-Wigner: derivatives of the atan bounds
+  double dlf_dm0, dlf_dw0;  // the x-independent parts of dlog f/dm and dlog f/dw:
+                            // (da1 - da0)/(a1 - a0) + 1/m (and 1/w)
 };
 
 struct PhsAdjVisit {
