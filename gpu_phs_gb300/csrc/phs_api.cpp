@@ -314,6 +314,8 @@ struct phs_process {
   bool has_friends = false;
   DevBuf d_prog, d_prog_ff, d_prog_adj;
   DevBuf d_ch_begin;                  // inverse map: first event per generating channel
+  DevBuf d_inv_groups;                // inverse map: channels by tree shape, group starts
+  int n_inv_groups = 0;
   std::vector<int64_t> ch_begin_up;   // content of d_ch_begin
   Segments segs;
   // host-path pipeline
@@ -386,6 +388,7 @@ extern "C" int phs_process_destroy(phs_process_t h) {
   h->d_prog_ff.release();
   h->d_prog_adj.release();
   h->d_ch_begin.release();
+  h->d_inv_groups.release();
   h->segs.release();
   delete h;
   return PHS_OK;
@@ -437,6 +440,42 @@ extern "C" int phs_process_set_beams(phs_process_t h, double E1, double E2) {
                       cudaMemcpyHostToDevice));
   CUDA_TRY(cudaMemcpy(h->d_prog_ff.ptr, prog_ff.data(), prog_ff.size() * sizeof(PhsChannelFF),
                       cudaMemcpyHostToDevice));
+  // channels of equal tree shape share the inverse map's geometry: order them by shape
+  {
+    std::vector<std::vector<int32_t>> keys;
+    std::vector<std::vector<int32_t>> members;
+    for (int c = 0; c < (int)prog.size(); c++) {
+      const PhsChannel &ch = prog[c];
+      std::vector<int32_t> key = {ch.n_out, ch.n_visits, ch.n_vol};
+      for (int i = 0; i < ch.n_vol; i++) {
+        key.push_back(ch.comb[i][0]);
+        key.push_back(ch.comb[i][1]);
+      }
+      for (int v = 0; v < ch.n_visits; v++) {
+        const PhsVisit &V = ch.visit[v];
+        key.insert(key.end(), {V.slot[0], V.slot[1], V.friend_sign, V.carry, V.push,
+                               V.both_leaves, V.self_root, V.x_phi, V.x_ct});
+        for (int j = 0; j < 2; j++)
+          key.insert(key.end(), {V.child[j].internal, V.child[j].x_msq, V.child[j].out_index});
+      }
+      size_t g = 0;
+      while (g < keys.size() && keys[g] != key) g++;
+      if (g == keys.size()) {
+        keys.push_back(key);
+        members.emplace_back();
+      }
+      members[g].push_back(c);
+    }
+    std::vector<int32_t> table;  // [order n_channels][begin n_groups + 1]
+    for (const auto &m : members) table.insert(table.end(), m.begin(), m.end());
+    int32_t at = 0;
+    table.push_back(at);
+    for (const auto &m : members) table.push_back(at += (int32_t)m.size());
+    if ((rc = h->d_inv_groups.reserve(table.size() * sizeof(int32_t)))) return rc;
+    CUDA_TRY(cudaMemcpy(h->d_inv_groups.ptr, table.data(), table.size() * sizeof(int32_t),
+                        cudaMemcpyHostToDevice));
+    h->n_inv_groups = (int)members.size();
+  }
   h->prog = std::move(prog);
   h->prog_ff = std::move(prog_ff);
   h->prog_adj = std::move(prog_adj);
@@ -676,9 +715,13 @@ extern "C" int phs_inverse_device(phs_process_t h, int64_t n_events, const int64
   a.n_out = h->p.n_out;
   a.n_x = h->p.n_x;
   a.stack_depth = h->stack_depth;
+  a.max_visits = h->max_visits;
+  a.group_order = h->d_inv_groups.as<int32_t>();
+  a.group_begin = a.group_order + nch;
+  a.n_groups = h->n_inv_groups;
   const int64_t tiles = (n_events + PHS_INV_BLOCK - 1) / PHS_INV_BLOCK;
   const int64_t cap = (int64_t)sm_count(h->device) *
-                      phs_inverse_blocks_per_sm(a.n_out, a.stack_depth, E1 != nullptr);
+                      phs_inverse_blocks_per_sm(a.n_out, a.stack_depth, a.max_visits, E1 != nullptr);
   CUDA_TRY(phs_launch_inverse(a, (int)std::max<int64_t>(1, std::min(tiles, cap)), st));
   return PHS_OK;
 }

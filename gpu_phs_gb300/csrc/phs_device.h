@@ -145,12 +145,17 @@ struct PhsInvLaunch {
   const double *factor_own;    // [n]: the generating channel's factor, or null
   double *all_factors;         // [n][n_channels]
   double *x_out;               // [n_channels][n][n_x]
+  // channels of equal tree shape (the geometry of the inverse map is the same for them):
+  // group g is group_order[group_begin[g] .. group_begin[g + 1]), each channel once
+  const int32_t *group_order;
+  const int32_t *group_begin;
+  int32_t n_groups;
   int64_t n_events;
-  int32_t n_channels, n_out, n_x, stack_depth;
+  int32_t n_channels, n_out, n_x, stack_depth, max_visits;
 };
 cudaError_t phs_launch_inverse(const PhsInvLaunch &a, int n_blocks, cudaStream_t stream);
-int phs_inverse_blocks_per_sm(int n_out, int stack_depth, bool per_event);
-size_t phs_inverse_smem_bytes(int n_out, int stack_depth);
+int phs_inverse_blocks_per_sm(int n_out, int stack_depth, int max_visits, bool per_event);
+size_t phs_inverse_smem_bytes(int n_out, int stack_depth, int max_visits);
 
 // Per-channel x grid of the warm-up (phs_grid.cu): weights [n_channels][n_x][PHS_GRID_BINS].
 #define PHS_GRID_BINS 10

@@ -30,6 +30,9 @@
 #include "phs_program.h"
 
 #define PHS_INV_STATE 23  // doubles per saved frame: G[16], ct, st, cos phi, sin phi, msq, p_decay, m
+// per visit, from the geometry walk to the mapping pass: msq of both daughters, cos(theta)
+// and x_phi of daughter 1, sqrt(lambda) / msq of the visited branch
+#define PHS_INV_GEO 5
 
 namespace {
 
@@ -109,16 +112,17 @@ __device__ __forceinline__ double inv_load(const double *stk, int depth, int k) 
   return stk[(depth * PHS_INV_STATE + k) * PHS_INV_BLOCK + threadIdx.x];
 }
 
-// One (event, channel): writes the channel's x entries of xr and returns its factor.
+// The geometry of one (event, channel shape): the walk of the visit program without the
+// mappings, leaving per visit in geo (slot (v PHS_INV_GEO + k) PHS_INV_BLOCK) what the
+// mappings of every channel of that shape need (inverse_maps).
 // pm: this thread's momentum slots, component (4 j + mu) at pm[(4 j + mu) * PHS_INV_BLOCK]:
 // the CM momenta in slots 0..n_out-1, the channel's internal branches after them.
 // The arithmetic keeps the reference's operation order (this file is compiled without
 // contraction): x(p) is ill-conditioned near the poles of each decay (cos(theta) -> +-1,
 // where 1 - cos^2 cancels) and for soft daughters of fast branches, and there any other
 // rounding order moves the result by far more than the input's own rounding does.
-template <bool PER_EVENT>
-__device__ double inverse_event(const PhsChannel &ch, double *pm, double sqrts, double *xr,
-                                double *stk) {
+__device__ void inverse_geometry(const PhsChannel &ch, double *pm, double sqrts, double *stk,
+                                 double *geo) {
   const double s = sqrts * sqrts;
   // internal momenta as sums of their daughters in post-order (_combine_particles,
   // phs.cu:1262-1283)
@@ -133,7 +137,6 @@ __device__ double inverse_event(const PhsChannel &ch, double *pm, double sqrts, 
   double Gp[16];
   double ct0 = 1.0, st0 = 0.0, cp0 = 1.0, sp0 = 0.0;
   double msq_b = s, pd_b = 0.0, m_b = sqrts;
-  double factor = 1.0;
   int sp = 0;
   const int n_visits = ch.n_visits;
   for (int v = 0; v < n_visits; v++) {
@@ -187,25 +190,14 @@ __device__ double inverse_event(const PhsChannel &ch, double *pm, double sqrts, 
     cmsq[0] = q0[0] * q0[0] - q0[1] * q0[1] - q0[2] * q0[2] - q0[3] * q0[3];
     cmsq[1] = q1[0] * q1[0] - q1[1] * q1[1] - q1[2] * q1[2] - q1[3] * q1[3];
 
-    // inverse msq maps of the internal daughters
-#pragma unroll
-    for (int j = 0; j < 2; j++) {
-      const PhsChild &C = V.child[j];
-      if (C.internal) {
-        double a0 = C.a0, a1 = C.a1, a2 = C.a2, mn = C.msq_min, mx = C.msq_max, mmax;
-        if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, a0, a1, a2, mn, mx, mmax);
-        double x, f;
-        map_msq_inverse(C.map_id, cmsq[j], s, C.m, C.w, mn, mx, a0, a1, a2, x, f);
-        xr[C.x_msq] = x;
-        factor *= f;
-      }
-    }
+    geo[(PHS_INV_GEO * v + 0) * PHS_INV_BLOCK] = cmsq[0];
+    geo[(PHS_INV_GEO * v + 1) * PHS_INV_BLOCK] = cmsq[1];
 
     // Kallen function at the visited branch
     const double d = msq_b - cmsq[0] - cmsq[1];
     const double sl = sqrt(d * d - 4.0 * cmsq[0] * cmsq[1]);
     const double pd = sl / (2.0 * m_b);
-    factor *= sl / msq_b;
+    geo[(PHS_INV_GEO * v + 4) * PHS_INV_BLOCK] = sl / msq_b;
 
     // angles of daughter 1 in the branch's frame (azimuthal_angle, polar_angle_ct,
     // phs.cu:913-922)
@@ -214,20 +206,9 @@ __device__ double inverse_event(const PhsChannel &ch, double *pm, double sqrts, 
     const double qz = G[12] * q0[0] + G[13] * q0[1] + G[14] * q0[2] + G[15] * q0[3];
     double phi = atan2(qy, qx);
     if (phi < 0.0) phi += 2.0 * PHS_PI;
-    xr[V.x_phi] = phi / (2.0 * PHS_PI);
+    geo[(PHS_INV_GEO * v + 3) * PHS_INV_BLOCK] = phi / (2.0 * PHS_PI);
     const double ct = qz / sqrt(qx * qx + qy * qy + qz * qz);
-    const double st = sqrt(1.0 - ct * ct);
-    double b0 = V.b0, b1 = V.b1;
-    if (PER_EVENT && V.ct_class == PHS_CT_COLLINEAR) {
-      b0 = V.m * V.m / s;
-      b1 = log((b0 + 1.0) / b0);
-    }
-    {
-      double x, f;
-      map_ct_inverse(V.ct_class, ct, b0, b1, x, f);
-      xr[V.x_ct] = x;
-      factor *= f;
-    }
+    geo[(PHS_INV_GEO * v + 2) * PHS_INV_BLOCK] = ct;
     if (V.both_leaves) {
       if (sp > 0) {
         sp--;
@@ -243,6 +224,7 @@ __device__ double inverse_event(const PhsChannel &ch, double *pm, double sqrts, 
       }
       continue;
     }
+    const double st = sqrt(1.0 - ct * ct);
     double sph, cph;
     sincos(phi, &sph, &cph);
     if (V.push >= 0) {
@@ -272,6 +254,43 @@ __device__ double inverse_event(const PhsChannel &ch, double *pm, double sqrts, 
       m_b = sqrt(msq_b);
     }
   }
+}
+
+// The mappings of one (event, channel) after inverse_geometry of its shape: writes the
+// channel's x entries of xr and returns its factor, in the reference's order of factors.
+template <bool PER_EVENT>
+__device__ double inverse_maps(const PhsChannel &ch, double sqrts, const double *geo, double *xr) {
+  const double s = sqrts * sqrts;
+  double factor = 1.0;
+  const int n_visits = ch.n_visits;
+  for (int v = 0; v < n_visits; v++) {
+    const PhsVisit &V = ch.visit[v];
+    // inverse msq maps of the internal daughters
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const PhsChild &C = V.child[j];
+      if (C.internal) {
+        double a0 = C.a0, a1 = C.a1, a2 = C.a2, mn = C.msq_min, mx = C.msq_max, mmax;
+        if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, a0, a1, a2, mn, mx, mmax);
+        double x, f;
+        map_msq_inverse(C.map_id, geo[(PHS_INV_GEO * v + j) * PHS_INV_BLOCK], s, C.m, C.w, mn, mx,
+                        a0, a1, a2, x, f);
+        xr[C.x_msq] = x;
+        factor *= f;
+      }
+    }
+    factor *= geo[(PHS_INV_GEO * v + 4) * PHS_INV_BLOCK];  // sqrt(lambda) / msq
+    xr[V.x_phi] = geo[(PHS_INV_GEO * v + 3) * PHS_INV_BLOCK];
+    double b0 = V.b0, b1 = V.b1;
+    if (PER_EVENT && V.ct_class == PHS_CT_COLLINEAR) {
+      b0 = V.m * V.m / s;
+      b1 = log((b0 + 1.0) / b0);
+    }
+    double x, f;
+    map_ct_inverse(V.ct_class, geo[(PHS_INV_GEO * v + 2) * PHS_INV_BLOCK], b0, b1, x, f);
+    xr[V.x_ct] = x;
+    factor *= f;
+  }
   return factor;
 }
 
@@ -281,6 +300,7 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
   extern __shared__ double sm[];
   double *pm = sm;                                                  // [4 (2 n_out - 1)][block]
   double *stk = sm + (size_t)4 * (2 * a.n_out - 1) * PHS_INV_BLOCK;  // frame stack
+  double *geo = stk + (size_t)PHS_INV_STATE * a.stack_depth * PHS_INV_BLOCK;  // per-visit geometry
   const int tid = threadIdx.x;
   const int64_t n_tiles = (a.n_events + PHS_INV_BLOCK - 1) / PHS_INV_BLOCK;
   const PhsChannel &ch0 = a.channels[0];
@@ -361,12 +381,19 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
         pm[(4 * k + 2) * PHS_INV_BLOCK + tid] = y_z.x;
         pm[(4 * k + 3) * PHS_INV_BLOCK + tid] = dadd(dmul(-lab_bg, e_x.x), dmul(lab_ga, y_z.y));
       }
+      // the geometry once per tree shape, then the mappings of each channel of that shape
       const bool has_own = a.x_own != nullptr;
-      for (int c = 0; c < a.n_channels; c++) {
-        if (c == own_e && has_own) continue;
-        double *xr = a.x_out + ((int64_t)c * a.n_events + e) * a.n_x;
-        a.all_factors[e * a.n_channels + c] =
-            inverse_event<PER_EVENT>(a.channels[c], pm + tid, sqrts, xr, stk);
+      for (int g = 0; g < a.n_groups; g++) {
+        const int gb = a.group_begin[g], ge = a.group_begin[g + 1];
+        if (has_own && ge - gb == 1 && a.group_order[gb] == own_e) continue;
+        inverse_geometry(a.channels[a.group_order[gb]], pm + tid, sqrts, stk, geo + tid);
+        for (int i = gb; i < ge; i++) {
+          const int c = a.group_order[i];
+          if (c == own_e && has_own) continue;
+          double *xr = a.x_out + ((int64_t)c * a.n_events + e) * a.n_x;
+          a.all_factors[e * a.n_channels + c] =
+              inverse_maps<PER_EVENT>(a.channels[c], sqrts, geo + tid, xr);
+        }
       }
     }
     __syncthreads();  // dense_ev is refilled by the next tile
@@ -375,14 +402,14 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
 
 }  // namespace
 
-size_t phs_inverse_smem_bytes(int n_out, int stack_depth) {
-  return ((size_t)4 * (2 * n_out - 1) + (size_t)PHS_INV_STATE * stack_depth) * PHS_INV_BLOCK *
-         sizeof(double);
+size_t phs_inverse_smem_bytes(int n_out, int stack_depth, int max_visits) {
+  return ((size_t)4 * (2 * n_out - 1) + (size_t)PHS_INV_STATE * stack_depth +
+          (size_t)PHS_INV_GEO * max_visits) * PHS_INV_BLOCK * sizeof(double);
 }
 
-int phs_inverse_blocks_per_sm(int n_out, int stack_depth, bool per_event) {
+int phs_inverse_blocks_per_sm(int n_out, int stack_depth, int max_visits, bool per_event) {
   int n = 0;
-  const size_t smem = phs_inverse_smem_bytes(n_out, stack_depth);
+  const size_t smem = phs_inverse_smem_bytes(n_out, stack_depth, max_visits);
   if (per_event)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phs_inverse_kernel<true>, PHS_INV_BLOCK, smem);
   else
@@ -392,7 +419,7 @@ int phs_inverse_blocks_per_sm(int n_out, int stack_depth, bool per_event) {
 
 cudaError_t phs_launch_inverse(const PhsInvLaunch &a, int n_blocks, cudaStream_t stream) {
   if (a.n_events <= 0) return cudaSuccess;
-  const size_t smem = phs_inverse_smem_bytes(a.n_out, a.stack_depth);
+  const size_t smem = phs_inverse_smem_bytes(a.n_out, a.stack_depth, a.max_visits);
   const bool per_event = a.E1 && a.E2;
   if (smem > 48 * 1024) {
     cudaError_t e = per_event
