@@ -314,8 +314,10 @@ struct phs_process {
   bool has_friends = false;
   DevBuf d_prog, d_prog_ff, d_prog_adj;
   DevBuf d_ch_begin;                  // inverse map: first event per generating channel
-  DevBuf d_inv_groups;                // inverse map: channels by tree shape, group starts
+  DevBuf d_inv_groups;                // inverse map: channels by tree shape, group starts,
+                                      // mapping reuse masks
   int n_inv_groups = 0;
+  size_t inv_reuse_offset = 0;        // byte offset of the reuse masks in d_inv_groups
   std::vector<int64_t> ch_begin_up;   // content of d_ch_begin
   Segments segs;
   // host-path pipeline
@@ -466,15 +468,61 @@ extern "C" int phs_process_set_beams(phs_process_t h, double E1, double E2) {
       }
       members[g].push_back(c);
     }
-    std::vector<int32_t> table;  // [order n_channels][begin n_groups + 1]
-    for (const auto &m : members) table.insert(table.end(), m.begin(), m.end());
+    // within a shape, channels in order of their mappings, so that equal ones follow each
+    // other: a channel reuses the previous channel's mapping results wherever the two have
+    // the same mapping (position 3 v + 0/1: a daughter's msq map, 3 v + 2: the cos(theta) map)
+    auto mapping = [&](int c, int v, int k) {
+      std::vector<double> sig;
+      const PhsVisit &V = prog[c].visit[v];
+      if (k < 2) {
+        const PhsChild &C = V.child[k];
+        if (!C.internal) return sig;
+        sig = {(double)C.map_id, C.m, C.w, C.m_min, C.a0, C.a1, C.a2, C.msq_min, C.msq_max};
+      } else {
+        sig = {(double)V.ct_class, V.b0, V.b1, V.m};
+      }
+      return sig;
+    };
+    auto same = [](const std::vector<double> &x, const std::vector<double> &y) {
+      return x.size() == y.size() && (x.empty() || memcmp(x.data(), y.data(), x.size() * sizeof(double)) == 0);
+    };
+    std::vector<int32_t> order;
+    std::vector<uint64_t> reuse;
+    for (auto &m : members) {
+      const int nv = prog[m[0]].n_visits;
+      std::stable_sort(m.begin(), m.end(), [&](int c1, int c2) {
+        for (int v = 0; v < nv; v++)
+          for (int k = 0; k < 3; k++) {
+            const auto x = mapping(c1, v, k), y = mapping(c2, v, k);
+            if (!same(x, y)) return std::lexicographical_compare(x.begin(), x.end(), y.begin(), y.end());
+          }
+        return false;
+      });
+      for (size_t i = 0; i < m.size(); i++) {
+        uint64_t mask = 0;
+        if (i > 0)
+          for (int v = 0; v < nv && 3 * v + 2 < 64; v++)
+            for (int k = 0; k < 3; k++) {
+              const auto x = mapping(m[i], v, k);
+              if (!x.empty() && same(x, mapping(m[i - 1], v, k))) mask |= 1ull << (3 * v + k);
+            }
+        order.push_back(m[i]);
+        reuse.push_back(mask);
+      }
+    }
+    // [order n_channels][begin n_groups + 1], then the reuse masks (8-byte aligned)
+    std::vector<int32_t> table = order;
     int32_t at = 0;
     table.push_back(at);
     for (const auto &m : members) table.push_back(at += (int32_t)m.size());
-    if ((rc = h->d_inv_groups.reserve(table.size() * sizeof(int32_t)))) return rc;
-    CUDA_TRY(cudaMemcpy(h->d_inv_groups.ptr, table.data(), table.size() * sizeof(int32_t),
-                        cudaMemcpyHostToDevice));
+    if (table.size() % 2) table.push_back(0);
+    const size_t head = table.size() * sizeof(int32_t);
+    if ((rc = h->d_inv_groups.reserve(head + reuse.size() * sizeof(uint64_t)))) return rc;
+    CUDA_TRY(cudaMemcpy(h->d_inv_groups.ptr, table.data(), head, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(static_cast<char *>(h->d_inv_groups.ptr) + head, reuse.data(),
+                        reuse.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
     h->n_inv_groups = (int)members.size();
+    h->inv_reuse_offset = head;
   }
   h->prog = std::move(prog);
   h->prog_ff = std::move(prog_ff);
@@ -718,6 +766,8 @@ extern "C" int phs_inverse_device(phs_process_t h, int64_t n_events, const int64
   a.max_visits = h->max_visits;
   a.group_order = h->d_inv_groups.as<int32_t>();
   a.group_begin = a.group_order + nch;
+  a.group_reuse = reinterpret_cast<const uint64_t *>(
+      static_cast<const char *>(h->d_inv_groups.ptr) + h->inv_reuse_offset);
   a.n_groups = h->n_inv_groups;
   const int64_t tiles = (n_events + PHS_INV_BLOCK - 1) / PHS_INV_BLOCK;
   const int64_t cap = (int64_t)sm_count(h->device) *

@@ -149,6 +149,8 @@ struct PhsInvLaunch {
   // group g is group_order[group_begin[g] .. group_begin[g + 1]), each channel once
   const int32_t *group_order;
   const int32_t *group_begin;
+  const uint64_t *group_reuse;  // [n_channels] by group_order position: mappings equal to the
+                                // previous channel's (bit 3 visit + 0/1 daughter msq, + 2 ct)
   int32_t n_groups;
   int64_t n_events;
   int32_t n_channels, n_out, n_x, stack_depth, max_visits;

@@ -31,8 +31,10 @@
 
 #define PHS_INV_STATE 23  // doubles per saved frame: G[16], ct, st, cos phi, sin phi, msq, p_decay, m
 // per visit, from the geometry walk to the mapping pass: msq of both daughters, cos(theta)
-// and x_phi of daughter 1, sqrt(lambda) / msq of the visited branch
-#define PHS_INV_GEO 5
+// and x_phi of daughter 1, sqrt(lambda) / msq of the visited branch (slots 0-4); then the
+// last mapping results (x, f) of daughter 0, daughter 1 and cos(theta) (slots 5-10), which
+// the next channel of the shape reuses where its mapping is the same
+#define PHS_INV_GEO 11
 
 namespace {
 
@@ -258,8 +260,12 @@ __device__ void inverse_geometry(const PhsChannel &ch, double *pm, double sqrts,
 
 // The mappings of one (event, channel) after inverse_geometry of its shape: writes the
 // channel's x entries of xr and returns its factor, in the reference's order of factors.
+// Bit 3 v + k of reuse (k = 0, 1: the daughters' msq maps, 2: the cos(theta) map): the
+// previous channel of the shape had the same mapping there, so its (x, f) is taken as is.
+// xr null: the mappings run (the next channel may reuse them) but write nothing.
 template <bool PER_EVENT>
-__device__ double inverse_maps(const PhsChannel &ch, double sqrts, const double *geo, double *xr) {
+__device__ double inverse_maps(const PhsChannel &ch, double sqrts, double *geo, double *xr,
+                               uint64_t reuse) {
   const double s = sqrts * sqrts;
   double factor = 1.0;
   const int n_visits = ch.n_visits;
@@ -270,25 +276,41 @@ __device__ double inverse_maps(const PhsChannel &ch, double sqrts, const double 
     for (int j = 0; j < 2; j++) {
       const PhsChild &C = V.child[j];
       if (C.internal) {
-        double a0 = C.a0, a1 = C.a1, a2 = C.a2, mn = C.msq_min, mx = C.msq_max, mmax;
-        if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, a0, a1, a2, mn, mx, mmax);
+        double *cache = geo + (PHS_INV_GEO * v + 5 + 2 * j) * PHS_INV_BLOCK;
         double x, f;
-        map_msq_inverse(C.map_id, geo[(PHS_INV_GEO * v + j) * PHS_INV_BLOCK], s, C.m, C.w, mn, mx,
-                        a0, a1, a2, x, f);
-        xr[C.x_msq] = x;
+        if (reuse >> (3 * v + j) & 1) {
+          x = cache[0];
+          f = cache[PHS_INV_BLOCK];
+        } else {
+          double a0 = C.a0, a1 = C.a1, a2 = C.a2, mn = C.msq_min, mx = C.msq_max, mmax;
+          if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, a0, a1, a2, mn, mx, mmax);
+          map_msq_inverse(C.map_id, geo[(PHS_INV_GEO * v + j) * PHS_INV_BLOCK], s, C.m, C.w, mn,
+                          mx, a0, a1, a2, x, f);
+          cache[0] = x;
+          cache[PHS_INV_BLOCK] = f;
+        }
+        if (xr) xr[C.x_msq] = x;
         factor *= f;
       }
     }
     factor *= geo[(PHS_INV_GEO * v + 4) * PHS_INV_BLOCK];  // sqrt(lambda) / msq
-    xr[V.x_phi] = geo[(PHS_INV_GEO * v + 3) * PHS_INV_BLOCK];
-    double b0 = V.b0, b1 = V.b1;
-    if (PER_EVENT && V.ct_class == PHS_CT_COLLINEAR) {
-      b0 = V.m * V.m / s;
-      b1 = log((b0 + 1.0) / b0);
-    }
+    if (xr) xr[V.x_phi] = geo[(PHS_INV_GEO * v + 3) * PHS_INV_BLOCK];
+    double *cache = geo + (PHS_INV_GEO * v + 9) * PHS_INV_BLOCK;
     double x, f;
-    map_ct_inverse(V.ct_class, geo[(PHS_INV_GEO * v + 2) * PHS_INV_BLOCK], b0, b1, x, f);
-    xr[V.x_ct] = x;
+    if (reuse >> (3 * v + 2) & 1) {
+      x = cache[0];
+      f = cache[PHS_INV_BLOCK];
+    } else {
+      double b0 = V.b0, b1 = V.b1;
+      if (PER_EVENT && V.ct_class == PHS_CT_COLLINEAR) {
+        b0 = V.m * V.m / s;
+        b1 = log((b0 + 1.0) / b0);
+      }
+      map_ct_inverse(V.ct_class, geo[(PHS_INV_GEO * v + 2) * PHS_INV_BLOCK], b0, b1, x, f);
+      cache[0] = x;
+      cache[PHS_INV_BLOCK] = f;
+    }
+    if (xr) xr[V.x_ct] = x;
     factor *= f;
   }
   return factor;
@@ -389,10 +411,15 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
         inverse_geometry(a.channels[a.group_order[gb]], pm + tid, sqrts, stk, geo + tid);
         for (int i = gb; i < ge; i++) {
           const int c = a.group_order[i];
-          if (c == own_e && has_own) continue;
-          double *xr = a.x_out + ((int64_t)c * a.n_events + e) * a.n_x;
-          a.all_factors[e * a.n_channels + c] =
-              inverse_maps<PER_EVENT>(a.channels[c], sqrts, geo + tid, xr);
+          // the generating channel keeps its own row, but its mappings still run when a
+          // later channel of the shape reuses them
+          const bool own_row = c == own_e && has_own;
+          if (own_row && (i + 1 == ge || a.group_reuse[i + 1] == 0)) continue;
+          double *xr = own_row ? nullptr : a.x_out + ((int64_t)c * a.n_events + e) * a.n_x;
+          // the first channel of a shape computes every mapping
+          const uint64_t reuse = i == gb ? 0ull : a.group_reuse[i];
+          const double fac = inverse_maps<PER_EVENT>(a.channels[c], sqrts, geo + tid, xr, reuse);
+          if (!own_row) a.all_factors[e * a.n_channels + c] = fac;
         }
       }
     }
