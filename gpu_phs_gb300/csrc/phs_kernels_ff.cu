@@ -355,6 +355,15 @@ __device__ __forceinline__ void fill_ff_tables(FFTables &T) {
   }
 }
 
+// An x value for the pre-test, which needs only the row's first few (msq) entries: the L2
+// fetches 64 bytes around it rather than its default larger prefetch, so rows whose angle
+// entries only the walk reads (for the events that survive) are not pulled in whole.
+__device__ __forceinline__ double ld_x_narrow(const double *p) {
+  double v;
+  asm volatile("ld.global.L2::64B.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+
 // Saved mass intervals of the pre-test: in shared memory inside the fused kernel (slots of
 // the float-float frame stack, which that kernel owns anyway), in registers in the
 // stand-alone test kernel (the depth is at most PHS_STACK_DEPTH).
@@ -419,7 +428,8 @@ __device__ __forceinline__ bool phs_ok_f32(const PhsLaunch &a, const PhsSegment 
         cmax[j] = 0.0f;
       } else {
         float e;
-        const float msq = msq_f32((code >> 1) & 127, A[j], B[j].x, B[j].y, xe[(code >> 8) & 255], e);
+        const float msq = msq_f32((code >> 1) & 127, A[j], B[j].x, B[j].y,
+                                  ld_x_narrow(xe + ((code >> 8) & 255)), e);
         fails = fails || msq + e < 0.0f;                // negative for certain: not ok
         lo[j] = sqrtf(fmaxf(msq - e, 0.0f)) * dn;       // NaN bounds decide nothing
         hi[j] = sqrtf(fmaxf(msq + e, 0.0f)) * up;
