@@ -167,7 +167,7 @@ int sm_count(int device) {
 }
 
 int grid_for(int64_t n_tiles, int device, int stack_depth, bool per_event, int variant) {
-  const int warps_per_block = PHS_FWD_BLOCK / 32;
+  const int warps_per_block = phs_forward_block_size(variant) / 32;
   int64_t want = (n_tiles + warps_per_block - 1) / warps_per_block;
   int64_t cap =
       (int64_t)sm_count(device) * phs_forward_blocks_per_sm(stack_depth, per_event, variant);
@@ -189,15 +189,20 @@ int grid_for_ff(int64_t n_tiles, int device, int stack_depth, int variant) {
 // it.  launch(v) enqueues variant v.
 const int64_t kTuneEvents = 1 << 18;
 
+const int kMaxVariants = 16;
+static_assert(PHS_F64_VARIANTS <= kMaxVariants && PHS_FF_VARIANTS <= kMaxVariants,
+              "launch_tuned keeps one timing per variant");
+
 template <class Launch>
 int launch_tuned(int &variant, int n_variants, int64_t n_events, cudaStream_t st, Launch launch) {
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   cudaStreamIsCapturing(st, &cap);
+  if (n_variants > kMaxVariants) return fail(PHS_ERR_INVALID_ARG, "too many kernel variants");
   if (variant < 0 && n_events >= kTuneEvents && cap == cudaStreamCaptureStatusNone) {
     cudaEvent_t e0, e1;
     CUDA_TRY(cudaEventCreate(&e0));
     CUDA_TRY(cudaEventCreate(&e1));
-    float best[8];
+    float best[kMaxVariants];
     for (int v = 0; v < n_variants; v++) best[v] = 1e30f;
     for (int rep = 0; rep < 2; rep++) {
       for (int v = 0; v < n_variants; v++) {
@@ -270,8 +275,9 @@ int launch_f64_tuned(int &variant, Segments &S, PhsLaunch a, int device, int dep
     if (int rc = attach_pass_buffers(S, a)) return rc;
   const int n_variants = per_event ? PHS_F64_VARIANTS_PER_EVENT : PHS_F64_VARIANTS;
   return launch_tuned(variant, n_variants, n_events, st, [&](int v) {
-    // per-event beams have no pre-test: a pinned split form runs as the compacting one
-    if (per_event && v >= PHS_F64_VARIANTS_PER_EVENT) v -= 2;
+    // per-event beams have no pre-test: a pinned split form runs as the compacting or
+    // one-pass form of the same block shape
+    if (per_event && v >= PHS_F64_VARIANTS_PER_EVENT) v -= 4;
     cudaError_t e = cudaSuccess;
     if (a.work) e = cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), st);
     if (e == cudaSuccess && v >= PHS_F64_VARIANTS_PER_EVENT)
@@ -483,8 +489,14 @@ extern "C" int phs_process_set_beams(phs_process_t h, double E1, double E2) {
       }
       return sig;
     };
-    auto same = [](const std::vector<double> &x, const std::vector<double> &y) {
-      return x.size() == y.size() && (x.empty() || memcmp(x.data(), y.data(), x.size() * sizeof(double)) == 0);
+    // signatures compare by their bits (a strict weak order even with -0.0 or NaN)
+    auto bits = [](const std::vector<double> &x) {
+      std::vector<uint64_t> b(x.size());
+      if (!x.empty()) memcpy(b.data(), x.data(), x.size() * sizeof(double));
+      return b;
+    };
+    auto same = [&](const std::vector<double> &x, const std::vector<double> &y) {
+      return bits(x) == bits(y);
     };
     std::vector<int32_t> order;
     std::vector<uint64_t> reuse;
@@ -493,8 +505,8 @@ extern "C" int phs_process_set_beams(phs_process_t h, double E1, double E2) {
       std::stable_sort(m.begin(), m.end(), [&](int c1, int c2) {
         for (int v = 0; v < nv; v++)
           for (int k = 0; k < 3; k++) {
-            const auto x = mapping(c1, v, k), y = mapping(c2, v, k);
-            if (!same(x, y)) return std::lexicographical_compare(x.begin(), x.end(), y.begin(), y.end());
+            const auto x = bits(mapping(c1, v, k)), y = bits(mapping(c2, v, k));
+            if (x != y) return x < y;
           }
         return false;
       });

@@ -46,18 +46,20 @@ struct PhsLaunch {
 // Block size and resident blocks per SM of the forward kernel.
 #define PHS_FWD_BLOCK 128
 
-// variant 0: one pass per event; 1 and 2: compacting (pass A tests every event and writes
-// the failures, pass B computes the passing events densely) with registers for 4 or 3
-// resident blocks per SM; 3 and 4: split (the FP32 pre-test of phs_launch_pretest, then
-// the FP64 walk over its survivors; uniform beams only, needs the a.pass_* buffers and
-// a.work zeroed), 4 or 3 blocks.  PHS_F64_VARIANTS of them; the first
+// Variants, each a form at one block shape (threads per block x resident blocks per SM):
+// 0: one pass, 128 x 4; 1, 2: compacting (pass A tests every event and writes the
+// failures, pass B computes the passing events densely), 128 x 4 and 128 x 3; 3, 4: one
+// pass, 256 x 2 and 64 x 8; 5-8: split (the FP32 pre-test of phs_launch_pretest, then the
+// FP64 walk over its survivors; uniform beams only, needs the a.pass_* buffers and a.work
+// zeroed), 128 x 4, 128 x 3, 256 x 2, 64 x 8.  PHS_F64_VARIANTS of them; the first
 // PHS_F64_VARIANTS_PER_EVENT serve per-event beams.
-#define PHS_F64_VARIANTS 5
-#define PHS_F64_VARIANTS_PER_EVENT 3
+#define PHS_F64_VARIANTS 9
+#define PHS_F64_VARIANTS_PER_EVENT 5
 cudaError_t phs_launch_forward_f64(const PhsLaunch &a, int n_blocks, int variant,
                                    cudaStream_t stream);
 int phs_forward_blocks_per_sm(int stack_depth, bool per_event, int variant);
-size_t phs_forward_smem_bytes(int stack_depth);
+int phs_forward_block_size(int variant);
+size_t phs_forward_smem_bytes(int stack_depth, int block = PHS_FWD_BLOCK);
 
 // Philox4x32-10 uniform doubles for events [first_event, first_event + n_events) of the
 // stream `seed`, row length n_x (the layout is documented in gpu_phs_gb300/philox.py).

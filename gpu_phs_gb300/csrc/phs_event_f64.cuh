@@ -237,17 +237,20 @@ __device__ __forceinline__ void fill_trig_table(double2 *tab) {
   }
 }
 
+// Frame stack slot k of depth `depth`: one column per thread of a BLOCK-thread block.
+template <int BLOCK>
 __device__ __forceinline__ void stack_store(double *smem, int depth, int k, double v) {
-  smem[(depth * PHS_STATE + k) * PHS_FWD_BLOCK + threadIdx.x] = v;
+  smem[(depth * PHS_STATE + k) * BLOCK + threadIdx.x] = v;
 }
+template <int BLOCK>
 __device__ __forceinline__ double stack_load(const double *smem, int depth, int k) {
-  return smem[(depth * PHS_STATE + k) * PHS_FWD_BLOCK + threadIdx.x];
+  return smem[(depth * PHS_STATE + k) * BLOCK + threadIdx.x];
 }
 
 // One event: segment `seg`, local index `local` (< seg.ev_count).  smem is this block's
-// frame stack, PHS_STATE * stack_depth doubles per thread; trig the block's table of
-// sincos2pi_tab.
-template <bool PER_EVENT>
+// frame stack, PHS_STATE * stack_depth doubles per thread of a BLOCK-thread block; trig the
+// block's table of sincos2pi_tab.
+template <bool PER_EVENT, int BLOCK = PHS_FWD_BLOCK>
 __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegment &seg,
                                               int64_t local, double *smem, const double2 *trig) {
   const PhsChannel &ch = a.channels[seg.channel];
@@ -404,12 +407,12 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
     if (V.push >= 0) {
       const bool j0 = V.push == 0;
 #pragma unroll
-      for (int i = 0; i < 16; i++) stack_store(smem, sp, i, Ln[i]);
-      stack_store(smem, sp, 16, j0 ? cmsq[0] : cmsq[1]);
-      stack_store(smem, sp, 17, j0 ? cm[0] : cm[1]);
-      stack_store(smem, sp, 18, j0 ? pc : -pc);
-      stack_store(smem, sp, 19, j0 ? cmax[0] : cmax[1]);
-      stack_store(smem, sp, 20, j0 ? ce0 : ce1);
+      for (int i = 0; i < 16; i++) stack_store<BLOCK>(smem, sp, i, Ln[i]);
+      stack_store<BLOCK>(smem, sp, 16, j0 ? cmsq[0] : cmsq[1]);
+      stack_store<BLOCK>(smem, sp, 17, j0 ? cm[0] : cm[1]);
+      stack_store<BLOCK>(smem, sp, 18, j0 ? pc : -pc);
+      stack_store<BLOCK>(smem, sp, 19, j0 ? cmax[0] : cmax[1]);
+      stack_store<BLOCK>(smem, sp, 20, j0 ? ce0 : ce1);
       sp++;
     }
     if (V.carry >= 0) {
@@ -424,12 +427,12 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
     } else if (sp > 0) {
       sp--;
 #pragma unroll
-      for (int i = 0; i < 16; i++) L[i] = stack_load(smem, sp, i);
-      msq_b = stack_load(smem, sp, 16);
-      m_b = stack_load(smem, sp, 17);
-      p_b = stack_load(smem, sp, 18);
-      mmax_b = stack_load(smem, sp, 19);
-      E_b = stack_load(smem, sp, 20);
+      for (int i = 0; i < 16; i++) L[i] = stack_load<BLOCK>(smem, sp, i);
+      msq_b = stack_load<BLOCK>(smem, sp, 16);
+      m_b = stack_load<BLOCK>(smem, sp, 17);
+      p_b = stack_load<BLOCK>(smem, sp, 18);
+      mmax_b = stack_load<BLOCK>(smem, sp, 19);
+      E_b = stack_load<BLOCK>(smem, sp, 20);
     }
   }
 
@@ -462,7 +465,7 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
 // fails gets its outputs here (momenta 0, factor 0, ok 0, the channel volume); one that
 // passes gets them from phs_event_f64 in pass B.  Returns ok.  smem: the event's frame
 // stack (only the msq, m and m_max slots are used).
-template <bool PER_EVENT>
+template <bool PER_EVENT, int BLOCK = PHS_FWD_BLOCK>
 __device__ __forceinline__ bool phs_ok_f64(const PhsLaunch &a, const PhsSegment &seg,
                                            int64_t local, double *smem) {
   const PhsChannel &ch = a.channels[seg.channel];
@@ -499,9 +502,9 @@ __device__ __forceinline__ bool phs_ok_f64(const PhsLaunch &a, const PhsSegment 
     ok = ok && (lda > 0.0) && (m_b > dadd(cm[0], cm[1])) && (m_b <= mmax_b);
     if (V.push >= 0) {
       const bool j0 = V.push == 0;
-      stack_store(smem, sp, 16, j0 ? cmsq[0] : cmsq[1]);
-      stack_store(smem, sp, 17, j0 ? cm[0] : cm[1]);
-      stack_store(smem, sp, 19, j0 ? cmax[0] : cmax[1]);
+      stack_store<BLOCK>(smem, sp, 16, j0 ? cmsq[0] : cmsq[1]);
+      stack_store<BLOCK>(smem, sp, 17, j0 ? cm[0] : cm[1]);
+      stack_store<BLOCK>(smem, sp, 19, j0 ? cmax[0] : cmax[1]);
       sp++;
     }
     if (V.carry >= 0) {
@@ -511,9 +514,9 @@ __device__ __forceinline__ bool phs_ok_f64(const PhsLaunch &a, const PhsSegment 
       mmax_b = j0 ? cmax[0] : cmax[1];
     } else if (sp > 0) {
       sp--;
-      msq_b = stack_load(smem, sp, 16);
-      m_b = stack_load(smem, sp, 17);
-      mmax_b = stack_load(smem, sp, 19);
+      msq_b = stack_load<BLOCK>(smem, sp, 16);
+      m_b = stack_load<BLOCK>(smem, sp, 17);
+      mmax_b = stack_load<BLOCK>(smem, sp, 19);
     }
   }
   if (!ok) {

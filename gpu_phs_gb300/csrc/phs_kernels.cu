@@ -17,32 +17,36 @@
 namespace {
 
 // The sin/cos table sits after the frame stack and the queues (phs_forward_smem_bytes).
+template <int BLOCK = PHS_FWD_BLOCK>
 __device__ __forceinline__ double2 *phs_trig_table(double *smem, int stack_depth) {
-  return reinterpret_cast<double2 *>(smem + (size_t)stack_depth * PHS_STATE * PHS_FWD_BLOCK +
-                                     (size_t)(PHS_FWD_BLOCK / 32) * 64);
+  return reinterpret_cast<double2 *>(smem + (size_t)stack_depth * PHS_STATE * BLOCK +
+                                     (size_t)(BLOCK / 32) * 64);
 }
 
 // COMPACT: events whose kinematic test fails need no angles or boosts.  Where many fail
 // (low ok fractions: multi-channel batches, hard cuts), pass A tests each event, writes
 // the failures, and queues the rest per warp; pass B runs them densely.  Where nearly all
 // pass, the plain loop avoids the second msq evaluation; the launcher times both.
-template <bool PER_EVENT, bool COMPACT, int MIN_BLOCKS>
-__global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
+// BLOCK threads per block (the block shape the autotuner tries), MIN_BLOCKS resident.
+template <bool PER_EVENT, bool COMPACT, int MIN_BLOCKS, int BLOCK = PHS_FWD_BLOCK>
+__global__ void __launch_bounds__(BLOCK, MIN_BLOCKS)
     phs_forward_f64_kernel(const __grid_constant__ PhsLaunch a) {
   extern __shared__ double smem[];
   const int lane = threadIdx.x & 31;
   const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  double2 *trig = phs_trig_table(smem, a.stack_depth);
+  double2 *trig = phs_trig_table<BLOCK>(smem, a.stack_depth);
   fill_trig_table(trig);
   __syncthreads();
   if constexpr (COMPACT) {
-    int64_t *q = reinterpret_cast<int64_t *>(smem + (size_t)a.stack_depth * PHS_STATE * PHS_FWD_BLOCK) +
+    int64_t *q = reinterpret_cast<int64_t *>(smem + (size_t)a.stack_depth * PHS_STATE * BLOCK) +
                  (threadIdx.x >> 5) * 64;
     compacting_loop<PHS_CHUNK_TILES>(
         a, q,
-        [&](const PhsSegment &sg, int64_t loc) { return phs_ok_f64<PER_EVENT>(a, sg, loc, smem); },
-        [&](int, const PhsSegment &sg, int64_t loc) { phs_event_f64<PER_EVENT>(a, sg, loc, smem, trig); });
+        [&](const PhsSegment &sg, int64_t loc) { return phs_ok_f64<PER_EVENT, BLOCK>(a, sg, loc, smem); },
+        [&](int, const PhsSegment &sg, int64_t loc) {
+          phs_event_f64<PER_EVENT, BLOCK>(a, sg, loc, smem, trig);
+        });
   } else {
     for (int64_t tile = warp0; tile < a.n_tiles; tile += n_warps) {
       // the segment holding this tile (warp-uniform binary search on tile_begin)
@@ -55,7 +59,7 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
       const PhsSegment seg = segs[lo];
       const int64_t local = (tile - seg.tile_begin) * 32 + lane;
       if (local >= seg.ev_count) continue;
-      phs_event_f64<PER_EVENT>(a, seg, local, smem, trig);
+      phs_event_f64<PER_EVENT, BLOCK>(a, seg, local, smem, trig);
     }
   }
 }
@@ -98,12 +102,12 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, 4)
 // FP64 walk over the queued events, 32 of one segment per warp claim (a.work counts the
 // claims, zeroed before the launch).  The pre-test only settles failures that the FP64
 // test makes too, so the outputs are the one-pass kernel's bits.  Uniform beams only.
-template <int MIN_BLOCKS>
-__global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
+template <int MIN_BLOCKS, int BLOCK = PHS_FWD_BLOCK>
+__global__ void __launch_bounds__(BLOCK, MIN_BLOCKS)
     phs_f64_walk_kernel(const __grid_constant__ PhsLaunch a) {
   extern __shared__ double smem[];
   const int lane = threadIdx.x & 31;
-  double2 *trig = phs_trig_table(smem, a.stack_depth);
+  double2 *trig = phs_trig_table<BLOCK>(smem, a.stack_depth);
   fill_trig_table(trig);
   __syncthreads();
   const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
@@ -122,7 +126,7 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
     const PhsSegment seg = segs[lo];
     const int64_t idx = (t - a.pass_tile[lo]) * 32 + lane;
     if (idx >= (int64_t)a.pass_count[lo]) continue;
-    phs_event_f64<false>(a, seg, a.pass_queue[seg.tile_begin * 32 + idx], smem, trig);
+    phs_event_f64<false, BLOCK>(a, seg, a.pass_queue[seg.tile_begin * 32 + idx], smem, trig);
   }
 }
 
@@ -218,68 +222,106 @@ cudaError_t phs_launch_fma_rate(void *out, int fp64, int blocks, int threads, in
   return cudaGetLastError();
 }
 
-size_t phs_forward_smem_bytes(int stack_depth) {
+size_t phs_forward_smem_bytes(int stack_depth, int block) {
   // frame stack, the compacting variant's per-warp queues (64 events per warp), the
   // sin/cos table
-  return (size_t)stack_depth * PHS_STATE * PHS_FWD_BLOCK * sizeof(double) +
-         (size_t)(PHS_FWD_BLOCK / 32) * 64 * sizeof(int64_t) + 64 * sizeof(double2);
+  return (size_t)stack_depth * PHS_STATE * block * sizeof(double) +
+         (size_t)(block / 32) * 64 * sizeof(int64_t) + 64 * sizeof(double2);
 }
 
-// variant 0: one pass, registers for 4 resident blocks per SM; 1: compacting, 4 blocks;
-// 2: compacting, 3 blocks (no spills); 3 and 4: split (FP32 pre-test, then the walk over
-// its survivors) with 4 or 3 blocks, uniform beams only.
+// Variants (each at one block shape, BLOCK threads, and a register budget): 0: one pass,
+// 128 threads x 4 blocks per SM; 1, 2: compacting, 128 x 4 and 128 x 3 (no spills);
+// 3, 4: one pass, 256 x 2 and 64 x 8; 5-8: split (the FP32 pre-test, then the walk over its
+// survivors; uniform beams only), 128 x 4, 128 x 3, 256 x 2, 64 x 8.  The 128-register
+// budget is the same for 64 x 8, 128 x 4 and 256 x 2.
+static int f64_block(int variant) {
+  switch (variant) {
+    case 3: case 7: return 256;
+    case 4: case 8: return 64;
+    default: return PHS_FWD_BLOCK;
+  }
+}
+
 template <bool PER_EVENT>
 static const void *f64_kernel(int variant) {
   switch (variant) {
     case 1: return (const void *)phs_forward_f64_kernel<PER_EVENT, true, 4>;
     case 2: return (const void *)phs_forward_f64_kernel<PER_EVENT, true, 3>;
-    case 3: return (const void *)phs_f64_walk_kernel<4>;
-    case 4: return (const void *)phs_f64_walk_kernel<3>;
+    case 3: return (const void *)phs_forward_f64_kernel<PER_EVENT, false, 2, 256>;
+    case 4: return (const void *)phs_forward_f64_kernel<PER_EVENT, false, 8, 64>;
+    case 5: return (const void *)phs_f64_walk_kernel<4>;
+    case 6: return (const void *)phs_f64_walk_kernel<3>;
+    case 7: return (const void *)phs_f64_walk_kernel<2, 256>;
+    case 8: return (const void *)phs_f64_walk_kernel<8, 64>;
     default: return (const void *)phs_forward_f64_kernel<PER_EVENT, false, 4>;
   }
 }
 
+int phs_forward_block_size(int variant) { return f64_block(variant); }
+
+// Shared memory above the 48 KB default (256-thread blocks with two saved frames) needs
+// the kernel's opt-in.
+static cudaError_t allow_smem(const void *kernel, size_t smem) {
+  if (smem <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
 int phs_forward_blocks_per_sm(int stack_depth, bool per_event, int variant) {
   int n = 0;
-  const size_t smem = phs_forward_smem_bytes(stack_depth);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &n, per_event ? f64_kernel<true>(variant) : f64_kernel<false>(variant), PHS_FWD_BLOCK, smem);
+  const int block = f64_block(variant);
+  const size_t smem = phs_forward_smem_bytes(stack_depth, block);
+  const void *k = per_event ? f64_kernel<true>(variant) : f64_kernel<false>(variant);
+  if (allow_smem(k, smem) != cudaSuccess) return 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, block, smem);
   return n > 0 ? n : 1;
 }
 
 template <bool PER_EVENT>
-static void launch_f64(const PhsLaunch &a, int n_blocks, int variant, size_t smem,
-                       cudaStream_t stream) {
+static void launch_f64(const PhsLaunch &a, int n_blocks, int variant, cudaStream_t stream) {
+  const int block = f64_block(variant);
+  const size_t smem = phs_forward_smem_bytes(a.stack_depth, block);
+  if (allow_smem(f64_kernel<PER_EVENT>(variant), smem) != cudaSuccess) return;
   switch (variant) {
     case 1:
-      phs_forward_f64_kernel<PER_EVENT, true, 4><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+      phs_forward_f64_kernel<PER_EVENT, true, 4><<<n_blocks, block, smem, stream>>>(a);
       break;
     case 2:
-      phs_forward_f64_kernel<PER_EVENT, true, 3><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+      phs_forward_f64_kernel<PER_EVENT, true, 3><<<n_blocks, block, smem, stream>>>(a);
+      break;
+    case 3:
+      phs_forward_f64_kernel<PER_EVENT, false, 2, 256><<<n_blocks, block, smem, stream>>>(a);
+      break;
+    case 4:
+      phs_forward_f64_kernel<PER_EVENT, false, 8, 64><<<n_blocks, block, smem, stream>>>(a);
       break;
     default:
-      phs_forward_f64_kernel<PER_EVENT, false, 4><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+      phs_forward_f64_kernel<PER_EVENT, false, 4><<<n_blocks, block, smem, stream>>>(a);
   }
 }
 
 cudaError_t phs_launch_forward_f64(const PhsLaunch &a, int n_blocks, int variant,
                                    cudaStream_t stream) {
   if (a.n_tiles <= 0) return cudaSuccess;
-  const size_t smem = phs_forward_smem_bytes(a.stack_depth);
-  if (variant >= 3) {
+  if (variant >= 5) {
     if (a.E1 || a.E2) return cudaErrorInvalidValue;  // the pre-test needs uniform beams
     cudaError_t e = phs_launch_pretest(a, stream);
     if (e != cudaSuccess) return e;
-    if (variant == 3)
-      phs_f64_walk_kernel<4><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
-    else
-      phs_f64_walk_kernel<3><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+    const int block = f64_block(variant);
+    const size_t smem = phs_forward_smem_bytes(a.stack_depth, block);
+    e = allow_smem(f64_kernel<false>(variant), smem);
+    if (e != cudaSuccess) return e;
+    switch (variant) {
+      case 5: phs_f64_walk_kernel<4><<<n_blocks, block, smem, stream>>>(a); break;
+      case 6: phs_f64_walk_kernel<3><<<n_blocks, block, smem, stream>>>(a); break;
+      case 7: phs_f64_walk_kernel<2, 256><<<n_blocks, block, smem, stream>>>(a); break;
+      default: phs_f64_walk_kernel<8, 64><<<n_blocks, block, smem, stream>>>(a);
+    }
     return cudaGetLastError();
   }
   if (a.E1 && a.E2)
-    launch_f64<true>(a, n_blocks, variant, smem, stream);
+    launch_f64<true>(a, n_blocks, variant, stream);
   else
-    launch_f64<false>(a, n_blocks, variant, smem, stream);
+    launch_f64<false>(a, n_blocks, variant, stream);
   return cudaGetLastError();
 }
 
@@ -287,8 +329,8 @@ cudaError_t phs_launch_forward_exact(const PhsLaunch &a, int n_blocks, cudaStrea
   if (a.n_tiles <= 0) return cudaSuccess;
   cudaError_t e = phs_launch_count_scan(a.exact_count, a.exact_tile, a.n_segments, stream);
   if (e != cudaSuccess) return e;
-  phs_forward_exact_kernel<<<n_blocks, PHS_FWD_BLOCK, phs_forward_smem_bytes(a.stack_depth),
-                             stream>>>(a);
+  phs_forward_exact_kernel<<<n_blocks, PHS_FWD_BLOCK,
+                             phs_forward_smem_bytes(a.stack_depth, PHS_FWD_BLOCK), stream>>>(a);
   return cudaGetLastError();
 }
 
@@ -365,7 +407,7 @@ cudaError_t phs_launch_forward_f64_noalloc(PhsLaunch a, const PhsChannel *channe
   a.segments = s->segments;
   a.n_segments = n_segments;
   if (a.n_tiles <= 0) return cudaSuccess;
-  const size_t smem = phs_forward_smem_bytes(a.stack_depth);
+  const size_t smem = phs_forward_smem_bytes(a.stack_depth, PHS_FWD_BLOCK);
   phs_forward_f64_kernel<false, false, 4><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
   return cudaGetLastError();
 }

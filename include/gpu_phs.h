@@ -93,9 +93,10 @@ int phs_process_set_precision(phs_process_t proc, int precision);
  * first launch of at least 2^18 events (outside stream capture) has timed them.  FP32 pair
  * (ff_variant): 0-3: bit 0 register budget for 4 (1) or 3 (0) resident blocks per SM, bit 1
  * the compacting two-pass form; 4 and 5: the split form (an FP32 pre-test kernel, then the
- * float-float walk over the events it passed) with 3 or 4 blocks.  FP64 (f64_variant): 0 one
- * pass, 1 and 2 compacting (registers for 4 or 3 resident blocks), 3 and 4 split (the FP32
- * pre-test, then the FP64 walk; 4 or 3 blocks; per-event beams run 3 and 4 as 1 and 2).  The
+ * float-float walk over the events it passed) with 3 or 4 blocks.  FP64 (f64_variant), each
+ * at one block shape (threads per block x resident blocks per SM): 0 one pass 128 x 4; 1, 2
+ * compacting 128 x 4, 128 x 3; 3, 4 one pass 256 x 2, 64 x 8; 5-8 split (the FP32 pre-test,
+ * then the FP64 walk) 128 x 4, 128 x 3, 256 x 2, 64 x 8 (per-event beams run 5-8 as 1-4).  The
  * compacting and split forms test every event first and compute only the passing ones,
  * densely; they win where many events fail the kinematic test.  Variants compute identical
  * bits.  Either pointer may be NULL. */

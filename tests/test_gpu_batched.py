@@ -81,10 +81,10 @@ def _gen_batch(torch, spaces, counts, x, prec, ff_v=-1, f64_v=-1):
     return [t.clone() for t in out]
 
 
-@pytest.mark.parametrize("prec,n_var", [(0, 5), (1, 6)])
+@pytest.mark.parametrize("prec,n_var", [(0, 9), (1, 6)])
 def test_kernel_variants_identical_bits(torch, prec, n_var):
-    """Every kernel variant (register budgets, one-pass, compacting or split) computes the
-    same bits: the compacting and split forms run the same event code on the events that
+    """Every kernel variant (block shapes, register budgets, one-pass, compacting or split)
+    computes the same bits: the compacting and split forms run the same event code on the events that
     pass their pre-test, and the pre-test writes the outputs of failing events exactly as
     the one-pass form does."""
     from gpu_phs_gb300.api import Batch, PhaseSpace, philox_fill
@@ -102,10 +102,10 @@ def test_kernel_variants_identical_bits(torch, prec, n_var):
             assert torch.equal(a, b), f"variant {v} differs from variant 0"
 
 
-@pytest.mark.parametrize("f64_v", [1, 2, 3, 4])
+@pytest.mark.parametrize("f64_v", [1, 2, 3, 4, 5, 6, 7, 8])
 def test_compacting_fp64_vs_oracle_low_ok_fraction(torch, f64_v):
-    """The 13 TeV configuration (about 4% of events pass) through a compacting or split
-    variant, against the oracle."""
+    """The 13 TeV configuration (about 4% of events pass) through every FP64 variant but the
+    default one pass (block shapes, compacting, split), against the oracle."""
     from conftest import momentum_rel_err
     from gpu_phs_gb300.api import PhaseSpace
     from gpu_phs_gb300.philox import uniform_x
@@ -148,7 +148,8 @@ def test_split_form_many_segments_and_empty_channels(torch):
 
 def test_per_event_beams_with_a_split_variant_pinned(torch):
     """The FP32 pre-test needs uniform beams: with per-event beams a pinned split variant
-    runs as the compacting one, with the same bits as the one-pass kernel."""
+    runs as the compacting or one-pass variant of its block shape, with the same bits as
+    the default one-pass kernel."""
     from gpu_phs_gb300.api import PhaseSpace, philox_x
     proc = P.tt()
     n = 100_000
@@ -157,7 +158,7 @@ def test_per_event_beams_with_a_split_variant_pinned(torch):
     E1 = 300 + 400 * torch.rand(n, generator=g, device="cuda", dtype=torch.float64)
     E2 = 300 + 400 * torch.rand(n, generator=g, device="cuda", dtype=torch.float64)
     outs = []
-    for v in (0, 3, 4):
+    for v in (0, 3, 4, 5, 6, 7, 8):
         ps = PhaseSpace(proc)
         ps.set_variants(-1, v)
         ev = ps.generate_beams(x, E1, E2)
