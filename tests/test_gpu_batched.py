@@ -71,6 +71,44 @@ def test_process_graph_replay(torch):
     assert torch.equal(out.p, ref.p) and torch.equal(out.ok, ref.ok)
 
 
+@pytest.mark.parametrize("prec,variant", [(0, 5), (0, 8), (1, 5), (1, 4)])
+def test_split_forms_in_cuda_graphs(torch, prec, variant):
+    """A split variant pinned before capture (so the graph holds its pre-test, scan, walk,
+    and for FP32 pairs the exact path, with their counter resets): replays equal the
+    one-pass kernel's outputs, twice in a row."""
+    from gpu_phs_gb300.api import Batch, PhaseSpace, batch_graph, philox_fill
+    procs, counts = P.batched(seed=77, n_channels=64, total_events=1 << 19)
+    spaces = [PhaseSpace(p, 500.0, 500.0) for p in procs]
+    ref = None
+    xo = po = None
+    for v in (0, variant):
+        batch = Batch(spaces)
+        batch.set_precision(prec)
+        batch.set_variants(v if prec else -1, -1 if prec else v)
+        xo, po = batch.offsets(counts)
+        if ref is None:
+            x = torch.empty(int(xo[-1]), dtype=torch.float64, device="cuda")
+            philox_fill(x, int(xo[-1]), 1, seed=9)
+        n = int(counts.sum())
+        bufs = (torch.empty(int(po[-1]), dtype=torch.float64, device="cuda"),
+                torch.empty(n, dtype=torch.float64, device="cuda"),
+                torch.empty(n, dtype=torch.float64, device="cuda"),
+                torch.empty(n, dtype=torch.uint8, device="cuda"))
+        g = batch_graph(batch, x, counts, *bufs)
+        outs = []
+        for _ in range(2):
+            for t in bufs:
+                t.fill_(7)
+            g.launch()
+            torch.cuda.synchronize()
+            outs.append([t.clone() for t in bufs])
+        if ref is None:
+            ref = outs[0]
+        for o in outs:
+            for a, b in zip(ref, o):
+                assert torch.equal(a, b)
+
+
 def _gen_batch(torch, spaces, counts, x, prec, ff_v=-1, f64_v=-1):
     from gpu_phs_gb300.api import Batch
     batch = Batch(spaces)
