@@ -12,6 +12,9 @@
 //      own frame with the inverse rotation+boost, L_pre = L_post eta L1^T eta, so the boost
 //      chain is recomputed backwards.  Adjoints of frames and states travel up the tree
 //      with a stack that mirrors the forward one.
+// Friend (beam-axis) visits rotate the decay frame onto an axis computed from the parent
+// frame; the forward pass keeps that axis per visit, and the reverse walk rebuilds the
+// rotation and differentiates it (a forward-mode evaluation with three tangents).
 // Uniform beams only.  Events with ok = 0 get zero derivatives.
 #include <cuda_runtime.h>
 #include <math.h>
@@ -32,7 +35,71 @@ namespace {
 struct AdjLayout {
   int state0, ang0, der0, pop0, stack0;  // offsets (in slots) of the per-thread regions
   int trig0;                             // the block's sin/cos table (2 slots)
+  int fr0;                               // friend visits: the rotation axis, 3 per visit
 };
+
+// A value with its derivatives along three directions (forward-mode differentiation).
+struct D3 {
+  double v, d[3];
+};
+__device__ __forceinline__ D3 d3(double v, int k) {
+  D3 r = {v, {0.0, 0.0, 0.0}};
+  if (k >= 0) r.d[k] = 1.0;
+  return r;
+}
+__device__ __forceinline__ D3 operator+(D3 a, D3 b) {
+  return {a.v + b.v, {a.d[0] + b.d[0], a.d[1] + b.d[1], a.d[2] + b.d[2]}};
+}
+__device__ __forceinline__ D3 operator-(D3 a, D3 b) {
+  return {a.v - b.v, {a.d[0] - b.d[0], a.d[1] - b.d[1], a.d[2] - b.d[2]}};
+}
+__device__ __forceinline__ D3 operator-(D3 a) { return {-a.v, {-a.d[0], -a.d[1], -a.d[2]}}; }
+__device__ __forceinline__ D3 operator*(D3 a, D3 b) {
+  return {a.v * b.v, {a.d[0] * b.v + a.v * b.d[0], a.d[1] * b.v + a.v * b.d[1],
+                      a.d[2] * b.v + a.v * b.d[2]}};
+}
+__device__ __forceinline__ D3 operator/(D3 a, D3 b) {
+  const double q = a.v / b.v, r = 1.0 / b.v;
+  return {q, {(a.d[0] - q * b.d[0]) * r, (a.d[1] - q * b.d[1]) * r, (a.d[2] - q * b.d[2]) * r}};
+}
+__device__ __forceinline__ D3 d3_sqrt(D3 a) {
+  const double s = sqrt(a.v), h = 0.5 / s;
+  return {s, {a.d[0] * h, a.d[1] * h, a.d[2] * h}};
+}
+
+// dR[i]/d(bx, by, bz) of rot_z_onto (same formula and branch): J[3 i + k].
+__device__ __forceinline__ void rot_z_onto_jacobian(double bx0, double by0, double bz0,
+                                                    double J[27]) {
+  D3 bx = d3(bx0, 0), by = d3(by0, 1), bz = d3(bz0, 2);
+  const D3 n = d3_sqrt(bx * bx + by * by + bz * bz);
+  bx = bx / n;
+  by = by / n;
+  bz = bz / n;
+  const D3 t = bx * bx + by * by;
+  D3 r00 = d3(1.0, -1), r01 = d3(0.0, -1), r11 = bz;
+  if (t.v > 0.0) {
+    const D3 w = (d3(1.0, -1) - bz) / t;
+    r00 = bz + w * (by * by);
+    r01 = -(w * (bx * by));
+    r11 = bz + w * (bx * bx);
+  }
+  const D3 R[9] = {r00, r01, bx, r01, r11, by, -bx, -by, bz};
+#pragma unroll
+  for (int i = 0; i < 9; i++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) J[3 * i + k] = R[i].d[k];
+}
+
+// Q = R_f A(theta, phi), the friend visit's spatial rotation (phs_event_f64.cuh).
+__device__ __forceinline__ void friend_rotation(const double Rf[9], double ct, double st,
+                                                double cphi, double sphi, double Q[9]) {
+  const double A[9] = {ct * cphi, -sphi, st * cphi, ct * sphi, cphi, st * sphi, -st, 0.0, ct};
+#pragma unroll
+  for (int r = 0; r < 3; r++)
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+      Q[3 * r + c] = Rf[3 * r] * A[c] + Rf[3 * r + 1] * A[3 + c] + Rf[3 * r + 2] * A[6 + c];
+}
 
 __device__ __forceinline__ double &slot(double *sm, int i) {
   return sm[i * PHS_ADJ_BLOCK + threadIdx.x];
@@ -110,6 +177,9 @@ __device__ __forceinline__ void ct_derivs(int ct_class, double x, double b0, dou
   }
 }
 
+// FRIENDS: the process has friend visits (a separate instantiation keeps their code out of
+// the register allocation of the others).
+template <bool FRIENDS>
 __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
     phs_adjoint_kernel(const __grid_constant__ PhsLaunch a, const PhsAdjChannel *__restrict__ adj,
                        const double *__restrict__ pbar, const double *__restrict__ jbar,
@@ -217,15 +287,39 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
         slot(sm, b + 5) = dst;
         slot(sm, b + 6) = dlf;
       }
-      const double e01 = -bg * st, e03 = bg * ct, e11 = ct * cphi, e12 = -sphi, e13 = st * cphi;
-      const double e21 = ct * sphi, e22 = cphi, e23 = st * sphi, e31 = -ga * st, e33 = ga * ct;
+      if (FRIENDS && V.friend_sign != 0) {
+        // L1 = B_z(bg) diag(1, R_f A(theta, phi)), R_f onto the friend beam's direction in
+        // the branch's rest frame; the axis is kept for the reverse walk
+        const double ff = V.friend_sign;
+        const double u0 = L[0] - ff * L[12];
+        const double ax = -(L[1] - ff * L[13]), ay = -(L[2] - ff * L[14]);
+        const double az = -bg * u0 - ga * (L[3] - ff * L[15]);
+        const int fb = lay.fr0 + 3 * v;
+        slot(sm, fb + 0) = ax;
+        slot(sm, fb + 1) = ay;
+        slot(sm, fb + 2) = az;
+        double Rf[9], Q[9];
+        rot_z_onto(ax, ay, az, Rf);
+        friend_rotation(Rf, ct, st, cphi, sphi, Q);
 #pragma unroll
-      for (int r = 0; r < 4; r++) {
-        const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
-        L[4 * r + 0] = l0 * ga + l3 * bg;
-        L[4 * r + 1] = l0 * e01 + l1 * e11 + l2 * e21 + l3 * e31;
-        L[4 * r + 2] = l1 * e12 + l2 * e22;
-        L[4 * r + 3] = l0 * e03 + l1 * e13 + l2 * e23 + l3 * e33;
+        for (int r = 0; r < 4; r++) {
+          const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
+          L[4 * r + 0] = l0 * ga + l3 * bg;
+#pragma unroll
+          for (int c = 0; c < 3; c++)
+            L[4 * r + 1 + c] = (l0 * bg + l3 * ga) * Q[6 + c] + l1 * Q[c] + l2 * Q[3 + c];
+        }
+      } else {
+        const double e01 = -bg * st, e03 = bg * ct, e11 = ct * cphi, e12 = -sphi, e13 = st * cphi;
+        const double e21 = ct * sphi, e22 = cphi, e23 = st * sphi, e31 = -ga * st, e33 = ga * ct;
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+          const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
+          L[4 * r + 0] = l0 * ga + l3 * bg;
+          L[4 * r + 1] = l0 * e01 + l1 * e11 + l2 * e21 + l3 * e31;
+          L[4 * r + 2] = l1 * e12 + l2 * e22;
+          L[4 * r + 3] = l0 * e03 + l1 * e13 + l2 * e23 + l3 * e33;
+        }
       }
       if (V.push >= 0) {
         const bool j0 = V.push == 0;
@@ -347,45 +441,132 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
           pcb += (j == 0 ? 1.0 : -1.0) * c_pb[j];
         }
       }
-      // parent frame L_pre = L eta L1^T eta; adjoints L1bar = L_pre^T Lb, Lpre_bar = Lb L1^T.
-      // L1 has zeros at (0,2), (1,0), (2,0), (3,2), and only its other 12 entries carry
-      // adjoints; the loops skip the zero terms (the compiler folds the constant ones).
       const double eta[4] = {1.0, -1.0, -1.0, -1.0};
-      double Lp[16], Lpb[16], L1b[16];
+      double Lp[16], Lpb[16];
+      double gab, bgb, ctb, stb, cpb, spb;
+      if (FRIENDS && V.friend_sign != 0) {
+        // friend visit: L1 = F = B_z(bg) diag(1, Q), Q = R_f(axis) A(theta, phi), axis from
+        // the parent frame (kept by the forward pass).  L_pre = L eta F^T eta,
+        // Lpre_bar = Lb F^T, Fbar = L_pre^T Lb, then through Q to the angles, R_f and the
+        // axis, and from the axis back to the parent frame, bg and gamma.
+        const double ff = V.friend_sign;
+        const int fb = lay.fr0 + 3 * v;
+        const double ax = slot(sm, fb + 0), ay = slot(sm, fb + 1), az = slot(sm, fb + 2);
+        double Rf[9], Q[9];
+        rot_z_onto(ax, ay, az, Rf);
+        friend_rotation(Rf, ct, st, cphi, sphi, Q);
+        const double F[16] = {ga,  bg * Q[6], bg * Q[7], bg * Q[8],
+                              0.0, Q[0],      Q[1],      Q[2],
+                              0.0, Q[3],      Q[4],      Q[5],
+                              bg,  ga * Q[6], ga * Q[7], ga * Q[8]};
 #pragma unroll
-      for (int r = 0; r < 4; r++)
+        for (int r = 0; r < 4; r++)
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-          double acc = 0.0, accb = 0.0;
+          for (int c = 0; c < 4; c++) {
+            double acc = 0.0, accb = 0.0;
 #pragma unroll
-          for (int k = 0; k < 4; k++) {
-            if ((c == 0 && k == 2) || (c == 1 && k == 0) || (c == 2 && k == 0) || (c == 3 && k == 2))
+            for (int k = 0; k < 4; k++) {
+              if ((c == 1 || c == 2) && k == 0) continue;  // F's zeros
+              acc += L[4 * r + k] * (eta[k] * eta[c]) * F[4 * c + k];
+              accb += Lb[4 * r + k] * F[4 * c + k];
+            }
+            Lp[4 * r + c] = acc;
+            Lpb[4 * r + c] = accb;
+          }
+        double Fb[16];
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+          for (int c = 0; c < 4; c++) {
+            double acc = 0.0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) acc += Lp[4 * k + r] * Lb[4 * k + c];
+            Fb[4 * r + c] = acc;
+          }
+        gab = Fb[0] + Fb[13] * Q[6] + Fb[14] * Q[7] + Fb[15] * Q[8];
+        bgb = Fb[12] + Fb[1] * Q[6] + Fb[2] * Q[7] + Fb[3] * Q[8];
+        double Qb[9];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          Qb[c] = Fb[5 + c];
+          Qb[3 + c] = Fb[9 + c];
+          Qb[6 + c] = bg * Fb[1 + c] + ga * Fb[13 + c];
+        }
+        // Q = R_f A: Abar = R_f^T Qbar, R_f bar = Qbar A^T
+        const double A[9] = {ct * cphi, -sphi, st * cphi, ct * sphi, cphi, st * sphi, -st, 0.0, ct};
+        double Ab[9], Rb[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3; j++) {
+            Ab[3 * i + j] = Rf[i] * Qb[j] + Rf[3 + i] * Qb[3 + j] + Rf[6 + i] * Qb[6 + j];
+            Rb[3 * i + j] = Qb[3 * i] * A[3 * j] + Qb[3 * i + 1] * A[3 * j + 1] + Qb[3 * i + 2] * A[3 * j + 2];
+          }
+        ctb = Ab[0] * cphi + Ab[3] * sphi + Ab[8];
+        stb = Ab[2] * cphi + Ab[5] * sphi - Ab[6];
+        cpb = Ab[0] * ct + Ab[2] * st + Ab[4];
+        spb = -Ab[1] + Ab[3] * ct + Ab[5] * st;
+        // R_f(axis): axis bar = J^T R_f bar
+        double J[27];
+        rot_z_onto_jacobian(ax, ay, az, J);
+        double axb[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int i = 0; i < 9; i++)
+#pragma unroll
+          for (int k = 0; k < 3; k++) axb[k] += Rb[i] * J[3 * i + k];
+        // axis = (-(Lp01 - ff Lp31), -(Lp02 - ff Lp32), -bg u0 - gamma (Lp03 - ff Lp33)),
+        // u0 = Lp00 - ff Lp30
+        const double u0 = Lp[0] - ff * Lp[12];
+        Lpb[1] -= axb[0];
+        Lpb[13] += ff * axb[0];
+        Lpb[2] -= axb[1];
+        Lpb[14] += ff * axb[1];
+        Lpb[0] -= bg * axb[2];
+        Lpb[12] += ff * bg * axb[2];
+        Lpb[3] -= ga * axb[2];
+        Lpb[15] += ff * ga * axb[2];
+        bgb -= u0 * axb[2];
+        gab -= (Lp[3] - ff * Lp[15]) * axb[2];
+      } else {
+        // parent frame L_pre = L eta L1^T eta; adjoints L1bar = L_pre^T Lb, Lpre_bar = Lb L1^T.
+        // L1 has zeros at (0,2), (1,0), (2,0), (3,2), and only its other 12 entries carry
+        // adjoints; the loops skip the zero terms (the compiler folds the constant ones).
+        double L1b[16];
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+          for (int c = 0; c < 4; c++) {
+            double acc = 0.0, accb = 0.0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+              if ((c == 0 && k == 2) || (c == 1 && k == 0) || (c == 2 && k == 0) || (c == 3 && k == 2))
+                continue;
+              acc += L[4 * r + k] * (eta[k] * eta[c]) * L1[4 * c + k];
+              accb += Lb[4 * r + k] * L1[4 * c + k];
+            }
+            Lp[4 * r + c] = acc;
+            Lpb[4 * r + c] = accb;
+          }
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+          for (int c = 0; c < 4; c++) {
+            if ((r == 0 && c == 2) || (r == 1 && c == 0) || (r == 2 && c == 0) || (r == 3 && c == 2)) {
+              L1b[4 * r + c] = 0.0;
               continue;
-            acc += L[4 * r + k] * (eta[k] * eta[c]) * L1[4 * c + k];
-            accb += Lb[4 * r + k] * L1[4 * c + k];
+            }
+            double acc = 0.0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) acc += Lp[4 * k + r] * Lb[4 * k + c];
+            L1b[4 * r + c] = acc;
           }
-          Lp[4 * r + c] = acc;
-          Lpb[4 * r + c] = accb;
-        }
-#pragma unroll
-      for (int r = 0; r < 4; r++)
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-          if ((r == 0 && c == 2) || (r == 1 && c == 0) || (r == 2 && c == 0) || (r == 3 && c == 2)) {
-            L1b[4 * r + c] = 0.0;
-            continue;
-          }
-          double acc = 0.0;
-#pragma unroll
-          for (int k = 0; k < 4; k++) acc += Lp[4 * k + r] * Lb[4 * k + c];
-          L1b[4 * r + c] = acc;
-        }
-      const double gab = L1b[0] - L1b[13] * st + L1b[15] * ct;
-      const double bgb = -L1b[1] * st + L1b[3] * ct + L1b[12];
-      const double ctb = L1b[3] * bg + L1b[5] * cphi + L1b[9] * sphi + L1b[15] * ga;
-      const double stb = -L1b[1] * bg + L1b[7] * cphi + L1b[11] * sphi - L1b[13] * ga;
-      const double cpb = L1b[5] * ct + L1b[7] * st + L1b[10];
-      const double spb = -L1b[6] + L1b[9] * ct + L1b[11] * st;
+        gab = L1b[0] - L1b[13] * st + L1b[15] * ct;
+        bgb = -L1b[1] * st + L1b[3] * ct + L1b[12];
+        ctb = L1b[3] * bg + L1b[5] * cphi + L1b[9] * sphi + L1b[15] * ga;
+        stb = -L1b[1] * bg + L1b[7] * cphi + L1b[11] * sphi - L1b[13] * ga;
+        cpb = L1b[5] * ct + L1b[7] * st + L1b[10];
+        spb = -L1b[6] + L1b[9] * ct + L1b[11] * st;
+      }
       xb[V.x_phi] = 2.0 * PHS_PI * (-sphi * cpb + cphi * spb);
       xb[V.x_ct] = ctb * slot(sm, ab + 4) + stb * slot(sm, ab + 5) + jb * slot(sm, ab + 6);
       // bg = p rm, gamma = E rm
@@ -452,43 +633,51 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
 
 }  // namespace
 
-void phs_adjoint_sizes(int max_visits, int max_pops, int stack_depth, int *state0, int *ang0,
-                       int *der0, int *pop0, int *stack0, int *trig0, size_t *smem) {
+void phs_adjoint_sizes(int max_visits, int max_pops, int stack_depth, bool friends, int *state0,
+                       int *ang0, int *der0, int *pop0, int *stack0, int *trig0, int *fr0,
+                       size_t *smem) {
   *state0 = 0;
   *ang0 = PHS_ADJ_STATE * max_visits;
   *der0 = *ang0 + PHS_ADJ_ANG * max_visits;
   *pop0 = *der0 + PHS_ADJ_DER * max_visits;
   *stack0 = *pop0 + 16 * max_pops;
   *trig0 = *stack0 + PHS_STATE * (stack_depth > 0 ? stack_depth : 0);
-  const int slots = *trig0 + (int)(64 * sizeof(double2) / (PHS_ADJ_BLOCK * sizeof(double)));
+  *fr0 = *trig0 + (int)(64 * sizeof(double2) / (PHS_ADJ_BLOCK * sizeof(double)));
+  const int slots = *fr0 + (friends ? 3 * max_visits : 0);
   *smem = (size_t)slots * PHS_ADJ_BLOCK * sizeof(double);
 }
 
 cudaError_t phs_launch_adjoint(const PhsLaunch &a, const PhsAdjChannel *adj, const double *pbar,
                                const double *jbar, double *xbar, double *thbar, int th_stride,
-                               int max_visits, int max_pops, int n_blocks, cudaStream_t stream) {
+                               int max_visits, int max_pops, bool friends, int n_blocks,
+                               cudaStream_t stream) {
   if (a.n_tiles <= 0) return cudaSuccess;
   AdjLayout lay;
   size_t smem;
-  phs_adjoint_sizes(max_visits, max_pops, a.stack_depth, &lay.state0, &lay.ang0, &lay.der0,
-                    &lay.pop0, &lay.stack0, &lay.trig0, &smem);
+  phs_adjoint_sizes(max_visits, max_pops, a.stack_depth, friends, &lay.state0, &lay.ang0,
+                    &lay.der0, &lay.pop0, &lay.stack0, &lay.trig0, &lay.fr0, &smem);
+  const void *k = friends ? (const void *)phs_adjoint_kernel<true> : (const void *)phs_adjoint_kernel<false>;
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(phs_adjoint_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  phs_adjoint_kernel<<<n_blocks, PHS_ADJ_BLOCK, smem, stream>>>(a, adj, pbar, jbar, xbar, thbar,
-                                                                th_stride, lay);
+  if (friends)
+    phs_adjoint_kernel<true><<<n_blocks, PHS_ADJ_BLOCK, smem, stream>>>(a, adj, pbar, jbar, xbar,
+                                                                      thbar, th_stride, lay);
+  else
+    phs_adjoint_kernel<false><<<n_blocks, PHS_ADJ_BLOCK, smem, stream>>>(a, adj, pbar, jbar, xbar,
+                                                                       thbar, th_stride, lay);
   return cudaGetLastError();
 }
 
-int phs_adjoint_blocks_per_sm(int max_visits, int max_pops, int stack_depth) {
-  int s0, a0, d0, p0, k0, t0;
+int phs_adjoint_blocks_per_sm(int max_visits, int max_pops, int stack_depth, bool friends) {
+  int s0, a0, d0, p0, k0, t0, f0;
   size_t smem;
-  phs_adjoint_sizes(max_visits, max_pops, stack_depth, &s0, &a0, &d0, &p0, &k0, &t0, &smem);
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(phs_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  phs_adjoint_sizes(max_visits, max_pops, stack_depth, friends, &s0, &a0, &d0, &p0, &k0, &t0, &f0,
+                    &smem);
+  const void *k = friends ? (const void *)phs_adjoint_kernel<true> : (const void *)phs_adjoint_kernel<false>;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phs_adjoint_kernel, PHS_ADJ_BLOCK, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, PHS_ADJ_BLOCK, smem);
   return n > 0 ? n : 1;
 }

@@ -702,8 +702,6 @@ extern "C" int phs_adjoint_device(phs_process_t h, int64_t n_events, const int64
   if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
   if (n_events > 0 && (!x || !pbar || !xbar || !thbar))
     return fail(PHS_ERR_INVALID_ARG, "null data pointer");
-  if (h->has_friends)
-    return fail(PHS_ERR_UNSUPPORTED, "the adjoint does not cover friend (beam-axis) boosts");
   DeviceGuard g(h->device);
   int64_t one = n_events;
   int rc = build_segments(h->segs, counts ? counts : &one, h->p.n_channels, h->lay, 0, 0, 0, false);
@@ -715,12 +713,13 @@ extern "C" int phs_adjoint_device(phs_process_t h, int64_t n_events, const int64
   a.x = x;
   if ((rc = attach_segments(h->segs, a, (cudaStream_t)stream))) return rc;
   if (a.n_tiles == 0) return PHS_OK;
-  const int per_sm = phs_adjoint_blocks_per_sm(h->max_visits, h->max_pops, h->stack_depth);
+  const int per_sm =
+      phs_adjoint_blocks_per_sm(h->max_visits, h->max_pops, h->stack_depth, h->has_friends);
   const int64_t want = (a.n_tiles + PHS_ADJ_BLOCK_HOST / 32 - 1) / (PHS_ADJ_BLOCK_HOST / 32);
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sm_count(h->device) * per_sm));
   CUDA_TRY(phs_launch_adjoint(a, h->d_prog_adj.as<PhsAdjChannel>(), pbar, jbar, xbar, thbar,
-                              2 * std::max(1, h->p.n_out - 2), h->max_visits, h->max_pops, grid,
-                              (cudaStream_t)stream));
+                              2 * std::max(1, h->p.n_out - 2), h->max_visits, h->max_pops,
+                              h->has_friends, grid, (cudaStream_t)stream));
   return PHS_OK;
 }
 

@@ -128,10 +128,12 @@ cudaError_t phs_launch_forward_exact(const PhsLaunch &a, int n_blocks, cudaStrea
 // [event][th_stride] (d/dm, d/dGamma per Breit-Wigner branch, at 2 * its msq x index).
 cudaError_t phs_launch_adjoint(const PhsLaunch &a, const PhsAdjChannel *adj, const double *pbar,
                                const double *jbar, double *xbar, double *thbar, int th_stride,
-                               int max_visits, int max_pops, int n_blocks, cudaStream_t stream);
-int phs_adjoint_blocks_per_sm(int max_visits, int max_pops, int stack_depth);
-void phs_adjoint_sizes(int max_visits, int max_pops, int stack_depth, int *state0, int *ang0,
-                       int *der0, int *pop0, int *stack0, int *trig0, size_t *smem);
+                               int max_visits, int max_pops, bool friends, int n_blocks,
+                               cudaStream_t stream);
+int phs_adjoint_blocks_per_sm(int max_visits, int max_pops, int stack_depth, bool friends);
+void phs_adjoint_sizes(int max_visits, int max_pops, int stack_depth, bool friends, int *state0,
+                       int *ang0, int *der0, int *pop0, int *stack0, int *trig0, int *fr0,
+                       size_t *smem);
 #define PHS_ADJ_BLOCK_HOST 64
 
 // Inverse map (phs_inverse.cu): for every event and every channel, the x row and factor

@@ -144,7 +144,9 @@ int phs_generate_device_noalloc(phs_process_t proc, double E1, double E2, int64_
  *   thbar [n_events][n_out - 2][2]   the same for d/dm and d/dGamma of the Breit-Wigner
  *                                    branch whose msq x index is the middle index (0 else).
  * ok = 0 events get zeros.  The boost chain is recomputed backwards from the last frame;
- * no per-branch matrices are stored.  No counterpart in the reference (forward only). */
+ * no per-branch matrices are stored (friend visits keep their 3-vector rotation axis).  All
+ * trees the forward map takes, friend boosts included.  No counterpart in the reference
+ * (forward only). */
 int phs_adjoint_device(phs_process_t proc, int64_t n_events, const int64_t *channel_counts,
                        const double *x, const double *pbar, const double *jbar, double *xbar,
                        double *thbar, void *stream);

@@ -144,3 +144,43 @@ def test_autograd_binding(torch):
     assert torch.equal(x.grad, xbar)
     assert torch.allclose(theta.grad, thbar.sum(0).cpu())
     assert theta.grad[1, 0] != 0      # d/dm of the t branch
+
+
+@pytest.mark.parametrize("k", [0, 1, 2, 3])
+def test_adjoint_friend_channels_against_finite_differences(torch, k):
+    """Channels of Whizard's bwbw process whose decays are measured from a beam axis (friend
+    boosts; t-channel mappings and collinear angles too), one at a time, against FP64
+    central finite differences as above."""
+    from conftest import golden, load_process
+    from gpu_phs_gb300.api import PhaseSpace
+    z = golden("whizard_bwbw")
+    full = load_process(z)
+    friends = [c for c in range(full.n_channels) if np.any(full.friends[c] != 0)]
+    assert len(friends) >= 4
+    proc = full.subset([friends[4 * k]])
+    proc.sqrts = 1000.0
+    n, h = 4000, 1e-6
+    x = torch.from_numpy(uniform_x(700 + k, n, proc.n_x)).cuda()
+    ps = PhaseSpace(proc, 500.0, 500.0)
+    g = torch.Generator(device="cuda").manual_seed(10 + k)
+    pbar = torch.randn((n, proc.n_out, 4), generator=g, device="cuda", dtype=torch.float64)
+    jbar = torch.randn(n, generator=g, device="cuda", dtype=torch.float64)
+    xbar, _ = ps.vjp(x, pbar, jbar)
+    ev = ps.generate(x)
+    keep = ev.ok.bool().cpu().numpy() & (margins(ev.p.cpu().numpy(), proc) > 1e-4)
+    keep &= ((x > 2 * h) & (x < 1 - 2 * h)).all(dim=1).cpu().numpy()
+    fd = torch.zeros_like(x)
+    for i in range(proc.n_x):
+        xp, xm = x.clone(), x.clone()
+        xp[:, i] += h
+        xm[:, i] -= h
+        lp, okp = loss(torch, ps, xp, pbar, jbar)
+        lm, okm = loss(torch, ps, xm, pbar, jbar)
+        fd[:, i] = (lp - lm) / (2 * h)
+        keep &= (okp & okm).cpu().numpy()
+    a, b = xbar.cpu().numpy()[keep], fd.cpu().numpy()[keep]
+    scale = np.abs(b).max(axis=1, keepdims=True) + 1.0
+    rel = np.abs(a - b) / scale
+    assert keep.sum() > 0.3 * n
+    assert np.median(rel) < 1e-7, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])
+    assert np.quantile(rel, 0.99) < 1e-4, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])

@@ -238,15 +238,3 @@ def test_whizard_abi_all_channels(torch):
     assert np.all(np.abs(fac - g) <= 0.5e-7 + 2e-3 * np.abs(g))
     lib.c_whizard_reset_generator()
     lib.c_whizard_finalize_gpu_phs()
-
-
-def test_adjoint_rejects_friend_channels(torch):
-    from gpu_phs_gb300.api import PhaseSpace
-    z = golden("whizard_bwbw")
-    proc = load_process(z)
-    ps = PhaseSpace(proc, 500.0, 500.0)
-    x = torch.from_numpy(np.ascontiguousarray(z["x"])).cuda()
-    counts = counts_of(z["channel"], proc.n_channels)
-    pbar = torch.zeros((x.shape[0], proc.n_out, 4), dtype=torch.float64, device="cuda")
-    with pytest.raises(Exception, match="friend"):
-        ps.vjp(x, pbar, None, counts)
