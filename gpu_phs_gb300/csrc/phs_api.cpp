@@ -257,7 +257,20 @@ int launch_ff_tuned(int &variant, Segments &S, PhsLaunch a, int device, int dept
   a.exact_queue = S.exact_q.as<int32_t>();
   a.exact_tile = S.exact_t.as<int64_t>();
   const int exact_grid = sm_count(device) * 4;
-  return launch_tuned(variant, PHS_FF_VARIANTS, n_events, st, [&](int v) {
+  // per-event beams: the float-float one pass at either register budget (variants 0, 1;
+  // the pre-test needs uniform constants), or the FP64 compacting kernel (2, 3: FP64
+  // variants 1, 2), whose FP64 results meet this precision's bar too and which wins where
+  // few events pass
+  const bool per_event = a.E1 != nullptr;
+  return launch_tuned(variant, per_event ? 4 : PHS_FF_VARIANTS, n_events, st, [&](int v) {
+    if (per_event && v >= 2) {
+      const int f64v = v >= 4 ? 1 + (v & 1) : v - 1;
+      cudaError_t e = cudaMemsetAsync(a.work, 0, 2 * sizeof(unsigned long long), st);
+      if (e == cudaSuccess)
+        e = phs_launch_forward_f64(a, grid_for(a.n_tiles, device, depth, true, f64v), f64v, st);
+      return e;
+    }
+    if (per_event) v &= 1;
     cudaError_t e = cudaMemsetAsync(a.exact_count, 0, (size_t)a.n_segments * sizeof(unsigned int), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(a.work, 0, 2 * sizeof(unsigned long long), st);
     if (e == cudaSuccess && v >= 4)
@@ -310,7 +323,7 @@ struct phs_process {
   bool beams = false;
   double E1 = 0, E2 = 0;
   int precision = PHS_PRECISION_F64;
-  int ff_variant = -1;  // autotuned FP32-pair kernel variant (-1: not tuned yet)
+  int ff_variant_ev[2] = {-1, -1};  // autotuned FP32-pair variant: uniform, per-event beams
   int f64_variant[2] = {-1, -1};  // autotuned FP64 variant: uniform, per-event beams
   std::vector<PhsChannel> prog;
   std::vector<PhsChannelFF> prog_ff;
@@ -562,7 +575,7 @@ extern "C" int phs_process_set_precision(phs_process_t h, int precision) {
 
 extern "C" int phs_process_tuning(phs_process_t h, int *ff_variant, int *f64_variant) {
   if (int rc = check_proc(h)) return rc;
-  if (ff_variant) *ff_variant = h->ff_variant;
+  if (ff_variant) *ff_variant = h->ff_variant_ev[0];
   if (f64_variant) *f64_variant = h->f64_variant[0];
   return PHS_OK;
 }
@@ -580,7 +593,7 @@ static int check_variants(int ff_variant, int f64_variant) {
 extern "C" int phs_process_set_variants(phs_process_t h, int ff_variant, int f64_variant) {
   if (int rc = check_proc(h)) return rc;
   if (int rc = check_variants(ff_variant, f64_variant)) return rc;
-  h->ff_variant = ff_variant;
+  h->ff_variant_ev[0] = h->ff_variant_ev[1] = ff_variant;
   h->f64_variant[0] = h->f64_variant[1] = f64_variant;
   return PHS_OK;
 }
@@ -648,8 +661,9 @@ static int launch_process(phs_process_t h, Segments &S, int64_t n_events, const 
   for (auto &g : S.host) g.ev_begin -= ev0;
   if ((rc = attach_segments(S, a, stream))) return rc;
   if (a.n_tiles == 0) return PHS_OK;
-  if (h->precision == PHS_PRECISION_F32X2 && E1 == nullptr)
-    return launch_ff_tuned(h->ff_variant, S, a, h->device, h->stack_depth, n_events, stream);
+  if (h->precision == PHS_PRECISION_F32X2)
+    return launch_ff_tuned(h->ff_variant_ev[E1 != nullptr], S, a, h->device, h->stack_depth,
+                           n_events, stream);
   return launch_f64_tuned(h->f64_variant[E1 != nullptr], S, a, h->device, h->stack_depth, n_events,
                           stream);
 }

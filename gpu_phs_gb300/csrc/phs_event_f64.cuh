@@ -148,6 +148,20 @@ __device__ __forceinline__ void rot_z_onto(double bx, double by, double bz, doub
   R[6] = -bx; R[7] = -by; R[8] = bz;
 }
 
+// The channel's phase-space volume at sqrt(s) (phs_cpu.cpp:194-213), bottom-up in post-order
+// with the reference's operation order: for the per-event-beam paths.
+__device__ __forceinline__ double channel_volume(const PhsChannel &ch, double sqrts) {
+  double vol[PHS_MAX_VISITS];
+  const double c_int = 4 * PHS_TWOPI2, c_root = 4 * PHS_TWOPI5;
+  for (int i = 0; i < ch.n_vol; i++) {
+    int k1 = ch.vol_child[i][0], k2 = ch.vol_child[i][1];
+    double v1 = k1 >= 0 ? vol[k1] : 1.0, v2 = k2 >= 0 ? vol[k2] : 1.0;
+    vol[i] = ch.vol_is_root[i] ? dmul(v1, v2) / c_root
+                               : dmul(dmul(dmul(v1, v2), sqrts), sqrts) / c_int;
+  }
+  return vol[ch.n_vol - 1];
+}
+
 // Mapping constants at one sqrt(s) (phs_cpu.cpp:452-531), for the per-event-beam path.
 __device__ void child_constants(const PhsChild &C, double sqrts, double m_tot, double &a0,
                                 double &a1, double &a2, double &msq_min, double &msq_max,
@@ -436,20 +450,7 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
     }
   }
 
-  double volume = ch.volume;
-  if (PER_EVENT) {
-    // phs_cpu.cpp:194-213, bottom-up in post-order with the reference's operation order
-    double vol[PHS_MAX_VISITS];
-    const double c_int = 4 * PHS_TWOPI2, c_root = 4 * PHS_TWOPI5;
-    for (int i = 0; i < ch.n_vol; i++) {
-      int k1 = ch.vol_child[i][0], k2 = ch.vol_child[i][1];
-      double v1 = k1 >= 0 ? vol[k1] : 1.0, v2 = k2 >= 0 ? vol[k2] : 1.0;
-      vol[i] = ch.vol_is_root[i] ? dmul(v1, v2) / c_root
-                                 : dmul(dmul(dmul(v1, v2), sqrts), sqrts) / c_int;
-    }
-    volume = vol[ch.n_vol - 1];
-  }
-  a.volume[ev] = volume;
+  a.volume[ev] = PER_EVENT ? channel_volume(ch, sqrts) : ch.volume;
   a.factor[ev * a.factor_stride + seg.factor_col] = ok ? factor : 0.0;
   a.ok[ev] = ok ? 1 : 0;
   if (!ok) {

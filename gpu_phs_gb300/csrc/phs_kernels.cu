@@ -71,6 +71,7 @@ __global__ void __launch_bounds__(BLOCK, MIN_BLOCKS)
 // of the FP32-pair kernel keeps that kernel's body small.  Warps claim 32 events of one
 // segment (a.exact_work counts the claims), so each runs one channel's program; the counts
 // are read on the device, so the launch can sit in a CUDA graph behind the FP32-pair one.
+template <bool PER_EVENT>
 __global__ void __launch_bounds__(PHS_FWD_BLOCK, 4)
     phs_forward_exact_kernel(const __grid_constant__ PhsLaunch a) {
   extern __shared__ double smem[];
@@ -93,7 +94,7 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, 4)
     const PhsSegment seg = segs[lo];
     const int64_t idx = (t - a.exact_tile[lo]) * 32 + lane;
     if (idx >= (int64_t)a.exact_count[lo]) continue;
-    phs_event_f64<false>(a, seg, a.exact_queue[seg.tile_begin * 32 + idx], smem, trig);
+    phs_event_f64<PER_EVENT>(a, seg, a.exact_queue[seg.tile_begin * 32 + idx], smem, trig);
   }
 }
 
@@ -329,8 +330,11 @@ cudaError_t phs_launch_forward_exact(const PhsLaunch &a, int n_blocks, cudaStrea
   if (a.n_tiles <= 0) return cudaSuccess;
   cudaError_t e = phs_launch_count_scan(a.exact_count, a.exact_tile, a.n_segments, stream);
   if (e != cudaSuccess) return e;
-  phs_forward_exact_kernel<<<n_blocks, PHS_FWD_BLOCK,
-                             phs_forward_smem_bytes(a.stack_depth, PHS_FWD_BLOCK), stream>>>(a);
+  const size_t smem = phs_forward_smem_bytes(a.stack_depth, PHS_FWD_BLOCK);
+  if (a.E1 && a.E2)
+    phs_forward_exact_kernel<true><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+  else
+    phs_forward_exact_kernel<false><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
   return cudaGetLastError();
 }
 

@@ -50,33 +50,62 @@ __device__ __forceinline__ bool msq_near_zero(ff v, float s) {
   return fabsf(v.hi) <= PHS_FF_MSQ_ZERO * s;
 }
 
+// The constants of an internal child that depend on sqrt(s): the mapping's a1 (Breit-Wigner:
+// a1 - a0) and a2, pi/2 - a1, msq_max and the ok test's m_max.  From the channel program for
+// uniform beams; per event from the FP64 constants (child_constants, as the reference's GPU
+// path computes them) for per-event beams.
+struct ChildVar {
+  ff a1, a2, u1, msq_max, m_max;
+};
+__device__ __forceinline__ ChildVar child_var(const PhsChildFF &C) {
+  return {ld(C.a1), ld(C.a2), ld(C.u1), ld(C.msq_max), ld(C.m_max)};
+}
+__device__ __forceinline__ ChildVar child_var(const PhsChildFF &C, const PhsChild &C64,
+                                              double sqrts, double m_tot) {
+  double a0, a1, a2, mn, mx, mmax;
+  child_constants(C64, sqrts, m_tot, a0, a1, a2, mn, mx, mmax);
+  ChildVar r;
+  r.a2 = ff_from_double(a2);
+  r.msq_max = ff_from_double(mx);
+  r.m_max = ff_from_double(mmax);
+  if (C.map_id == PHS_MAP_SCHANNEL) {
+    r.a1 = ff_from_double(a1 - a0);
+    // pi/2 - a1: exact for a1 >= pi/4 (the only case that uses it), then pi/2's low part
+    r.u1 = ff_from_double((1.5707963267948966 - a1) + 6.123233995736766e-17);
+  } else {
+    r.a1 = ff_from_double(a1);
+    r.u1 = ff_from_float(0.0f);
+  }
+  return r;
+}
+
 // msq from x in float-float; returns false when the event must take the exact path.
 // x arrives as a float-float pair truncated from the double, so x < 0.5 is decided on its
 // high part exactly as the reference decides it on the double.
-__device__ __forceinline__ bool map_msq_ff(const PhsChildFF &C, double xd, const FFTables &T,
-                                           ff &msq, ff &f) {
+__device__ __forceinline__ bool map_msq_ff(const PhsChildFF &C, const ChildVar &cv, double xd,
+                                           const FFTables &T, ff &msq, ff &f) {
   const ff x = ff_from_double_int(xd);
   switch (C.map_id) {
     case PHS_MAP_NO:
-      msq = ff_add(ld(C.msq_min), ff_mul(x, ff_sub(ld(C.msq_max), ld(C.msq_min))));
-      f = ld(C.a2);
+      msq = ff_add(ld(C.msq_min), ff_mul(x, ff_sub(cv.msq_max, ld(C.msq_min))));
+      f = cv.a2;
       return true;
     case PHS_MAP_SCHANNEL: {
       // z = (1-x) a0 + x a1; next to +-pi/2, tan z = -+cot(pi/2 -+ z) with pi/2 -+ z formed
       // from the host's pi/2 - a1 and pi/2 + a0, so its relative accuracy holds there.
       // Lanes of a warp fall on different sides: the argument and the quotient are
       // selected, and every lane runs one sincos and one division.
-      ff z = ff_add(ld(C.a0), ff_mul(x, ld(C.a1)));   // a1 holds a1 - a0
+      ff z = ff_add(ld(C.a0), ff_mul(x, cv.a1));   // a1 holds a1 - a0
       if (!(fabsf(z.hi) < 1.5707962f)) return false;   // the reference's |z| < pi/2 test
       const bool hs = z.hi > 0.78539816f, ls = z.hi < -0.78539816f, cot = hs || ls;
       ff w = z;
-      if (cot) w = ff_add(hs ? ld(C.u1) : ld(C.u0), ff_mul(hs ? ff_one_minus_double_int(xd) : x, ld(C.a1)));
+      if (cot) w = ff_add(hs ? cv.u1 : ld(C.u0), ff_mul(hs ? ff_one_minus_double_int(xd) : x, cv.a1));
       ff sw, cw;
       ff_sincos(w, T, sw, cw);
       ff t = ff_div_fast(cot ? cw : sw, cot ? sw : cw);
       if (ls) t = ff_neg(t);
       msq = ff_add(ld(C.m2), ff_mul(ld(C.mw), t));
-      f = ff_mul(ld(C.a2), ff_add_f(ff_sqr(t), 1.0f));
+      f = ff_mul(cv.a2, ff_add_f(ff_sqr(t), 1.0f));
       return true;
     }
     case PHS_MAP_COLLINEAR:
@@ -87,10 +116,10 @@ __device__ __forceinline__ bool map_msq_ff(const PhsChildFF &C, double xd, const
       // one exponential for all five: the t/u-channel maps take x >= 0.5 from the other
       // end, with the argument and the sum selected per lane
       const bool upper = (C.map_id == PHS_MAP_TCHANNEL || C.map_id == PHS_MAP_UCHANNEL) && !(x.hi < 0.5f);
-      const ff msq1 = ff_mul(ld(C.a0), ff_exp(ff_mul(upper ? ff_one_minus_double_int(xd) : x, ld(C.a1)), T));
-      msq = upper ? ff_add(ff_sub(ld(C.a0), msq1), ld(C.msq_max))
+      const ff msq1 = ff_mul(ld(C.a0), ff_exp(ff_mul(upper ? ff_one_minus_double_int(xd) : x, cv.a1), T));
+      msq = upper ? ff_add(ff_sub(ld(C.a0), msq1), cv.msq_max)
                   : ff_add(ff_sub(msq1, ld(C.a0)), ld(C.msq_min));
-      f = ff_mul(ld(C.a2), msq1);
+      f = ff_mul(cv.a2, msq1);
       return true;
     }
   }
@@ -102,7 +131,10 @@ __device__ __forceinline__ ff ff_twice(ff a) { return ff_make(f_add(a.hi, a.hi),
 __device__ __forceinline__ ff ff_half(ff a) { return ff_make(f_mul(a.hi, 0.5f), f_mul(a.lo, 0.5f)); }
 
 // One event in float-float.  Returns false if it must be recomputed on the exact path
-// (outputs written so far are then overwritten).
+// (outputs written so far are then overwritten).  PER_EVENT: beam energies a.E1/a.E2 per
+// event; the constants that depend on sqrt(s) come from FP64 per event (as the FP64 path
+// computes them) and the walk stays in float-float.
+template <bool PER_EVENT = false>
 __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegment &seg,
                                              int64_t local, const FFTables &T, float *fst) {
   const PhsChannelFF &ch = a.channels_ff[seg.channel];
@@ -111,20 +143,35 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
   const double *xe = a.x + seg.x_base + local * seg.x_stride;
   double *out = a.p + seg.p_base + local * 4 * (int64_t)ch.n_out;
   const ff zero = ff_from_float(0.0f), one = ff_from_float(1.0f);
-  const float s_scale = ch.s.hi;
+
+  // beams: the channel's, or this event's (phs_event_f64's expressions)
+  ff sqrts_f = ld(ch.sqrts), s_f = ld(ch.s), lab_bg = ld(ch.lab_bg), lab_ga = ld(ch.lab_gamma);
+  bool lab = ch.lab != 0;
+  double sqrts64 = 0.0, s64 = 0.0;
+  if (PER_EVENT) {
+    const double E1 = a.E1[ev], E2 = a.E2[ev], r = sqrt(dmul(E1, E2));
+    sqrts64 = dmul(2.0, r);
+    s64 = dmul(sqrts64, sqrts64);
+    const double bg = dsub(E1, E2) / dmul(2.0, r);
+    lab = E1 != E2;
+    sqrts_f = ff_from_double(sqrts64);
+    s_f = ff_from_double(s64);
+    lab_bg = ff_from_double(bg);
+    lab_ga = ff_from_double(sqrt(1.0 + bg * bg));
+  }
+  const float s_scale = s_f.hi;
 
   // the frame of the visited branch, updated in place row by row
   ff L[16];
 #pragma unroll
   for (int i = 0; i < 16; i++) L[i] = zero;
-  const bool lab = ch.lab != 0;
-  L[0] = lab ? ld(ch.lab_gamma) : one;
+  L[0] = lab ? lab_ga : one;
   L[5] = one;
   L[10] = one;
   L[15] = L[0];
-  L[3] = lab ? ld(ch.lab_bg) : zero;
+  L[3] = lab ? lab_bg : zero;
   L[12] = L[3];
-  ff msq_b = ld(ch.s), m_b = ld(ch.sqrts), p_b = zero, mmax_b = ld(ch.sqrts);
+  ff msq_b = s_f, m_b = sqrts_f, p_b = zero, mmax_b = sqrts_f;
   ff factor = one;
   bool ok = true;
   int sp = 0;
@@ -142,7 +189,10 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
         cmax[j] = zero;
       } else {
         ff f;
-        if (!map_msq_ff(C, xe[C.x_msq], T, cmsq[j], f)) return false;
+        const ChildVar cv = PER_EVENT
+            ? child_var(C, a.channels[seg.channel].visit[v].child[j], sqrts64, a.channels[seg.channel].m_tot)
+            : child_var(C);
+        if (!map_msq_ff(C, cv, xe[C.x_msq], T, cmsq[j], f)) return false;
         factor = ff_mul(factor, f);
         if (msq_near_zero(cmsq[j], s_scale)) return false;
         if (cmsq[j].hi < 0.0f) {  // the reference takes sqrt of a negative: not ok
@@ -150,7 +200,7 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
           cmsq[j] = zero;
         }
         cm[j] = ff_sqrt_fast(cmsq[j]);
-        cmax[j] = ld(C.m_max);
+        cmax[j] = cv.m_max;
       }
     }
     // kinematic test at the visited branch, decided here only away from its limits
@@ -183,7 +233,13 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
     const ff xct = ff_from_double_int(xctd);
     ff ct, st, fct;
     if (V.ct_class == PHS_CT_COLLINEAR) {
-      const ff b0 = ld(V.b0), b1 = ld(V.b1);
+      ff b0 = ld(V.b0), b1 = ld(V.b1);
+      if (PER_EVENT) {
+        const double m = a.channels[seg.channel].visit[v].m;
+        const double b0d = dmul(m, m) / s64;
+        b0 = ff_from_double(b0d);
+        b1 = ff_from_double(log(dadd(b0d, 1.0) / b0d));
+      }
       const bool lower = xct.hi < 0.5f;
       const ff tmp = ff_mul(b0, ff_exp(ff_mul(ff_twice(lower ? xct : ff_one_minus_double_int(xctd)), b1), T));
       ct = lower ? ff_add_f(ff_sub(tmp, b0), -1.0f) : ff_add_f(ff_sub(b0, tmp), 1.0f);
@@ -270,7 +326,7 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
     }
   }
 
-  a.volume[ev] = ch.volume;
+  a.volume[ev] = PER_EVENT ? channel_volume(a.channels[seg.channel], sqrts64) : ch.volume;
   a.factor[ev * a.factor_stride + seg.factor_col] = ok ? ff_to_double(factor) : 0.0;
   a.ok[ev] = ok ? 1 : 0;
   if (!ok) {
@@ -494,9 +550,10 @@ __device__ __forceinline__ void write_failed_tile(const PhsLaunch &a, const PhsS
 // MIN_BLOCKS: resident blocks per SM the register allocation targets; COMPACT: the
 // two-pass form of phs_kernels.cu (pass A, here in FP32, settles the events that clearly
 // fail; pass B computes the rest densely).  The autotuner in phs_api.cpp picks the faster instantiation per process.
-template <int MIN_BLOCKS, bool COMPACT>
+template <int MIN_BLOCKS, bool COMPACT, bool PER_EVENT = false>
 __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
     phs_forward_ff_kernel(const __grid_constant__ PhsLaunch a) {
+  static_assert(!(COMPACT && PER_EVENT), "the FP32 pre-test needs uniform beams");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FFTables &T = *reinterpret_cast<FFTables *>(smem_raw);
   // the float-float frame stack and the FP64 one share memory (fstack_store): a thread
@@ -537,7 +594,7 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
       const PhsSegment seg = segs[lo];
       const int64_t local = (tile - seg.tile_begin) * 32 + lane;
       if (local >= seg.ev_count) continue;
-      if (!phs_event_ff(a, seg, local, T, fst)) to_exact(lo, local);
+      if (!phs_event_ff<PER_EVENT>(a, seg, local, T, fst)) to_exact(lo, local);
     }
   }
 }
@@ -709,6 +766,17 @@ int phs_forward_ff_blocks_per_sm(int stack_depth, int variant) {
 
 cudaError_t phs_launch_forward_ff(const PhsLaunch &a, int n_blocks, int variant, cudaStream_t stream) {
   if (a.n_tiles <= 0) return cudaSuccess;
+  if (a.E1 || a.E2) {
+    // per-event beams: the one-pass walk (the pre-test needs uniform constants); bit 0 of
+    // the variant picks the register budget
+    if (!a.E1 || !a.E2) return cudaErrorInvalidValue;
+    const size_t smem = phs_forward_ff_smem_bytes(a.stack_depth);
+    if (variant & 1)
+      phs_forward_ff_kernel<4, false, true><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+    else
+      phs_forward_ff_kernel<3, false, true><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
+    return cudaGetLastError();
+  }
   if (variant >= 4) {
     cudaError_t e = phs_launch_pretest(a, stream);
     if (e != cudaSuccess) return e;

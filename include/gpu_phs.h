@@ -85,8 +85,11 @@ int phs_process_destroy(phs_process_t proc);
 int phs_process_set_beams(phs_process_t proc, double E1, double E2);
 
 /* Arithmetic of the uniform-beam generate calls (phs_generate_device/_host and batches built
- * afterwards keep their own setting): PHS_PRECISION_F64 or PHS_PRECISION_F32X2.  Per-event
- * beams always use FP64.  No counterpart in the reference (FP64 only). */
+ * afterwards keep their own setting): PHS_PRECISION_F64 or PHS_PRECISION_F32X2.  With
+ * per-event beams (phs_generate_beams_device) F32X2 evaluates the constants that depend on
+ * sqrt(s) per event in FP64 and walks in float-float, or runs the FP64 compacting kernel
+ * where the autotuner finds that faster (few events passing).  No counterpart in the
+ * reference (FP64 only). */
 int phs_process_set_precision(phs_process_t proc, int precision);
 
 /* The autotuned kernel variants of the handle's uniform-beam launches, or -1 before the

@@ -177,3 +177,72 @@ def test_ff_matches_f64_kernel_tt_full_size(torch):
     ferr = ((eb.factor[sel] - ea.factor[sel]).abs() / ea.factor[sel].abs()).max().item()
     assert ferr < 1e-7, ferr
     assert torch.equal(ea.volume, eb.volume)
+
+
+@pytest.mark.parametrize("beams", ["asymmetric", "random"])
+@pytest.mark.parametrize("builder", [P.tt, P.precision])
+def test_ff_per_event_beams(torch, builder, beams):
+    """Per-event beam energies in FP32-pair arithmetic: the constants that depend on sqrt(s)
+    per event in FP64, the walk in float-float; against the oracle at the same bar."""
+    from gpu_phs_gb300.api import PhaseSpace
+    proc = builder()
+    n = 50_000
+    sq = proc.sqrts
+    x = uniform_x(13, n, proc.n_x)
+    rng = np.random.default_rng(3)
+    if beams == "asymmetric":
+        E1, E2 = np.full(n, 0.6 * sq), np.full(n, 0.42 * sq)
+    else:
+        E1, E2 = rng.uniform(0.3, 0.7, n) * sq, rng.uniform(0.3, 0.7, n) * sq
+    r = oracle.Oracle(proc, sq).generate(x, E1=E1, E2=E2)
+    ps = PhaseSpace(proc)
+    ps.set_precision(1)
+    ev = ps.generate_beams(torch.from_numpy(x).cuda(), torch.from_numpy(E1).cuda(),
+                           torch.from_numpy(E2).cuda())
+    torch.cuda.synchronize()
+    got = (ev.p.cpu().numpy(), ev.factor.cpu().numpy(), ev.volume.cpu().numpy(), ev.ok.cpu().numpy())
+    check(got, r.p, r.factor, r.volume, r.ok, sq)
+
+
+def test_ff_per_event_beams_exact_path(torch):
+    """bwbw's 61 channels with per-event beams in FP32-pair arithmetic: its 16 friend
+    channels and the events near kinematic limits go through the exact path per event."""
+    from gpu_phs_gb300.api import PhaseSpace
+    z = golden("whizard_bwbw")
+    proc = load_process(z)
+    x = np.ascontiguousarray(z["x"])
+    n = x.shape[0]
+    rng = np.random.default_rng(8)
+    E1, E2 = rng.uniform(350, 650, n), rng.uniform(350, 650, n)
+    counts = counts_of(z["channel"], proc.n_channels)
+    r = oracle.Oracle(proc, 1000.0).generate(x, z["channel"], E1=E1, E2=E2)
+    ps = PhaseSpace(proc)
+    ps.set_precision(1)
+    ev = ps.generate_beams(torch.from_numpy(x).cuda(), torch.from_numpy(E1).cuda(),
+                           torch.from_numpy(E2).cuda(), counts)
+    torch.cuda.synchronize()
+    got = (ev.p.cpu().numpy(), ev.factor.cpu().numpy(), ev.volume.cpu().numpy(), ev.ok.cpu().numpy())
+    check(got, r.p, r.factor, r.volume, r.ok, 1000.0)
+
+
+def test_ff_per_event_beams_fp64_candidates(torch):
+    """With per-event beams the FP32-pair autotuner may pick the FP64 compacting kernel
+    (variants 2 and 3 there): pinned, it gives the FP64 path's bits."""
+    from gpu_phs_gb300.api import PhaseSpace, philox_x
+    proc = P.precision()
+    n = 100_000
+    x = philox_x(n, proc.n_x, seed=21)
+    g = torch.Generator(device="cuda").manual_seed(6)
+    E1 = proc.sqrts * (0.3 + 0.4 * torch.rand(n, generator=g, device="cuda", dtype=torch.float64))
+    E2 = proc.sqrts * (0.3 + 0.4 * torch.rand(n, generator=g, device="cuda", dtype=torch.float64))
+    ref = PhaseSpace(proc)
+    ref.set_variants(-1, 0)
+    r = ref.generate_beams(x, E1, E2)
+    for v in (2, 3):
+        ps = PhaseSpace(proc)
+        ps.set_precision(1)
+        ps.set_variants(v, -1)
+        ev = ps.generate_beams(x, E1, E2)
+        torch.cuda.synchronize()
+        for a, b in ((r.p, ev.p), (r.factor, ev.factor), (r.volume, ev.volume), (r.ok, ev.ok)):
+            assert torch.equal(a, b)
