@@ -199,6 +199,25 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64, pin=
                             "error_vs_fp64": _errors(torch, out_tt, o, proc.sqrts)}
     del o
 
+    # per-event beam energies on the same tt x (E1, E2 uniform in [0.3, 0.7] sqrt(s)): FP64
+    # and FP32 pairs (constants per event in FP64, the walk in float-float)
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    E1 = proc.sqrts * (0.3 + 0.4 * torch.rand(n, generator=g, device="cuda", dtype=torch.float64))
+    E2 = proc.sqrts * (0.3 + 0.4 * torch.rand(n, generator=g, device="cuda", dtype=torch.float64))
+    pe = {}
+    for prec in (0, 1):
+        ps = PhaseSpace(proc)
+        ps.set_precision(prec)
+        o = ps.alloc(n)
+        pe[prec] = (_time_calls(torch, lambda: ps.generate_beams(x_tt, E1, E2, out=o), steps,
+                                warmup, stream), o)
+    res["per_event_beams_tt"] = {
+        "n_events": n, "beams": "E1, E2 uniform in [0.3, 0.7] sqrt(s) per event",
+        "fp64_events_per_s": n / pe[0][0] * 1e3, "fp32_mixed_events_per_s": n / pe[1][0] * 1e3,
+        "speedup": pe[0][0] / pe[1][0],
+        "error_vs_fp64": _errors(torch, pe[0][1], pe[1][1], proc.sqrts)}
+    del pe, E1, E2
+
     # Four forms per workload, three of them FP64 with identical output bits: the plain FP64
     # kernel (one pass: every event walked in full), FP64 compacting (an FP64 pass tests
     # every event first, only those that pass are walked), FP64 split (an FP32 pre-test with
