@@ -278,10 +278,11 @@ int phs_forward_blocks_per_sm(int stack_depth, bool per_event, int variant) {
 }
 
 template <bool PER_EVENT>
-static void launch_f64(const PhsLaunch &a, int n_blocks, int variant, cudaStream_t stream) {
+static cudaError_t launch_f64(const PhsLaunch &a, int n_blocks, int variant, cudaStream_t stream) {
   const int block = f64_block(variant);
   const size_t smem = phs_forward_smem_bytes(a.stack_depth, block);
-  if (allow_smem(f64_kernel<PER_EVENT>(variant), smem) != cudaSuccess) return;
+  const cudaError_t e = allow_smem(f64_kernel<PER_EVENT>(variant), smem);
+  if (e != cudaSuccess) return e;
   switch (variant) {
     case 1:
       phs_forward_f64_kernel<PER_EVENT, true, 4><<<n_blocks, block, smem, stream>>>(a);
@@ -298,6 +299,7 @@ static void launch_f64(const PhsLaunch &a, int n_blocks, int variant, cudaStream
     default:
       phs_forward_f64_kernel<PER_EVENT, false, 4><<<n_blocks, block, smem, stream>>>(a);
   }
+  return cudaGetLastError();
 }
 
 cudaError_t phs_launch_forward_f64(const PhsLaunch &a, int n_blocks, int variant,
@@ -319,11 +321,8 @@ cudaError_t phs_launch_forward_f64(const PhsLaunch &a, int n_blocks, int variant
     }
     return cudaGetLastError();
   }
-  if (a.E1 && a.E2)
-    launch_f64<true>(a, n_blocks, variant, stream);
-  else
-    launch_f64<false>(a, n_blocks, variant, stream);
-  return cudaGetLastError();
+  return a.E1 && a.E2 ? launch_f64<true>(a, n_blocks, variant, stream)
+                      : launch_f64<false>(a, n_blocks, variant, stream);
 }
 
 cudaError_t phs_launch_forward_exact(const PhsLaunch &a, int n_blocks, cudaStream_t stream) {
