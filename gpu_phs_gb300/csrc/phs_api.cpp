@@ -791,12 +791,15 @@ extern "C" int phs_inverse_device(phs_process_t h, int64_t n_events, const int64
   a.max_visits = h->max_visits;
   a.group_order = h->d_inv_groups.as<int32_t>();
   a.group_begin = a.group_order + nch;
-  a.group_reuse = reinterpret_cast<const uint64_t *>(
-      static_cast<const char *>(h->d_inv_groups.ptr) + h->inv_reuse_offset);
+  const bool cache = phs_inverse_fits_cache(a.n_out, a.stack_depth, a.max_visits);
+  a.group_reuse = cache ? reinterpret_cast<const uint64_t *>(
+                              static_cast<const char *>(h->d_inv_groups.ptr) + h->inv_reuse_offset)
+                        : nullptr;
   a.n_groups = h->n_inv_groups;
   const int64_t tiles = (n_events + PHS_INV_BLOCK - 1) / PHS_INV_BLOCK;
   const int64_t cap = (int64_t)sm_count(h->device) *
-                      phs_inverse_blocks_per_sm(a.n_out, a.stack_depth, a.max_visits, E1 != nullptr);
+                      phs_inverse_blocks_per_sm(a.n_out, a.stack_depth, a.max_visits,
+                                                E1 != nullptr, cache);
   CUDA_TRY(phs_launch_inverse(a, (int)std::max<int64_t>(1, std::min(tiles, cap)), st));
   return PHS_OK;
 }

@@ -154,14 +154,19 @@ struct PhsInvLaunch {
   const int32_t *group_order;
   const int32_t *group_begin;
   const uint64_t *group_reuse;  // [n_channels] by group_order position: mappings equal to the
-                                // previous channel's (bit 3 visit + 0/1 daughter msq, + 2 ct)
+                                // previous channel's (bit 3 visit + 0/1 daughter msq, + 2 ct);
+                                // null: no reuse (and no shared memory for it)
   int32_t n_groups;
   int64_t n_events;
   int32_t n_channels, n_out, n_x, stack_depth, max_visits;
 };
 cudaError_t phs_launch_inverse(const PhsInvLaunch &a, int n_blocks, cudaStream_t stream);
-int phs_inverse_blocks_per_sm(int n_out, int stack_depth, int max_visits, bool per_event);
-size_t phs_inverse_smem_bytes(int n_out, int stack_depth, int max_visits);
+// cache: the per-visit mapping results that channels of a shape reuse (a.group_reuse set);
+// phs_inverse_fits_cache tells whether the block's shared memory holds them.
+int phs_inverse_blocks_per_sm(int n_out, int stack_depth, int max_visits, bool per_event,
+                              bool cache);
+size_t phs_inverse_smem_bytes(int n_out, int stack_depth, int max_visits, bool cache);
+bool phs_inverse_fits_cache(int n_out, int stack_depth, int max_visits);
 
 // Per-channel x grid of the warm-up (phs_grid.cu): weights [n_channels][n_x][PHS_GRID_BINS].
 #define PHS_GRID_BINS 10

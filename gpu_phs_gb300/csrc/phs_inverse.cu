@@ -31,10 +31,12 @@
 
 #define PHS_INV_STATE 23  // doubles per saved frame: G[16], ct, st, cos phi, sin phi, msq, p_decay, m
 // per visit, from the geometry walk to the mapping pass: msq of both daughters, cos(theta)
-// and x_phi of daughter 1, sqrt(lambda) / msq of the visited branch (slots 0-4); then the
-// last mapping results (x, f) of daughter 0, daughter 1 and cos(theta) (slots 5-10), which
-// the next channel of the shape reuses where its mapping is the same
-#define PHS_INV_GEO 11
+// and x_phi of daughter 1, sqrt(lambda) / msq of the visited branch
+#define PHS_INV_GEO 5
+// per visit, the last mapping results (x, f) of daughter 0, daughter 1 and cos(theta), which
+// the next channel of the shape reuses where its mapping is the same (left out when the
+// block's shared memory would not hold it: the largest trees)
+#define PHS_INV_CACHE 6
 
 namespace {
 
@@ -261,11 +263,12 @@ __device__ void inverse_geometry(const PhsChannel &ch, double *pm, double sqrts,
 // The mappings of one (event, channel) after inverse_geometry of its shape: writes the
 // channel's x entries of xr and returns its factor, in the reference's order of factors.
 // Bit 3 v + k of reuse (k = 0, 1: the daughters' msq maps, 2: the cos(theta) map): the
-// previous channel of the shape had the same mapping there, so its (x, f) is taken as is.
-// xr null: the mappings run (the next channel may reuse them) but write nothing.
+// previous channel of the shape had the same mapping there, so its (x, f) is taken from
+// cache (null: no cache, reuse 0).  xr null: the mappings run (the next channel may reuse
+// them) but write nothing.
 template <bool PER_EVENT>
-__device__ double inverse_maps(const PhsChannel &ch, double sqrts, double *geo, double *xr,
-                               uint64_t reuse) {
+__device__ double inverse_maps(const PhsChannel &ch, double sqrts, const double *geo,
+                               double *cache, double *xr, uint64_t reuse) {
   const double s = sqrts * sqrts;
   double factor = 1.0;
   const int n_visits = ch.n_visits;
@@ -276,18 +279,20 @@ __device__ double inverse_maps(const PhsChannel &ch, double sqrts, double *geo, 
     for (int j = 0; j < 2; j++) {
       const PhsChild &C = V.child[j];
       if (C.internal) {
-        double *cache = geo + (PHS_INV_GEO * v + 5 + 2 * j) * PHS_INV_BLOCK;
+        double *slot = cache ? cache + (PHS_INV_CACHE * v + 2 * j) * PHS_INV_BLOCK : nullptr;
         double x, f;
         if (reuse >> (3 * v + j) & 1) {
-          x = cache[0];
-          f = cache[PHS_INV_BLOCK];
+          x = slot[0];
+          f = slot[PHS_INV_BLOCK];
         } else {
           double a0 = C.a0, a1 = C.a1, a2 = C.a2, mn = C.msq_min, mx = C.msq_max, mmax;
           if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, a0, a1, a2, mn, mx, mmax);
           map_msq_inverse(C.map_id, geo[(PHS_INV_GEO * v + j) * PHS_INV_BLOCK], s, C.m, C.w, mn,
                           mx, a0, a1, a2, x, f);
-          cache[0] = x;
-          cache[PHS_INV_BLOCK] = f;
+          if (slot) {
+            slot[0] = x;
+            slot[PHS_INV_BLOCK] = f;
+          }
         }
         if (xr) xr[C.x_msq] = x;
         factor *= f;
@@ -295,11 +300,11 @@ __device__ double inverse_maps(const PhsChannel &ch, double sqrts, double *geo, 
     }
     factor *= geo[(PHS_INV_GEO * v + 4) * PHS_INV_BLOCK];  // sqrt(lambda) / msq
     if (xr) xr[V.x_phi] = geo[(PHS_INV_GEO * v + 3) * PHS_INV_BLOCK];
-    double *cache = geo + (PHS_INV_GEO * v + 9) * PHS_INV_BLOCK;
+    double *slot = cache ? cache + (PHS_INV_CACHE * v + 4) * PHS_INV_BLOCK : nullptr;
     double x, f;
     if (reuse >> (3 * v + 2) & 1) {
-      x = cache[0];
-      f = cache[PHS_INV_BLOCK];
+      x = slot[0];
+      f = slot[PHS_INV_BLOCK];
     } else {
       double b0 = V.b0, b1 = V.b1;
       if (PER_EVENT && V.ct_class == PHS_CT_COLLINEAR) {
@@ -307,8 +312,10 @@ __device__ double inverse_maps(const PhsChannel &ch, double sqrts, double *geo, 
         b1 = log((b0 + 1.0) / b0);
       }
       map_ct_inverse(V.ct_class, geo[(PHS_INV_GEO * v + 2) * PHS_INV_BLOCK], b0, b1, x, f);
-      cache[0] = x;
-      cache[PHS_INV_BLOCK] = f;
+      if (slot) {
+        slot[0] = x;
+        slot[PHS_INV_BLOCK] = f;
+      }
     }
     if (xr) xr[V.x_ct] = x;
     factor *= f;
@@ -323,6 +330,8 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
   double *pm = sm;                                                  // [4 (2 n_out - 1)][block]
   double *stk = sm + (size_t)4 * (2 * a.n_out - 1) * PHS_INV_BLOCK;  // frame stack
   double *geo = stk + (size_t)PHS_INV_STATE * a.stack_depth * PHS_INV_BLOCK;  // per-visit geometry
+  double *cache = a.group_reuse ? geo + (size_t)PHS_INV_GEO * a.max_visits * PHS_INV_BLOCK
+                                : nullptr;  // per-visit mapping results
   const int tid = threadIdx.x;
   const int64_t n_tiles = (a.n_events + PHS_INV_BLOCK - 1) / PHS_INV_BLOCK;
   const PhsChannel &ch0 = a.channels[0];
@@ -414,11 +423,12 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
           // the generating channel keeps its own row, but its mappings still run when a
           // later channel of the shape reuses them
           const bool own_row = c == own_e && has_own;
-          if (own_row && (i + 1 == ge || a.group_reuse[i + 1] == 0)) continue;
+          if (own_row && (!cache || i + 1 == ge || a.group_reuse[i + 1] == 0)) continue;
           double *xr = own_row ? nullptr : a.x_out + ((int64_t)c * a.n_events + e) * a.n_x;
           // the first channel of a shape computes every mapping
-          const uint64_t reuse = i == gb ? 0ull : a.group_reuse[i];
-          const double fac = inverse_maps<PER_EVENT>(a.channels[c], sqrts, geo + tid, xr, reuse);
+          const uint64_t reuse = i == gb || !cache ? 0ull : a.group_reuse[i];
+          const double fac = inverse_maps<PER_EVENT>(a.channels[c], sqrts, geo + tid,
+                                                     cache ? cache + tid : nullptr, xr, reuse);
           if (!own_row) a.all_factors[e * a.n_channels + c] = fac;
         }
       }
@@ -429,24 +439,32 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
 
 }  // namespace
 
-size_t phs_inverse_smem_bytes(int n_out, int stack_depth, int max_visits) {
+size_t phs_inverse_smem_bytes(int n_out, int stack_depth, int max_visits, bool cache) {
   return ((size_t)4 * (2 * n_out - 1) + (size_t)PHS_INV_STATE * stack_depth +
-          (size_t)PHS_INV_GEO * max_visits) * PHS_INV_BLOCK * sizeof(double);
+          (size_t)(PHS_INV_GEO + (cache ? PHS_INV_CACHE : 0)) * max_visits) *
+         PHS_INV_BLOCK * sizeof(double);
 }
 
-int phs_inverse_blocks_per_sm(int n_out, int stack_depth, int max_visits, bool per_event) {
+bool phs_inverse_fits_cache(int n_out, int stack_depth, int max_visits) {
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return phs_inverse_smem_bytes(n_out, stack_depth, max_visits, true) <= (size_t)optin;
+}
+
+int phs_inverse_blocks_per_sm(int n_out, int stack_depth, int max_visits, bool per_event, bool cache) {
   int n = 0;
-  const size_t smem = phs_inverse_smem_bytes(n_out, stack_depth, max_visits);
-  if (per_event)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phs_inverse_kernel<true>, PHS_INV_BLOCK, smem);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, phs_inverse_kernel<false>, PHS_INV_BLOCK, smem);
+  const size_t smem = phs_inverse_smem_bytes(n_out, stack_depth, max_visits, cache);
+  const void *k = per_event ? (const void *)phs_inverse_kernel<true> : (const void *)phs_inverse_kernel<false>;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, PHS_INV_BLOCK, smem);
   return n > 0 ? n : 1;
 }
 
 cudaError_t phs_launch_inverse(const PhsInvLaunch &a, int n_blocks, cudaStream_t stream) {
   if (a.n_events <= 0) return cudaSuccess;
-  const size_t smem = phs_inverse_smem_bytes(a.n_out, a.stack_depth, a.max_visits);
+  const size_t smem = phs_inverse_smem_bytes(a.n_out, a.stack_depth, a.max_visits,
+                                             a.group_reuse != nullptr);
   const bool per_event = a.E1 && a.E2;
   if (smem > 48 * 1024) {
     cudaError_t e = per_event

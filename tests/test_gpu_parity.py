@@ -33,10 +33,12 @@ def torch():
     return torch
 
 
-def run_gpu(torch, proc, x, sqrts, counts=None, E=None):
+def run_gpu(torch, proc, x, sqrts, counts=None, E=None, precision=0, variants=(-1, -1)):
     from gpu_phs_gb300.api import PhaseSpace
     ps = PhaseSpace(proc)
     ps.set_beams(*(E if E else (sqrts / 2, sqrts / 2)))
+    ps.set_precision(precision)
+    ps.set_variants(*variants)
     xd = torch.from_numpy(np.ascontiguousarray(x)).cuda()
     ev = ps.generate(xd, counts)
     torch.cuda.synchronize()
@@ -119,6 +121,93 @@ def test_edge_sizes(torch, n):
         assert_parity(got, r.p, r.factor, r.volume, r.ok)
     else:
         assert got[0].shape == (0, 6, 4)
+
+
+# (precision, (FP32-pair variant, FP64 variant)): the split forms and a non-default shape
+SPLIT_FORMS = [(0, (-1, 6)), (0, (-1, 8)), (1, (5, -1)), (1, (3, -1))]
+
+
+@pytest.mark.parametrize("form", SPLIT_FORMS)
+@pytest.mark.parametrize("n", [0, 1, 31, 33, 1025])
+def test_edge_sizes_compacting_and_split_forms(torch, n, form):
+    """Partial and single tiles, one-tile segments and no events at all through the
+    pre-test, scan and walk kernels (and the fused compacting FP32-pair form)."""
+    prec, variants = form
+    proc = P.tt()
+    x = uniform_x(15, max(n, 1), proc.n_x)[:n]
+    got = run_gpu(torch, proc, x, 1000.0, precision=prec, variants=variants)
+    if not n:
+        assert got[0].shape == (0, 6, 4)
+        return
+    r = oracle.Oracle(proc, 1000.0).generate(x)
+    if prec == 0:
+        assert_parity(got, r.p, r.factor, r.volume, r.ok)
+    else:
+        p, f, v, ok = got
+        assert np.array_equal(ok, r.ok)
+        sel = r.ok == 1
+        assert momentum_rel_err(p[sel], r.p[sel], 1000.0).max() <= 1e-7
+        assert np.all(p[~sel] == 0) and np.all(f[~sel] == 0)
+
+
+@pytest.mark.parametrize("n_out", [10, 12])
+def test_largest_trees(torch, n_out):
+    """The API's largest trees (up to 12 outgoing particles, 11 visits, 32 x per event):
+    balanced and caterpillar channels of nested resonances, FP64 against the oracle, FP32
+    pairs at their bar, and the inverse map's round trip."""
+    from gpu_phs_gb300.api import PhaseSpace
+
+    def balanced(leaves):
+        if len(leaves) == 1:
+            return leaves[0]
+        h = len(leaves) // 2
+        return (balanced(leaves[:h]), balanced(leaves[h:]))
+
+    def caterpillar(leaves):
+        t = leaves[0]
+        for k in leaves[1:]:
+            t = (t, k)
+        return t
+
+    def resonances(t, maps, depth=0):
+        # nested Breit-Wigners, 25 GeV per particle below them: kinematically compatible
+        if isinstance(t, int):
+            return 1 << t
+        code = resonances(t[0], maps, depth + 1) | resonances(t[1], maps, depth + 1)
+        if depth:
+            m = 25.0 * bin(code).count("1")
+            maps[code] = (P.MAP_SCHANNEL, m, 0.02 * m)
+        return code
+
+    leaves = list(range(n_out))
+    trees = [balanced(leaves), caterpillar(leaves), balanced(leaves[::-1])]
+    maps = []
+    for t in trees:
+        mp = {}
+        resonances(t, mp)
+        maps.append(mp)
+    proc = P.process_from_trees(trees, maps, [P.M_ELECTRON, P.M_ELECTRON] + [0.0] * n_out,
+                                sqrts=1000.0)
+    counts = np.array([3000, 1, 2999], np.int64)
+    chan = np.repeat(np.arange(3), counts).astype(np.int32)
+    x = uniform_x(41, int(counts.sum()), proc.n_x)
+    r = oracle.Oracle(proc, 1000.0).generate(x, chan)
+    got = run_gpu(torch, proc, x, 1000.0, counts)
+    assert_parity(got, r.p, r.factor, r.volume, r.ok)
+    assert r.ok.mean() > 0.1
+    ff = run_gpu(torch, proc, x, 1000.0, counts, precision=1)
+    assert np.array_equal(ff[3], r.ok)
+    sel = r.ok == 1
+    assert momentum_rel_err(ff[0][sel], r.p[sel], 1000.0).max() <= 1e-7
+    # inverse map: the generating channel's own x comes back
+    ps = PhaseSpace(proc, 500.0, 500.0)
+    xd = torch.from_numpy(x).cuda()
+    ev = ps.generate(xd, counts)
+    fa, xo = ps.inverse(ev.p, counts, ev.ok)
+    xo = xo.cpu().numpy()
+    own = xo[chan, np.arange(x.shape[0])]
+    okb = ev.ok.cpu().numpy() == 1
+    assert np.abs(own[okb] - x[okb]).max() < 1e-6
 
 
 def test_multichannel_uneven_counts(torch):
