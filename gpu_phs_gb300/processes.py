@@ -232,6 +232,44 @@ def random_process(rng: np.random.Generator, n_out: int, n_channels: int, sqrts:
     return process_from_trees(trees, maps, flv, name=name, sqrts=sqrts)
 
 
+def nested_resonances(n_out: int, sqrts: float = 1000.0, per_particle: float = 25.0) -> Process:
+    """Three channels over n_out massless particles -- a balanced tree, a caterpillar and
+    the balanced tree over the reversed particles -- whose internal branches below the root
+    are Breit-Wigner resonances of per_particle GeV per particle below them (width 2 %),
+    so that nested resonances are kinematically compatible: the largest trees the API
+    takes with a sizeable ok fraction."""
+    def balanced(leaves):
+        if len(leaves) == 1:
+            return leaves[0]
+        h = len(leaves) // 2
+        return (balanced(leaves[:h]), balanced(leaves[h:]))
+
+    def caterpillar(leaves):
+        t = leaves[0]
+        for k in leaves[1:]:
+            t = (t, k)
+        return t
+
+    def resonances(t, mp, depth=0):
+        if isinstance(t, int):
+            return 1 << t
+        code = resonances(t[0], mp, depth + 1) | resonances(t[1], mp, depth + 1)
+        if depth:
+            m = per_particle * bin(code).count("1")
+            mp[code] = (MAP_SCHANNEL, m, 0.02 * m)
+        return code
+
+    leaves = list(range(n_out))
+    trees = [balanced(leaves), caterpillar(leaves), balanced(leaves[::-1])]
+    maps = []
+    for t in trees:
+        mp: Dict[int, Tuple[int, float, float]] = {}
+        resonances(t, mp)
+        maps.append(mp)
+    return process_from_trees(trees, maps, [M_ELECTRON, M_ELECTRON] + [0.0] * n_out,
+                              name=f"nested_resonances_{n_out}", sqrts=sqrts)
+
+
 def batched(seed: int = 2024, n_channels: int = 64, total_events: int = 1 << 24,
             sqrts: float = 1000.0) -> Tuple[List[Process], np.ndarray]:
     """The batched workload: n_channels single-channel processes with 3-8 outgoing

@@ -184,3 +184,36 @@ def test_adjoint_friend_channels_against_finite_differences(torch, k):
     assert keep.sum() > 0.3 * n
     assert np.median(rel) < 1e-7, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])
     assert np.quantile(rel, 0.99) < 1e-4, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])
+
+
+@pytest.mark.parametrize("channel", [0, 1])
+def test_adjoint_largest_trees_against_finite_differences(torch, channel):
+    """12 outgoing particles (11 visits, 32 x, a two-deep frame stack): the balanced tree
+    and the caterpillar of nested resonances, against finite differences as above."""
+    from gpu_phs_gb300.api import PhaseSpace
+    proc = P.nested_resonances(12).subset([channel])
+    n, h = 3000, 1e-6
+    x = torch.from_numpy(uniform_x(900 + channel, n, proc.n_x)).cuda()
+    ps = PhaseSpace(proc, 500.0, 500.0)
+    g = torch.Generator(device="cuda").manual_seed(20 + channel)
+    pbar = torch.randn((n, proc.n_out, 4), generator=g, device="cuda", dtype=torch.float64)
+    jbar = torch.randn(n, generator=g, device="cuda", dtype=torch.float64)
+    xbar, _ = ps.vjp(x, pbar, jbar)
+    ev = ps.generate(x)
+    keep = ev.ok.bool().cpu().numpy() & (margins(ev.p.cpu().numpy(), proc) > 1e-4)
+    keep &= ((x > 2 * h) & (x < 1 - 2 * h)).all(dim=1).cpu().numpy()
+    fd = torch.zeros_like(x)
+    for i in range(proc.n_x):
+        xp, xm = x.clone(), x.clone()
+        xp[:, i] += h
+        xm[:, i] -= h
+        lp, okp = loss(torch, ps, xp, pbar, jbar)
+        lm, okm = loss(torch, ps, xm, pbar, jbar)
+        fd[:, i] = (lp - lm) / (2 * h)
+        keep &= (okp & okm).cpu().numpy()
+    a, b = xbar.cpu().numpy()[keep], fd.cpu().numpy()[keep]
+    scale = np.abs(b).max(axis=1, keepdims=True) + 1.0
+    rel = np.abs(a - b) / scale
+    assert keep.sum() > 0.05 * n
+    assert np.median(rel) < 1e-7, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])
+    assert np.quantile(rel, 0.99) < 1e-4, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])

@@ -156,38 +156,7 @@ def test_largest_trees(torch, n_out):
     balanced and caterpillar channels of nested resonances, FP64 against the oracle, FP32
     pairs at their bar, and the inverse map's round trip."""
     from gpu_phs_gb300.api import PhaseSpace
-
-    def balanced(leaves):
-        if len(leaves) == 1:
-            return leaves[0]
-        h = len(leaves) // 2
-        return (balanced(leaves[:h]), balanced(leaves[h:]))
-
-    def caterpillar(leaves):
-        t = leaves[0]
-        for k in leaves[1:]:
-            t = (t, k)
-        return t
-
-    def resonances(t, maps, depth=0):
-        # nested Breit-Wigners, 25 GeV per particle below them: kinematically compatible
-        if isinstance(t, int):
-            return 1 << t
-        code = resonances(t[0], maps, depth + 1) | resonances(t[1], maps, depth + 1)
-        if depth:
-            m = 25.0 * bin(code).count("1")
-            maps[code] = (P.MAP_SCHANNEL, m, 0.02 * m)
-        return code
-
-    leaves = list(range(n_out))
-    trees = [balanced(leaves), caterpillar(leaves), balanced(leaves[::-1])]
-    maps = []
-    for t in trees:
-        mp = {}
-        resonances(t, mp)
-        maps.append(mp)
-    proc = P.process_from_trees(trees, maps, [P.M_ELECTRON, P.M_ELECTRON] + [0.0] * n_out,
-                                sqrts=1000.0)
+    proc = P.nested_resonances(n_out)
     counts = np.array([3000, 1, 2999], np.int64)
     chan = np.repeat(np.arange(3), counts).astype(np.int32)
     x = uniform_x(41, int(counts.sum()), proc.n_x)
