@@ -365,7 +365,68 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64, pin=
         "algorithmic_bytes_per_step": wbytes + rbytes,
         "ok_fraction": ev.ok.double().mean().item(),
         "launch": "one persistent kernel: 128 events per block, every channel per event"}
+    del fac, xo, ev, x, ps
+    res["whizard_abi_bwbw_61ch"] = whizard_abi_rate(proc, 1 << 17, max(2, min(steps, 5)))
     return res
+
+
+def whizard_abi_rate(proc, n: int, steps: int) -> dict:
+    """The drop-in call as Whizard makes it: the 14-symbol C ABI set up for the process,
+    then c_whizard_gen_phs_from_x_gpu on host arrays (x in; momenta, every channel's factor
+    and x, volumes and ok flags out), host wall clock per call."""
+    import ctypes as C
+    from gpu_phs_gb300 import _lib
+    from gpu_phs_gb300.philox import uniform_x
+    lib = _lib.load()
+    ip = lambda v: C.byref(C.c_int(v))
+    nch, n_x, n_out = proc.n_channels, proc.n_x, proc.n_out
+    lib.c_whizard_set_particle_structure(ip(nch), ip(nch), ip(nch), ip(n_x), ip(proc.n_in), ip(n_out))
+    keep = [np.ascontiguousarray(proc.flv_masses), np.ascontiguousarray(proc.flv_widths)]
+    lib.c_whizard_set_flavors(keep[0].ctypes.data, keep[1].ctypes.data)
+    lib.c_whizard_init_mappings()
+    for c in range(nch):
+        a = [np.ascontiguousarray(proc.map_ids[c], np.int32), np.ascontiguousarray(proc.map_masses[c]),
+             np.ascontiguousarray(proc.map_widths[c])]
+        keep += a
+        lib.c_whizard_fill_mapping(ip(c + 1), *[t.ctypes.data for t in a])
+    lib.c_whizard_init_tree_structures()
+    for c in range(nch):
+        a = [np.ascontiguousarray(t[c], np.int32) for t in (proc.d1, proc.d2, proc.has_children, proc.friends)]
+        keep += a
+        lib.c_whizard_fill_tree_structure(ip(c + 1), *[t.ctypes.data for t in a])
+    lib.c_whizard_init_gpu_phs()
+    counts = np.full(nch, n // nch, np.int64)
+    counts[: n - int(counts.sum())] += 1
+    limits = np.ascontiguousarray(np.cumsum(counts), np.int32)
+    lib.c_whizard_init_channel_ids(ip(n), ip(nch), limits.ctypes.data)
+    x = np.ascontiguousarray(uniform_x(SEED, n, n_x))
+    E1, E2 = np.full(n, proc.sqrts / 2), np.full(n, proc.sqrts / 2)
+    factors, volumes = np.zeros(n * nch), np.zeros(n)
+    oks = np.zeros(n, np.uint8)
+    p = np.zeros(n * n_out * 4)
+    x_out = np.zeros(n * n_x * nch)
+    flag = C.c_bool(False)
+
+    def call():
+        lib.c_whizard_gen_phs_from_x_gpu(E1.ctypes.data, E2.ctypes.data, C.byref(flag), ip(n),
+                                         ip(nch), ip(n_x), x.ctypes.data, factors.ctypes.data,
+                                         volumes.ctypes.data, oks.ctypes.data, p.ctypes.data,
+                                         x_out.ctypes.data)
+    call()
+    err = lib.phs_last_error().decode()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        call()
+    dt = (time.perf_counter() - t0) / steps
+    lib.c_whizard_reset_generator()
+    lib.c_whizard_finalize_gpu_phs()
+    out_bytes = n * (32 * n_out + 8 * nch + 8 + 1 + 8 * n_x * nch)
+    return {"n_events": n, "n_channels": nch, "ms_per_call": dt * 1e3,
+            "events_per_s": n / dt, "channel_inversions_per_s": n * nch / dt,
+            "h2d_bytes_per_call": n * (8 * n_x + 16), "d2h_bytes_per_call": out_bytes,
+            "error": err or None,
+            "path": "c_whizard_gen_phs_from_x_gpu (host arrays): forward, all-channel inverse, "
+                    "copies back of momenta, factors [n][61], x [61][n][n_x], volumes, ok"}
 
 
 def whizard_process(name: str):

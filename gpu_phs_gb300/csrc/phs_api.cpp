@@ -738,6 +738,11 @@ extern "C" int phs_adjoint_device(phs_process_t h, int64_t n_events, const int64
 }
 
 // Inverse map: all-channel factors and x of generated events.
+static int inverse_launch(phs_process_t h, int64_t n_events, const int64_t *d_ch_begin,
+                          const double *E1, const double *E2, const double *p, const uint8_t *ok,
+                          const double *x_own, const double *factor_own, double *all_factors,
+                          double *x_out, cudaStream_t st);
+
 extern "C" int phs_inverse_device(phs_process_t h, int64_t n_events, const int64_t *counts,
                                   const double *E1, const double *E2, const double *p,
                                   const uint8_t *ok, const double *x_own,
@@ -771,10 +776,20 @@ extern "C" int phs_inverse_device(phs_process_t h, int64_t n_events, const int64
     CUDA_TRY(cudaStreamSynchronize(st));
     h->ch_begin_up = begin;
   }
+  return inverse_launch(h, n_events, h->d_ch_begin.as<int64_t>(), E1, E2, p, ok, x_own,
+                        factor_own, all_factors, x_out, st);
+}
+
+// The inverse-map launch of n_events (channel starts d_ch_begin[n_channels] on the device).
+static int inverse_launch(phs_process_t h, int64_t n_events, const int64_t *d_ch_begin,
+                          const double *E1, const double *E2, const double *p, const uint8_t *ok,
+                          const double *x_own, const double *factor_own, double *all_factors,
+                          double *x_out, cudaStream_t st) {
+  const int nch = h->p.n_channels;
   PhsInvLaunch a;
   memset(&a, 0, sizeof a);
   a.channels = h->d_prog.as<PhsChannel>();
-  a.ch_begin = h->d_ch_begin.as<int64_t>();
+  a.ch_begin = d_ch_begin;
   a.p = p;
   a.ok = ok;
   a.E1 = E1;
@@ -1202,6 +1217,9 @@ struct Whizard {
   DevBuf dx, dp, df, dv, dok;
   DevBuf dfa, dxo;  // all-channel factors and x of the inverse map
   DevBuf dsparse, din;  // device handoff in the reference's layouts, built on request
+  DevBuf dchb;          // per chunk of the call, each channel's first event in the chunk
+  cudaStream_t streams[2] = {nullptr, nullptr};  // compute, copies
+  cudaEvent_t done[2] = {nullptr, nullptr};      // a chunk's kernels are done (by parity)
   bool sparse_ok = false, in_ok = false, last_uniform = true;
   double last_e1 = 0, last_e2 = 0;
   std::vector<uint32_t> internal;  // bit code: an internal branch of some channel
@@ -1217,7 +1235,7 @@ void whizard_log(int rc) {
 void whizard_release_device() {
   W.dx.release(); W.dp.release(); W.df.release(); W.dv.release(); W.dok.release();
   W.dfa.release(); W.dxo.release();
-  W.dsparse.release(); W.din.release();
+  W.dsparse.release(); W.din.release(); W.dchb.release();
   W.sparse_ok = W.in_ok = false;
   W.last_events = 0;
 }
@@ -1356,6 +1374,12 @@ extern "C" void c_whizard_finalize_gpu_phs(void) {
   if (W.proc) phs_process_destroy(W.proc);
   W.proc = nullptr;
   whizard_release_device();
+  for (int i = 0; i < 2; i++) {
+    if (W.streams[i]) cudaStreamDestroy(W.streams[i]);
+    if (W.done[i]) cudaEventDestroy(W.done[i]);
+    W.streams[i] = nullptr;
+    W.done[i] = nullptr;
+  }
   W.map_id.clear(); W.map_m.clear(); W.map_w.clear();
   W.d1.clear(); W.d2.clear(); W.hc.clear(); W.fr.clear();
   W.flv_m.clear(); W.flv_w.clear();
@@ -1402,40 +1426,106 @@ extern "C" void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in,
     if ((rc = W.df.reserve(n * sizeof(double) * (uniform ? 1 : 3)))) break;
     if ((rc = W.dv.reserve(n * sizeof(double)))) break;
     if ((rc = W.dok.reserve(n))) break;
+    if ((rc = W.dfa.reserve((size_t)n * nch * sizeof(double)))) break;
     cudaError_t e = cudaMemcpy(W.dx.ptr, x, n * n_x * sizeof(double), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy of x: %s", cudaGetErrorString(e)); break; }
     double *df = W.df.as<double>();
+    const double *dE1 = nullptr, *dE2 = nullptr;
     if (uniform) {
       if ((rc = phs_process_set_beams(W.proc, E1_in[0], E2_in[0]))) break;
-      rc = phs_generate_device(W.proc, n, counts.data(), W.dx.as<double>(), W.dp.as<double>(), df,
-                               W.dv.as<double>(), W.dok.as<uint8_t>(), nullptr);
     } else {
-      double *dE1 = df + n, *dE2 = df + 2 * n;
-      cudaMemcpy(dE1, E1_in, n * sizeof(double), cudaMemcpyHostToDevice);
-      cudaMemcpy(dE2, E2_in, n * sizeof(double), cudaMemcpyHostToDevice);
-      rc = phs_generate_beams_device(W.proc, n, counts.data(), dE1, dE2, W.dx.as<double>(),
-                                     W.dp.as<double>(), df, W.dv.as<double>(),
-                                     W.dok.as<uint8_t>(), nullptr);
+      e = cudaMemcpy(df + n, E1_in, n * sizeof(double), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = cudaMemcpy(df + 2 * n, E2_in, n * sizeof(double), cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy of beams: %s", cudaGetErrorString(e)); break; }
+      dE1 = df + n;
+      dE2 = df + 2 * n;
     }
-    if (rc) break;
-    // the inverse map fills factors[n_channels * i + c] and x_out[n_x * n * c + n_x * i + k]
-    // for every channel (do_inverse_mapping is forced on, whizard_gpu_phs.cpp:118;
-    // layouts phs.cu:1580-1585); the generating channel keeps its own x and factor
-    if ((rc = W.dfa.reserve((size_t)n * nch * sizeof(double)))) break;
-    if ((rc = W.dxo.reserve((size_t)n * nch * n_x * sizeof(double)))) break;
-    rc = phs_inverse_device(W.proc, n, counts.data(), uniform ? nullptr : df + n,
-                            uniform ? nullptr : df + 2 * n, W.dp.as<double>(),
-                            W.dok.as<uint8_t>(), W.dx.as<double>(), df, W.dfa.as<double>(),
-                            W.dxo.as<double>(), nullptr);
-    if (rc) break;
-    e = cudaMemcpy(p, W.dp.ptr, n * 4 * n_out * sizeof(double), cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess)
-      e = cudaMemcpy(factors, W.dfa.ptr, (size_t)n * nch * sizeof(double), cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && x_out)
-      e = cudaMemcpy(x_out, W.dxo.ptr, (size_t)n * nch * n_x * sizeof(double), cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(volumes, W.dv.ptr, n * sizeof(double), cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(oks, W.dok.ptr, n, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e)); break; }
+    // Chunks of events: the forward map and the inverse map (factors [n][n_channels] in
+    // place, x of every channel into one of two chunk buffers) of chunk k + 1 are queued on
+    // the compute stream before the host waits for chunk k's copies into the caller's
+    // arrays on the copy stream (copies into pageable memory return when done), so the
+    // GPU computes while the copies run.
+    const int64_t chunk = std::max<int64_t>(1 << 14, (n + 7) / 8);
+    const int64_t n_chunks = (n + chunk - 1) / chunk;
+    std::vector<int64_t> cnt((size_t)n_chunks * nch, 0), beg((size_t)n_chunks * nch, 0);
+    {
+      int64_t c_lo = 0;
+      for (int c = 0; c < nch; c++) {
+        const int64_t c_hi = c_lo + counts[c];
+        for (int64_t k = 0; k < n_chunks; k++) {
+          const int64_t e0 = k * chunk, e1 = std::min(n, e0 + chunk);
+          cnt[k * nch + c] = std::max<int64_t>(0, std::min(e1, c_hi) - std::max(e0, c_lo));
+        }
+        c_lo = c_hi;
+      }
+      for (int64_t k = 0; k < n_chunks; k++)
+        for (int c = 1; c < nch; c++) beg[k * nch + c] = beg[k * nch + c - 1] + cnt[k * nch + c - 1];
+    }
+    if ((rc = W.dchb.reserve(beg.size() * sizeof(int64_t)))) break;
+    if ((rc = W.dxo.reserve(2 * (size_t)nch * chunk * n_x * sizeof(double)))) break;
+    e = cudaMemcpy(W.dchb.ptr, beg.data(), beg.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+    for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+      if (!W.streams[i]) e = cudaStreamCreateWithFlags(&W.streams[i], cudaStreamNonBlocking);
+      if (e == cudaSuccess && !W.done[i]) e = cudaEventCreateWithFlags(&W.done[i], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "set-up: %s", cudaGetErrorString(e)); break; }
+    cudaStream_t cs = W.streams[0], ms = W.streams[1];
+    auto compute = [&](int64_t k) -> int {
+      const int64_t e0 = k * chunk, nk = std::min(n, e0 + chunk) - e0;
+      const int64_t *ck = cnt.data() + k * nch;
+      double *xo = W.dxo.as<double>() + (size_t)(k & 1) * nch * chunk * n_x;
+      const double *xk = W.dx.as<double>() + e0 * n_x;
+      double *pk = W.dp.as<double>() + e0 * 4 * n_out;
+      int r = uniform
+          ? phs_generate_device(W.proc, nk, ck, xk, pk, df + e0, W.dv.as<double>() + e0,
+                                W.dok.as<uint8_t>() + e0, cs)
+          : phs_generate_beams_device(W.proc, nk, ck, dE1 + e0, dE2 + e0, xk, pk, df + e0,
+                                      W.dv.as<double>() + e0, W.dok.as<uint8_t>() + e0, cs);
+      if (r) return r;
+      // do_inverse_mapping is forced on (whizard_gpu_phs.cpp:118): every channel's factor
+      // and x; the generating channel keeps its own x and factor (phs.cu:1580-1585)
+      r = inverse_launch(W.proc, nk, W.dchb.as<int64_t>() + k * nch, uniform ? nullptr : dE1 + e0,
+                         uniform ? nullptr : dE2 + e0, pk, W.dok.as<uint8_t>() + e0, xk, df + e0,
+                         W.dfa.as<double>() + e0 * nch, xo, cs);
+      if (r) return r;
+      const cudaError_t ee = cudaEventRecord(W.done[k & 1], cs);
+      return ee == cudaSuccess ? PHS_OK : fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(ee));
+    };
+    // copies of chunk k into the caller's arrays: p[4 n_out i + ..], factors[n_channels i + c],
+    // x_out[n_x n c + n_x i + k], volumes, oks
+    auto copy_back = [&](int64_t k) -> cudaError_t {
+      const int64_t e0 = k * chunk, nk = std::min(n, e0 + chunk) - e0;
+      const double *xo = W.dxo.as<double>() + (size_t)(k & 1) * nch * chunk * n_x;
+      cudaError_t ee = cudaStreamWaitEvent(ms, W.done[k & 1], 0);
+      if (ee == cudaSuccess)
+        ee = cudaMemcpyAsync(p + e0 * 4 * n_out, W.dp.as<double>() + e0 * 4 * n_out,
+                             nk * 4 * n_out * sizeof(double), cudaMemcpyDeviceToHost, ms);
+      if (ee == cudaSuccess)
+        ee = cudaMemcpyAsync(factors + e0 * nch, W.dfa.as<double>() + e0 * nch,
+                             nk * nch * sizeof(double), cudaMemcpyDeviceToHost, ms);
+      if (ee == cudaSuccess && x_out)
+        ee = cudaMemcpy2DAsync(x_out + e0 * n_x, (size_t)n * n_x * sizeof(double), xo,
+                               (size_t)nk * n_x * sizeof(double), (size_t)nk * n_x * sizeof(double),
+                               nch, cudaMemcpyDeviceToHost, ms);
+      if (ee == cudaSuccess)
+        ee = cudaMemcpyAsync(volumes + e0, W.dv.as<double>() + e0, nk * sizeof(double),
+                             cudaMemcpyDeviceToHost, ms);
+      if (ee == cudaSuccess)
+        ee = cudaMemcpyAsync(oks + e0, W.dok.as<uint8_t>() + e0, nk, cudaMemcpyDeviceToHost, ms);
+      if (ee == cudaSuccess) ee = cudaStreamSynchronize(ms);
+      return ee;
+    };
+    for (int64_t k = 0; k <= n_chunks && rc == PHS_OK; k++) {
+      if (k < n_chunks) rc = compute(k);
+      if (rc == PHS_OK && k > 0) {
+        e = copy_back(k - 1);
+        if (e != cudaSuccess) rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
+      }
+    }
+    if (rc) {
+      cudaStreamSynchronize(cs);
+      break;
+    }
     W.last_events = n;
     W.sparse_ok = W.in_ok = false;  // the handoff buffers are rebuilt on request
     W.last_uniform = uniform;

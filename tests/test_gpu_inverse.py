@@ -238,3 +238,72 @@ def test_whizard_abi_all_channels(torch):
     assert np.all(np.abs(fac - g) <= 0.5e-7 + 2e-3 * np.abs(g))
     lib.c_whizard_reset_generator()
     lib.c_whizard_finalize_gpu_phs()
+
+
+@pytest.mark.parametrize("beams", ["uniform", "per_event"])
+def test_whizard_abi_chunked_call_equals_handle_api(torch, beams):
+    """100 000 bwbw events through c_whizard_gen_phs_from_x_gpu, which pipelines chunks of
+    events (compute of one chunk beside the copies of the previous): momenta, every
+    channel's factors and x, volumes and ok flags equal the handle API's forward and
+    inverse calls on the whole batch, bit for bit."""
+    from gpu_phs_gb300 import _lib
+    from gpu_phs_gb300.api import PhaseSpace
+    lib = _lib.load()
+    z = golden("whizard_bwbw")
+    proc = load_process(z)
+    ip = lambda v: C.byref(C.c_int(v))
+    nch, n_x, n_out = proc.n_channels, proc.n_x, proc.n_out
+    lib.c_whizard_set_particle_structure(ip(nch), ip(nch), ip(nch), ip(n_x), ip(2), ip(n_out))
+    fm = np.ascontiguousarray(proc.flv_masses)
+    fw = np.ascontiguousarray(proc.flv_widths)
+    lib.c_whizard_set_flavors(fm.ctypes.data, fw.ctypes.data)
+    lib.c_whizard_init_mappings()
+    keep = []
+    for c in range(nch):
+        a = [np.ascontiguousarray(proc.map_ids[c], np.int32), np.ascontiguousarray(proc.map_masses[c]),
+             np.ascontiguousarray(proc.map_widths[c])]
+        keep += a
+        lib.c_whizard_fill_mapping(ip(c + 1), *[t.ctypes.data for t in a])
+    lib.c_whizard_init_tree_structures()
+    for c in range(nch):
+        a = [np.ascontiguousarray(t[c], np.int32) for t in (proc.d1, proc.d2, proc.has_children, proc.friends)]
+        keep += a
+        lib.c_whizard_fill_tree_structure(ip(c + 1), *[t.ctypes.data for t in a])
+    lib.c_whizard_init_gpu_phs()
+    n = 100_000
+    rng = np.random.default_rng(17)
+    counts = rng.multinomial(n, np.full(nch, 1.0 / nch)).astype(np.int64)
+    counts[5] = 0                                      # an empty channel inside
+    counts[0] += n - int(counts.sum())
+    limits = np.ascontiguousarray(np.cumsum(counts), np.int32)
+    lib.c_whizard_init_channel_ids(ip(n), ip(nch), limits.ctypes.data)
+    x = np.ascontiguousarray(uniform_x(18, n, n_x))
+    if beams == "uniform":
+        E1, E2 = np.full(n, 500.0), np.full(n, 500.0)
+    else:
+        E1, E2 = rng.uniform(400, 600, n), rng.uniform(400, 600, n)
+    factors, volumes = np.zeros(n * nch), np.zeros(n)
+    oks = np.zeros(n, np.uint8)
+    p = np.zeros(n * n_out * 4)
+    x_out = np.zeros(n * n_x * nch)
+    lib.c_whizard_gen_phs_from_x_gpu(E1.ctypes.data, E2.ctypes.data, C.byref(C.c_bool(False)),
+                                     ip(n), ip(nch), ip(n_x), x.ctypes.data, factors.ctypes.data,
+                                     volumes.ctypes.data, oks.ctypes.data, p.ctypes.data,
+                                     x_out.ctypes.data)
+    assert lib.phs_last_error().decode() == ""
+    lib.c_whizard_reset_generator()
+    lib.c_whizard_finalize_gpu_phs()
+    ps = PhaseSpace(proc, 500.0, 500.0)
+    xd = torch.from_numpy(x).cuda()
+    if beams == "uniform":
+        ev = ps.generate(xd, counts)
+        fa, xo = ps.inverse(ev.p, counts, ev.ok, xd, ev.factor)
+    else:
+        e1, e2 = torch.from_numpy(E1).cuda(), torch.from_numpy(E2).cuda()
+        ev = ps.generate_beams(xd, e1, e2, counts)
+        fa, xo = ps.inverse(ev.p, counts, ev.ok, xd, ev.factor, E1=e1, E2=e2)
+    assert np.array_equal(p.reshape(n, n_out, 4), ev.p.cpu().numpy())
+    assert np.array_equal(volumes, ev.volume.cpu().numpy())
+    assert np.array_equal(oks, ev.ok.cpu().numpy())
+    assert np.array_equal(factors.reshape(n, nch), fa.cpu().numpy())
+    assert np.array_equal(x_out.reshape(nch, n, n_x), xo.cpu().numpy())
