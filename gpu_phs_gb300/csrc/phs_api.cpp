@@ -336,6 +336,8 @@ struct phs_process {
   DevBuf d_inv_groups;                // inverse map: channels by tree shape, group starts,
                                       // mapping reuse masks
   int n_inv_groups = 0;
+  std::vector<int32_t> inv_order;     // the channels in the group order (host copy)
+  std::vector<int32_t> inv_group_begin;  // each group's first position in it, then n_channels
   size_t inv_reuse_offset = 0;        // byte offset of the reuse masks in d_inv_groups
   std::vector<int64_t> ch_begin_up;   // content of d_ch_begin
   Segments segs;
@@ -548,6 +550,8 @@ extern "C" int phs_process_set_beams(phs_process_t h, double E1, double E2) {
                         reuse.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
     h->n_inv_groups = (int)members.size();
     h->inv_reuse_offset = head;
+    h->inv_order = order;
+    h->inv_group_begin.assign(table.begin() + order.size(), table.begin() + order.size() + members.size() + 1);
   }
   h->prog = std::move(prog);
   h->prog_ff = std::move(prog_ff);
@@ -741,7 +745,8 @@ extern "C" int phs_adjoint_device(phs_process_t h, int64_t n_events, const int64
 static int inverse_launch(phs_process_t h, int64_t n_events, const int64_t *d_ch_begin,
                           const double *E1, const double *E2, const double *p, const uint8_t *ok,
                           const double *x_own, const double *factor_own, double *all_factors,
-                          double *x_out, cudaStream_t st);
+                          double *x_out, cudaStream_t st, int order_lo = 0, int order_hi = -1,
+                          bool write_fixed = true, int64_t x_ch_stride = 0);
 
 extern "C" int phs_inverse_device(phs_process_t h, int64_t n_events, const int64_t *counts,
                                   const double *E1, const double *E2, const double *p,
@@ -780,11 +785,14 @@ extern "C" int phs_inverse_device(phs_process_t h, int64_t n_events, const int64
                         factor_own, all_factors, x_out, st);
 }
 
-// The inverse-map launch of n_events (channel starts d_ch_begin[n_channels] on the device).
+// The inverse-map launch of n_events (channel starts d_ch_begin[n_channels] on the device)
+// for the channels at group-order positions [order_lo, order_hi) (order_hi < 0: to the end);
+// x_out holds x_ch_stride rows per channel (0: n_events).
 static int inverse_launch(phs_process_t h, int64_t n_events, const int64_t *d_ch_begin,
                           const double *E1, const double *E2, const double *p, const uint8_t *ok,
                           const double *x_own, const double *factor_own, double *all_factors,
-                          double *x_out, cudaStream_t st) {
+                          double *x_out, cudaStream_t st, int order_lo, int order_hi,
+                          bool write_fixed, int64_t x_ch_stride) {
   const int nch = h->p.n_channels;
   PhsInvLaunch a;
   memset(&a, 0, sizeof a);
@@ -799,6 +807,7 @@ static int inverse_launch(phs_process_t h, int64_t n_events, const int64_t *d_ch
   a.all_factors = all_factors;
   a.x_out = x_out;
   a.n_events = n_events;
+  a.x_ch_stride = x_ch_stride > 0 ? x_ch_stride : n_events;
   a.n_channels = nch;
   a.n_out = h->p.n_out;
   a.n_x = h->p.n_x;
@@ -811,6 +820,9 @@ static int inverse_launch(phs_process_t h, int64_t n_events, const int64_t *d_ch
                               static_cast<const char *>(h->d_inv_groups.ptr) + h->inv_reuse_offset)
                         : nullptr;
   a.n_groups = h->n_inv_groups;
+  a.order_lo = order_lo;
+  a.order_hi = order_hi < 0 ? nch : order_hi;
+  a.write_fixed = write_fixed ? 1 : 0;
   const int64_t tiles = (n_events + PHS_INV_BLOCK - 1) / PHS_INV_BLOCK;
   const int64_t cap = (int64_t)sm_count(h->device) *
                       phs_inverse_blocks_per_sm(a.n_out, a.stack_depth, a.max_visits,
@@ -1203,6 +1215,13 @@ extern "C" int phs_measure_fma_peak(int fp64, double *gflops) {
 // Process-global state, as in the reference (global_phs.cpp, whizard_gpu_phs.cpp:10): one
 // process per library instance, driven by Whizard's single host thread.
 namespace {
+// The inverse map of a Whizard call runs in up to this many launches over slices of the
+// channels, whose copies back overlap the next slice's kernel.
+constexpr int kWhizardSlices = 8;
+// The last slice runs in up to this many chunks of events: the factors of a chunk's events
+// are final when it ends, and their copy overlaps the next chunk.
+constexpr int kWhizardLastChunks = 4;
+constexpr int kWhizardLaunches = kWhizardSlices - 1 + kWhizardLastChunks;
 struct Whizard {
   std::mutex mu;
   int n_channels = 0, n_trees = 0, n_groves = 0, n_x = 0, n_in = 0, n_out = 0;
@@ -1217,9 +1236,9 @@ struct Whizard {
   DevBuf dx, dp, df, dv, dok;
   DevBuf dfa, dxo;  // all-channel factors and x of the inverse map
   DevBuf dsparse, din;  // device handoff in the reference's layouts, built on request
-  DevBuf dchb;          // per chunk of the call, each channel's first event in the chunk
-  cudaStream_t streams[2] = {nullptr, nullptr};  // compute, copies
-  cudaEvent_t done[2] = {nullptr, nullptr};      // a chunk's kernels are done (by parity)
+  DevBuf dchb;          // each channel's first event
+  cudaStream_t streams[3] = {nullptr, nullptr, nullptr};  // compute, copies, compute
+  cudaEvent_t done[kWhizardLaunches + 1] = {};  // the forward map, each inverse launch done
   bool sparse_ok = false, in_ok = false, last_uniform = true;
   double last_e1 = 0, last_e2 = 0;
   std::vector<uint32_t> internal;  // bit code: an internal branch of some channel
@@ -1374,11 +1393,13 @@ extern "C" void c_whizard_finalize_gpu_phs(void) {
   if (W.proc) phs_process_destroy(W.proc);
   W.proc = nullptr;
   whizard_release_device();
-  for (int i = 0; i < 2; i++) {
-    if (W.streams[i]) cudaStreamDestroy(W.streams[i]);
-    if (W.done[i]) cudaEventDestroy(W.done[i]);
-    W.streams[i] = nullptr;
-    W.done[i] = nullptr;
+  for (cudaStream_t &st : W.streams) {
+    if (st) cudaStreamDestroy(st);
+    st = nullptr;
+  }
+  for (cudaEvent_t &ev : W.done) {
+    if (ev) cudaEventDestroy(ev);
+    ev = nullptr;
   }
   W.map_id.clear(); W.map_m.clear(); W.map_w.clear();
   W.d1.clear(); W.d2.clear(); W.hc.clear(); W.fr.clear();
@@ -1440,90 +1461,110 @@ extern "C" void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in,
       dE1 = df + n;
       dE2 = df + 2 * n;
     }
-    // Chunks of events: the forward map and the inverse map (factors [n][n_channels] in
-    // place, x of every channel into one of two chunk buffers) of chunk k + 1 are queued on
-    // the compute stream before the host waits for chunk k's copies into the caller's
-    // arrays on the copy stream (copies into pageable memory return when done), so the
-    // GPU computes while the copies run.
-    const int64_t chunk = std::max<int64_t>(1 << 14, (n + 7) / 8);
-    const int64_t n_chunks = (n + chunk - 1) / chunk;
-    std::vector<int64_t> cnt((size_t)n_chunks * nch, 0), beg((size_t)n_chunks * nch, 0);
-    {
-      int64_t c_lo = 0;
-      for (int c = 0; c < nch; c++) {
-        const int64_t c_hi = c_lo + counts[c];
-        for (int64_t k = 0; k < n_chunks; k++) {
-          const int64_t e0 = k * chunk, e1 = std::min(n, e0 + chunk);
-          cnt[k * nch + c] = std::max<int64_t>(0, std::min(e1, c_hi) - std::max(e0, c_lo));
-        }
-        c_lo = c_hi;
-      }
-      for (int64_t k = 0; k < n_chunks; k++)
-        for (int c = 1; c < nch; c++) beg[k * nch + c] = beg[k * nch + c - 1] + cnt[k * nch + c - 1];
-    }
-    if ((rc = W.dchb.reserve(beg.size() * sizeof(int64_t)))) break;
-    if ((rc = W.dxo.reserve(2 * (size_t)nch * chunk * n_x * sizeof(double)))) break;
-    e = cudaMemcpy(W.dchb.ptr, beg.data(), beg.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
-    for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+    // The forward map of every event, then the inverse map (factors [n][n_channels], x
+    // [n_channels][n][n_x]) in launches over slices of the channels in the order of the
+    // tree-shape groups (cut where a group ends, if one ends near the even cut: the geometry
+    // of a shape is computed once per event and launch), each over every event so that it
+    // fills the GPU, the last slice in chunks of events; the launches alternate over two
+    // compute streams, so that one's tail overlaps the next one's start.  Everything is
+    // queued first; the copies into the caller's arrays then follow on the copy stream (a
+    // copy into pageable memory returns when done): the momenta, volumes and ok flags after
+    // the forward map, each launch's x rows (contiguous per channel on both sides) beside
+    // the following kernels, and after each chunk of the last slice the factors of its
+    // events, which every earlier launch has finished.
+    const int n_slices_max = (int64_t)n * nch < (1 << 20) ? 1 : std::min(nch, kWhizardSlices);
+    std::vector<int64_t> beg(nch, 0);
+    for (int c = 1; c < nch; c++) beg[c] = beg[c - 1] + counts[c - 1];
+    if ((rc = W.dxo.reserve((size_t)nch * n * n_x * sizeof(double)))) break;
+    for (int i = 0; i < 3 && e == cudaSuccess; i++)
       if (!W.streams[i]) e = cudaStreamCreateWithFlags(&W.streams[i], cudaStreamNonBlocking);
-      if (e == cudaSuccess && !W.done[i]) e = cudaEventCreateWithFlags(&W.done[i], cudaEventDisableTiming);
-    }
+    for (int i = 0; i < kWhizardLaunches + 1 && e == cudaSuccess; i++)
+      if (!W.done[i]) e = cudaEventCreateWithFlags(&W.done[i], cudaEventDisableTiming);
     if (e != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "set-up: %s", cudaGetErrorString(e)); break; }
-    cudaStream_t cs = W.streams[0], ms = W.streams[1];
-    auto compute = [&](int64_t k) -> int {
-      const int64_t e0 = k * chunk, nk = std::min(n, e0 + chunk) - e0;
-      const int64_t *ck = cnt.data() + k * nch;
-      double *xo = W.dxo.as<double>() + (size_t)(k & 1) * nch * chunk * n_x;
-      const double *xk = W.dx.as<double>() + e0 * n_x;
-      double *pk = W.dp.as<double>() + e0 * 4 * n_out;
-      int r = uniform
-          ? phs_generate_device(W.proc, nk, ck, xk, pk, df + e0, W.dv.as<double>() + e0,
-                                W.dok.as<uint8_t>() + e0, cs)
-          : phs_generate_beams_device(W.proc, nk, ck, dE1 + e0, dE2 + e0, xk, pk, df + e0,
-                                      W.dv.as<double>() + e0, W.dok.as<uint8_t>() + e0, cs);
-      if (r) return r;
-      // do_inverse_mapping is forced on (whizard_gpu_phs.cpp:118): every channel's factor
-      // and x; the generating channel keeps its own x and factor (phs.cu:1580-1585)
-      r = inverse_launch(W.proc, nk, W.dchb.as<int64_t>() + k * nch, uniform ? nullptr : dE1 + e0,
-                         uniform ? nullptr : dE2 + e0, pk, W.dok.as<uint8_t>() + e0, xk, df + e0,
-                         W.dfa.as<double>() + e0 * nch, xo, cs);
-      if (r) return r;
-      const cudaError_t ee = cudaEventRecord(W.done[k & 1], cs);
-      return ee == cudaSuccess ? PHS_OK : fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(ee));
-    };
-    // copies of chunk k into the caller's arrays: p[4 n_out i + ..], factors[n_channels i + c],
-    // x_out[n_x n c + n_x i + k], volumes, oks
-    auto copy_back = [&](int64_t k) -> cudaError_t {
-      const int64_t e0 = k * chunk, nk = std::min(n, e0 + chunk) - e0;
-      const double *xo = W.dxo.as<double>() + (size_t)(k & 1) * nch * chunk * n_x;
-      cudaError_t ee = cudaStreamWaitEvent(ms, W.done[k & 1], 0);
-      if (ee == cudaSuccess)
-        ee = cudaMemcpyAsync(p + e0 * 4 * n_out, W.dp.as<double>() + e0 * 4 * n_out,
-                             nk * 4 * n_out * sizeof(double), cudaMemcpyDeviceToHost, ms);
-      if (ee == cudaSuccess)
-        ee = cudaMemcpyAsync(factors + e0 * nch, W.dfa.as<double>() + e0 * nch,
-                             nk * nch * sizeof(double), cudaMemcpyDeviceToHost, ms);
-      if (ee == cudaSuccess && x_out)
-        ee = cudaMemcpy2DAsync(x_out + e0 * n_x, (size_t)n * n_x * sizeof(double), xo,
-                               (size_t)nk * n_x * sizeof(double), (size_t)nk * n_x * sizeof(double),
-                               nch, cudaMemcpyDeviceToHost, ms);
-      if (ee == cudaSuccess)
-        ee = cudaMemcpyAsync(volumes + e0, W.dv.as<double>() + e0, nk * sizeof(double),
-                             cudaMemcpyDeviceToHost, ms);
-      if (ee == cudaSuccess)
-        ee = cudaMemcpyAsync(oks + e0, W.dok.as<uint8_t>() + e0, nk, cudaMemcpyDeviceToHost, ms);
-      if (ee == cudaSuccess) ee = cudaStreamSynchronize(ms);
-      return ee;
-    };
-    for (int64_t k = 0; k <= n_chunks && rc == PHS_OK; k++) {
-      if (k < n_chunks) rc = compute(k);
-      if (rc == PHS_OK && k > 0) {
-        e = copy_back(k - 1);
-        if (e != cudaSuccess) rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
-      }
+    cudaStream_t cs[2] = {W.streams[0], W.streams[2]}, ms = W.streams[1];
+    double *dp = W.dp.as<double>(), *dv = W.dv.as<double>(), *dxo = W.dxo.as<double>();
+    uint8_t *dok = W.dok.as<uint8_t>();
+    rc = uniform ? phs_generate_device(W.proc, n, counts.data(), W.dx.as<double>(), dp, df, dv, dok, cs[0])
+                 : phs_generate_beams_device(W.proc, n, counts.data(), dE1, dE2, W.dx.as<double>(),
+                                             dp, df, dv, dok, cs[0]);
+    if (rc == PHS_OK && (e = cudaEventRecord(W.done[0], cs[0])) != cudaSuccess)
+      rc = fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(e));
+    if (rc == PHS_OK && (e = cudaStreamWaitEvent(cs[1], W.done[0], 0)) != cudaSuccess)
+      rc = fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(e));
+    if (rc == PHS_OK && (int)W.proc->inv_group_begin.size() < 2) rc = fail(PHS_ERR_STATE, "inverse map: channel groups not built");
+    if (rc) {
+      cudaStreamSynchronize(cs[0]);
+      break;
+    }
+    std::vector<int> slice = {0};
+    for (int k = 1; k < n_slices_max; k++) {
+      const double want = (double)nch * k / n_slices_max, half = 0.5 * nch / n_slices_max;
+      int cut = -1;
+      for (int32_t b : W.proc->inv_group_begin)
+        if (b > slice.back() && b < nch && (cut < 0 || fabs(b - want) < fabs(cut - want))) cut = b;
+      if (cut < 0 || fabs(cut - want) > half) cut = (int)llround(want);
+      if (cut > slice.back() && cut < nch) slice.push_back(cut);
+    }
+    slice.push_back(nch);
+    const int n_slices = (int)slice.size() - 1;
+    // launches: {first position, end position, first event, end event}
+    struct Unit { int lo, hi; int64_t e0, e1; };
+    std::vector<Unit> units;
+    for (int k = 0; k + 1 < n_slices; k++) units.push_back({slice[k], slice[k + 1], 0, n});
+    const int n_last = n_slices > 1 ? (int)std::min<int64_t>(kWhizardLastChunks, std::max<int64_t>(1, n >> 15)) : 1;
+    for (int j = 0; j < n_last; j++)
+      units.push_back({slice[n_slices - 1], nch, n * j / n_last, n * (j + 1) / n_last});
+    // channel starts relative to each launch's first event
+    std::vector<int64_t> begs((size_t)units.size() * nch);
+    for (size_t u = 0; u < units.size(); u++)
+      for (int c = 0; c < nch; c++) begs[u * nch + c] = beg[c] - units[u].e0;
+    if ((rc = W.dchb.reserve(begs.size() * sizeof(int64_t)))) break;
+    e = cudaMemcpy(W.dchb.ptr, begs.data(), begs.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy of channel starts: %s", cudaGetErrorString(e)); break; }
+    // do_inverse_mapping is forced on (whizard_gpu_phs.cpp:118): every channel's factor and
+    // x; the generating channel keeps its own x and factor (phs.cu:1580-1585), written with
+    // the other no-arithmetic outputs by the first launch (over every event)
+    for (size_t u = 0; u < units.size() && rc == PHS_OK; u++) {
+      const Unit &U = units[u];
+      const int64_t e0 = U.e0;
+      rc = inverse_launch(W.proc, U.e1 - e0, W.dchb.as<int64_t>() + u * nch,
+                          uniform ? nullptr : dE1 + e0, uniform ? nullptr : dE2 + e0,
+                          dp + e0 * 4 * n_out, dok + e0, W.dx.as<double>() + e0 * n_x, df + e0,
+                          W.dfa.as<double>() + e0 * nch, dxo + e0 * n_x, cs[u & 1], U.lo, U.hi,
+                          u == 0, n);
+      if (rc == PHS_OK && (e = cudaEventRecord(W.done[u + 1], cs[u & 1])) != cudaSuccess)
+        rc = fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(e));
     }
     if (rc) {
-      cudaStreamSynchronize(cs);
+      cudaStreamSynchronize(cs[0]);
+      cudaStreamSynchronize(cs[1]);
+      break;
+    }
+    const int32_t *order = W.proc->inv_order.data();
+    e = cudaStreamWaitEvent(ms, W.done[0], 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(p, dp, n * 4 * n_out * sizeof(double), cudaMemcpyDeviceToHost, ms);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(volumes, dv, n * sizeof(double), cudaMemcpyDeviceToHost, ms);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(oks, dok, n, cudaMemcpyDeviceToHost, ms);
+    // the copy stream waits for the launches in order: launch u's rows are copied after
+    // every launch up to u (the first one's fixed outputs included) is done
+    for (size_t u = 0; u < units.size() && e == cudaSuccess; u++) {
+      const Unit &U = units[u];
+      e = cudaStreamWaitEvent(ms, W.done[u + 1], 0);
+      for (int i = U.lo; i < U.hi && e == cudaSuccess && x_out; i++) {
+        const size_t off = ((size_t)order[i] * n + U.e0) * n_x;
+        e = cudaMemcpyAsync(x_out + off, dxo + off, (size_t)(U.e1 - U.e0) * n_x * sizeof(double),
+                            cudaMemcpyDeviceToHost, ms);
+      }
+      if (e == cudaSuccess && U.hi == nch)
+        e = cudaMemcpyAsync(factors + U.e0 * nch, W.dfa.as<double>() + U.e0 * nch,
+                            (size_t)(U.e1 - U.e0) * nch * sizeof(double), cudaMemcpyDeviceToHost, ms);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ms);
+    if (e != cudaSuccess) {
+      rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
+      cudaStreamSynchronize(cs[0]);
+      cudaStreamSynchronize(cs[1]);
       break;
     }
     W.last_events = n;

@@ -148,7 +148,7 @@ struct PhsInvLaunch {
   const double *x_own;         // [n][n_x]: the generating channel's x (copied), or null
   const double *factor_own;    // [n]: the generating channel's factor, or null
   double *all_factors;         // [n][n_channels]
-  double *x_out;               // [n_channels][n][n_x]
+  double *x_out;               // [n_channels][x_ch_stride][n_x], events 0 .. n - 1 of each
   // channels of equal tree shape (the geometry of the inverse map is the same for them):
   // group g is group_order[group_begin[g] .. group_begin[g + 1]), each channel once
   const int32_t *group_order;
@@ -157,7 +157,13 @@ struct PhsInvLaunch {
                                 // previous channel's (bit 3 visit + 0/1 daughter msq, + 2 ct);
                                 // null: no reuse (and no shared memory for it)
   int32_t n_groups;
+  // this launch inverts the channels at group_order positions [order_lo, order_hi) (all:
+  // 0, n_channels); write_fixed: it also writes every channel's outputs that need no
+  // arithmetic (own rows, x padding, ok = false events), which one launch of a split set does
+  int32_t order_lo, order_hi, write_fixed;
   int64_t n_events;
+  int64_t x_ch_stride;         // rows per channel in x_out (n_events, or more for a launch
+                               // over a range of the events of a longer array)
   int32_t n_channels, n_out, n_x, stack_depth, max_visits;
 };
 cudaError_t phs_launch_inverse(const PhsInvLaunch &a, int n_blocks, cudaStream_t stream);

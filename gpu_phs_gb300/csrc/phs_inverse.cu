@@ -358,8 +358,8 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
       own = lo;
       ok = a.ok ? a.ok[ev] != 0 : true;
       const double *xo = a.x_own ? a.x_own + ev * a.n_x : nullptr;
-      for (int c = 0; c < a.n_channels; c++) {
-        double *xr = a.x_out + ((int64_t)c * a.n_events + ev) * a.n_x;
+      for (int c = 0; c < (a.write_fixed ? a.n_channels : 0); c++) {
+        double *xr = a.x_out + ((int64_t)c * a.x_ch_stride + ev) * a.n_x;
         double *fo = a.all_factors + ev * a.n_channels + c;
         if (c == own && xo) {
           // the generating channel keeps its own x and factor (_move_x/_move_factors)
@@ -413,20 +413,22 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
         pm[(4 * k + 3) * PHS_INV_BLOCK + tid] = dadd(dmul(-lab_bg, e_x.x), dmul(lab_ga, y_z.y));
       }
       // the geometry once per tree shape, then the mappings of each channel of that shape
+      // (of this launch's slice of the group order)
       const bool has_own = a.x_own != nullptr;
       for (int g = 0; g < a.n_groups; g++) {
         const int gb = a.group_begin[g], ge = a.group_begin[g + 1];
-        if (has_own && ge - gb == 1 && a.group_order[gb] == own_e) continue;
+        const int lo = max(gb, a.order_lo), hi = min(ge, a.order_hi);
+        if (lo >= hi || (has_own && hi - lo == 1 && a.group_order[lo] == own_e)) continue;
         inverse_geometry(a.channels[a.group_order[gb]], pm + tid, sqrts, stk, geo + tid);
-        for (int i = gb; i < ge; i++) {
+        for (int i = lo; i < hi; i++) {
           const int c = a.group_order[i];
           // the generating channel keeps its own row, but its mappings still run when a
           // later channel of the shape reuses them
           const bool own_row = c == own_e && has_own;
-          if (own_row && (!cache || i + 1 == ge || a.group_reuse[i + 1] == 0)) continue;
-          double *xr = own_row ? nullptr : a.x_out + ((int64_t)c * a.n_events + e) * a.n_x;
-          // the first channel of a shape computes every mapping
-          const uint64_t reuse = i == gb || !cache ? 0ull : a.group_reuse[i];
+          if (own_row && (!cache || i + 1 == hi || a.group_reuse[i + 1] == 0)) continue;
+          double *xr = own_row ? nullptr : a.x_out + ((int64_t)c * a.x_ch_stride + e) * a.n_x;
+          // the first channel of a shape (or of the slice) computes every mapping
+          const uint64_t reuse = i == lo || !cache ? 0ull : a.group_reuse[i];
           const double fac = inverse_maps<PER_EVENT>(a.channels[c], sqrts, geo + tid,
                                                      cache ? cache + tid : nullptr, xr, reuse);
           if (!own_row) a.all_factors[e * a.n_channels + c] = fac;

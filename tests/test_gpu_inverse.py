@@ -241,11 +241,12 @@ def test_whizard_abi_all_channels(torch):
 
 
 @pytest.mark.parametrize("beams", ["uniform", "per_event"])
-def test_whizard_abi_chunked_call_equals_handle_api(torch, beams):
-    """100 000 bwbw events through c_whizard_gen_phs_from_x_gpu, which pipelines chunks of
-    events (compute of one chunk beside the copies of the previous): momenta, every
-    channel's factors and x, volumes and ok flags equal the handle API's forward and
-    inverse calls on the whole batch, bit for bit."""
+def test_whizard_abi_pipelined_call_equals_handle_api(torch, beams):
+    """100 000 bwbw events through c_whizard_gen_phs_from_x_gpu, which runs the inverse map
+    in launches over slices of the channels (the last slice in chunks of events) beside the
+    copies of the finished ones: momenta, every channel's factors and x, volumes and ok
+    flags equal the handle API's forward and inverse calls on the whole batch (one inverse
+    launch), bit for bit."""
     from gpu_phs_gb300 import _lib
     from gpu_phs_gb300.api import PhaseSpace
     lib = _lib.load()
