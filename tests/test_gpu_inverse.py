@@ -240,18 +240,14 @@ def test_whizard_abi_all_channels(torch):
     lib.c_whizard_finalize_gpu_phs()
 
 
-@pytest.mark.parametrize("beams", ["uniform", "per_event"])
-def test_whizard_abi_pipelined_call_equals_handle_api(torch, beams):
-    """100 000 bwbw events through c_whizard_gen_phs_from_x_gpu, which runs the inverse map
-    in launches over slices of the channels (the last slice in chunks of events) beside the
-    copies of the finished ones: momenta, every channel's factors and x, volumes and ok
-    flags equal the handle API's forward and inverse calls on the whole batch (one inverse
-    launch), bit for bit."""
+def whizard_call_vs_handle_api(torch, name, n, counts, beams):
+    """n events of the sample process `name` (events per channel `counts`) through
+    c_whizard_gen_phs_from_x_gpu and through the handle API's forward and inverse calls on
+    the whole batch: every output equal bit for bit."""
     from gpu_phs_gb300 import _lib
     from gpu_phs_gb300.api import PhaseSpace
     lib = _lib.load()
-    z = golden("whizard_bwbw")
-    proc = load_process(z)
+    proc = load_process(golden(f"whizard_{name}"))
     ip = lambda v: C.byref(C.c_int(v))
     nch, n_x, n_out = proc.n_channels, proc.n_x, proc.n_out
     lib.c_whizard_set_particle_structure(ip(nch), ip(nch), ip(nch), ip(n_x), ip(2), ip(n_out))
@@ -271,13 +267,10 @@ def test_whizard_abi_pipelined_call_equals_handle_api(torch, beams):
         keep += a
         lib.c_whizard_fill_tree_structure(ip(c + 1), *[t.ctypes.data for t in a])
     lib.c_whizard_init_gpu_phs()
-    n = 100_000
-    rng = np.random.default_rng(17)
-    counts = rng.multinomial(n, np.full(nch, 1.0 / nch)).astype(np.int64)
-    counts[5] = 0                                      # an empty channel inside
-    counts[0] += n - int(counts.sum())
+    assert int(counts.sum()) == n
     limits = np.ascontiguousarray(np.cumsum(counts), np.int32)
     lib.c_whizard_init_channel_ids(ip(n), ip(nch), limits.ctypes.data)
+    rng = np.random.default_rng(17)
     x = np.ascontiguousarray(uniform_x(18, n, n_x))
     if beams == "uniform":
         E1, E2 = np.full(n, 500.0), np.full(n, 500.0)
@@ -308,3 +301,25 @@ def test_whizard_abi_pipelined_call_equals_handle_api(torch, beams):
     assert np.array_equal(oks, ev.ok.cpu().numpy())
     assert np.array_equal(factors.reshape(n, nch), fa.cpu().numpy())
     assert np.array_equal(x_out.reshape(nch, n, n_x), xo.cpu().numpy())
+
+
+@pytest.mark.parametrize("beams", ["uniform", "per_event"])
+def test_whizard_abi_pipelined_call_equals_handle_api(torch, beams):
+    """100 000 bwbw events (61 channels, one of them empty) through
+    c_whizard_gen_phs_from_x_gpu, which runs the inverse map in launches over slices of the
+    channels (the last slice in chunks of events) beside the copies of the finished ones:
+    momenta, every channel's factors and x, volumes and ok flags equal the handle API's
+    forward and inverse calls on the whole batch (one inverse launch), bit for bit."""
+    n, nch = 100_000, 61
+    counts = np.random.default_rng(17).multinomial(n, np.full(nch, 1.0 / nch)).astype(np.int64)
+    counts[5] = 0                                      # an empty channel inside
+    counts[0] += n - int(counts.sum())
+    whizard_call_vs_handle_api(torch, "bwbw", n, counts, beams)
+
+
+def test_whizard_abi_pipelined_call_few_channels(torch):
+    """ttH (3 channels, fewer than the call's slices), 400 000 events with the first channel
+    empty: one slice per channel, the last one in chunks of uneven events; equal to the
+    handle API bit for bit."""
+    whizard_call_vs_handle_api(torch, "ttH", 400_000, np.array([0, 300_001, 99_999], np.int64),
+                               "uniform")
