@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/gpu_phs.h"
@@ -1222,6 +1223,10 @@ constexpr int kWhizardSlices = 8;
 // are final when it ends, and their copy overlaps the next chunk.
 constexpr int kWhizardLastChunks = 4;
 constexpr int kWhizardLaunches = kWhizardSlices - 1 + kWhizardLastChunks;
+// The forward map of a Whizard call runs in up to this many chunks of events, each of at
+// least kWhizardChunkMin events (a launch that fills the GPU).
+constexpr int kWhizardChunks = 8;
+constexpr int64_t kWhizardChunkMin = 1 << 18;
 struct Whizard {
   std::mutex mu;
   int n_channels = 0, n_trees = 0, n_groves = 0, n_x = 0, n_in = 0, n_out = 0;
@@ -1234,11 +1239,12 @@ struct Whizard {
   int64_t batch_size = 0;
   phs_process_t proc = nullptr;
   DevBuf dx, dp, df, dv, dok;
-  DevBuf dfa, dxo;  // all-channel factors and x of the inverse map
+  DevBuf dfa, dxo;  // all-channel factors and x of the inverse map (more than one channel)
   DevBuf dsparse, din;  // device handoff in the reference's layouts, built on request
-  DevBuf dchb;          // each channel's first event
-  cudaStream_t streams[3] = {nullptr, nullptr, nullptr};  // compute, copies, compute
+  DevBuf dchb;          // per inverse launch, each channel's first event relative to its own
+  cudaStream_t streams[4] = {};                 // compute, copies back, compute, copies in
   cudaEvent_t done[kWhizardLaunches + 1] = {};  // the forward map, each inverse launch done
+  cudaEvent_t x_in[kWhizardChunks] = {}, fwd[kWhizardChunks] = {};  // per forward chunk
   bool sparse_ok = false, in_ok = false, last_uniform = true;
   double last_e1 = 0, last_e2 = 0;
   std::vector<uint32_t> internal;  // bit code: an internal branch of some channel
@@ -1246,6 +1252,26 @@ struct Whizard {
   int msq_threads = 0, cb_threads = 0, ab_threads = 0;
 };
 Whizard W;
+
+// Whether every event has the first event's beams (the process's compiled constants serve
+// them all); large arrays are scanned by several host threads.
+bool beams_uniform(const double *E1, const double *E2, int64_t n) {
+  auto scan = [&](int64_t lo, int64_t hi) {
+    for (int64_t i = lo; i < hi; i++)
+      if (E1[i] != E1[0] || E2[i] != E2[0]) return false;
+    return true;
+  };
+  const int64_t per = 1 << 20;
+  const int n_threads = (int)std::min<int64_t>(16, (n + per - 1) / per);
+  if (n_threads <= 1) return scan(0, n);
+  std::vector<char> ok(n_threads, 1);
+  std::vector<std::thread> th;
+  for (int t = 1; t < n_threads; t++)
+    th.emplace_back([&, t] { ok[t] = scan(n * t / n_threads, n * (t + 1) / n_threads); });
+  ok[0] = scan(0, n / n_threads);
+  for (auto &t : th) t.join();
+  return std::all_of(ok.begin(), ok.end(), [](char v) { return v != 0; });
+}
 
 void whizard_log(int rc) {
   if (rc) fprintf(stderr, "gpu_phs: %s\n", g_err.c_str());
@@ -1397,9 +1423,12 @@ extern "C" void c_whizard_finalize_gpu_phs(void) {
     if (st) cudaStreamDestroy(st);
     st = nullptr;
   }
-  for (cudaEvent_t &ev : W.done) {
-    if (ev) cudaEventDestroy(ev);
-    ev = nullptr;
+  for (cudaEvent_t *evs : {W.done, W.x_in, W.fwd}) {
+    const int m = evs == W.done ? kWhizardLaunches + 1 : kWhizardChunks;
+    for (int i = 0; i < m; i++) {
+      if (evs[i]) cudaEventDestroy(evs[i]);
+      evs[i] = nullptr;
+    }
   }
   W.map_id.clear(); W.map_m.clear(); W.map_w.clear();
   W.d1.clear(); W.d2.clear(); W.hc.clear(); W.fr.clear();
@@ -1439,116 +1468,164 @@ extern "C" void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in,
                 "events, not %lld", (long long)sum, (long long)n);
       break;
     }
-    bool uniform = true;
-    for (int64_t i = 1; i < n && uniform; i++) uniform = E1_in[i] == E1_in[0] && E2_in[i] == E2_in[0];
+    const bool uniform = beams_uniform(E1_in, E2_in, n);
     DeviceGuard g(W.proc->device);
     if ((rc = W.dx.reserve(n * n_x * sizeof(double)))) break;
     if ((rc = W.dp.reserve(n * 4 * n_out * sizeof(double)))) break;
     if ((rc = W.df.reserve(n * sizeof(double) * (uniform ? 1 : 3)))) break;
     if ((rc = W.dv.reserve(n * sizeof(double)))) break;
     if ((rc = W.dok.reserve(n))) break;
-    if ((rc = W.dfa.reserve((size_t)n * nch * sizeof(double)))) break;
-    cudaError_t e = cudaMemcpy(W.dx.ptr, x, n * n_x * sizeof(double), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy of x: %s", cudaGetErrorString(e)); break; }
-    double *df = W.df.as<double>();
-    const double *dE1 = nullptr, *dE2 = nullptr;
-    if (uniform) {
-      if ((rc = phs_process_set_beams(W.proc, E1_in[0], E2_in[0]))) break;
-    } else {
-      e = cudaMemcpy(df + n, E1_in, n * sizeof(double), cudaMemcpyHostToDevice);
-      if (e == cudaSuccess) e = cudaMemcpy(df + 2 * n, E2_in, n * sizeof(double), cudaMemcpyHostToDevice);
-      if (e != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy of beams: %s", cudaGetErrorString(e)); break; }
-      dE1 = df + n;
-      dE2 = df + 2 * n;
-    }
-    // The forward map of every event, then the inverse map (factors [n][n_channels], x
-    // [n_channels][n][n_x]) in launches over slices of the channels in the order of the
-    // tree-shape groups (cut where a group ends, if one ends near the even cut: the geometry
-    // of a shape is computed once per event and launch), each over every event so that it
-    // fills the GPU, the last slice in chunks of events; the launches alternate over two
-    // compute streams, so that one's tail overlaps the next one's start.  Everything is
-    // queued first; the copies into the caller's arrays then follow on the copy stream (a
-    // copy into pageable memory returns when done): the momenta, volumes and ok flags after
-    // the forward map, each launch's x rows (contiguous per channel on both sides) beside
-    // the following kernels, and after each chunk of the last slice the factors of its
-    // events, which every earlier launch has finished.
-    const int n_slices_max = (int64_t)n * nch < (1 << 20) ? 1 : std::min(nch, kWhizardSlices);
-    std::vector<int64_t> beg(nch, 0);
-    for (int c = 1; c < nch; c++) beg[c] = beg[c - 1] + counts[c - 1];
-    if ((rc = W.dxo.reserve((size_t)nch * n * n_x * sizeof(double)))) break;
-    for (int i = 0; i < 3 && e == cudaSuccess; i++)
+    if (nch > 1 && (rc = W.dfa.reserve((size_t)n * nch * sizeof(double)))) break;
+    if (nch > 1 && (rc = W.dxo.reserve((size_t)nch * n * n_x * sizeof(double)))) break;
+    if (uniform && (rc = phs_process_set_beams(W.proc, E1_in[0], E2_in[0]))) break;
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 4 && e == cudaSuccess; i++)
       if (!W.streams[i]) e = cudaStreamCreateWithFlags(&W.streams[i], cudaStreamNonBlocking);
-    for (int i = 0; i < kWhizardLaunches + 1 && e == cudaSuccess; i++)
+    for (int i = 0; i <= kWhizardLaunches && e == cudaSuccess; i++)
       if (!W.done[i]) e = cudaEventCreateWithFlags(&W.done[i], cudaEventDisableTiming);
+    for (int i = 0; i < kWhizardChunks && e == cudaSuccess; i++) {
+      if (!W.x_in[i]) e = cudaEventCreateWithFlags(&W.x_in[i], cudaEventDisableTiming);
+      if (e == cudaSuccess && !W.fwd[i]) e = cudaEventCreateWithFlags(&W.fwd[i], cudaEventDisableTiming);
+    }
     if (e != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "set-up: %s", cudaGetErrorString(e)); break; }
-    cudaStream_t cs[2] = {W.streams[0], W.streams[2]}, ms = W.streams[1];
-    double *dp = W.dp.as<double>(), *dv = W.dv.as<double>(), *dxo = W.dxo.as<double>();
+    cudaStream_t cs[2] = {W.streams[0], W.streams[2]}, ms = W.streams[1], hs = W.streams[3];
+    double *dx = W.dx.as<double>(), *dp = W.dp.as<double>(), *df = W.df.as<double>();
+    double *dv = W.dv.as<double>(), *dxo = W.dxo.as<double>();
     uint8_t *dok = W.dok.as<uint8_t>();
-    rc = uniform ? phs_generate_device(W.proc, n, counts.data(), W.dx.as<double>(), dp, df, dv, dok, cs[0])
-                 : phs_generate_beams_device(W.proc, n, counts.data(), dE1, dE2, W.dx.as<double>(),
-                                             dp, df, dv, dok, cs[0]);
-    if (rc == PHS_OK && (e = cudaEventRecord(W.done[0], cs[0])) != cudaSuccess)
-      rc = fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(e));
-    if (rc == PHS_OK && (e = cudaStreamWaitEvent(cs[1], W.done[0], 0)) != cudaSuccess)
-      rc = fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(e));
-    if (rc == PHS_OK && (int)W.proc->inv_group_begin.size() < 2) rc = fail(PHS_ERR_STATE, "inverse map: channel groups not built");
+    const double *dE1 = uniform ? nullptr : df + n, *dE2 = uniform ? nullptr : df + 2 * n;
+    // The forward map in chunks of events: the copy in of chunk k + 1 (on its own stream;
+    // a copy from pageable memory returns when done) and the copies back of chunk k - 1
+    // (momenta, volumes, ok flags; with one channel also its x and factors, which are the
+    // input's and the forward map's) run beside the kernels of chunk k.
+    const int64_t fchunk = std::max<int64_t>(kWhizardChunkMin, (n + kWhizardChunks - 1) / kWhizardChunks);
+    const int n_fchunks = (int)((n + fchunk - 1) / fchunk);
+    std::vector<int64_t> beg(nch, 0), fcnt((size_t)n_fchunks * nch, 0);
+    for (int c = 1; c < nch; c++) beg[c] = beg[c - 1] + counts[c - 1];
+    for (int c = 0; c < nch; c++)
+      for (int k = 0; k < n_fchunks; k++) {
+        const int64_t e0 = k * fchunk, e1 = std::min(n, e0 + fchunk);
+        fcnt[(size_t)k * nch + c] =
+            std::max<int64_t>(0, std::min(e1, beg[c] + counts[c]) - std::max(e0, beg[c]));
+      }
+    auto copy_in = [&](int k) -> cudaError_t {
+      const int64_t e0 = k * fchunk, nk = std::min(n, e0 + fchunk) - e0;
+      cudaError_t ee = cudaMemcpyAsync(dx + e0 * n_x, x + e0 * n_x, nk * n_x * sizeof(double),
+                                       cudaMemcpyHostToDevice, hs);
+      if (ee == cudaSuccess && !uniform)
+        ee = cudaMemcpyAsync(df + n + e0, E1_in + e0, nk * sizeof(double), cudaMemcpyHostToDevice, hs);
+      if (ee == cudaSuccess && !uniform)
+        ee = cudaMemcpyAsync(df + 2 * n + e0, E2_in + e0, nk * sizeof(double), cudaMemcpyHostToDevice, hs);
+      return ee == cudaSuccess ? cudaEventRecord(W.x_in[k], hs) : ee;
+    };
+    auto forward = [&](int k) -> int {
+      const int64_t e0 = k * fchunk, nk = std::min(n, e0 + fchunk) - e0;
+      const int64_t *ck = fcnt.data() + (size_t)k * nch;
+      cudaError_t ee = cudaStreamWaitEvent(cs[0], W.x_in[k], 0);
+      if (ee != cudaSuccess) return fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(ee));
+      int r = uniform
+          ? phs_generate_device(W.proc, nk, ck, dx + e0 * n_x, dp + e0 * 4 * n_out, df + e0,
+                                dv + e0, dok + e0, cs[0])
+          : phs_generate_beams_device(W.proc, nk, ck, dE1 + e0, dE2 + e0, dx + e0 * n_x,
+                                      dp + e0 * 4 * n_out, df + e0, dv + e0, dok + e0, cs[0]);
+      if (r) return r;
+      ee = cudaEventRecord(W.fwd[k], cs[0]);
+      return ee == cudaSuccess ? PHS_OK : fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(ee));
+    };
+    auto copy_back = [&](int k) -> cudaError_t {
+      const int64_t e0 = k * fchunk, nk = std::min(n, e0 + fchunk) - e0;
+      cudaError_t ee = cudaStreamWaitEvent(ms, W.fwd[k], 0);
+      if (ee == cudaSuccess)
+        ee = cudaMemcpyAsync(p + e0 * 4 * n_out, dp + e0 * 4 * n_out, nk * 4 * n_out * sizeof(double),
+                             cudaMemcpyDeviceToHost, ms);
+      if (ee == cudaSuccess)
+        ee = cudaMemcpyAsync(volumes + e0, dv + e0, nk * sizeof(double), cudaMemcpyDeviceToHost, ms);
+      if (ee == cudaSuccess) ee = cudaMemcpyAsync(oks + e0, dok + e0, nk, cudaMemcpyDeviceToHost, ms);
+      // one channel: the generating channel keeps its own x and factor (phs.cu:1580-1585)
+      if (ee == cudaSuccess && nch == 1 && x_out)
+        ee = cudaMemcpyAsync(x_out + e0 * n_x, dx + e0 * n_x, nk * n_x * sizeof(double),
+                             cudaMemcpyDeviceToHost, ms);
+      if (ee == cudaSuccess && nch == 1)
+        ee = cudaMemcpyAsync(factors + e0, df + e0, nk * sizeof(double), cudaMemcpyDeviceToHost, ms);
+      return ee;
+    };
+    if ((e = copy_in(0)) != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy in: %s", cudaGetErrorString(e)); break; }
+    if ((rc = forward(0))) { cudaStreamSynchronize(cs[0]); break; }
+    for (int k = 1; k < n_fchunks && rc == PHS_OK; k++) {
+      if ((e = copy_in(k)) != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy in: %s", cudaGetErrorString(e)); break; }
+      if ((rc = forward(k))) break;
+      if ((e = copy_back(k - 1)) != cudaSuccess) rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
+    }
     if (rc) {
+      cudaStreamSynchronize(hs);
       cudaStreamSynchronize(cs[0]);
+      cudaStreamSynchronize(ms);
       break;
     }
-    std::vector<int> slice = {0};
-    for (int k = 1; k < n_slices_max; k++) {
-      const double want = (double)nch * k / n_slices_max, half = 0.5 * nch / n_slices_max;
-      int cut = -1;
-      for (int32_t b : W.proc->inv_group_begin)
-        if (b > slice.back() && b < nch && (cut < 0 || fabs(b - want) < fabs(cut - want))) cut = b;
-      if (cut < 0 || fabs(cut - want) > half) cut = (int)llround(want);
-      if (cut > slice.back() && cut < nch) slice.push_back(cut);
-    }
-    slice.push_back(nch);
-    const int n_slices = (int)slice.size() - 1;
-    // launches: {first position, end position, first event, end event}
+    // More than one channel: the inverse map (factors [n][n_channels], x [n_channels][n][n_x])
+    // in launches over slices of the channels in the order of the tree-shape groups (cut
+    // where a group ends, if one ends near the even cut: the geometry of a shape is computed
+    // once per event and launch), each over every event so that it fills the GPU, the last
+    // slice in chunks of events; the launches alternate over two compute streams, so that
+    // one's tail overlaps the next one's start.  They are queued before the last forward
+    // chunk's copies back; the copies of each launch's x rows (contiguous per channel on both
+    // sides) then run beside the later kernels, and after each chunk of the last slice the
+    // factors of its events, which every earlier launch has finished.
     struct Unit { int lo, hi; int64_t e0, e1; };
     std::vector<Unit> units;
-    for (int k = 0; k + 1 < n_slices; k++) units.push_back({slice[k], slice[k + 1], 0, n});
-    const int n_last = n_slices > 1 ? (int)std::min<int64_t>(kWhizardLastChunks, std::max<int64_t>(1, n >> 15)) : 1;
-    for (int j = 0; j < n_last; j++)
-      units.push_back({slice[n_slices - 1], nch, n * j / n_last, n * (j + 1) / n_last});
-    // channel starts relative to each launch's first event
-    std::vector<int64_t> begs((size_t)units.size() * nch);
-    for (size_t u = 0; u < units.size(); u++)
-      for (int c = 0; c < nch; c++) begs[u * nch + c] = beg[c] - units[u].e0;
-    if ((rc = W.dchb.reserve(begs.size() * sizeof(int64_t)))) break;
-    e = cudaMemcpy(W.dchb.ptr, begs.data(), begs.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy of channel starts: %s", cudaGetErrorString(e)); break; }
-    // do_inverse_mapping is forced on (whizard_gpu_phs.cpp:118): every channel's factor and
-    // x; the generating channel keeps its own x and factor (phs.cu:1580-1585), written with
-    // the other no-arithmetic outputs by the first launch (over every event)
-    for (size_t u = 0; u < units.size() && rc == PHS_OK; u++) {
-      const Unit &U = units[u];
-      const int64_t e0 = U.e0;
-      rc = inverse_launch(W.proc, U.e1 - e0, W.dchb.as<int64_t>() + u * nch,
-                          uniform ? nullptr : dE1 + e0, uniform ? nullptr : dE2 + e0,
-                          dp + e0 * 4 * n_out, dok + e0, W.dx.as<double>() + e0 * n_x, df + e0,
-                          W.dfa.as<double>() + e0 * nch, dxo + e0 * n_x, cs[u & 1], U.lo, U.hi,
-                          u == 0, n);
-      if (rc == PHS_OK && (e = cudaEventRecord(W.done[u + 1], cs[u & 1])) != cudaSuccess)
-        rc = fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(e));
+    if (nch > 1) {
+      if ((int)W.proc->inv_group_begin.size() < 2 || (int)W.proc->inv_order.size() != nch) {
+        rc = fail(PHS_ERR_STATE, "inverse map: channel groups not built");
+        cudaStreamSynchronize(cs[0]);
+        cudaStreamSynchronize(ms);
+        break;
+      }
+      const int n_slices_max = (int64_t)n * nch < (1 << 20) ? 1 : std::min(nch, kWhizardSlices);
+      std::vector<int> slice = {0};
+      for (int k = 1; k < n_slices_max; k++) {
+        const double want = (double)nch * k / n_slices_max, half = 0.5 * nch / n_slices_max;
+        int cut = -1;
+        for (int32_t b : W.proc->inv_group_begin)
+          if (b > slice.back() && b < nch && (cut < 0 || fabs(b - want) < fabs(cut - want))) cut = b;
+        if (cut < 0 || fabs(cut - want) > half) cut = (int)llround(want);
+        if (cut > slice.back() && cut < nch) slice.push_back(cut);
+      }
+      slice.push_back(nch);
+      const int n_slices = (int)slice.size() - 1;
+      for (int k = 0; k + 1 < n_slices; k++) units.push_back({slice[k], slice[k + 1], 0, n});
+      const int n_last =
+          n_slices > 1 ? (int)std::min<int64_t>(kWhizardLastChunks, std::max<int64_t>(1, n >> 15)) : 1;
+      for (int j = 0; j < n_last; j++)
+        units.push_back({slice[n_slices - 1], nch, n * j / n_last, n * (j + 1) / n_last});
+      // channel starts relative to each launch's first event
+      std::vector<int64_t> begs((size_t)units.size() * nch);
+      for (size_t u = 0; u < units.size(); u++)
+        for (int c = 0; c < nch; c++) begs[u * nch + c] = beg[c] - units[u].e0;
+      if ((rc = W.dchb.reserve(begs.size() * sizeof(int64_t)))) { cudaStreamSynchronize(cs[0]); break; }
+      e = cudaMemcpyAsync(W.dchb.ptr, begs.data(), begs.size() * sizeof(int64_t), cudaMemcpyHostToDevice, cs[0]);
+      if (e == cudaSuccess) e = cudaEventRecord(W.done[0], cs[0]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(cs[1], W.done[0], 0);
+      if (e != cudaSuccess) rc = fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(e));
+      // do_inverse_mapping is forced on (whizard_gpu_phs.cpp:118): every channel's factor
+      // and x; the generating channel keeps its own x and factor (phs.cu:1580-1585), written
+      // with the other no-arithmetic outputs by the first launch (over every event)
+      for (size_t u = 0; u < units.size() && rc == PHS_OK; u++) {
+        const Unit &U = units[u];
+        const int64_t e0 = U.e0;
+        rc = inverse_launch(W.proc, U.e1 - e0, W.dchb.as<int64_t>() + u * nch,
+                            uniform ? nullptr : dE1 + e0, uniform ? nullptr : dE2 + e0,
+                            dp + e0 * 4 * n_out, dok + e0, dx + e0 * n_x, df + e0,
+                            W.dfa.as<double>() + e0 * nch, dxo + e0 * n_x, cs[u & 1], U.lo, U.hi,
+                            u == 0, n);
+        if (rc == PHS_OK && (e = cudaEventRecord(W.done[u + 1], cs[u & 1])) != cudaSuccess)
+          rc = fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(e));
+      }
     }
-    if (rc) {
-      cudaStreamSynchronize(cs[0]);
-      cudaStreamSynchronize(cs[1]);
-      break;
-    }
+    if (rc == PHS_OK && (e = copy_back(n_fchunks - 1)) != cudaSuccess)
+      rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
     const int32_t *order = W.proc->inv_order.data();
-    e = cudaStreamWaitEvent(ms, W.done[0], 0);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(p, dp, n * 4 * n_out * sizeof(double), cudaMemcpyDeviceToHost, ms);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(volumes, dv, n * sizeof(double), cudaMemcpyDeviceToHost, ms);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(oks, dok, n, cudaMemcpyDeviceToHost, ms);
     // the copy stream waits for the launches in order: launch u's rows are copied after
     // every launch up to u (the first one's fixed outputs included) is done
-    for (size_t u = 0; u < units.size() && e == cudaSuccess; u++) {
+    for (size_t u = 0; u < units.size() && rc == PHS_OK && e == cudaSuccess; u++) {
       const Unit &U = units[u];
       e = cudaStreamWaitEvent(ms, W.done[u + 1], 0);
       for (int i = U.lo; i < U.hi && e == cudaSuccess && x_out; i++) {
@@ -1559,12 +1636,12 @@ extern "C" void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in,
       if (e == cudaSuccess && U.hi == nch)
         e = cudaMemcpyAsync(factors + U.e0 * nch, W.dfa.as<double>() + U.e0 * nch,
                             (size_t)(U.e1 - U.e0) * nch * sizeof(double), cudaMemcpyDeviceToHost, ms);
+      if (e != cudaSuccess) rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
     }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ms);
-    if (e != cudaSuccess) {
+    if (rc == PHS_OK && (e = cudaStreamSynchronize(ms)) != cudaSuccess)
       rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
-      cudaStreamSynchronize(cs[0]);
-      cudaStreamSynchronize(cs[1]);
+    if (rc) {
+      for (cudaStream_t st : W.streams) cudaStreamSynchronize(st);
       break;
     }
     W.last_events = n;

@@ -241,13 +241,14 @@ def test_whizard_abi_all_channels(torch):
 
 
 def whizard_call_vs_handle_api(torch, name, n, counts, beams):
-    """n events of the sample process `name` (events per channel `counts`) through
-    c_whizard_gen_phs_from_x_gpu and through the handle API's forward and inverse calls on
-    the whole batch: every output equal bit for bit."""
+    """n events of the process `name` (a sample file's, or a builder of processes.py;
+    events per channel `counts`) through c_whizard_gen_phs_from_x_gpu and through the
+    handle API's forward and inverse calls on the whole batch: every output equal bit for
+    bit."""
     from gpu_phs_gb300 import _lib
     from gpu_phs_gb300.api import PhaseSpace
     lib = _lib.load()
-    proc = load_process(golden(f"whizard_{name}"))
+    proc = getattr(P, name)() if hasattr(P, name) else load_process(golden(f"whizard_{name}"))
     ip = lambda v: C.byref(C.c_int(v))
     nch, n_x, n_out = proc.n_channels, proc.n_x, proc.n_out
     lib.c_whizard_set_particle_structure(ip(nch), ip(nch), ip(nch), ip(n_x), ip(2), ip(n_out))
@@ -315,6 +316,14 @@ def test_whizard_abi_pipelined_call_equals_handle_api(torch, beams):
     counts[5] = 0                                      # an empty channel inside
     counts[0] += n - int(counts.sum())
     whizard_call_vs_handle_api(torch, "bwbw", n, counts, beams)
+
+
+@pytest.mark.parametrize("beams", ["uniform", "per_event"])
+def test_whizard_abi_one_channel_chunked(torch, beams):
+    """The tt tree alone (one channel), 600 001 events: the forward map runs in chunks of
+    events with the copies in and back beside the kernels, x and factors of the one channel
+    come from the input and the forward map; equal to the handle API bit for bit."""
+    whizard_call_vs_handle_api(torch, "tt", 600_001, np.array([600_001], np.int64), beams)
 
 
 def test_whizard_abi_pipelined_call_few_channels(torch):
