@@ -370,10 +370,11 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64, pin=
     return res
 
 
-def whizard_abi_rate(proc, n: int, steps: int) -> dict:
+def whizard_abi_rate(proc, n: int, steps: int, x_host=None) -> dict:
     """The drop-in call as Whizard makes it: the 14-symbol C ABI set up for the process,
-    then c_whizard_gen_phs_from_x_gpu on host arrays (x in; momenta, every channel's factor
-    and x, volumes and ok flags out), host wall clock per call."""
+    then c_whizard_gen_phs_from_x_gpu on host arrays (x in, x_host or Philox seed SEED;
+    momenta, every channel's factor and x, volumes and ok flags out), host wall clock per
+    call."""
     import ctypes as C
     from gpu_phs_gb300 import _lib
     from gpu_phs_gb300.philox import uniform_x
@@ -399,7 +400,7 @@ def whizard_abi_rate(proc, n: int, steps: int) -> dict:
     counts[: n - int(counts.sum())] += 1
     limits = np.ascontiguousarray(np.cumsum(counts), np.int32)
     lib.c_whizard_init_channel_ids(ip(n), ip(nch), limits.ctypes.data)
-    x = np.ascontiguousarray(uniform_x(SEED, n, n_x))
+    x = np.ascontiguousarray(uniform_x(SEED, n, n_x) if x_host is None else x_host)
     E1, E2 = np.full(n, proc.sqrts / 2), np.full(n, proc.sqrts / 2)
     factors, volumes = np.zeros(n * nch), np.zeros(n)
     oks = np.zeros(n, np.uint8)
@@ -423,7 +424,7 @@ def whizard_abi_rate(proc, n: int, steps: int) -> dict:
     out_bytes = n * (32 * n_out + 8 * nch + 8 + 1 + 8 * n_x * nch)
     return {"n_events": n, "n_channels": nch, "ms_per_call": dt * 1e3,
             "events_per_s": n / dt, "channel_inversions_per_s": n * nch / dt,
-            "h2d_bytes_per_call": n * (8 * n_x + 16), "d2h_bytes_per_call": out_bytes,
+            "h2d_bytes_per_call": n * 8 * n_x, "d2h_bytes_per_call": out_bytes,
             "error": err or None,
             "path": "c_whizard_gen_phs_from_x_gpu (host arrays): forward, all-channel inverse, "
                     "copies back of momenta, factors [n][61], x [61][n][n_x], volumes, ok"}
@@ -629,6 +630,20 @@ def run_ours(args):
                "path": "phs_generate_host (C ABI), pinned host buffers, 512 Ki-event chunks on 3 streams",
                "steps": e2e_steps}
 
+    # the drop-in call, c_whizard_gen_phs_from_x_gpu, on the same workload with the host
+    # arrays Whizard passes (pageable): x in; momenta, volumes, ok flags and, as its forced
+    # inverse mapping adds, every channel's x and factor (one channel: the input x and the
+    # forward factor) out
+    e2e_abi = None
+    if not args.no_e2e and world == 1:
+        r = whizard_abi_rate(proc, n, max(2, min(args.steps, 5)), x.cpu().numpy())
+        e2e_abi = {"value": r["events_per_s"], "unit": "events/s",
+                   "h2d_bytes_per_step": r["h2d_bytes_per_call"],
+                   "d2h_bytes_per_step": r["d2h_bytes_per_call"], "ms_per_call": r["ms_per_call"],
+                   "error": r["error"],
+                   "path": "c_whizard_gen_phs_from_x_gpu (the reference's C ABI), pageable host "
+                           "arrays, equal beams (read on the host, not copied)"}
+
     variants = None
     if not args.no_variants and world == 1:
         variants = measure_variants(torch, args.steps, args.warmup, x, out, ms_per_step,
@@ -673,6 +688,7 @@ def run_ours(args):
                                           "instructions the library math expands into"}},
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "e2e_whizard_abi": e2e_abi,
             "variants": variants,
             "gpu_launches": args.steps,
             "clocks": clocks,
