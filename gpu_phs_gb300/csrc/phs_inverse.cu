@@ -336,16 +336,20 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
   const int64_t n_tiles = (a.n_events + PHS_INV_BLOCK - 1) / PHS_INV_BLOCK;
   const PhsChannel &ch0 = a.channels[0];
 
-  __shared__ int64_t dense_ev[PHS_INV_BLOCK];  // the tile's ok events, packed
-  __shared__ int dense_own[PHS_INV_BLOCK];
+  // the ok events of this block's tiles, queued: a walk takes PHS_INV_BLOCK of them at a
+  // time, so every thread has an event (the rest, fewer, wait for the next tile)
+  __shared__ int64_t q_ev[2 * PHS_INV_BLOCK];
+  __shared__ int q_own[2 * PHS_INV_BLOCK];
   __shared__ int warp_ok[PHS_INV_BLOCK / 32];
   const int lane = tid & 31, wid = tid >> 5;
+  int queued = 0;  // block-uniform
 
-  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+  for (int64_t tile = blockIdx.x;; tile += gridDim.x) {
+    const bool more = tile < n_tiles;
     // 1. per event: the outputs that need no arithmetic (the generating channel's own x and
     // factor, x padding beyond a channel's n_x_used, zeros for ok = false events)
     const int64_t ev = tile * PHS_INV_BLOCK + tid;
-    const bool valid = ev < a.n_events;
+    const bool valid = more && ev < a.n_events;
     int own = 0;
     bool ok = false;
     if (valid) {
@@ -375,8 +379,8 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
         }
       }
     }
-    // 2. pack the ok events: thread d takes the d-th, so the inversions run in full warps
-    // (an FP64 instruction costs the pipe the same whatever the number of active lanes)
+    // 2. queue the ok events: the inversions run in full warps (an FP64 instruction costs
+    // the pipe the same whatever the number of active lanes)
     const unsigned m = __ballot_sync(0xffffffffu, ok);
     if (lane == 0) warp_ok[wid] = __popc(m);
     __syncthreads();
@@ -386,15 +390,21 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
       n_ok += warp_ok[w];
     }
     if (ok) {
-      const int d = before + __popc(m & ((1u << lane) - 1u));
-      dense_ev[d] = ev;
-      dense_own[d] = own;
+      const int d = queued + before + __popc(m & ((1u << lane) - 1u));
+      q_ev[d] = ev;
+      q_own[d] = own;
     }
-    __syncthreads();
-    // 3. every other channel of the d-th ok event
-    if (tid < n_ok) {
-      const int64_t e = dense_ev[tid];
-      const int own_e = dense_own[tid];
+    queued += n_ok;
+    __syncthreads();  // the queue is complete; warp_ok is read
+    if (queued < PHS_INV_BLOCK && (more || queued == 0)) {
+      if (!more) break;
+      continue;
+    }
+    const int n_walk = min(queued, PHS_INV_BLOCK);
+    // 3. every other channel of the tid-th queued event
+    if (tid < n_walk) {
+      const int64_t e = q_ev[tid];
+      const int own_e = q_own[tid];
       double sqrts = ch0.sqrts, lab_bg = ch0.lab ? ch0.lab_bg : 0.0;
       double lab_ga = ch0.lab ? ch0.lab_gamma : 1.0;
       if (PER_EVENT) {
@@ -435,7 +445,23 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
         }
       }
     }
-    __syncthreads();  // dense_ev is refilled by the next tile
+    __syncthreads();  // every walked entry is read
+    // the events beyond the walked ones move to the front (fewer than PHS_INV_BLOCK)
+    const int rest = queued - n_walk;
+    int64_t e_rest = 0;
+    int o_rest = 0;
+    if (tid < rest) {
+      e_rest = q_ev[PHS_INV_BLOCK + tid];
+      o_rest = q_own[PHS_INV_BLOCK + tid];
+    }
+    __syncthreads();
+    if (tid < rest) {
+      q_ev[tid] = e_rest;
+      q_own[tid] = o_rest;
+    }
+    queued = rest;
+    __syncthreads();
+    if (!more && queued == 0) break;
   }
 }
 
