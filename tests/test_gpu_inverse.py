@@ -240,11 +240,11 @@ def test_whizard_abi_all_channels(torch):
     lib.c_whizard_finalize_gpu_phs()
 
 
-def whizard_call_vs_handle_api(torch, name, n, counts, beams):
+def whizard_call_vs_handle_api(torch, name, n, counts, beams, calls=None):
     """n events of the process `name` (a sample file's, or a builder of processes.py;
     events per channel `counts`) through c_whizard_gen_phs_from_x_gpu and through the
     handle API's forward and inverse calls on the whole batch: every output equal bit for
-    bit."""
+    bit.  calls: several (n, counts) in turn after one set-up, instead."""
     from gpu_phs_gb300 import _lib
     from gpu_phs_gb300.api import PhaseSpace
     lib = _lib.load()
@@ -268,40 +268,41 @@ def whizard_call_vs_handle_api(torch, name, n, counts, beams):
         keep += a
         lib.c_whizard_fill_tree_structure(ip(c + 1), *[t.ctypes.data for t in a])
     lib.c_whizard_init_gpu_phs()
-    assert int(counts.sum()) == n
-    limits = np.ascontiguousarray(np.cumsum(counts), np.int32)
-    lib.c_whizard_init_channel_ids(ip(n), ip(nch), limits.ctypes.data)
+    ps = PhaseSpace(proc, 500.0, 500.0)
     rng = np.random.default_rng(17)
-    x = np.ascontiguousarray(uniform_x(18, n, n_x))
-    if beams == "uniform":
-        E1, E2 = np.full(n, 500.0), np.full(n, 500.0)
-    else:
-        E1, E2 = rng.uniform(400, 600, n), rng.uniform(400, 600, n)
-    factors, volumes = np.zeros(n * nch), np.zeros(n)
-    oks = np.zeros(n, np.uint8)
-    p = np.zeros(n * n_out * 4)
-    x_out = np.zeros(n * n_x * nch)
-    lib.c_whizard_gen_phs_from_x_gpu(E1.ctypes.data, E2.ctypes.data, C.byref(C.c_bool(False)),
-                                     ip(n), ip(nch), ip(n_x), x.ctypes.data, factors.ctypes.data,
-                                     volumes.ctypes.data, oks.ctypes.data, p.ctypes.data,
-                                     x_out.ctypes.data)
-    assert lib.phs_last_error().decode() == ""
+    for k, (n, counts) in enumerate(calls or [(n, counts)]):
+        assert int(counts.sum()) == n
+        limits = np.ascontiguousarray(np.cumsum(counts), np.int32)
+        lib.c_whizard_init_channel_ids(ip(n), ip(nch), limits.ctypes.data)
+        x = np.ascontiguousarray(uniform_x(18 + k, n, n_x))
+        if beams == "uniform":
+            E1, E2 = np.full(n, 500.0), np.full(n, 500.0)
+        else:
+            E1, E2 = rng.uniform(400, 600, n), rng.uniform(400, 600, n)
+        factors, volumes = np.zeros(n * nch), np.zeros(n)
+        oks = np.zeros(n, np.uint8)
+        p = np.zeros(n * n_out * 4)
+        x_out = np.zeros(n * n_x * nch)
+        lib.c_whizard_gen_phs_from_x_gpu(E1.ctypes.data, E2.ctypes.data, C.byref(C.c_bool(False)),
+                                         ip(n), ip(nch), ip(n_x), x.ctypes.data, factors.ctypes.data,
+                                         volumes.ctypes.data, oks.ctypes.data, p.ctypes.data,
+                                         x_out.ctypes.data)
+        assert lib.phs_last_error().decode() == ""
+        xd = torch.from_numpy(x).cuda()
+        if beams == "uniform":
+            ev = ps.generate(xd, counts)
+            fa, xo = ps.inverse(ev.p, counts, ev.ok, xd, ev.factor)
+        else:
+            e1, e2 = torch.from_numpy(E1).cuda(), torch.from_numpy(E2).cuda()
+            ev = ps.generate_beams(xd, e1, e2, counts)
+            fa, xo = ps.inverse(ev.p, counts, ev.ok, xd, ev.factor, E1=e1, E2=e2)
+        assert np.array_equal(p.reshape(n, n_out, 4), ev.p.cpu().numpy())
+        assert np.array_equal(volumes, ev.volume.cpu().numpy())
+        assert np.array_equal(oks, ev.ok.cpu().numpy())
+        assert np.array_equal(factors.reshape(n, nch), fa.cpu().numpy())
+        assert np.array_equal(x_out.reshape(nch, n, n_x), xo.cpu().numpy())
     lib.c_whizard_reset_generator()
     lib.c_whizard_finalize_gpu_phs()
-    ps = PhaseSpace(proc, 500.0, 500.0)
-    xd = torch.from_numpy(x).cuda()
-    if beams == "uniform":
-        ev = ps.generate(xd, counts)
-        fa, xo = ps.inverse(ev.p, counts, ev.ok, xd, ev.factor)
-    else:
-        e1, e2 = torch.from_numpy(E1).cuda(), torch.from_numpy(E2).cuda()
-        ev = ps.generate_beams(xd, e1, e2, counts)
-        fa, xo = ps.inverse(ev.p, counts, ev.ok, xd, ev.factor, E1=e1, E2=e2)
-    assert np.array_equal(p.reshape(n, n_out, 4), ev.p.cpu().numpy())
-    assert np.array_equal(volumes, ev.volume.cpu().numpy())
-    assert np.array_equal(oks, ev.ok.cpu().numpy())
-    assert np.array_equal(factors.reshape(n, nch), fa.cpu().numpy())
-    assert np.array_equal(x_out.reshape(nch, n, n_x), xo.cpu().numpy())
 
 
 @pytest.mark.parametrize("beams", ["uniform", "per_event"])
@@ -332,3 +333,14 @@ def test_whizard_abi_pipelined_call_few_channels(torch):
     handle API bit for bit."""
     whizard_call_vs_handle_api(torch, "ttH", 400_000, np.array([0, 300_001, 99_999], np.int64),
                                "uniform")
+
+
+@pytest.mark.parametrize("beams", ["uniform", "per_event"])
+def test_whizard_abi_calls_of_changing_size(torch, beams):
+    """Calls of 700 000, 3 000 and 300 000 ttH events after one set-up (buffers grown,
+    then reused with shorter rows; chunked and unchunked forward maps, sliced and single
+    inverse launches), each equal to the handle API bit for bit."""
+    calls = [(700_000, np.array([200_000, 0, 500_000], np.int64)),
+             (3_000, np.array([1_000, 1_500, 500], np.int64)),
+             (300_000, np.array([100_000, 150_000, 50_000], np.int64))]
+    whizard_call_vs_handle_api(torch, "ttH", 0, None, beams, calls=calls)
