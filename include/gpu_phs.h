@@ -262,7 +262,11 @@ void c_whizard_init_gpu_phs(void);
 /* whizard_gpu_phs.cpp:110 */
 void c_whizard_finalize_gpu_phs(void);
 /* whizard_gpu_phs.cpp:114 -- host arrays; factors [n_events][n_channels], x_out
- * [n_channels][n_events][n_x] (phs.cu:1580-1585) */
+ * [n_channels][n_events][n_x] (phs.cu:1580-1585).  Synchronous.  The forward map runs in
+ * chunks of events with the copies in and back beside the kernels, the inverse map in
+ * launches over slices of the channels beside the copies of the finished ones; the
+ * results equal one unchunked pass bit for bit.  Device buffers grow to the largest call
+ * and stay until c_whizard_reset_generator or c_whizard_finalize_gpu_phs. */
 void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in, bool *requires_boost_to_lab,
                                   int *n_events, int *n_channels, int *n_x, double *x,
                                   double *factors, double *volumes, bool *oks, double *p,
