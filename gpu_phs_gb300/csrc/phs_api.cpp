@@ -1458,6 +1458,7 @@ extern "C" void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in,
       rc = fail(PHS_ERR_INVALID_ARG, "n_channels/n_x differ from the particle structure");
       break;
     }
+    if (n < 0) { rc = fail(PHS_ERR_INVALID_ARG, "n_events = %lld < 0", (long long)n); break; }
     if (n == 0) break;
     if (!x || !factors || !volumes || !oks || !p) { rc = fail(PHS_ERR_INVALID_ARG, "null data pointer"); break; }
     std::vector<int64_t> counts = W.counts;

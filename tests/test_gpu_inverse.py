@@ -240,6 +240,26 @@ def test_whizard_abi_all_channels(torch):
     lib.c_whizard_finalize_gpu_phs()
 
 
+def whizard_setup(lib, proc):
+    """The Whizard ABI's set-up calls for proc, up to c_whizard_init_gpu_phs."""
+    ip = lambda v: C.byref(C.c_int(v))
+    nch, n_x, n_out = proc.n_channels, proc.n_x, proc.n_out
+    lib.c_whizard_set_particle_structure(ip(nch), ip(nch), ip(nch), ip(n_x), ip(2), ip(n_out))
+    fm = np.ascontiguousarray(proc.flv_masses)
+    fw = np.ascontiguousarray(proc.flv_widths)
+    lib.c_whizard_set_flavors(fm.ctypes.data, fw.ctypes.data)
+    lib.c_whizard_init_mappings()
+    for c in range(nch):
+        a = [np.ascontiguousarray(proc.map_ids[c], np.int32), np.ascontiguousarray(proc.map_masses[c]),
+             np.ascontiguousarray(proc.map_widths[c])]
+        lib.c_whizard_fill_mapping(ip(c + 1), *[t.ctypes.data for t in a])
+    lib.c_whizard_init_tree_structures()
+    for c in range(nch):
+        a = [np.ascontiguousarray(t[c], np.int32) for t in (proc.d1, proc.d2, proc.has_children, proc.friends)]
+        lib.c_whizard_fill_tree_structure(ip(c + 1), *[t.ctypes.data for t in a])
+    lib.c_whizard_init_gpu_phs()
+
+
 def whizard_call_vs_handle_api(torch, name, n, counts, beams, calls=None):
     """n events of the process `name` (a sample file's, or a builder of processes.py;
     events per channel `counts`) through c_whizard_gen_phs_from_x_gpu and through the
@@ -251,23 +271,7 @@ def whizard_call_vs_handle_api(torch, name, n, counts, beams, calls=None):
     proc = getattr(P, name)() if hasattr(P, name) else load_process(golden(f"whizard_{name}"))
     ip = lambda v: C.byref(C.c_int(v))
     nch, n_x, n_out = proc.n_channels, proc.n_x, proc.n_out
-    lib.c_whizard_set_particle_structure(ip(nch), ip(nch), ip(nch), ip(n_x), ip(2), ip(n_out))
-    fm = np.ascontiguousarray(proc.flv_masses)
-    fw = np.ascontiguousarray(proc.flv_widths)
-    lib.c_whizard_set_flavors(fm.ctypes.data, fw.ctypes.data)
-    lib.c_whizard_init_mappings()
-    keep = []
-    for c in range(nch):
-        a = [np.ascontiguousarray(proc.map_ids[c], np.int32), np.ascontiguousarray(proc.map_masses[c]),
-             np.ascontiguousarray(proc.map_widths[c])]
-        keep += a
-        lib.c_whizard_fill_mapping(ip(c + 1), *[t.ctypes.data for t in a])
-    lib.c_whizard_init_tree_structures()
-    for c in range(nch):
-        a = [np.ascontiguousarray(t[c], np.int32) for t in (proc.d1, proc.d2, proc.has_children, proc.friends)]
-        keep += a
-        lib.c_whizard_fill_tree_structure(ip(c + 1), *[t.ctypes.data for t in a])
-    lib.c_whizard_init_gpu_phs()
+    whizard_setup(lib, proc)
     ps = PhaseSpace(proc, 500.0, 500.0)
     rng = np.random.default_rng(17)
     for k, (n, counts) in enumerate(calls or [(n, counts)]):
@@ -344,3 +348,37 @@ def test_whizard_abi_calls_of_changing_size(torch, beams):
              (3_000, np.array([1_000, 1_500, 500], np.int64)),
              (300_000, np.array([100_000, 150_000, 50_000], np.int64))]
     whizard_call_vs_handle_api(torch, "ttH", 0, None, beams, calls=calls)
+
+
+def test_whizard_abi_rejects_bad_calls(torch):
+    """A negative event count, a channel count or n_x other than the set-up's and event
+    counts that differ from c_whizard_init_channel_ids are refused with a message (the call
+    returns nothing); a valid call afterwards succeeds."""
+    from gpu_phs_gb300 import _lib
+    lib = _lib.load()
+    proc = load_process(golden("whizard_ttH"))
+    ip = lambda v: C.byref(C.c_int(v))
+    nch, n_x, n_out = proc.n_channels, proc.n_x, proc.n_out
+    whizard_setup(lib, proc)
+    n = 30
+    limits = np.ascontiguousarray(np.cumsum([10, 10, 10]), np.int32)
+    lib.c_whizard_init_channel_ids(ip(n), ip(nch), limits.ctypes.data)
+    x = np.ascontiguousarray(uniform_x(3, n, n_x))
+    E = np.full(n, 500.0)
+    f, v, ok, p, xo = np.zeros(n * nch), np.zeros(n), np.zeros(n, np.uint8), np.zeros(n * n_out * 4), np.zeros(n * n_x * nch)
+
+    def call(n_ev, n_ch, nx):
+        lib.c_whizard_gen_phs_from_x_gpu(E.ctypes.data, E.ctypes.data, C.byref(C.c_bool(False)),
+                                         ip(n_ev), ip(n_ch), ip(nx), x.ctypes.data, f.ctypes.data,
+                                         v.ctypes.data, ok.ctypes.data, p.ctypes.data, xo.ctypes.data)
+        return lib.phs_last_error().decode()
+    try:
+        assert "< 0" in call(-5, nch, n_x)
+        assert "n_channels/n_x" in call(n, nch + 1, n_x)
+        assert "n_channels/n_x" in call(n, nch, n_x + 1)
+        assert "cover" in call(n - 1, nch, n_x)
+        assert call(n, nch, n_x) == ""
+        assert ok.sum() > 0
+    finally:
+        lib.c_whizard_reset_generator()
+        lib.c_whizard_finalize_gpu_phs()
