@@ -698,7 +698,7 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-PROFILE_CASES = ("f64_tt", "f64_batched", "f64_split_batched", "ff_batched", "inverse_bwbw",
+PROFILE_CASES = ("f64_tt", "ff_tt", "f64_batched", "f64_split_batched", "ff_batched", "inverse_bwbw",
                  "adjoint_tt")
 
 
@@ -709,11 +709,15 @@ def run_case(name: str) -> None:
     import torch
     from gpu_phs_gb300 import processes as P
     from gpu_phs_gb300.api import Batch, PhaseSpace, philox_fill, philox_x
-    if name == "f64_tt":              # 2^21 tt events, FP64 one pass
+    if name in ("f64_tt", "ff_tt"):   # 2^21 tt events, FP64 or FP32-pair one pass
         proc = P.tt()
         n = 1 << 21
         ps = PhaseSpace(proc, 500.0, 500.0)
-        ps.set_variants(-1, 0)
+        if name == "ff_tt":
+            ps.set_precision(1)
+            ps.set_variants(1, -1)
+        else:
+            ps.set_variants(-1, 0)
         x = philox_x(n, proc.n_x, SEED)
         o = ps.alloc(n)
         for _ in range(2):
