@@ -7,6 +7,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -1494,10 +1496,10 @@ extern "C" void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in,
     double *dv = W.dv.as<double>(), *dxo = W.dxo.as<double>();
     uint8_t *dok = W.dok.as<uint8_t>();
     const double *dE1 = uniform ? nullptr : df + n, *dE2 = uniform ? nullptr : df + 2 * n;
-    // The forward map in chunks of events: the copy in of chunk k + 1 (on its own stream;
-    // a copy from pageable memory returns when done) and the copies back of chunk k - 1
-    // (momenta, volumes, ok flags; with one channel also its x and factors, which are the
-    // input's and the forward map's) run beside the kernels of chunk k.
+    // The forward map in chunks of events: the copies in of the next chunks (on their own
+    // stream) and the copies back of chunk k - 1 (momenta, volumes, ok flags; with one
+    // channel also its x and factors, which are the input's and the forward map's) run
+    // beside the kernels of chunk k.
     const int64_t fchunk = std::max<int64_t>(kWhizardChunkMin, (n + kWhizardChunks - 1) / kWhizardChunks);
     const int n_fchunks = (int)((n + fchunk - 1) / fchunk);
     std::vector<int64_t> beg(nch, 0), fcnt((size_t)n_fchunks * nch, 0);
@@ -1549,13 +1551,45 @@ extern "C" void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in,
         ee = cudaMemcpyAsync(factors + e0, df + e0, nk * sizeof(double), cudaMemcpyDeviceToHost, ms);
       return ee;
     };
-    if ((e = copy_in(0)) != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy in: %s", cudaGetErrorString(e)); break; }
-    if ((rc = forward(0))) { cudaStreamSynchronize(cs[0]); break; }
-    for (int k = 1; k < n_fchunks && rc == PHS_OK; k++) {
-      if ((e = copy_in(k)) != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy in: %s", cudaGetErrorString(e)); break; }
-      if ((rc = forward(k))) break;
-      if ((e = copy_back(k - 1)) != cudaSuccess) rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
+    // With more than one chunk the copies in run on a helper thread (a copy from pageable
+    // memory holds its thread until done), so that they overlap the copies back, which this
+    // thread issues; chunk k's kernels are queued once its copy in is.
+    std::mutex in_mu;
+    std::condition_variable in_cv;
+    int in_queued = 0;
+    cudaError_t in_err = cudaSuccess;
+    std::atomic<bool> in_stop{false};
+    std::thread loader;
+    if (n_fchunks > 1) {
+      const int dev = W.proc->device;
+      loader = std::thread([&, dev] {
+        cudaError_t ee = cudaSetDevice(dev);
+        for (int k = 0; k < n_fchunks && ee == cudaSuccess && !in_stop.load(); k++) {
+          ee = copy_in(k);
+          std::lock_guard<std::mutex> lk(in_mu);
+          if (ee == cudaSuccess) in_queued = k + 1;
+          in_cv.notify_all();
+        }
+        std::lock_guard<std::mutex> lk(in_mu);
+        in_err = ee;
+        if (ee == cudaSuccess && in_queued < n_fchunks) in_err = cudaErrorNotReady;  // stopped
+        in_cv.notify_all();
+      });
     }
+    auto wait_in = [&](int k) -> cudaError_t {
+      if (n_fchunks == 1) return copy_in(0);
+      std::unique_lock<std::mutex> lk(in_mu);
+      in_cv.wait(lk, [&] { return in_queued > k || in_err != cudaSuccess; });
+      return in_queued > k ? cudaSuccess : in_err;
+    };
+    for (int k = 0; k < n_fchunks && rc == PHS_OK; k++) {
+      if ((e = wait_in(k)) != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy in: %s", cudaGetErrorString(e)); break; }
+      if ((rc = forward(k))) break;
+      if (k > 0 && (e = copy_back(k - 1)) != cudaSuccess)
+        rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
+    }
+    if (rc) in_stop = true;
+    if (loader.joinable()) loader.join();
     if (rc) {
       cudaStreamSynchronize(hs);
       cudaStreamSynchronize(cs[0]);
