@@ -364,7 +364,7 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64, pin=
         "hbm_gbs": (wbytes + rbytes) / t_inv * 1e-6,
         "algorithmic_bytes_per_step": wbytes + rbytes,
         "ok_fraction": ev.ok.double().mean().item(),
-        "launch": "one persistent kernel: 128 events per block, every channel per event"}
+        "launch": "one persistent kernel: 64 events per block at a time, every channel per event"}
     del fac, xo, ev, x, ps
     res["whizard_abi_bwbw_61ch"] = whizard_abi_rate(proc, 1 << 17, max(2, min(steps, 5)))
     return res

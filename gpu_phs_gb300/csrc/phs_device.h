@@ -138,7 +138,7 @@ void phs_adjoint_sizes(int max_visits, int max_pops, int stack_depth, bool frien
 
 // Inverse map (phs_inverse.cu): for every event and every channel, the x row and factor
 // that channel assigns to the event's momenta.
-#define PHS_INV_BLOCK 128
+#define PHS_INV_BLOCK 64
 struct PhsInvLaunch {
   const PhsChannel *channels;  // device, per channel (uniform-beam constants)
   const int64_t *ch_begin;     // device, [n_channels]: first event of each generating channel

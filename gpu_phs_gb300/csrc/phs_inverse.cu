@@ -6,8 +6,9 @@
 // The reference runs this as a host loop over channels, each iteration a chain of
 // event-parallel kernels (combine, msq, one launch per boost level, with and without
 // friends) that round-trip msq, p_decay, phi/ct/st and a 4x4 matrix per boost through HBM.
-// Here one persistent kernel does all of it: a block takes 128 consecutive events, stages
-// their CM-frame momenta in shared memory once, and every thread then walks the visit
+// Here one persistent kernel does all of it: a block takes PHS_INV_BLOCK consecutive events
+// at a time, queues the ok ones, stages their CM-frame momenta in shared memory once, and
+// every thread then walks the visit
 // program (phs_program.h) of each channel in turn for its event, with the running frame in
 // registers and the channel's branch momenta in its shared-memory column.  Per (event,
 // channel) the only HBM traffic is the x row and the factor written.
