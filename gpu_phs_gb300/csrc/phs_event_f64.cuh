@@ -178,8 +178,11 @@ __device__ void child_constants(const PhsChild &C, double sqrts, double m_tot, d
       a2 = a1 / s;
       break;
     case PHS_MAP_SCHANNEL: {
+      // a0 = atan((msq_min - m^2) / (m w)) does not depend on sqrt(s): the compiled
+      // program's value (the host's atan of the same argument bits, as the reference's CPU
+      // path computes it) serves every event
       double msq0 = dmul(m, m), mw = dmul(m, w);
-      a0 = atan(dsub(msq_min, msq0) / mw);
+      a0 = C.a0;
       a1 = atan(dsub(msq_max, msq0) / mw);
       a2 = dmul(dsub(a1, a0), mw) / s;
       break;

@@ -52,8 +52,8 @@ __device__ __forceinline__ bool msq_near_zero(ff v, float s) {
 
 // The constants of an internal child that depend on sqrt(s): the mapping's a1 (Breit-Wigner:
 // a1 - a0) and a2, pi/2 - a1, msq_max and the ok test's m_max.  From the channel program for
-// uniform beams; per event from the FP64 constants (child_constants, as the reference's GPU
-// path computes them) for per-event beams.
+// uniform beams; per event from the FP64 constants for per-event beams (child_constants:
+// what depends on sqrt(s) per event, as the reference's GPU path computes it).
 struct ChildVar {
   ff a1, a2, u1, msq_max, m_max;
 };
