@@ -1663,10 +1663,19 @@ extern "C" void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in,
     for (size_t u = 0; u < units.size() && rc == PHS_OK && e == cudaSuccess; u++) {
       const Unit &U = units[u];
       e = cudaStreamWaitEvent(ms, W.done[u + 1], 0);
-      for (int i = U.lo; i < U.hi && e == cudaSuccess && x_out; i++) {
+      // device rows sit where the caller's do: a run of channels whose ids step evenly
+      // goes as one strided copy (one copy per row costs far more than its bytes)
+      const size_t width = (size_t)(U.e1 - U.e0) * n_x * sizeof(double);
+      for (int i = U.lo; i < U.hi && e == cudaSuccess && x_out;) {
+        const int step = i + 1 < U.hi ? order[i + 1] - order[i] : 0;
+        int j = i + 1;
+        if (step > 0)
+          while (j < U.hi && order[j] - order[j - 1] == step) j++;
+        const size_t pitch = step > 0 ? (size_t)step * n * n_x * sizeof(double) : width;
         const size_t off = ((size_t)order[i] * n + U.e0) * n_x;
-        e = cudaMemcpyAsync(x_out + off, dxo + off, (size_t)(U.e1 - U.e0) * n_x * sizeof(double),
-                            cudaMemcpyDeviceToHost, ms);
+        e = cudaMemcpy2DAsync(x_out + off, pitch, dxo + off, pitch, width, j - i,
+                              cudaMemcpyDeviceToHost, ms);
+        i = j;
       }
       if (e == cudaSuccess && U.hi == nch)
         e = cudaMemcpyAsync(factors + U.e0 * nch, W.dfa.as<double>() + U.e0 * nch,
