@@ -1275,6 +1275,23 @@ bool beams_uniform(const double *E1, const double *E2, int64_t n) {
   return std::all_of(ok.begin(), ok.end(), [](char v) { return v != 0; });
 }
 
+// Cuts of the group order of n_channels channels into at most n_slices slices of about
+// equal size: at the end of a tree-shape group (group_begin) where one lies within half a
+// slice of the even cut, else at the even cut.  Returns the n_slices' + 1 boundaries.
+std::vector<int> channel_slices(int n_channels, int n_slices, const std::vector<int32_t> &group_begin) {
+  std::vector<int> slice = {0};
+  for (int k = 1; k < n_slices; k++) {
+    const double want = (double)n_channels * k / n_slices, half = 0.5 * n_channels / n_slices;
+    int cut = -1;
+    for (int32_t b : group_begin)
+      if (b > slice.back() && b < n_channels && (cut < 0 || fabs(b - want) < fabs(cut - want))) cut = b;
+    if (cut < 0 || fabs(cut - want) > half) cut = (int)llround(want);
+    if (cut > slice.back() && cut < n_channels) slice.push_back(cut);
+  }
+  slice.push_back(n_channels);
+  return slice;
+}
+
 void whizard_log(int rc) {
   if (rc) fprintf(stderr, "gpu_phs: %s\n", g_err.c_str());
 }
@@ -1614,17 +1631,9 @@ extern "C" void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in,
         cudaStreamSynchronize(ms);
         break;
       }
-      const int n_slices_max = (int64_t)n * nch < (1 << 20) ? 1 : std::min(nch, kWhizardSlices);
-      std::vector<int> slice = {0};
-      for (int k = 1; k < n_slices_max; k++) {
-        const double want = (double)nch * k / n_slices_max, half = 0.5 * nch / n_slices_max;
-        int cut = -1;
-        for (int32_t b : W.proc->inv_group_begin)
-          if (b > slice.back() && b < nch && (cut < 0 || fabs(b - want) < fabs(cut - want))) cut = b;
-        if (cut < 0 || fabs(cut - want) > half) cut = (int)llround(want);
-        if (cut > slice.back() && cut < nch) slice.push_back(cut);
-      }
-      slice.push_back(nch);
+      const std::vector<int> slice = channel_slices(
+          nch, (int64_t)n * nch < (1 << 20) ? 1 : std::min(nch, kWhizardSlices),
+          W.proc->inv_group_begin);
       const int n_slices = (int)slice.size() - 1;
       for (int k = 0; k + 1 < n_slices; k++) units.push_back({slice[k], slice[k + 1], 0, n});
       const int n_last =
