@@ -306,6 +306,25 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64, pin=
     res["batched_64ch"]["max_abs_momentum_diff_gev"] = dp
     res["batched_64ch"]["factor_max_rel"] = (
         (bufs["fp32_mixed"][1][sel] / bufs["fp64_one_pass"][1][sel] - 1).abs().max().item())
+    # the per-particle relative momentum error of the other workloads, channel by channel
+    # (flat momenta, each channel's events [count][n_out][4] from its offset)
+    mx, sq, n_p, e = 0.0, 0.0, 0, 0
+    okf = bufs["fp32_mixed"][3].bool()
+    for i, (sp, c) in enumerate(zip(spaces, counts)):
+        c, no = int(c), sp.proc.n_out
+        both = (sel & okf)[e:e + c]
+        a = p6[int(po[i]):int(po[i + 1])].view(c, no, 4)[both]
+        b = pf[int(po[i]):int(po[i + 1])].view(c, no, 4)[both]
+        if a.numel():
+            r = (b - a).abs().amax(-1) / a[..., 0].abs().clamp(min=1e-3 * sp.proc.sqrts)
+            mx = max(mx, r.max().item())
+            sq += r.pow(2).sum().item()
+            n_p += r.numel()
+        e += c
+    res["batched_64ch"]["momentum_max_rel"] = mx
+    res["batched_64ch"]["momentum_rms_rel"] = (sq / max(n_p, 1)) ** 0.5
+    res["batched_64ch"]["momentum_rel_definition"] = \
+        "per particle max_mu |dp^mu| / max(E, 1e-3 sqrt(s)), events ok in both"
     del bufs, xb, spaces
 
     # adjoint: forward + reverse on 1e6 tt events with random cotangents
