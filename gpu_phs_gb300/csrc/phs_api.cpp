@@ -11,6 +11,7 @@
 #include <condition_variable>
 #include <mutex>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -1268,9 +1269,17 @@ bool beams_uniform(const double *E1, const double *E2, int64_t n) {
   if (n_threads <= 1) return scan(0, n);
   std::vector<char> ok(n_threads, 1);
   std::vector<std::thread> th;
-  for (int t = 1; t < n_threads; t++)
-    th.emplace_back([&, t] { ok[t] = scan(n * t / n_threads, n * (t + 1) / n_threads); });
+  int started = 1;
+  try {
+    for (; started < n_threads; started++)
+      th.emplace_back([&, started] {
+        ok[started] = scan(n * started / n_threads, n * (started + 1) / n_threads);
+      });
+  } catch (const std::system_error &) {
+    // no more threads: this one scans the parts not handed out
+  }
   ok[0] = scan(0, n / n_threads);
+  for (int t = started; t < n_threads; t++) ok[t] = scan(n * t / n_threads, n * (t + 1) / n_threads);
   for (auto &t : th) t.join();
   return std::all_of(ok.begin(), ok.end(), [](char v) { return v != 0; });
 }
@@ -1465,244 +1474,260 @@ extern "C" void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in,
   std::lock_guard<std::mutex> lk(W.mu);
   g_err.clear();  // the call returns nothing: phs_last_error() reports this call alone
   int rc = PHS_OK;
-  do {
-    if (!W.proc) { rc = fail(PHS_ERR_STATE, "c_whizard_gen_phs_from_x_gpu: init_gpu_phs not done"); break; }
-    if (!n_events_p || !n_channels_p || !n_x_p || !E1_in || !E2_in) {
-      rc = fail(PHS_ERR_INVALID_ARG, "c_whizard_gen_phs_from_x_gpu: null argument");
-      break;
-    }
-    const int64_t n = *n_events_p;
-    const int nch = *n_channels_p, n_x = *n_x_p, n_out = W.n_out;
-    if (nch != W.n_channels || n_x != W.n_x) {
-      rc = fail(PHS_ERR_INVALID_ARG, "n_channels/n_x differ from the particle structure");
-      break;
-    }
-    if (n < 0) { rc = fail(PHS_ERR_INVALID_ARG, "n_events = %lld < 0", (long long)n); break; }
-    if (n == 0) break;
-    if (!x || !factors || !volumes || !oks || !p) { rc = fail(PHS_ERR_INVALID_ARG, "null data pointer"); break; }
-    std::vector<int64_t> counts = W.counts;
-    int64_t sum = 0;
-    for (auto c : counts) sum += c;
-    if (counts.size() != (size_t)nch || sum != n) {
-      rc = fail(PHS_ERR_INVALID_ARG, "channel ids from c_whizard_init_channel_ids cover %lld "
-                "events, not %lld", (long long)sum, (long long)n);
-      break;
-    }
-    const bool uniform = beams_uniform(E1_in, E2_in, n);
-    DeviceGuard g(W.proc->device);
-    if ((rc = W.dx.reserve(n * n_x * sizeof(double)))) break;
-    if ((rc = W.dp.reserve(n * 4 * n_out * sizeof(double)))) break;
-    if ((rc = W.df.reserve(n * sizeof(double) * (uniform ? 1 : 3)))) break;
-    if ((rc = W.dv.reserve(n * sizeof(double)))) break;
-    if ((rc = W.dok.reserve(n))) break;
-    if (nch > 1 && (rc = W.dfa.reserve((size_t)n * nch * sizeof(double)))) break;
-    if (nch > 1 && (rc = W.dxo.reserve((size_t)nch * n * n_x * sizeof(double)))) break;
-    if (uniform && (rc = phs_process_set_beams(W.proc, E1_in[0], E2_in[0]))) break;
-    cudaError_t e = cudaSuccess;
-    for (int i = 0; i < 4 && e == cudaSuccess; i++)
-      if (!W.streams[i]) e = cudaStreamCreateWithFlags(&W.streams[i], cudaStreamNonBlocking);
-    for (int i = 0; i <= kWhizardLaunches && e == cudaSuccess; i++)
-      if (!W.done[i]) e = cudaEventCreateWithFlags(&W.done[i], cudaEventDisableTiming);
-    for (int i = 0; i < kWhizardChunks && e == cudaSuccess; i++) {
-      if (!W.x_in[i]) e = cudaEventCreateWithFlags(&W.x_in[i], cudaEventDisableTiming);
-      if (e == cudaSuccess && !W.fwd[i]) e = cudaEventCreateWithFlags(&W.fwd[i], cudaEventDisableTiming);
-    }
-    if (e != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "set-up: %s", cudaGetErrorString(e)); break; }
-    cudaStream_t cs[2] = {W.streams[0], W.streams[2]}, ms = W.streams[1], hs = W.streams[3];
-    double *dx = W.dx.as<double>(), *dp = W.dp.as<double>(), *df = W.df.as<double>();
-    double *dv = W.dv.as<double>(), *dxo = W.dxo.as<double>();
-    uint8_t *dok = W.dok.as<uint8_t>();
-    const double *dE1 = uniform ? nullptr : df + n, *dE2 = uniform ? nullptr : df + 2 * n;
-    // The forward map in chunks of events: the copies in of the next chunks (on their own
-    // stream) and the copies back of chunk k - 1 (momenta, volumes, ok flags; with one
-    // channel also its x and factors, which are the input's and the forward map's) run
-    // beside the kernels of chunk k.
-    const int64_t fchunk = std::max<int64_t>(kWhizardChunkMin, (n + kWhizardChunks - 1) / kWhizardChunks);
-    const int n_fchunks = (int)((n + fchunk - 1) / fchunk);
-    std::vector<int64_t> beg(nch, 0), fcnt((size_t)n_fchunks * nch, 0);
-    for (int c = 1; c < nch; c++) beg[c] = beg[c - 1] + counts[c - 1];
-    for (int c = 0; c < nch; c++)
-      for (int k = 0; k < n_fchunks; k++) {
-        const int64_t e0 = k * fchunk, e1 = std::min(n, e0 + fchunk);
-        fcnt[(size_t)k * nch + c] =
-            std::max<int64_t>(0, std::min(e1, beg[c] + counts[c]) - std::max(e0, beg[c]));
+  try {  // nothing may leave a C entry point by an exception
+    do {
+      if (!W.proc) { rc = fail(PHS_ERR_STATE, "c_whizard_gen_phs_from_x_gpu: init_gpu_phs not done"); break; }
+      if (!n_events_p || !n_channels_p || !n_x_p || !E1_in || !E2_in) {
+        rc = fail(PHS_ERR_INVALID_ARG, "c_whizard_gen_phs_from_x_gpu: null argument");
+        break;
       }
-    auto copy_in = [&](int k) -> cudaError_t {
-      const int64_t e0 = k * fchunk, nk = std::min(n, e0 + fchunk) - e0;
-      cudaError_t ee = cudaMemcpyAsync(dx + e0 * n_x, x + e0 * n_x, nk * n_x * sizeof(double),
-                                       cudaMemcpyHostToDevice, hs);
-      if (ee == cudaSuccess && !uniform)
-        ee = cudaMemcpyAsync(df + n + e0, E1_in + e0, nk * sizeof(double), cudaMemcpyHostToDevice, hs);
-      if (ee == cudaSuccess && !uniform)
-        ee = cudaMemcpyAsync(df + 2 * n + e0, E2_in + e0, nk * sizeof(double), cudaMemcpyHostToDevice, hs);
-      return ee == cudaSuccess ? cudaEventRecord(W.x_in[k], hs) : ee;
-    };
-    auto forward = [&](int k) -> int {
-      const int64_t e0 = k * fchunk, nk = std::min(n, e0 + fchunk) - e0;
-      const int64_t *ck = fcnt.data() + (size_t)k * nch;
-      cudaError_t ee = cudaStreamWaitEvent(cs[0], W.x_in[k], 0);
-      if (ee != cudaSuccess) return fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(ee));
-      int r = uniform
-          ? phs_generate_device(W.proc, nk, ck, dx + e0 * n_x, dp + e0 * 4 * n_out, df + e0,
-                                dv + e0, dok + e0, cs[0])
-          : phs_generate_beams_device(W.proc, nk, ck, dE1 + e0, dE2 + e0, dx + e0 * n_x,
-                                      dp + e0 * 4 * n_out, df + e0, dv + e0, dok + e0, cs[0]);
-      if (r) return r;
-      ee = cudaEventRecord(W.fwd[k], cs[0]);
-      return ee == cudaSuccess ? PHS_OK : fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(ee));
-    };
-    auto copy_back = [&](int k) -> cudaError_t {
-      const int64_t e0 = k * fchunk, nk = std::min(n, e0 + fchunk) - e0;
-      cudaError_t ee = cudaStreamWaitEvent(ms, W.fwd[k], 0);
-      if (ee == cudaSuccess)
-        ee = cudaMemcpyAsync(p + e0 * 4 * n_out, dp + e0 * 4 * n_out, nk * 4 * n_out * sizeof(double),
-                             cudaMemcpyDeviceToHost, ms);
-      if (ee == cudaSuccess)
-        ee = cudaMemcpyAsync(volumes + e0, dv + e0, nk * sizeof(double), cudaMemcpyDeviceToHost, ms);
-      if (ee == cudaSuccess) ee = cudaMemcpyAsync(oks + e0, dok + e0, nk, cudaMemcpyDeviceToHost, ms);
-      // one channel: the generating channel keeps its own x and factor (phs.cu:1580-1585)
-      if (ee == cudaSuccess && nch == 1 && x_out)
-        ee = cudaMemcpyAsync(x_out + e0 * n_x, dx + e0 * n_x, nk * n_x * sizeof(double),
-                             cudaMemcpyDeviceToHost, ms);
-      if (ee == cudaSuccess && nch == 1)
-        ee = cudaMemcpyAsync(factors + e0, df + e0, nk * sizeof(double), cudaMemcpyDeviceToHost, ms);
-      return ee;
-    };
-    // With more than one chunk the copies in run on a helper thread (a copy from pageable
-    // memory holds its thread until done), so that they overlap the copies back, which this
-    // thread issues; chunk k's kernels are queued once its copy in is.
-    std::mutex in_mu;
-    std::condition_variable in_cv;
-    int in_queued = 0;
-    cudaError_t in_err = cudaSuccess;
-    std::atomic<bool> in_stop{false};
-    std::thread loader;
-    if (n_fchunks > 1) {
-      const int dev = W.proc->device;
-      loader = std::thread([&, dev] {
-        cudaError_t ee = cudaSetDevice(dev);
-        for (int k = 0; k < n_fchunks && ee == cudaSuccess && !in_stop.load(); k++) {
-          ee = copy_in(k);
-          std::lock_guard<std::mutex> lk(in_mu);
-          if (ee == cudaSuccess) in_queued = k + 1;
-          in_cv.notify_all();
+      const int64_t n = *n_events_p;
+      const int nch = *n_channels_p, n_x = *n_x_p, n_out = W.n_out;
+      if (nch != W.n_channels || n_x != W.n_x) {
+        rc = fail(PHS_ERR_INVALID_ARG, "n_channels/n_x differ from the particle structure");
+        break;
+      }
+      if (n < 0) { rc = fail(PHS_ERR_INVALID_ARG, "n_events = %lld < 0", (long long)n); break; }
+      if (n == 0) break;
+      if (!x || !factors || !volumes || !oks || !p) { rc = fail(PHS_ERR_INVALID_ARG, "null data pointer"); break; }
+      std::vector<int64_t> counts = W.counts;
+      int64_t sum = 0;
+      for (auto c : counts) sum += c;
+      if (counts.size() != (size_t)nch || sum != n) {
+        rc = fail(PHS_ERR_INVALID_ARG, "channel ids from c_whizard_init_channel_ids cover %lld "
+                  "events, not %lld", (long long)sum, (long long)n);
+        break;
+      }
+      const bool uniform = beams_uniform(E1_in, E2_in, n);
+      DeviceGuard g(W.proc->device);
+      if ((rc = W.dx.reserve(n * n_x * sizeof(double)))) break;
+      if ((rc = W.dp.reserve(n * 4 * n_out * sizeof(double)))) break;
+      if ((rc = W.df.reserve(n * sizeof(double) * (uniform ? 1 : 3)))) break;
+      if ((rc = W.dv.reserve(n * sizeof(double)))) break;
+      if ((rc = W.dok.reserve(n))) break;
+      if (nch > 1 && (rc = W.dfa.reserve((size_t)n * nch * sizeof(double)))) break;
+      if (nch > 1 && (rc = W.dxo.reserve((size_t)nch * n * n_x * sizeof(double)))) break;
+      if (uniform && (rc = phs_process_set_beams(W.proc, E1_in[0], E2_in[0]))) break;
+      cudaError_t e = cudaSuccess;
+      for (int i = 0; i < 4 && e == cudaSuccess; i++)
+        if (!W.streams[i]) e = cudaStreamCreateWithFlags(&W.streams[i], cudaStreamNonBlocking);
+      for (int i = 0; i <= kWhizardLaunches && e == cudaSuccess; i++)
+        if (!W.done[i]) e = cudaEventCreateWithFlags(&W.done[i], cudaEventDisableTiming);
+      for (int i = 0; i < kWhizardChunks && e == cudaSuccess; i++) {
+        if (!W.x_in[i]) e = cudaEventCreateWithFlags(&W.x_in[i], cudaEventDisableTiming);
+        if (e == cudaSuccess && !W.fwd[i]) e = cudaEventCreateWithFlags(&W.fwd[i], cudaEventDisableTiming);
+      }
+      if (e != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "set-up: %s", cudaGetErrorString(e)); break; }
+      cudaStream_t cs[2] = {W.streams[0], W.streams[2]}, ms = W.streams[1], hs = W.streams[3];
+      double *dx = W.dx.as<double>(), *dp = W.dp.as<double>(), *df = W.df.as<double>();
+      double *dv = W.dv.as<double>(), *dxo = W.dxo.as<double>();
+      uint8_t *dok = W.dok.as<uint8_t>();
+      const double *dE1 = uniform ? nullptr : df + n, *dE2 = uniform ? nullptr : df + 2 * n;
+      // The forward map in chunks of events: the copies in of the next chunks (on their own
+      // stream) and the copies back of chunk k - 1 (momenta, volumes, ok flags; with one
+      // channel also its x and factors, which are the input's and the forward map's) run
+      // beside the kernels of chunk k.
+      const int64_t fchunk = std::max<int64_t>(kWhizardChunkMin, (n + kWhizardChunks - 1) / kWhizardChunks);
+      const int n_fchunks = (int)((n + fchunk - 1) / fchunk);
+      std::vector<int64_t> beg(nch, 0), fcnt((size_t)n_fchunks * nch, 0);
+      for (int c = 1; c < nch; c++) beg[c] = beg[c - 1] + counts[c - 1];
+      for (int c = 0; c < nch; c++)
+        for (int k = 0; k < n_fchunks; k++) {
+          const int64_t e0 = k * fchunk, e1 = std::min(n, e0 + fchunk);
+          fcnt[(size_t)k * nch + c] =
+              std::max<int64_t>(0, std::min(e1, beg[c] + counts[c]) - std::max(e0, beg[c]));
         }
-        std::lock_guard<std::mutex> lk(in_mu);
-        in_err = ee;
-        if (ee == cudaSuccess && in_queued < n_fchunks) in_err = cudaErrorNotReady;  // stopped
-        in_cv.notify_all();
-      });
-    }
-    auto wait_in = [&](int k) -> cudaError_t {
-      if (n_fchunks == 1) return copy_in(0);
-      std::unique_lock<std::mutex> lk(in_mu);
-      in_cv.wait(lk, [&] { return in_queued > k || in_err != cudaSuccess; });
-      return in_queued > k ? cudaSuccess : in_err;
-    };
-    for (int k = 0; k < n_fchunks && rc == PHS_OK; k++) {
-      if ((e = wait_in(k)) != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy in: %s", cudaGetErrorString(e)); break; }
-      if ((rc = forward(k))) break;
-      if (k > 0 && (e = copy_back(k - 1)) != cudaSuccess)
-        rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
-    }
-    if (rc) in_stop = true;
-    if (loader.joinable()) loader.join();
-    if (rc) {
-      cudaStreamSynchronize(hs);
-      cudaStreamSynchronize(cs[0]);
-      cudaStreamSynchronize(ms);
-      break;
-    }
-    // More than one channel: the inverse map (factors [n][n_channels], x [n_channels][n][n_x])
-    // in launches over slices of the channels in the order of the tree-shape groups (cut
-    // where a group ends, if one ends near the even cut: the geometry of a shape is computed
-    // once per event and launch), each over every event so that it fills the GPU, the last
-    // slice in chunks of events; the launches alternate over two compute streams, so that
-    // one's tail overlaps the next one's start.  They are queued before the last forward
-    // chunk's copies back; the copies of each launch's x rows (contiguous per channel on both
-    // sides) then run beside the later kernels, and after each chunk of the last slice the
-    // factors of its events, which every earlier launch has finished.
-    struct Unit { int lo, hi; int64_t e0, e1; };
-    std::vector<Unit> units;
-    if (nch > 1) {
-      if ((int)W.proc->inv_group_begin.size() < 2 || (int)W.proc->inv_order.size() != nch) {
-        rc = fail(PHS_ERR_STATE, "inverse map: channel groups not built");
+      auto copy_in = [&](int k) -> cudaError_t {
+        const int64_t e0 = k * fchunk, nk = std::min(n, e0 + fchunk) - e0;
+        cudaError_t ee = cudaMemcpyAsync(dx + e0 * n_x, x + e0 * n_x, nk * n_x * sizeof(double),
+                                         cudaMemcpyHostToDevice, hs);
+        if (ee == cudaSuccess && !uniform)
+          ee = cudaMemcpyAsync(df + n + e0, E1_in + e0, nk * sizeof(double), cudaMemcpyHostToDevice, hs);
+        if (ee == cudaSuccess && !uniform)
+          ee = cudaMemcpyAsync(df + 2 * n + e0, E2_in + e0, nk * sizeof(double), cudaMemcpyHostToDevice, hs);
+        return ee == cudaSuccess ? cudaEventRecord(W.x_in[k], hs) : ee;
+      };
+      auto forward = [&](int k) -> int {
+        const int64_t e0 = k * fchunk, nk = std::min(n, e0 + fchunk) - e0;
+        const int64_t *ck = fcnt.data() + (size_t)k * nch;
+        cudaError_t ee = cudaStreamWaitEvent(cs[0], W.x_in[k], 0);
+        if (ee != cudaSuccess) return fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(ee));
+        int r = uniform
+            ? phs_generate_device(W.proc, nk, ck, dx + e0 * n_x, dp + e0 * 4 * n_out, df + e0,
+                                  dv + e0, dok + e0, cs[0])
+            : phs_generate_beams_device(W.proc, nk, ck, dE1 + e0, dE2 + e0, dx + e0 * n_x,
+                                        dp + e0 * 4 * n_out, df + e0, dv + e0, dok + e0, cs[0]);
+        if (r) return r;
+        ee = cudaEventRecord(W.fwd[k], cs[0]);
+        return ee == cudaSuccess ? PHS_OK : fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(ee));
+      };
+      auto copy_back = [&](int k) -> cudaError_t {
+        const int64_t e0 = k * fchunk, nk = std::min(n, e0 + fchunk) - e0;
+        cudaError_t ee = cudaStreamWaitEvent(ms, W.fwd[k], 0);
+        if (ee == cudaSuccess)
+          ee = cudaMemcpyAsync(p + e0 * 4 * n_out, dp + e0 * 4 * n_out, nk * 4 * n_out * sizeof(double),
+                               cudaMemcpyDeviceToHost, ms);
+        if (ee == cudaSuccess)
+          ee = cudaMemcpyAsync(volumes + e0, dv + e0, nk * sizeof(double), cudaMemcpyDeviceToHost, ms);
+        if (ee == cudaSuccess) ee = cudaMemcpyAsync(oks + e0, dok + e0, nk, cudaMemcpyDeviceToHost, ms);
+        // one channel: the generating channel keeps its own x and factor (phs.cu:1580-1585)
+        if (ee == cudaSuccess && nch == 1 && x_out)
+          ee = cudaMemcpyAsync(x_out + e0 * n_x, dx + e0 * n_x, nk * n_x * sizeof(double),
+                               cudaMemcpyDeviceToHost, ms);
+        if (ee == cudaSuccess && nch == 1)
+          ee = cudaMemcpyAsync(factors + e0, df + e0, nk * sizeof(double), cudaMemcpyDeviceToHost, ms);
+        return ee;
+      };
+      // With more than one chunk the copies in run on a helper thread (a copy from pageable
+      // memory holds its thread until done), so that they overlap the copies back, which this
+      // thread issues; chunk k's kernels are queued once its copy in is.
+      std::mutex in_mu;
+      std::condition_variable in_cv;
+      int in_queued = 0;
+      cudaError_t in_err = cudaSuccess;
+      std::atomic<bool> in_stop{false};
+      std::thread loader;
+      bool threaded = false;
+      if (n_fchunks > 1) {
+        const int dev = W.proc->device;
+        try {
+          loader = std::thread([&, dev] {
+            cudaError_t ee = cudaSetDevice(dev);
+            for (int k = 0; k < n_fchunks && ee == cudaSuccess && !in_stop.load(); k++) {
+              ee = copy_in(k);
+              std::lock_guard<std::mutex> lk(in_mu);
+              if (ee == cudaSuccess) in_queued = k + 1;
+              in_cv.notify_all();
+            }
+            std::lock_guard<std::mutex> lk(in_mu);
+            in_err = ee;
+            if (ee == cudaSuccess && in_queued < n_fchunks) in_err = cudaErrorNotReady;  // stopped
+            in_cv.notify_all();
+          });
+          threaded = true;
+        } catch (const std::system_error &) {
+          // no helper thread: this thread copies each chunk in before its kernels
+        }
+      }
+      auto wait_in = [&](int k) -> cudaError_t {
+        if (!threaded) return copy_in(k);
+        std::unique_lock<std::mutex> lk(in_mu);
+        in_cv.wait(lk, [&] { return in_queued > k || in_err != cudaSuccess; });
+        return in_queued > k ? cudaSuccess : in_err;
+      };
+      try {  // the helper thread is joined below whatever happens here
+        for (int k = 0; k < n_fchunks && rc == PHS_OK; k++) {
+          if ((e = wait_in(k)) != cudaSuccess) { rc = fail(PHS_ERR_CUDA, "copy in: %s", cudaGetErrorString(e)); break; }
+          if ((rc = forward(k))) break;
+          if (k > 0 && (e = copy_back(k - 1)) != cudaSuccess)
+            rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
+        }
+      } catch (const std::exception &ex) {
+        rc = fail(PHS_ERR_ALLOC, "host: %s", ex.what());
+      }
+      if (rc) in_stop = true;
+      if (loader.joinable()) loader.join();
+      if (rc) {
+        cudaStreamSynchronize(hs);
         cudaStreamSynchronize(cs[0]);
         cudaStreamSynchronize(ms);
         break;
       }
-      const std::vector<int> slice = channel_slices(
-          nch, (int64_t)n * nch < (1 << 20) ? 1 : std::min(nch, kWhizardSlices),
-          W.proc->inv_group_begin);
-      const int n_slices = (int)slice.size() - 1;
-      for (int k = 0; k + 1 < n_slices; k++) units.push_back({slice[k], slice[k + 1], 0, n});
-      const int n_last =
-          n_slices > 1 ? (int)std::min<int64_t>(kWhizardLastChunks, std::max<int64_t>(1, n >> 15)) : 1;
-      for (int j = 0; j < n_last; j++)
-        units.push_back({slice[n_slices - 1], nch, n * j / n_last, n * (j + 1) / n_last});
-      // channel starts relative to each launch's first event
-      std::vector<int64_t> begs((size_t)units.size() * nch);
-      for (size_t u = 0; u < units.size(); u++)
-        for (int c = 0; c < nch; c++) begs[u * nch + c] = beg[c] - units[u].e0;
-      if ((rc = W.dchb.reserve(begs.size() * sizeof(int64_t)))) { cudaStreamSynchronize(cs[0]); break; }
-      e = cudaMemcpyAsync(W.dchb.ptr, begs.data(), begs.size() * sizeof(int64_t), cudaMemcpyHostToDevice, cs[0]);
-      if (e == cudaSuccess) e = cudaEventRecord(W.done[0], cs[0]);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(cs[1], W.done[0], 0);
-      if (e != cudaSuccess) rc = fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(e));
-      // do_inverse_mapping is forced on (whizard_gpu_phs.cpp:118): every channel's factor
-      // and x; the generating channel keeps its own x and factor (phs.cu:1580-1585), written
-      // with the other no-arithmetic outputs by the first launch (over every event)
-      for (size_t u = 0; u < units.size() && rc == PHS_OK; u++) {
+      // More than one channel: the inverse map (factors [n][n_channels], x [n_channels][n][n_x])
+      // in launches over slices of the channels in the order of the tree-shape groups (cut
+      // where a group ends, if one ends near the even cut: the geometry of a shape is computed
+      // once per event and launch), each over every event so that it fills the GPU, the last
+      // slice in chunks of events; the launches alternate over two compute streams, so that
+      // one's tail overlaps the next one's start.  They are queued before the last forward
+      // chunk's copies back; the copies of each launch's x rows (contiguous per channel on both
+      // sides) then run beside the later kernels, and after each chunk of the last slice the
+      // factors of its events, which every earlier launch has finished.
+      struct Unit { int lo, hi; int64_t e0, e1; };
+      std::vector<Unit> units;
+      if (nch > 1) {
+        if ((int)W.proc->inv_group_begin.size() < 2 || (int)W.proc->inv_order.size() != nch) {
+          rc = fail(PHS_ERR_STATE, "inverse map: channel groups not built");
+          cudaStreamSynchronize(cs[0]);
+          cudaStreamSynchronize(ms);
+          break;
+        }
+        const std::vector<int> slice = channel_slices(
+            nch, (int64_t)n * nch < (1 << 20) ? 1 : std::min(nch, kWhizardSlices),
+            W.proc->inv_group_begin);
+        const int n_slices = (int)slice.size() - 1;
+        for (int k = 0; k + 1 < n_slices; k++) units.push_back({slice[k], slice[k + 1], 0, n});
+        const int n_last =
+            n_slices > 1 ? (int)std::min<int64_t>(kWhizardLastChunks, std::max<int64_t>(1, n >> 15)) : 1;
+        for (int j = 0; j < n_last; j++)
+          units.push_back({slice[n_slices - 1], nch, n * j / n_last, n * (j + 1) / n_last});
+        // channel starts relative to each launch's first event
+        std::vector<int64_t> begs((size_t)units.size() * nch);
+        for (size_t u = 0; u < units.size(); u++)
+          for (int c = 0; c < nch; c++) begs[u * nch + c] = beg[c] - units[u].e0;
+        if ((rc = W.dchb.reserve(begs.size() * sizeof(int64_t)))) { cudaStreamSynchronize(cs[0]); break; }
+        e = cudaMemcpyAsync(W.dchb.ptr, begs.data(), begs.size() * sizeof(int64_t), cudaMemcpyHostToDevice, cs[0]);
+        if (e == cudaSuccess) e = cudaEventRecord(W.done[0], cs[0]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(cs[1], W.done[0], 0);
+        if (e != cudaSuccess) rc = fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(e));
+        // do_inverse_mapping is forced on (whizard_gpu_phs.cpp:118): every channel's factor
+        // and x; the generating channel keeps its own x and factor (phs.cu:1580-1585), written
+        // with the other no-arithmetic outputs by the first launch (over every event)
+        for (size_t u = 0; u < units.size() && rc == PHS_OK; u++) {
+          const Unit &U = units[u];
+          const int64_t e0 = U.e0;
+          rc = inverse_launch(W.proc, U.e1 - e0, W.dchb.as<int64_t>() + u * nch,
+                              uniform ? nullptr : dE1 + e0, uniform ? nullptr : dE2 + e0,
+                              dp + e0 * 4 * n_out, dok + e0, dx + e0 * n_x, df + e0,
+                              W.dfa.as<double>() + e0 * nch, dxo + e0 * n_x, cs[u & 1], U.lo, U.hi,
+                              u == 0, n);
+          if (rc == PHS_OK && (e = cudaEventRecord(W.done[u + 1], cs[u & 1])) != cudaSuccess)
+            rc = fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(e));
+        }
+      }
+      if (rc == PHS_OK && (e = copy_back(n_fchunks - 1)) != cudaSuccess)
+        rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
+      const int32_t *order = W.proc->inv_order.data();
+      // the copy stream waits for the launches in order: launch u's rows are copied after
+      // every launch up to u (the first one's fixed outputs included) is done
+      for (size_t u = 0; u < units.size() && rc == PHS_OK && e == cudaSuccess; u++) {
         const Unit &U = units[u];
-        const int64_t e0 = U.e0;
-        rc = inverse_launch(W.proc, U.e1 - e0, W.dchb.as<int64_t>() + u * nch,
-                            uniform ? nullptr : dE1 + e0, uniform ? nullptr : dE2 + e0,
-                            dp + e0 * 4 * n_out, dok + e0, dx + e0 * n_x, df + e0,
-                            W.dfa.as<double>() + e0 * nch, dxo + e0 * n_x, cs[u & 1], U.lo, U.hi,
-                            u == 0, n);
-        if (rc == PHS_OK && (e = cudaEventRecord(W.done[u + 1], cs[u & 1])) != cudaSuccess)
-          rc = fail(PHS_ERR_CUDA, "%s", cudaGetErrorString(e));
+        e = cudaStreamWaitEvent(ms, W.done[u + 1], 0);
+        // device rows sit where the caller's do: a run of channels whose ids step evenly
+        // goes as one strided copy (one copy per row costs far more than its bytes)
+        const size_t width = (size_t)(U.e1 - U.e0) * n_x * sizeof(double);
+        for (int i = U.lo; i < U.hi && e == cudaSuccess && x_out;) {
+          const int step = i + 1 < U.hi ? order[i + 1] - order[i] : 0;
+          int j = i + 1;
+          if (step > 0)
+            while (j < U.hi && order[j] - order[j - 1] == step) j++;
+          const size_t pitch = step > 0 ? (size_t)step * n * n_x * sizeof(double) : width;
+          const size_t off = ((size_t)order[i] * n + U.e0) * n_x;
+          e = cudaMemcpy2DAsync(x_out + off, pitch, dxo + off, pitch, width, j - i,
+                                cudaMemcpyDeviceToHost, ms);
+          i = j;
+        }
+        if (e == cudaSuccess && U.hi == nch)
+          e = cudaMemcpyAsync(factors + U.e0 * nch, W.dfa.as<double>() + U.e0 * nch,
+                              (size_t)(U.e1 - U.e0) * nch * sizeof(double), cudaMemcpyDeviceToHost, ms);
+        if (e != cudaSuccess) rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
       }
-    }
-    if (rc == PHS_OK && (e = copy_back(n_fchunks - 1)) != cudaSuccess)
-      rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
-    const int32_t *order = W.proc->inv_order.data();
-    // the copy stream waits for the launches in order: launch u's rows are copied after
-    // every launch up to u (the first one's fixed outputs included) is done
-    for (size_t u = 0; u < units.size() && rc == PHS_OK && e == cudaSuccess; u++) {
-      const Unit &U = units[u];
-      e = cudaStreamWaitEvent(ms, W.done[u + 1], 0);
-      // device rows sit where the caller's do: a run of channels whose ids step evenly
-      // goes as one strided copy (one copy per row costs far more than its bytes)
-      const size_t width = (size_t)(U.e1 - U.e0) * n_x * sizeof(double);
-      for (int i = U.lo; i < U.hi && e == cudaSuccess && x_out;) {
-        const int step = i + 1 < U.hi ? order[i + 1] - order[i] : 0;
-        int j = i + 1;
-        if (step > 0)
-          while (j < U.hi && order[j] - order[j - 1] == step) j++;
-        const size_t pitch = step > 0 ? (size_t)step * n * n_x * sizeof(double) : width;
-        const size_t off = ((size_t)order[i] * n + U.e0) * n_x;
-        e = cudaMemcpy2DAsync(x_out + off, pitch, dxo + off, pitch, width, j - i,
-                              cudaMemcpyDeviceToHost, ms);
-        i = j;
+      if (rc == PHS_OK && (e = cudaStreamSynchronize(ms)) != cudaSuccess)
+        rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
+      if (rc) {
+        for (cudaStream_t st : W.streams) cudaStreamSynchronize(st);
+        break;
       }
-      if (e == cudaSuccess && U.hi == nch)
-        e = cudaMemcpyAsync(factors + U.e0 * nch, W.dfa.as<double>() + U.e0 * nch,
-                            (size_t)(U.e1 - U.e0) * nch * sizeof(double), cudaMemcpyDeviceToHost, ms);
-      if (e != cudaSuccess) rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
-    }
-    if (rc == PHS_OK && (e = cudaStreamSynchronize(ms)) != cudaSuccess)
-      rc = fail(PHS_ERR_CUDA, "copy back: %s", cudaGetErrorString(e));
-    if (rc) {
-      for (cudaStream_t st : W.streams) cudaStreamSynchronize(st);
-      break;
-    }
-    W.last_events = n;
-    W.sparse_ok = W.in_ok = false;  // the handoff buffers are rebuilt on request
-    W.last_uniform = uniform;
-    W.last_e1 = E1_in[0];
-    W.last_e2 = E2_in[0];
-  } while (0);
+      W.last_events = n;
+      W.sparse_ok = W.in_ok = false;  // the handoff buffers are rebuilt on request
+      W.last_uniform = uniform;
+      W.last_e1 = E1_in[0];
+      W.last_e2 = E2_in[0];
+    } while (0);
+  } catch (const std::exception &ex) {
+    rc = fail(PHS_ERR_ALLOC, "c_whizard_gen_phs_from_x_gpu: %s", ex.what());
+    for (cudaStream_t st : W.streams)
+      if (st) cudaStreamSynchronize(st);
+  }
   whizard_log(rc);
 }
 
