@@ -1,7 +1,7 @@
-"""ctypes front end for the CPU checkers.  TEST INFRASTRUCTURE ONLY.
+"""ctypes front end for the CPU oracles.  TEST INFRASTRUCTURE ONLY.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
-module.  Two checkers, both built by oracle/Makefile:
+module.  Two oracles, both built by oracle/Makefile:
 
 * ``Oracle``    -- the C restatement in phs_oracle.c (_build/libphsoracle.so).
 * ``RefCPU``    -- the reference's own phs_cpu.cpp driven by ref_harness.cpp

@@ -1,7 +1,7 @@
 /*
  * phs_oracle.c -- CPU restatement of gpu_phs's forward phase-space generator.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA path: only
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle for the CUDA path: only
  * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it.
  * Nothing in the gpu_phs_gb300 package links, imports or calls it.
  *

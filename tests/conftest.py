@@ -15,7 +15,7 @@ def pytest_configure(config):
 
 
 @pytest.fixture(scope="session", autouse=True)
-def _built_checkers():
+def _built_oracles():
     """The CPU oracle is a few ms of gcc; build it if this checkout has no copy yet."""
     so = os.path.join(ROOT, "oracle", "_build", "libphsoracle.so")
     if not os.path.exists(so):
