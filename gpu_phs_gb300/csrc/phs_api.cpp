@@ -33,6 +33,25 @@ static int fail(int code, const char *fmt, ...) {
   return code;
 }
 
+// Entry points run their bodies through these: no exception may leave a C function, so a
+// host failure (std::bad_alloc, std::system_error) becomes PHS_ERR_ALLOC with its message;
+// the void Whizard calls also print it, as they print every error.
+template <class Body>
+static int guarded(Body &&body) {
+  try {
+    return body();
+  } catch (const std::exception &ex) {
+    return fail(PHS_ERR_ALLOC, "host: %s", ex.what());
+  } catch (...) {
+    return fail(PHS_ERR_ALLOC, "host: unknown exception");
+  }
+}
+template <class Body>
+static void guarded_void(Body &&body) {
+  if (guarded([&]() -> int { body(); return PHS_OK; }) != PHS_OK)
+    fprintf(stderr, "gpu_phs: %s\n", g_err.c_str());
+}
+
 #define CUDA_TRY(call)                                                                    \
   do {                                                                                    \
     cudaError_t e_ = (call);                                                              \
@@ -362,230 +381,240 @@ extern "C" int phs_process_create(phs_process_t *out, int n_in, int n_out, int n
                                   const int *d1, const int *d2, const int *hc, const int *friends,
                                   const int *map_ids, const double *map_m, const double *map_w,
                                   const double *flv_m, const double *flv_w) {
-  if (!out) return fail(PHS_ERR_INVALID_ARG, "null output handle pointer");
-  *out = nullptr;
-  if (!d1 || !d2 || !hc || !map_ids || !map_m || !map_w || !flv_m)
-    return fail(PHS_ERR_INVALID_ARG, "null table pointer");
-  phs::Process P;
-  P.n_in = n_in;
-  P.n_out = n_out;
-  P.n_channels = n_channels;
-  P.n_x = n_x;
-  std::string err;
-  int rc = phs::validate_process(P, err);
-  if (rc) return fail(rc, "%s", err.c_str());
-  P.n_prt = (1 << (n_in + n_out)) - 1;
-  P.n_prt_out = (1 << n_out) - 1;
-  const size_t nt = (size_t)n_channels * P.n_prt, nm = (size_t)n_channels * P.n_prt_out;
-  P.d1.assign(d1, d1 + nt);
-  P.d2.assign(d2, d2 + nt);
-  P.has_children.assign(hc, hc + nt);
-  P.friends = friends ? std::vector<int>(friends, friends + nt) : std::vector<int>(nt, 0);
-  P.map_id.assign(map_ids, map_ids + nm);
-  P.map_m.assign(map_m, map_m + nm);
-  P.map_w.assign(map_w, map_w + nm);
-  P.flv_m.assign(flv_m, flv_m + n_in + n_out);
-  P.flv_w = flv_w ? std::vector<double>(flv_w, flv_w + n_in + n_out)
-                  : std::vector<double>(n_in + n_out, 0.0);
-  // structural validation at a nominal sqrt(s) (constants are recompiled by set_beams)
-  for (int c = 0; c < n_channels; c++) {
-    PhsChannel tmp;
-    phs::ChannelInfo info;
-    double m_tot = 0;
-    for (int k = 0; k < n_out; k++) m_tot += P.flv_m[n_in + k];
-    rc = phs::compile_channel(P, c, 2 * m_tot + 1000.0, tmp, info, err);
+  return guarded([&]() -> int {
+    if (!out) return fail(PHS_ERR_INVALID_ARG, "null output handle pointer");
+    *out = nullptr;
+    if (!d1 || !d2 || !hc || !map_ids || !map_m || !map_w || !flv_m)
+      return fail(PHS_ERR_INVALID_ARG, "null table pointer");
+    phs::Process P;
+    P.n_in = n_in;
+    P.n_out = n_out;
+    P.n_channels = n_channels;
+    P.n_x = n_x;
+    std::string err;
+    int rc = phs::validate_process(P, err);
     if (rc) return fail(rc, "%s", err.c_str());
-  }
-  phs_process *h = new phs_process;
-  h->p = std::move(P);
-  cudaGetDevice(&h->device);
-  *out = h;
-  return PHS_OK;
+    P.n_prt = (1 << (n_in + n_out)) - 1;
+    P.n_prt_out = (1 << n_out) - 1;
+    const size_t nt = (size_t)n_channels * P.n_prt, nm = (size_t)n_channels * P.n_prt_out;
+    P.d1.assign(d1, d1 + nt);
+    P.d2.assign(d2, d2 + nt);
+    P.has_children.assign(hc, hc + nt);
+    P.friends = friends ? std::vector<int>(friends, friends + nt) : std::vector<int>(nt, 0);
+    P.map_id.assign(map_ids, map_ids + nm);
+    P.map_m.assign(map_m, map_m + nm);
+    P.map_w.assign(map_w, map_w + nm);
+    P.flv_m.assign(flv_m, flv_m + n_in + n_out);
+    P.flv_w = flv_w ? std::vector<double>(flv_w, flv_w + n_in + n_out)
+                    : std::vector<double>(n_in + n_out, 0.0);
+    // structural validation at a nominal sqrt(s) (constants are recompiled by set_beams)
+    for (int c = 0; c < n_channels; c++) {
+      PhsChannel tmp;
+      phs::ChannelInfo info;
+      double m_tot = 0;
+      for (int k = 0; k < n_out; k++) m_tot += P.flv_m[n_in + k];
+      rc = phs::compile_channel(P, c, 2 * m_tot + 1000.0, tmp, info, err);
+      if (rc) return fail(rc, "%s", err.c_str());
+    }
+    phs_process *h = new phs_process;
+    h->p = std::move(P);
+    cudaGetDevice(&h->device);
+    *out = h;
+    return PHS_OK;
+  });
 }
 
 extern "C" int phs_process_destroy(phs_process_t h) {
-  if (!h) return PHS_OK;
-  DeviceGuard g(h->device);
-  for (int s = 0; s < phs_process::kStreams; s++) {
-    if (h->streams[s]) cudaStreamDestroy(h->streams[s]);
-    h->bx[s].release(); h->bp[s].release(); h->bf[s].release(); h->bv[s].release();
-    h->bo[s].release(); h->pseg[s].release();
-  }
-  h->d_prog.release();
-  h->d_prog_ff.release();
-  h->d_prog_adj.release();
-  h->d_ch_begin.release();
-  h->d_inv_groups.release();
-  h->segs.release();
-  delete h;
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (!h) return PHS_OK;
+    DeviceGuard g(h->device);
+    for (int s = 0; s < phs_process::kStreams; s++) {
+      if (h->streams[s]) cudaStreamDestroy(h->streams[s]);
+      h->bx[s].release(); h->bp[s].release(); h->bf[s].release(); h->bv[s].release();
+      h->bo[s].release(); h->pseg[s].release();
+    }
+    h->d_prog.release();
+    h->d_prog_ff.release();
+    h->d_prog_adj.release();
+    h->d_ch_begin.release();
+    h->d_inv_groups.release();
+    h->segs.release();
+    delete h;
+    return PHS_OK;
+  });
 }
 
 extern "C" int phs_process_set_beams(phs_process_t h, double E1, double E2) {
-  if (int rc = check_proc(h)) return rc;
-  if (!(E1 > 0) || !(E2 > 0) || !isfinite(E1) || !isfinite(E2))
-    return fail(PHS_ERR_INVALID_ARG, "beam energies must be positive and finite");
-  if (h->beams && h->E1 == E1 && h->E2 == E2) return PHS_OK;
-  DeviceGuard g(h->device);
-  const phs::Process &P = h->p;
-  const double sqrts = 2 * sqrt(E1 * E2);
-  double m_tot = 0;
-  for (int k = 0; k < P.n_out; k++) m_tot += P.flv_m[P.n_in + k];
-  if (!(sqrts > m_tot))
-    return fail(PHS_ERR_INVALID_ARG, "sqrt(s) = %g is below the final-state mass sum %g", sqrts,
-                m_tot);
-  std::vector<PhsChannel> prog(P.n_channels);
-  int depth = 0;
-  std::string err;
-  const double bg = (E1 - E2) / (2 * sqrt(E1 * E2));
-  for (int c = 0; c < P.n_channels; c++) {
-    phs::ChannelInfo info;
-    int rc = phs::compile_channel(P, c, sqrts, prog[c], info, err);
-    if (rc) return fail(rc, "%s", err.c_str());
-    prog[c].sqrts = sqrts;
-    prog[c].lab = E1 != E2;
-    prog[c].lab_bg = bg;
-    prog[c].lab_gamma = sqrt(1 + bg * bg);
-    depth = std::max(depth, info.stack_depth);
-  }
-  std::vector<PhsChannelFF> prog_ff(prog.size());
-  std::vector<PhsAdjChannel> prog_adj(prog.size());
-  int max_visits = 0, max_pops = 0;
-  for (size_t c = 0; c < prog.size(); c++) {
-    phs::channel_to_ff(prog[c], prog_ff[c]);
-    phs::channel_adjoint(prog[c], prog_adj[c]);
-    max_visits = std::max(max_visits, (int)prog[c].n_visits);
-    max_pops = std::max(max_pops, (int)prog_adj[c].n_pops);
-  }
-  int rc = h->d_prog.reserve(prog.size() * sizeof(PhsChannel));
-  if (rc) return rc;
-  if ((rc = h->d_prog_ff.reserve(prog_ff.size() * sizeof(PhsChannelFF)))) return rc;
-  if ((rc = h->d_prog_adj.reserve(prog_adj.size() * sizeof(PhsAdjChannel)))) return rc;
-  CUDA_TRY(cudaMemcpy(h->d_prog_adj.ptr, prog_adj.data(), prog_adj.size() * sizeof(PhsAdjChannel),
-                      cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(h->d_prog.ptr, prog.data(), prog.size() * sizeof(PhsChannel),
-                      cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(h->d_prog_ff.ptr, prog_ff.data(), prog_ff.size() * sizeof(PhsChannelFF),
-                      cudaMemcpyHostToDevice));
-  // channels of equal tree shape share the inverse map's geometry: order them by shape
-  {
-    std::vector<std::vector<int32_t>> keys;
-    std::vector<std::vector<int32_t>> members;
-    for (int c = 0; c < (int)prog.size(); c++) {
-      const PhsChannel &ch = prog[c];
-      std::vector<int32_t> key = {ch.n_out, ch.n_visits, ch.n_vol};
-      for (int i = 0; i < ch.n_vol; i++) {
-        key.push_back(ch.comb[i][0]);
-        key.push_back(ch.comb[i][1]);
-      }
-      for (int v = 0; v < ch.n_visits; v++) {
-        const PhsVisit &V = ch.visit[v];
-        key.insert(key.end(), {V.slot[0], V.slot[1], V.friend_sign, V.carry, V.push,
-                               V.both_leaves, V.self_root, V.x_phi, V.x_ct});
-        for (int j = 0; j < 2; j++)
-          key.insert(key.end(), {V.child[j].internal, V.child[j].x_msq, V.child[j].out_index});
-      }
-      size_t g = 0;
-      while (g < keys.size() && keys[g] != key) g++;
-      if (g == keys.size()) {
-        keys.push_back(key);
-        members.emplace_back();
-      }
-      members[g].push_back(c);
+  return guarded([&]() -> int {
+    if (int rc = check_proc(h)) return rc;
+    if (!(E1 > 0) || !(E2 > 0) || !isfinite(E1) || !isfinite(E2))
+      return fail(PHS_ERR_INVALID_ARG, "beam energies must be positive and finite");
+    if (h->beams && h->E1 == E1 && h->E2 == E2) return PHS_OK;
+    DeviceGuard g(h->device);
+    const phs::Process &P = h->p;
+    const double sqrts = 2 * sqrt(E1 * E2);
+    double m_tot = 0;
+    for (int k = 0; k < P.n_out; k++) m_tot += P.flv_m[P.n_in + k];
+    if (!(sqrts > m_tot))
+      return fail(PHS_ERR_INVALID_ARG, "sqrt(s) = %g is below the final-state mass sum %g", sqrts,
+                  m_tot);
+    std::vector<PhsChannel> prog(P.n_channels);
+    int depth = 0;
+    std::string err;
+    const double bg = (E1 - E2) / (2 * sqrt(E1 * E2));
+    for (int c = 0; c < P.n_channels; c++) {
+      phs::ChannelInfo info;
+      int rc = phs::compile_channel(P, c, sqrts, prog[c], info, err);
+      if (rc) return fail(rc, "%s", err.c_str());
+      prog[c].sqrts = sqrts;
+      prog[c].lab = E1 != E2;
+      prog[c].lab_bg = bg;
+      prog[c].lab_gamma = sqrt(1 + bg * bg);
+      depth = std::max(depth, info.stack_depth);
     }
-    // within a shape, channels in order of their mappings, so that equal ones follow each
-    // other: a channel reuses the previous channel's mapping results wherever the two have
-    // the same mapping (position 3 v + 0/1: a daughter's msq map, 3 v + 2: the cos(theta) map)
-    auto mapping = [&](int c, int v, int k) {
-      std::vector<double> sig;
-      const PhsVisit &V = prog[c].visit[v];
-      if (k < 2) {
-        const PhsChild &C = V.child[k];
-        if (!C.internal) return sig;
-        sig = {(double)C.map_id, C.m, C.w, C.m_min, C.a0, C.a1, C.a2, C.msq_min, C.msq_max};
-      } else {
-        sig = {(double)V.ct_class, V.b0, V.b1, V.m};
+    std::vector<PhsChannelFF> prog_ff(prog.size());
+    std::vector<PhsAdjChannel> prog_adj(prog.size());
+    int max_visits = 0, max_pops = 0;
+    for (size_t c = 0; c < prog.size(); c++) {
+      phs::channel_to_ff(prog[c], prog_ff[c]);
+      phs::channel_adjoint(prog[c], prog_adj[c]);
+      max_visits = std::max(max_visits, (int)prog[c].n_visits);
+      max_pops = std::max(max_pops, (int)prog_adj[c].n_pops);
+    }
+    int rc = h->d_prog.reserve(prog.size() * sizeof(PhsChannel));
+    if (rc) return rc;
+    if ((rc = h->d_prog_ff.reserve(prog_ff.size() * sizeof(PhsChannelFF)))) return rc;
+    if ((rc = h->d_prog_adj.reserve(prog_adj.size() * sizeof(PhsAdjChannel)))) return rc;
+    CUDA_TRY(cudaMemcpy(h->d_prog_adj.ptr, prog_adj.data(), prog_adj.size() * sizeof(PhsAdjChannel),
+                        cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(h->d_prog.ptr, prog.data(), prog.size() * sizeof(PhsChannel),
+                        cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(h->d_prog_ff.ptr, prog_ff.data(), prog_ff.size() * sizeof(PhsChannelFF),
+                        cudaMemcpyHostToDevice));
+    // channels of equal tree shape share the inverse map's geometry: order them by shape
+    {
+      std::vector<std::vector<int32_t>> keys;
+      std::vector<std::vector<int32_t>> members;
+      for (int c = 0; c < (int)prog.size(); c++) {
+        const PhsChannel &ch = prog[c];
+        std::vector<int32_t> key = {ch.n_out, ch.n_visits, ch.n_vol};
+        for (int i = 0; i < ch.n_vol; i++) {
+          key.push_back(ch.comb[i][0]);
+          key.push_back(ch.comb[i][1]);
+        }
+        for (int v = 0; v < ch.n_visits; v++) {
+          const PhsVisit &V = ch.visit[v];
+          key.insert(key.end(), {V.slot[0], V.slot[1], V.friend_sign, V.carry, V.push,
+                                 V.both_leaves, V.self_root, V.x_phi, V.x_ct});
+          for (int j = 0; j < 2; j++)
+            key.insert(key.end(), {V.child[j].internal, V.child[j].x_msq, V.child[j].out_index});
+        }
+        size_t g = 0;
+        while (g < keys.size() && keys[g] != key) g++;
+        if (g == keys.size()) {
+          keys.push_back(key);
+          members.emplace_back();
+        }
+        members[g].push_back(c);
       }
-      return sig;
-    };
-    // signatures compare by their bits (a strict weak order even with -0.0 or NaN)
-    auto bits = [](const std::vector<double> &x) {
-      std::vector<uint64_t> b(x.size());
-      if (!x.empty()) memcpy(b.data(), x.data(), x.size() * sizeof(double));
-      return b;
-    };
-    auto same = [&](const std::vector<double> &x, const std::vector<double> &y) {
-      return bits(x) == bits(y);
-    };
-    std::vector<int32_t> order;
-    std::vector<uint64_t> reuse;
-    for (auto &m : members) {
-      const int nv = prog[m[0]].n_visits;
-      std::stable_sort(m.begin(), m.end(), [&](int c1, int c2) {
-        for (int v = 0; v < nv; v++)
-          for (int k = 0; k < 3; k++) {
-            const auto x = bits(mapping(c1, v, k)), y = bits(mapping(c2, v, k));
-            if (x != y) return x < y;
-          }
-        return false;
-      });
-      for (size_t i = 0; i < m.size(); i++) {
-        uint64_t mask = 0;
-        if (i > 0)
-          for (int v = 0; v < nv && 3 * v + 2 < 64; v++)
+      // within a shape, channels in order of their mappings, so that equal ones follow each
+      // other: a channel reuses the previous channel's mapping results wherever the two have
+      // the same mapping (position 3 v + 0/1: a daughter's msq map, 3 v + 2: the cos(theta) map)
+      auto mapping = [&](int c, int v, int k) {
+        std::vector<double> sig;
+        const PhsVisit &V = prog[c].visit[v];
+        if (k < 2) {
+          const PhsChild &C = V.child[k];
+          if (!C.internal) return sig;
+          sig = {(double)C.map_id, C.m, C.w, C.m_min, C.a0, C.a1, C.a2, C.msq_min, C.msq_max};
+        } else {
+          sig = {(double)V.ct_class, V.b0, V.b1, V.m};
+        }
+        return sig;
+      };
+      // signatures compare by their bits (a strict weak order even with -0.0 or NaN)
+      auto bits = [](const std::vector<double> &x) {
+        std::vector<uint64_t> b(x.size());
+        if (!x.empty()) memcpy(b.data(), x.data(), x.size() * sizeof(double));
+        return b;
+      };
+      auto same = [&](const std::vector<double> &x, const std::vector<double> &y) {
+        return bits(x) == bits(y);
+      };
+      std::vector<int32_t> order;
+      std::vector<uint64_t> reuse;
+      for (auto &m : members) {
+        const int nv = prog[m[0]].n_visits;
+        std::stable_sort(m.begin(), m.end(), [&](int c1, int c2) {
+          for (int v = 0; v < nv; v++)
             for (int k = 0; k < 3; k++) {
-              const auto x = mapping(m[i], v, k);
-              if (!x.empty() && same(x, mapping(m[i - 1], v, k))) mask |= 1ull << (3 * v + k);
+              const auto x = bits(mapping(c1, v, k)), y = bits(mapping(c2, v, k));
+              if (x != y) return x < y;
             }
-        order.push_back(m[i]);
-        reuse.push_back(mask);
+          return false;
+        });
+        for (size_t i = 0; i < m.size(); i++) {
+          uint64_t mask = 0;
+          if (i > 0)
+            for (int v = 0; v < nv && 3 * v + 2 < 64; v++)
+              for (int k = 0; k < 3; k++) {
+                const auto x = mapping(m[i], v, k);
+                if (!x.empty() && same(x, mapping(m[i - 1], v, k))) mask |= 1ull << (3 * v + k);
+              }
+          order.push_back(m[i]);
+          reuse.push_back(mask);
+        }
       }
+      // [order n_channels][begin n_groups + 1], then the reuse masks (8-byte aligned)
+      std::vector<int32_t> table = order;
+      int32_t at = 0;
+      table.push_back(at);
+      for (const auto &m : members) table.push_back(at += (int32_t)m.size());
+      if (table.size() % 2) table.push_back(0);
+      const size_t head = table.size() * sizeof(int32_t);
+      if ((rc = h->d_inv_groups.reserve(head + reuse.size() * sizeof(uint64_t)))) return rc;
+      CUDA_TRY(cudaMemcpy(h->d_inv_groups.ptr, table.data(), head, cudaMemcpyHostToDevice));
+      CUDA_TRY(cudaMemcpy(static_cast<char *>(h->d_inv_groups.ptr) + head, reuse.data(),
+                          reuse.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
+      h->n_inv_groups = (int)members.size();
+      h->inv_reuse_offset = head;
+      h->inv_order = order;
+      h->inv_group_begin.assign(table.begin() + order.size(), table.begin() + order.size() + members.size() + 1);
     }
-    // [order n_channels][begin n_groups + 1], then the reuse masks (8-byte aligned)
-    std::vector<int32_t> table = order;
-    int32_t at = 0;
-    table.push_back(at);
-    for (const auto &m : members) table.push_back(at += (int32_t)m.size());
-    if (table.size() % 2) table.push_back(0);
-    const size_t head = table.size() * sizeof(int32_t);
-    if ((rc = h->d_inv_groups.reserve(head + reuse.size() * sizeof(uint64_t)))) return rc;
-    CUDA_TRY(cudaMemcpy(h->d_inv_groups.ptr, table.data(), head, cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaMemcpy(static_cast<char *>(h->d_inv_groups.ptr) + head, reuse.data(),
-                        reuse.size() * sizeof(uint64_t), cudaMemcpyHostToDevice));
-    h->n_inv_groups = (int)members.size();
-    h->inv_reuse_offset = head;
-    h->inv_order = order;
-    h->inv_group_begin.assign(table.begin() + order.size(), table.begin() + order.size() + members.size() + 1);
-  }
-  h->prog = std::move(prog);
-  h->prog_ff = std::move(prog_ff);
-  h->prog_adj = std::move(prog_adj);
-  h->max_visits = max_visits;
-  h->max_pops = max_pops;
-  h->lay.assign(P.n_channels, ChanLayout{P.n_out, P.n_x});
-  h->has_friends = false;
-  for (const auto &ch : h->prog)
-    for (int v = 0; v < ch.n_visits; v++) h->has_friends |= ch.visit[v].friend_sign != 0;
-  h->stack_depth = depth;
-  h->E1 = E1;
-  h->E2 = E2;
-  h->beams = true;
-  return PHS_OK;
+    h->prog = std::move(prog);
+    h->prog_ff = std::move(prog_ff);
+    h->prog_adj = std::move(prog_adj);
+    h->max_visits = max_visits;
+    h->max_pops = max_pops;
+    h->lay.assign(P.n_channels, ChanLayout{P.n_out, P.n_x});
+    h->has_friends = false;
+    for (const auto &ch : h->prog)
+      for (int v = 0; v < ch.n_visits; v++) h->has_friends |= ch.visit[v].friend_sign != 0;
+    h->stack_depth = depth;
+    h->E1 = E1;
+    h->E2 = E2;
+    h->beams = true;
+    return PHS_OK;
+  });
 }
 
 extern "C" int phs_process_set_precision(phs_process_t h, int precision) {
-  if (int rc = check_proc(h)) return rc;
-  if (precision != PHS_PRECISION_F64 && precision != PHS_PRECISION_F32X2)
-    return fail(PHS_ERR_INVALID_ARG, "unknown precision mode %d", precision);
-  h->precision = precision;
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (int rc = check_proc(h)) return rc;
+    if (precision != PHS_PRECISION_F64 && precision != PHS_PRECISION_F32X2)
+      return fail(PHS_ERR_INVALID_ARG, "unknown precision mode %d", precision);
+    h->precision = precision;
+    return PHS_OK;
+  });
 }
 
 extern "C" int phs_process_tuning(phs_process_t h, int *ff_variant, int *f64_variant) {
-  if (int rc = check_proc(h)) return rc;
-  if (ff_variant) *ff_variant = h->ff_variant_ev[0];
-  if (f64_variant) *f64_variant = h->f64_variant[0];
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (int rc = check_proc(h)) return rc;
+    if (ff_variant) *ff_variant = h->ff_variant_ev[0];
+    if (f64_variant) *f64_variant = h->f64_variant[0];
+    return PHS_OK;
+  });
 }
 
 static int check_variants(int ff_variant, int f64_variant) {
@@ -599,31 +628,35 @@ static int check_variants(int ff_variant, int f64_variant) {
 }
 
 extern "C" int phs_process_set_variants(phs_process_t h, int ff_variant, int f64_variant) {
-  if (int rc = check_proc(h)) return rc;
-  if (int rc = check_variants(ff_variant, f64_variant)) return rc;
-  h->ff_variant_ev[0] = h->ff_variant_ev[1] = ff_variant;
-  h->f64_variant[0] = h->f64_variant[1] = f64_variant;
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (int rc = check_proc(h)) return rc;
+    if (int rc = check_variants(ff_variant, f64_variant)) return rc;
+    h->ff_variant_ev[0] = h->ff_variant_ev[1] = ff_variant;
+    h->f64_variant[0] = h->f64_variant[1] = f64_variant;
+    return PHS_OK;
+  });
 }
 
 extern "C" int phs_process_info(phs_process_t h, int *n_in, int *n_out, int *n_channels, int *n_x,
                                 int *depth) {
-  if (int rc = check_proc(h)) return rc;
-  if (n_in) *n_in = h->p.n_in;
-  if (n_out) *n_out = h->p.n_out;
-  if (n_channels) *n_channels = h->p.n_channels;
-  if (n_x) *n_x = h->p.n_x;
-  if (depth) {
-    int d = 0;
-    for (int c = 0; c < h->p.n_channels; c++) {
-      PhsChannel tmp;
-      phs::ChannelInfo info;
-      std::string err;
-      if (phs::compile_channel(h->p, c, 1e4, tmp, info, err) == 0) d = std::max(d, info.stack_depth);
+  return guarded([&]() -> int {
+    if (int rc = check_proc(h)) return rc;
+    if (n_in) *n_in = h->p.n_in;
+    if (n_out) *n_out = h->p.n_out;
+    if (n_channels) *n_channels = h->p.n_channels;
+    if (n_x) *n_x = h->p.n_x;
+    if (depth) {
+      int d = 0;
+      for (int c = 0; c < h->p.n_channels; c++) {
+        PhsChannel tmp;
+        phs::ChannelInfo info;
+        std::string err;
+        if (phs::compile_channel(h->p, c, 1e4, tmp, info, err) == 0) d = std::max(d, info.stack_depth);
+      }
+      *depth = d;
     }
-    *depth = d;
-  }
-  return PHS_OK;
+    return PHS_OK;
+  });
 }
 
 static int check_counts(const int64_t *counts, int n_channels, int64_t n_events) {
@@ -686,63 +719,69 @@ static int check_ptrs(int64_t n, const void *x, const void *p, const void *f, co
 extern "C" int phs_generate_device(phs_process_t h, int64_t n_events, const int64_t *counts,
                                    const double *x, double *p, double *f, double *v, uint8_t *ok,
                                    void *stream) {
-  if (int rc = check_proc(h)) return rc;
-  if (!h->beams) return fail(PHS_ERR_STATE, "phs_process_set_beams has not been called");
-  if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
-  if (int rc = check_ptrs(n_events, x, p, f, v, ok)) return rc;
-  DeviceGuard g(h->device);
-  return launch_process(h, h->segs, n_events, counts, 0, x, p, f, v, ok, nullptr, nullptr, 1,
-                        false, (cudaStream_t)stream);
+  return guarded([&]() -> int {
+    if (int rc = check_proc(h)) return rc;
+    if (!h->beams) return fail(PHS_ERR_STATE, "phs_process_set_beams has not been called");
+    if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
+    if (int rc = check_ptrs(n_events, x, p, f, v, ok)) return rc;
+    DeviceGuard g(h->device);
+    return launch_process(h, h->segs, n_events, counts, 0, x, p, f, v, ok, nullptr, nullptr, 1,
+                          false, (cudaStream_t)stream);
+  });
 }
 
 extern "C" int phs_generate_beams_device(phs_process_t h, int64_t n_events, const int64_t *counts,
                                          const double *E1, const double *E2, const double *x,
                                          double *p, double *f, double *v, uint8_t *ok,
                                          void *stream) {
-  if (int rc = check_proc(h)) return rc;
-  if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
-  if (int rc = check_ptrs(n_events, x, p, f, v, ok)) return rc;
-  if (n_events > 0 && (!E1 || !E2)) return fail(PHS_ERR_INVALID_ARG, "null beam energy pointer");
-  DeviceGuard g(h->device);
-  if (!h->beams) {
-    // programs need compiling once; per-event constants replace the uniform ones
-    double m_tot = 0;
-    for (int k = 0; k < h->p.n_out; k++) m_tot += h->p.flv_m[h->p.n_in + k];
-    int rc = phs_process_set_beams(h, m_tot + 500.0, m_tot + 500.0);
-    if (rc) return rc;
-  }
-  return launch_process(h, h->segs, n_events, counts, 0, x, p, f, v, ok, E1, E2, 1, false,
-                        (cudaStream_t)stream);
+  return guarded([&]() -> int {
+    if (int rc = check_proc(h)) return rc;
+    if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
+    if (int rc = check_ptrs(n_events, x, p, f, v, ok)) return rc;
+    if (n_events > 0 && (!E1 || !E2)) return fail(PHS_ERR_INVALID_ARG, "null beam energy pointer");
+    DeviceGuard g(h->device);
+    if (!h->beams) {
+      // programs need compiling once; per-event constants replace the uniform ones
+      double m_tot = 0;
+      for (int k = 0; k < h->p.n_out; k++) m_tot += h->p.flv_m[h->p.n_in + k];
+      int rc = phs_process_set_beams(h, m_tot + 500.0, m_tot + 500.0);
+      if (rc) return rc;
+    }
+    return launch_process(h, h->segs, n_events, counts, 0, x, p, f, v, ok, E1, E2, 1, false,
+                          (cudaStream_t)stream);
+  });
 }
 
 // Reverse-mode derivatives for cotangents pbar (momenta) and jbar (log-Jacobian).
 extern "C" int phs_adjoint_device(phs_process_t h, int64_t n_events, const int64_t *counts,
                                   const double *x, const double *pbar, const double *jbar,
                                   double *xbar, double *thbar, void *stream) {
-  if (int rc = check_proc(h)) return rc;
-  if (!h->beams) return fail(PHS_ERR_STATE, "phs_process_set_beams has not been called");
-  if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
-  if (n_events > 0 && (!x || !pbar || !xbar || !thbar))
-    return fail(PHS_ERR_INVALID_ARG, "null data pointer");
-  DeviceGuard g(h->device);
-  int64_t one = n_events;
-  int rc = build_segments(h->segs, counts ? counts : &one, h->p.n_channels, h->lay, 0, 0, 0, false);
-  if (rc) return rc;
-  PhsLaunch a;
-  memset(&a, 0, sizeof a);
-  a.channels = h->d_prog.as<PhsChannel>();
-  a.stack_depth = h->stack_depth;
-  a.x = x;
-  if ((rc = attach_segments(h->segs, a, (cudaStream_t)stream))) return rc;
-  if (a.n_tiles == 0) return PHS_OK;
-  const int per_sm =
-      phs_adjoint_blocks_per_sm(h->max_visits, h->max_pops, h->stack_depth, h->has_friends);
-  const int64_t want = (a.n_tiles + PHS_ADJ_BLOCK_HOST / 32 - 1) / (PHS_ADJ_BLOCK_HOST / 32);
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sm_count(h->device) * per_sm));
-  CUDA_TRY(phs_launch_adjoint(a, h->d_prog_adj.as<PhsAdjChannel>(), pbar, jbar, xbar, thbar,
-                              2 * std::max(1, h->p.n_out - 2), h->max_visits, h->max_pops,
-                              h->has_friends, grid, (cudaStream_t)stream));
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (int rc = check_proc(h)) return rc;
+    if (!h->beams) return fail(PHS_ERR_STATE, "phs_process_set_beams has not been called");
+    if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
+    if (n_events > 0 && (!x || !pbar || !xbar || !thbar))
+      return fail(PHS_ERR_INVALID_ARG, "null data pointer");
+    DeviceGuard g(h->device);
+    int64_t one = n_events;
+    int rc = build_segments(h->segs, counts ? counts : &one, h->p.n_channels, h->lay, 0, 0, 0, false);
+    if (rc) return rc;
+    PhsLaunch a;
+    memset(&a, 0, sizeof a);
+    a.channels = h->d_prog.as<PhsChannel>();
+    a.stack_depth = h->stack_depth;
+    a.x = x;
+    if ((rc = attach_segments(h->segs, a, (cudaStream_t)stream))) return rc;
+    if (a.n_tiles == 0) return PHS_OK;
+    const int per_sm =
+        phs_adjoint_blocks_per_sm(h->max_visits, h->max_pops, h->stack_depth, h->has_friends);
+    const int64_t want = (a.n_tiles + PHS_ADJ_BLOCK_HOST / 32 - 1) / (PHS_ADJ_BLOCK_HOST / 32);
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sm_count(h->device) * per_sm));
+    CUDA_TRY(phs_launch_adjoint(a, h->d_prog_adj.as<PhsAdjChannel>(), pbar, jbar, xbar, thbar,
+                                2 * std::max(1, h->p.n_out - 2), h->max_visits, h->max_pops,
+                                h->has_friends, grid, (cudaStream_t)stream));
+    return PHS_OK;
+  });
 }
 
 // Inverse map: all-channel factors and x of generated events.
@@ -757,36 +796,38 @@ extern "C" int phs_inverse_device(phs_process_t h, int64_t n_events, const int64
                                   const uint8_t *ok, const double *x_own,
                                   const double *factor_own, double *all_factors, double *x_out,
                                   void *stream) {
-  if (int rc = check_proc(h)) return rc;
-  if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
-  if (n_events > 0 && (!p || !all_factors || !x_out))
-    return fail(PHS_ERR_INVALID_ARG, "null data pointer");
-  if ((E1 == nullptr) != (E2 == nullptr))
-    return fail(PHS_ERR_INVALID_ARG, "give both beam energy arrays or neither");
-  if (((uintptr_t)p & 15) != 0) return fail(PHS_ERR_INVALID_ARG, "p must be 16-byte aligned");
-  DeviceGuard g(h->device);
-  if (!h->beams) {
-    if (!E1) return fail(PHS_ERR_STATE, "phs_process_set_beams has not been called");
-    double m_tot = 0;
-    for (int k = 0; k < h->p.n_out; k++) m_tot += h->p.flv_m[h->p.n_in + k];
-    int rc = phs_process_set_beams(h, m_tot + 500.0, m_tot + 500.0);
-    if (rc) return rc;
-  }
-  if (n_events == 0) return PHS_OK;
-  const int nch = h->p.n_channels;
-  std::vector<int64_t> begin(nch, 0);
-  for (int c = 1; c < nch; c++) begin[c] = begin[c - 1] + (counts ? counts[c - 1] : n_events);
-  cudaStream_t st = (cudaStream_t)stream;
-  if (begin != h->ch_begin_up) {
-    int rc = h->d_ch_begin.reserve(nch * sizeof(int64_t));
-    if (rc) return rc;
-    CUDA_TRY(cudaMemcpyAsync(h->d_ch_begin.ptr, begin.data(), nch * sizeof(int64_t),
-                             cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
-    h->ch_begin_up = begin;
-  }
-  return inverse_launch(h, n_events, h->d_ch_begin.as<int64_t>(), E1, E2, p, ok, x_own,
-                        factor_own, all_factors, x_out, st);
+  return guarded([&]() -> int {
+    if (int rc = check_proc(h)) return rc;
+    if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
+    if (n_events > 0 && (!p || !all_factors || !x_out))
+      return fail(PHS_ERR_INVALID_ARG, "null data pointer");
+    if ((E1 == nullptr) != (E2 == nullptr))
+      return fail(PHS_ERR_INVALID_ARG, "give both beam energy arrays or neither");
+    if (((uintptr_t)p & 15) != 0) return fail(PHS_ERR_INVALID_ARG, "p must be 16-byte aligned");
+    DeviceGuard g(h->device);
+    if (!h->beams) {
+      if (!E1) return fail(PHS_ERR_STATE, "phs_process_set_beams has not been called");
+      double m_tot = 0;
+      for (int k = 0; k < h->p.n_out; k++) m_tot += h->p.flv_m[h->p.n_in + k];
+      int rc = phs_process_set_beams(h, m_tot + 500.0, m_tot + 500.0);
+      if (rc) return rc;
+    }
+    if (n_events == 0) return PHS_OK;
+    const int nch = h->p.n_channels;
+    std::vector<int64_t> begin(nch, 0);
+    for (int c = 1; c < nch; c++) begin[c] = begin[c - 1] + (counts ? counts[c - 1] : n_events);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (begin != h->ch_begin_up) {
+      int rc = h->d_ch_begin.reserve(nch * sizeof(int64_t));
+      if (rc) return rc;
+      CUDA_TRY(cudaMemcpyAsync(h->d_ch_begin.ptr, begin.data(), nch * sizeof(int64_t),
+                               cudaMemcpyHostToDevice, st));
+      CUDA_TRY(cudaStreamSynchronize(st));
+      h->ch_begin_up = begin;
+    }
+    return inverse_launch(h, n_events, h->d_ch_begin.as<int64_t>(), E1, E2, p, ok, x_own,
+                          factor_own, all_factors, x_out, st);
+  });
 }
 
 // The inverse-map launch of n_events (channel starts d_ch_begin[n_channels] on the device)
@@ -840,51 +881,53 @@ static int inverse_launch(phs_process_t h, int64_t n_events, const int64_t *d_ch
 // after its previous chunk's copies back have been ordered before the next copy in.
 extern "C" int phs_generate_host(phs_process_t h, int64_t n_events, const int64_t *counts,
                                  const double *x, double *p, double *f, double *v, uint8_t *ok) {
-  if (int rc = check_proc(h)) return rc;
-  if (!h->beams) return fail(PHS_ERR_STATE, "phs_process_set_beams has not been called");
-  if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
-  if (n_events > 0 && (!x || !p || !f || !v || !ok)) return fail(PHS_ERR_INVALID_ARG, "null data pointer");
-  if (n_events == 0) return PHS_OK;
-  DeviceGuard g(h->device);
-  const int n_out = h->p.n_out, n_x = h->p.n_x, nch = h->p.n_channels;
-  const int64_t chunk = std::min<int64_t>(n_events, 1 << 19);
-  for (int s = 0; s < phs_process::kStreams; s++) {
-    if (!h->streams[s]) CUDA_TRY(cudaStreamCreateWithFlags(&h->streams[s], cudaStreamNonBlocking));
-    int rc;
-    if ((rc = h->bx[s].reserve(chunk * n_x * sizeof(double)))) return rc;
-    if ((rc = h->bp[s].reserve(chunk * 4 * n_out * sizeof(double)))) return rc;
-    if ((rc = h->bf[s].reserve(chunk * sizeof(double)))) return rc;
-    if ((rc = h->bv[s].reserve(chunk * sizeof(double)))) return rc;
-    if ((rc = h->bo[s].reserve(chunk))) return rc;
-  }
-  std::vector<int64_t> cnt(nch, 0), prefix(nch + 1, 0);
-  if (counts) std::copy(counts, counts + nch, cnt.begin()); else cnt[0] = n_events;
-  for (int c = 0; c < nch; c++) prefix[c + 1] = prefix[c] + cnt[c];
-  int k = 0;
-  for (int64_t e0 = 0; e0 < n_events; e0 += chunk, k++) {
-    const int s = k % phs_process::kStreams;
-    cudaStream_t st = h->streams[s];
-    const int64_t n = std::min(chunk, n_events - e0);
-    // this chunk's per-channel counts
-    std::vector<int64_t> cc(nch, 0);
-    for (int c = 0; c < nch; c++) {
-      int64_t lo = std::max(prefix[c], e0), hi = std::min(prefix[c + 1], e0 + n);
-      cc[c] = hi > lo ? hi - lo : 0;
+  return guarded([&]() -> int {
+    if (int rc = check_proc(h)) return rc;
+    if (!h->beams) return fail(PHS_ERR_STATE, "phs_process_set_beams has not been called");
+    if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
+    if (n_events > 0 && (!x || !p || !f || !v || !ok)) return fail(PHS_ERR_INVALID_ARG, "null data pointer");
+    if (n_events == 0) return PHS_OK;
+    DeviceGuard g(h->device);
+    const int n_out = h->p.n_out, n_x = h->p.n_x, nch = h->p.n_channels;
+    const int64_t chunk = std::min<int64_t>(n_events, 1 << 19);
+    for (int s = 0; s < phs_process::kStreams; s++) {
+      if (!h->streams[s]) CUDA_TRY(cudaStreamCreateWithFlags(&h->streams[s], cudaStreamNonBlocking));
+      int rc;
+      if ((rc = h->bx[s].reserve(chunk * n_x * sizeof(double)))) return rc;
+      if ((rc = h->bp[s].reserve(chunk * 4 * n_out * sizeof(double)))) return rc;
+      if ((rc = h->bf[s].reserve(chunk * sizeof(double)))) return rc;
+      if ((rc = h->bv[s].reserve(chunk * sizeof(double)))) return rc;
+      if ((rc = h->bo[s].reserve(chunk))) return rc;
     }
-    CUDA_TRY(cudaMemcpyAsync(h->bx[s].ptr, x + e0 * n_x, n * n_x * sizeof(double),
-                             cudaMemcpyHostToDevice, st));
-    int rc = launch_process(h, h->pseg[s], n, cc.data(), 0, h->bx[s].as<double>(),
-                            h->bp[s].as<double>(), h->bf[s].as<double>(), h->bv[s].as<double>(),
-                            h->bo[s].as<uint8_t>(), nullptr, nullptr, 1, false, st);
-    if (rc) return rc;
-    CUDA_TRY(cudaMemcpyAsync(p + e0 * 4 * n_out, h->bp[s].ptr, n * 4 * n_out * sizeof(double),
-                             cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaMemcpyAsync(f + e0, h->bf[s].ptr, n * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaMemcpyAsync(v + e0, h->bv[s].ptr, n * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaMemcpyAsync(ok + e0, h->bo[s].ptr, n, cudaMemcpyDeviceToHost, st));
-  }
-  for (int s = 0; s < phs_process::kStreams; s++) CUDA_TRY(cudaStreamSynchronize(h->streams[s]));
-  return PHS_OK;
+    std::vector<int64_t> cnt(nch, 0), prefix(nch + 1, 0);
+    if (counts) std::copy(counts, counts + nch, cnt.begin()); else cnt[0] = n_events;
+    for (int c = 0; c < nch; c++) prefix[c + 1] = prefix[c] + cnt[c];
+    int k = 0;
+    for (int64_t e0 = 0; e0 < n_events; e0 += chunk, k++) {
+      const int s = k % phs_process::kStreams;
+      cudaStream_t st = h->streams[s];
+      const int64_t n = std::min(chunk, n_events - e0);
+      // this chunk's per-channel counts
+      std::vector<int64_t> cc(nch, 0);
+      for (int c = 0; c < nch; c++) {
+        int64_t lo = std::max(prefix[c], e0), hi = std::min(prefix[c + 1], e0 + n);
+        cc[c] = hi > lo ? hi - lo : 0;
+      }
+      CUDA_TRY(cudaMemcpyAsync(h->bx[s].ptr, x + e0 * n_x, n * n_x * sizeof(double),
+                               cudaMemcpyHostToDevice, st));
+      int rc = launch_process(h, h->pseg[s], n, cc.data(), 0, h->bx[s].as<double>(),
+                              h->bp[s].as<double>(), h->bf[s].as<double>(), h->bv[s].as<double>(),
+                              h->bo[s].as<uint8_t>(), nullptr, nullptr, 1, false, st);
+      if (rc) return rc;
+      CUDA_TRY(cudaMemcpyAsync(p + e0 * 4 * n_out, h->bp[s].ptr, n * 4 * n_out * sizeof(double),
+                               cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaMemcpyAsync(f + e0, h->bf[s].ptr, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaMemcpyAsync(v + e0, h->bv[s].ptr, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaMemcpyAsync(ok + e0, h->bo[s].ptr, n, cudaMemcpyDeviceToHost, st));
+    }
+    for (int s = 0; s < phs_process::kStreams; s++) CUDA_TRY(cudaStreamSynchronize(h->streams[s]));
+    return PHS_OK;
+  });
 }
 
 // ---------------------------------------------------------------------------- batches
@@ -902,128 +945,144 @@ struct phs_batch {
 };
 
 extern "C" int phs_batch_create(phs_batch_t *out, int n_procs, const phs_process_t *procs) {
-  if (!out) return fail(PHS_ERR_INVALID_ARG, "null output handle pointer");
-  *out = nullptr;
-  if (n_procs < 1 || !procs) return fail(PHS_ERR_INVALID_ARG, "no processes");
-  phs_batch *b = new phs_batch;
-  cudaGetDevice(&b->device);
-  for (int i = 0; i < n_procs; i++) {
-    phs_process_t h = procs[i];
-    if (!h || !h->beams) {
-      delete b;
-      return fail(PHS_ERR_STATE, "process %d is null or has no beams set", i);
+  return guarded([&]() -> int {
+    if (!out) return fail(PHS_ERR_INVALID_ARG, "null output handle pointer");
+    *out = nullptr;
+    if (n_procs < 1 || !procs) return fail(PHS_ERR_INVALID_ARG, "no processes");
+    phs_batch *b = new phs_batch;
+    cudaGetDevice(&b->device);
+    for (int i = 0; i < n_procs; i++) {
+      phs_process_t h = procs[i];
+      if (!h || !h->beams) {
+        delete b;
+        return fail(PHS_ERR_STATE, "process %d is null or has no beams set", i);
+      }
+      b->prog.insert(b->prog.end(), h->prog.begin(), h->prog.end());
+      b->prog_ff.insert(b->prog_ff.end(), h->prog_ff.begin(), h->prog_ff.end());
+      b->lay.insert(b->lay.end(), h->lay.begin(), h->lay.end());
+      b->stack_depth = std::max(b->stack_depth, h->stack_depth);
     }
-    b->prog.insert(b->prog.end(), h->prog.begin(), h->prog.end());
-    b->prog_ff.insert(b->prog_ff.end(), h->prog_ff.begin(), h->prog_ff.end());
-    b->lay.insert(b->lay.end(), h->lay.begin(), h->lay.end());
-    b->stack_depth = std::max(b->stack_depth, h->stack_depth);
-  }
-  DeviceGuard g(b->device);
-  int rc = b->d_prog.reserve(b->prog.size() * sizeof(PhsChannel));
-  if (rc) { delete b; return rc; }
-  rc = b->d_prog_ff.reserve(b->prog_ff.size() * sizeof(PhsChannelFF));
-  if (rc) { b->d_prog.release(); delete b; return rc; }
-  cudaError_t e = cudaMemcpy(b->d_prog.ptr, b->prog.data(), b->prog.size() * sizeof(PhsChannel),
-                             cudaMemcpyHostToDevice);
-  if (e == cudaSuccess)
-    e = cudaMemcpy(b->d_prog_ff.ptr, b->prog_ff.data(), b->prog_ff.size() * sizeof(PhsChannelFF),
-                   cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) {
-    b->d_prog.release();
-    b->d_prog_ff.release();
-    delete b;
-    return fail(PHS_ERR_CUDA, "cudaMemcpy of batch programs failed: %s", cudaGetErrorString(e));
-  }
-  *out = b;
-  return PHS_OK;
+    DeviceGuard g(b->device);
+    int rc = b->d_prog.reserve(b->prog.size() * sizeof(PhsChannel));
+    if (rc) { delete b; return rc; }
+    rc = b->d_prog_ff.reserve(b->prog_ff.size() * sizeof(PhsChannelFF));
+    if (rc) { b->d_prog.release(); delete b; return rc; }
+    cudaError_t e = cudaMemcpy(b->d_prog.ptr, b->prog.data(), b->prog.size() * sizeof(PhsChannel),
+                               cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_prog_ff.ptr, b->prog_ff.data(), b->prog_ff.size() * sizeof(PhsChannelFF),
+                     cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      b->d_prog.release();
+      b->d_prog_ff.release();
+      delete b;
+      return fail(PHS_ERR_CUDA, "cudaMemcpy of batch programs failed: %s", cudaGetErrorString(e));
+    }
+    *out = b;
+    return PHS_OK;
+  });
 }
 
 extern "C" int phs_batch_destroy(phs_batch_t b) {
-  if (!b) return PHS_OK;
-  DeviceGuard g(b->device);
-  b->d_prog.release();
-  b->d_prog_ff.release();
-  b->segs.release();
-  delete b;
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (!b) return PHS_OK;
+    DeviceGuard g(b->device);
+    b->d_prog.release();
+    b->d_prog_ff.release();
+    b->segs.release();
+    delete b;
+    return PHS_OK;
+  });
 }
 
 extern "C" int phs_batch_info(phs_batch_t b, int *n_channels, int64_t *x_stride_sum, int *max_n_out) {
-  if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
-  if (n_channels) *n_channels = (int)b->prog.size();
-  int64_t xs = 0;
-  int mo = 0;
-  for (auto &l : b->lay) { xs += l.x_stride; mo = std::max(mo, l.n_out); }
-  if (x_stride_sum) *x_stride_sum = xs;
-  if (max_n_out) *max_n_out = mo;
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
+    if (n_channels) *n_channels = (int)b->prog.size();
+    int64_t xs = 0;
+    int mo = 0;
+    for (auto &l : b->lay) { xs += l.x_stride; mo = std::max(mo, l.n_out); }
+    if (x_stride_sum) *x_stride_sum = xs;
+    if (max_n_out) *max_n_out = mo;
+    return PHS_OK;
+  });
 }
 
 extern "C" int phs_batch_offsets(phs_batch_t b, const int64_t *counts, int64_t *xo, int64_t *po) {
-  if (!b || !counts || !xo || !po) return fail(PHS_ERR_INVALID_ARG, "null argument");
-  const int n = (int)b->prog.size();
-  xo[0] = po[0] = 0;
-  for (int c = 0; c < n; c++) {
-    xo[c + 1] = xo[c] + counts[c] * b->lay[c].x_stride;
-    po[c + 1] = po[c] + counts[c] * 4 * b->lay[c].n_out;
-  }
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (!b || !counts || !xo || !po) return fail(PHS_ERR_INVALID_ARG, "null argument");
+    const int n = (int)b->prog.size();
+    xo[0] = po[0] = 0;
+    for (int c = 0; c < n; c++) {
+      xo[c + 1] = xo[c] + counts[c] * b->lay[c].x_stride;
+      po[c + 1] = po[c] + counts[c] * 4 * b->lay[c].n_out;
+    }
+    return PHS_OK;
+  });
 }
 
 extern "C" int phs_batch_generate_device(phs_batch_t b, const int64_t *counts, const double *x,
                                          double *p, double *f, double *v, uint8_t *ok,
                                          void *stream) {
-  if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
-  if (!counts) return fail(PHS_ERR_INVALID_ARG, "null counts");
-  const int n = (int)b->prog.size();
-  int64_t n_events = 0;
-  for (int c = 0; c < n; c++) n_events += counts[c] > 0 ? counts[c] : 0;
-  if (int rc = check_counts(counts, n, n_events)) return rc;
-  if (int rc = check_ptrs(n_events, x, p, f, v, ok)) return rc;
-  DeviceGuard g(b->device);
-  int rc = build_segments(b->segs, counts, n, b->lay, 0, 0, 0, false);
-  if (rc) return rc;
-  PhsLaunch a;
-  memset(&a, 0, sizeof a);
-  a.channels = b->d_prog.as<PhsChannel>();
-  a.channels_ff = b->d_prog_ff.as<PhsChannelFF>();
-  a.stack_depth = b->stack_depth;
-  a.x = x;
-  a.p = p;
-  a.factor = f;
-  a.volume = v;
-  a.ok = ok;
-  a.factor_stride = 1;
-  if ((rc = attach_segments(b->segs, a, (cudaStream_t)stream))) return rc;
-  if (a.n_tiles == 0) return PHS_OK;
-  if (b->precision == PHS_PRECISION_F32X2)
-    return launch_ff_tuned(b->ff_variant, b->segs, a, b->device, b->stack_depth, n_events,
-                           (cudaStream_t)stream);
-  return launch_f64_tuned(b->f64_variant, b->segs, a, b->device, b->stack_depth, n_events,
-                          (cudaStream_t)stream);
+  return guarded([&]() -> int {
+    if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
+    if (!counts) return fail(PHS_ERR_INVALID_ARG, "null counts");
+    const int n = (int)b->prog.size();
+    int64_t n_events = 0;
+    for (int c = 0; c < n; c++) n_events += counts[c] > 0 ? counts[c] : 0;
+    if (int rc = check_counts(counts, n, n_events)) return rc;
+    if (int rc = check_ptrs(n_events, x, p, f, v, ok)) return rc;
+    DeviceGuard g(b->device);
+    int rc = build_segments(b->segs, counts, n, b->lay, 0, 0, 0, false);
+    if (rc) return rc;
+    PhsLaunch a;
+    memset(&a, 0, sizeof a);
+    a.channels = b->d_prog.as<PhsChannel>();
+    a.channels_ff = b->d_prog_ff.as<PhsChannelFF>();
+    a.stack_depth = b->stack_depth;
+    a.x = x;
+    a.p = p;
+    a.factor = f;
+    a.volume = v;
+    a.ok = ok;
+    a.factor_stride = 1;
+    if ((rc = attach_segments(b->segs, a, (cudaStream_t)stream))) return rc;
+    if (a.n_tiles == 0) return PHS_OK;
+    if (b->precision == PHS_PRECISION_F32X2)
+      return launch_ff_tuned(b->ff_variant, b->segs, a, b->device, b->stack_depth, n_events,
+                             (cudaStream_t)stream);
+    return launch_f64_tuned(b->f64_variant, b->segs, a, b->device, b->stack_depth, n_events,
+                            (cudaStream_t)stream);
+  });
 }
 
 extern "C" int phs_batch_set_variants(phs_batch_t b, int ff_variant, int f64_variant) {
-  if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
-  if (int rc = check_variants(ff_variant, f64_variant)) return rc;
-  b->ff_variant = ff_variant;
-  b->f64_variant = f64_variant;
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
+    if (int rc = check_variants(ff_variant, f64_variant)) return rc;
+    b->ff_variant = ff_variant;
+    b->f64_variant = f64_variant;
+    return PHS_OK;
+  });
 }
 
 extern "C" int phs_batch_tuning(phs_batch_t b, int *ff_variant, int *f64_variant) {
-  if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
-  if (ff_variant) *ff_variant = b->ff_variant;
-  if (f64_variant) *f64_variant = b->f64_variant;
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
+    if (ff_variant) *ff_variant = b->ff_variant;
+    if (f64_variant) *f64_variant = b->f64_variant;
+    return PHS_OK;
+  });
 }
 
 extern "C" int phs_batch_set_precision(phs_batch_t b, int precision) {
-  if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
-  if (precision != PHS_PRECISION_F64 && precision != PHS_PRECISION_F32X2)
-    return fail(PHS_ERR_INVALID_ARG, "unknown precision mode %d", precision);
-  b->precision = precision;
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
+    if (precision != PHS_PRECISION_F64 && precision != PHS_PRECISION_F32X2)
+      return fail(PHS_ERR_INVALID_ARG, "unknown precision mode %d", precision);
+    b->precision = precision;
+    return PHS_OK;
+  });
 }
 
 // ------------------------------------------------------- generation without allocation
@@ -1038,59 +1097,61 @@ extern "C" int phs_generate_device_noalloc(phs_process_t h, double E1, double E2
                                            int64_t n_events, const int64_t *counts,
                                            const double *x, double *p, double *f, double *v,
                                            uint8_t *ok, void *stream) {
-  if (int rc = check_proc(h)) return rc;
-  if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
-  if (int rc = check_ptrs(n_events, x, p, f, v, ok)) return rc;
-  if (!(E1 > 0) || !(E2 > 0) || !isfinite(E1) || !isfinite(E2))
-    return fail(PHS_ERR_INVALID_ARG, "beam energies must be positive and finite");
-  const phs::Process &P = h->p;
-  if (P.n_channels > PHS_NOALLOC_MAX_CHANNELS)
-    return fail(PHS_ERR_UNSUPPORTED, "phs_generate_device_noalloc takes at most %d channels "
-                "(its static device scratch holds %zu bytes); this process has %d",
-                PHS_NOALLOC_MAX_CHANNELS, phs_noalloc_scratch_bytes(), P.n_channels);
-  const double sqrts = 2 * sqrt(E1 * E2);
-  double m_tot = 0;
-  for (int k = 0; k < P.n_out; k++) m_tot += P.flv_m[P.n_in + k];
-  if (!(sqrts > m_tot))
-    return fail(PHS_ERR_INVALID_ARG, "sqrt(s) = %g is below the final-state mass sum %g", sqrts,
-                m_tot);
-  DeviceGuard g(h->device);
-  std::vector<PhsChannel> prog(P.n_channels);
-  int depth = 0;
-  std::string err;
-  const double bg = (E1 - E2) / (2 * sqrt(E1 * E2));
-  for (int c = 0; c < P.n_channels; c++) {
-    phs::ChannelInfo info;
-    int rc = phs::compile_channel(P, c, sqrts, prog[c], info, err);
-    if (rc) return fail(rc, "%s", err.c_str());
-    prog[c].sqrts = sqrts;
-    prog[c].lab = E1 != E2;
-    prog[c].lab_bg = bg;
-    prog[c].lab_gamma = sqrt(1 + bg * bg);
-    depth = std::max(depth, info.stack_depth);
-  }
-  std::vector<ChanLayout> lay(P.n_channels, ChanLayout{P.n_out, P.n_x});
-  int64_t one = n_events;
-  Segments S;
-  int rc = build_segments(S, counts ? counts : &one, P.n_channels, lay, 0, 0, 0, false);
-  if (rc) return rc;
-  PhsLaunch a;
-  memset(&a, 0, sizeof a);
-  a.stack_depth = depth;
-  a.n_tiles = S.n_tiles;
-  a.x = x;
-  a.p = p;
-  a.factor = f;
-  a.volume = v;
-  a.ok = ok;
-  a.factor_stride = 1;
-  if (S.host.size() <= PHS_INLINE_SEGS) std::copy(S.host.begin(), S.host.end(), a.seg_inline);
-  const int grid = a.n_tiles > 0 ? grid_for(a.n_tiles, h->device, depth, false, 0) : 1;
-  cudaError_t e = phs_launch_forward_f64_noalloc(a, prog.data(), P.n_channels, S.host.data(),
-                                                 (int)S.host.size(), grid, (cudaStream_t)stream);
-  if (e != cudaSuccess)
-    return fail(PHS_ERR_CUDA, "phs_generate_device_noalloc: %s", cudaGetErrorString(e));
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (int rc = check_proc(h)) return rc;
+    if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
+    if (int rc = check_ptrs(n_events, x, p, f, v, ok)) return rc;
+    if (!(E1 > 0) || !(E2 > 0) || !isfinite(E1) || !isfinite(E2))
+      return fail(PHS_ERR_INVALID_ARG, "beam energies must be positive and finite");
+    const phs::Process &P = h->p;
+    if (P.n_channels > PHS_NOALLOC_MAX_CHANNELS)
+      return fail(PHS_ERR_UNSUPPORTED, "phs_generate_device_noalloc takes at most %d channels "
+                  "(its static device scratch holds %zu bytes); this process has %d",
+                  PHS_NOALLOC_MAX_CHANNELS, phs_noalloc_scratch_bytes(), P.n_channels);
+    const double sqrts = 2 * sqrt(E1 * E2);
+    double m_tot = 0;
+    for (int k = 0; k < P.n_out; k++) m_tot += P.flv_m[P.n_in + k];
+    if (!(sqrts > m_tot))
+      return fail(PHS_ERR_INVALID_ARG, "sqrt(s) = %g is below the final-state mass sum %g", sqrts,
+                  m_tot);
+    DeviceGuard g(h->device);
+    std::vector<PhsChannel> prog(P.n_channels);
+    int depth = 0;
+    std::string err;
+    const double bg = (E1 - E2) / (2 * sqrt(E1 * E2));
+    for (int c = 0; c < P.n_channels; c++) {
+      phs::ChannelInfo info;
+      int rc = phs::compile_channel(P, c, sqrts, prog[c], info, err);
+      if (rc) return fail(rc, "%s", err.c_str());
+      prog[c].sqrts = sqrts;
+      prog[c].lab = E1 != E2;
+      prog[c].lab_bg = bg;
+      prog[c].lab_gamma = sqrt(1 + bg * bg);
+      depth = std::max(depth, info.stack_depth);
+    }
+    std::vector<ChanLayout> lay(P.n_channels, ChanLayout{P.n_out, P.n_x});
+    int64_t one = n_events;
+    Segments S;
+    int rc = build_segments(S, counts ? counts : &one, P.n_channels, lay, 0, 0, 0, false);
+    if (rc) return rc;
+    PhsLaunch a;
+    memset(&a, 0, sizeof a);
+    a.stack_depth = depth;
+    a.n_tiles = S.n_tiles;
+    a.x = x;
+    a.p = p;
+    a.factor = f;
+    a.volume = v;
+    a.ok = ok;
+    a.factor_stride = 1;
+    if (S.host.size() <= PHS_INLINE_SEGS) std::copy(S.host.begin(), S.host.end(), a.seg_inline);
+    const int grid = a.n_tiles > 0 ? grid_for(a.n_tiles, h->device, depth, false, 0) : 1;
+    cudaError_t e = phs_launch_forward_f64_noalloc(a, prog.data(), P.n_channels, S.host.data(),
+                                                   (int)S.host.size(), grid, (cudaStream_t)stream);
+    if (e != cudaSuccess)
+      return fail(PHS_ERR_CUDA, "phs_generate_device_noalloc: %s", cudaGetErrorString(e));
+    return PHS_OK;
+  });
 }
 
 // ----------------------------------------------------------------------- CUDA graphs
@@ -1147,72 +1208,84 @@ static int capture_graph(phs_graph_t *out, int device, Call call) {
 extern "C" int phs_batch_graph_create(phs_graph_t *out, phs_batch_t b, const int64_t *counts,
                                       const double *x, double *p, double *f, double *v,
                                       uint8_t *ok) {
-  if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
-  return capture_graph(out, b->device, [&](cudaStream_t st) {
-    return phs_batch_generate_device(b, counts, x, p, f, v, ok, st);
+  return guarded([&]() -> int {
+    if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
+    return capture_graph(out, b->device, [&](cudaStream_t st) {
+      return phs_batch_generate_device(b, counts, x, p, f, v, ok, st);
+    });
   });
 }
 
 extern "C" int phs_process_graph_create(phs_graph_t *out, phs_process_t h, int64_t n_events,
                                         const int64_t *counts, const double *x, double *p,
                                         double *f, double *v, uint8_t *ok) {
-  if (int rc = check_proc(h)) return rc;
-  return capture_graph(out, h->device, [&](cudaStream_t st) {
-    return phs_generate_device(h, n_events, counts, x, p, f, v, ok, st);
+  return guarded([&]() -> int {
+    if (int rc = check_proc(h)) return rc;
+    return capture_graph(out, h->device, [&](cudaStream_t st) {
+      return phs_generate_device(h, n_events, counts, x, p, f, v, ok, st);
+    });
   });
 }
 
 extern "C" int phs_graph_launch(phs_graph_t G, void *stream) {
-  if (!G) return fail(PHS_ERR_INVALID_ARG, "null graph handle");
-  DeviceGuard g(G->device);
-  CUDA_TRY(cudaGraphLaunch(G->exec, (cudaStream_t)stream));
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (!G) return fail(PHS_ERR_INVALID_ARG, "null graph handle");
+    DeviceGuard g(G->device);
+    CUDA_TRY(cudaGraphLaunch(G->exec, (cudaStream_t)stream));
+    return PHS_OK;
+  });
 }
 
 extern "C" int phs_graph_destroy(phs_graph_t G) {
-  if (!G) return PHS_OK;
-  DeviceGuard g(G->device);
-  if (G->exec) cudaGraphExecDestroy(G->exec);
-  if (G->graph) cudaGraphDestroy(G->graph);
-  delete G;
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (!G) return PHS_OK;
+    DeviceGuard g(G->device);
+    if (G->exec) cudaGraphExecDestroy(G->exec);
+    if (G->graph) cudaGraphDestroy(G->graph);
+    delete G;
+    return PHS_OK;
+  });
 }
 
 // ---------------------------------------------------------------------- random numbers
 extern "C" int phs_philox_fill(double *x, int64_t n_events, int n_x, uint64_t seed,
                                int64_t first_event, void *stream) {
-  if (n_events < 0 || n_x < 1 || first_event < 0) return fail(PHS_ERR_INVALID_ARG, "bad sizes");
-  if (n_events > 0 && !x) return fail(PHS_ERR_INVALID_ARG, "null x");
-  CUDA_TRY(phs_launch_philox(x, n_events, n_x, seed, first_event, (cudaStream_t)stream));
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (n_events < 0 || n_x < 1 || first_event < 0) return fail(PHS_ERR_INVALID_ARG, "bad sizes");
+    if (n_events > 0 && !x) return fail(PHS_ERR_INVALID_ARG, "null x");
+    CUDA_TRY(phs_launch_philox(x, n_events, n_x, seed, first_event, (cudaStream_t)stream));
+    return PHS_OK;
+  });
 }
 
 // --------------------------------------------------------------- peak measurement
 extern "C" int phs_measure_fma_peak(int fp64, double *gflops) {
-  if (!gflops) return fail(PHS_ERR_INVALID_ARG, "null output");
-  int dev = 0;
-  CUDA_TRY(cudaGetDevice(&dev));
-  const int blocks = sm_count(dev) * 8, threads = 256, iters = fp64 ? 4096 : 65536;
-  DevBuf out;
-  if (int rc = out.reserve((size_t)blocks * threads * 8)) return rc;
-  cudaEvent_t e0, e1;
-  CUDA_TRY(cudaEventCreate(&e0));
-  CUDA_TRY(cudaEventCreate(&e1));
-  float best = 1e30f;
-  for (int rep = 0; rep < 4; rep++) {
-    CUDA_TRY(cudaEventRecord(e0, nullptr));
-    CUDA_TRY(phs_launch_fma_rate(out.ptr, fp64, blocks, threads, iters, nullptr));
-    CUDA_TRY(cudaEventRecord(e1, nullptr));
-    CUDA_TRY(cudaEventSynchronize(e1));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (rep > 0) best = std::min(best, ms);
-  }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  out.release();
-  *gflops = 16.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e9;
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (!gflops) return fail(PHS_ERR_INVALID_ARG, "null output");
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    const int blocks = sm_count(dev) * 8, threads = 256, iters = fp64 ? 4096 : 65536;
+    DevBuf out;
+    if (int rc = out.reserve((size_t)blocks * threads * 8)) return rc;
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; rep++) {
+      CUDA_TRY(cudaEventRecord(e0, nullptr));
+      CUDA_TRY(phs_launch_fma_rate(out.ptr, fp64, blocks, threads, iters, nullptr));
+      CUDA_TRY(cudaEventRecord(e1, nullptr));
+      CUDA_TRY(cudaEventSynchronize(e1));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) best = std::min(best, ms);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    out.release();
+    *gflops = 16.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e9;
+    return PHS_OK;
+  });
 }
 
 // -------------------------------------------------------------------- Whizard binding
@@ -1316,153 +1389,173 @@ void whizard_release_device() {
 
 extern "C" void c_whizard_set_particle_structure(int *n_channels, int *n_trees, int *n_groves,
                                                  int *n_x, int *n_in, int *n_out) {
-  std::lock_guard<std::mutex> lk(W.mu);
-  if (!n_channels || !n_trees || !n_groves || !n_x || !n_in || !n_out) {
-    whizard_log(fail(PHS_ERR_INVALID_ARG, "c_whizard_set_particle_structure: null argument"));
-    return;
-  }
-  if (*n_out < 2 || *n_out > PHS_MAX_OUT || *n_in < 1 || *n_in > 2 || *n_channels < 1) {
-    whizard_log(fail(PHS_ERR_UNSUPPORTED, "c_whizard_set_particle_structure: n_in=%d n_out=%d "
-                     "n_channels=%d not supported", *n_in, *n_out, *n_channels));
-    return;
-  }
-  W.n_channels = *n_channels;
-  W.n_trees = *n_trees;
-  W.n_groves = *n_groves;
-  W.n_x = *n_x;
-  W.n_in = *n_in;
-  W.n_out = *n_out;
-  W.n_prt = (1 << (W.n_in + W.n_out)) - 1;
-  W.n_prt_out = (1 << W.n_out) - 1;
-  W.flv_m.assign(W.n_in + W.n_out, 0.0);
-  W.flv_w.assign(W.n_in + W.n_out, 0.0);
-  W.structure = true;
-  W.flavors = W.mappings = W.trees = false;
+  guarded_void([&]() {
+    std::lock_guard<std::mutex> lk(W.mu);
+    if (!n_channels || !n_trees || !n_groves || !n_x || !n_in || !n_out) {
+      whizard_log(fail(PHS_ERR_INVALID_ARG, "c_whizard_set_particle_structure: null argument"));
+      return;
+    }
+    if (*n_out < 2 || *n_out > PHS_MAX_OUT || *n_in < 1 || *n_in > 2 || *n_channels < 1) {
+      whizard_log(fail(PHS_ERR_UNSUPPORTED, "c_whizard_set_particle_structure: n_in=%d n_out=%d "
+                       "n_channels=%d not supported", *n_in, *n_out, *n_channels));
+      return;
+    }
+    W.n_channels = *n_channels;
+    W.n_trees = *n_trees;
+    W.n_groves = *n_groves;
+    W.n_x = *n_x;
+    W.n_in = *n_in;
+    W.n_out = *n_out;
+    W.n_prt = (1 << (W.n_in + W.n_out)) - 1;
+    W.n_prt_out = (1 << W.n_out) - 1;
+    W.flv_m.assign(W.n_in + W.n_out, 0.0);
+    W.flv_w.assign(W.n_in + W.n_out, 0.0);
+    W.structure = true;
+    W.flavors = W.mappings = W.trees = false;
+  });
 }
 
 extern "C" void c_whizard_set_flavors(double *masses, double *widths) {
-  std::lock_guard<std::mutex> lk(W.mu);
-  if (!W.structure || !masses || !widths) {
-    whizard_log(fail(PHS_ERR_STATE, "c_whizard_set_flavors: no particle structure or null input"));
-    return;
-  }
-  std::copy(masses, masses + W.n_in + W.n_out, W.flv_m.begin());
-  std::copy(widths, widths + W.n_in + W.n_out, W.flv_w.begin());
-  W.flavors = true;
+  guarded_void([&]() {
+    std::lock_guard<std::mutex> lk(W.mu);
+    if (!W.structure || !masses || !widths) {
+      whizard_log(fail(PHS_ERR_STATE, "c_whizard_set_flavors: no particle structure or null input"));
+      return;
+    }
+    std::copy(masses, masses + W.n_in + W.n_out, W.flv_m.begin());
+    std::copy(widths, widths + W.n_in + W.n_out, W.flv_w.begin());
+    W.flavors = true;
+  });
 }
 
 extern "C" void c_whizard_init_mappings(void) {
-  std::lock_guard<std::mutex> lk(W.mu);
-  if (!W.structure) { whizard_log(fail(PHS_ERR_STATE, "c_whizard_init_mappings: no particle structure")); return; }
-  const size_t n = (size_t)W.n_channels * W.n_prt_out;
-  W.map_id.assign(n, 0);
-  W.map_m.assign(n, 0.0);
-  W.map_w.assign(n, 0.0);
-  W.mappings = true;
+  guarded_void([&]() {
+    std::lock_guard<std::mutex> lk(W.mu);
+    if (!W.structure) { whizard_log(fail(PHS_ERR_STATE, "c_whizard_init_mappings: no particle structure")); return; }
+    const size_t n = (size_t)W.n_channels * W.n_prt_out;
+    W.map_id.assign(n, 0);
+    W.map_m.assign(n, 0.0);
+    W.map_w.assign(n, 0.0);
+    W.mappings = true;
+  });
 }
 
 extern "C" void c_whizard_fill_mapping(int *channel, int *map_ids, double *masses, double *widths) {
-  std::lock_guard<std::mutex> lk(W.mu);
-  if (!W.mappings || !channel || !map_ids || !masses || !widths || *channel < 1 ||
-      *channel > W.n_channels) {
-    whizard_log(fail(PHS_ERR_INVALID_ARG, "c_whizard_fill_mapping: bad channel or state"));
-    return;
-  }
-  const size_t o = (size_t)(*channel - 1) * W.n_prt_out;
-  std::copy(map_ids, map_ids + W.n_prt_out, W.map_id.begin() + o);
-  std::copy(masses, masses + W.n_prt_out, W.map_m.begin() + o);
-  std::copy(widths, widths + W.n_prt_out, W.map_w.begin() + o);
+  guarded_void([&]() {
+    std::lock_guard<std::mutex> lk(W.mu);
+    if (!W.mappings || !channel || !map_ids || !masses || !widths || *channel < 1 ||
+        *channel > W.n_channels) {
+      whizard_log(fail(PHS_ERR_INVALID_ARG, "c_whizard_fill_mapping: bad channel or state"));
+      return;
+    }
+    const size_t o = (size_t)(*channel - 1) * W.n_prt_out;
+    std::copy(map_ids, map_ids + W.n_prt_out, W.map_id.begin() + o);
+    std::copy(masses, masses + W.n_prt_out, W.map_m.begin() + o);
+    std::copy(widths, widths + W.n_prt_out, W.map_w.begin() + o);
+  });
 }
 
 extern "C" void c_whizard_init_tree_structures(void) {
-  std::lock_guard<std::mutex> lk(W.mu);
-  if (!W.structure) { whizard_log(fail(PHS_ERR_STATE, "c_whizard_init_tree_structures: no particle structure")); return; }
-  const size_t n = (size_t)W.n_channels * W.n_prt;
-  W.d1.assign(n, 0);
-  W.d2.assign(n, 0);
-  W.hc.assign(n, 0);
-  W.fr.assign(n, 0);
-  W.trees = true;
+  guarded_void([&]() {
+    std::lock_guard<std::mutex> lk(W.mu);
+    if (!W.structure) { whizard_log(fail(PHS_ERR_STATE, "c_whizard_init_tree_structures: no particle structure")); return; }
+    const size_t n = (size_t)W.n_channels * W.n_prt;
+    W.d1.assign(n, 0);
+    W.d2.assign(n, 0);
+    W.hc.assign(n, 0);
+    W.fr.assign(n, 0);
+    W.trees = true;
+  });
 }
 
 extern "C" void c_whizard_fill_tree_structure(int *channel, int *d1, int *d2, int *hc, int *friends) {
-  std::lock_guard<std::mutex> lk(W.mu);
-  if (!W.trees || !channel || !d1 || !d2 || !hc || !friends || *channel < 1 ||
-      *channel > W.n_channels) {
-    whizard_log(fail(PHS_ERR_INVALID_ARG, "c_whizard_fill_tree_structure: bad channel or state"));
-    return;
-  }
-  const size_t o = (size_t)(*channel - 1) * W.n_prt;
-  std::copy(d1, d1 + W.n_prt, W.d1.begin() + o);
-  std::copy(d2, d2 + W.n_prt, W.d2.begin() + o);
-  std::copy(hc, hc + W.n_prt, W.hc.begin() + o);
-  std::copy(friends, friends + W.n_prt, W.fr.begin() + o);
+  guarded_void([&]() {
+    std::lock_guard<std::mutex> lk(W.mu);
+    if (!W.trees || !channel || !d1 || !d2 || !hc || !friends || *channel < 1 ||
+        *channel > W.n_channels) {
+      whizard_log(fail(PHS_ERR_INVALID_ARG, "c_whizard_fill_tree_structure: bad channel or state"));
+      return;
+    }
+    const size_t o = (size_t)(*channel - 1) * W.n_prt;
+    std::copy(d1, d1 + W.n_prt, W.d1.begin() + o);
+    std::copy(d2, d2 + W.n_prt, W.d2.begin() + o);
+    std::copy(hc, hc + W.n_prt, W.hc.begin() + o);
+    std::copy(friends, friends + W.n_prt, W.fr.begin() + o);
+  });
 }
 
 // channel_limits[c] is the cumulative number of events up to and including channel c; events
 // are grouped by channel (whizard_gpu_phs.cpp:89-98).  Empty channels anywhere are allowed.
 extern "C" void c_whizard_init_channel_ids(int *batch_size, int *n_channels, int *channel_limits) {
-  std::lock_guard<std::mutex> lk(W.mu);
-  if (!batch_size || !n_channels || !channel_limits || *n_channels < 1 || *batch_size < 0) {
-    whizard_log(fail(PHS_ERR_INVALID_ARG, "c_whizard_init_channel_ids: bad arguments"));
-    return;
-  }
-  W.counts.assign(*n_channels, 0);
-  int64_t prev = 0;
-  for (int c = 0; c < *n_channels; c++) {
-    int64_t lim = std::min<int64_t>(channel_limits[c], *batch_size);
-    W.counts[c] = std::max<int64_t>(0, lim - prev);
-    prev = std::max(prev, lim);
-  }
-  W.batch_size = *batch_size;
+  guarded_void([&]() {
+    std::lock_guard<std::mutex> lk(W.mu);
+    if (!batch_size || !n_channels || !channel_limits || *n_channels < 1 || *batch_size < 0) {
+      whizard_log(fail(PHS_ERR_INVALID_ARG, "c_whizard_init_channel_ids: bad arguments"));
+      return;
+    }
+    W.counts.assign(*n_channels, 0);
+    int64_t prev = 0;
+    for (int c = 0; c < *n_channels; c++) {
+      int64_t lim = std::min<int64_t>(channel_limits[c], *batch_size);
+      W.counts[c] = std::max<int64_t>(0, lim - prev);
+      prev = std::max(prev, lim);
+    }
+    W.batch_size = *batch_size;
+  });
 }
 
 extern "C" void c_whizard_set_threads(int *msq_threads, int *cb_threads, int *ab_threads) {
-  std::lock_guard<std::mutex> lk(W.mu);
-  W.msq_threads = msq_threads ? *msq_threads : 0;
-  W.cb_threads = cb_threads ? *cb_threads : 0;
-  W.ab_threads = ab_threads ? *ab_threads : 0;
+  guarded_void([&]() {
+    std::lock_guard<std::mutex> lk(W.mu);
+    W.msq_threads = msq_threads ? *msq_threads : 0;
+    W.cb_threads = cb_threads ? *cb_threads : 0;
+    W.ab_threads = ab_threads ? *ab_threads : 0;
+  });
 }
 
 extern "C" void c_whizard_init_gpu_phs(void) {
-  std::lock_guard<std::mutex> lk(W.mu);
-  if (!W.structure || !W.flavors || !W.mappings || !W.trees) {
-    whizard_log(fail(PHS_ERR_STATE, "c_whizard_init_gpu_phs: structure, flavors, mappings and "
-                     "trees must be set first"));
-    return;
-  }
-  if (W.proc) { phs_process_destroy(W.proc); W.proc = nullptr; }
-  // codes of internal branches over all channels, for the sparse momentum handoff
-  W.internal.assign((1 << PHS_SPARSE_MAX_OUT) / 32, 0u);
-  for (int c = 0; c < W.n_channels && W.n_out <= PHS_SPARSE_MAX_OUT; c++)
-    for (int code = 1; code < (1 << W.n_out); code++)
-      if (W.hc[(size_t)c * W.n_prt + code - 1]) W.internal[code >> 5] |= 1u << (code & 31);
-  whizard_log(phs_process_create(&W.proc, W.n_in, W.n_out, W.n_channels, W.n_x, W.d1.data(),
-                                 W.d2.data(), W.hc.data(), W.fr.data(), W.map_id.data(),
-                                 W.map_m.data(), W.map_w.data(), W.flv_m.data(), W.flv_w.data()));
+  guarded_void([&]() {
+    std::lock_guard<std::mutex> lk(W.mu);
+    if (!W.structure || !W.flavors || !W.mappings || !W.trees) {
+      whizard_log(fail(PHS_ERR_STATE, "c_whizard_init_gpu_phs: structure, flavors, mappings and "
+                       "trees must be set first"));
+      return;
+    }
+    if (W.proc) { phs_process_destroy(W.proc); W.proc = nullptr; }
+    // codes of internal branches over all channels, for the sparse momentum handoff
+    W.internal.assign((1 << PHS_SPARSE_MAX_OUT) / 32, 0u);
+    for (int c = 0; c < W.n_channels && W.n_out <= PHS_SPARSE_MAX_OUT; c++)
+      for (int code = 1; code < (1 << W.n_out); code++)
+        if (W.hc[(size_t)c * W.n_prt + code - 1]) W.internal[code >> 5] |= 1u << (code & 31);
+    whizard_log(phs_process_create(&W.proc, W.n_in, W.n_out, W.n_channels, W.n_x, W.d1.data(),
+                                   W.d2.data(), W.hc.data(), W.fr.data(), W.map_id.data(),
+                                   W.map_m.data(), W.map_w.data(), W.flv_m.data(), W.flv_w.data()));
+  });
 }
 
 extern "C" void c_whizard_finalize_gpu_phs(void) {
-  std::lock_guard<std::mutex> lk(W.mu);
-  if (W.proc) phs_process_destroy(W.proc);
-  W.proc = nullptr;
-  whizard_release_device();
-  for (cudaStream_t &st : W.streams) {
-    if (st) cudaStreamDestroy(st);
-    st = nullptr;
-  }
-  for (cudaEvent_t *evs : {W.done, W.x_in, W.fwd}) {
-    const int m = evs == W.done ? kWhizardLaunches + 1 : kWhizardChunks;
-    for (int i = 0; i < m; i++) {
-      if (evs[i]) cudaEventDestroy(evs[i]);
-      evs[i] = nullptr;
+  guarded_void([&]() {
+    std::lock_guard<std::mutex> lk(W.mu);
+    if (W.proc) phs_process_destroy(W.proc);
+    W.proc = nullptr;
+    whizard_release_device();
+    for (cudaStream_t &st : W.streams) {
+      if (st) cudaStreamDestroy(st);
+      st = nullptr;
     }
-  }
-  W.map_id.clear(); W.map_m.clear(); W.map_w.clear();
-  W.d1.clear(); W.d2.clear(); W.hc.clear(); W.fr.clear();
-  W.flv_m.clear(); W.flv_w.clear();
-  W.counts.clear();
-  W.structure = W.flavors = W.mappings = W.trees = false;
+    for (cudaEvent_t *evs : {W.done, W.x_in, W.fwd}) {
+      const int m = evs == W.done ? kWhizardLaunches + 1 : kWhizardChunks;
+      for (int i = 0; i < m; i++) {
+        if (evs[i]) cudaEventDestroy(evs[i]);
+        evs[i] = nullptr;
+      }
+    }
+    W.map_id.clear(); W.map_m.clear(); W.map_w.clear();
+    W.d1.clear(); W.d2.clear(); W.hc.clear(); W.fr.clear();
+    W.flv_m.clear(); W.flv_w.clear();
+    W.counts.clear();
+    W.structure = W.flavors = W.mappings = W.trees = false;
+  });
 }
 
 extern "C" void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in,
@@ -1803,73 +1896,77 @@ bool *get_ok_device_pointer() {
 }
 
 extern "C" void c_whizard_reset_generator(void) {
-  std::lock_guard<std::mutex> lk(W.mu);
-  // phs.cu:1303-1308: drops the flavors and the retained device buffers
-  std::fill(W.flv_m.begin(), W.flv_m.end(), 0.0);
-  std::fill(W.flv_w.begin(), W.flv_w.end(), 0.0);
-  W.flavors = false;
-  whizard_release_device();
+  guarded_void([&]() {
+    std::lock_guard<std::mutex> lk(W.mu);
+    // phs.cu:1303-1308: drops the flavors and the retained device buffers
+    std::fill(W.flv_m.begin(), W.flv_m.end(), 0.0);
+    std::fill(W.flv_w.begin(), W.flv_w.end(), 0.0);
+    W.flavors = false;
+    whizard_release_device();
+  });
 }
 
 extern "C" void c_whizard_show_module(void) {
-  std::lock_guard<std::mutex> lk(W.mu);
-  printf("n_channels: %d\n", W.n_channels);
-  printf("n_ext_in: %d\n", W.n_in);
-  printf("n_ext_out: %d\n", W.n_out);
-  printf("n_ext_tot: %d\n", W.n_in + W.n_out);
-  printf("n_prt: %d\n", W.n_prt);
-  printf("n_prt_out: %d\n", W.n_prt_out);
-  printf("n_x: %d\n", W.n_x);
-  printf("root_branch: %d\n", W.n_prt_out - 1);
-  printf("n_branches: %d\n", 2 * W.n_out - 1);
-  printf("\nMappings: \n");
-  if (!W.mappings) {
-    printf(" MAPPINGS NOT SET UP!\n");
-    return;
-  }
-  for (int c = 0; c < W.n_channels; c++) {
-    printf(" c: %d\n ids: ", c);
-    for (int i = 0; i < W.n_prt_out; i++) printf("%d ", W.map_id[(size_t)c * W.n_prt_out + i]);
-    printf("\n masses: ");
-    for (int i = 0; i < W.n_prt_out; i++) printf("%lf ", W.map_m[(size_t)c * W.n_prt_out + i]);
-    printf("\n widths: ");
-    for (int i = 0; i < W.n_prt_out; i++) printf("%lf ", W.map_w[(size_t)c * W.n_prt_out + i]);
-    printf("\n");
-  }
-  if (W.trees) {
-    printf("Children: \n");
-    for (int c = 0; c < W.n_channels; c++) {
-      for (auto *t : {&W.d1, &W.d2, &W.hc}) {
-        for (int i = 0; i < W.n_prt; i++) printf("%d ", (*t)[(size_t)c * W.n_prt + i]);
-        printf("\n");
-      }
+  guarded_void([&]() {
+    std::lock_guard<std::mutex> lk(W.mu);
+    printf("n_channels: %d\n", W.n_channels);
+    printf("n_ext_in: %d\n", W.n_in);
+    printf("n_ext_out: %d\n", W.n_out);
+    printf("n_ext_tot: %d\n", W.n_in + W.n_out);
+    printf("n_prt: %d\n", W.n_prt);
+    printf("n_prt_out: %d\n", W.n_prt_out);
+    printf("n_x: %d\n", W.n_x);
+    printf("root_branch: %d\n", W.n_prt_out - 1);
+    printf("n_branches: %d\n", 2 * W.n_out - 1);
+    printf("\nMappings: \n");
+    if (!W.mappings) {
+      printf(" MAPPINGS NOT SET UP!\n");
+      return;
     }
-    printf("Friends: \n");
     for (int c = 0; c < W.n_channels; c++) {
-      printf("channel %d: ", c);
-      for (int i = 0; i < W.n_prt; i++) printf("%d ", W.fr[(size_t)c * W.n_prt + i]);
+      printf(" c: %d\n ids: ", c);
+      for (int i = 0; i < W.n_prt_out; i++) printf("%d ", W.map_id[(size_t)c * W.n_prt_out + i]);
+      printf("\n masses: ");
+      for (int i = 0; i < W.n_prt_out; i++) printf("%lf ", W.map_m[(size_t)c * W.n_prt_out + i]);
+      printf("\n widths: ");
+      for (int i = 0; i < W.n_prt_out; i++) printf("%lf ", W.map_w[(size_t)c * W.n_prt_out + i]);
       printf("\n");
     }
-  }
-  if (W.proc && W.proc->beams) {
-    printf("Visit programs (sqrt(s) = %g): \n", W.proc->prog[0].sqrts);
-    for (int c = 0; c < W.n_channels; c++) {
-      const PhsChannel &ch = W.proc->prog[c];
-      printf("  channel %d: %d visits, volume %.17g\n", c, ch.n_visits, ch.volume);
-      for (int v = 0; v < ch.n_visits; v++) {
-        const PhsVisit &V = ch.visit[v];
-        printf("    visit %d: x_phi %d x_ct %d ct_class %d carry %d push %d children", v, V.x_phi,
-               V.x_ct, V.ct_class, V.carry, V.push);
-        for (int j = 0; j < 2; j++) {
-          const PhsChild &C = V.child[j];
-          if (C.internal) printf(" [map %d x %d]", C.map_id, C.x_msq);
-          else printf(" [leaf %d]", C.out_index);
+    if (W.trees) {
+      printf("Children: \n");
+      for (int c = 0; c < W.n_channels; c++) {
+        for (auto *t : {&W.d1, &W.d2, &W.hc}) {
+          for (int i = 0; i < W.n_prt; i++) printf("%d ", (*t)[(size_t)c * W.n_prt + i]);
+          printf("\n");
         }
+      }
+      printf("Friends: \n");
+      for (int c = 0; c < W.n_channels; c++) {
+        printf("channel %d: ", c);
+        for (int i = 0; i < W.n_prt; i++) printf("%d ", W.fr[(size_t)c * W.n_prt + i]);
         printf("\n");
       }
     }
-  }
-  printf("END OF MODULE\n");
+    if (W.proc && W.proc->beams) {
+      printf("Visit programs (sqrt(s) = %g): \n", W.proc->prog[0].sqrts);
+      for (int c = 0; c < W.n_channels; c++) {
+        const PhsChannel &ch = W.proc->prog[c];
+        printf("  channel %d: %d visits, volume %.17g\n", c, ch.n_visits, ch.volume);
+        for (int v = 0; v < ch.n_visits; v++) {
+          const PhsVisit &V = ch.visit[v];
+          printf("    visit %d: x_phi %d x_ct %d ct_class %d carry %d push %d children", v, V.x_phi,
+                 V.x_ct, V.ct_class, V.carry, V.push);
+          for (int j = 0; j < 2; j++) {
+            const PhsChild &C = V.child[j];
+            if (C.internal) printf(" [map %d x %d]", C.map_id, C.x_msq);
+            else printf(" [leaf %d]", C.out_index);
+          }
+          printf("\n");
+        }
+      }
+    }
+    printf("END OF MODULE\n");
+  });
 }
 
 // -------------------------------------------------------------------------- x grids
@@ -1881,37 +1978,41 @@ struct phs_grid {
 };
 
 extern "C" int phs_grid_create(phs_grid_t *out, int n_channels, int n_x) {
-  if (!out) return fail(PHS_ERR_INVALID_ARG, "null output handle pointer");
-  *out = nullptr;
-  if (n_channels < 1 || n_x < 1) return fail(PHS_ERR_INVALID_ARG, "n_channels and n_x must be >= 1");
-  phs_grid *g = new phs_grid;
-  cudaGetDevice(&g->device);
-  g->n_channels = n_channels;
-  g->n_x = n_x;
-  const size_t nb = (size_t)n_channels * n_x * PHS_GRID_BINS;
-  int rc = g->weights.reserve(nb * sizeof(double));
-  if (!rc) rc = g->bins.reserve(nb * sizeof(unsigned long long));
-  if (!rc) rc = g->n_ok.reserve(n_channels * sizeof(unsigned long long));
-  if (rc) { delete g; return rc; }
-  std::vector<double> w(nb, 1.0 / PHS_GRID_BINS);   // rng.cpp:19-29: uniform start
-  cudaError_t e = cudaMemcpy(g->weights.ptr, w.data(), nb * sizeof(double), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) {
-    delete g;
-    return fail(PHS_ERR_CUDA, "grid upload: %s", cudaGetErrorString(e));
-  }
-  *out = g;
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (!out) return fail(PHS_ERR_INVALID_ARG, "null output handle pointer");
+    *out = nullptr;
+    if (n_channels < 1 || n_x < 1) return fail(PHS_ERR_INVALID_ARG, "n_channels and n_x must be >= 1");
+    phs_grid *g = new phs_grid;
+    cudaGetDevice(&g->device);
+    g->n_channels = n_channels;
+    g->n_x = n_x;
+    const size_t nb = (size_t)n_channels * n_x * PHS_GRID_BINS;
+    int rc = g->weights.reserve(nb * sizeof(double));
+    if (!rc) rc = g->bins.reserve(nb * sizeof(unsigned long long));
+    if (!rc) rc = g->n_ok.reserve(n_channels * sizeof(unsigned long long));
+    if (rc) { delete g; return rc; }
+    std::vector<double> w(nb, 1.0 / PHS_GRID_BINS);   // rng.cpp:19-29: uniform start
+    cudaError_t e = cudaMemcpy(g->weights.ptr, w.data(), nb * sizeof(double), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      delete g;
+      return fail(PHS_ERR_CUDA, "grid upload: %s", cudaGetErrorString(e));
+    }
+    *out = g;
+    return PHS_OK;
+  });
 }
 
 extern "C" int phs_grid_destroy(phs_grid_t g) {
-  if (!g) return PHS_OK;
-  DeviceGuard dg(g->device);
-  g->weights.release();
-  g->bins.release();
-  g->n_ok.release();
-  g->ch_begin.release();
-  delete g;
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (!g) return PHS_OK;
+    DeviceGuard dg(g->device);
+    g->weights.release();
+    g->bins.release();
+    g->n_ok.release();
+    g->ch_begin.release();
+    delete g;
+    return PHS_OK;
+  });
 }
 
 static int grid_channels(phs_grid_t g, int64_t n_events, const int64_t *counts, cudaStream_t st) {
@@ -1931,37 +2032,43 @@ static int grid_channels(phs_grid_t g, int64_t n_events, const int64_t *counts, 
 extern "C" int phs_grid_sample_device(phs_grid_t g, int64_t n_events, const int64_t *counts,
                                       uint64_t seed, int64_t first_event, double *x,
                                       void *stream) {
-  if (!g) return fail(PHS_ERR_INVALID_ARG, "null grid handle");
-  if (n_events > 0 && !x) return fail(PHS_ERR_INVALID_ARG, "null x");
-  DeviceGuard dg(g->device);
-  cudaStream_t st = (cudaStream_t)stream;
-  if (int rc = grid_channels(g, n_events, counts, st)) return rc;
-  if (n_events == 0) return PHS_OK;
-  CUDA_TRY(phs_launch_philox(x, n_events, g->n_x, seed, first_event, st));
-  CUDA_TRY(phs_launch_grid_sample(x, n_events, g->n_x, g->ch_begin.as<int64_t>(), g->n_channels,
-                                  g->weights.as<double>(), sm_count(g->device), st));
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (!g) return fail(PHS_ERR_INVALID_ARG, "null grid handle");
+    if (n_events > 0 && !x) return fail(PHS_ERR_INVALID_ARG, "null x");
+    DeviceGuard dg(g->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (int rc = grid_channels(g, n_events, counts, st)) return rc;
+    if (n_events == 0) return PHS_OK;
+    CUDA_TRY(phs_launch_philox(x, n_events, g->n_x, seed, first_event, st));
+    CUDA_TRY(phs_launch_grid_sample(x, n_events, g->n_x, g->ch_begin.as<int64_t>(), g->n_channels,
+                                    g->weights.as<double>(), sm_count(g->device), st));
+    return PHS_OK;
+  });
 }
 
 extern "C" int phs_grid_update_device(phs_grid_t g, int64_t n_events, const int64_t *counts,
                                       const double *x, const uint8_t *oks, void *stream) {
-  if (!g) return fail(PHS_ERR_INVALID_ARG, "null grid handle");
-  if (n_events > 0 && (!x || !oks)) return fail(PHS_ERR_INVALID_ARG, "null data pointer");
-  DeviceGuard dg(g->device);
-  cudaStream_t st = (cudaStream_t)stream;
-  if (int rc = grid_channels(g, n_events, counts, st)) return rc;
-  CUDA_TRY(phs_launch_grid_update(x, oks, n_events, g->n_x, g->ch_begin.as<int64_t>(),
-                                  g->n_channels, g->bins.as<unsigned long long>(),
-                                  g->n_ok.as<unsigned long long>(), g->weights.as<double>(),
-                                  sm_count(g->device), st));
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (!g) return fail(PHS_ERR_INVALID_ARG, "null grid handle");
+    if (n_events > 0 && (!x || !oks)) return fail(PHS_ERR_INVALID_ARG, "null data pointer");
+    DeviceGuard dg(g->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (int rc = grid_channels(g, n_events, counts, st)) return rc;
+    CUDA_TRY(phs_launch_grid_update(x, oks, n_events, g->n_x, g->ch_begin.as<int64_t>(),
+                                    g->n_channels, g->bins.as<unsigned long long>(),
+                                    g->n_ok.as<unsigned long long>(), g->weights.as<double>(),
+                                    sm_count(g->device), st));
+    return PHS_OK;
+  });
 }
 
 extern "C" int phs_grid_weights(phs_grid_t g, double *weights) {
-  if (!g || !weights) return fail(PHS_ERR_INVALID_ARG, "null argument");
-  DeviceGuard dg(g->device);
-  CUDA_TRY(cudaMemcpy(weights, g->weights.ptr,
-                      (size_t)g->n_channels * g->n_x * PHS_GRID_BINS * sizeof(double),
-                      cudaMemcpyDeviceToHost));
-  return PHS_OK;
+  return guarded([&]() -> int {
+    if (!g || !weights) return fail(PHS_ERR_INVALID_ARG, "null argument");
+    DeviceGuard dg(g->device);
+    CUDA_TRY(cudaMemcpy(weights, g->weights.ptr,
+                        (size_t)g->n_channels * g->n_x * PHS_GRID_BINS * sizeof(double),
+                        cudaMemcpyDeviceToHost));
+    return PHS_OK;
+  });
 }
