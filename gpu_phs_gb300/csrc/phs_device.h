@@ -137,7 +137,9 @@ void phs_adjoint_sizes(int max_visits, int max_pops, int stack_depth, bool frien
 #define PHS_ADJ_BLOCK_HOST 64
 
 // Inverse map (phs_inverse.cu): for every event and every channel, the x row and factor
-// that channel assigns to the event's momenta.
+// that channel assigns to the event's momenta.  Threads per block (and events per tile and
+// per walk): with ~84 doubles of shared memory per thread, 64-thread blocks keep 5 blocks
+// (10 warps) resident per SM where 128-thread blocks keep 2 (8 warps).
 #define PHS_INV_BLOCK 64
 struct PhsInvLaunch {
   const PhsChannel *channels;  // device, per channel (uniform-beam constants)
