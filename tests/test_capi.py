@@ -39,6 +39,14 @@ def test_exports_every_declared_symbol(lib):
         assert getattr(lib, s) is not None
 
 
+def test_every_declared_function_has_a_prototype():
+    """The loader declares argument and result types for every function of the header:
+    without them ctypes would pass 64-bit pointers as 32-bit ints."""
+    declared = _lib.header_symbols()
+    missing = [s for s in declared if s not in _lib._SIGS]
+    assert not missing, missing
+
+
 def test_exports_the_device_handoff_with_cpp_linkage(lib):
     """include/gpu_phs_transfer.h declares the reference's transfer_to_whizard.h functions
     with C++ linkage: the library exports them under their Itanium-mangled names."""
