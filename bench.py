@@ -253,7 +253,20 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64, pin=
             torch.equal(getattr(outs["fp64_one_pass"], f), getattr(outs[k], f))
             for k in ("fp64_compacting", "fp64_split") for f in ("p", "factor", "volume", "ok")),
         "error_vs_fp64": _errors(torch, outs["fp64_one_pass"], outs["fp32_mixed"], proc.sqrts)}
-    del outs, x
+    # the reference CPU path beside it, on all n events (the GPU's x), checked event by event
+    # against the FP64 split form and the FP32-pair form
+    threads = os.cpu_count() or 1
+    gen, kind = cpu_generator(proc, proc.sqrts)
+    rate, passes, ref = cpu_time(gen, x.cpu().numpy(), 2.0, threads)
+    rows = torch.full((n,), proc.n_out, dtype=torch.int64, device="cuda")
+    res["precision_13TeV"]["cpu_baseline"] = {
+        "value": rate, "unit": "events/s", "cores": threads, "kind": kind,
+        "sample": f"all {n} events (the GPU's x), {passes} passes, all host threads"}
+    for k in ("fp64_split", "fp32_mixed"):
+        o = outs[k]
+        res["precision_13TeV"][f"{k}_parity_vs_cpu"] = parity_vs_cpu(
+            torch, ref, o.p.view(-1), o.factor, o.volume, o.ok, rows, proc.sqrts)
+    del outs, x, ref, gen
 
     procs, counts = P.batched(seed=2024, n_channels=64, total_events=1 << 24)
     spaces = [PhaseSpace(p, 500.0, 500.0) for p in procs]
@@ -287,7 +300,9 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64, pin=
     res["batched_64ch"] = {
         "n_channels": 64, "n_events": n, "n_out_range": [3, 8],
         "counts": "power law, exponent 1.5, seed 2024",
-        "launch": "one persistent kernel per step, replayed from a CUDA graph",
+        "launch": "one CUDA-graph replay per step: one pass and compacting are one "
+                  "persistent kernel; the split forms replay the FP32 pre-test, a scan, the "
+                  "walk and (FP32 pairs) the exact FP64 path's scan and kernel",
         **{f"{k}_events_per_s": n / bres[k] * 1e3 for k, _, _ in forms},
         "kernel_variants": tuned,
         "speedup_vs_plain_fp64": bres["fp64_one_pass"] / bres["fp32_mixed"],
@@ -325,6 +340,34 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64, pin=
     res["batched_64ch"]["momentum_rms_rel"] = (sq / max(n_p, 1)) ** 0.5
     res["batched_64ch"]["momentum_rel_definition"] = \
         "per particle max_mu |dp^mu| / max(E, 1e-3 sqrt(s)), events ok in both"
+    # the reference CPU path beside it: every channel's events through its own process on
+    # all host threads, timed over the whole batch and checked event by event
+    threads = os.cpu_count() or 1
+    xh = xb.cpu().numpy()
+    flat = FlatResult(int(po[-1]), n)
+    el, kinds, e = 0.0, set(), 0
+    for i, (sp, c) in enumerate(zip(spaces, counts)):
+        c = int(c)
+        if c:
+            gen, kind = cpu_generator(sp.proc, sp.proc.sqrts)
+            kinds.add(kind)
+            xc = xh[xo[i]:xo[i + 1]].reshape(c, sp.proc.n_x)
+            t0 = time.perf_counter()
+            r = gen.generate(xc, threads=threads)
+            el += time.perf_counter() - t0
+            flat.p[po[i]:po[i + 1]] = r.p.reshape(-1)
+            flat.factor[e:e + c], flat.volume[e:e + c], flat.ok[e:e + c] = r.factor, r.volume, r.ok
+        e += c
+    rows = torch.from_numpy(np.repeat([sp.proc.n_out for sp in spaces], counts)).to("cuda")
+    res["batched_64ch"]["cpu_baseline"] = {
+        "value": n / el, "unit": "events/s", "cores": threads, "kind": "/".join(sorted(kinds)),
+        "sample": f"all {n} events of the batch (the GPU's x), one pass per channel, all host "
+                  "threads"}
+    for k in ("fp64_split", "fp32_mixed"):
+        bp, bf, bv, bo = bufs[k]
+        res["batched_64ch"][f"{k}_parity_vs_cpu"] = parity_vs_cpu(
+            torch, flat, bp, bf, bv, bo, rows, 1000.0)
+    del flat, xh
     del bufs, xb, spaces
 
     # adjoint: forward + reverse on 1e6 tt events with random cotangents
@@ -459,65 +502,79 @@ def whizard_process(name: str):
                    z["flv_widths"], n_x=int(meta[2]), name=f"whizard_{name}", sqrts=1000.0)
 
 
-def cpu_reference_rate(proc, sqrts, seconds: float, max_events: int, prefer_ref: bool = True):
-    """Events/s of the reference CPU path (oracle/_ref if it loads here, else the C
-    restatement) on all host threads, on the first events of the same Philox stream."""
-    from gpu_phs_gb300.philox import uniform_x
+def cpu_generator(proc, sqrts):
+    """The reference CPU path for one process: the reference's own phs_cpu.cpp (oracle/_ref)
+    where it was built on this machine, else its C restatement.  Returns (generator, kind)."""
     from oracle import oracle
-    threads = os.cpu_count() or 1
-    kind = "port"
-    gen = None
-    if prefer_ref and oracle.ref_available():
+    if oracle.ref_available():
         try:
-            gen = oracle.RefCPU(proc, sqrts)
-            kind = "reference"
+            return oracle.RefCPU(proc, sqrts), "reference"
         except OSError:
-            gen = None
-    if gen is None:
-        gen = oracle.Oracle(proc, sqrts)
-    n = 65536
-    x = uniform_x(SEED, n, proc.n_x)
-    t = time.perf_counter()
-    gen.generate(x, threads=threads)
-    rate = n / (time.perf_counter() - t)
-    n = int(min(max_events, max(4096, rate * seconds / 4)))
-    x = uniform_x(SEED, n, proc.n_x)
-    done, t0 = 0, time.perf_counter()
+            pass
+    return oracle.Oracle(proc, sqrts), "port"
+
+
+def cpu_time(gen, x, min_seconds: float, threads: int):
+    """Events/s of gen over x (all host threads), repeated until min_seconds have passed
+    (at least once); returns (rate, passes, the last pass's outputs)."""
+    done, passes, t0 = 0, 0, time.perf_counter()
     while True:
-        gen.generate(x, threads=threads)
-        done += n
+        r = gen.generate(x, threads=threads)
+        done += x.shape[0]
+        passes += 1
         el = time.perf_counter() - t0
-        if el >= seconds:
-            break
-    return done / el, kind, threads, n, gen, x
+        if el >= min_seconds:
+            return done / el, passes, r
+
+
+def parity_vs_cpu(torch, ref, p, factor, volume, ok, n_out_rows, sqrts):
+    """The GPU outputs (device tensors; p flat) against the CPU path's on the same events:
+    ok-flag mismatches; over the events ok on both sides, the largest per-particle momentum
+    error max_mu |dp| / max(E, 1e-3 sqrt(s)) and the largest relative factor error; the
+    largest relative volume error over all events."""
+    dev = p.device
+    rok = torch.from_numpy(ref.ok).to(dev)
+    res = {"events": int(rok.numel()), "ok_mismatches_vs_cpu": int((ok != rok).sum().item())}
+    both = rok.bool() & ok.bool()
+    rf = torch.from_numpy(ref.factor).to(dev)
+    fr = (factor[both] - rf[both]).abs() / rf[both].abs()
+    res["factor_max_rel_vs_cpu"] = fr.max().item() if fr.numel() else 0.0
+    del rf
+    rv = torch.from_numpy(ref.volume).to(dev)
+    res["volume_max_rel_vs_cpu"] = ((volume - rv).abs() / rv.abs()).max().item()
+    del rv
+    rows = torch.repeat_interleave(both, n_out_rows)
+    rp = torch.from_numpy(ref.p.reshape(-1)).to(dev).view(-1, 4)[rows]
+    d = (p.view(-1, 4)[rows] - rp).abs().amax(-1) / rp[:, 0].abs().clamp(min=1e-3 * sqrts)
+    res["momentum_max_rel_vs_cpu"] = d.max().item() if d.numel() else 0.0
+    res["definition"] = "per particle max_mu |dp^mu| / max(E, 1e-3 sqrt(s)), events ok on both"
+    return res
+
+
+class FlatResult:
+    """CPU outputs of a batch, flat in the batch's layout."""
+
+    def __init__(self, n_p, n):
+        self.p = np.zeros(n_p)
+        self.factor = np.zeros(n)
+        self.volume = np.zeros(n)
+        self.ok = np.zeros(n, np.uint8)
 
 
 def run_reference(args):
+    """The reference CPU path on this machine's host cores, all threads, on the same
+    workload as our arm: every step generates all n events of the workload (the first n
+    events of the same Philox stream)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    proc, _ = workload(args.config)
-    from gpu_phs_gb300.philox import uniform_x
     from oracle import oracle
+    proc, n = workload(args.config)
+    if args.events:
+        n = args.events
     threads = os.cpu_count() or 1
-    kind = "port"
-    gen = None
-    if oracle.ref_available():
-        try:
-            gen = oracle.RefCPU(proc, proc.sqrts)
-            kind = "reference"
-        except OSError:
-            gen = None
-    if gen is None:
-        gen = oracle.Oracle(proc, proc.sqrts)
-    # size each step so that warmup + steps stay within about a minute
-    n = 65536
-    x = uniform_x(SEED, n, proc.n_x)
-    t = time.perf_counter()
-    gen.generate(x, threads=threads)
-    rate = n / (time.perf_counter() - t)
-    n = int(min(1 << 21, max(4096, rate * 60.0 / max(1, args.steps + args.warmup))))
-    x = uniform_x(SEED, n, proc.n_x)
+    gen, kind = cpu_generator(proc, proc.sqrts)
+    x = oracle.uniform_x(SEED, n, proc.n_x, threads=threads)
     for _ in range(args.warmup):
         gen.generate(x, threads=threads)
     t0 = time.perf_counter()
@@ -525,14 +582,15 @@ def run_reference(args):
         gen.generate(x, threads=threads)
     el = time.perf_counter() - t0
     value = n * args.steps / el
-    sample = f"{n} events of the {proc.name} workload per step (first events of the Philox stream)"
+    sample = (f"all {n} events of the {proc.name} workload per step (the GPU arm's events), "
+              f"{args.steps} steps")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "events/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (Philox4x32-10 x)",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (Philox4x32-10 x, seed 1234)",
         "config": {"workload": proc.name, "n_events_per_step": n, "n_x": proc.n_x,
-                   "n_out": proc.n_out, "sqrts_gev": proc.sqrts,
+                   "n_out": proc.n_out, "sqrts_gev": proc.sqrts, "same_config": True,
                    "path": "reference phs_cpu.cpp set_msq_cpu + set_angles_cpu" if kind == "reference"
                    else "C restatement of phs_cpu.cpp (oracle/phs_oracle.c)"},
         "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": kind,
@@ -676,11 +734,20 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        rate, kind, threads, sample_n, _, _ = cpu_reference_rate(proc, proc.sqrts, args.cpu_seconds,
-                                                                  1 << 21)
+        # the reference CPU path on the same n events (x copied from the device), repeated
+        # for about --cpu-seconds on all host threads; its outputs of the last pass are
+        # checked against the GPU's of the timed run, event by event
+        threads = os.cpu_count() or 1
+        gen, kind = cpu_generator(proc, proc.sqrts)
+        xh = x.cpu().numpy()
+        rate, passes, ref = cpu_time(gen, xh, args.cpu_seconds, threads)
+        rows = torch.full((n,), proc.n_out, dtype=torch.int64, device=x.device)
         cpu = {"value": rate, "unit": "events/s", "cores": threads, "kind": kind,
-               "sample": f"{sample_n} events of the same workload, repeated for "
-                         f"{args.cpu_seconds:.0f} s on all host threads"}
+               "sample": f"all {n} events of the workload (the GPU's x), {passes} passes, "
+                         f"all host threads",
+               "parity_vs_gpu": parity_vs_cpu(torch, ref, out.p.view(-1), out.factor, out.volume,
+                                              out.ok, rows, proc.sqrts)}
+        del ref, xh, gen
 
     if rank == 0:
         line = {
@@ -693,18 +760,21 @@ def run_ours(args):
                        "sqrts_gev": proc.sqrts, "parallelism": f"replicas x{world}",
                        "l2": "inputs (x 1.12 GB) and outputs larger than L2; no flush"},
             "ok_fraction": ok_frac,
-            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak,
-                         "unit": "GB/s", "frac": achieved_gbs / hbm_peak, "traffic": traffic,
-                         "peak_kind": peak_kind, "bytes_per_event": bpe,
-                         "kernel_ms": launch_ms,
-                         "fp64": {"achieved_gflops": fp64_achieved, "peak_gflops": fp64_peak,
-                                  "frac": fp64_achieved / fp64_peak, "flops_per_event": fpe,
-                                  "peak_kind": "measured (phs_measure_fma_peak, DFMA chains)",
-                                  "pipe_utilization_ncu": pipe_pct / 100 if pipe_pct else None,
-                                  "note": "the binding roof: frac counts each transcendental "
-                                          "as one operation; ncu's FP64-pipe utilisation "
-                                          "(profiles/fwd_f64_tt_ncu.md) counts the "
-                                          "instructions the library math expands into"}},
+            # the binding roof is the FP64 pipe: achieved = the flops model's operations
+            # per event x events per launch / the launch's CUDA-event time, against the
+            # measured DFMA peak; HBM (a few percent) beside it
+            "roofline": {"bound": "fp64", "achieved": fp64_achieved / 1e3,
+                         "peak": fp64_peak / 1e3, "unit": "TFLOP/s",
+                         "frac": fp64_achieved / fp64_peak, "traffic": traffic,
+                         "peak_kind": "measured (phs_measure_fma_peak: DFMA chains on every SM)",
+                         "flops_per_event": fpe, "kernel_ms": launch_ms,
+                         "pipe_utilization_ncu": pipe_pct / 100 if pipe_pct else None,
+                         "note": "frac counts each transcendental call as one operation; the "
+                                 "ncu FP64-pipe utilisation counts the instructions the "
+                                 "library math expands into",
+                         "hbm": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                                 "frac": achieved_gbs / hbm_peak, "peak_kind": peak_kind,
+                                 "bytes_per_event": bpe}},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "e2e_whizard_abi": e2e_abi,

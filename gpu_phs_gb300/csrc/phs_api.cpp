@@ -1092,7 +1092,10 @@ extern "C" int phs_batch_set_precision(phs_batch_t b, int precision) {
 // cudaMalloc.  Nothing on this path calls cudaMalloc, cudaFree or an allocating library
 // routine.  At most PHS_NOALLOC_MAX_CHANNELS channels.  The first call on a device
 // resolves the scratch array's address (make it before any stream capture).  Calls that
-// overlap on the GPU share the scratch array and race.
+// overlap on the GPU share the scratch array and race.  It always runs the plain FP64
+// one-pass kernel (variant 0), whatever precision or variants the handle has set.  Its
+// uploads read the host vectors of this call, which are gone when it returns, so a call on
+// a stream that is being captured is refused before anything is enqueued.
 extern "C" int phs_generate_device_noalloc(phs_process_t h, double E1, double E2,
                                            int64_t n_events, const int64_t *counts,
                                            const double *x, double *p, double *f, double *v,
@@ -1115,6 +1118,17 @@ extern "C" int phs_generate_device_noalloc(phs_process_t h, double E1, double E2
       return fail(PHS_ERR_INVALID_ARG, "sqrt(s) = %g is below the final-state mass sum %g", sqrts,
                   m_tot);
     DeviceGuard g(h->device);
+    {
+      cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+      cudaError_t e = cudaStreamIsCapturing((cudaStream_t)stream, &cap);
+      if (e != cudaSuccess)
+        return fail(PHS_ERR_CUDA, "phs_generate_device_noalloc: cudaStreamIsCapturing: %s",
+                    cudaGetErrorString(e));
+      if (cap != cudaStreamCaptureStatusNone)
+        return fail(PHS_ERR_UNSUPPORTED, "phs_generate_device_noalloc refuses a stream that is "
+                    "being captured: its uploads read host memory that is released when the "
+                    "call returns");
+    }
     std::vector<PhsChannel> prog(P.n_channels);
     int depth = 0;
     std::string err;

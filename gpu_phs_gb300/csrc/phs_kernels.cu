@@ -10,6 +10,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "phs_device.h"
 #include "phs_event_f64.cuh"
 #include "phs_program.h"
@@ -337,11 +339,19 @@ cudaError_t phs_launch_forward_exact(const PhsLaunch &a, int n_blocks, cudaStrea
   return cudaGetLastError();
 }
 
+// SMs of the current device (grid caps of the grid-stride kernels below).
+static int current_sm_count() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 1;
+}
+
 cudaError_t phs_launch_whizard_sparse(const PhsSparseLaunch &a, cudaStream_t stream) {
   const int64_t total = a.n_events * a.n_prt;
   if (total <= 0) return cudaSuccess;
-  const int64_t blocks = (total + 255) / 256;
-  phs_whizard_sparse_kernel<<<(int)(blocks < 152 * 32 ? blocks : 152 * 32), 256, 0, stream>>>(a);
+  const int64_t blocks = (total + 255) / 256, cap = (int64_t)current_sm_count() * 32;
+  phs_whizard_sparse_kernel<<<(int)(blocks < cap ? blocks : cap), 256, 0, stream>>>(a);
   return cudaGetLastError();
 }
 
@@ -349,8 +359,8 @@ cudaError_t phs_launch_philox(double *x, int64_t n_events, int32_t n_x, uint64_t
                               int64_t first_event, cudaStream_t stream) {
   const int64_t n = n_events * n_x;
   if (n <= 0) return cudaSuccess;
-  const int64_t blocks_needed = ((n >> 1) + 2 + 255) / 256;
-  const int grid = (int)(blocks_needed < 152 * 16 ? blocks_needed : 152 * 16);
+  const int64_t blocks_needed = ((n >> 1) + 2 + 255) / 256, cap = (int64_t)current_sm_count() * 16;
+  const int grid = (int)(blocks_needed < cap ? blocks_needed : cap);
   phs_philox_kernel<<<grid, 256, 0, stream>>>(x, first_event * n_x, n, seed);
   return cudaGetLastError();
 }
@@ -375,8 +385,10 @@ struct PhsNoAllocScratch {
 static __device__ __align__(256) unsigned char phs_noalloc_scratch[sizeof(PhsNoAllocScratch)];
 
 // Device address of the scratch array per device (filled at set-up; in host code the
-// array's name only stands in for the symbol and is never a device address).
+// array's name only stands in for the symbol and is never a device address).  The mutex
+// orders first calls from several host threads.
 static void *g_noalloc_addr[256];
+static std::mutex g_noalloc_mu;
 
 size_t phs_noalloc_scratch_bytes() { return sizeof(PhsNoAllocScratch); }
 
@@ -389,14 +401,19 @@ cudaError_t phs_launch_forward_f64_noalloc(PhsLaunch a, const PhsChannel *channe
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
-  if (!g_noalloc_addr[dev]) {
-    // set-up, once per device, with that device current
-    void *ptr = nullptr;
-    e = cudaGetSymbolAddress(&ptr, phs_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_noalloc_addr[dev] = ptr;
+  void *addr = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      // set-up, once per device, with that device current
+      void *ptr = nullptr;
+      e = cudaGetSymbolAddress(&ptr, phs_noalloc_scratch);
+      if (e != cudaSuccess) return e;
+      g_noalloc_addr[dev] = ptr;
+    }
+    addr = g_noalloc_addr[dev];
   }
-  PhsNoAllocScratch *s = static_cast<PhsNoAllocScratch *>(g_noalloc_addr[dev]);
+  PhsNoAllocScratch *s = static_cast<PhsNoAllocScratch *>(addr);
   // pageable host sources: each copy has read its source when the call returns
   e = cudaMemcpyAsync(s->channels, channels, (size_t)n_channels * sizeof(PhsChannel),
                       cudaMemcpyHostToDevice, stream);
@@ -411,6 +428,8 @@ cudaError_t phs_launch_forward_f64_noalloc(PhsLaunch a, const PhsChannel *channe
   a.n_segments = n_segments;
   if (a.n_tiles <= 0) return cudaSuccess;
   const size_t smem = phs_forward_smem_bytes(a.stack_depth, PHS_FWD_BLOCK);
+  e = allow_smem(f64_kernel<false>(0), smem);
+  if (e != cudaSuccess) return e;
   phs_forward_f64_kernel<false, false, 4><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
   return cudaGetLastError();
 }

@@ -128,14 +128,21 @@ int phs_generate_beams_device(phs_process_t proc, int64_t n_events, const int64_
                               const double *E1, const double *E2, const double *x, double *p,
                               double *factors, double *volumes, uint8_t *oks, void *stream);
 
-/* As phs_generate_device, for callers that cannot allocate device memory (a host that owns
- * the device heap through its own allocator, a sandbox or plug-in host that denies
- * cudaMalloc, or a loop that must not synchronise the device): takes the beam energies
- * itself and needs no phs_process_set_beams.  It allocates nothing: the channel programs
- * and event segments go into one static device array of the library, so the process may
- * have at most 256 channels (PHS_ERR_UNSUPPORTED beyond).  The first call on a device
- * resolves that array's address; make it before any stream capture.  All calls share the
- * array, so calls that overlap on the GPU race.  No counterpart in the reference. */
+/* Forward generation for callers that cannot allocate device memory (a host that owns the
+ * device heap through its own allocator, a sandbox or plug-in host that denies cudaMalloc,
+ * or a loop that must not pay for the device-wide synchronisation cudaMalloc/cudaFree
+ * imply).  Uniform beams E1, E2 given here (no phs_process_set_beams needed).  It always
+ * runs the plain FP64 one-pass kernel (128 threads x 4 blocks per SM): the precision and
+ * the kernel variants set on the handle do not apply; its outputs equal phs_generate_device's
+ * FP64 outputs bit for bit.  It allocates nothing: the channel programs, compiled on the
+ * host at every call, and the event segments go into one static device array of the
+ * library, so the process may have at most 256 channels (PHS_ERR_UNSUPPORTED beyond).  Those
+ * uploads come from pageable host memory, so the call may block the host until they are
+ * staged and may synchronise with `stream`.  The first call on a device resolves that
+ * array's address; make it before any stream capture.  A call on a stream that is being
+ * captured is refused (PHS_ERR_UNSUPPORTED) before anything is enqueued, since the uploads
+ * read host memory that is released when the call returns.  All calls share the array,
+ * so calls that overlap on the GPU race.  No counterpart in the reference. */
 int phs_generate_device_noalloc(phs_process_t proc, double E1, double E2, int64_t n_events,
                                 const int64_t *channel_counts, const double *x, double *p,
                                 double *factors, double *volumes, uint8_t *oks, void *stream);

@@ -20,7 +20,17 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libphsoracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libphsref.so")
-REF_SRC = "/root/reference"
+
+
+def reference_dir() -> str:
+    """Directory of the reference sources: $GPU_PHS_REFERENCE_DIR, else the default of
+    oracle/Makefile (REF).  It need not exist: the GPU machine has no reference sources."""
+    env = os.environ.get("GPU_PHS_REFERENCE_DIR")
+    if env:
+        return env
+    r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+    return r.stdout.strip()
+
 
 _pd = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _pi = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
@@ -30,8 +40,9 @@ _pu8 = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
 def build(ref: bool = True) -> None:
     """Compile the restatement, and the reference harness when the reference sources exist."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    if ref and os.path.isdir(REF_SRC):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+    src = reference_dir()
+    if ref and os.path.exists(os.path.join(src, "phs_cpu.cpp")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={src}"], check=True)
 
 
 def _load(path: str) -> C.CDLL:
@@ -166,6 +177,24 @@ class Oracle:
                                   vp(x_own, np.float64), vp(factor_own, np.float64),
                                   fac.reshape(-1), xo.reshape(-1), threads)
         return fac, xo
+
+
+def uniform_x(seed: int, n_events: int, n_x: int, first_event: int = 0,
+              threads: int = 0) -> np.ndarray:
+    """The Philox stream of gpu_phs_gb300.philox.uniform_x (the same values), computed by
+    the oracle library on all host threads: for full-size workloads."""
+    L = Oracle.lib()
+    if not hasattr(L, "_ux"):
+        L.oracle_uniform_x.restype = C.c_int
+        L.oracle_uniform_x.argtypes = [C.c_uint64, C.c_long, C.c_long, C.c_int, _pd, C.c_int]
+        L._ux = True
+    x = np.empty((n_events, n_x), np.float64)
+    if n_events:
+        rc = L.oracle_uniform_x(seed, first_event, n_events, n_x, x.reshape(-1),
+                                threads or os.cpu_count() or 1)
+        if rc != 0:
+            raise ValueError("bad sizes")
+    return x
 
 
 def ref_available() -> bool:

@@ -900,3 +900,61 @@ int oracle_inverse(const oracle_t *o, long n_events, int n_x, const double *p,
   for (int t = 1; t < n_threads; t++) pthread_join(th[t], NULL);
   return 0;
 }
+
+/* ------------------------------------------------------------------------ Philox x
+ * The benchmark's x stream on the host, multi-threaded: Philox4x32-10 (Salmon et al.,
+ * SC'11) with the layout of gpu_phs_gb300/philox.py (element e of the flat array takes
+ * block e >> 1, counter (block lo, block hi, 0, 0), key (seed lo, seed hi); the output
+ * words give two doubles ((r0 << 32 | r1) >> 11) 2^-53 and ((r2 << 32 | r3) >> 11) 2^-53,
+ * element e the (e & 1)-th).  For full-size comparisons, where numpy is too slow. */
+typedef struct {
+  uint64_t seed;
+  long e0, n; /* flat elements [e0, e0 + n) of the stream, written to out[0 .. n) */
+  double *out;
+} philox_job_t;
+
+static void philox_block(uint64_t block, uint64_t seed, double u[2]) {
+  uint32_t c0 = (uint32_t)block, c1 = (uint32_t)(block >> 32), c2 = 0, c3 = 0;
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  for (int r = 0; r < 10; r++) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n1 = (uint32_t)p1;
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1, n3 = (uint32_t)p0;
+    c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  u[0] = (double)((((uint64_t)c0 << 32) | c1) >> 11) * 0x1.0p-53;
+  u[1] = (double)((((uint64_t)c2 << 32) | c3) >> 11) * 0x1.0p-53;
+}
+
+static void *run_philox(void *arg) {
+  const philox_job_t *j = (const philox_job_t *)arg;
+  for (long i = 0; i < j->n; i++) {
+    const long e = j->e0 + i;
+    double u[2];
+    philox_block((uint64_t)(e >> 1), j->seed, u);
+    j->out[i] = u[e & 1];
+  }
+  return NULL;
+}
+
+int oracle_uniform_x(uint64_t seed, long first_event, long n_events, int n_x, double *x,
+                     int n_threads) {
+  if (n_events < 0 || n_x < 1 || first_event < 0) return -1;
+  const long n = n_events * n_x, e0 = first_event * n_x;
+  if (n_threads < 1) n_threads = 1;
+  if (n_threads > 512) n_threads = 512;
+  if (n < 4096L * n_threads) n_threads = 1;
+  philox_job_t jobs[512];
+  pthread_t th[512];
+  for (int t = 0; t < n_threads; t++) {
+    const long lo = n * t / n_threads, hi = n * (t + 1) / n_threads;
+    philox_job_t jb = {seed, e0 + lo, hi - lo, x + lo};
+    jobs[t] = jb;
+  }
+  for (int t = 1; t < n_threads; t++) pthread_create(&th[t], NULL, run_philox, &jobs[t]);
+  run_philox(&jobs[0]);
+  for (int t = 1; t < n_threads; t++) pthread_join(th[t], NULL);
+  return 0;
+}

@@ -1,5 +1,6 @@
-"""Regenerates the golden fixtures in tests/golden/ (run in a checkout that has the
-reference at /root/reference; the fixtures themselves travel without it).
+"""Regenerates the golden fixtures in tests/golden/ (run where the reference sources are:
+the directory oracle.reference_dir() names, $GPU_PHS_REFERENCE_DIR or oracle/Makefile's
+REF; the fixtures themselves travel without it).
 
 Two kinds of fixture, each a compressed .npz:
 
@@ -34,7 +35,7 @@ from gpu_phs_gb300.philox import uniform_x  # noqa: E402
 from gpu_phs_gb300.refformat import read_ref  # noqa: E402
 from oracle import oracle  # noqa: E402
 
-SAMPLES = "/root/reference/samples"
+SAMPLES = os.path.join(oracle.reference_dir(), "samples")
 
 
 def proc_arrays(proc, prefix=""):

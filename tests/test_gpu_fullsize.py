@@ -1,0 +1,172 @@
+"""Parity with the CPU oracle at the sizes the benchmark runs, every event compared:
+
+* WW (one s-channel tree at sqrt(s) = 500 GeV), 1e6 events;
+* tt (the 6-particle top-pair tree at 1 TeV), 1e7 events;
+* the 13 TeV 2 -> 6 massless tree with collinear maps, 2^24 events (96 % fail the
+  kinematic test);
+* the 64-channel batch (seeded trees with 3-8 outgoing particles at 1 TeV, power-law
+  counts), 2^24 events in one launch, each channel against its own oracle run.
+
+Each runs through every FP64 form of the forward map -- one pass (variant 0), compacting
+(variant 2: an FP64 pre-pass tests every event, the walk runs over the survivors) and
+split (variant 6: the FP32 pre-test with error bounds, then the FP64 walk) -- and through
+the FP32-pair form (one pass and split).  The oracle runs on all host cores.
+
+Bar, as in test_gpu_parity.py: FP64 -- ok flags bit-exact, momenta within 1e-12 of
+max(E, 1e-3 sqrt(s)), factors within 1e-12 relative, volumes within 1e-15 relative, zero
+momenta and factor where ok = 0.  FP32 pairs -- ok flags bit-exact, momenta and factors
+within 1e-7 (the float-float walk carries ~48 bits).  A failure lists the first
+mismatching events.
+
+The comparison runs on the GPU (torch): the oracle's outputs are uploaded once per
+workload and each form's outputs are checked against them in place.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from gpu_phs_gb300 import processes as P
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+SEED = 1234            # the benchmark's Philox seed
+F64_FORMS = [("fp64_one_pass", 0, (-1, 0)), ("fp64_compacting", 0, (-1, 2)),
+             ("fp64_split", 0, (-1, 6))]
+FF_FORMS = [("fp32_pair_one_pass", 1, (1, -1)), ("fp32_pair_split", 1, (5, -1))]
+TOL = {0: (1e-12, 1e-12), 1: (1e-7, 1e-7)}   # precision -> (momenta, factors)
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _threads():
+    return os.cpu_count() or 1
+
+
+class Ref:
+    """The oracle's outputs of one workload on the device (p flat in the GPU layout)."""
+
+    def __init__(self, torch, p, factor, volume, ok, sqrts):
+        dev = "cuda"
+        self.p = torch.from_numpy(p).to(dev)
+        self.factor = torch.from_numpy(factor).to(dev)
+        self.volume = torch.from_numpy(volume).to(dev)
+        self.ok = torch.from_numpy(ok).to(dev)
+        self.sqrts = sqrts
+
+
+def compare(torch, ref: Ref, p, factor, volume, ok, n_out_rows, precision, label):
+    """p: flat momenta; n_out_rows: per event the number of particle rows (a tensor of
+    n_out per event), so that rows can be matched to events."""
+    tol_p, tol_f = TOL[precision]
+    bad = torch.nonzero(ok != ref.ok).flatten()
+    msg = []
+    if bad.numel():
+        idx = bad[:10].tolist()
+        msg.append(f"{bad.numel()} ok-flag mismatches, first events {idx} "
+                   f"(gpu {ok[bad[:10]].tolist()}, oracle {ref.ok[bad[:10]].tolist()})")
+    sel = ref.ok.bool()
+    # factors
+    fr = (factor[sel] - ref.factor[sel]).abs() / ref.factor[sel].abs()
+    fmax = fr.max().item() if fr.numel() else 0.0
+    if fmax > tol_f:
+        msg.append(f"factor error {fmax:.3e} > {tol_f:g}")
+    # volumes (every event)
+    vr = ((volume - ref.volume).abs() / ref.volume.abs()).max().item()
+    if vr > 1e-15 and precision == 0:
+        msg.append(f"volume error {vr:.3e}")
+    # momenta, per particle row
+    rows_ok = torch.repeat_interleave(sel, n_out_rows)
+    P4 = p.view(-1, 4)
+    R4 = ref.p.view(-1, 4)
+    d = (P4[rows_ok] - R4[rows_ok]).abs().amax(-1)
+    rel = d / R4[rows_ok][:, 0].abs().clamp(min=1e-3 * ref.sqrts)
+    pmax = rel.max().item() if rel.numel() else 0.0
+    if pmax > tol_p:
+        msg.append(f"momentum error {pmax:.3e} > {tol_p:g}")
+    zero_p = bool((P4[~rows_ok] == 0).all().item())
+    zero_f = bool((factor[~sel] == 0).all().item())
+    if not (zero_p and zero_f):
+        msg.append("ok = 0 events with non-zero momenta or factor")
+    print(f"{label}: {int(ok.numel())} events, ok {sel.float().mean().item():.4f}, "
+          f"ok mismatches {bad.numel()}, max momentum {pmax:.2e}, factor {fmax:.2e}, "
+          f"volume {vr:.2e}")
+    assert not msg, f"{label}: " + "; ".join(msg)
+
+
+def _single(torch, builder, n):
+    from gpu_phs_gb300.api import PhaseSpace, philox_x
+    proc = builder()
+    x = philox_x(n, proc.n_x, SEED)
+    xh = x.cpu().numpy()
+    r = oracle.Oracle(proc, proc.sqrts).generate(xh, threads=_threads())
+    ref = Ref(torch, r.p.reshape(-1), r.factor, r.volume, r.ok, proc.sqrts)
+    del r, xh
+    rows = torch.full((n,), proc.n_out, dtype=torch.int64, device="cuda")
+    for label, prec, variants in F64_FORMS + FF_FORMS:
+        ps = PhaseSpace(proc, proc.sqrts / 2, proc.sqrts / 2)
+        ps.set_precision(prec)
+        ps.set_variants(*variants)
+        ev = ps.generate(x)
+        torch.cuda.synchronize()
+        compare(torch, ref, ev.p.view(-1), ev.factor, ev.volume, ev.ok, rows, prec,
+                f"{proc.name} {label}")
+        del ev
+        ps.close()
+
+
+def test_ww_1e6_every_form(torch):
+    _single(torch, P.ww, 1_000_000)
+
+
+def test_tt_1e7_every_form(torch):
+    _single(torch, P.tt, 10_000_000)
+
+
+def test_precision_13tev_2p24_every_form(torch):
+    _single(torch, P.precision, 1 << 24)
+
+
+def test_batched_64ch_2p24_every_form(torch):
+    """One launch over the 64-channel batch per form; the oracle per channel."""
+    from gpu_phs_gb300.api import Batch, PhaseSpace, philox_fill
+    procs, counts = P.batched(seed=2024, n_channels=64, total_events=1 << 24)
+    spaces = [PhaseSpace(p, 500.0, 500.0) for p in procs]
+    n = int(counts.sum())
+    probe = Batch(spaces)
+    xo, po = probe.offsets(counts)
+    probe.close()
+    xb = torch.empty(int(xo[-1]), dtype=torch.float64, device="cuda")
+    philox_fill(xb, int(xo[-1]), 1, SEED)
+    xh = xb.cpu().numpy()
+    rp = np.zeros(int(po[-1]))
+    rf, rv = np.zeros(n), np.zeros(n)
+    rok = np.zeros(n, np.uint8)
+    e = 0
+    for i, (proc, c) in enumerate(zip(procs, counts)):
+        c = int(c)
+        if c:
+            r = oracle.Oracle(proc, 1000.0).generate(xh[xo[i]:xo[i + 1]].reshape(c, proc.n_x),
+                                                     threads=_threads())
+            rp[po[i]:po[i + 1]] = r.p.reshape(-1)
+            rf[e:e + c], rv[e:e + c], rok[e:e + c] = r.factor, r.volume, r.ok
+        e += c
+    ref = Ref(torch, rp, rf, rv, rok, 1000.0)
+    del rp, xh
+    rows = torch.from_numpy(np.repeat([p.n_out for p in procs], counts)).to("cuda")
+    for label, prec, variants in F64_FORMS + FF_FORMS:
+        b = Batch(spaces)
+        b.set_precision(prec)
+        b.set_variants(*variants)
+        p, f, v, ok = b.generate(xb, counts)
+        torch.cuda.synchronize()
+        compare(torch, ref, p, f, v, ok, rows, prec, f"batched_64ch {label}")
+        del p, f, v, ok
+        b.close()

@@ -139,10 +139,22 @@ def test_oracle_rejects_bad_trees():
         oracle.Oracle(bad, 500.0)
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/samples"), reason="reference samples absent")
+SAMPLES = os.path.join(oracle.reference_dir(), "samples")
+
+
+@pytest.mark.skipif(not os.path.isdir(SAMPLES), reason="reference samples absent")
 def test_ref_reader_matches_fixture():
     from gpu_phs_gb300.refformat import read_ref
-    proc, fr, ev = read_ref("/root/reference/samples/ttH.ref")
+    proc, fr, ev = read_ref(os.path.join(SAMPLES, "ttH.ref"))
     z = golden("whizard_ttH")
     assert np.array_equal(proc.d1, z["d1"]) and np.array_equal(proc.map_ids, z["map_ids"])
     assert len(ev.ok) == 999 and ev.x.shape == (999, 5)
+
+
+def test_oracle_philox_matches_numpy_stream():
+    """The threaded C Philox of the oracle library (used for full-size comparisons) gives
+    the stream of gpu_phs_gb300.philox.uniform_x, at odd offsets and 64-bit seeds too."""
+    for n, nx, e0, seed in [(1000, 14, 0, 42), (777, 5, 123, 7), (1, 3, 9, 1234),
+                            (50_001, 16, 3, 2**40 + 5), (0, 8, 0, 1)]:
+        a = oracle.uniform_x(seed, n, nx, e0, threads=4)
+        assert np.array_equal(a, uniform_x(seed, n, nx, first_event=e0)), (n, nx, e0)

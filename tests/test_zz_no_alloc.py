@@ -30,12 +30,12 @@ def torch():
     return torch
 
 
-def _noalloc(lib, ps, E, x, counts, out, torch):
+def _noalloc(lib, ps, E, x, counts, out, torch, E2=None):
     c = None if counts is None else np.ascontiguousarray(counts, np.int64)
     rc = lib.phs_generate_device_noalloc(
-        ps.h, E, E, x.shape[0], None if c is None else c.ctypes.data, x.data_ptr(),
-        out.p.data_ptr(), out.factor.data_ptr(), out.volume.data_ptr(), out.ok.data_ptr(),
-        torch.cuda.current_stream().cuda_stream)
+        ps.h, E, E if E2 is None else E2, x.shape[0], None if c is None else c.ctypes.data,
+        x.data_ptr(), out.p.data_ptr(), out.factor.data_ptr(), out.volume.data_ptr(),
+        out.ok.data_ptr(), torch.cuda.current_stream().cuda_stream)
     assert rc == 0, lib.phs_last_error().decode()
 
 
@@ -92,6 +92,56 @@ def test_noalloc_allocates_no_device_memory(torch):
     torch.cuda.synchronize()
     assert torch.cuda.mem_get_info()[0] == free0
     assert _same(outs[1], outs[0]) and _same(outs[2], outs[0])
+
+
+def test_noalloc_unequal_beams_match_set_beams(torch):
+    """E1 != E2: the call compiles the constants at sqrt(s) = 2 sqrt(E1 E2) and the lab boost
+    itself; two calls in a row equal set_beams(E1, E2) + phs_generate_device bit for bit."""
+    from gpu_phs_gb300 import _lib
+    from gpu_phs_gb300.api import PhaseSpace
+    lib = _lib.load()
+    for proc, n in ((P.tt(), 100_003), (P.ww(), 40_000)):
+        x = torch.from_numpy(uniform_x(33, n, proc.n_x)).cuda()
+        ref = PhaseSpace(proc, 600.0, 400.0).generate(x)
+        ps = PhaseSpace(proc)
+        for rep in range(2):
+            out = ps.alloc(n)
+            _noalloc(lib, ps, 600.0, x, None, out, torch, E2=400.0)
+            torch.cuda.synchronize()
+            assert _same(out, ref), f"{proc.name}: call {rep + 1} differs from phs_generate_device"
+        # the lab boost moved the momenta: the unboosted run differs
+        sym = PhaseSpace(proc, 500.0, 500.0).generate(x)
+        assert not torch.equal(sym.p, ref.p)
+
+
+def test_noalloc_refuses_a_capturing_stream(torch):
+    """Its uploads read host memory that is gone when the call returns, so a call on a
+    stream under capture is refused before it enqueues anything; the next plain call works."""
+    from gpu_phs_gb300 import _lib
+    from gpu_phs_gb300.api import PhaseSpace
+    lib = _lib.load()
+    proc = P.tt()
+    n = 4096
+    x = torch.from_numpy(uniform_x(34, n, proc.n_x)).cuda()
+    ps = PhaseSpace(proc)
+    out = ps.alloc(n)
+    _noalloc(lib, ps, 500.0, x, None, out, torch)      # set-up outside capture
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    rc = None
+    with torch.cuda.graph(g, stream=s):
+        rc = lib.phs_generate_device_noalloc(
+            ps.h, 500.0, 500.0, n, None, x.data_ptr(), out.p.data_ptr(), out.factor.data_ptr(),
+            out.volume.data_ptr(), out.ok.data_ptr(), s.cuda_stream)
+        msg = lib.phs_last_error().decode()
+    assert rc == PHS_ERR_UNSUPPORTED
+    assert "captured" in msg
+    del g
+    again = ps.alloc(n)
+    _noalloc(lib, ps, 500.0, x, None, again, torch)
+    torch.cuda.synchronize()
+    assert _same(again, out)
 
 
 def test_noalloc_rejects_more_channels_than_its_scratch_holds(torch):
