@@ -370,7 +370,11 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64, pin=
     del flat, xh
     del bufs, xb, spaces
 
-    # adjoint: forward + reverse on 1e6 tt events with random cotangents
+    # adjoint: forward + reverse on 1e6 tt events with random cotangents, in the recompute
+    # form (parent frames recovered with inverse boosts) and the stored-matrix form (every
+    # visit's parent frame written to a device buffer and read back, as the reference keeps
+    # its boost chain in device memory)
+    from gpu_phs_gb300.api import ADJOINT_RECOMPUTE, ADJOINT_STORED
     proc = P.tt()
     n = 1_000_000
     ps = PhaseSpace(proc, proc.sqrts / 2, proc.sqrts / 2)
@@ -381,19 +385,45 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64, pin=
     jbar = torch.randn(n, dtype=torch.float64, device="cuda", generator=g)
     o = ps.alloc(n)
     t_fwd = _time_calls(torch, lambda: ps.generate(x, out=o), steps, warmup, stream)
-    torch.cuda.reset_peak_memory_stats()
-    base = torch.cuda.memory_allocated()
-    t_adj = _time_calls(torch, lambda: ps.vjp(x, pbar, jbar), steps, warmup, stream)
-    n_internal = proc.n_out - 1
+    in_bytes = (x.numel() + pbar.numel() + jbar.numel()) * 8
+
+    def adjoint_memory(storage):
+        """Device bytes of one vjp call in this storage form: the inputs, what torch
+        allocates for the outputs (peak allocated during the call), and what the library
+        holds after the call (cudaMemGetInfo minus torch's reserved growth)."""
+        ps.set_adjoint_storage(ADJOINT_RECOMPUTE)       # releases a stored-matrix buffer
+        ps.set_adjoint_storage(storage)
+        torch.cuda.synchronize()
+        free0, res0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_reserved()
+        torch.cuda.reset_peak_memory_stats()
+        alloc0 = torch.cuda.memory_allocated()
+        xb, tb = ps.vjp(x, pbar, jbar)
+        torch.cuda.synchronize()
+        lib_held = (free0 - torch.cuda.mem_get_info()[0]) - (torch.cuda.memory_reserved() - res0)
+        out_peak = torch.cuda.max_memory_allocated() - alloc0
+        del xb, tb
+        return {"inputs_bytes_per_event": in_bytes / n, "outputs_bytes_per_event": out_peak / n,
+                "library_scratch_bytes_per_event": lib_held / n,
+                "peak_device_bytes_per_event": (in_bytes + out_peak + lib_held) / n}
+
+    forms = {}
+    for name, storage in (("recompute", ADJOINT_RECOMPUTE), ("stored_matrix", ADJOINT_STORED)):
+        mem = adjoint_memory(storage)
+        t_adj = _time_calls(torch, lambda: ps.vjp(x, pbar, jbar), steps, warmup, stream)
+        forms[name] = {"adjoint_ms": t_adj, "adjoint_over_forward": t_adj / t_fwd,
+                       "fwd_plus_bwd_events_per_s": n / (t_fwd + t_adj) * 1e3, **mem}
+    ps.set_adjoint_storage(ADJOINT_RECOMPUTE)
+    rc = forms["recompute"]
     res["adjoint_tt"] = {
-        "n_events": n, "n_x": proc.n_x,
-        "forward_ms": t_fwd, "adjoint_ms": t_adj, "adjoint_over_forward": t_adj / t_fwd,
-        "fwd_plus_bwd_events_per_s": n / (t_fwd + t_adj) * 1e3,
+        "n_events": n, "n_x": proc.n_x, "forward_ms": t_fwd,
+        "adjoint_ms": rc["adjoint_ms"], "adjoint_over_forward": rc["adjoint_over_forward"],
+        "fwd_plus_bwd_events_per_s": rc["fwd_plus_bwd_events_per_s"],
         "outputs": "d(momenta, log factor)/dx and d/d(m, Gamma) of every Breit-Wigner branch",
-        "peak_hbm_bytes_per_event": (torch.cuda.max_memory_allocated() - base) / n,
-        "output_bytes_per_event": 8 * proc.n_x + 16 * (proc.n_out - 2),
-        "stored_matrix_checkpoint_bytes_per_event": 16 * 8 * n_internal,
-        "scratch": "per-visit state in shared memory; the boost chain is recomputed in reverse"}
+        "forms": forms,
+        "memory": "measured per call: inputs + torch's peak allocation for the outputs + the "
+                  "library's device buffer (cudaMemGetInfo change net of torch's reserve)",
+        "default": "recompute: parent frames recovered with inverse boosts, per-visit state in "
+                   "shared memory, no device scratch"}
     del x, pbar, jbar, o
 
     # inverse map: Whizard's bwbw process (61 channels, 16 with friend boosts), every

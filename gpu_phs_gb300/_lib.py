@@ -26,6 +26,7 @@ _SIGS = {
     "phs_process_set_beams": (I, [P, D, D]),
     "phs_process_info": (I, [P, P, P, P, P, P]),
     "phs_process_set_precision": (I, [P, I]),
+    "phs_process_set_adjoint_storage": (I, [P, I]),
     "phs_process_tuning": (I, [P, P, P]),
     "phs_process_set_variants": (I, [P, I, I]),
     "phs_batch_tuning": (I, [P, P, P]),

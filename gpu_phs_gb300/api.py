@@ -40,6 +40,8 @@ class Events:
 
 PRECISION_F64 = 0     # IEEE FP64 throughout
 PRECISION_F32X2 = 1   # float-float pairs on the FP32 pipe, FP64 next to kinematic limits
+ADJOINT_RECOMPUTE = 0  # vjp recovers parent frames with inverse boosts (no scratch)
+ADJOINT_STORED = 1     # vjp keeps every visit's parent frame in a device buffer
 
 
 class PhaseSpace:
@@ -66,6 +68,11 @@ class PhaseSpace:
     def set_precision(self, precision: int) -> None:
         """PRECISION_F64 (default) or PRECISION_F32X2 for the uniform-beam generate calls."""
         check(load().phs_process_set_precision(self.h, int(precision)))
+
+    def set_adjoint_storage(self, storage: int) -> None:
+        """ADJOINT_RECOMPUTE (default) or ADJOINT_STORED for vjp (the stored-matrix form,
+        kept for comparison: a device buffer of n x max visits x 128 bytes)."""
+        check(load().phs_process_set_adjoint_storage(self.h, int(storage)))
 
     def tuning(self):
         """(ff_variant, f64_variant) the autotuner chose (-1: not tuned yet)."""

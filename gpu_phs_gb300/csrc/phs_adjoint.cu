@@ -16,6 +16,13 @@
 // frame; the forward pass keeps that axis per visit, and the reverse walk rebuilds the
 // rotation and differentiates it (a forward-mode evaluation with three tangents).
 // Uniform beams only.  Events with ok = 0 get zero derivatives.
+//
+// STORED instantiations are the stored-matrix form for comparison: the forward pass writes
+// every visit's parent frame (16 doubles per visit and event) to a device buffer, as the
+// reference keeps its per-event boost chain in device memory (Ld, 16 N_BOOSTS doubles per
+// event, phs.cu:1421-1422), and the reverse walk reads the parent frames back instead of
+// recovering them with the inverse boost.  Same derivatives up to rounding; it costs the
+// buffer (n_events x max_visits x 128 bytes) and its HBM traffic.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -178,13 +185,14 @@ __device__ __forceinline__ void ct_derivs(int ct_class, double x, double b0, dou
 }
 
 // FRIENDS: the process has friend visits (a separate instantiation keeps their code out of
-// the register allocation of the others).
-template <bool FRIENDS>
+// the register allocation of the others).  STORED: the stored-matrix form (above); store
+// holds frame slot (v * 16 + i) of event ev at store[(v * 16 + i) * store_events + ev].
+template <bool FRIENDS, bool STORED>
 __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
     phs_adjoint_kernel(const __grid_constant__ PhsLaunch a, const PhsAdjChannel *__restrict__ adj,
                        const double *__restrict__ pbar, const double *__restrict__ jbar,
                        double *__restrict__ xbar, double *__restrict__ thbar, int th_stride,
-                       AdjLayout lay) {
+                       AdjLayout lay, double *__restrict__ store, int64_t store_events) {
   extern __shared__ double sm[];
   const int lane = threadIdx.x & 31;
   const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -233,6 +241,10 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
     int sp = 0, np = 0;
     for (int v = 0; v < n_visits; v++) {
       const PhsVisit &V = ch.visit[v];
+      if (STORED) {
+#pragma unroll
+        for (int i = 0; i < 16; i++) store[(int64_t)(v * 16 + i) * store_events + ev] = L[i];
+      }
       slot(sm, lay.state0 + PHS_ADJ_STATE * v + 0) = msq_b;
       slot(sm, lay.state0 + PHS_ADJ_STATE * v + 1) = m_b;
       slot(sm, lay.state0 + PHS_ADJ_STATE * v + 2) = p_b;
@@ -467,10 +479,10 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
 #pragma unroll
             for (int k = 0; k < 4; k++) {
               if ((c == 1 || c == 2) && k == 0) continue;  // F's zeros
-              acc += L[4 * r + k] * (eta[k] * eta[c]) * F[4 * c + k];
+              if (!STORED) acc += L[4 * r + k] * (eta[k] * eta[c]) * F[4 * c + k];
               accb += Lb[4 * r + k] * F[4 * c + k];
             }
-            Lp[4 * r + c] = acc;
+            Lp[4 * r + c] = STORED ? store[(int64_t)(v * 16 + 4 * r + c) * store_events + ev] : acc;
             Lpb[4 * r + c] = accb;
           }
         double Fb[16];
@@ -541,10 +553,10 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
             for (int k = 0; k < 4; k++) {
               if ((c == 0 && k == 2) || (c == 1 && k == 0) || (c == 2 && k == 0) || (c == 3 && k == 2))
                 continue;
-              acc += L[4 * r + k] * (eta[k] * eta[c]) * L1[4 * c + k];
+              if (!STORED) acc += L[4 * r + k] * (eta[k] * eta[c]) * L1[4 * c + k];
               accb += Lb[4 * r + k] * L1[4 * c + k];
             }
-            Lp[4 * r + c] = acc;
+            Lp[4 * r + c] = STORED ? store[(int64_t)(v * 16 + 4 * r + c) * store_events + ev] : acc;
             Lpb[4 * r + c] = accb;
           }
 #pragma unroll
@@ -647,35 +659,51 @@ void phs_adjoint_sizes(int max_visits, int max_pops, int stack_depth, bool frien
   *smem = (size_t)slots * PHS_ADJ_BLOCK * sizeof(double);
 }
 
+template <bool FRIENDS, bool STORED>
+static const void *adjoint_kernel() {
+  return (const void *)phs_adjoint_kernel<FRIENDS, STORED>;
+}
+
+static const void *adjoint_kernel(bool friends, bool stored) {
+  if (stored) return friends ? adjoint_kernel<true, true>() : adjoint_kernel<false, true>();
+  return friends ? adjoint_kernel<true, false>() : adjoint_kernel<false, false>();
+}
+
 cudaError_t phs_launch_adjoint(const PhsLaunch &a, const PhsAdjChannel *adj, const double *pbar,
                                const double *jbar, double *xbar, double *thbar, int th_stride,
                                int max_visits, int max_pops, bool friends, int n_blocks,
-                               cudaStream_t stream) {
+                               cudaStream_t stream, double *store, int64_t store_events) {
   if (a.n_tiles <= 0) return cudaSuccess;
   AdjLayout lay;
   size_t smem;
   phs_adjoint_sizes(max_visits, max_pops, a.stack_depth, friends, &lay.state0, &lay.ang0,
                     &lay.der0, &lay.pop0, &lay.stack0, &lay.trig0, &lay.fr0, &smem);
-  const void *k = friends ? (const void *)phs_adjoint_kernel<true> : (const void *)phs_adjoint_kernel<false>;
+  const bool stored = store != nullptr;
+  const void *k = adjoint_kernel(friends, stored);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  if (friends)
-    phs_adjoint_kernel<true><<<n_blocks, PHS_ADJ_BLOCK, smem, stream>>>(a, adj, pbar, jbar, xbar,
-                                                                      thbar, th_stride, lay);
-  else
-    phs_adjoint_kernel<false><<<n_blocks, PHS_ADJ_BLOCK, smem, stream>>>(a, adj, pbar, jbar, xbar,
-                                                                       thbar, th_stride, lay);
+#define PHS_ADJ_LAUNCH(F, S)                                                                   \
+  phs_adjoint_kernel<F, S><<<n_blocks, PHS_ADJ_BLOCK, smem, stream>>>(a, adj, pbar, jbar, xbar, \
+                                                                     thbar, th_stride, lay,     \
+                                                                     store, store_events)
+  if (stored) {
+    if (friends) PHS_ADJ_LAUNCH(true, true); else PHS_ADJ_LAUNCH(false, true);
+  } else {
+    if (friends) PHS_ADJ_LAUNCH(true, false); else PHS_ADJ_LAUNCH(false, false);
+  }
+#undef PHS_ADJ_LAUNCH
   return cudaGetLastError();
 }
 
-int phs_adjoint_blocks_per_sm(int max_visits, int max_pops, int stack_depth, bool friends) {
+int phs_adjoint_blocks_per_sm(int max_visits, int max_pops, int stack_depth, bool friends,
+                              bool stored) {
   int s0, a0, d0, p0, k0, t0, f0;
   size_t smem;
   phs_adjoint_sizes(max_visits, max_pops, stack_depth, friends, &s0, &a0, &d0, &p0, &k0, &t0, &f0,
                     &smem);
-  const void *k = friends ? (const void *)phs_adjoint_kernel<true> : (const void *)phs_adjoint_kernel<false>;
+  const void *k = adjoint_kernel(friends, stored);
   if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int n = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, PHS_ADJ_BLOCK, smem);

@@ -355,6 +355,8 @@ struct phs_process {
   int stack_depth = 0, max_visits = 0, max_pops = 0;
   bool has_friends = false;
   DevBuf d_prog, d_prog_ff, d_prog_adj;
+  int adjoint_storage = PHS_ADJOINT_RECOMPUTE;
+  DevBuf d_adj_store;                 // stored-matrix adjoint: the parent frames per visit
   DevBuf d_ch_begin;                  // inverse map: first event per generating channel
   DevBuf d_inv_groups;                // inverse map: channels by tree shape, group starts,
                                       // mapping reuse masks
@@ -436,6 +438,7 @@ extern "C" int phs_process_destroy(phs_process_t h) {
     h->d_prog.release();
     h->d_prog_ff.release();
     h->d_prog_adj.release();
+    h->d_adj_store.release();
     h->d_ch_begin.release();
     h->d_inv_groups.release();
     h->segs.release();
@@ -773,13 +776,35 @@ extern "C" int phs_adjoint_device(phs_process_t h, int64_t n_events, const int64
     a.x = x;
     if ((rc = attach_segments(h->segs, a, (cudaStream_t)stream))) return rc;
     if (a.n_tiles == 0) return PHS_OK;
-    const int per_sm =
-        phs_adjoint_blocks_per_sm(h->max_visits, h->max_pops, h->stack_depth, h->has_friends);
+    const bool stored = h->adjoint_storage == PHS_ADJOINT_STORED;
+    double *store = nullptr;
+    if (stored) {
+      // the stored-matrix form: every visit's parent frame of every event
+      if ((rc = h->d_adj_store.reserve((size_t)n_events * h->max_visits * 16 * sizeof(double))))
+        return rc;
+      store = h->d_adj_store.as<double>();
+    }
+    const int per_sm = phs_adjoint_blocks_per_sm(h->max_visits, h->max_pops, h->stack_depth,
+                                                 h->has_friends, stored);
     const int64_t want = (a.n_tiles + PHS_ADJ_BLOCK_HOST / 32 - 1) / (PHS_ADJ_BLOCK_HOST / 32);
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sm_count(h->device) * per_sm));
     CUDA_TRY(phs_launch_adjoint(a, h->d_prog_adj.as<PhsAdjChannel>(), pbar, jbar, xbar, thbar,
                                 2 * std::max(1, h->p.n_out - 2), h->max_visits, h->max_pops,
-                                h->has_friends, grid, (cudaStream_t)stream));
+                                h->has_friends, grid, (cudaStream_t)stream, store, n_events));
+    return PHS_OK;
+  });
+}
+
+extern "C" int phs_process_set_adjoint_storage(phs_process_t h, int storage) {
+  return guarded([&]() -> int {
+    if (int rc = check_proc(h)) return rc;
+    if (storage != PHS_ADJOINT_RECOMPUTE && storage != PHS_ADJOINT_STORED)
+      return fail(PHS_ERR_INVALID_ARG, "unknown adjoint storage mode %d", storage);
+    h->adjoint_storage = storage;
+    if (storage == PHS_ADJOINT_RECOMPUTE) {
+      DeviceGuard g(h->device);
+      h->d_adj_store.release();
+    }
     return PHS_OK;
   });
 }

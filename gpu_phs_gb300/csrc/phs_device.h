@@ -126,11 +126,15 @@ cudaError_t phs_launch_forward_exact(const PhsLaunch &a, int n_blocks, cudaStrea
 
 // Reverse-mode derivatives (phs_adjoint.cu): xbar [event][x stride] and thbar
 // [event][th_stride] (d/dm, d/dGamma per Breit-Wigner branch, at 2 * its msq x index).
+// store == null: the recompute form (no scratch); else the stored-matrix form, with
+// store[max_visits * 16 * store_events] doubles (store_events >= the launch's events).
 cudaError_t phs_launch_adjoint(const PhsLaunch &a, const PhsAdjChannel *adj, const double *pbar,
                                const double *jbar, double *xbar, double *thbar, int th_stride,
                                int max_visits, int max_pops, bool friends, int n_blocks,
-                               cudaStream_t stream);
-int phs_adjoint_blocks_per_sm(int max_visits, int max_pops, int stack_depth, bool friends);
+                               cudaStream_t stream, double *store = nullptr,
+                               int64_t store_events = 0);
+int phs_adjoint_blocks_per_sm(int max_visits, int max_pops, int stack_depth, bool friends,
+                              bool stored = false);
 void phs_adjoint_sizes(int max_visits, int max_pops, int stack_depth, bool friends, int *state0,
                        int *ang0, int *der0, int *pop0, int *stack0, int *trig0, int *fr0,
                        size_t *smem);

@@ -161,6 +161,18 @@ int phs_adjoint_device(phs_process_t proc, int64_t n_events, const int64_t *chan
                        const double *x, const double *pbar, const double *jbar, double *xbar,
                        double *thbar, void *stream);
 
+/* How phs_adjoint_device gets each visit's parent frame in its reverse walk.
+ * PHS_ADJOINT_RECOMPUTE (default): recovered from the child's frame with the inverse
+ * rotation+boost; no device memory beyond the outputs.  PHS_ADJOINT_STORED: the
+ * stored-matrix form the reference's device path uses for its boost chain (Ld, 16 doubles
+ * per boost and event, phs.cu:1421-1422): the forward pass writes the frames to a device
+ * buffer the handle keeps (n_events x max visits x 128 bytes, grown as needed, released
+ * when the mode goes back to RECOMPUTE), the reverse walk reads them back.  Same derivatives
+ * up to rounding; kept for the memory and time comparison. */
+#define PHS_ADJOINT_RECOMPUTE 0
+#define PHS_ADJOINT_STORED 1
+int phs_process_set_adjoint_storage(phs_process_t proc, int storage);
+
 /* Inverse map on device pointers: for events grouped by generating channel
  * (channel_counts), with lab momenta p [n_events][n_out][4] (16-byte aligned), writes for
  * EVERY channel c the x row and factor that channel assigns to the same momenta:

@@ -87,6 +87,8 @@ class Oracle:
                                           _pd, _pd, _pd, _pu8, C.c_int]
             L.oracle_generate_beams.argtypes = [C.c_void_p, C.c_long, C.c_int, _pd, C.c_void_p,
                                                 _pd, _pd, _pd, _pd, _pd, _pu8, C.c_int]
+            L.oracle_generate_cond.argtypes = [C.c_void_p, C.c_long, C.c_int, _pd, C.c_void_p,
+                                               _pd, _pd, _pd, _pu8, _pd, C.c_int]
             L.oracle_set_friends.restype = C.c_int
             L.oracle_set_friends.argtypes = [C.c_void_p, _pi]
             L.oracle_inverse.restype = C.c_int
@@ -127,7 +129,9 @@ class Oracle:
 
     def generate(self, x: np.ndarray, channels: Optional[np.ndarray] = None,
                  threads: int = 0, E1: Optional[np.ndarray] = None,
-                 E2: Optional[np.ndarray] = None) -> Result:
+                 E2: Optional[np.ndarray] = None, condition: bool = False) -> Result:
+        """condition=True (uniform beams) also returns r.kappa, the per-event condition of
+        the Kallen functions (oracle_generate_cond in phs_oracle.c)."""
         x = np.ascontiguousarray(x, np.float64)
         n, n_x = x.shape
         r = Result(n, self.proc.n_out)
@@ -136,7 +140,13 @@ class Oracle:
             channels = np.ascontiguousarray(channels, np.int32)
             chp = channels.ctypes.data_as(C.c_void_p)
         threads = threads or os.cpu_count() or 1
-        if E1 is None:
+        if condition:
+            if E1 is not None:
+                raise ValueError("condition numbers are computed for uniform beams")
+            r.kappa = np.zeros(n)
+            self.lib().oracle_generate_cond(self.h, n, n_x, x.reshape(-1), chp, r.p.reshape(-1),
+                                            r.factor, r.volume, r.ok, r.kappa, threads)
+        elif E1 is None:
             self.lib().oracle_generate(self.h, n, n_x, x.reshape(-1), chp, r.p.reshape(-1),
                                        r.factor, r.volume, r.ok, threads)
         else:

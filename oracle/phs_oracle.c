@@ -264,6 +264,7 @@ typedef struct {
   double *p2, *p_decay; /* [code] */
   double (*p)[4];       /* [code][4] */
   int ok;
+  double kappa;         /* condition of the Kallen functions (see oracle_generate_cond) */
 } ev_t;
 
 /* Rotation taking the z axis onto the direction of (bx, by, bz) about the axis z x b
@@ -322,6 +323,15 @@ static void set_msq(ev_t *e, int code, double *factor, double *volume) {
   double m1 = sqrt(msq1), m2 = sqrt(msq2), m = sqrt(msq);
   double lda = (msq - msq1 - msq2) * (msq - msq1 - msq2) - 4 * msq1 * msq2;
   if (lda > 0 && m > m1 + m2 && m <= m_max) {
+    {
+      /* relative change of lda per relative change of msq, msq1, msq2 (summed): how much
+       * the branch amplifies one-ulp differences of the mapped masses (it diverges at
+       * threshold, where lda -> 0); kept apart from every value the restatement returns */
+      const double d = msq - msq1 - msq2;
+      const double k = (fabs(2 * d) * msq + fabs(2 * d + 4 * msq2) * msq1 +
+                        fabs(2 * d + 4 * msq1) * msq2) / lda;
+      if (k > e->kappa) e->kappa = k;
+    }
     e->p_decay[k1] = sqrt(lda) / (2 * m);
     e->p_decay[k2] = -e->p_decay[k1];
     *factor *= sqrt(lda) / msq;
@@ -481,6 +491,7 @@ typedef struct {
   const double *E1, *E2; /* NULL: uniform beams at o->sqrts, constants precomputed */
   double *p, *factors, *volumes;
   unsigned char *oks;
+  double *kappa; /* optional per-event output */
 } job_t;
 
 static void *run_job(void *arg) {
@@ -514,7 +525,7 @@ static void *run_job(void *arg) {
       e.b = o->b + (size_t)c * o->stride * 3;
     }
     e.m_tot = o->mass_sum[c * o->stride + nc];
-    e.p2 = p2; e.p_decay = pd; e.p = pp; e.ok = 1;
+    e.p2 = p2; e.p_decay = pd; e.p = pp; e.ok = 1; e.kappa = 0;
     /* phs_cpu.cpp:586-593 */
     memset(pd, 0, (nc + 1) * sizeof(double));
     memset(pp, 0, (nc + 1) * sizeof(double[4]));
@@ -547,6 +558,7 @@ static void *run_job(void *arg) {
       j->volumes[ev] = volume_rec(o, c, nc, e.sqrts);
       j->oks[ev] = 0;
     }
+    if (j->kappa) j->kappa[ev] = e.kappa;
   }
   free(p2); free(pd); free(pp); free(a_ev); free(b_ev);
   return NULL;
@@ -573,7 +585,21 @@ static int run_threads(job_t *base, long n_events, int n_threads) {
  * reference CPU path's semantics, phs_cpu.cpp:550-600).  channels may be NULL (all 0). */
 int oracle_generate(const oracle_t *o, long n_events, int n_x, const double *x, const int *channels,
                     double *p, double *factors, double *volumes, unsigned char *oks, int n_threads) {
-  job_t j = {o, 0, 0, n_x, x, channels, NULL, NULL, p, factors, volumes, oks};
+  job_t j = {o, 0, 0, n_x, x, channels, NULL, NULL, p, factors, volumes, oks, NULL};
+  return run_threads(&j, n_events, n_threads);
+}
+
+/* As oracle_generate, and per event kappa[ev] = the largest, over the branches whose
+ * kinematic test passed, of sum_q |d lda / d q| q / lda (q = msq of the branch and of its
+ * two daughters, lda the Kallen function): the relative change of sqrt(lda), and so of the
+ * factor, is kappa / 2 times a relative change of the masses.  A one-ulp difference of a
+ * transcendental function (tan, exp, log) between two libraries moves a mapped mass by
+ * about one ulp, so two correct FP64 implementations can disagree on the factor by a few
+ * ulps times kappa.  0 for events that fail the test before any branch passes. */
+int oracle_generate_cond(const oracle_t *o, long n_events, int n_x, const double *x,
+                         const int *channels, double *p, double *factors, double *volumes,
+                         unsigned char *oks, double *kappa, int n_threads) {
+  job_t j = {o, 0, 0, n_x, x, channels, NULL, NULL, p, factors, volumes, oks, kappa};
   return run_threads(&j, n_events, n_threads);
 }
 
@@ -583,7 +609,7 @@ int oracle_generate(const oracle_t *o, long n_events, int n_x, const double *x, 
 int oracle_generate_beams(const oracle_t *o, long n_events, int n_x, const double *x,
                           const int *channels, const double *E1, const double *E2, double *p,
                           double *factors, double *volumes, unsigned char *oks, int n_threads) {
-  job_t j = {o, 0, 0, n_x, x, channels, E1, E2, p, factors, volumes, oks};
+  job_t j = {o, 0, 0, n_x, x, channels, E1, E2, p, factors, volumes, oks, NULL};
   return run_threads(&j, n_events, n_threads);
 }
 

@@ -1,5 +1,19 @@
 """The adjoint kernel against FP64 central finite differences (h = 1e-6) of the forward
-kernel, on the tt tree, excluding events within 1e-4 of a kinematic limit."""
+kernel, on the tt tree, Whizard's friend channels and the 12-particle trees.
+
+Every kept derivative is checked against a bound, not a quantile:
+
+    |adjoint - FD(h)| <= 1e-7 * scale + 2 |FD(h) - FD(2h)| + 4e-15 * |loss| / h
+
+scale: the event's largest derivative + 1 (x), or |FD| + its mean over the events
+(mapping parameters).  FD(2h) - FD(h) is three times the h^2 truncation error of FD(h), so
+the second term bounds the difference quotient's own error where the map curves strongly
+(Breit-Wigner tails near +-pi/2); the third is the rounding of two loss evaluations
+divided by 2h.  Events are excluded only by stated criteria: ok = 0, within 1e-4 of a
+kinematic limit (relative margin of a mass to its threshold or upper bound), an ok flag
+that changes at x +- h or x +- 2h, an x within 2h of 0 or 1, or within 2h of 0.5 (where
+the two-sided exponential maps switch branches and the derivative jumps).
+"""
 import numpy as np
 import pytest
 
@@ -48,11 +62,69 @@ def margins(p, proc):
     return out
 
 
+TOL = 1e-7        # relative to the event's derivative scale
+ROUND = 4e-15     # relative rounding of one loss evaluation (FP64 forward map and the sum)
+
+
 def loss(torch, ps, x, pbar, jbar):
+    """sum pbar . p + jbar log(factor) per event, its ok flag and its magnitude
+    sum |pbar| |p| + |jbar log(factor)| (the scale of its rounding error)."""
     ev = ps.generate(x)
     ok = ev.ok.bool()
     lj = torch.where(ok, torch.log(torch.where(ok, ev.factor, torch.ones_like(ev.factor))), 0.0)
-    return (pbar * ev.p).sum(dim=(1, 2)) + jbar * lj, ok
+    mag = (pbar.abs() * ev.p.abs()).sum(dim=(1, 2)) + (jbar * lj).abs()
+    return (pbar * ev.p).sum(dim=(1, 2)) + jbar * lj, ok, mag
+
+
+def x_finite_differences(torch, ps, x, pbar, jbar, h):
+    """Central differences of the loss in every x at steps h and 2h, whether the event is
+    ok at all of x +- h, x +- 2h, and the largest loss magnitude seen."""
+    fd1, fd2 = torch.zeros_like(x), torch.zeros_like(x)
+    ok_all = torch.ones(x.shape[0], dtype=torch.bool, device=x.device)
+    mag = torch.zeros(x.shape[0], dtype=torch.float64, device=x.device)
+    for k in range(x.shape[1]):
+        val = {}
+        for m in (1, -1, 2, -2):
+            xs = x.clone()
+            xs[:, k] += m * h
+            val[m], ok, mg = loss(torch, ps, xs, pbar, jbar)
+            ok_all &= ok
+            mag = torch.maximum(mag, mg)
+        fd1[:, k] = (val[1] - val[-1]) / (2 * h)
+        fd2[:, k] = (val[2] - val[-2]) / (4 * h)
+    return fd1, fd2, ok_all, mag
+
+
+def x_keep(torch, ev, x, proc, h):
+    """The stated exclusions that need no finite differences: ok = 0, within 1e-4 of a
+    kinematic limit, an x within 2h of 0, 1 or 0.5."""
+    keep = ev.ok.bool().cpu().numpy() & (margins(ev.p.cpu().numpy(), proc) > 1e-4)
+    keep &= ((x > 2 * h) & (x < 1 - 2 * h)).all(dim=1).cpu().numpy()
+    keep &= ((x - 0.5).abs() > 2 * h).all(dim=1).cpu().numpy()
+    return keep
+
+
+def assert_bound(a, fd1, fd2, mag, h, scale, what):
+    """|a - fd1| <= TOL scale + 2 |fd1 - fd2| + ROUND mag / h, element by element."""
+    bound = TOL * scale + 2 * np.abs(fd1 - fd2) + ROUND * mag / h
+    ratio = np.abs(a - fd1) / bound
+    q = np.quantile(np.abs(a - fd1) / scale, [0.5, 0.99, 1.0])
+    worst = ratio.max() if ratio.size else 0.0
+    print(f"{what}: {a.shape[0]} events, worst |adjoint - FD| / bound {worst:.3g}, "
+          f"|adjoint - FD| / scale median {q[0]:.2e} 99% {q[1]:.2e} max {q[2]:.2e}")
+    assert worst <= 1.0, (what, worst, np.unravel_index(np.argmax(ratio), ratio.shape))
+
+
+def check_x_derivatives(torch, ps, proc, x, pbar, jbar, h, min_kept, what):
+    xbar, _ = ps.vjp(x, pbar, jbar)
+    ev = ps.generate(x)
+    keep = x_keep(torch, ev, x, proc, h)
+    fd1, fd2, ok_all, mag = x_finite_differences(torch, ps, x, pbar, jbar, h)
+    keep &= ok_all.cpu().numpy()
+    assert keep.sum() > min_kept * x.shape[0], keep.sum()
+    a, b, b2 = (t.cpu().numpy()[keep] for t in (xbar, fd1, fd2))
+    scale = np.abs(b).max(axis=1, keepdims=True) + 1.0
+    assert_bound(a, b, b2, mag.cpu().numpy()[keep][:, None], h, scale, what)
 
 
 def test_adjoint_x_against_finite_differences(torch):
@@ -64,25 +136,7 @@ def test_adjoint_x_against_finite_differences(torch):
     g = torch.Generator(device="cuda").manual_seed(1)
     pbar = torch.randn((n, proc.n_out, 4), generator=g, device="cuda", dtype=torch.float64)
     jbar = torch.randn(n, generator=g, device="cuda", dtype=torch.float64)
-    xbar, _ = ps.vjp(x, pbar, jbar)
-    ev = ps.generate(x)
-    keep = ev.ok.bool().cpu().numpy() & (margins(ev.p.cpu().numpy(), proc) > 1e-4)
-    keep &= ((x > 2 * h) & (x < 1 - 2 * h)).all(dim=1).cpu().numpy()
-    fd = torch.zeros_like(x)
-    for k in range(proc.n_x):
-        xp, xm = x.clone(), x.clone()
-        xp[:, k] += h
-        xm[:, k] -= h
-        lp, okp = loss(torch, ps, xp, pbar, jbar)
-        lm, okm = loss(torch, ps, xm, pbar, jbar)
-        fd[:, k] = (lp - lm) / (2 * h)
-        keep &= (okp & okm).cpu().numpy()
-    a, b = xbar.cpu().numpy()[keep], fd.cpu().numpy()[keep]
-    scale = np.abs(b).max(axis=1, keepdims=True) + 1.0
-    rel = np.abs(a - b) / scale
-    assert keep.sum() > 0.9 * n
-    assert np.median(rel) < 1e-7
-    assert np.quantile(rel, 0.999) < 1e-4, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])
+    check_x_derivatives(torch, ps, proc, x, pbar, jbar, h, 0.9, "tt dx")
 
 
 def test_adjoint_parameters_against_finite_differences(torch):
@@ -106,27 +160,24 @@ def test_adjoint_parameters_against_finite_differences(torch):
         ad = sum(thbar[:, slot[c], col] for c in branch_codes)
         val = base.map_masses[0, branch_codes[0] - 1] if col == 0 else base.map_widths[0, branch_codes[0] - 1]
         h = 1e-6 * val
-        ls = []
-        oks = []
-        for sgn in (1, -1):
+        ls, k, mag = {}, keep.copy(), np.zeros(n)
+        for m in (1, -1, 2, -2):
             proc = base.subset([0])
-            arr = proc.map_masses if col == 0 else proc.map_widths
-            arr = arr.copy()
+            arr = (proc.map_masses if col == 0 else proc.map_widths).copy()
             for c in branch_codes:
-                arr[0, c - 1] += sgn * h
+                arr[0, c - 1] += m * h
             if col == 0:
                 proc.map_masses = arr
             else:
                 proc.map_widths = arr
-            l_, ok_ = loss(torch, PhaseSpace(proc, 500.0, 500.0), x, pbar, jbar)
-            ls.append(l_)
-            oks.append(ok_.cpu().numpy())
-        fd = ((ls[0] - ls[1]) / (2 * h)).cpu().numpy()
-        k = keep & oks[0] & oks[1]
-        a, b = ad.cpu().numpy()[k], fd[k]
-        rel = np.abs(a - b) / (np.abs(b) + np.abs(b).mean())
-        assert np.median(rel) < 1e-6, (name, np.quantile(rel, [0.5, 0.99, 1.0]))
-        assert np.quantile(rel, 0.99) < 1e-3, (name, np.quantile(rel, [0.5, 0.99, 1.0]))
+            ls[m], ok_, mg = loss(torch, PhaseSpace(proc, 500.0, 500.0), x, pbar, jbar)
+            k &= ok_.cpu().numpy()
+            mag = np.maximum(mag, mg.cpu().numpy())
+        fd1 = ((ls[1] - ls[-1]) / (2 * h)).cpu().numpy()[k]
+        fd2 = ((ls[2] - ls[-2]) / (4 * h)).cpu().numpy()[k]
+        a = ad.cpu().numpy()[k]
+        assert k.sum() > 0.9 * n
+        assert_bound(a, fd1, fd2, mag[k], h, np.abs(fd1) + np.abs(fd1).mean(), f"tt d/d{name}")
 
 
 def test_autograd_binding(torch):
@@ -165,25 +216,7 @@ def test_adjoint_friend_channels_against_finite_differences(torch, k):
     g = torch.Generator(device="cuda").manual_seed(10 + k)
     pbar = torch.randn((n, proc.n_out, 4), generator=g, device="cuda", dtype=torch.float64)
     jbar = torch.randn(n, generator=g, device="cuda", dtype=torch.float64)
-    xbar, _ = ps.vjp(x, pbar, jbar)
-    ev = ps.generate(x)
-    keep = ev.ok.bool().cpu().numpy() & (margins(ev.p.cpu().numpy(), proc) > 1e-4)
-    keep &= ((x > 2 * h) & (x < 1 - 2 * h)).all(dim=1).cpu().numpy()
-    fd = torch.zeros_like(x)
-    for i in range(proc.n_x):
-        xp, xm = x.clone(), x.clone()
-        xp[:, i] += h
-        xm[:, i] -= h
-        lp, okp = loss(torch, ps, xp, pbar, jbar)
-        lm, okm = loss(torch, ps, xm, pbar, jbar)
-        fd[:, i] = (lp - lm) / (2 * h)
-        keep &= (okp & okm).cpu().numpy()
-    a, b = xbar.cpu().numpy()[keep], fd.cpu().numpy()[keep]
-    scale = np.abs(b).max(axis=1, keepdims=True) + 1.0
-    rel = np.abs(a - b) / scale
-    assert keep.sum() > 0.3 * n
-    assert np.median(rel) < 1e-7, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])
-    assert np.quantile(rel, 0.99) < 1e-4, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])
+    check_x_derivatives(torch, ps, proc, x, pbar, jbar, h, 0.3, f"bwbw friend channel {k} dx")
 
 
 @pytest.mark.parametrize("channel", [0, 1])
@@ -198,22 +231,35 @@ def test_adjoint_largest_trees_against_finite_differences(torch, channel):
     g = torch.Generator(device="cuda").manual_seed(20 + channel)
     pbar = torch.randn((n, proc.n_out, 4), generator=g, device="cuda", dtype=torch.float64)
     jbar = torch.randn(n, generator=g, device="cuda", dtype=torch.float64)
-    xbar, _ = ps.vjp(x, pbar, jbar)
-    ev = ps.generate(x)
-    keep = ev.ok.bool().cpu().numpy() & (margins(ev.p.cpu().numpy(), proc) > 1e-4)
-    keep &= ((x > 2 * h) & (x < 1 - 2 * h)).all(dim=1).cpu().numpy()
-    fd = torch.zeros_like(x)
-    for i in range(proc.n_x):
-        xp, xm = x.clone(), x.clone()
-        xp[:, i] += h
-        xm[:, i] -= h
-        lp, okp = loss(torch, ps, xp, pbar, jbar)
-        lm, okm = loss(torch, ps, xm, pbar, jbar)
-        fd[:, i] = (lp - lm) / (2 * h)
-        keep &= (okp & okm).cpu().numpy()
-    a, b = xbar.cpu().numpy()[keep], fd.cpu().numpy()[keep]
-    scale = np.abs(b).max(axis=1, keepdims=True) + 1.0
-    rel = np.abs(a - b) / scale
-    assert keep.sum() > 0.05 * n
-    assert np.median(rel) < 1e-7, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])
-    assert np.quantile(rel, 0.99) < 1e-4, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])
+    check_x_derivatives(torch, ps, proc, x, pbar, jbar, h, 0.05, f"12-particle tree {channel} dx")
+
+
+def test_stored_matrix_form_against_finite_differences_and_recompute(torch):
+    """The stored-matrix adjoint (every visit's parent frame kept in a device buffer, read
+    back in the reverse walk) on the tt tree: within the finite-difference bound above, close
+    to the recompute form, and holding n x max visits x 128 bytes of device memory exactly
+    while it is selected."""
+    from gpu_phs_gb300.api import ADJOINT_RECOMPUTE, ADJOINT_STORED, PhaseSpace
+    proc = P.tt()
+    n, h = 10_000, 1e-6
+    x = torch.from_numpy(uniform_x(407, n, proc.n_x)).cuda()
+    ps = PhaseSpace(proc, 500.0, 500.0)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    pbar = torch.randn((n, proc.n_out, 4), generator=g, device="cuda", dtype=torch.float64)
+    jbar = torch.randn(n, generator=g, device="cuda", dtype=torch.float64)
+    xr, tr = ps.vjp(x, pbar, jbar)
+    ps.set_adjoint_storage(ADJOINT_STORED)
+    xs, ts = ps.vjp(x, pbar, jbar)
+    torch.cuda.synchronize()
+    scale = xr.abs().amax(dim=1, keepdim=True) + 1.0
+    assert ((xs - xr).abs() / scale).max().item() < 1e-9
+    assert ((ts - tr).abs() / (tr.abs().amax(dim=(1, 2), keepdim=True) + 1.0)).max().item() < 1e-9
+    # the buffer the handle holds: released on the switch back (nothing else allocates here)
+    free_a = torch.cuda.mem_get_info()[0]
+    ps.set_adjoint_storage(ADJOINT_RECOMPUTE)
+    torch.cuda.synchronize()
+    held = torch.cuda.mem_get_info()[0] - free_a
+    want = n * (proc.n_out - 1) * 16 * 8
+    assert want <= held <= want + (2 << 20), (held, want)   # cudaMalloc's 2 MiB pages
+    ps.set_adjoint_storage(ADJOINT_STORED)
+    check_x_derivatives(torch, ps, proc, x, pbar, jbar, h, 0.9, "tt dx, stored-matrix form")

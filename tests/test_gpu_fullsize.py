@@ -18,6 +18,14 @@ momenta and factor where ok = 0.  FP32 pairs -- ok flags bit-exact, momenta and 
 within 1e-7 (the float-float walk carries ~48 bits).  A failure lists the first
 mismatching events.
 
+One stated exception to the FP64 bar: CUDA's and glibc's tan/exp/log may differ by an ulp
+or two, which moves a mapped mass by about an ulp; next to a kinematic threshold the
+Kallen function amplifies that.  The oracle reports per event kappa, the relative change
+of sqrt(lambda) per relative change of the masses (times 2, the largest over the event's
+branches; oracle_generate_cond).  An event's FP64 momentum and factor tolerance is
+max(1e-12, 8 u kappa), u = 2^-53: 1e-12 unless kappa > 1100 (about 1 event in 10^4, all
+within ~1e-3 of a threshold).  Every event that uses the wider tolerance is printed.
+
 The comparison runs on the GPU (torch): the oracle's outputs are uploaded once per
 workload and each form's outputs are checked against them in place.
 """
@@ -53,13 +61,17 @@ def _threads():
 class Ref:
     """The oracle's outputs of one workload on the device (p flat in the GPU layout)."""
 
-    def __init__(self, torch, p, factor, volume, ok, sqrts):
+    def __init__(self, torch, p, factor, volume, ok, sqrts, kappa):
         dev = "cuda"
         self.p = torch.from_numpy(p).to(dev)
         self.factor = torch.from_numpy(factor).to(dev)
         self.volume = torch.from_numpy(volume).to(dev)
         self.ok = torch.from_numpy(ok).to(dev)
+        self.kappa = torch.from_numpy(kappa).to(dev)
         self.sqrts = sqrts
+
+
+U = 2.0 ** -53
 
 
 def compare(torch, ref: Ref, p, factor, volume, ok, n_out_rows, precision, label):
@@ -73,11 +85,20 @@ def compare(torch, ref: Ref, p, factor, volume, ok, n_out_rows, precision, label
         msg.append(f"{bad.numel()} ok-flag mismatches, first events {idx} "
                    f"(gpu {ok[bad[:10]].tolist()}, oracle {ref.ok[bad[:10]].tolist()})")
     sel = ref.ok.bool()
+    # per event tolerance: the FP64 bar widened by the Kallen condition (module docstring)
+    tol_ev = ref.kappa[sel] * (8 * U)
+    tol_ev = tol_ev.clamp(min=tol_f) if precision == 0 else torch.full_like(tol_ev, tol_f)
     # factors
     fr = (factor[sel] - ref.factor[sel]).abs() / ref.factor[sel].abs()
     fmax = fr.max().item() if fr.numel() else 0.0
-    if fmax > tol_f:
-        msg.append(f"factor error {fmax:.3e} > {tol_f:g}")
+    worst_f = (fr / tol_ev).max().item() if fr.numel() else 0.0
+    if worst_f > 1.0:
+        msg.append(f"factor error {fmax:.3e} > its tolerance ({worst_f:.2f} x)")
+    wide = torch.nonzero(fr > tol_f).flatten()
+    ev_sel = torch.nonzero(sel).flatten()
+    for i in wide[:20].tolist():
+        print(f"  {label}: event {ev_sel[i].item()} factor error {fr[i].item():.2e}, "
+              f"kappa {ref.kappa[sel][i].item():.3g}, tolerance {tol_ev[i].item():.2e}")
     # volumes (every event)
     vr = ((volume - ref.volume).abs() / ref.volume.abs()).max().item()
     if vr > 1e-15 and precision == 0:
@@ -89,15 +110,21 @@ def compare(torch, ref: Ref, p, factor, volume, ok, n_out_rows, precision, label
     d = (P4[rows_ok] - R4[rows_ok]).abs().amax(-1)
     rel = d / R4[rows_ok][:, 0].abs().clamp(min=1e-3 * ref.sqrts)
     pmax = rel.max().item() if rel.numel() else 0.0
+    tol_row = torch.repeat_interleave(tol_ev.clamp(min=tol_p) if precision == 0
+                                      else torch.full_like(tol_ev, tol_p), n_out_rows[sel])
+    worst_p = (rel / tol_row).max().item() if rel.numel() else 0.0
+    if worst_p > 1.0:
+        msg.append(f"momentum error {pmax:.3e} > its tolerance ({worst_p:.2f} x)")
     if pmax > tol_p:
-        msg.append(f"momentum error {pmax:.3e} > {tol_p:g}")
+        print(f"  {label}: {int((rel > tol_p).sum().item())} particle rows above {tol_p:g} "
+              f"within their kappa tolerance")
     zero_p = bool((P4[~rows_ok] == 0).all().item())
     zero_f = bool((factor[~sel] == 0).all().item())
     if not (zero_p and zero_f):
         msg.append("ok = 0 events with non-zero momenta or factor")
     print(f"{label}: {int(ok.numel())} events, ok {sel.float().mean().item():.4f}, "
           f"ok mismatches {bad.numel()}, max momentum {pmax:.2e}, factor {fmax:.2e}, "
-          f"volume {vr:.2e}")
+          f"volume {vr:.2e}, events above {tol_f:g} (kappa tolerance) {wide.numel()}")
     assert not msg, f"{label}: " + "; ".join(msg)
 
 
@@ -106,8 +133,8 @@ def _single(torch, builder, n):
     proc = builder()
     x = philox_x(n, proc.n_x, SEED)
     xh = x.cpu().numpy()
-    r = oracle.Oracle(proc, proc.sqrts).generate(xh, threads=_threads())
-    ref = Ref(torch, r.p.reshape(-1), r.factor, r.volume, r.ok, proc.sqrts)
+    r = oracle.Oracle(proc, proc.sqrts).generate(xh, threads=_threads(), condition=True)
+    ref = Ref(torch, r.p.reshape(-1), r.factor, r.volume, r.ok, proc.sqrts, r.kappa)
     del r, xh
     rows = torch.full((n,), proc.n_out, dtype=torch.int64, device="cuda")
     for label, prec, variants in F64_FORMS + FF_FORMS:
@@ -147,18 +174,19 @@ def test_batched_64ch_2p24_every_form(torch):
     philox_fill(xb, int(xo[-1]), 1, SEED)
     xh = xb.cpu().numpy()
     rp = np.zeros(int(po[-1]))
-    rf, rv = np.zeros(n), np.zeros(n)
+    rf, rv, rk = np.zeros(n), np.zeros(n), np.zeros(n)
     rok = np.zeros(n, np.uint8)
     e = 0
     for i, (proc, c) in enumerate(zip(procs, counts)):
         c = int(c)
         if c:
             r = oracle.Oracle(proc, 1000.0).generate(xh[xo[i]:xo[i + 1]].reshape(c, proc.n_x),
-                                                     threads=_threads())
+                                                     threads=_threads(), condition=True)
             rp[po[i]:po[i + 1]] = r.p.reshape(-1)
             rf[e:e + c], rv[e:e + c], rok[e:e + c] = r.factor, r.volume, r.ok
+            rk[e:e + c] = r.kappa
         e += c
-    ref = Ref(torch, rp, rf, rv, rok, 1000.0)
+    ref = Ref(torch, rp, rf, rv, rok, 1000.0, rk)
     del rp, xh
     rows = torch.from_numpy(np.repeat([p.n_out for p in procs], counts)).to("cuda")
     for label, prec, variants in F64_FORMS + FF_FORMS:

@@ -158,3 +158,18 @@ def test_oracle_philox_matches_numpy_stream():
                             (50_001, 16, 3, 2**40 + 5), (0, 8, 0, 1)]:
         a = oracle.uniform_x(seed, n, nx, e0, threads=4)
         assert np.array_equal(a, uniform_x(seed, n, nx, first_event=e0)), (n, nx, e0)
+
+
+def test_oracle_condition_output_leaves_results_unchanged():
+    """generate(condition=True) returns the same bits plus the Kallen condition kappa:
+    >= 1 for every ok event of the tt tree (each branch has a sum of three terms over lda,
+    one of them >= lda), and largest for the events closest to a threshold."""
+    proc = P.tt()
+    x = uniform_x(77, 20_000, proc.n_x)
+    o = oracle.Oracle(proc, proc.sqrts)
+    a, b = o.generate(x), o.generate(x, condition=True)
+    for f in ("p", "factor", "volume", "ok"):
+        assert np.array_equal(getattr(a, f), getattr(b, f))
+    k = b.kappa[b.ok == 1]
+    assert (k >= 1.0).all() and np.isfinite(k).all()
+    assert (b.kappa[b.ok == 0] >= 0).all()
