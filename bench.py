@@ -818,7 +818,7 @@ def run_ours(args):
 
 
 PROFILE_CASES = ("f64_tt", "ff_tt", "f64_batched", "f64_split_batched", "ff_batched", "inverse_bwbw",
-                 "adjoint_tt")
+                 "adjoint_tt", "adjoint_tt_stored")
 
 
 def run_case(name: str) -> None:
@@ -867,10 +867,13 @@ def run_case(name: str) -> None:
         ev = ps.generate(x, counts)
         for _ in range(2):
             ps.inverse(ev.p, counts, ev.ok, x, ev.factor)
-    elif name == "adjoint_tt":        # 2^20 tt events
+    elif name in ("adjoint_tt", "adjoint_tt_stored"):   # 2^20 tt events, recompute / stored
+        from gpu_phs_gb300.api import ADJOINT_STORED
         proc = P.tt()
         n = 1 << 20
         ps = PhaseSpace(proc, 500.0, 500.0)
+        if name == "adjoint_tt_stored":
+            ps.set_adjoint_storage(ADJOINT_STORED)
         x = philox_x(n, proc.n_x, SEED)
         g = torch.Generator(device="cuda").manual_seed(SEED)
         pbar = torch.randn((n, proc.n_out, 4), dtype=torch.float64, device="cuda", generator=g)

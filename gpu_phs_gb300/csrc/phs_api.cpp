@@ -893,10 +893,11 @@ static int inverse_launch(phs_process_t h, int64_t n_events, const int64_t *d_ch
   a.order_lo = order_lo;
   a.order_hi = order_hi < 0 ? nch : order_hi;
   a.write_fixed = write_fixed ? 1 : 0;
+  a.lab = h->prog.empty() ? 0 : h->prog[0].lab;
   const int64_t tiles = (n_events + PHS_INV_BLOCK - 1) / PHS_INV_BLOCK;
   const int64_t cap = (int64_t)sm_count(h->device) *
                       phs_inverse_blocks_per_sm(a.n_out, a.stack_depth, a.max_visits,
-                                                E1 != nullptr, cache);
+                                                E1 != nullptr, cache, !a.lab);
   CUDA_TRY(phs_launch_inverse(a, (int)std::max<int64_t>(1, std::min(tiles, cap)), st));
   return PHS_OK;
 }

@@ -171,13 +171,17 @@ struct PhsInvLaunch {
   int64_t x_ch_stride;         // rows per channel in x_out (n_events, or more for a launch
                                // over a range of the events of a longer array)
   int32_t n_channels, n_out, n_x, stack_depth, max_visits;
+  int32_t lab;                 // uniform beams: 1 when E1 != E2 (the programs' lab boost)
 };
 cudaError_t phs_launch_inverse(const PhsInvLaunch &a, int n_blocks, cudaStream_t stream);
 // cache: the per-visit mapping results that channels of a shape reuse (a.group_reuse set);
-// phs_inverse_fits_cache tells whether the block's shared memory holds them.
+// phs_inverse_fits_cache tells whether the block's shared memory holds them.  lab_rows:
+// uniform beams without a lab boost, where the kernel reads the outgoing momenta from p
+// instead of staging them in shared memory (4 n_out doubles less per thread).
 int phs_inverse_blocks_per_sm(int n_out, int stack_depth, int max_visits, bool per_event,
-                              bool cache);
-size_t phs_inverse_smem_bytes(int n_out, int stack_depth, int max_visits, bool cache);
+                              bool cache, bool lab_rows);
+size_t phs_inverse_smem_bytes(int n_out, int stack_depth, int max_visits, bool cache,
+                              bool lab_rows);
 bool phs_inverse_fits_cache(int n_out, int stack_depth, int max_visits);
 
 // Per-channel x grid of the warm-up (phs_grid.cu): weights [n_channels][n_x][PHS_GRID_BINS].

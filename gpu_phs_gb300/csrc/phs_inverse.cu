@@ -117,25 +117,42 @@ __device__ __forceinline__ double inv_load(const double *stk, int depth, int k) 
   return stk[(depth * PHS_INV_STATE + k) * PHS_INV_BLOCK + threadIdx.x];
 }
 
+// Momentum slots of one thread's event: slot j < n_out is outgoing particle j, slot
+// n_out + i the i-th internal branch in post-order.  Internal sums sit in shared memory at
+// pm[(4 (j - n_out) + mu) PHS_INV_BLOCK].  The outgoing momenta are either staged in shared
+// memory below them (pm[(4 j + mu) PHS_INV_BLOCK], the CM momenta after the inverse lab
+// boost) or, where there is no lab boost (CM = lab, the same bits), read from the event's
+// row of p through the L1 (lab != null): that leaves 4 n_out doubles per thread of shared
+// memory free for more resident blocks.
+struct InvMomenta {
+  double *pm;          // internal sums (and, lab == null, the staged outgoing momenta first)
+  const double *lab;   // the event's p row, or null
+  int n_out;
+  __device__ __forceinline__ double get(int j, int mu) const {
+    if (lab) return j < n_out ? __ldg(lab + 4 * j + mu) : pm[(4 * (j - n_out) + mu) * PHS_INV_BLOCK];
+    return pm[(4 * j + mu) * PHS_INV_BLOCK];
+  }
+  __device__ __forceinline__ void set_internal(int j, int mu, double v) const {
+    pm[(4 * (lab ? j - n_out : j) + mu) * PHS_INV_BLOCK] = v;
+  }
+};
+
 // The geometry of one (event, channel shape): the walk of the visit program without the
 // mappings, leaving per visit in geo (slot (v PHS_INV_GEO + k) PHS_INV_BLOCK) what the
 // mappings of every channel of that shape need (inverse_maps).
-// pm: this thread's momentum slots, component (4 j + mu) at pm[(4 j + mu) * PHS_INV_BLOCK]:
-// the CM momenta in slots 0..n_out-1, the channel's internal branches after them.
 // The arithmetic keeps the reference's operation order (this file is compiled without
 // contraction): x(p) is ill-conditioned near the poles of each decay (cos(theta) -> +-1,
 // where 1 - cos^2 cancels) and for soft daughters of fast branches, and there any other
 // rounding order moves the result by far more than the input's own rounding does.
-__device__ void inverse_geometry(const PhsChannel &ch, double *pm, double sqrts, double *stk,
-                                 double *geo) {
+__device__ void inverse_geometry(const PhsChannel &ch, const InvMomenta &pm, double sqrts,
+                                 double *stk, double *geo) {
   const double s = sqrts * sqrts;
   // internal momenta as sums of their daughters in post-order (_combine_particles,
-  // phs.cu:1262-1283)
-  for (int i = 0; i < ch.n_vol; i++) {
+  // phs.cu:1262-1283); the root's (the last) is never a daughter
+  for (int i = 0; i + 1 < ch.n_vol; i++) {
     const int a = ch.comb[i][0], b = ch.comb[i][1], o = ch.n_out + i;
 #pragma unroll
-    for (int mu = 0; mu < 4; mu++)
-      pm[(4 * o + mu) * PHS_INV_BLOCK] = pm[(4 * a + mu) * PHS_INV_BLOCK] + pm[(4 * b + mu) * PHS_INV_BLOCK];
+    for (int mu = 0; mu < 4; mu++) pm.set_internal(o, mu, pm.get(a, mu) + pm.get(b, mu));
   }
   // carried state of the visited branch: its parent's frame Gp and angles, its msq, decay
   // momentum and mass
@@ -188,8 +205,8 @@ __device__ void inverse_geometry(const PhsChannel &ch, double *pm, double sqrts,
     double q0[4], q1[4];
 #pragma unroll
     for (int mu = 0; mu < 4; mu++) {
-      q0[mu] = pm[(4 * V.slot[0] + mu) * PHS_INV_BLOCK];
-      q1[mu] = pm[(4 * V.slot[1] + mu) * PHS_INV_BLOCK];
+      q0[mu] = pm.get(V.slot[0], mu);
+      q1[mu] = pm.get(V.slot[1], mu);
     }
     double cmsq[2];
     cmsq[0] = q0[0] * q0[0] - q0[1] * q0[1] - q0[2] * q0[2] - q0[3] * q0[3];
@@ -324,12 +341,15 @@ __device__ double inverse_maps(const PhsChannel &ch, double sqrts, const double 
   return factor;
 }
 
-template <bool PER_EVENT>
+// LAB_ROWS: no lab boost (uniform beams with E1 = E2): the outgoing momenta are read from p
+// instead of staged in shared memory (InvMomenta).
+template <bool PER_EVENT, bool LAB_ROWS>
 __global__ void __launch_bounds__(PHS_INV_BLOCK)
     phs_inverse_kernel(const __grid_constant__ PhsInvLaunch a) {
+  static_assert(!(PER_EVENT && LAB_ROWS), "per-event beams stage their CM momenta");
   extern __shared__ double sm[];
-  double *pm = sm;                                                  // [4 (2 n_out - 1)][block]
-  double *stk = sm + (size_t)4 * (2 * a.n_out - 1) * PHS_INV_BLOCK;  // frame stack
+  double *pm = sm;  // [4 (n_out - 1), or 4 (2 n_out - 1) with staging][block]
+  double *stk = sm + (size_t)4 * (LAB_ROWS ? a.n_out - 1 : 2 * a.n_out - 1) * PHS_INV_BLOCK;  // frame stack
   double *geo = stk + (size_t)PHS_INV_STATE * a.stack_depth * PHS_INV_BLOCK;  // per-visit geometry
   double *cache = a.group_reuse ? geo + (size_t)PHS_INV_GEO * a.max_visits * PHS_INV_BLOCK
                                 : nullptr;  // per-visit mapping results
@@ -415,14 +435,18 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
         lab_ga = sqrt(1.0 + lab_bg * lab_bg);
       }
       // this event's momenta, lab -> CM (the inverse of phs.cu:1286-1301)
-      const double2 *pe = reinterpret_cast<const double2 *>(a.p + e * 4 * (int64_t)a.n_out);
-      for (int k = 0; k < a.n_out; k++) {
-        const double2 e_x = pe[2 * k], y_z = pe[2 * k + 1];
-        pm[(4 * k + 0) * PHS_INV_BLOCK + tid] = dsub(dmul(lab_ga, e_x.x), dmul(lab_bg, y_z.y));
-        pm[(4 * k + 1) * PHS_INV_BLOCK + tid] = e_x.y;
-        pm[(4 * k + 2) * PHS_INV_BLOCK + tid] = y_z.x;
-        pm[(4 * k + 3) * PHS_INV_BLOCK + tid] = dadd(dmul(-lab_bg, e_x.x), dmul(lab_ga, y_z.y));
+      const double *prow = a.p + e * 4 * (int64_t)a.n_out;
+      if (!LAB_ROWS) {
+        const double2 *pe = reinterpret_cast<const double2 *>(prow);
+        for (int k = 0; k < a.n_out; k++) {
+          const double2 e_x = pe[2 * k], y_z = pe[2 * k + 1];
+          pm[(4 * k + 0) * PHS_INV_BLOCK + tid] = dsub(dmul(lab_ga, e_x.x), dmul(lab_bg, y_z.y));
+          pm[(4 * k + 1) * PHS_INV_BLOCK + tid] = e_x.y;
+          pm[(4 * k + 2) * PHS_INV_BLOCK + tid] = y_z.x;
+          pm[(4 * k + 3) * PHS_INV_BLOCK + tid] = dadd(dmul(-lab_bg, e_x.x), dmul(lab_ga, y_z.y));
+        }
       }
+      const InvMomenta mom{pm + tid, LAB_ROWS ? prow : nullptr, a.n_out};
       // the geometry once per tree shape, then the mappings of each channel of that shape
       // (of this launch's slice of the group order)
       const bool has_own = a.x_own != nullptr;
@@ -430,7 +454,7 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
         const int gb = a.group_begin[g], ge = a.group_begin[g + 1];
         const int lo = max(gb, a.order_lo), hi = min(ge, a.order_hi);
         if (lo >= hi || (has_own && hi - lo == 1 && a.group_order[lo] == own_e)) continue;
-        inverse_geometry(a.channels[a.group_order[gb]], pm + tid, sqrts, stk, geo + tid);
+        inverse_geometry(a.channels[a.group_order[gb]], mom, sqrts, stk, geo + tid);
         for (int i = lo; i < hi; i++) {
           const int c = a.group_order[i];
           // the generating channel keeps its own row, but its mappings still run when a
@@ -468,8 +492,8 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
 
 }  // namespace
 
-size_t phs_inverse_smem_bytes(int n_out, int stack_depth, int max_visits, bool cache) {
-  return ((size_t)4 * (2 * n_out - 1) + (size_t)PHS_INV_STATE * stack_depth +
+size_t phs_inverse_smem_bytes(int n_out, int stack_depth, int max_visits, bool cache, bool lab_rows) {
+  return ((size_t)4 * (lab_rows ? n_out - 1 : 2 * n_out - 1) + (size_t)PHS_INV_STATE * stack_depth +
           (size_t)(PHS_INV_GEO + (cache ? PHS_INV_CACHE : 0)) * max_visits) *
          PHS_INV_BLOCK * sizeof(double);
 }
@@ -478,13 +502,21 @@ bool phs_inverse_fits_cache(int n_out, int stack_depth, int max_visits) {
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  return phs_inverse_smem_bytes(n_out, stack_depth, max_visits, true) <= (size_t)optin;
+  return phs_inverse_smem_bytes(n_out, stack_depth, max_visits, true, false) <= (size_t)optin;
 }
 
-int phs_inverse_blocks_per_sm(int n_out, int stack_depth, int max_visits, bool per_event, bool cache) {
+static const void *inverse_kernel(bool per_event, bool lab_rows) {
+  if (per_event) return (const void *)phs_inverse_kernel<true, false>;
+  return lab_rows ? (const void *)phs_inverse_kernel<false, true>
+                  : (const void *)phs_inverse_kernel<false, false>;
+}
+
+int phs_inverse_blocks_per_sm(int n_out, int stack_depth, int max_visits, bool per_event,
+                              bool cache, bool lab_rows) {
   int n = 0;
-  const size_t smem = phs_inverse_smem_bytes(n_out, stack_depth, max_visits, cache);
-  const void *k = per_event ? (const void *)phs_inverse_kernel<true> : (const void *)phs_inverse_kernel<false>;
+  lab_rows = lab_rows && !per_event;
+  const size_t smem = phs_inverse_smem_bytes(n_out, stack_depth, max_visits, cache, lab_rows);
+  const void *k = inverse_kernel(per_event, lab_rows);
   if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, PHS_INV_BLOCK, smem);
   return n > 0 ? n : 1;
@@ -492,18 +524,20 @@ int phs_inverse_blocks_per_sm(int n_out, int stack_depth, int max_visits, bool p
 
 cudaError_t phs_launch_inverse(const PhsInvLaunch &a, int n_blocks, cudaStream_t stream) {
   if (a.n_events <= 0) return cudaSuccess;
-  const size_t smem = phs_inverse_smem_bytes(a.n_out, a.stack_depth, a.max_visits,
-                                             a.group_reuse != nullptr);
   const bool per_event = a.E1 && a.E2;
+  const bool lab_rows = !per_event && !a.lab;
+  const size_t smem = phs_inverse_smem_bytes(a.n_out, a.stack_depth, a.max_visits,
+                                             a.group_reuse != nullptr, lab_rows);
+  const void *k = inverse_kernel(per_event, lab_rows);
   if (smem > 48 * 1024) {
-    cudaError_t e = per_event
-        ? cudaFuncSetAttribute(phs_inverse_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-        : cudaFuncSetAttribute(phs_inverse_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
   if (per_event)
-    phs_inverse_kernel<true><<<n_blocks, PHS_INV_BLOCK, smem, stream>>>(a);
+    phs_inverse_kernel<true, false><<<n_blocks, PHS_INV_BLOCK, smem, stream>>>(a);
+  else if (lab_rows)
+    phs_inverse_kernel<false, true><<<n_blocks, PHS_INV_BLOCK, smem, stream>>>(a);
   else
-    phs_inverse_kernel<false><<<n_blocks, PHS_INV_BLOCK, smem, stream>>>(a);
+    phs_inverse_kernel<false, false><<<n_blocks, PHS_INV_BLOCK, smem, stream>>>(a);
   return cudaGetLastError();
 }

@@ -1,0 +1,75 @@
+"""Host-side checks of the float-float helpers in phs_ff.h (the header compiles as plain
+C++): the integer-only conversions between doubles and float pairs that the FP32-pair
+kernels use to keep conversions off the FP64 pipe, against long-double references."""
+import os
+import subprocess
+import tempfile
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, "gpu_phs_gb300", "csrc")
+
+DRIVER = r"""
+#include <cstdio>
+#include <cmath>
+#include <random>
+#include "phs_ff.h"
+int main() {
+  std::mt19937_64 rng(12345);
+  std::uniform_real_distribution<double> u(-1.0, 1.0);
+  long bad_to = 0, bad_from = 0, bad_om = 0, n = 0;
+  double worst_to = 0;
+  for (int i = 0; i < 2000000; i++) {
+    // a normalized pair: hi any float, lo within half an ulp of hi
+    const double mag = std::ldexp(1.0, (int)(u(rng) * 60));
+    const float hi = (float)(u(rng) * mag);
+    if (hi == 0.0f) continue;
+    const int e = std::ilogb(hi);
+    float lo = (float)(u(rng) * std::ldexp(1.0, e - 24) * (i % 7 == 0 ? 1e-6 : 1.0));
+    ff a = fast_two_sum(hi, lo);                      // renormalized
+    const long double exact = (long double)a.hi + (long double)a.lo;
+    const double got = ff_to_double_int(a);
+    // within one ulp of the double nearest to the exact sum (bits below it are dropped)
+    const double near = (double)exact;
+    const double ulp = std::nextafter(std::fabs(near), INFINITY) - std::fabs(near);
+    const double err = std::fabs(got - near) / ulp;
+    if (err > 1.0) bad_to++;
+    if (err > worst_to) worst_to = err;
+    // double -> pair (truncation to 48 bits) and back: within 2^-47 relative
+    const double d = u(rng) * mag;
+    if (d != 0.0) {
+      const ff f = ff_from_double_int(d);
+      const long double back = (long double)f.hi + (long double)f.lo;
+      if (std::fabs((double)((back - d) / d)) > std::ldexp(1.0, -47)) bad_from++;
+    }
+    // 1 - x for x in [0, 1): relative accuracy 2^-46, also as x -> 1
+    const double x = std::fabs(u(rng));
+    const ff om = ff_one_minus_double_int(x);
+    const long double want = 1.0L - (long double)x;
+    if (want > 0 && std::fabs((double)(((long double)om.hi + om.lo - want) / want)) > std::ldexp(1.0, -46))
+      bad_om++;
+    n++;
+  }
+  std::printf("%ld %ld %ld %ld %.3f\n", n, bad_to, bad_from, bad_om, worst_to);
+  return 0;
+}
+"""
+
+
+def test_integer_conversions_of_float_pairs():
+    try:
+        subprocess.run(["g++", "--version"], check=True, capture_output=True)
+    except (OSError, subprocess.CalledProcessError):
+        pytest.skip("g++ not available")
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = os.path.join(d, "ff.cpp"), os.path.join(d, "ff")
+        with open(src, "w") as fh:
+            fh.write(DRIVER)
+        subprocess.run(["g++", "-O2", "-ffp-contract=off", "-std=c++17", "-I", CSRC, src, "-o", exe],
+                       check=True)
+        n, bad_to, bad_from, bad_om, worst = subprocess.run(
+            [exe], check=True, capture_output=True, text=True).stdout.split()
+    assert int(n) > 1_900_000
+    assert int(bad_to) == 0, f"ff_to_double_int off by more than an ulp ({worst} ulp)"
+    assert int(bad_from) == 0 and int(bad_om) == 0
