@@ -526,11 +526,15 @@ __device__ __forceinline__ void write_failed_event(const PhsLaunch &a, const Phs
 
 // The same for the events of a warp tile (first event local0) whose lanes are set in
 // `failed`, with the momentum rows written by the whole warp (the tile's rows are
-// contiguous): 512 bytes per store instruction.
+// contiguous): 512 bytes per store instruction.  Volume, factor and ok are written for
+// every event of the tile (`valid`), the survivors' with the failed values that the walk
+// kernel behind this one overwrites: whole 32-byte sectors, where writes of the failing
+// lanes alone would leave partial sectors for the DRAM to merge.
 __device__ __forceinline__ void write_failed_tile(const PhsLaunch &a, const PhsSegment &seg,
-                                                  int64_t local0, unsigned failed) {
+                                                  int64_t local0, unsigned failed,
+                                                  unsigned valid) {
   const int lane = threadIdx.x & 31;
-  if (failed >> lane & 1) {
+  if (valid >> lane & 1) {
     const int64_t ev = seg.ev_begin + local0 + lane;
     a.volume[ev] = a.channels_ff[seg.channel].volume;
     a.factor[ev * a.factor_stride + seg.factor_col] = 0.0;
@@ -630,9 +634,10 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, PHS_FF_TEST_MIN_BLOCKS)
       const bool pass = valid && phs_ok_f32(a, seg, local, st);
       const unsigned m = __ballot_sync(0xffffffffu, pass);
       const unsigned failed = __ballot_sync(0xffffffffu, valid && !pass);
+      const unsigned in_seg = __ballot_sync(0xffffffffu, valid);
       if (pass) buf[n_pass + __popc(m & ((1u << lane) - 1u))] = (int32_t)local;
       n_pass += __popc(m);
-      if (failed) write_failed_tile(a, seg, local0, failed);
+      if (failed) write_failed_tile(a, seg, local0, failed, in_seg);
     }
     __syncwarp();
     if (n_pass > 0) {
