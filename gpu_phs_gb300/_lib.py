@@ -21,6 +21,7 @@ D = C.c_double
 _SIGS = {
     "phs_last_error": (C.c_char_p, []),
     "phs_version": (C.c_char_p, []),
+    "phs_set_device_allocator": (I, [P, P, P]),
     "phs_process_create": (I, [C.POINTER(P), I, I, I, I, P, P, P, P, P, P, P, P, P]),
     "phs_process_destroy": (I, [P]),
     "phs_process_set_beams": (I, [P, D, D]),

@@ -75,7 +75,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
             sys.stdout.write(lg)
     if force or jobs or _stale(LIB, objs):
         tmp = LIB + ".tmp"
-        _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread",
+        _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread", "-ldl",
               "-Xlinker", "-rpath", "-Xlinker", os.path.join(CUDA_HOME, "lib64")])
         shutil.move(tmp, LIB)
     return LIB

@@ -15,10 +15,22 @@
 #include <thread>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/gpu_phs.h"
 #include "../../include/gpu_phs_transfer.h"
 #include "phs_device.h"
 #include "phs_host.h"
+
+// NVTX range around an entry point's body (tracing under nsys or ncu --nvtx; the NVTX
+// calls are no-ops unless a tool is attached).
+namespace {
+struct TraceRange {
+  explicit TraceRange(const char *name) { nvtxRangePushA(name); }
+  ~TraceRange() { nvtxRangePop(); }
+};
+}  // namespace
+#define PHS_TRACE(name) TraceRange phs_trace_range_(name)
 
 // ---------------------------------------------------------------------------- errors
 static thread_local std::string g_err;
@@ -60,31 +72,67 @@ static void guarded_void(Body &&body) {
   } while (0)
 
 extern "C" const char *phs_last_error(void) { return g_err.c_str(); }
+
 extern "C" const char *phs_version(void) { return "gpu_phs_gb300 0.1 (sm_103a, fp64 fused)"; }
 
 // ------------------------------------------------------------------- device buffers
 namespace {
 
+// The device allocator of the library's buffers (phs_set_device_allocator): null
+// functions mean cudaMalloc/cudaFree.
+struct DeviceAllocator {
+  phs_device_alloc_fn alloc = nullptr;
+  phs_device_free_fn free = nullptr;
+  void *user = nullptr;
+};
+std::mutex g_alloc_mu;
+DeviceAllocator g_alloc;
+
+DeviceAllocator current_allocator() {
+  std::lock_guard<std::mutex> lock(g_alloc_mu);
+  return g_alloc;
+}
+
 struct DevBuf {
   void *ptr = nullptr;
   size_t cap = 0;
+  DeviceAllocator by;  // the allocator that made ptr (its free hands it back)
   int reserve(size_t bytes) {
     if (bytes <= cap) return PHS_OK;
-    if (ptr) cudaFree(ptr);
-    ptr = nullptr;
-    cap = 0;
-    cudaError_t e = cudaMalloc(&ptr, bytes);
-    if (e != cudaSuccess) {
-      ptr = nullptr;
-      return fail(PHS_ERR_ALLOC, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    release();
+    const DeviceAllocator a = current_allocator();
+    if (a.alloc) {
+      void *p = nullptr;
+      const int rc = a.alloc(&p, bytes, a.user);
+      if (rc != 0 || !p)
+        return fail(PHS_ERR_ALLOC, "the device allocator failed for %zu bytes (returned %d)",
+                    bytes, rc);
+      ptr = p;
+    } else {
+      cudaError_t e = cudaMalloc(&ptr, bytes);
+      if (e != cudaSuccess) {
+        ptr = nullptr;
+        return fail(PHS_ERR_ALLOC, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+      }
     }
+    by = a;
     cap = bytes;
     return PHS_OK;
   }
   void release() {
-    if (ptr) cudaFree(ptr);
+    if (ptr) {
+      if (by.alloc) {
+        // as cudaFree would: no kernel that uses the buffer is still running when the
+        // caller's allocator gets it back
+        cudaDeviceSynchronize();
+        if (by.free) by.free(ptr, by.user);
+      } else {
+        cudaFree(ptr);
+      }
+    }
     ptr = nullptr;
     cap = 0;
+    by = DeviceAllocator();
   }
   template <class T> T *as() const { return static_cast<T *>(ptr); }
 };
@@ -339,6 +387,17 @@ struct DeviceGuard {
 
 }  // namespace
 
+extern "C" int phs_set_device_allocator(phs_device_alloc_fn alloc, phs_device_free_fn free_fn,
+                                        void *user) {
+  if ((alloc == nullptr) != (free_fn == nullptr))
+    return fail(PHS_ERR_INVALID_ARG, "give both allocator functions or neither");
+  std::lock_guard<std::mutex> lock(g_alloc_mu);
+  g_alloc.alloc = alloc;
+  g_alloc.free = free_fn;
+  g_alloc.user = user;
+  return PHS_OK;
+}
+
 // -------------------------------------------------------------------------- process
 struct phs_process {
   phs::Process p;
@@ -448,6 +507,7 @@ extern "C" int phs_process_destroy(phs_process_t h) {
 }
 
 extern "C" int phs_process_set_beams(phs_process_t h, double E1, double E2) {
+  PHS_TRACE("phs_process_set_beams");
   return guarded([&]() -> int {
     if (int rc = check_proc(h)) return rc;
     if (!(E1 > 0) || !(E2 > 0) || !isfinite(E1) || !isfinite(E2))
@@ -722,6 +782,7 @@ static int check_ptrs(int64_t n, const void *x, const void *p, const void *f, co
 extern "C" int phs_generate_device(phs_process_t h, int64_t n_events, const int64_t *counts,
                                    const double *x, double *p, double *f, double *v, uint8_t *ok,
                                    void *stream) {
+  PHS_TRACE("phs_generate_device");
   return guarded([&]() -> int {
     if (int rc = check_proc(h)) return rc;
     if (!h->beams) return fail(PHS_ERR_STATE, "phs_process_set_beams has not been called");
@@ -737,6 +798,7 @@ extern "C" int phs_generate_beams_device(phs_process_t h, int64_t n_events, cons
                                          const double *E1, const double *E2, const double *x,
                                          double *p, double *f, double *v, uint8_t *ok,
                                          void *stream) {
+  PHS_TRACE("phs_generate_beams_device");
   return guarded([&]() -> int {
     if (int rc = check_proc(h)) return rc;
     if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
@@ -759,6 +821,7 @@ extern "C" int phs_generate_beams_device(phs_process_t h, int64_t n_events, cons
 extern "C" int phs_adjoint_device(phs_process_t h, int64_t n_events, const int64_t *counts,
                                   const double *x, const double *pbar, const double *jbar,
                                   double *xbar, double *thbar, void *stream) {
+  PHS_TRACE("phs_adjoint_device");
   return guarded([&]() -> int {
     if (int rc = check_proc(h)) return rc;
     if (!h->beams) return fail(PHS_ERR_STATE, "phs_process_set_beams has not been called");
@@ -821,6 +884,7 @@ extern "C" int phs_inverse_device(phs_process_t h, int64_t n_events, const int64
                                   const uint8_t *ok, const double *x_own,
                                   const double *factor_own, double *all_factors, double *x_out,
                                   void *stream) {
+  PHS_TRACE("phs_inverse_device");
   return guarded([&]() -> int {
     if (int rc = check_proc(h)) return rc;
     if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
@@ -907,6 +971,7 @@ static int inverse_launch(phs_process_t h, int64_t n_events, const int64_t *d_ch
 // after its previous chunk's copies back have been ordered before the next copy in.
 extern "C" int phs_generate_host(phs_process_t h, int64_t n_events, const int64_t *counts,
                                  const double *x, double *p, double *f, double *v, uint8_t *ok) {
+  PHS_TRACE("phs_generate_host");
   return guarded([&]() -> int {
     if (int rc = check_proc(h)) return rc;
     if (!h->beams) return fail(PHS_ERR_STATE, "phs_process_set_beams has not been called");
@@ -1050,6 +1115,7 @@ extern "C" int phs_batch_offsets(phs_batch_t b, const int64_t *counts, int64_t *
 extern "C" int phs_batch_generate_device(phs_batch_t b, const int64_t *counts, const double *x,
                                          double *p, double *f, double *v, uint8_t *ok,
                                          void *stream) {
+  PHS_TRACE("phs_batch_generate_device");
   return guarded([&]() -> int {
     if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
     if (!counts) return fail(PHS_ERR_INVALID_ARG, "null counts");
@@ -1126,6 +1192,7 @@ extern "C" int phs_generate_device_noalloc(phs_process_t h, double E1, double E2
                                            int64_t n_events, const int64_t *counts,
                                            const double *x, double *p, double *f, double *v,
                                            uint8_t *ok, void *stream) {
+  PHS_TRACE("phs_generate_device_noalloc");
   return guarded([&]() -> int {
     if (int rc = check_proc(h)) return rc;
     if (int rc = check_counts(counts, h->p.n_channels, n_events)) return rc;
@@ -1248,6 +1315,7 @@ static int capture_graph(phs_graph_t *out, int device, Call call) {
 extern "C" int phs_batch_graph_create(phs_graph_t *out, phs_batch_t b, const int64_t *counts,
                                       const double *x, double *p, double *f, double *v,
                                       uint8_t *ok) {
+  PHS_TRACE("phs_batch_graph_create");
   return guarded([&]() -> int {
     if (!b) return fail(PHS_ERR_INVALID_ARG, "null batch handle");
     return capture_graph(out, b->device, [&](cudaStream_t st) {
@@ -1259,6 +1327,7 @@ extern "C" int phs_batch_graph_create(phs_graph_t *out, phs_batch_t b, const int
 extern "C" int phs_process_graph_create(phs_graph_t *out, phs_process_t h, int64_t n_events,
                                         const int64_t *counts, const double *x, double *p,
                                         double *f, double *v, uint8_t *ok) {
+  PHS_TRACE("phs_process_graph_create");
   return guarded([&]() -> int {
     if (int rc = check_proc(h)) return rc;
     return capture_graph(out, h->device, [&](cudaStream_t st) {
@@ -1268,6 +1337,7 @@ extern "C" int phs_process_graph_create(phs_graph_t *out, phs_process_t h, int64
 }
 
 extern "C" int phs_graph_launch(phs_graph_t G, void *stream) {
+  PHS_TRACE("phs_graph_launch");
   return guarded([&]() -> int {
     if (!G) return fail(PHS_ERR_INVALID_ARG, "null graph handle");
     DeviceGuard g(G->device);
@@ -1290,6 +1360,7 @@ extern "C" int phs_graph_destroy(phs_graph_t G) {
 // ---------------------------------------------------------------------- random numbers
 extern "C" int phs_philox_fill(double *x, int64_t n_events, int n_x, uint64_t seed,
                                int64_t first_event, void *stream) {
+  PHS_TRACE("phs_philox_fill");
   return guarded([&]() -> int {
     if (n_events < 0 || n_x < 1 || first_event < 0) return fail(PHS_ERR_INVALID_ARG, "bad sizes");
     if (n_events > 0 && !x) return fail(PHS_ERR_INVALID_ARG, "null x");
@@ -1603,6 +1674,7 @@ extern "C" void c_whizard_gen_phs_from_x_gpu(double *E1_in, double *E2_in,
                                              int *n_channels_p, int *n_x_p, double *x,
                                              double *factors, double *volumes, bool *oks,
                                              double *p, double *x_out) {
+  PHS_TRACE("c_whizard_gen_phs_from_x_gpu");
   (void)requires_boost_to_lab;  // stored but unused by the reference (phs.cu:1559)
   std::lock_guard<std::mutex> lk(W.mu);
   g_err.clear();  // the call returns nothing: phs_last_error() reports this call alone
@@ -2072,6 +2144,7 @@ static int grid_channels(phs_grid_t g, int64_t n_events, const int64_t *counts, 
 extern "C" int phs_grid_sample_device(phs_grid_t g, int64_t n_events, const int64_t *counts,
                                       uint64_t seed, int64_t first_event, double *x,
                                       void *stream) {
+  PHS_TRACE("phs_grid_sample_device");
   return guarded([&]() -> int {
     if (!g) return fail(PHS_ERR_INVALID_ARG, "null grid handle");
     if (n_events > 0 && !x) return fail(PHS_ERR_INVALID_ARG, "null x");
@@ -2088,6 +2161,7 @@ extern "C" int phs_grid_sample_device(phs_grid_t g, int64_t n_events, const int6
 
 extern "C" int phs_grid_update_device(phs_grid_t g, int64_t n_events, const int64_t *counts,
                                       const double *x, const uint8_t *oks, void *stream) {
+  PHS_TRACE("phs_grid_update_device");
   return guarded([&]() -> int {
     if (!g) return fail(PHS_ERR_INVALID_ARG, "null grid handle");
     if (n_events > 0 && (!x || !oks)) return fail(PHS_ERR_INVALID_ARG, "null data pointer");

@@ -141,6 +141,10 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
   if (ch.exact_only) return false;
   const int64_t ev = seg.ev_begin + local;
   const double *xe = a.x + seg.x_base + local * seg.x_stride;
+  // the walk reads the row's x one visit at a time, each index from the program: fetch the
+  // row's cache lines into L1 now, so only the first access waits for DRAM
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(xe));
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(xe + seg.x_stride - 1));
   double *out = a.p + seg.p_base + local * 4 * (int64_t)ch.n_out;
   const ff zero = ff_from_float(0.0f), one = ff_from_float(1.0f);
 

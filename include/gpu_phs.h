@@ -64,6 +64,23 @@ typedef struct phs_batch *phs_batch_t;
 const char *phs_last_error(void);
 const char *phs_version(void);
 
+/* Device memory of the library's own buffers (channel programs, segment tables, work
+ * queues, the host path's chunk buffers, the stored-matrix adjoint's frames): by default
+ * cudaMalloc and cudaFree.  A caller that owns the device heap through an allocator of its
+ * own (a pool, an arena, a framework's caching allocator) routes them through it: alloc
+ * sets *ptr to at least `bytes` of device memory of the current device, 256-byte aligned,
+ * and returns 0, or returns non-zero (the library call then fails with PHS_ERR_ALLOC and
+ * the size in its message); free takes back a pointer alloc gave.  Before handing a buffer
+ * back the library synchronizes the device, as cudaFree does.  Both NULL restore the
+ * default; a buffer is always freed by the allocator that made it.  Process-wide; the
+ * library calls the functions from the thread of the API call that needs the buffer.
+ * Returns PHS_ERR_INVALID_ARG if only one of the two is given.  No counterpart in the
+ * reference, which allocates and frees its device memory inside every generate call
+ * (phs.cu:1338-1426, 1604-1635). */
+typedef int (*phs_device_alloc_fn)(void **ptr, size_t bytes, void *user);
+typedef void (*phs_device_free_fn)(void *ptr, void *user);
+int phs_set_device_allocator(phs_device_alloc_fn alloc, phs_device_free_fn free, void *user);
+
 /* ------------------------------------------------------------------ handle API: process */
 
 /* Validates and stores a process.  Replaces the reference's global set-up sequence

@@ -125,3 +125,46 @@ def test_null_handles_are_errors(lib):
     assert lib.phs_generate_device(None, 0, None, None, None, None, None, None, None) == -1
     assert lib.phs_batch_generate_device(None, None, None, None, None, None, None, None) == -1
     assert lib.phs_process_destroy(None) == 0
+
+
+ALLOC_FN = C.CFUNCTYPE(C.c_int, C.POINTER(C.c_void_p), C.c_size_t, C.c_void_p)
+FREE_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p)
+
+
+def test_device_allocator_failure_is_reported(lib):
+    """An allocation failure injected through the device-allocator hook surfaces as
+    PHS_ERR_ALLOC with the size in the message, and nothing is freed that was not made
+    (host only: set_beams fails at its first device buffer, before any copy)."""
+    from gpu_phs_gb300.api import _ptr
+    asked, freed = [], []
+
+    @ALLOC_FN
+    def failing_alloc(ptr, nbytes, user):
+        asked.append(nbytes)
+        return 7
+
+    @FREE_FN
+    def record_free(ptr, user):
+        freed.append(ptr)
+
+    assert lib.phs_set_device_allocator(failing_alloc, None, None) == -1   # both or neither
+    assert lib.phs_set_device_allocator(failing_alloc, record_free, None) == 0
+    try:
+        proc = P.ww()
+        keep = [np.ascontiguousarray(a, dt) for a, dt in (
+            (proc.d1, np.int32), (proc.d2, np.int32), (proc.has_children, np.int32),
+            (proc.friends, np.int32), (proc.map_ids, np.int32), (proc.map_masses, np.float64),
+            (proc.map_widths, np.float64), (proc.flv_masses, np.float64),
+            (proc.flv_widths, np.float64))]
+        h = C.c_void_p()
+        assert lib.phs_process_create(C.byref(h), proc.n_in, proc.n_out, proc.n_channels,
+                                      proc.n_x, *[_ptr(a) for a in keep]) == 0
+        rc = lib.phs_process_set_beams(h, 250.0, 250.0)
+        assert rc == -6                      # PHS_ERR_ALLOC
+        msg = lib.phs_last_error().decode()
+        assert "device allocator failed" in msg and str(asked[0]) in msg
+        assert len(asked) == 1 and asked[0] > 0
+        assert lib.phs_process_destroy(h) == 0
+        assert freed == []
+    finally:
+        assert lib.phs_set_device_allocator(None, None, None) == 0
