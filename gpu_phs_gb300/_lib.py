@@ -9,6 +9,8 @@ from typing import List
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libgpuphs.so")
+# the bounds-checked build of the same library (csrc/phs_check.h), for tests
+CHECKED_PATH = os.path.join(HERE, "libgpuphs_checked.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "gpu_phs.h")
 
 _lib = None
@@ -22,6 +24,8 @@ _SIGS = {
     "phs_last_error": (C.c_char_p, []),
     "phs_version": (C.c_char_p, []),
     "phs_set_device_allocator": (I, [P, P, P]),
+    "phs_is_checked_build": (I, []),
+    "phs_check_status": (I, [P, P]),
     "phs_process_create": (I, [C.POINTER(P), I, I, I, I, P, P, P, P, P, P, P, P, P]),
     "phs_process_destroy": (I, [P]),
     "phs_process_set_beams": (I, [P, D, D]),
@@ -87,21 +91,57 @@ def header_symbols() -> List[str]:
     return sorted(set(re.findall(r"\b((?:phs|c_whizard)_\w+)\s*\(", text)))
 
 
-def load() -> C.CDLL:
-    """Loads libgpuphs.so (built by gpu_phs_gb300.build)."""
-    global _lib
-    if _lib is not None:
-        return _lib
-    if not os.path.exists(LIB_PATH):
-        raise ImportError(f"{LIB_PATH} is missing: build it with "
+def _open(path: str) -> C.CDLL:
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with "
                           "`python -c 'import __graft_entry__ as g; g.build()'`")
-    lib = C.CDLL(LIB_PATH)
+    lib = C.CDLL(path)
     for name, (res, args) in _SIGS.items():
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    _lib = lib
     return lib
+
+
+def load() -> C.CDLL:
+    """Loads libgpuphs.so (built by gpu_phs_gb300.build).  Inside `using(lib)` it returns
+    that library instead."""
+    global _lib
+    if _active is not None:
+        return _active
+    if _lib is None:
+        _lib = _open(LIB_PATH)
+    return _lib
+
+
+_checked = None
+_active = None
+
+
+def load_checked() -> C.CDLL:
+    """Loads libgpuphs_checked.so, the bounds-checked build, beside the regular one (its
+    own symbols and kernels: ctypes opens each library with local symbol binding)."""
+    global _checked
+    if _checked is None:
+        _checked = _open(CHECKED_PATH)
+    return _checked
+
+
+class using:
+    """with using(lib): the Python API (PhaseSpace, Batch, ...) calls `lib` instead of
+    libgpuphs.so.  Handles made inside belong to that library: close them inside."""
+
+    def __init__(self, lib: C.CDLL):
+        self.lib = lib
+
+    def __enter__(self):
+        global _active
+        self.prev, _active = _active, self.lib
+        return self.lib
+
+    def __exit__(self, *exc):
+        global _active
+        _active = self.prev
 
 
 def check(rc: int) -> None:

@@ -17,6 +17,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgpuphs.so")
+# the bounds-checked build (-DPHS_CHECKED, csrc/phs_check.h): a second library for tests
+BUILD_CHECKED = os.path.join(HERE, "_build_checked")
+LIB_CHECKED = os.path.join(HERE, "libgpuphs_checked.so")
 ROOT = os.path.dirname(HERE)
 
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
@@ -46,9 +49,9 @@ def _stale(out: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, force: bool = False) -> str:
-    """Compile and link; returns the library path.  Raises RuntimeError on failure."""
-    os.makedirs(BUILD, exist_ok=True)
+def _jobs(build_dir, lib, defines, force):
+    """Compile commands of one library (those whose object is stale) and its objects."""
+    os.makedirs(build_dir, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     inc_dir = os.path.join(ROOT, "include")
     headers += [os.path.join(inc_dir, f) for f in os.listdir(inc_dir) if f.endswith(".h")]
@@ -56,28 +59,45 @@ def build(verbose: bool = False, force: bool = False) -> str:
     jobs, objs = [], []
     for src in CU_SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
+        o = os.path.join(build_dir, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
             jobs.append([NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                         "-Xptxas", "-v", *CU_FLAGS.get(src, []), *inc, "-c", s, "-o", o])
+                         "-Xptxas", "-v", *defines, *CU_FLAGS.get(src, []), *inc, "-c", s, "-o", o])
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
+        o = os.path.join(build_dir, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
             jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
-                         "-Wall", "-Wno-unused-function", *inc, "-c", s, "-o", o])
-    with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
-        logs = list(ex.map(_run, jobs))
+                         "-Wall", "-Wno-unused-function", *defines, *inc, "-c", s, "-o", o])
+    return jobs, objs
+
+
+def _link(lib, objs):
+    tmp = lib + ".tmp"
+    _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread", "-ldl",
+          "-Xlinker", "-rpath", "-Xlinker", os.path.join(CUDA_HOME, "lib64")])
+    shutil.move(tmp, lib)
+
+
+def build(verbose: bool = False, force: bool = False, checked: bool = True) -> str:
+    """Compile and link libgpuphs.so and (checked=True) libgpuphs_checked.so, every
+    translation unit of both in parallel; returns the library path.  Raises RuntimeError
+    on failure."""
+    libs = [(BUILD, LIB, [])]
+    if checked:
+        libs.append((BUILD_CHECKED, LIB_CHECKED, ["-DPHS_CHECKED"]))
+    plans = [(lib, *_jobs(d, lib, defs, force)) for d, lib, defs in libs]
+    all_jobs = [j for _, jobs, _ in plans for j in jobs]
+    with ThreadPoolExecutor(max_workers=max(1, len(all_jobs))) as ex:
+        logs = list(ex.map(_run, all_jobs))
     if verbose:
         for lg in logs:
             sys.stdout.write(lg)
-    if force or jobs or _stale(LIB, objs):
-        tmp = LIB + ".tmp"
-        _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread", "-ldl",
-              "-Xlinker", "-rpath", "-Xlinker", os.path.join(CUDA_HOME, "lib64")])
-        shutil.move(tmp, LIB)
+    for lib, jobs, objs in plans:
+        if force or jobs or _stale(lib, objs):
+            _link(lib, objs)
     return LIB
 
 

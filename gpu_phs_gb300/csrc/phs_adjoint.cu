@@ -43,6 +43,7 @@ struct AdjLayout {
   int state0, ang0, der0, pop0, stack0;  // offsets (in slots) of the per-thread regions
   int trig0;                             // the block's sin/cos table (2 slots)
   int fr0;                               // friend visits: the rotation axis, 3 per visit
+  int nv, npops, depth;                  // visits, pop frames and stack depth the regions hold
 };
 
 // A value with its derivatives along three directions (forward-mode differentiation).
@@ -211,8 +212,15 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
     const PhsSegment seg = segs[lo];
     const int64_t local = (tile - seg.tile_begin) * 32 + lane;
     if (local >= seg.ev_count) continue;
+    if (!phs_in(seg.channel, a.n_programs, PHS_CHK_CHANNEL)) continue;
     const PhsChannel &ch = a.channels[seg.channel];
     const PhsAdjChannel &ad = adj[seg.channel];
+    // checked build: the rows of x, xbar (x's layout), pbar (p's) and thbar, and a program
+    // that fits the shared-memory regions sized for it
+    if (!event_in_bounds(a, seg, local, ch.n_out, ch.n_visits) ||
+        !phs_in(ch.n_visits - 1, lay.nv, PHS_CHK_VISITS) ||
+        !phs_in(ad.n_pops, lay.npops + 1, PHS_CHK_VISITS))
+      continue;
     const int64_t ev = seg.ev_begin + local;
     const double *xe = a.x + seg.x_base + local * seg.x_stride;
     double *xb = xbar + seg.x_base + local * seg.x_stride;
@@ -241,7 +249,7 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
     int sp = 0, np = 0;
     for (int v = 0; v < n_visits; v++) {
       const PhsVisit &V = ch.visit[v];
-      if (STORED) {
+      if (STORED && phs_in(ev, store_events, PHS_CHK_STORE)) {
 #pragma unroll
         for (int i = 0; i < 16; i++) store[(int64_t)(v * 16 + i) * store_events + ev] = L[i];
       }
@@ -259,7 +267,7 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
           cmax[j] = 0.0;
         } else {
           double f, aux;
-          const double xm = xe[C.x_msq];
+          const double xm = xrow_at(xe, C.x_msq, seg.x_stride);
           map_msq(C.map_id, xm, s, C.m, C.w, C.msq_min, C.msq_max, C.a0, C.a1, C.a2, cmsq[j], f,
                   aux);
           cm[j] = sqrt(cmsq[j]);
@@ -267,8 +275,10 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
           double dd[6];
           map_derivs(C, ad.visit[v].child[j], xm, aux, dd[0], dd[1], dd[2], dd[3], dd[4], dd[5]);
           const int cv = ad.visit[v].child_visit[j];
+          if (phs_in(cv, n_visits, PHS_CHK_VISITS)) {
 #pragma unroll
-          for (int k = 0; k < 6; k++) slot(sm, lay.der0 + PHS_ADJ_DER * cv + k) = dd[k];
+            for (int k = 0; k < 6; k++) slot(sm, lay.der0 + PHS_ADJ_DER * cv + k) = dd[k];
+          }
         }
       }
       const double d = dsub(dsub(msq_b, cmsq[0]), cmsq[1]);
@@ -285,11 +295,13 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
       const double bg = p_b * rm;
       const double ga = V.self_root ? 1.0 : E_b * rm;
       double sphi, cphi, ct, st, fct;
-      sincos2pi_tab(xe[V.x_phi], trig, sphi, cphi);
-      map_ct(V.ct_class, xe[V.x_ct], V.b0, V.b1, ct, st, fct);
+      const double x_phi = xrow_at(xe, V.x_phi, seg.x_stride);
+      const double x_ct = xrow_at(xe, V.x_ct, seg.x_stride);
+      sincos2pi_tab(x_phi, trig, sphi, cphi);
+      map_ct(V.ct_class, x_ct, V.b0, V.b1, ct, st, fct);
       {
         double dct, dst, dlf;
-        ct_derivs(V.ct_class, xe[V.x_ct], V.b0, V.b1, ct, st, dct, dst, dlf);
+        ct_derivs(V.ct_class, x_ct, V.b0, V.b1, ct, st, dct, dst, dlf);
         const int b = lay.ang0 + PHS_ADJ_ANG * v;
         slot(sm, b + 0) = cphi;
         slot(sm, b + 1) = sphi;
@@ -333,7 +345,7 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
           L[4 * r + 3] = l0 * e03 + l1 * e13 + l2 * e23 + l3 * e33;
         }
       }
-      if (V.push >= 0) {
+      if (V.push >= 0 && phs_in(sp, lay.depth, PHS_CHK_STACK)) {
         const bool j0 = V.push == 0;
         const int base = lay.stack0 + PHS_STATE * sp;
 #pragma unroll
@@ -354,8 +366,10 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
         E_b = j0 ? ce0 : ce1;
       } else if (sp > 0) {
         // the frame the reverse walk resumes with after this pop
+        if (phs_in(np, lay.npops, PHS_CHK_STACK)) {
 #pragma unroll
-        for (int i = 0; i < 16; i++) slot(sm, lay.pop0 + 16 * np + i) = L[i];
+          for (int i = 0; i < 16; i++) slot(sm, lay.pop0 + 16 * np + i) = L[i];
+        }
         np++;
         sp--;
         const int base = lay.stack0 + PHS_STATE * sp;
@@ -392,16 +406,18 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
         if (!C.internal) {
           cmsq[j] = C.msq_leaf;
           cm[j] = C.m_leaf;
-        } else {
+        } else if (phs_in(A.child_visit[j], n_visits, PHS_CHK_VISITS)) {
           cmsq[j] = slot(sm, lay.state0 + PHS_ADJ_STATE * A.child_visit[j] + 0);
           cm[j] = slot(sm, lay.state0 + PHS_ADJ_STATE * A.child_visit[j] + 1);
+        } else {
+          cmsq[j] = cm[j] = 1.0;
         }
       }
       if (V.carry >= 0) {
         const int j = V.carry;
         c_msqb[j] = sb_msq; c_mb[j] = sb_m; c_pb[j] = sb_p; c_Eb[j] = sb_E;
       }
-      if (V.push >= 0) {
+      if (V.push >= 0 && phs_in(asp - 1, lay.depth, PHS_CHK_STACK)) {
         asp--;
         const int base = lay.stack0 + PHS_ADJ_FRAME * asp;
 #pragma unroll
@@ -434,7 +450,7 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
 #pragma unroll
       for (int j = 0; j < 2; j++) {
         const PhsChild &C = V.child[j];
-        if (!C.internal) {
+        if (!C.internal && phs_in(C.out_index, ch.n_out, PHS_CHK_ADJ)) {
           const double sj = j == 0 ? 1.0 : -1.0;
           const double ce = j == 0 ? ce0 : ce1;
           const double *P = pb + 4 * C.out_index;
@@ -448,7 +464,7 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
           }
           ceb[j] += v0;
           pcb += sj * v3;
-        } else {
+        } else if (C.internal) {
           ceb[j] += c_Eb[j];
           pcb += (j == 0 ? 1.0 : -1.0) * c_pb[j];
         }
@@ -482,7 +498,8 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
               if (!STORED) acc += L[4 * r + k] * (eta[k] * eta[c]) * F[4 * c + k];
               accb += Lb[4 * r + k] * F[4 * c + k];
             }
-            Lp[4 * r + c] = STORED ? store[(int64_t)(v * 16 + 4 * r + c) * store_events + ev] : acc;
+            Lp[4 * r + c] = STORED && phs_in(ev, store_events, PHS_CHK_STORE)
+                                ? store[(int64_t)(v * 16 + 4 * r + c) * store_events + ev] : acc;
             Lpb[4 * r + c] = accb;
           }
         double Fb[16];
@@ -556,7 +573,8 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
               if (!STORED) acc += L[4 * r + k] * (eta[k] * eta[c]) * L1[4 * c + k];
               accb += Lb[4 * r + k] * L1[4 * c + k];
             }
-            Lp[4 * r + c] = STORED ? store[(int64_t)(v * 16 + 4 * r + c) * store_events + ev] : acc;
+            Lp[4 * r + c] = STORED && phs_in(ev, store_events, PHS_CHK_STORE)
+                                ? store[(int64_t)(v * 16 + 4 * r + c) * store_events + ev] : acc;
             Lpb[4 * r + c] = accb;
           }
 #pragma unroll
@@ -579,8 +597,9 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
         cpb = L1b[5] * ct + L1b[7] * st + L1b[10];
         spb = -L1b[6] + L1b[9] * ct + L1b[11] * st;
       }
-      xb[V.x_phi] = 2.0 * PHS_PI * (-sphi * cpb + cphi * spb);
-      xb[V.x_ct] = ctb * slot(sm, ab + 4) + stb * slot(sm, ab + 5) + jb * slot(sm, ab + 6);
+      if (phs_in(V.x_phi, seg.x_stride, PHS_CHK_ADJ)) xb[V.x_phi] = 2.0 * PHS_PI * (-sphi * cpb + cphi * spb);
+      if (phs_in(V.x_ct, seg.x_stride, PHS_CHK_ADJ))
+        xb[V.x_ct] = ctb * slot(sm, ab + 4) + stb * slot(sm, ab + 5) + jb * slot(sm, ab + 6);
       // bg = p rm, gamma = E rm
       double vb_p = 0.0, vb_E = 0.0, rmb = 0.0;
       if (!V.self_root) {
@@ -604,7 +623,9 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
 #pragma unroll
       for (int j = 0; j < 2; j++) {
         const PhsChild &C = V.child[j];
-        if (!C.internal) continue;
+        if (!C.internal || !phs_in(A.child_visit[j], n_visits, PHS_CHK_VISITS) ||
+            !phs_in(C.x_msq, seg.x_stride, PHS_CHK_ADJ))
+          continue;
         const double msqb = cmsqb[j] + c_msqb[j] + c_mb[j] / (2.0 * cm[j]);
         const int db = lay.der0 + PHS_ADJ_DER * A.child_visit[j];
         xb[C.x_msq] = msqb * slot(sm, db + 0) + jb * slot(sm, db + 1);
@@ -615,7 +636,8 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
       }
       // on to the previous visit
       if (v > 0) {
-        if (A.entered_by_pop) {
+        if (A.entered_by_pop && phs_in(asp, lay.depth, PHS_CHK_STACK) &&
+            phs_in(A.pop_slot, lay.npops, PHS_CHK_STACK)) {
           const int base = lay.stack0 + PHS_ADJ_FRAME * asp;
 #pragma unroll
           for (int i = 0; i < 16; i++) slot(sm, base + i) = Lpb[i];
@@ -678,6 +700,9 @@ cudaError_t phs_launch_adjoint(const PhsLaunch &a, const PhsAdjChannel *adj, con
   size_t smem;
   phs_adjoint_sizes(max_visits, max_pops, a.stack_depth, friends, &lay.state0, &lay.ang0,
                     &lay.der0, &lay.pop0, &lay.stack0, &lay.trig0, &lay.fr0, &smem);
+  lay.nv = max_visits;
+  lay.npops = max_pops;
+  lay.depth = a.stack_depth;
   const bool stored = store != nullptr;
   const void *k = adjoint_kernel(friends, stored);
   if (smem > 48 * 1024) {
@@ -709,3 +734,5 @@ int phs_adjoint_blocks_per_sm(int max_visits, int max_pops, int stack_depth, boo
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, PHS_ADJ_BLOCK, smem);
   return n > 0 ? n : 1;
 }
+
+PHS_CHECK_COLLECTOR(phs_check_collect_adjoint)

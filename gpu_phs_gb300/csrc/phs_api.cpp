@@ -206,6 +206,13 @@ int attach_segments(Segments &S, PhsLaunch &a, cudaStream_t stream) {
   a.n_segments = (int32_t)S.host.size();
   a.n_tiles = S.n_tiles;
   a.n_chunks = S.n_chunks;
+  // the arrays' extents as the segments address them (the checked build's bounds)
+  a.x_len = a.p_len = a.ev_len = 0;
+  for (const PhsSegment &g : S.host) {
+    a.x_len = std::max(a.x_len, g.x_base + g.ev_count * g.x_stride);
+    a.p_len = std::max(a.p_len, g.p_base + g.ev_count * 4 * (int64_t)g.n_out);
+    a.ev_len = std::max(a.ev_len, g.ev_begin + g.ev_count);
+  }
   a.segments = nullptr;
   if (int rc = S.work.reserve(2 * sizeof(unsigned long long))) return rc;
   a.work = S.work.as<unsigned long long>();
@@ -396,6 +403,40 @@ extern "C" int phs_set_device_allocator(phs_device_alloc_fn alloc, phs_device_fr
   g_alloc.free = free_fn;
   g_alloc.user = user;
   return PHS_OK;
+}
+
+extern "C" int phs_is_checked_build(void) {
+#ifdef PHS_CHECKED
+  return 1;
+#else
+  return 0;
+#endif
+}
+
+extern "C" int phs_check_status(uint64_t *sites, int64_t *first_index) {
+  return guarded([&]() -> int {
+    if (!sites) return fail(PHS_ERR_INVALID_ARG, "null sites pointer");
+    *sites = 0;
+    if (first_index) *first_index = 0;
+    if (!phs_is_checked_build())
+      return fail(PHS_ERR_UNSUPPORTED, "bounds checks are compiled into libgpuphs_checked.so only");
+    cudaError_t (*collect[])(unsigned long long *, long long *) = {
+        phs_check_collect_kernels, phs_check_collect_ff, phs_check_collect_adjoint,
+        phs_check_collect_inverse, phs_check_collect_grid};
+    CUDA_TRY(cudaDeviceSynchronize());
+    bool have_first = false;
+    for (auto fn : collect) {
+      unsigned long long w = 0;
+      long long f = 0;
+      CUDA_TRY(fn(&w, &f));
+      if (w && !have_first && first_index) {
+        *first_index = f;
+        have_first = true;
+      }
+      *sites |= w;
+    }
+    return PHS_OK;
+  });
 }
 
 // -------------------------------------------------------------------------- process
@@ -761,6 +802,7 @@ static int launch_process(phs_process_t h, Segments &S, int64_t n_events, const 
   a.factor_stride = fstride;
   a.E1 = E1;
   a.E2 = E2;
+  a.n_programs = h->p.n_channels;
   // segment events are numbered from ev0 within this launch's output arrays
   for (auto &g : S.host) g.ev_begin -= ev0;
   if ((rc = attach_segments(S, a, stream))) return rc;
@@ -837,6 +879,8 @@ extern "C" int phs_adjoint_device(phs_process_t h, int64_t n_events, const int64
     a.channels = h->d_prog.as<PhsChannel>();
     a.stack_depth = h->stack_depth;
     a.x = x;
+    a.factor_stride = 1;
+    a.n_programs = h->p.n_channels;
     if ((rc = attach_segments(h->segs, a, (cudaStream_t)stream))) return rc;
     if (a.n_tiles == 0) return PHS_OK;
     const bool stored = h->adjoint_storage == PHS_ADJOINT_STORED;
@@ -1138,6 +1182,7 @@ extern "C" int phs_batch_generate_device(phs_batch_t b, const int64_t *counts, c
     a.volume = v;
     a.ok = ok;
     a.factor_stride = 1;
+    a.n_programs = n;
     if ((rc = attach_segments(b->segs, a, (cudaStream_t)stream))) return rc;
     if (a.n_tiles == 0) return PHS_OK;
     if (b->precision == PHS_PRECISION_F32X2)
@@ -1251,6 +1296,10 @@ extern "C" int phs_generate_device_noalloc(phs_process_t h, double E1, double E2
     a.volume = v;
     a.ok = ok;
     a.factor_stride = 1;
+    a.n_programs = P.n_channels;
+    a.x_len = n_events * P.n_x;
+    a.p_len = n_events * 4 * (int64_t)P.n_out;
+    a.ev_len = n_events;
     if (S.host.size() <= PHS_INLINE_SEGS) std::copy(S.host.begin(), S.host.end(), a.seg_inline);
     const int grid = a.n_tiles > 0 ? grid_for(a.n_tiles, h->device, depth, false, 0) : 1;
     cudaError_t e = phs_launch_forward_f64_noalloc(a, prog.data(), P.n_channels, S.host.data(),

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "phs_check.h"
 #include "phs_program.h"
 
 #define PHS_INLINE_SEGS 64
@@ -41,6 +42,10 @@ struct PhsLaunch {
   unsigned int *pass_count;
   int64_t *pass_tile;
   int32_t *pass_queue;
+  // extents for the checked build's bounds checks (phs_check.h): elements of x and p,
+  // entries of volume and ok (factor: ev_len * factor_stride), channel programs
+  int64_t x_len, p_len, ev_len;
+  int32_t n_programs;
 };
 
 // Block size and resident blocks per SM of the forward kernel.

@@ -267,10 +267,31 @@ __device__ __forceinline__ double stack_load(const double *smem, int depth, int 
 // One event: segment `seg`, local index `local` (< seg.ev_count).  smem is this block's
 // frame stack, PHS_STATE * stack_depth doubles per thread of a BLOCK-thread block; trig the
 // block's table of sincos2pi_tab.
+// Checked build (phs_check.h): the event's channel, its whole x row, momentum row and event
+// entries, and its program's visit count, before anything is read or written.
+__device__ __forceinline__ bool event_in_bounds(const PhsLaunch &a, const PhsSegment &seg,
+                                                int64_t local, int n_out, int n_visits) {
+  const int64_t xrow = seg.x_base + local * seg.x_stride;
+  const int64_t prow = seg.p_base + local * 4 * (int64_t)n_out;
+  const int64_t ev = seg.ev_begin + local;
+  return phs_in(local, seg.ev_count, PHS_CHK_EVENT) && phs_in(xrow, a.x_len, PHS_CHK_X) &&
+         phs_in(xrow + seg.x_stride - 1, a.x_len, PHS_CHK_X) && phs_in(prow, a.p_len, PHS_CHK_P) &&
+         phs_in(prow + 4 * (int64_t)n_out - 1, a.p_len, PHS_CHK_P) &&
+         phs_in(ev, a.ev_len, PHS_CHK_EVENT) && phs_in(seg.factor_col, a.factor_stride, PHS_CHK_EVENT) &&
+         phs_in(n_visits - 1, PHS_MAX_VISITS, PHS_CHK_VISITS);
+}
+
+// x[k] of an event row (checked build: k within the row; 0 otherwise).
+__device__ __forceinline__ double xrow_at(const double *xe, int k, int stride) {
+  return phs_in(k, stride, PHS_CHK_X) ? xe[k] : 0.0;
+}
+
 template <bool PER_EVENT, int BLOCK = PHS_FWD_BLOCK>
 __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegment &seg,
                                               int64_t local, double *smem, const double2 *trig) {
+  if (!phs_in(seg.channel, a.n_programs, PHS_CHK_CHANNEL)) return;
   const PhsChannel &ch = a.channels[seg.channel];
+  if (!event_in_bounds(a, seg, local, ch.n_out, ch.n_visits)) return;
   const int64_t ev = seg.ev_begin + local;
   const double *xe = a.x + seg.x_base + local * seg.x_stride;
   double *out = a.p + seg.p_base + local * 4 * (int64_t)ch.n_out;
@@ -319,7 +340,8 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
         cmax[j] = C.m_max;
         if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, a0, a1, a2, mn, mx, cmax[j]);
         double f;
-        map_msq(C.map_id, xe[C.x_msq], s, C.m, C.w, mn, mx, a0, a1, a2, cmsq[j], f);
+        map_msq(C.map_id, xrow_at(xe, C.x_msq, seg.x_stride), s, C.m, C.w, mn, mx, a0, a1, a2,
+                cmsq[j], f);
         factor *= f;
         cm[j] = sqrt(cmsq[j]);
       }
@@ -343,14 +365,14 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
     const double bg = p_b * rm;
     const double ga = V.self_root ? 1.0 : E_b * rm;
     double sphi, cphi;
-    sincos2pi_tab(xe[V.x_phi], trig, sphi, cphi);
+    sincos2pi_tab(xrow_at(xe, V.x_phi, seg.x_stride), trig, sphi, cphi);
     double b0 = V.b0, b1 = V.b1;
     if (PER_EVENT && V.ct_class == PHS_CT_COLLINEAR) {
       b0 = dmul(V.m, V.m) / s;
       b1 = log(dadd(b0, 1.0) / b0);
     }
     double ct, st, fct;
-    map_ct(V.ct_class, xe[V.x_ct], b0, b1, ct, st, fct);
+    map_ct(V.ct_class, xrow_at(xe, V.x_ct, seg.x_stride), b0, b1, ct, st, fct);
     factor *= fct;
     const double e01 = -bg * st, e03 = bg * ct, e11 = ct * cphi, e12 = -sphi, e13 = st * cphi;
     const double e21 = ct * sphi, e22 = cphi, e23 = st * sphi, e31 = -ga * st, e33 = ga * ct;
@@ -410,7 +432,7 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
 #pragma unroll
     for (int j = 0; j < 2; j++) {
       const PhsChild &C = V.child[j];
-      if (!C.internal) {
+      if (!C.internal && phs_in(C.out_index, ch.n_out, PHS_CHK_P)) {
         double pj = j == 0 ? pc : -pc;
         const double E = j == 0 ? ce0 : ce1;
         double2 *o = reinterpret_cast<double2 *>(out + 4 * C.out_index);
@@ -421,7 +443,7 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
 
     // next frame: push one internal child, carry the other (or pop)
     // (selects instead of indexing keep the child values in registers)
-    if (V.push >= 0) {
+    if (V.push >= 0 && phs_in(sp, a.stack_depth, PHS_CHK_STACK)) {
       const bool j0 = V.push == 0;
 #pragma unroll
       for (int i = 0; i < 16; i++) stack_store<BLOCK>(smem, sp, i, Ln[i]);
@@ -472,7 +494,9 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
 template <bool PER_EVENT, int BLOCK = PHS_FWD_BLOCK>
 __device__ __forceinline__ bool phs_ok_f64(const PhsLaunch &a, const PhsSegment &seg,
                                            int64_t local, double *smem) {
+  if (!phs_in(seg.channel, a.n_programs, PHS_CHK_CHANNEL)) return false;
   const PhsChannel &ch = a.channels[seg.channel];
+  if (!event_in_bounds(a, seg, local, ch.n_out, ch.n_visits)) return false;
   const int64_t ev = seg.ev_begin + local;
   const double *xe = a.x + seg.x_base + local * seg.x_stride;
   double sqrts = ch.sqrts;
@@ -497,14 +521,15 @@ __device__ __forceinline__ bool phs_ok_f64(const PhsLaunch &a, const PhsSegment 
         cmax[j] = C.m_max;
         if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, a0, a1, a2, mn, mx, cmax[j]);
         double f;
-        map_msq(C.map_id, xe[C.x_msq], s, C.m, C.w, mn, mx, a0, a1, a2, cmsq[j], f);
+        map_msq(C.map_id, xrow_at(xe, C.x_msq, seg.x_stride), s, C.m, C.w, mn, mx, a0, a1, a2,
+                cmsq[j], f);
         cm[j] = sqrt(cmsq[j]);
       }
     }
     const double d = dsub(dsub(msq_b, cmsq[0]), cmsq[1]);
     const double lda = dsub(dmul(d, d), dmul(dmul(4.0, cmsq[0]), cmsq[1]));
     ok = ok && (lda > 0.0) && (m_b > dadd(cm[0], cm[1])) && (m_b <= mmax_b);
-    if (V.push >= 0) {
+    if (V.push >= 0 && phs_in(sp, a.stack_depth, PHS_CHK_STACK)) {
       const bool j0 = V.push == 0;
       stack_store<BLOCK>(smem, sp, 16, j0 ? cmsq[0] : cmsq[1]);
       stack_store<BLOCK>(smem, sp, 17, j0 ? cm[0] : cm[1]);
@@ -619,7 +644,8 @@ __device__ __forceinline__ void compacting_loop(const PhsLaunch &a, int64_t *q, 
         take = qn < 32 ? qn : 32;
       } else if (stage == 1) {
         if (m != 0) {
-          if (passed) q[qn + __popc(m & ((1u << lane) - 1u))] = local;
+          const int slot = qn + __popc(m & ((1u << lane) - 1u));
+          if (passed && phs_in(slot, 64, PHS_CHK_QUEUE)) q[slot] = local;
           qn += __popc(m);
           qseg = cseg;
         }
@@ -630,7 +656,7 @@ __device__ __forceinline__ void compacting_loop(const PhsLaunch &a, int64_t *q, 
         take = 32;
       }
       __syncwarp();
-      const int64_t l = lane < take ? q[qn - take + lane] : -1;
+      const int64_t l = lane < take && phs_in(qn - take + lane, 64, PHS_CHK_QUEUE) ? q[qn - take + lane] : -1;
       __syncwarp();
       qn -= take;
       if (l >= 0) pass_b(qseg, segs[qseg], l);

@@ -32,7 +32,9 @@ __global__ void phs_grid_sample_kernel(double *x, int64_t n_events, int n_x,
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t ev = i / n_x;
     const int d = (int)(i - ev * n_x);
-    const double *w = weights + ((int64_t)channel_of(ch_begin, n_channels, ev) * n_x + d) * PHS_GRID_BINS;
+    const int ch = channel_of(ch_begin, n_channels, ev);
+    if (!phs_in(ch, n_channels, PHS_CHK_GRID)) continue;
+    const double *w = weights + ((int64_t)ch * n_x + d) * PHS_GRID_BINS;
     const double u = x[i];
     double c = 0.0;
     int b = 0;
@@ -74,7 +76,7 @@ __global__ void phs_grid_count_kernel(const double *x, const uint8_t *ok, int64_
         key = c * PHS_GRID_BINS + b;
       }
       const unsigned m = __match_any_sync(0xffffffffu, key);
-      if (key >= 0 && lane == __ffs(m) - 1) {
+      if (key >= 0 && lane == __ffs(m) - 1 && phs_in(key, (int64_t)n_channels * PHS_GRID_BINS, PHS_CHK_GRID)) {
         const int cc = key / PHS_GRID_BINS, b = key % PHS_GRID_BINS;
         atomicAdd(&bins[((int64_t)cc * n_x + d) * PHS_GRID_BINS + b], (unsigned long long)__popc(m));
       }
@@ -127,3 +129,5 @@ cudaError_t phs_launch_grid_update(const double *x, const uint8_t *ok, int64_t n
   phs_grid_normalise_kernel<<<g2, 256, 0, stream>>>(bins, n_ok, n_channels, n_x, weights);
   return cudaGetLastError();
 }
+
+PHS_CHECK_COLLECTOR(phs_check_collect_grid)

@@ -128,11 +128,14 @@ struct InvMomenta {
   double *pm;          // internal sums (and, lab == null, the staged outgoing momenta first)
   const double *lab;   // the event's p row, or null
   int n_out;
+  // checked build: slot j of the 2 n_out - 1 (the root's sum is never formed or read)
   __device__ __forceinline__ double get(int j, int mu) const {
+    if (!phs_in(j, 2 * n_out - 2, PHS_CHK_SLOT)) return 0.0;
     if (lab) return j < n_out ? __ldg(lab + 4 * j + mu) : pm[(4 * (j - n_out) + mu) * PHS_INV_BLOCK];
     return pm[(4 * j + mu) * PHS_INV_BLOCK];
   }
   __device__ __forceinline__ void set_internal(int j, int mu, double v) const {
+    if (!phs_in(j - n_out, n_out - 2, PHS_CHK_SLOT)) return;
     pm[(4 * (lab ? j - n_out : j) + mu) * PHS_INV_BLOCK] = v;
   }
 };
@@ -145,7 +148,7 @@ struct InvMomenta {
 // where 1 - cos^2 cancels) and for soft daughters of fast branches, and there any other
 // rounding order moves the result by far more than the input's own rounding does.
 __device__ void inverse_geometry(const PhsChannel &ch, const InvMomenta &pm, double sqrts,
-                                 double *stk, double *geo) {
+                                 double *stk, double *geo, int stack_depth) {
   const double s = sqrts * sqrts;
   // internal momenta as sums of their daughters in post-order (_combine_particles,
   // phs.cu:1262-1283); the root's (the last) is never a daughter
@@ -249,7 +252,7 @@ __device__ void inverse_geometry(const PhsChannel &ch, const InvMomenta &pm, dou
     const double st = sqrt(1.0 - ct * ct);
     double sph, cph;
     sincos(phi, &sph, &cph);
-    if (V.push >= 0) {
+    if (V.push >= 0 && phs_in(sp, stack_depth, PHS_CHK_STACK)) {
       const bool j0 = V.push == 0;
 #pragma unroll
       for (int i = 0; i < 16; i++) inv_store(stk, sp, i, G[i]);
@@ -286,7 +289,7 @@ __device__ void inverse_geometry(const PhsChannel &ch, const InvMomenta &pm, dou
 // them) but write nothing.
 template <bool PER_EVENT>
 __device__ double inverse_maps(const PhsChannel &ch, double sqrts, const double *geo,
-                               double *cache, double *xr, uint64_t reuse) {
+                               double *cache, double *xr, uint64_t reuse, int n_x) {
   const double s = sqrts * sqrts;
   double factor = 1.0;
   const int n_visits = ch.n_visits;
@@ -312,12 +315,12 @@ __device__ double inverse_maps(const PhsChannel &ch, double sqrts, const double 
             slot[PHS_INV_BLOCK] = f;
           }
         }
-        if (xr) xr[C.x_msq] = x;
+        if (xr && phs_in(C.x_msq, n_x, PHS_CHK_INV)) xr[C.x_msq] = x;
         factor *= f;
       }
     }
     factor *= geo[(PHS_INV_GEO * v + 4) * PHS_INV_BLOCK];  // sqrt(lambda) / msq
-    if (xr) xr[V.x_phi] = geo[(PHS_INV_GEO * v + 3) * PHS_INV_BLOCK];
+    if (xr && phs_in(V.x_phi, n_x, PHS_CHK_INV)) xr[V.x_phi] = geo[(PHS_INV_GEO * v + 3) * PHS_INV_BLOCK];
     double *slot = cache ? cache + (PHS_INV_CACHE * v + 4) * PHS_INV_BLOCK : nullptr;
     double x, f;
     if (reuse >> (3 * v + 2) & 1) {
@@ -335,7 +338,7 @@ __device__ double inverse_maps(const PhsChannel &ch, double sqrts, const double 
         slot[PHS_INV_BLOCK] = f;
       }
     }
-    if (xr) xr[V.x_ct] = x;
+    if (xr && phs_in(V.x_ct, n_x, PHS_CHK_INV)) xr[V.x_ct] = x;
     factor *= f;
   }
   return factor;
@@ -383,7 +386,10 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
       own = lo;
       ok = a.ok ? a.ok[ev] != 0 : true;
       const double *xo = a.x_own ? a.x_own + ev * a.n_x : nullptr;
-      for (int c = 0; c < (a.write_fixed ? a.n_channels : 0); c++) {
+      // (checked build: a row beyond x_out's events writes nothing; no early exit, the
+      // block's barriers below must be reached by every thread)
+      const bool rows_in = phs_in(ev, a.x_ch_stride, PHS_CHK_INV);
+      for (int c = 0; c < (a.write_fixed && rows_in ? a.n_channels : 0); c++) {
         double *xr = a.x_out + ((int64_t)c * a.x_ch_stride + ev) * a.n_x;
         double *fo = a.all_factors + ev * a.n_channels + c;
         if (c == own && xo) {
@@ -412,8 +418,10 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
     }
     if (ok) {
       const int d = queued + before + __popc(m & ((1u << lane) - 1u));
-      q_ev[d] = ev;
-      q_own[d] = own;
+      if (phs_in(d, 2 * PHS_INV_BLOCK, PHS_CHK_SLOT)) {
+        q_ev[d] = ev;
+        q_own[d] = own;
+      }
     }
     queued += n_ok;
     __syncthreads();  // the queue is complete; warp_ok is read
@@ -423,7 +431,8 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
     }
     const int n_walk = min(queued, PHS_INV_BLOCK);
     // 3. every other channel of the tid-th queued event
-    if (tid < n_walk) {
+    if (tid < n_walk && phs_in(q_ev[tid], a.n_events, PHS_CHK_SLOT) &&
+        phs_in(q_ev[tid], a.x_ch_stride, PHS_CHK_INV)) {
       const int64_t e = q_ev[tid];
       const int own_e = q_own[tid];
       double sqrts = ch0.sqrts, lab_bg = ch0.lab ? ch0.lab_bg : 0.0;
@@ -454,9 +463,18 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
         const int gb = a.group_begin[g], ge = a.group_begin[g + 1];
         const int lo = max(gb, a.order_lo), hi = min(ge, a.order_hi);
         if (lo >= hi || (has_own && hi - lo == 1 && a.group_order[lo] == own_e)) continue;
-        inverse_geometry(a.channels[a.group_order[gb]], mom, sqrts, stk, geo + tid);
+        // checked build: the group's entries, its shape's program and the regions sized for it
+        if (!phs_in(gb, a.n_channels, PHS_CHK_SLOT) || !phs_in(hi - 1, a.n_channels, PHS_CHK_SLOT) ||
+            !phs_in(a.group_order[gb], a.n_channels, PHS_CHK_CHANNEL) ||
+            !phs_in(a.channels[a.group_order[gb]].n_visits - 1, a.max_visits, PHS_CHK_VISITS) ||
+            !phs_in(a.channels[a.group_order[gb]].n_out - 1, a.n_out, PHS_CHK_SLOT))
+          continue;
+        inverse_geometry(a.channels[a.group_order[gb]], mom, sqrts, stk, geo + tid, a.stack_depth);
         for (int i = lo; i < hi; i++) {
           const int c = a.group_order[i];
+          if (!phs_in(c, a.n_channels, PHS_CHK_CHANNEL) ||
+              !phs_in(a.channels[c].n_visits - 1, a.max_visits, PHS_CHK_VISITS))
+            continue;
           // the generating channel keeps its own row, but its mappings still run when a
           // later channel of the shape reuses them
           const bool own_row = c == own_e && has_own;
@@ -465,7 +483,7 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
           // the first channel of a shape (or of the slice) computes every mapping
           const uint64_t reuse = i == lo || !cache ? 0ull : a.group_reuse[i];
           const double fac = inverse_maps<PER_EVENT>(a.channels[c], sqrts, geo + tid,
-                                                     cache ? cache + tid : nullptr, xr, reuse);
+                                                     cache ? cache + tid : nullptr, xr, reuse, a.n_x);
           if (!own_row) a.all_factors[e * a.n_channels + c] = fac;
         }
       }
@@ -475,7 +493,7 @@ __global__ void __launch_bounds__(PHS_INV_BLOCK)
     const int rest = queued - n_walk;
     int64_t e_rest = 0;
     int o_rest = 0;
-    if (tid < rest) {
+    if (tid < rest && phs_in(PHS_INV_BLOCK + tid, 2 * PHS_INV_BLOCK, PHS_CHK_SLOT)) {
       e_rest = q_ev[PHS_INV_BLOCK + tid];
       o_rest = q_own[PHS_INV_BLOCK + tid];
     }
@@ -541,3 +559,5 @@ cudaError_t phs_launch_inverse(const PhsInvLaunch &a, int n_blocks, cudaStream_t
     phs_inverse_kernel<false, false><<<n_blocks, PHS_INV_BLOCK, smem, stream>>>(a);
   return cudaGetLastError();
 }
+
+PHS_CHECK_COLLECTOR(phs_check_collect_inverse)

@@ -96,6 +96,10 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, 4)
     const PhsSegment seg = segs[lo];
     const int64_t idx = (t - a.exact_tile[lo]) * 32 + lane;
     if (idx >= (int64_t)a.exact_count[lo]) continue;
+    // the queue slot lies in the segment's run of a.n_tiles * 32 entries, the event in the segment
+    if (!phs_in(idx, seg.ev_count, PHS_CHK_QUEUE) ||
+        !phs_in(seg.tile_begin * 32 + idx, a.n_tiles * 32, PHS_CHK_QUEUE))
+      continue;
     phs_event_f64<PER_EVENT>(a, seg, a.exact_queue[seg.tile_begin * 32 + idx], smem, trig);
   }
 }
@@ -129,6 +133,9 @@ __global__ void __launch_bounds__(BLOCK, MIN_BLOCKS)
     const PhsSegment seg = segs[lo];
     const int64_t idx = (t - a.pass_tile[lo]) * 32 + lane;
     if (idx >= (int64_t)a.pass_count[lo]) continue;
+    if (!phs_in(idx, seg.ev_count, PHS_CHK_QUEUE) ||
+        !phs_in(seg.tile_begin * 32 + idx, a.n_tiles * 32, PHS_CHK_QUEUE))
+      continue;
     phs_event_f64<false, BLOCK>(a, seg, a.pass_queue[seg.tile_begin * 32 + idx], smem, trig);
   }
 }
@@ -433,3 +440,5 @@ cudaError_t phs_launch_forward_f64_noalloc(PhsLaunch a, const PhsChannel *channe
   phs_forward_f64_kernel<false, false, 4><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
   return cudaGetLastError();
 }
+
+PHS_CHECK_COLLECTOR(phs_check_collect_kernels)

@@ -126,7 +126,6 @@ __device__ __forceinline__ bool map_msq_ff(const PhsChildFF &C, const ChildVar &
   return false;
 }
 
-__device__ __forceinline__ ff ldx(const double *xe, int i) { return ff_from_double_int(xe[i]); }
 __device__ __forceinline__ ff ff_twice(ff a) { return ff_make(f_add(a.hi, a.hi), f_add(a.lo, a.lo)); }
 __device__ __forceinline__ ff ff_half(ff a) { return ff_make(f_mul(a.hi, 0.5f), f_mul(a.lo, 0.5f)); }
 
@@ -137,8 +136,10 @@ __device__ __forceinline__ ff ff_half(ff a) { return ff_make(f_mul(a.hi, 0.5f), 
 template <bool PER_EVENT = false>
 __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegment &seg,
                                              int64_t local, const FFTables &T, float *fst) {
+  if (!phs_in(seg.channel, a.n_programs, PHS_CHK_CHANNEL)) return true;
   const PhsChannelFF &ch = a.channels_ff[seg.channel];
   if (ch.exact_only) return false;
+  if (!event_in_bounds(a, seg, local, ch.n_out, ch.n_visits)) return true;
   const int64_t ev = seg.ev_begin + local;
   const double *xe = a.x + seg.x_base + local * seg.x_stride;
   // the walk reads the row's x one visit at a time, each index from the program: fetch the
@@ -196,7 +197,7 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
         const ChildVar cv = PER_EVENT
             ? child_var(C, a.channels[seg.channel].visit[v].child[j], sqrts64, a.channels[seg.channel].m_tot)
             : child_var(C);
-        if (!map_msq_ff(C, cv, xe[C.x_msq], T, cmsq[j], f)) return false;
+        if (!map_msq_ff(C, cv, xrow_at(xe, C.x_msq, seg.x_stride), T, cmsq[j], f)) return false;
         factor = ff_mul(factor, f);
         if (msq_near_zero(cmsq[j], s_scale)) return false;
         if (cmsq[j].hi < 0.0f) {  // the reference takes sqrt of a negative: not ok
@@ -232,8 +233,8 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
     const ff bg = ff_mul(p_b, rm);
     const ff ga = ff_sqrt_fast(ff_add_f(ff_sqr(bg), 1.0f));
     ff sphi, cphi;
-    ff_sincos2pi(ldx(xe, V.x_phi), T, sphi, cphi);
-    const double xctd = xe[V.x_ct];
+    ff_sincos2pi(ff_from_double_int(xrow_at(xe, V.x_phi, seg.x_stride)), T, sphi, cphi);
+    const double xctd = xrow_at(xe, V.x_ct, seg.x_stride);
     const ff xct = ff_from_double_int(xctd);
     ff ct, st, fct;
     if (V.ct_class == PHS_CT_COLLINEAR) {
@@ -291,7 +292,7 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
 #pragma unroll
     for (int j = 0; j < 2; j++) {
       const PhsChildFF &C = V.child[j];
-      if (!C.internal) {
+      if (!C.internal && phs_in(C.out_index, ch.n_out, PHS_CHK_P)) {
         const ff pj = j == 0 ? pc : ff_neg(pc);
         const ff E = ff_sqrt_fast(ff_add(cmsq[j], ff_sqr(pj)));
         double2 *o = reinterpret_cast<double2 *>(out + 4 * C.out_index);
@@ -303,7 +304,7 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
       }
     }
 
-    if (V.push >= 0) {
+    if (V.push >= 0 && phs_in(sp, a.stack_depth, PHS_CHK_STACK)) {
       const bool j0 = V.push == 0;
 #pragma unroll
       for (int i = 0; i < 16; i++) fstack_store(fst, sp, i, L[i]);
@@ -389,9 +390,12 @@ __device__ __forceinline__ float msq_f32(int map_id, float4 c, float c4, float c
 // Queues event `local` of segment si for the exact FP64 launch (each event at most once,
 // so the slot stays below the segment's event count).
 __device__ __forceinline__ void queue_exact(const PhsLaunch &a, int si, int64_t local) {
+  if (!phs_in(si, a.n_segments, PHS_CHK_SEGMENT)) return;
   const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
   const unsigned slot = atomicAdd(a.exact_count + si, 1u);
-  a.exact_queue[segs[si].tile_begin * 32 + slot] = (int32_t)local;
+  if (phs_in(slot, segs[si].ev_count, PHS_CHK_QUEUE) &&
+      phs_in(segs[si].tile_begin * 32 + slot, a.n_tiles * 32, PHS_CHK_QUEUE))
+    a.exact_queue[segs[si].tile_begin * 32 + slot] = (int32_t)local;
 }
 
 // The reduction tables of the float-float functions, built per block in shared memory,
@@ -465,8 +469,10 @@ struct RegBounds {
 template <class Bounds>
 __device__ __forceinline__ bool phs_ok_f32(const PhsLaunch &a, const PhsSegment &seg,
                                            int64_t local, Bounds &stack) {
+  if (!phs_in(seg.channel, a.n_programs, PHS_CHK_CHANNEL)) return true;
   const PhsChannelFF &ch = a.channels_ff[seg.channel];
   if (ch.exact_only) return true;
+  if (!event_in_bounds(a, seg, local, ch.n_out, ch.n_visits)) return true;
   const double *xe = a.x + seg.x_base + local * seg.x_stride;
   const float up = 1.0f + 1e-6f, dn = 1.0f - 1e-6f;
   float mlo_b = ch.sqrts.hi * dn, mhi_b = ch.sqrts.hi * up, mmax_b = ch.sqrts.hi;
@@ -488,8 +494,9 @@ __device__ __forceinline__ bool phs_ok_f32(const PhsLaunch &a, const PhsSegment 
         cmax[j] = 0.0f;
       } else {
         float e;
+        const int xi = (code >> 8) & 255;
         const float msq = msq_f32((code >> 1) & 127, A[j], B[j].x, B[j].y,
-                                  ld_x_narrow(xe + ((code >> 8) & 255)), e);
+                                  phs_in(xi, seg.x_stride, PHS_CHK_X) ? ld_x_narrow(xe + xi) : 0.0, e);
         fails = fails || msq + e < 0.0f;                // negative for certain: not ok
         lo[j] = sqrtf(fmaxf(msq - e, 0.0f)) * dn;       // NaN bounds decide nothing
         hi[j] = sqrtf(fmaxf(msq + e, 0.0f)) * up;
@@ -499,7 +506,7 @@ __device__ __forceinline__ bool phs_ok_f32(const PhsLaunch &a, const PhsSegment 
     fails = fails || mhi_b < (lo[0] + lo[1]) * dn;     // below threshold for certain
     const int push = ((code0 >> 16) & 3) - 1, carry = ((code0 >> 18) & 3) - 1;
     if (!((code0 >> 20) & 1)) fails = fails || mlo_b > mmax_b * up;  // above the bound for certain
-    if (push >= 0) {
+    if (push >= 0 && phs_in(sp, a.stack_depth, PHS_CHK_STACK)) {
       const bool j0 = push == 0;
       stack.push(sp, j0 ? lo[0] : lo[1], j0 ? hi[0] : hi[1], j0 ? cmax[0] : cmax[1]);
       sp++;
@@ -520,6 +527,9 @@ __device__ __forceinline__ bool phs_ok_f32(const PhsLaunch &a, const PhsSegment 
 // The outputs of an event that fails the kinematic test (as the walk writes them).
 __device__ __forceinline__ void write_failed_event(const PhsLaunch &a, const PhsSegment &seg,
                                                    int64_t local) {
+  if (!phs_in(seg.channel, a.n_programs, PHS_CHK_CHANNEL) ||
+      !event_in_bounds(a, seg, local, seg.n_out, 1))
+    return;
   const int64_t ev = seg.ev_begin + local;
   a.volume[ev] = a.channels_ff[seg.channel].volume;
   a.factor[ev * a.factor_stride + seg.factor_col] = 0.0;
@@ -538,6 +548,11 @@ __device__ __forceinline__ void write_failed_tile(const PhsLaunch &a, const PhsS
                                                   int64_t local0, unsigned failed,
                                                   unsigned valid) {
   const int lane = threadIdx.x & 31;
+  // checked build: the tile's first and last valid event and the channel
+  if (!phs_in(seg.channel, a.n_programs, PHS_CHK_CHANNEL) ||
+      !event_in_bounds(a, seg, local0, seg.n_out, 1) ||
+      !event_in_bounds(a, seg, local0 + 31 - __clz(valid), seg.n_out, 1))
+    return;
   if (valid >> lane & 1) {
     const int64_t ev = seg.ev_begin + local0 + lane;
     a.volume[ev] = a.channels_ff[seg.channel].volume;
@@ -639,7 +654,8 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, PHS_FF_TEST_MIN_BLOCKS)
       const unsigned m = __ballot_sync(0xffffffffu, pass);
       const unsigned failed = __ballot_sync(0xffffffffu, valid && !pass);
       const unsigned in_seg = __ballot_sync(0xffffffffu, valid);
-      if (pass) buf[n_pass + __popc(m & ((1u << lane) - 1u))] = (int32_t)local;
+      const int slot = n_pass + __popc(m & ((1u << lane) - 1u));
+      if (pass && phs_in(slot, PHS_CHUNK_TILES * 32, PHS_CHK_QUEUE)) buf[slot] = (int32_t)local;
       n_pass += __popc(m);
       if (failed) write_failed_tile(a, seg, local0, failed, in_seg);
     }
@@ -650,7 +666,10 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, PHS_FF_TEST_MIN_BLOCKS)
       base = __shfl_sync(0xffffffffu, base, 0);
       // base + n_pass <= ev_count: at most ev_count events of the segment pass
       int32_t *dst = a.pass_queue + seg.tile_begin * 32 + base;
-      for (int i = lane; i < n_pass; i += 32) dst[i] = buf[i];
+      if (phs_in(base + n_pass - 1, seg.ev_count, PHS_CHK_QUEUE) &&
+          phs_in(seg.tile_begin * 32 + base + n_pass - 1, a.n_tiles * 32, PHS_CHK_QUEUE) &&
+          phs_in(n_pass - 1, PHS_CHUNK_TILES * 32, PHS_CHK_QUEUE))
+        for (int i = lane; i < n_pass; i += 32) dst[i] = buf[i];
     }
     __syncwarp();
   }
@@ -715,6 +734,9 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
     const PhsSegment &seg = segs[lo];
     const int64_t idx = (t - a.pass_tile[lo]) * 32 + lane;
     if (idx >= (int64_t)a.pass_count[lo]) continue;
+    if (!phs_in(idx, seg.ev_count, PHS_CHK_QUEUE) ||
+        !phs_in(seg.tile_begin * 32 + idx, a.n_tiles * 32, PHS_CHK_QUEUE))
+      continue;
     const int64_t local = a.pass_queue[seg.tile_begin * 32 + idx];
     if (!phs_event_ff(a, seg, local, T, fst)) {
       queue_exact(a, lo, local);
@@ -805,3 +827,5 @@ cudaError_t phs_launch_forward_ff(const PhsLaunch &a, int n_blocks, int variant,
   }
   return cudaGetLastError();
 }
+
+PHS_CHECK_COLLECTOR(phs_check_collect_ff)

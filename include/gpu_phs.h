@@ -77,6 +77,20 @@ const char *phs_version(void);
  * Returns PHS_ERR_INVALID_ARG if only one of the two is given.  No counterpart in the
  * reference, which allocates and frees its device memory inside every generate call
  * (phs.cu:1338-1426, 1604-1635). */
+/* The bounds-checked build.  libgpuphs_checked.so is this library compiled with
+ * -DPHS_CHECKED: every index its kernels compute from run-time data (programs, segment
+ * tables, queues, event rows, stack depths) is compared with the extent of the array it
+ * addresses before the access; an index out of range is not used (a read gives 0, a write
+ * is dropped), and its site is recorded.  phs_check_status waits for the device, returns
+ * the sites recorded since its last call as a bit mask (bit numbers: PhsCheckSite in the
+ * library's phs_check.h: 0 channel, 1 x, 2 momenta, 3 event arrays, 4 frame stack, 5 visit
+ * count, 6 queue slot, 7 segment, 8 adjoint arrays, 9 stored frames, 10 inverse outputs,
+ * 11 inverse slots and queues, 12 grid) and the first offending index, and clears them.
+ * In libgpuphs.so the checks are not compiled in: phs_is_checked_build() returns 0 and
+ * phs_check_status PHS_ERR_UNSUPPORTED.  No counterpart in the reference. */
+int phs_is_checked_build(void);
+int phs_check_status(uint64_t *sites, int64_t *first_index);
+
 typedef int (*phs_device_alloc_fn)(void **ptr, size_t bytes, void *user);
 typedef void (*phs_device_free_fn)(void *ptr, void *user);
 int phs_set_device_allocator(phs_device_alloc_fn alloc, phs_device_free_fn free, void *user);
