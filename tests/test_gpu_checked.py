@@ -5,9 +5,10 @@ memory-safety check of the library on the GPU in place of compute-sanitizer, whi
 available on the GPU pool.
 
 Every case runs through both libraries on the same inputs: the checked build must record
-no out-of-range index (phs_check_status) and give the regular build's outputs bit for bit
-(the checks skip only out-of-range accesses, so equal outputs also show none was
-skipped).  Cases: FP64 one pass, compacting and split forms and the FP32-pair one pass,
+no out-of-range index (phs_check_status; every skipped access records its site) and give
+the regular build's outputs -- bit for bit for the forward, inverse and grid kernels, and
+within 1e-10 of each row's largest entry for the adjoint, whose file is compiled with FMA
+contraction: the checks' branches change which multiply-adds the compiler fuses.  Cases: FP64 one pass, compacting and split forms and the FP32-pair one pass,
 compacting and split forms (with their exact FP64 path) on tt, the 13 TeV tree, a batch
 of random trees with more than 64 segments, Whizard's bwbw channels (friend boosts) with
 uniform, boosted and per-event beams; the adjoint in both storage forms; the inverse map
@@ -61,10 +62,17 @@ def run_both(libs, torch, fn):
     return outs
 
 
-def assert_same(outs, what):
+def assert_same(outs, what, rtol=0.0):
+    """Bit for bit (rtol 0), or floating outputs within rtol of each row's largest entry."""
     a, b = outs
     for i, (u, v) in enumerate(zip(a, b)):
-        assert u.shape == v.shape and bool((u == v).all()), f"{what}: output {i} differs"
+        assert u.shape == v.shape, f"{what}: output {i} shape"
+        if rtol == 0.0 or not v.is_floating_point():
+            assert bool((u == v).all()), f"{what}: output {i} differs"
+            continue
+        scale = v.abs().reshape(v.shape[0], -1).amax(dim=1).clamp(min=1e-300)
+        rel = ((u - v).abs().reshape(v.shape[0], -1).amax(dim=1) / scale).max().item()
+        assert rel <= rtol, f"{what}: output {i} differs by {rel:.2e} of its row scale"
 
 
 def forward_forms(torch, proc, counts, n, E=(500.0, 500.0)):
@@ -165,7 +173,7 @@ def test_adjoint_both_storage_forms(torch, libs):
                 res += list(ps.vjp(x, pbar, jbar))
                 ps.close()
             return res
-        assert_same(run_both(libs, torch, fn), f"adjoint {proc.name}")
+        assert_same(run_both(libs, torch, fn), f"adjoint {proc.name}", rtol=1e-10)
 
 
 def test_inverse_map(torch, libs):
