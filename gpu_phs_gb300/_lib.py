@@ -144,6 +144,8 @@ class using:
         _active = self.prev
 
 
-def check(rc: int) -> None:
+def check(rc: int, lib: C.CDLL = None) -> None:
+    """Raises PhsError for a non-zero status, with the message of `lib` (the library that
+    made the call; default: load())."""
     if rc != 0:
-        raise PhsError(rc, load().phs_last_error().decode())
+        raise PhsError(rc, (lib or load()).phs_last_error().decode())

@@ -44,7 +44,16 @@ ADJOINT_RECOMPUTE = 0  # vjp recovers parent frames with inverse boosts (no scra
 ADJOINT_STORED = 1     # vjp keeps every visit's parent frame in a device buffer
 
 
-class PhaseSpace:
+class _Handle:
+    """A library handle: its calls report errors from the library that made it."""
+
+    _L = None
+
+    def _check(self, rc: int) -> None:
+        check(rc, self._L)
+
+
+class PhaseSpace(_Handle):
     """One process on the current CUDA device."""
 
     def __init__(self, proc: Process, E1: Optional[float] = None, E2: Optional[float] = None):
@@ -57,32 +66,32 @@ class PhaseSpace:
             (proc.flv_widths, np.float64))]
         h = C.c_void_p()
         check(lib.phs_process_create(C.byref(h), proc.n_in, proc.n_out, proc.n_channels,
-                                     proc.n_x, *[_ptr(a) for a in self._keep]))
+                                     proc.n_x, *[_ptr(a) for a in self._keep]), lib)
         self.h = h
         if E1 is not None:
             self.set_beams(E1, E2 if E2 is not None else E1)
 
     def set_beams(self, E1: float, E2: float) -> None:
-        check(self._L.phs_process_set_beams(self.h, float(E1), float(E2)))
+        self._check(self._L.phs_process_set_beams(self.h, float(E1), float(E2)))
 
     def set_precision(self, precision: int) -> None:
         """PRECISION_F64 (default) or PRECISION_F32X2 for the uniform-beam generate calls."""
-        check(self._L.phs_process_set_precision(self.h, int(precision)))
+        self._check(self._L.phs_process_set_precision(self.h, int(precision)))
 
     def set_adjoint_storage(self, storage: int) -> None:
         """ADJOINT_RECOMPUTE (default) or ADJOINT_STORED for vjp (the stored-matrix form,
         kept for comparison: a device buffer of n x max visits x 128 bytes)."""
-        check(self._L.phs_process_set_adjoint_storage(self.h, int(storage)))
+        self._check(self._L.phs_process_set_adjoint_storage(self.h, int(storage)))
 
     def tuning(self):
         """(ff_variant, f64_variant) the autotuner chose (-1: not tuned yet)."""
         f, d = C.c_int(), C.c_int()
-        check(self._L.phs_process_tuning(self.h, C.byref(f), C.byref(d)))
+        self._check(self._L.phs_process_tuning(self.h, C.byref(f), C.byref(d)))
         return f.value, d.value
 
     def set_variants(self, ff_variant: int = -1, f64_variant: int = -1) -> None:
         """Pins the kernel variants (-1: autotune)."""
-        check(self._L.phs_process_set_variants(self.h, int(ff_variant), int(f64_variant)))
+        self._check(self._L.phs_process_set_variants(self.h, int(ff_variant), int(f64_variant)))
 
     def close(self) -> None:
         if getattr(self, "h", None):
@@ -97,7 +106,7 @@ class PhaseSpace:
 
     def info(self):
         v = [C.c_int() for _ in range(5)]
-        check(self._L.phs_process_info(self.h, *[C.byref(i) for i in v]))
+        self._check(self._L.phs_process_info(self.h, *[C.byref(i) for i in v]))
         return dict(zip(("n_in", "n_out", "n_channels", "n_x", "stack_depth"), [i.value for i in v]))
 
     def alloc(self, n: int, device="cuda") -> Events:
@@ -127,7 +136,7 @@ class PhaseSpace:
             raise ValueError(f"x must be [n, {self.proc.n_x}]")
         out = out or self.alloc(n, x.device)
         c = self._counts(counts, self.proc.n_channels, n)
-        check(self._L.phs_generate_device(self.h, n, _ptr(c), _ptr(x), _ptr(out.p),
+        self._check(self._L.phs_generate_device(self.h, n, _ptr(c), _ptr(x), _ptr(out.p),
                                          _ptr(out.factor), _ptr(out.volume), _ptr(out.ok),
                                          _stream(stream)))
         return out
@@ -138,7 +147,7 @@ class PhaseSpace:
         n = int(x.shape[0])
         out = out or self.alloc(n, x.device)
         c = self._counts(counts, self.proc.n_channels, n)
-        check(self._L.phs_generate_beams_device(self.h, n, _ptr(c), _ptr(E1), _ptr(E2), _ptr(x),
+        self._check(self._L.phs_generate_beams_device(self.h, n, _ptr(c), _ptr(E1), _ptr(E2), _ptr(x),
                                                _ptr(out.p), _ptr(out.factor), _ptr(out.volume),
                                                _ptr(out.ok), _stream(stream)))
         return out
@@ -154,7 +163,7 @@ class PhaseSpace:
         c = self._counts(counts, self.proc.n_channels, n)
         pbar = pbar.contiguous()
         jbar = jbar.contiguous() if jbar is not None else None
-        check(self._L.phs_adjoint_device(self.h, n, _ptr(c), _ptr(x), _ptr(pbar), _ptr(jbar),
+        self._check(self._L.phs_adjoint_device(self.h, n, _ptr(c), _ptr(x), _ptr(pbar), _ptr(jbar),
                                         _ptr(xbar), _ptr(thbar), _stream(stream)))
         return xbar, thbar
 
@@ -172,7 +181,7 @@ class PhaseSpace:
         fac = torch.empty((n, nch), dtype=torch.float64, device=p.device)
         xo = torch.empty((nch, n, self.proc.n_x), dtype=torch.float64, device=p.device)
         c = self._counts(counts, nch, n)
-        check(self._L.phs_inverse_device(self.h, n, _ptr(c), _ptr(E1), _ptr(E2), _ptr(p), _ptr(ok),
+        self._check(self._L.phs_inverse_device(self.h, n, _ptr(c), _ptr(E1), _ptr(E2), _ptr(p), _ptr(ok),
                                         _ptr(x), _ptr(factor), _ptr(fac), _ptr(xo),
                                         _stream(stream)))
         return fac, xo
@@ -186,12 +195,12 @@ class PhaseSpace:
                          torch.empty(n, dtype=torch.float64), torch.empty(n, dtype=torch.float64),
                          torch.empty(n, dtype=torch.uint8))
         c = self._counts(counts, self.proc.n_channels, n)
-        check(self._L.phs_generate_host(self.h, n, _ptr(c), _ptr(x), _ptr(out.p), _ptr(out.factor),
+        self._check(self._L.phs_generate_host(self.h, n, _ptr(c), _ptr(x), _ptr(out.p), _ptr(out.factor),
                                        _ptr(out.volume), _ptr(out.ok)))
         return out
 
 
-class Batch:
+class Batch(_Handle):
     """Many processes (uneven n_out, n_x and counts) in one persistent launch."""
 
     def __init__(self, spaces: Sequence[PhaseSpace]):
@@ -199,7 +208,7 @@ class Batch:
         self._L = self.spaces[0]._L if self.spaces else load()
         arr = (C.c_void_p * len(self.spaces))(*[s.h.value for s in self.spaces])
         h = C.c_void_p()
-        check(self._L.phs_batch_create(C.byref(h), len(self.spaces), C.cast(arr, C.c_void_p)))
+        self._check(self._L.phs_batch_create(C.byref(h), len(self.spaces), C.cast(arr, C.c_void_p)))
         self.h = h
         self.n_outs: List[int] = []
         self.n_xs: List[int] = []
@@ -223,21 +232,21 @@ class Batch:
         return len(self.n_outs)
 
     def set_precision(self, precision: int) -> None:
-        check(self._L.phs_batch_set_precision(self.h, int(precision)))
+        self._check(self._L.phs_batch_set_precision(self.h, int(precision)))
 
     def tuning(self):
         f, d = C.c_int(), C.c_int()
-        check(self._L.phs_batch_tuning(self.h, C.byref(f), C.byref(d)))
+        self._check(self._L.phs_batch_tuning(self.h, C.byref(f), C.byref(d)))
         return f.value, d.value
 
     def set_variants(self, ff_variant: int = -1, f64_variant: int = -1) -> None:
-        check(self._L.phs_batch_set_variants(self.h, int(ff_variant), int(f64_variant)))
+        self._check(self._L.phs_batch_set_variants(self.h, int(ff_variant), int(f64_variant)))
 
     def offsets(self, counts):
         c = np.ascontiguousarray(counts, np.int64)
         xo = np.zeros(self.n_channels + 1, np.int64)
         po = np.zeros(self.n_channels + 1, np.int64)
-        check(self._L.phs_batch_offsets(self.h, _ptr(c), _ptr(xo), _ptr(po)))
+        self._check(self._L.phs_batch_offsets(self.h, _ptr(c), _ptr(xo), _ptr(po)))
         return xo, po
 
     def generate(self, x, counts, p=None, factor=None, volume=None, ok=None, stream=None):
@@ -251,12 +260,12 @@ class Batch:
         factor = factor if factor is not None else torch.empty(n, dtype=torch.float64, device=dev)
         volume = volume if volume is not None else torch.empty(n, dtype=torch.float64, device=dev)
         ok = ok if ok is not None else torch.empty(n, dtype=torch.uint8, device=dev)
-        check(self._L.phs_batch_generate_device(self.h, _ptr(c), _ptr(x), _ptr(p), _ptr(factor),
+        self._check(self._L.phs_batch_generate_device(self.h, _ptr(c), _ptr(x), _ptr(p), _ptr(factor),
                                                _ptr(volume), _ptr(ok), _stream(stream)))
         return p, factor, volume, ok
 
 
-class Graph:
+class Graph(_Handle):
     """A captured generate call (fixed pointers and counts); launch() replays it."""
 
     def __init__(self, handle, lib=None):
@@ -264,7 +273,7 @@ class Graph:
         self._L = lib or load()
 
     def launch(self, stream=None) -> None:
-        check(self._L.phs_graph_launch(self.h, _stream(stream)))
+        self._check(self._L.phs_graph_launch(self.h, _stream(stream)))
 
     def close(self) -> None:
         if getattr(self, "h", None):
@@ -282,7 +291,7 @@ def batch_graph(batch: "Batch", x, counts, p, factor, volume, ok) -> Graph:
     c = np.ascontiguousarray(counts, np.int64)
     h = C.c_void_p()
     check(batch._L.phs_batch_graph_create(C.byref(h), batch.h, _ptr(c), _ptr(x), _ptr(p),
-                                          _ptr(factor), _ptr(volume), _ptr(ok)))
+                                          _ptr(factor), _ptr(volume), _ptr(ok)), batch._L)
     g = Graph(h, batch._L)
     g._keep = (batch, x, c, p, factor, volume, ok)
     return g
@@ -293,7 +302,7 @@ def process_graph(ps: PhaseSpace, x, out: Events, counts=None) -> Graph:
     c = ps._counts(counts, ps.proc.n_channels, n)
     h = C.c_void_p()
     check(ps._L.phs_process_graph_create(C.byref(h), ps.h, n, _ptr(c), _ptr(x), _ptr(out.p),
-                                         _ptr(out.factor), _ptr(out.volume), _ptr(out.ok)))
+                                         _ptr(out.factor), _ptr(out.volume), _ptr(out.ok)), ps._L)
     g = Graph(h, ps._L)
     g._keep = (ps, x, c, out)
     return g
@@ -302,14 +311,14 @@ def process_graph(ps: PhaseSpace, x, out: Events, counts=None) -> Graph:
 GRID_BINS = 10
 
 
-class Grid:
+class Grid(_Handle):
     """Per-channel x grid of the warm-up (rng.cpp): weights [n_channels, n_x, 10] on the
     device, uniform at first."""
 
     def __init__(self, n_channels: int, n_x: int):
         h = C.c_void_p()
         self._L = load()
-        check(self._L.phs_grid_create(C.byref(h), int(n_channels), int(n_x)))
+        self._check(self._L.phs_grid_create(C.byref(h), int(n_channels), int(n_x)))
         self.h, self.n_channels, self.n_x = h, int(n_channels), int(n_x)
 
     def close(self) -> None:
@@ -337,19 +346,19 @@ class Grid:
         x = out if out is not None else torch.empty((n_events, self.n_x), dtype=torch.float64,
                                                     device="cuda")
         c = self._counts(counts, n_events)
-        check(self._L.phs_grid_sample_device(self.h, int(n_events), _ptr(c), int(seed),
+        self._check(self._L.phs_grid_sample_device(self.h, int(n_events), _ptr(c), int(seed),
                                             int(first_event), _ptr(x), _stream(stream)))
         return x
 
     def update(self, x, ok, counts=None, stream=None) -> None:
         """Weights from the ok events' x (rng.cpp:34-67)."""
         c = self._counts(counts, int(x.shape[0]))
-        check(self._L.phs_grid_update_device(self.h, int(x.shape[0]), _ptr(c), _ptr(x), _ptr(ok),
+        self._check(self._L.phs_grid_update_device(self.h, int(x.shape[0]), _ptr(c), _ptr(x), _ptr(ok),
                                             _stream(stream)))
 
     def weights(self) -> np.ndarray:
         w = np.zeros((self.n_channels, self.n_x, GRID_BINS))
-        check(self._L.phs_grid_weights(self.h, w.ctypes.data))
+        self._check(self._L.phs_grid_weights(self.h, w.ctypes.data))
         return w
 
 
