@@ -56,6 +56,15 @@ def bytes_per_event(proc) -> int:
     return 8 * proc.n_x + 32 * proc.n_out + 8 + 8 + 1
 
 
+def hbm_roofline(total_bytes: float, ms: float, what: str) -> dict:
+    """HBM view of a form: algorithmic bytes of the whole step / its CUDA-event time, against
+    the measured copy bandwidth."""
+    peak, kind = peaks()
+    gbs = total_bytes / (ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+            "peak_kind": kind, "algorithmic_bytes_per_step": total_bytes, "what": what}
+
+
 def flops_per_event(proc) -> float:
     """FP64 operations of the minimal algorithm per event, one convention for all
     workloads: add/sub/mul/div/sqrt = 1, FMA = 2, each transcendental call = 1.  It
@@ -248,6 +257,10 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64, pin=
         "speedup_vs_plain_fp64": t["fp64_one_pass"] / t["fp32_mixed"],
         "speedup_vs_fp64_compacting": t["fp64_compacting"] / t["fp32_mixed"],
         "speedup_vs_fp64_split": t["fp64_split"] / t["fp32_mixed"],
+        "roofline": {k: hbm_roofline(n * bytes_per_event(proc), t[k],
+                                     "x rows read, momenta, factor, volume, ok written "
+                                     f"({bytes_per_event(proc)} B/event)")
+                     for k in ("fp64_split", "fp32_mixed")},
         "ok_fraction": outs["fp64_one_pass"].ok.double().mean().item(),
         "fp64_forms_identical_bits": all(
             torch.equal(getattr(outs["fp64_one_pass"], f), getattr(outs[k], f))
@@ -297,6 +310,7 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64, pin=
         per_channel_mism += int((ev.ok != bufs["fp64_split"][3][e:e + c]).sum().item())
         e += c
     ok64 = bufs["fp64_one_pass"][3]
+    batch_bytes = float(sum(int(c) * bytes_per_event(sp.proc) for sp, c in zip(spaces, counts)))
     res["batched_64ch"] = {
         "n_channels": 64, "n_events": n, "n_out_range": [3, 8],
         "counts": "power law, exponent 1.5, seed 2024",
@@ -308,6 +322,10 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64, pin=
         "speedup_vs_plain_fp64": bres["fp64_one_pass"] / bres["fp32_mixed"],
         "speedup_vs_fp64_compacting": bres["fp64_compacting"] / bres["fp32_mixed"],
         "speedup_vs_fp64_split": bres["fp64_split"] / bres["fp32_mixed"],
+        "roofline": {k: hbm_roofline(batch_bytes, bres[k],
+                                     "per channel: x rows read, momenta, factor, volume, ok "
+                                     "written, summed over the 64 channels' events")
+                     for k in ("fp64_split", "fp32_mixed")},
         "ok_fraction": ok64.double().mean().item(),
         "ok_mismatches_fp32_mixed_vs_fp64": int((ok64 != bufs["fp32_mixed"][3]).sum().item()),
         "fp64_forms_identical_bits": all(
