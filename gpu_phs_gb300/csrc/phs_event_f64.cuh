@@ -11,6 +11,7 @@
 #include <stdint.h>
 
 #include "phs_device.h"
+#include "phs_math.h"
 #include "phs_program.h"
 
 #define PHS_PI 3.14159265358979323846
@@ -183,7 +184,7 @@ __device__ void child_constants(const PhsChild &C, double sqrts, double m_tot, d
       // path computes it) serves every event
       double msq0 = dmul(m, m), mw = dmul(m, w);
       a0 = C.a0;
-      a1 = atan(dsub(msq_max, msq0) / mw);
+      a1 = phs_atan_bw(dsub(msq_max, msq0) / mw);   // argument >= 10^3 here in practice
       a2 = dmul(dsub(a1, a0), mw) / s;
       break;
     }

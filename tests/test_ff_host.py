@@ -73,3 +73,42 @@ def test_integer_conversions_of_float_pairs():
     assert int(n) > 1_900_000
     assert int(bad_to) == 0, f"ff_to_double_int off by more than an ulp ({worst} ulp)"
     assert int(bad_from) == 0 and int(bad_om) == 0
+
+
+ATAN_DRIVER = r"""
+#include <cmath>
+#include <cstdio>
+#include <random>
+#include "phs_math.h"
+int main() {
+  std::mt19937_64 rng(7);
+  std::uniform_real_distribution<double> u(3.0, 13.0);
+  double worst = 0;
+  for (int i = 0; i < 2000000; i++) {
+    const double x = std::pow(10.0, u(rng));          // 10^3 .. 10^13
+    const long double exact = atanl((long double)x);
+    const double got = phs_atan_bw(x);
+    const double ulp = std::nextafter(1.5707963267948966, 0.0) - 1.5707963267948966;
+    const double err = std::fabs((double)((long double)got - exact)) / std::fabs(ulp);
+    if (err > worst) worst = err;
+  }
+  std::printf("%.4f\n", worst);
+  return 0;
+}
+"""
+
+
+def test_atan_of_large_breit_wigner_arguments():
+    """phs_atan_bw: pi/2 - atan(1/u) by three series terms for u >= 1024, within one ulp
+    of atan(u) over 10^3 .. 10^13 (long double reference)."""
+    try:
+        subprocess.run(["g++", "--version"], check=True, capture_output=True)
+    except (OSError, subprocess.CalledProcessError):
+        pytest.skip("g++ not available")
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = os.path.join(d, "at.cpp"), os.path.join(d, "at")
+        with open(src, "w") as fh:
+            fh.write(ATAN_DRIVER)
+        subprocess.run(["g++", "-O2", "-std=c++17", "-I", CSRC, src, "-o", exe], check=True)
+        worst = float(subprocess.run([exe], check=True, capture_output=True, text=True).stdout)
+    assert worst <= 1.0, f"{worst} ulp"
