@@ -1012,7 +1012,24 @@ static int inverse_launch(phs_process_t h, int64_t n_events, const int64_t *d_ch
 
 // Host path: 512 Ki-event chunks rotate over three streams (measured best on GB300: copies in
 // both directions overlap the neighbours' kernels); each stream's buffers are reused only
-// after its previous chunk's copies back have been ordered before the next copy in.
+// after its previous chunk's copies back have been ordered before the next copy in.  The
+// first copy in and the last copies back overlap no kernel, so the chunks ramp up from an
+// eighth of the size at the start and down to an eighth at the end.
+static std::vector<int64_t> host_chunks(int64_t n, int64_t chunk) {
+  const int64_t ramp[3] = {chunk / 8, chunk / 4, chunk / 2};
+  const int64_t ends = 2 * (ramp[0] + ramp[1] + ramp[2]);
+  std::vector<int64_t> out;
+  if (ramp[0] < 1 || n < ends + chunk) {
+    for (int64_t e0 = 0; e0 < n; e0 += chunk) out.push_back(std::min(chunk, n - e0));
+    return out;
+  }
+  out.assign(ramp, ramp + 3);
+  const int64_t mid = n - ends, k = (mid + chunk - 1) / chunk;
+  for (int64_t i = 0; i < k; i++) out.push_back(mid / k + (i < mid % k ? 1 : 0));
+  out.insert(out.end(), {ramp[2], ramp[1], ramp[0]});
+  return out;
+}
+
 extern "C" int phs_generate_host(phs_process_t h, int64_t n_events, const int64_t *counts,
                                  const double *x, double *p, double *f, double *v, uint8_t *ok) {
   PHS_TRACE("phs_generate_host");
@@ -1038,10 +1055,10 @@ extern "C" int phs_generate_host(phs_process_t h, int64_t n_events, const int64_
     if (counts) std::copy(counts, counts + nch, cnt.begin()); else cnt[0] = n_events;
     for (int c = 0; c < nch; c++) prefix[c + 1] = prefix[c] + cnt[c];
     int k = 0;
-    for (int64_t e0 = 0; e0 < n_events; e0 += chunk, k++) {
-      const int s = k % phs_process::kStreams;
+    int64_t e0 = 0;
+    for (const int64_t n : host_chunks(n_events, chunk)) {
+      const int s = k++ % phs_process::kStreams;
       cudaStream_t st = h->streams[s];
-      const int64_t n = std::min(chunk, n_events - e0);
       // this chunk's per-channel counts
       std::vector<int64_t> cc(nch, 0);
       for (int c = 0; c < nch; c++) {
@@ -1059,6 +1076,7 @@ extern "C" int phs_generate_host(phs_process_t h, int64_t n_events, const int64_
       CUDA_TRY(cudaMemcpyAsync(f + e0, h->bf[s].ptr, n * sizeof(double), cudaMemcpyDeviceToHost, st));
       CUDA_TRY(cudaMemcpyAsync(v + e0, h->bv[s].ptr, n * sizeof(double), cudaMemcpyDeviceToHost, st));
       CUDA_TRY(cudaMemcpyAsync(ok + e0, h->bo[s].ptr, n, cudaMemcpyDeviceToHost, st));
+      e0 += n;
     }
     for (int s = 0; s < phs_process::kStreams; s++) CUDA_TRY(cudaStreamSynchronize(h->streams[s]));
     return PHS_OK;
