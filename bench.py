@@ -754,6 +754,21 @@ def run_ours(args):
                "d2h_bytes_per_step": n * (32 * proc.n_out + 8 + 8 + 1),
                "path": "phs_generate_host (C ABI), pinned host buffers, 512 Ki-event chunks on 3 streams",
                "steps": e2e_steps}
+        if world == 1:
+            # the same call with the FP32-mixed form (information: there the host copies,
+            # not the kernel, bound the call)
+            from gpu_phs_gb300.api import PRECISION_F32X2
+            ps_ff = PhaseSpace(proc, proc.sqrts / 2, proc.sqrts / 2)
+            ps_ff.set_precision(PRECISION_F32X2)
+            for _ in range(max(1, min(args.warmup, 3))):
+                ps_ff.generate_host(xh, out=outh)
+            t0 = time.perf_counter()
+            for _ in range(e2e_steps):
+                ps_ff.generate_host(xh, out=outh)
+            el_ff = time.perf_counter() - t0
+            e2e["fp32_mixed"] = {"value": n * e2e_steps / el_ff, "unit": "events/s",
+                                 "path": "phs_generate_host, FP32-mixed precision, same buffers"}
+            ps_ff.close()
 
     # the drop-in call, c_whizard_gen_phs_from_x_gpu, on the same workload with the host
     # arrays Whizard passes (pageable): x in; momenta, volumes, ok flags and, as its forced
