@@ -466,9 +466,12 @@ struct RegBounds {
   }
 };
 
+// staged: the channel's packed visits (PhsChannelFF::test as 4 float4 per visit) staged in
+// shared memory by the caller, or null: read from the channel program in global memory.
 template <class Bounds>
 __device__ __forceinline__ bool phs_ok_f32(const PhsLaunch &a, const PhsSegment &seg,
-                                           int64_t local, Bounds &stack) {
+                                           int64_t local, Bounds &stack,
+                                           const float4 *staged = nullptr) {
   if (!phs_in(seg.channel, a.n_programs, PHS_CHK_CHANNEL)) return true;
   const PhsChannelFF &ch = a.channels_ff[seg.channel];
   if (ch.exact_only) return true;
@@ -481,8 +484,14 @@ __device__ __forceinline__ bool phs_ok_f32(const PhsLaunch &a, const PhsSegment 
   const int n_visits = ch.n_visits;
   for (int v = 0; v < n_visits && !fails; v++) {
     // the visit in four independent 16-byte loads
-    const float4 *q = reinterpret_cast<const float4 *>(ch.test + v);
-    const float4 A[2] = {__ldg(q), __ldg(q + 2)}, B[2] = {__ldg(q + 1), __ldg(q + 3)};
+    float4 A[2], B[2];
+    if (staged) {
+      const float4 *q = staged + 4 * v;
+      A[0] = q[0]; B[0] = q[1]; A[1] = q[2]; B[1] = q[3];
+    } else {
+      const float4 *q = reinterpret_cast<const float4 *>(ch.test + v);
+      A[0] = __ldg(q); B[0] = __ldg(q + 1); A[1] = __ldg(q + 2); B[1] = __ldg(q + 3);
+    }
     const int code0 = __float_as_int(B[0].w);
     float lo[2], hi[2], cmax[2];
 #pragma unroll
@@ -630,8 +639,12 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, MIN_BLOCKS)
 __global__ void __launch_bounds__(PHS_FWD_BLOCK, PHS_FF_TEST_MIN_BLOCKS)
     phs_ff_test_kernel(const __grid_constant__ PhsLaunch a) {
   __shared__ int32_t gathered[PHS_FWD_BLOCK / 32][PHS_CHUNK_TILES * 32];
+  // each warp's chunk is of one channel: its packed visits, staged once per channel change
+  __shared__ float4 visits[PHS_FWD_BLOCK / 32][4 * PHS_MAX_VISITS];
   const int lane = threadIdx.x & 31;
   int32_t *buf = gathered[threadIdx.x >> 5];
+  float4 *prog = visits[threadIdx.x >> 5];
+  int staged_channel = -1;  // warp-uniform
   const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const PhsSegment *segs = a.n_segments <= PHS_INLINE_SEGS ? a.seg_inline : a.segments;
@@ -645,12 +658,21 @@ __global__ void __launch_bounds__(PHS_FWD_BLOCK, PHS_FF_TEST_MIN_BLOCKS)
     const int64_t t0 = (chunk - seg.chunk_begin) * PHS_CHUNK_TILES;
     const int64_t seg_tiles = (seg.ev_count + 31) / 32;
     const int n_t = (int)(seg_tiles - t0 < PHS_CHUNK_TILES ? seg_tiles - t0 : PHS_CHUNK_TILES);
+    if (seg.channel != staged_channel && phs_in(seg.channel, a.n_programs, PHS_CHK_CHANNEL)) {
+      const PhsChannelFF &ch = a.channels_ff[seg.channel];
+      const int nv = ch.n_visits < PHS_MAX_VISITS ? ch.n_visits : PHS_MAX_VISITS;
+      const float4 *src = reinterpret_cast<const float4 *>(ch.test);
+      __syncwarp();
+      for (int i = lane; i < 4 * nv; i += 32) prog[i] = __ldg(src + i);
+      __syncwarp();
+      staged_channel = seg.channel;
+    }
     int n_pass = 0;
     for (int t = 0; t < n_t; t++) {
       const int64_t local0 = (t0 + t) * 32, local = local0 + lane;
       const bool valid = local < seg.ev_count;
       RegBounds st;
-      const bool pass = valid && phs_ok_f32(a, seg, local, st);
+      const bool pass = valid && phs_ok_f32(a, seg, local, st, prog);
       const unsigned m = __ballot_sync(0xffffffffu, pass);
       const unsigned failed = __ballot_sync(0xffffffffu, valid && !pass);
       const unsigned in_seg = __ballot_sync(0xffffffffu, valid);
