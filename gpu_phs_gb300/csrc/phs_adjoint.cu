@@ -41,7 +41,7 @@ namespace {
 
 struct AdjLayout {
   int state0, ang0, der0, pop0, stack0;  // offsets (in slots) of the per-thread regions
-  int trig0;                             // the block's sin/cos table (2 slots)
+  int trig0;                             // the block's sin/cos table (8 slots)
   int fr0;                               // friend visits: the rotation axis, 3 per visit
   int nv, npops, depth;                  // visits, pop frames and stack depth the regions hold
 };
@@ -676,7 +676,9 @@ void phs_adjoint_sizes(int max_visits, int max_pops, int stack_depth, bool frien
   *pop0 = *der0 + PHS_ADJ_DER * max_visits;
   *stack0 = *pop0 + 16 * max_pops;
   *trig0 = *stack0 + PHS_STATE * (stack_depth > 0 ? stack_depth : 0);
-  *fr0 = *trig0 + (int)(64 * sizeof(double2) / (PHS_ADJ_BLOCK * sizeof(double)));
+  static_assert(PHS_TRIG_N * sizeof(double2) % (PHS_ADJ_BLOCK * sizeof(double)) == 0,
+                "the sin/cos table fills whole slots");
+  *fr0 = *trig0 + (int)(PHS_TRIG_N * sizeof(double2) / (PHS_ADJ_BLOCK * sizeof(double)));
   const int slots = *fr0 + (friends ? 3 * max_visits : 0);
   *smem = (size_t)slots * PHS_ADJ_BLOCK * sizeof(double);
 }

@@ -223,33 +223,57 @@ __device__ void child_constants(const PhsChild &C, double sqrts, double m_tot, d
   }
 }
 
-// sin and cos of 2 pi x for x in [0, 1]: the nearest multiple k/64 of x from a table,
-// tab[k] = (sin, cos)(2 pi k / 64), and the Taylor series of sine and cosine of the
-// remainder angle t = 2 pi (x - k/64), |t| <= pi/64 (terms through t^9 and t^10: the next
-// ones are below 1e-19), joined by the angle-addition formulas.  Within 2 ulp of
-// sincospi(2x), at about 3/4 of its cost.  x - k/64 is exact (Sterbenz).
+#define PHS_TRIG_N 256   // entries of the sin/cos table: (sin, cos)(2 pi k / 256)
+
+// sin and cos of 2 pi x: the nearest multiple k/256 of x, tab[k] = (sin, cos)(2 pi k / 256)
+// from a table, and the Taylor series of sine and cosine of the remainder angle
+// t = 2 pi (x - k/256), |t| <= pi/256 (terms through t^7 and t^6: the next ones are below
+// 2e-20 of the result), joined by the angle-addition formulas.  Within 2 ulp of
+// sincospi(2x).  x - k/256 is exact (Sterbenz); for 0 <= x < 2 (every x a phi mapping
+// reads) k and the remainder come from the bits of x with integer operations, which keeps
+// the reduction off the FP64 pipe (two FP64 operations: the remainder's conversion and its
+// product with 2 pi), otherwise from rint.
 __device__ __forceinline__ void sincos2pi_tab(double x, const double2 *tab, double &s, double &c) {
-  const double k = rint(x * 64.0);
-  const double t = (x - k * (1.0 / 64.0)) * 6.283185307179586;
+  const long long b = __double_as_longlong(x);
+  const int bexp = (int)(b >> 52);   // biased exponent (b >= 0: the sign bit is clear)
+  double t;
+  int k;
+  if (b >= 0 && bexp <= 1023) {
+    // x = M 2^(e - 52) with the 53-bit significand M; 256 x = M 2^-sh, sh = 44 - e
+    const bool small = bexp < 1023 - 9;   // x < 2^-9: k = 0, t = 2 pi x
+    const int e = small ? -9 : bexp - 1023;
+    const long long M = (b & ((1ll << 52) - 1)) | (1ll << 52);
+    const int sh = 44 - e;                                   // 44 .. 53
+    const int kk = (int)((M + (1ll << (sh - 1))) >> sh);     // round(256 x)
+    const long long r = M - ((long long)kk << sh);           // x - k/256 = r 2^(e - 52)
+    // 2 pi 2^(e - 52): 2 pi with its exponent lowered (a normal number, exact)
+    const double c2 = __longlong_as_double(__double_as_longlong(6.283185307179586) +
+                                           ((long long)(e - 52) << 52));
+    k = small ? 0 : kk;
+    t = (small ? x : (double)r) * (small ? 6.283185307179586 : c2);
+  } else {
+    const double kd = rint(x * (double)PHS_TRIG_N);
+    k = (int)((long long)kd & (PHS_TRIG_N - 1));
+    t = (x - kd * (1.0 / PHS_TRIG_N)) * 6.283185307179586;
+  }
   const double t2 = t * t;
-  const double sr = t + t * t2 * (-1.0 / 6 + t2 * (1.0 / 120 + t2 * (-1.0 / 5040 + t2 * (1.0 / 362880))));
-  const double cr = 1.0 + t2 * (-0.5 + t2 * (1.0 / 24 + t2 * (-1.0 / 720 + t2 * (1.0 / 40320 +
-                                                                               t2 * (-1.0 / 3628800)))));
-  const double2 v = tab[(int)k & 63];
+  const double sr = t + t * t2 * (-1.0 / 6 + t2 * (1.0 / 120 + t2 * (-1.0 / 5040)));
+  const double cr = 1.0 + t2 * (-0.5 + t2 * (1.0 / 24 + t2 * (-1.0 / 720)));
+  const double2 v = tab[k & (PHS_TRIG_N - 1)];
   s = v.x * cr + v.y * sr;
   c = v.y * cr - v.x * sr;
 }
 
-// Fills the 64-entry table of sincos2pi_tab (threads 0..63 of the block; the caller
-// synchronises).  Multiples of pi/2 are exact.
+// Fills the PHS_TRIG_N-entry table of sincos2pi_tab (the block's threads in turn; the
+// caller synchronises).  Multiples of pi/2 are exact.
 __device__ __forceinline__ void fill_trig_table(double2 *tab) {
-  if (threadIdx.x < 64) {
-    const int k = threadIdx.x;
+  for (int k = threadIdx.x; k < PHS_TRIG_N; k += blockDim.x) {
     double sv, cv;
-    sincospi(k / 32.0, &sv, &cv);
-    if (k % 16 == 0) {
-      sv = k == 16 ? 1.0 : (k == 48 ? -1.0 : 0.0);
-      cv = k == 0 ? 1.0 : (k == 32 ? -1.0 : 0.0);
+    sincospi(k / (PHS_TRIG_N / 2.0), &sv, &cv);
+    if (k % (PHS_TRIG_N / 4) == 0) {
+      const int q = k / (PHS_TRIG_N / 4);
+      sv = q == 1 ? 1.0 : (q == 3 ? -1.0 : 0.0);
+      cv = q == 0 ? 1.0 : (q == 2 ? -1.0 : 0.0);
     }
     tab[k] = make_double2(sv, cv);
   }

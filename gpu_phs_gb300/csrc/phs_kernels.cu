@@ -236,7 +236,7 @@ size_t phs_forward_smem_bytes(int stack_depth, int block) {
   // frame stack, the compacting variant's per-warp queues (64 events per warp), the
   // sin/cos table
   return (size_t)stack_depth * PHS_STATE * block * sizeof(double) +
-         (size_t)(block / 32) * 64 * sizeof(int64_t) + 64 * sizeof(double2);
+         (size_t)(block / 32) * 64 * sizeof(int64_t) + PHS_TRIG_N * sizeof(double2);
 }
 
 // Variants (each at one block shape, BLOCK threads, and a register budget): 0: one pass,
@@ -339,6 +339,9 @@ cudaError_t phs_launch_forward_exact(const PhsLaunch &a, int n_blocks, cudaStrea
   cudaError_t e = phs_launch_count_scan(a.exact_count, a.exact_tile, a.n_segments, stream);
   if (e != cudaSuccess) return e;
   const size_t smem = phs_forward_smem_bytes(a.stack_depth, PHS_FWD_BLOCK);
+  e = allow_smem(a.E1 && a.E2 ? (const void *)phs_forward_exact_kernel<true>
+                              : (const void *)phs_forward_exact_kernel<false>, smem);
+  if (e != cudaSuccess) return e;
   if (a.E1 && a.E2)
     phs_forward_exact_kernel<true><<<n_blocks, PHS_FWD_BLOCK, smem, stream>>>(a);
   else
