@@ -234,6 +234,7 @@ int compile_channel(const Process &p, int c, double sqrts, PhsChannel &out, Chan
     V.self_m_min = m_min;
     V.self_m_max = m_max;
     V.self_root = cur == R;
+    V.parent_root = cur != R && (kid(R, 0) == cur || kid(R, 1) == cur);
     // friends (extract_boost_origins, phs.cu:268-292): code 2^n_out pairs the branch with
     // the beam along -z, 2^(n_out+1) with the beam along +z; anything else is no friend
     const int fr = p.friends[ix(cur)];
@@ -379,6 +380,7 @@ void channel_to_ff(const PhsChannel &in, PhsChannelFF &out) {
     F.push = V.push;
     F.self_root = V.self_root;
     F.both_leaves = V.both_leaves;
+    F.parent_root = V.parent_root;
     F.b0 = split(V.b0);
     F.b1 = split(V.b1);
     F.self_m_max = split(V.self_m_max);

@@ -437,6 +437,23 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
       Ln[4] = 0.0; Ln[5] = e11; Ln[6] = e12;  Ln[7] = e13;
       Ln[8] = 0.0; Ln[9] = e21; Ln[10] = e22; Ln[11] = e23;
       Ln[12] = bg; Ln[13] = e31; Ln[14] = 0.0; Ln[15] = e33;
+    } else if (V.parent_root && !lab) {
+      // the parent frame is the root's rotation (its bg is 0 and its gamma 1): row 0 is
+      // (1, 0, 0, 0) and L[4], L[8], L[12], L[14] are 0, so half the products drop out
+      Ln[0] = ga;  Ln[1] = e01; Ln[2] = 0.0;  Ln[3] = e03;
+#pragma unroll
+      for (int r = 1; r < 4; r++) {
+        const double l1 = L[4 * r + 1], l2 = r < 3 ? L[4 * r + 2] : 0.0, l3 = L[4 * r + 3];
+        Ln[4 * r + 0] = l3 * bg;
+        Ln[4 * r + 3] = r < 3 ? l1 * e13 + l2 * e23 + l3 * e33 : l1 * e13 + l3 * e33;
+        if (!V.both_leaves) {
+          Ln[4 * r + 1] = r < 3 ? l1 * e11 + l2 * e21 + l3 * e31 : l1 * e11 + l3 * e31;
+          Ln[4 * r + 2] = r < 3 ? l1 * e12 + l2 * e22 : l1 * e12;
+        } else {
+          Ln[4 * r + 1] = 0.0;
+          Ln[4 * r + 2] = 0.0;
+        }
+      }
     } else {
 #pragma unroll
       for (int r = 0; r < 4; r++) {

@@ -172,6 +172,18 @@ FF_FN ff ff_dot2(ff a0, ff b0, ff a1, ff b1) {
   return fast_two_sum(s.hi, f_add(e, s.lo));
 }
 
+FF_FN ff ff_dot3(ff a0, ff b0, ff a1, ff b1, ff a2, ff b2) {
+  const ff p0 = two_prod(a0.hi, b0.hi), p1 = two_prod(a1.hi, b1.hi);
+  const ff p2 = two_prod(a2.hi, b2.hi);
+  float e = f_fma(a0.hi, b0.lo, f_fma(a0.lo, b0.hi, p0.lo));
+  e = f_add(e, f_fma(a1.hi, b1.lo, f_fma(a1.lo, b1.hi, p1.lo)));
+  e = f_add(e, f_fma(a2.hi, b2.lo, f_fma(a2.lo, b2.hi, p2.lo)));
+  ff s = two_sum(p0.hi, p1.hi);
+  e = f_add(e, s.lo);
+  s = two_sum(s.hi, p2.hi);
+  return fast_two_sum(s.hi, f_add(e, s.lo));
+}
+
 FF_FN ff ff_dot4(ff a0, ff b0, ff a1, ff b1, ff a2, ff b2, ff a3, ff b3) {
   const ff p0 = two_prod(a0.hi, b0.hi), p1 = two_prod(a1.hi, b1.hi);
   const ff p2 = two_prod(a2.hi, b2.hi), p3 = two_prod(a3.hi, b3.hi);

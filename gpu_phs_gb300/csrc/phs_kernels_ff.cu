@@ -274,6 +274,20 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
       L[4] = zero; L[5] = e11;  L[6] = e12;   L[7] = e13;
       L[8] = zero; L[9] = e21;  L[10] = e22;  L[11] = e23;
       L[12] = bg;  L[13] = e31; L[14] = zero; L[15] = e33;
+    } else if (V.parent_root && !lab) {
+      // the parent frame is the root's rotation (its bg is 0 and its gamma 1): row 0 is
+      // (1, 0, 0, 0) and L[4], L[8], L[12], L[14] are 0, so half the products drop out
+      L[0] = ga;   L[1] = e01;  L[2] = zero;  L[3] = e03;
+#pragma unroll
+      for (int r = 1; r < 4; r++) {
+        const ff l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
+        L[4 * r + 0] = ff_mul(l3, bg);
+        L[4 * r + 3] = r < 3 ? ff_dot3(l1, e13, l2, e23, l3, e33) : ff_dot2(l1, e13, l3, e33);
+        if (!V.both_leaves) {
+          L[4 * r + 1] = r < 3 ? ff_dot3(l1, e11, l2, e21, l3, e31) : ff_dot2(l1, e11, l3, e31);
+          L[4 * r + 2] = r < 3 ? ff_dot2(l1, e12, l2, e22) : ff_mul(l1, e12);
+        }
+      }
     } else {
       // row r of L L1 depends on row r of L only: update in place
 #pragma unroll

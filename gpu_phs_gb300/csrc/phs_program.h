@@ -68,7 +68,10 @@ struct PhsVisit {
   int32_t friend_sign;  // 0, or the beam (+1: along +z, -1: along -z) that the visited
                         // branch's decay angles are measured from (phs.cu:853-910)
   int8_t slot[2];       // inverse map: momentum slot of each child (see PhsChannel::comb)
-  int8_t pad1[2];
+  int8_t parent_root;   // 1 when the visited branch is a daughter of the root: without a lab
+                        // boost its parent frame is the root's rotation, rows
+                        // (1,0,0,0), (0,*,*,*), (0,*,*,*), (0,*,0,*)
+  int8_t pad1;
 };
 
 struct PhsChannel {
@@ -130,7 +133,8 @@ struct PhsChildFF {
 
 struct PhsVisitFF {
   PhsChildFF child[2];
-  int32_t x_phi, x_ct, ct_class, carry, push, self_root, both_leaves, pad;
+  int32_t x_phi, x_ct, ct_class, carry, push, self_root, both_leaves;
+  int32_t parent_root;  // as PhsVisit::parent_root
   PhsFF b0, b1, self_m_max;
 };
 
