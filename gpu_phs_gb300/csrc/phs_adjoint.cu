@@ -336,13 +336,33 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
       } else {
         const double e01 = -bg * st, e03 = bg * ct, e11 = ct * cphi, e12 = -sphi, e13 = st * cphi;
         const double e21 = ct * sphi, e22 = cphi, e23 = st * sphi, e31 = -ga * st, e33 = ga * ct;
+        if (V.self_root && !lab) {
+          // the parent frame is the identity
+          L[0] = ga;  L[1] = e01; L[2] = 0.0;  L[3] = e03;
+          L[4] = 0.0; L[5] = e11; L[6] = e12;  L[7] = e13;
+          L[8] = 0.0; L[9] = e21; L[10] = e22; L[11] = e23;
+          L[12] = bg; L[13] = e31; L[14] = 0.0; L[15] = e33;
+        } else if (V.parent_root && !lab) {
+          // the parent frame is the root's rotation (its bg is 0 and its gamma 1): row 0 is
+          // (1, 0, 0, 0) and L[4], L[8], L[12], L[14] are 0
+          L[0] = ga;  L[1] = e01; L[2] = 0.0;  L[3] = e03;
 #pragma unroll
-        for (int r = 0; r < 4; r++) {
-          const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
-          L[4 * r + 0] = l0 * ga + l3 * bg;
-          L[4 * r + 1] = l0 * e01 + l1 * e11 + l2 * e21 + l3 * e31;
-          L[4 * r + 2] = l1 * e12 + l2 * e22;
-          L[4 * r + 3] = l0 * e03 + l1 * e13 + l2 * e23 + l3 * e33;
+          for (int r = 1; r < 4; r++) {
+            const double l1 = L[4 * r + 1], l2 = r < 3 ? L[4 * r + 2] : 0.0, l3 = L[4 * r + 3];
+            L[4 * r + 0] = l3 * bg;
+            L[4 * r + 1] = r < 3 ? l1 * e11 + l2 * e21 + l3 * e31 : l1 * e11 + l3 * e31;
+            L[4 * r + 2] = r < 3 ? l1 * e12 + l2 * e22 : l1 * e12;
+            L[4 * r + 3] = r < 3 ? l1 * e13 + l2 * e23 + l3 * e33 : l1 * e13 + l3 * e33;
+          }
+        } else {
+#pragma unroll
+          for (int r = 0; r < 4; r++) {
+            const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
+            L[4 * r + 0] = l0 * ga + l3 * bg;
+            L[4 * r + 1] = l0 * e01 + l1 * e11 + l2 * e21 + l3 * e31;
+            L[4 * r + 2] = l1 * e12 + l2 * e22;
+            L[4 * r + 3] = l0 * e03 + l1 * e13 + l2 * e23 + l3 * e33;
+          }
         }
       }
       if (V.push >= 0 && phs_in(sp, lay.depth, PHS_CHK_STACK)) {
@@ -561,35 +581,41 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
         // L1 has zeros at (0,2), (1,0), (2,0), (3,2), and only its other 12 entries carry
         // adjoints; the loops skip the zero terms (the compiler folds the constant ones).
         double L1b[16];
+        if (V.self_root && !lab) {
+          // the root's parent frame is the identity: L1bar = Lb, and no parent adjoint
 #pragma unroll
-        for (int r = 0; r < 4; r++)
+          for (int i = 0; i < 16; i++) L1b[i] = Lb[i];
+        } else {
 #pragma unroll
-          for (int c = 0; c < 4; c++) {
-            double acc = 0.0, accb = 0.0;
+          for (int r = 0; r < 4; r++)
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-              if ((c == 0 && k == 2) || (c == 1 && k == 0) || (c == 2 && k == 0) || (c == 3 && k == 2))
+            for (int c = 0; c < 4; c++) {
+              double acc = 0.0, accb = 0.0;
+#pragma unroll
+              for (int k = 0; k < 4; k++) {
+                if ((c == 0 && k == 2) || (c == 1 && k == 0) || (c == 2 && k == 0) || (c == 3 && k == 2))
+                  continue;
+                if (!STORED) acc += L[4 * r + k] * (eta[k] * eta[c]) * L1[4 * c + k];
+                accb += Lb[4 * r + k] * L1[4 * c + k];
+              }
+              Lp[4 * r + c] = STORED && phs_in(ev, store_events, PHS_CHK_STORE)
+                                  ? store[(int64_t)(v * 16 + 4 * r + c) * store_events + ev] : acc;
+              Lpb[4 * r + c] = accb;
+            }
+#pragma unroll
+          for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+              if ((r == 0 && c == 2) || (r == 1 && c == 0) || (r == 2 && c == 0) || (r == 3 && c == 2)) {
+                L1b[4 * r + c] = 0.0;
                 continue;
-              if (!STORED) acc += L[4 * r + k] * (eta[k] * eta[c]) * L1[4 * c + k];
-              accb += Lb[4 * r + k] * L1[4 * c + k];
+              }
+              double acc = 0.0;
+#pragma unroll
+              for (int k = 0; k < 4; k++) acc += Lp[4 * k + r] * Lb[4 * k + c];
+              L1b[4 * r + c] = acc;
             }
-            Lp[4 * r + c] = STORED && phs_in(ev, store_events, PHS_CHK_STORE)
-                                ? store[(int64_t)(v * 16 + 4 * r + c) * store_events + ev] : acc;
-            Lpb[4 * r + c] = accb;
-          }
-#pragma unroll
-        for (int r = 0; r < 4; r++)
-#pragma unroll
-          for (int c = 0; c < 4; c++) {
-            if ((r == 0 && c == 2) || (r == 1 && c == 0) || (r == 2 && c == 0) || (r == 3 && c == 2)) {
-              L1b[4 * r + c] = 0.0;
-              continue;
-            }
-            double acc = 0.0;
-#pragma unroll
-            for (int k = 0; k < 4; k++) acc += Lp[4 * k + r] * Lb[4 * k + c];
-            L1b[4 * r + c] = acc;
-          }
+        }
         gab = L1b[0] - L1b[13] * st + L1b[15] * ct;
         bgb = -L1b[1] * st + L1b[3] * ct + L1b[12];
         ctb = L1b[3] * bg + L1b[5] * cphi + L1b[9] * sphi + L1b[15] * ga;

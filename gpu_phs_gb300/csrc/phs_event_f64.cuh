@@ -398,7 +398,7 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
     }
     double ct, st, fct;
     map_ct(V.ct_class, xrow_at(xe, V.x_ct, seg.x_stride), b0, b1, ct, st, fct);
-    factor *= fct;
+    if (V.ct_class == PHS_CT_COLLINEAR) factor *= fct;   // the uniform map's factor is 1
     const double e01 = -bg * st, e03 = bg * ct, e11 = ct * cphi, e12 = -sphi, e13 = st * cphi;
     const double e21 = ct * sphi, e22 = cphi, e23 = st * sphi, e31 = -ga * st, e33 = ga * ct;
 

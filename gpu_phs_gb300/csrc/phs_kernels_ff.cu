@@ -264,7 +264,7 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
       st = ff_twice(ff_sqrt_fast(ff_mul(u, xct)));
       fct = one;
     }
-    factor = ff_mul(factor, fct);
+    if (V.ct_class == PHS_CT_COLLINEAR) factor = ff_mul(factor, fct);   // uniform: 1
     const ff e01 = ff_neg(ff_mul(bg, st)), e03 = ff_mul(bg, ct), e11 = ff_mul(ct, cphi);
     const ff e12 = ff_neg(sphi), e13 = ff_mul(st, cphi), e21 = ff_mul(ct, sphi), e22 = cphi;
     const ff e23 = ff_mul(st, sphi), e31 = ff_neg(ff_mul(ga, st)), e33 = ff_mul(ga, ct);
