@@ -179,13 +179,24 @@ __device__ void inverse_geometry(const PhsChannel &ch, const InvMomenta &pm, dou
       const double t01 = -bg * st0 * cp0, t02 = -bg * st0 * sp0, t03 = -bg * ct0;
       const double t11 = ct0 * cp0, t12 = ct0 * sp0;
       const double t31 = ga * st0 * cp0, t32 = ga * st0 * sp0, t33 = ga * ct0;
+      if (V.parent_root) {
+        // the parent's frame is the root's, the identity: G is the step's own matrix (the
+        // product below with Gp = 1 gives the same bits)
+        G[0] = ga;    G[1] = t01;   G[2] = t02;  G[3] = t03;
+        G[4] = 0.0;   G[5] = t11;   G[6] = t12;  G[7] = -st0;
+        G[8] = 0.0;   G[9] = -sp0;  G[10] = cp0; G[11] = 0.0;
+        G[12] = -bg;  G[13] = t31;  G[14] = t32; G[15] = t33;
+      } else {
 #pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const double g0 = Gp[c], g1 = Gp[4 + c], g2 = Gp[8 + c], g3 = Gp[12 + c];
-        G[c] = ga * g0 + t01 * g1 + t02 * g2 + t03 * g3;
-        G[4 + c] = t11 * g1 + t12 * g2 + (-st0) * g3;
-        G[8 + c] = (-sp0) * g1 + cp0 * g2;
-        G[12 + c] = (-bg) * g0 + t31 * g1 + t32 * g2 + t33 * g3;
+        for (int c = 0; c < 4; c++) {
+          const double g0 = Gp[c], g1 = Gp[4 + c], g2 = Gp[8 + c], g3 = Gp[12 + c];
+          // row 0 only feeds the frames of internal daughters
+          if (!V.both_leaves) G[c] = ga * g0 + t01 * g1 + t02 * g2 + t03 * g3;
+          G[4 + c] = t11 * g1 + t12 * g2 + (-st0) * g3;
+          G[8 + c] = (-sp0) * g1 + cp0 * g2;
+          G[12 + c] = (-bg) * g0 + t31 * g1 + t32 * g2 + t33 * g3;
+        }
+        if (V.both_leaves) G[0] = G[1] = G[2] = G[3] = 0.0;
       }
       if (V.friend_sign != 0) {
         // rotate the friend beam's direction G (1, 0, 0, ff) onto z (phs.cu:1183-1206);
