@@ -210,6 +210,11 @@ int compile_channel(const Process &p, int c, double sqrts, PhsChannel &out, Chan
     ch.msq_max = m_max * m_max;
     ch.m_max = m_max;
     ch.m_min = m_min;
+    if (t == PHS_MAP_SCHANNEL) {
+      ch.msq0 = ch.m * ch.m;
+      ch.inv_mw = 1.0 / (ch.m * ch.w);
+      ch.inv_da = 1.0 / (ch.a1 - ch.a0);
+    }
   };
 
   // visit order: carry the child with fewer leaves, push the other

@@ -237,9 +237,10 @@ __device__ void inverse_geometry(const PhsChannel &ch, const InvMomenta &pm, dou
 
     // angles of daughter 1 in the branch's frame (azimuthal_angle, polar_angle_ct,
     // phs.cu:913-922)
-    const double qx = G[4] * q0[0] + G[5] * q0[1] + G[6] * q0[2] + G[7] * q0[3];
-    const double qy = G[8] * q0[0] + G[9] * q0[1] + G[10] * q0[2] + G[11] * q0[3];
-    const double qz = G[12] * q0[0] + G[13] * q0[1] + G[14] * q0[2] + G[15] * q0[3];
+    // (the root's frame is the identity: the same bits without the products)
+    const double qx = V.self_root ? q0[1] : G[4] * q0[0] + G[5] * q0[1] + G[6] * q0[2] + G[7] * q0[3];
+    const double qy = V.self_root ? q0[2] : G[8] * q0[0] + G[9] * q0[1] + G[10] * q0[2] + G[11] * q0[3];
+    const double qz = V.self_root ? q0[3] : G[12] * q0[0] + G[13] * q0[1] + G[14] * q0[2] + G[15] * q0[3];
     double phi = atan2(qy, qx);
     if (phi < 0.0) phi += 2.0 * PHS_PI;
     geo[(PHS_INV_GEO * v + 3) * PHS_INV_BLOCK] = phi / (2.0 * PHS_PI);
@@ -319,8 +320,16 @@ __device__ double inverse_maps(const PhsChannel &ch, double sqrts, const double 
         } else {
           double a0 = C.a0, a1 = C.a1, a2 = C.a2, mn = C.msq_min, mx = C.msq_max, mmax;
           if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, a0, a1, a2, mn, mx, mmax);
-          map_msq_inverse(C.map_id, geo[(PHS_INV_GEO * v + j) * PHS_INV_BLOCK], s, C.m, C.w, mn,
-                          mx, a0, a1, a2, x, f);
+          const double msq = geo[(PHS_INV_GEO * v + j) * PHS_INV_BLOCK];
+          if (C.map_id == PHS_MAP_SCHANNEL) {
+            // mapping_x_from_msq_schannel with its divisors m w and a1 - a0 (constants of the
+            // channel) as compiled reciprocals
+            const double z = (msq - C.msq0) * C.inv_mw;
+            x = PER_EVENT ? (atan(z) - a0) / (a1 - a0) : (atan(z) - a0) * C.inv_da;
+            f = a2 * (1.0 + z * z);
+          } else {
+            map_msq_inverse(C.map_id, msq, s, C.m, C.w, mn, mx, a0, a1, a2, x, f);
+          }
           if (slot) {
             slot[0] = x;
             slot[PHS_INV_BLOCK] = f;

@@ -49,6 +49,9 @@ struct PhsChild {
   double msq_min, msq_max;  // internal: m_min^2, m_max^2 at the handle's sqrt(s)
   double m_max;       // internal: sqrt(s) - m_tot + m_min (the ok test's upper bound)
   double m_min;       // internal: sum of leaf masses below it (phs.cu:61-78)
+  double msq0;        // internal Breit-Wigner: m^2
+  double inv_mw;      //   1 / (m w)
+  double inv_da;      //   1 / (a1 - a0) at the handle's sqrt(s) (the inverse map's divisors)
 };
 
 struct PhsVisit {
