@@ -146,7 +146,10 @@ struct InvMomenta {
 // The arithmetic keeps the reference's operation order (this file is compiled without
 // contraction): x(p) is ill-conditioned near the poles of each decay (cos(theta) -> +-1,
 // where 1 - cos^2 cancels) and for soft daughters of fast branches, and there any other
-// rounding order moves the result by far more than the input's own rounding does.
+// rounding order moves the result by far more than the input's own rounding does.  The
+// exceptions are divisions by constants of an output that is not ill-conditioned in them,
+// done as products with the constant's reciprocal (one rounding more): x_phi = phi / 2 pi
+// and the Breit-Wigner inverse's divisions by m w and a1 - a0.
 __device__ void inverse_geometry(const PhsChannel &ch, const InvMomenta &pm, double sqrts,
                                  double *stk, double *geo, int stack_depth) {
   const double s = sqrts * sqrts;
@@ -243,7 +246,7 @@ __device__ void inverse_geometry(const PhsChannel &ch, const InvMomenta &pm, dou
     const double qz = V.self_root ? q0[3] : G[12] * q0[0] + G[13] * q0[1] + G[14] * q0[2] + G[15] * q0[3];
     double phi = atan2(qy, qx);
     if (phi < 0.0) phi += 2.0 * PHS_PI;
-    geo[(PHS_INV_GEO * v + 3) * PHS_INV_BLOCK] = phi / (2.0 * PHS_PI);
+    geo[(PHS_INV_GEO * v + 3) * PHS_INV_BLOCK] = phi * (1.0 / (2.0 * PHS_PI));   // x_phi
     const double ct = qz / sqrt(qx * qx + qy * qy + qz * qz);
     geo[(PHS_INV_GEO * v + 2) * PHS_INV_BLOCK] = ct;
     if (V.both_leaves) {

@@ -3,8 +3,10 @@ Whizard's all_factors, its round trip through the forward map, and the Whizard A
 all-channel outputs.
 
 Bar (FP64).  The kernel keeps the oracle's (the reference's) operation order and is
-compiled without contraction, so the two differ only through the ulps of the
-transcendental functions (CUDA's vs glibc's atan2, sin, cos, log, atan).  The reference's
+compiled without contraction, except that it divides by a few constants (2 pi for x_phi,
+m w and a1 - a0 in the Breit-Wigner inverse) as products with their reciprocals, so the
+two differ through the ulps of the transcendental functions (CUDA's vs glibc's atan2, sin,
+cos, log, atan) and of those products.  The reference's
 algorithm amplifies such ulps on some elements: near the poles of a decay (1 - cos(theta)
 cancels in the collinear map), for light combinations (msq = E^2 - |p|^2 cancels), and
 through boosts of rounded rotations (a one-ulp change of one sin(phi) in the reference's
