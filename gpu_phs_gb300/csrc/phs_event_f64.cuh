@@ -437,6 +437,15 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
       Ln[4] = 0.0; Ln[5] = e11; Ln[6] = e12;  Ln[7] = e13;
       Ln[8] = 0.0; Ln[9] = e21; Ln[10] = e22; Ln[11] = e23;
       Ln[12] = bg; Ln[13] = e31; Ln[14] = 0.0; Ln[15] = e33;
+    } else if (PER_EVENT && V.self_root) {
+      // (per-event beams, where nearly every event has a lab boost; the uniform-beam kernels
+      // keep the general product, which leaves their registers to the common case)
+      // the parent frame is the lab boost B_z(lab_bg): rows 1 and 2 are unit rows, and the
+      // root's bg is 0 and its gamma 1
+      Ln[0] = L[0];   Ln[1] = L[3] * e31;  Ln[2] = 0.0;  Ln[3] = L[3] * e33;
+      Ln[4] = 0.0;    Ln[5] = e11;         Ln[6] = e12;  Ln[7] = e13;
+      Ln[8] = 0.0;    Ln[9] = e21;         Ln[10] = e22; Ln[11] = e23;
+      Ln[12] = L[12]; Ln[13] = L[15] * e31; Ln[14] = 0.0; Ln[15] = L[15] * e33;
     } else if (V.parent_root && !lab) {
       // the parent frame is the root's rotation (its bg is 0 and its gamma 1): row 0 is
       // (1, 0, 0, 0) and L[4], L[8], L[12], L[14] are 0, so half the products drop out
@@ -449,6 +458,22 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
         if (!V.both_leaves) {
           Ln[4 * r + 1] = r < 3 ? l1 * e11 + l2 * e21 + l3 * e31 : l1 * e11 + l3 * e31;
           Ln[4 * r + 2] = r < 3 ? l1 * e12 + l2 * e22 : l1 * e12;
+        } else {
+          Ln[4 * r + 1] = 0.0;
+          Ln[4 * r + 2] = 0.0;
+        }
+      }
+    } else if (PER_EVENT && V.parent_root) {
+      // the root's frame with the lab boost: entries (0,2), (1,0), (2,0), (3,2) are 0
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
+        const bool edge = r == 0 || r == 3;   // l2 = 0; otherwise l0 = 0
+        Ln[4 * r + 0] = edge ? l0 * ga + l3 * bg : l3 * bg;
+        Ln[4 * r + 3] = edge ? l0 * e03 + l1 * e13 + l3 * e33 : l1 * e13 + l2 * e23 + l3 * e33;
+        if (!V.both_leaves) {
+          Ln[4 * r + 1] = edge ? l0 * e01 + l1 * e11 + l3 * e31 : l1 * e11 + l2 * e21 + l3 * e31;
+          Ln[4 * r + 2] = edge ? l1 * e12 : l1 * e12 + l2 * e22;
         } else {
           Ln[4 * r + 1] = 0.0;
           Ln[4 * r + 2] = 0.0;

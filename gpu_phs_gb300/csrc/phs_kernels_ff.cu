@@ -274,6 +274,17 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
       L[4] = zero; L[5] = e11;  L[6] = e12;   L[7] = e13;
       L[8] = zero; L[9] = e21;  L[10] = e22;  L[11] = e23;
       L[12] = bg;  L[13] = e31; L[14] = zero; L[15] = e33;
+    } else if (PER_EVENT && V.self_root) {
+      // (per-event beams, where nearly every event has a lab boost; the uniform-beam kernels
+      // keep the general product, which leaves their registers to the common case)
+      // the parent frame is the lab boost B_z(lab_bg): rows 1 and 2 are unit rows
+      const ff g0 = L[0], b0 = L[3];
+      L[0] = ff_dot2(g0, ga, b0, bg);   L[1] = ff_dot2(g0, e01, b0, e31);
+      L[2] = zero;                      L[3] = ff_dot2(g0, e03, b0, e33);
+      L[4] = zero; L[5] = e11;  L[6] = e12;   L[7] = e13;
+      L[8] = zero; L[9] = e21;  L[10] = e22;  L[11] = e23;
+      L[12] = ff_dot2(b0, ga, g0, bg);  L[13] = ff_dot2(b0, e01, g0, e31);
+      L[14] = zero;                     L[15] = ff_dot2(b0, e03, g0, e33);
     } else if (V.parent_root && !lab) {
       // the parent frame is the root's rotation (its bg is 0 and its gamma 1): row 0 is
       // (1, 0, 0, 0) and L[4], L[8], L[12], L[14] are 0, so half the products drop out
@@ -286,6 +297,19 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
         if (!V.both_leaves) {
           L[4 * r + 1] = r < 3 ? ff_dot3(l1, e11, l2, e21, l3, e31) : ff_dot2(l1, e11, l3, e31);
           L[4 * r + 2] = r < 3 ? ff_dot2(l1, e12, l2, e22) : ff_mul(l1, e12);
+        }
+      }
+    } else if (PER_EVENT && V.parent_root) {
+      // the root's frame with the lab boost: entries (0,2), (1,0), (2,0), (3,2) are 0
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        const ff l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
+        const bool edge = r == 0 || r == 3;   // l2 = 0; otherwise l0 = 0
+        L[4 * r + 0] = edge ? ff_dot2(l0, ga, l3, bg) : ff_mul(l3, bg);
+        L[4 * r + 3] = edge ? ff_dot3(l0, e03, l1, e13, l3, e33) : ff_dot3(l1, e13, l2, e23, l3, e33);
+        if (!V.both_leaves) {
+          L[4 * r + 1] = edge ? ff_dot3(l0, e01, l1, e11, l3, e31) : ff_dot3(l1, e11, l2, e21, l3, e31);
+          L[4 * r + 2] = edge ? ff_mul(l1, e12) : ff_dot2(l1, e12, l2, e22);
         }
       }
     } else {
