@@ -164,28 +164,31 @@ __device__ __forceinline__ double channel_volume(const PhsChannel &ch, double sq
 }
 
 // Mapping constants at one sqrt(s) (phs_cpu.cpp:452-531), for the per-event-beam path.
-__device__ void child_constants(const PhsChild &C, double sqrts, double m_tot, double &a0,
-                                double &a1, double &a2, double &msq_min, double &msq_max,
-                                double &m_max) {
+// inv_s = 1/s of the event.  The reference divides a2 by s and the Breit-Wigner argument by
+// m w; here they are products with 1/s (once per event) and the compiled 1/(m w), within an
+// ulp of the quotients (a2 weights the factor; a1 = atan(u) at u >= 10^3 moves by ulp/u).
+// msq_min = m_min^2 and m^2 do not depend on sqrt(s): the compiled values (the same bits).
+__device__ void child_constants(const PhsChild &C, double sqrts, double m_tot, double inv_s,
+                                double &a0, double &a1, double &a2, double &msq_min,
+                                double &msq_max, double &m_max) {
   double m = C.m, w = C.w, m_min = C.m_min;
   m_max = dadd(dsub(sqrts, m_tot), m_min);
-  msq_min = dmul(m_min, m_min);
+  msq_min = C.msq_min;
   msq_max = dmul(m_max, m_max);
-  double s = dmul(sqrts, sqrts);
   a0 = a1 = a2 = 0.0;
   switch (C.map_id) {
     case PHS_MAP_NO:
       a1 = msq_max - msq_min;
-      a2 = a1 / s;
+      a2 = a1 * inv_s;
       break;
     case PHS_MAP_SCHANNEL: {
       // a0 = atan((msq_min - m^2) / (m w)) does not depend on sqrt(s): the compiled
       // program's value (the host's atan of the same argument bits, as the reference's CPU
       // path computes it) serves every event
-      double msq0 = dmul(m, m), mw = dmul(m, w);
+      const double mw = dmul(m, w);
       a0 = C.a0;
-      a1 = phs_atan_bw(dsub(msq_max, msq0) / mw);   // argument >= 10^3 here in practice
-      a2 = dmul(dsub(a1, a0), mw) / s;
+      a1 = phs_atan_bw(dsub(msq_max, C.msq0) * C.inv_mw);   // argument >= 10^3 here in practice
+      a2 = dmul(dsub(a1, a0), mw) * inv_s;
       break;
     }
     case PHS_MAP_RADIATION:
@@ -194,7 +197,7 @@ __device__ void child_constants(const PhsChild &C, double sqrts, double m_tot, d
       double msq0 = C.map_id == PHS_MAP_RADIATION ? dmul(w, w) : dmul(m, m);
       a0 = msq0;
       a1 = log(dadd(dsub(msq_max, msq_min) / msq0, 1.0));
-      a2 = a1 / s;
+      a2 = a1 * inv_s;
       break;
     }
     case PHS_MAP_TCHANNEL:
@@ -202,7 +205,7 @@ __device__ void child_constants(const PhsChild &C, double sqrts, double m_tot, d
       double msq0 = dmul(m, m);
       a0 = msq0;
       a1 = dmul(2.0, log(dadd(dsub(msq_max, msq_min) / dmul(2.0, msq0), 1.0)));
-      a2 = a1 / s;
+      a2 = a1 * inv_s;
       break;
     }
     case PHS_MAP_STEP_E: {
@@ -333,6 +336,7 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
     lab_ga = sqrt(1.0 + lab_bg * lab_bg);
   }
   const double s = dmul(sqrts, sqrts);
+  const double inv_s = PER_EVENT ? 1.0 / s : 0.0;   // per-event mapping constants
 
   // frame of the visited branch; the root's parent frame is the lab boost (or 1)
   double L[16];
@@ -363,7 +367,7 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
       } else {
         double a0 = C.a0, a1 = C.a1, a2 = C.a2, mn = C.msq_min, mx = C.msq_max;
         cmax[j] = C.m_max;
-        if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, a0, a1, a2, mn, mx, cmax[j]);
+        if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, inv_s, a0, a1, a2, mn, mx, cmax[j]);
         double f;
         map_msq(C.map_id, xrow_at(xe, C.x_msq, seg.x_stride), s, C.m, C.w, mn, mx, a0, a1, a2,
                 cmsq[j], f);
@@ -569,6 +573,7 @@ __device__ __forceinline__ bool phs_ok_f64(const PhsLaunch &a, const PhsSegment 
   double sqrts = ch.sqrts;
   if (PER_EVENT) sqrts = dmul(2.0, sqrt(dmul(a.E1[ev], a.E2[ev])));
   const double s = dmul(sqrts, sqrts);
+  const double inv_s = PER_EVENT ? 1.0 / s : 0.0;   // per-event mapping constants
   double msq_b = s, m_b = sqrts, mmax_b = sqrts;
   bool ok = true;
   int sp = 0;
@@ -586,7 +591,7 @@ __device__ __forceinline__ bool phs_ok_f64(const PhsLaunch &a, const PhsSegment 
       } else {
         double a0 = C.a0, a1 = C.a1, a2 = C.a2, mn = C.msq_min, mx = C.msq_max;
         cmax[j] = C.m_max;
-        if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, a0, a1, a2, mn, mx, cmax[j]);
+        if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, inv_s, a0, a1, a2, mn, mx, cmax[j]);
         double f;
         map_msq(C.map_id, xrow_at(xe, C.x_msq, seg.x_stride), s, C.m, C.w, mn, mx, a0, a1, a2,
                 cmsq[j], f);

@@ -322,7 +322,7 @@ __device__ double inverse_maps(const PhsChannel &ch, double sqrts, const double 
           f = slot[PHS_INV_BLOCK];
         } else {
           double a0 = C.a0, a1 = C.a1, a2 = C.a2, mn = C.msq_min, mx = C.msq_max, mmax;
-          if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, a0, a1, a2, mn, mx, mmax);
+          if (PER_EVENT) child_constants(C, sqrts, ch.m_tot, 1.0 / s, a0, a1, a2, mn, mx, mmax);
           const double msq = geo[(PHS_INV_GEO * v + j) * PHS_INV_BLOCK];
           if (C.map_id == PHS_MAP_SCHANNEL) {
             // mapping_x_from_msq_schannel with its divisors m w and a1 - a0 (constants of the

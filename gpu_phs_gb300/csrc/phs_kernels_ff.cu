@@ -61,9 +61,9 @@ __device__ __forceinline__ ChildVar child_var(const PhsChildFF &C) {
   return {ld(C.a1), ld(C.a2), ld(C.u1), ld(C.msq_max), ld(C.m_max)};
 }
 __device__ __forceinline__ ChildVar child_var(const PhsChildFF &C, const PhsChild &C64,
-                                              double sqrts, double m_tot) {
+                                              double sqrts, double m_tot, double inv_s) {
   double a0, a1, a2, mn, mx, mmax;
-  child_constants(C64, sqrts, m_tot, a0, a1, a2, mn, mx, mmax);
+  child_constants(C64, sqrts, m_tot, inv_s, a0, a1, a2, mn, mx, mmax);
   ChildVar r;
   r.a2 = ff_from_double(a2);
   r.msq_max = ff_from_double(mx);
@@ -152,11 +152,12 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
   // beams: the channel's, or this event's (phs_event_f64's expressions)
   ff sqrts_f = ld(ch.sqrts), s_f = ld(ch.s), lab_bg = ld(ch.lab_bg), lab_ga = ld(ch.lab_gamma);
   bool lab = ch.lab != 0;
-  double sqrts64 = 0.0, s64 = 0.0;
+  double sqrts64 = 0.0, s64 = 0.0, inv_s64 = 0.0;
   if (PER_EVENT) {
     const double E1 = a.E1[ev], E2 = a.E2[ev], r = sqrt(dmul(E1, E2));
     sqrts64 = dmul(2.0, r);
     s64 = dmul(sqrts64, sqrts64);
+    inv_s64 = 1.0 / s64;
     const double bg = dsub(E1, E2) / dmul(2.0, r);
     lab = E1 != E2;
     sqrts_f = ff_from_double(sqrts64);
@@ -195,7 +196,8 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
       } else {
         ff f;
         const ChildVar cv = PER_EVENT
-            ? child_var(C, a.channels[seg.channel].visit[v].child[j], sqrts64, a.channels[seg.channel].m_tot)
+            ? child_var(C, a.channels[seg.channel].visit[v].child[j], sqrts64, a.channels[seg.channel].m_tot,
+                        inv_s64)
             : child_var(C);
         if (!map_msq_ff(C, cv, xrow_at(xe, C.x_msq, seg.x_stride), T, cmsq[j], f)) return false;
         factor = ff_mul(factor, f);
