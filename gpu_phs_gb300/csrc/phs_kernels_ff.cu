@@ -64,16 +64,17 @@ __device__ __forceinline__ ChildVar child_var(const PhsChildFF &C, const PhsChil
                                               double sqrts, double m_tot, double inv_s) {
   double a0, a1, a2, mn, mx, mmax;
   child_constants(C64, sqrts, m_tot, inv_s, a0, a1, a2, mn, mx, mmax);
+  // to pairs with integer operations: the FP64 pipe is the per-event path's scarce one
   ChildVar r;
-  r.a2 = ff_from_double(a2);
-  r.msq_max = ff_from_double(mx);
-  r.m_max = ff_from_double(mmax);
+  r.a2 = ff_from_double_int(a2);
+  r.msq_max = ff_from_double_int(mx);
+  r.m_max = ff_from_double_int(mmax);
   if (C.map_id == PHS_MAP_SCHANNEL) {
-    r.a1 = ff_from_double(a1 - a0);
+    r.a1 = ff_from_double_int(a1 - a0);
     // pi/2 - a1: exact for a1 >= pi/4 (the only case that uses it), then pi/2's low part
-    r.u1 = ff_from_double((1.5707963267948966 - a1) + 6.123233995736766e-17);
+    r.u1 = ff_from_double_int((1.5707963267948966 - a1) + 6.123233995736766e-17);
   } else {
-    r.a1 = ff_from_double(a1);
+    r.a1 = ff_from_double_int(a1);
     r.u1 = ff_from_float(0.0f);
   }
   return r;
@@ -126,6 +127,14 @@ __device__ __forceinline__ bool map_msq_ff(const PhsChildFF &C, const ChildVar &
   return false;
 }
 
+// A pair as a double: two exact widenings and one add on the FP64 pipe (uniform beams,
+// where the walk is bound by FP32 issue), or with integer operations (per-event beams, where
+// the per-event constants keep the FP64 pipe busy).
+template <bool INT>
+__device__ __forceinline__ double widen(ff a) {
+  return INT ? ff_to_double_int(a) : ff_to_double(a);
+}
+
 __device__ __forceinline__ ff ff_twice(ff a) { return ff_make(f_add(a.hi, a.hi), f_add(a.lo, a.lo)); }
 __device__ __forceinline__ ff ff_half(ff a) { return ff_make(f_mul(a.hi, 0.5f), f_mul(a.lo, 0.5f)); }
 
@@ -160,10 +169,10 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
     inv_s64 = 1.0 / s64;
     const double bg = dsub(E1, E2) / dmul(2.0, r);
     lab = E1 != E2;
-    sqrts_f = ff_from_double(sqrts64);
-    s_f = ff_from_double(s64);
-    lab_bg = ff_from_double(bg);
-    lab_ga = ff_from_double(sqrt(1.0 + bg * bg));
+    sqrts_f = ff_from_double_int(sqrts64);
+    s_f = ff_from_double_int(s64);
+    lab_bg = ff_from_double_int(bg);
+    lab_ga = ff_from_double_int(sqrt(1.0 + bg * bg));
   }
   const float s_scale = s_f.hi;
 
@@ -244,8 +253,8 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
       if (PER_EVENT) {
         const double m = a.channels[seg.channel].visit[v].m;
         const double b0d = dmul(m, m) / s64;
-        b0 = ff_from_double(b0d);
-        b1 = ff_from_double(log(dadd(b0d, 1.0) / b0d));
+        b0 = ff_from_double_int(b0d);
+        b1 = ff_from_double_int(log(dadd(b0d, 1.0) / b0d));
       }
       const bool lower = xct.hi < 0.5f;
       const ff tmp = ff_mul(b0, ff_exp(ff_mul(ff_twice(lower ? xct : ff_one_minus_double_int(xctd)), b1), T));
@@ -337,10 +346,10 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
         const ff E = ff_sqrt_fast(ff_add(cmsq[j], ff_sqr(pj)));
         double2 *o = reinterpret_cast<double2 *>(out + 4 * C.out_index);
         // to double on the (otherwise idle) FP64 pipe: two exact widenings and one add
-        o[0] = make_double2(ff_to_double(ff_dot2(L[0], E, L[3], pj)),
-                            ff_to_double(ff_dot2(L[4], E, L[7], pj)));
-        o[1] = make_double2(ff_to_double(ff_dot2(L[8], E, L[11], pj)),
-                            ff_to_double(ff_dot2(L[12], E, L[15], pj)));
+        o[0] = make_double2(widen<PER_EVENT>(ff_dot2(L[0], E, L[3], pj)),
+                            widen<PER_EVENT>(ff_dot2(L[4], E, L[7], pj)));
+        o[1] = make_double2(widen<PER_EVENT>(ff_dot2(L[8], E, L[11], pj)),
+                            widen<PER_EVENT>(ff_dot2(L[12], E, L[15], pj)));
       }
     }
 
@@ -372,7 +381,7 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
   }
 
   a.volume[ev] = PER_EVENT ? channel_volume(a.channels[seg.channel], sqrts64) : ch.volume;
-  a.factor[ev * a.factor_stride + seg.factor_col] = ok ? ff_to_double(factor) : 0.0;
+  a.factor[ev * a.factor_stride + seg.factor_col] = ok ? widen<PER_EVENT>(factor) : 0.0;
   a.ok[ev] = ok ? 1 : 0;
   if (!ok) {
     double2 *o = reinterpret_cast<double2 *>(out);
