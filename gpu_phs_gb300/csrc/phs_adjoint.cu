@@ -585,6 +585,52 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
           // the root's parent frame is the identity: L1bar = Lb, and no parent adjoint
 #pragma unroll
           for (int i = 0; i < 16; i++) L1b[i] = Lb[i];
+        } else if (V.parent_root && !lab) {
+          // the parent frame is the root's rotation (the root's bg is 0, its gamma 1): row 0
+          // is (1, 0, 0, 0) and entries (1,0), (2,0), (3,0), (3,2) are 0.  Those are set, not
+          // recovered; the root's reverse step reads only the adjoints of L1's 12 entries
+          // that are not structurally 0, so the parent adjoint skips (0,2), (1,0), (2,0), (3,2).
+#pragma unroll
+          for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+              const int i = 4 * r + c;
+              const bool fixed = r == 0 || c == 0 || i == 14;
+              const bool unread = i == 2 || i == 4 || i == 8 || i == 14;
+              double acc = 0.0, accb = 0.0;
+#pragma unroll
+              for (int k = 0; k < 4; k++) {
+                if ((c == 0 && k == 2) || (c == 1 && k == 0) || (c == 2 && k == 0) || (c == 3 && k == 2))
+                  continue;
+                if (!STORED && !fixed) acc += L[4 * r + k] * (eta[k] * eta[c]) * L1[4 * c + k];
+                if (!unread) accb += Lb[4 * r + k] * L1[4 * c + k];
+              }
+              Lp[i] = fixed ? (i == 0 ? 1.0 : 0.0)
+                            : (STORED && phs_in(ev, store_events, PHS_CHK_STORE)
+                                   ? store[(int64_t)(v * 16 + i) * store_events + ev] : acc);
+              Lpb[i] = accb;
+            }
+          // L1bar = Lp^T Lb over Lp's entries that are not 0 (column 0 of Lp is (1, 0, 0, 0))
+#pragma unroll
+          for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+              if ((r == 0 && c == 2) || (r == 1 && c == 0) || (r == 2 && c == 0) || (r == 3 && c == 2)) {
+                L1b[4 * r + c] = 0.0;
+                continue;
+              }
+              if (r == 0) {
+                L1b[c] = Lb[c];
+                continue;
+              }
+              double acc = 0.0;
+#pragma unroll
+              for (int k = 1; k < 4; k++) {
+                if (k == 3 && r == 2) continue;   // Lp (3,2) = 0
+                acc += Lp[4 * k + r] * Lb[4 * k + c];
+              }
+              L1b[4 * r + c] = acc;
+            }
         } else {
 #pragma unroll
           for (int r = 0; r < 4; r++)
