@@ -150,15 +150,18 @@ __device__ __forceinline__ void rot_z_onto(double bx, double by, double bz, doub
 }
 
 // The channel's phase-space volume at sqrt(s) (phs_cpu.cpp:194-213), bottom-up in post-order
-// with the reference's operation order: for the per-event-beam paths.
+// with the reference's operation order: for the per-event-beam paths.  The divisions by
+// the two constants are the correctly rounded corrected products (phs_div_by_const): the
+// same bits.
 __device__ __forceinline__ double channel_volume(const PhsChannel &ch, double sqrts) {
   double vol[PHS_MAX_VISITS];
-  const double c_int = 4 * PHS_TWOPI2, c_root = 4 * PHS_TWOPI5;
+  constexpr double c_int = 4 * PHS_TWOPI2, c_root = 4 * PHS_TWOPI5;
+  constexpr double r_int = 1.0 / c_int, r_root = 1.0 / c_root;
   for (int i = 0; i < ch.n_vol; i++) {
     int k1 = ch.vol_child[i][0], k2 = ch.vol_child[i][1];
     double v1 = k1 >= 0 ? vol[k1] : 1.0, v2 = k2 >= 0 ? vol[k2] : 1.0;
-    vol[i] = ch.vol_is_root[i] ? dmul(v1, v2) / c_root
-                               : dmul(dmul(dmul(v1, v2), sqrts), sqrts) / c_int;
+    vol[i] = ch.vol_is_root[i] ? phs_div_by_const(dmul(v1, v2), c_root, r_root)
+                               : phs_div_by_const(dmul(dmul(dmul(v1, v2), sqrts), sqrts), c_int, r_int);
   }
   return vol[ch.n_vol - 1];
 }

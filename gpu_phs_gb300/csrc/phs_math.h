@@ -9,6 +9,7 @@
 // library's general atan; within an ulp of the exact value (pi/2 as a double plus its
 // rounding error, added last).  Smaller arguments use the library's atan.
 #pragma once
+#include <math.h>
 
 #if defined(__CUDACC__)
 #define PHS_MATH_FN __host__ __device__ __forceinline__
@@ -27,3 +28,13 @@ PHS_MATH_FN double phs_atan_large(double u) {
 
 // atan(u) of a Breit-Wigner bound: the series above for u >= 1024, else the library's.
 PHS_MATH_FN double phs_atan_bw(double u) { return u >= 1024.0 ? phs_atan_large(u) : atan(u); }
+
+// a / b for a constant b with rb = RN(1/b): the product a rb corrected once with its
+// residual, q + (a - b q) rb, the residual exact through the FMA.  With rb correctly
+// rounded this is a / b correctly rounded (Markstein's theorem on the corrected quotient;
+// the host test checks it bit for bit against the division for the constants the volume
+// program uses): three FP64 operations instead of a division's sequence.
+PHS_MATH_FN double phs_div_by_const(double a, double b, double rb) {
+  const double q = a * rb;
+  return fma(fma(-q, b, a), rb, q);
+}

@@ -1,6 +1,8 @@
-"""Host-side checks of the float-float helpers in phs_ff.h (the header compiles as plain
-C++): the integer-only conversions between doubles and float pairs that the FP32-pair
-kernels use to keep conversions off the FP64 pipe, against long-double references."""
+"""Host-side checks of the arithmetic helpers in phs_ff.h and phs_math.h (the headers
+compile as plain C++): the integer-only conversions between doubles and float pairs that
+the FP32-pair kernels use to keep conversions off the FP64 pipe, against long-double
+references; the series atan of large Breit-Wigner arguments; the corrected products that
+stand for the volume program's divisions by constants."""
 import os
 import subprocess
 import tempfile
@@ -112,3 +114,52 @@ def test_atan_of_large_breit_wigner_arguments():
         subprocess.run(["g++", "-O2", "-std=c++17", "-I", CSRC, src, "-o", exe], check=True)
         worst = float(subprocess.run([exe], check=True, capture_output=True, text=True).stdout)
     assert worst <= 1.0, f"{worst} ulp"
+
+
+DIV_DRIVER = r"""
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include "phs_math.h"
+int main() {
+  const double TWOPI2 = 39.47841760435743447534, TWOPI5 = 9792.62991312900650440772;
+  const double cs[2] = {4 * TWOPI2, 4 * TWOPI5};   // the volume program's divisors
+  std::mt19937_64 rng(11);
+  long n = 0, bad = 0;
+  for (double b : cs) {
+    volatile double one = 1.0;
+    const double rb = one / b;
+    for (int i = 0; i < 20000000; i++) {
+      // full random significand, exponent spread over 2^-300 .. 2^300, both signs
+      const uint64_t bits = (rng() & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(1023 - 300 + rng() % 601) << 52);
+      double a;
+      std::memcpy(&a, &bits, 8);
+      volatile double ref = a / b;
+      n++;
+      if (phs_div_by_const(a, b, rb) != ref) bad++;
+    }
+  }
+  std::printf("%ld %ld\n", n, bad);
+  return 0;
+}
+"""
+
+
+def test_corrected_products_equal_the_divisions_by_constants():
+    """phs_div_by_const(a, b, RN(1/b)) is a / b bit for bit for the volume program's
+    constants 4 (2 pi)^2 and 4 (2 pi)^5, over 4e7 random a of every magnitude."""
+    try:
+        subprocess.run(["g++", "--version"], check=True, capture_output=True)
+    except (OSError, subprocess.CalledProcessError):
+        pytest.skip("g++ not available")
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = os.path.join(d, "dv.cpp"), os.path.join(d, "dv")
+        with open(src, "w") as fh:
+            fh.write(DIV_DRIVER)
+        subprocess.run(["g++", "-O2", "-ffp-contract=off", "-std=c++17", "-I", CSRC, src, "-o", exe],
+                       check=True)
+        n, bad = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
+    assert int(n) == 40_000_000
+    assert int(bad) == 0
