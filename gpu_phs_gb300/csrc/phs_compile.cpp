@@ -349,6 +349,7 @@ void channel_to_ff(const PhsChannel &in, PhsChannelFF &out) {
   out.s = split(in.sqrts * in.sqrts);
   out.lab_bg = split(in.lab_bg);
   out.lab_gamma = split(in.lab_gamma);
+  out.m_tot = split(in.m_tot);
   out.volume = in.volume;
   for (int v = 0; v < in.n_visits; v++) {
     const PhsVisit &V = in.visit[v];
@@ -370,6 +371,8 @@ void channel_to_ff(const PhsChannel &in, PhsChannelFF &out) {
       G.msq_min = split(C.msq_min);
       G.msq_max = split(C.msq_max);
       G.m_max = split(C.m_max);
+      G.m_min = split(C.m_min);
+      if (C.map_id == PHS_MAP_SCHANNEL) G.inv_mw = split_ld(1.0L / ((long double)C.m * (long double)C.w));
       if (C.map_id == PHS_MAP_SCHANNEL) {
         const long double half_pi = 1.57079632679489661923132169163975144L;
         G.u0 = split_ld(half_pi + (long double)C.a0);

@@ -80,6 +80,37 @@ __device__ __forceinline__ ChildVar child_var(const PhsChildFF &C, const PhsChil
   return r;
 }
 
+// Per-event constants in float-float (the FP32 pipe) for the uniform map and for
+// Breit-Wigner maps whose range in widths u = (msq_max - m^2)/(m w) is at least 1024, where
+// a1 = atan(u) = pi/2 - atan(1/u) and atan(w) = w - w^3/3 + w^5/5 for w = 1/u (the next term
+// is below 2^-72 of pi/2, as in phs_math.h); pi/2 - a1 is that series itself.  Other maps
+// and smaller u take the FP64 constants.  sqrts, inv_s: the event's sqrt(s) and 1/s.
+__device__ __forceinline__ ChildVar child_var(const PhsChildFF &C, const PhsChild &C64, ff sqrts,
+                                              ff inv_s, ff m_tot, double sqrts64, double m_tot64) {
+  if (C.map_id == PHS_MAP_NO || C.map_id == PHS_MAP_SCHANNEL) {
+    ChildVar r;
+    r.m_max = ff_add(ff_sub(sqrts, m_tot), ld(C.m_min));
+    r.msq_max = ff_sqr(r.m_max);
+    if (C.map_id == PHS_MAP_NO) {
+      r.a1 = ff_sub(r.msq_max, ld(C.msq_min));
+      r.a2 = ff_mul(r.a1, inv_s);
+      r.u1 = ff_from_float(0.0f);
+      return r;
+    }
+    const ff u = ff_mul(ff_sub(r.msq_max, ld(C.m2)), ld(C.inv_mw));
+    if (u.hi >= 1024.0f) {
+      const ff w = ff_recip_fast(u), w2 = ff_sqr(w);
+      r.u1 = ff_add(w, ff_mul(ff_mul(w, w2), ff_add_f(ff_mul_f(w2, 0.2f), -1.0f / 3.0f)));
+      const ff a1 = ff_sub(ff_make(0.5f * FF_PI_HI, 0.5f * FF_PI_LO), r.u1);
+      r.a1 = ff_sub(a1, ld(C.a0));                       // a1 - a0
+      r.a2 = ff_mul(ff_mul(r.a1, ld(C.mw)), inv_s);
+      return r;
+    }
+  }
+  const double s64 = dmul(sqrts64, sqrts64);
+  return child_var(C, C64, sqrts64, m_tot64, 1.0 / s64);
+}
+
 // msq from x in float-float; returns false when the event must take the exact path.
 // x arrives as a float-float pair truncated from the double, so x < 0.5 is decided on its
 // high part exactly as the reference decides it on the double.
@@ -161,18 +192,22 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
   // beams: the channel's, or this event's (phs_event_f64's expressions)
   ff sqrts_f = ld(ch.sqrts), s_f = ld(ch.s), lab_bg = ld(ch.lab_bg), lab_ga = ld(ch.lab_gamma);
   bool lab = ch.lab != 0;
-  double sqrts64 = 0.0, s64 = 0.0, inv_s64 = 0.0;
+  double sqrts64 = 0.0, s64 = 0.0;
+  ff inv_s_f = zero;
   if (PER_EVENT) {
-    const double E1 = a.E1[ev], E2 = a.E2[ev], r = sqrt(dmul(E1, E2));
-    sqrts64 = dmul(2.0, r);
+    // the beams in float-float; sqrt(s) in FP64 as well for the volume, the collinear
+    // cos(theta) constants and the maps whose constants stay FP64
+    const double E1 = a.E1[ev], E2 = a.E2[ev];
+    sqrts64 = dmul(2.0, sqrt(dmul(E1, E2)));
     s64 = dmul(sqrts64, sqrts64);
-    inv_s64 = 1.0 / s64;
-    const double bg = dsub(E1, E2) / dmul(2.0, r);
+    const ff e1 = ff_from_double_int(E1), e2 = ff_from_double_int(E2);
+    const ff r = ff_sqrt_fast(ff_mul(e1, e2));
+    sqrts_f = ff_twice(r);
+    s_f = ff_sqr(sqrts_f);
+    inv_s_f = ff_recip_fast(s_f);
     lab = E1 != E2;
-    sqrts_f = ff_from_double_int(sqrts64);
-    s_f = ff_from_double_int(s64);
-    lab_bg = ff_from_double_int(bg);
-    lab_ga = ff_from_double_int(sqrt(1.0 + bg * bg));
+    lab_bg = ff_div_fast(ff_sub(e1, e2), sqrts_f);
+    lab_ga = ff_sqrt_fast(ff_add_f(ff_sqr(lab_bg), 1.0f));
   }
   const float s_scale = s_f.hi;
 
@@ -205,8 +240,8 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
       } else {
         ff f;
         const ChildVar cv = PER_EVENT
-            ? child_var(C, a.channels[seg.channel].visit[v].child[j], sqrts64, a.channels[seg.channel].m_tot,
-                        inv_s64)
+            ? child_var(C, a.channels[seg.channel].visit[v].child[j], sqrts_f, inv_s_f, ld(ch.m_tot),
+                        sqrts64, a.channels[seg.channel].m_tot)
             : child_var(C);
         if (!map_msq_ff(C, cv, xrow_at(xe, C.x_msq, seg.x_stride), T, cmsq[j], f)) return false;
         factor = ff_mul(factor, f);

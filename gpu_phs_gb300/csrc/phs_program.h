@@ -132,6 +132,8 @@ struct PhsChildFF {
   PhsFF a0, a1, a2;   // mapping constants; Breit-Wigner keeps a1 - a0 in a1
   PhsFF msq_min, msq_max, m_max;
   PhsFF u0, u1;       // Breit-Wigner: pi/2 + a0 and pi/2 - a1 (z near -+pi/2 as cot)
+  PhsFF m_min;        // internal: the sum of the leaf masses below it (per-event m_max)
+  PhsFF inv_mw;       // Breit-Wigner: 1 / (m w) (per-event a1)
 };
 
 struct PhsVisitFF {
@@ -159,6 +161,7 @@ struct PhsChannelFF {
   int32_t exact_only;  // 1: STEP_E/STEP_H mappings or a friend boost: FP64 path
   int32_t lab;
   PhsFF sqrts, s, lab_bg, lab_gamma;
+  PhsFF m_tot;        // the sum of all outgoing masses (per-event m_max)
   double volume;
   PhsVisitFF visit[PHS_MAX_VISITS];
   PhsTestVisit test[PHS_MAX_VISITS];
