@@ -631,6 +631,39 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
               }
               L1b[4 * r + c] = acc;
             }
+        } else if (V.both_leaves) {
+          // both daughters are leaves: their momenta read the frame's columns 0 and 3 only,
+          // and no daughter visit adds to its adjoint, so Lb's columns 1 and 2 are 0
+#pragma unroll
+          for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+              double acc = 0.0, accb = 0.0;
+#pragma unroll
+              for (int k = 0; k < 4; k++) {
+                if ((c == 0 && k == 2) || (c == 1 && k == 0) || (c == 2 && k == 0) || (c == 3 && k == 2))
+                  continue;
+                if (!STORED) acc += L[4 * r + k] * (eta[k] * eta[c]) * L1[4 * c + k];
+                if (k == 0 || k == 3) accb += Lb[4 * r + k] * L1[4 * c + k];
+              }
+              Lp[4 * r + c] = STORED && phs_in(ev, store_events, PHS_CHK_STORE)
+                                  ? store[(int64_t)(v * 16 + 4 * r + c) * store_events + ev] : acc;
+              Lpb[4 * r + c] = accb;
+            }
+#pragma unroll
+          for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+              if ((r == 0 && c == 2) || (r == 1 && c == 0) || (r == 2 && c == 0) || (r == 3 && c == 2) ||
+                  c == 1 || c == 2) {
+                L1b[4 * r + c] = 0.0;
+                continue;
+              }
+              double acc = 0.0;
+#pragma unroll
+              for (int k = 0; k < 4; k++) acc += Lp[4 * k + r] * Lb[4 * k + c];
+              L1b[4 * r + c] = acc;
+            }
         } else {
 #pragma unroll
           for (int r = 0; r < 4; r++)
