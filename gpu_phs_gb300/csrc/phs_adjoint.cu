@@ -333,6 +333,9 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
           for (int c = 0; c < 3; c++)
             L[4 * r + 1 + c] = (l0 * bg + l3 * ga) * Q[6 + c] + l1 * Q[c] + l2 * Q[3 + c];
         }
+      } else if (V.both_leaves) {
+        // both daughters are leaves: the frame stays the parent's.  The reverse walk forms
+        // the two columns the leaves read from it and needs no inverse boost to recover it.
       } else {
         const double e01 = -bg * st, e03 = bg * ct, e11 = ct * cphi, e12 = -sphi, e13 = st * cphi;
         const double e21 = ct * sphi, e22 = cphi, e23 = st * sphi, e31 = -ga * st, e33 = ga * ct;
@@ -465,6 +468,16 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
                        0.0, ct * cphi, -sphi, st * cphi,
                        0.0, ct * sphi, cphi,  st * sphi,
                        bg,  -ga * st, 0.0,   ga * ct};
+      // the frame's columns 0 and 3, which the leaves read: at a leaf-only visit (not a
+      // friend's) L is still the parent frame, and they are formed here
+      const bool kept = V.both_leaves && !(FRIENDS && V.friend_sign != 0);
+      double Lc0[4], Lc3[4];
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
+        Lc0[r] = kept ? l0 * ga + l3 * bg : l0;
+        Lc3[r] = kept ? l0 * L1[3] + l1 * L1[7] + l2 * L1[11] + l3 * L1[15] : l3;
+      }
       // leaf children: P_j = L (ce_j, 0, 0, +-pc)
       double pcb = 0.0, ceb[2] = {0.0, 0.0};
 #pragma unroll
@@ -479,8 +492,8 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
           for (int r = 0; r < 4; r++) {
             Lb[4 * r + 0] += P[r] * ce;
             Lb[4 * r + 3] += P[r] * sj * pc;
-            v0 += L[4 * r + 0] * P[r];
-            v3 += L[4 * r + 3] * P[r];
+            v0 += Lc0[r] * P[r];
+            v3 += Lc3[r] * P[r];
           }
           ceb[j] += v0;
           pcb += sj * v3;
@@ -581,7 +594,38 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
         // L1 has zeros at (0,2), (1,0), (2,0), (3,2), and only its other 12 entries carry
         // adjoints; the loops skip the zero terms (the compiler folds the constant ones).
         double L1b[16];
-        if (V.self_root && !lab) {
+        if (kept) {
+          // leaf-only visit: L is the parent frame itself.  The leaves read the frame's
+          // columns 0 and 3 only and no daughter visit adds to its adjoint, so Lb's columns
+          // 1 and 2 are 0: Lpre_bar = Lb L1^T over k = 0, 3 and L1bar = L^T Lb in columns 0, 3.
+#pragma unroll
+          for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+              double accb = 0.0;
+#pragma unroll
+              for (int k = 0; k < 4; k += 3) {
+                if ((c == 1 || c == 2) && k == 0) continue;   // L1's zeros
+                accb += Lb[4 * r + k] * L1[4 * c + k];
+              }
+              Lp[4 * r + c] = L[4 * r + c];
+              Lpb[4 * r + c] = accb;
+            }
+#pragma unroll
+          for (int r = 0; r < 4; r++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+              if ((r == 0 && c == 2) || (r == 1 && c == 0) || (r == 2 && c == 0) || (r == 3 && c == 2) ||
+                  c == 1 || c == 2) {
+                L1b[4 * r + c] = 0.0;
+                continue;
+              }
+              double acc = 0.0;
+#pragma unroll
+              for (int k = 0; k < 4; k++) acc += L[4 * k + r] * Lb[4 * k + c];
+              L1b[4 * r + c] = acc;
+            }
+        } else if (V.self_root && !lab) {
           // the root's parent frame is the identity: L1bar = Lb, and no parent adjoint
 #pragma unroll
           for (int i = 0; i < 16; i++) L1b[i] = Lb[i];
@@ -629,39 +673,6 @@ __global__ void __launch_bounds__(PHS_ADJ_BLOCK)
                 if (k == 3 && r == 2) continue;   // Lp (3,2) = 0
                 acc += Lp[4 * k + r] * Lb[4 * k + c];
               }
-              L1b[4 * r + c] = acc;
-            }
-        } else if (V.both_leaves) {
-          // both daughters are leaves: their momenta read the frame's columns 0 and 3 only,
-          // and no daughter visit adds to its adjoint, so Lb's columns 1 and 2 are 0
-#pragma unroll
-          for (int r = 0; r < 4; r++)
-#pragma unroll
-            for (int c = 0; c < 4; c++) {
-              double acc = 0.0, accb = 0.0;
-#pragma unroll
-              for (int k = 0; k < 4; k++) {
-                if ((c == 0 && k == 2) || (c == 1 && k == 0) || (c == 2 && k == 0) || (c == 3 && k == 2))
-                  continue;
-                if (!STORED) acc += L[4 * r + k] * (eta[k] * eta[c]) * L1[4 * c + k];
-                if (k == 0 || k == 3) accb += Lb[4 * r + k] * L1[4 * c + k];
-              }
-              Lp[4 * r + c] = STORED && phs_in(ev, store_events, PHS_CHK_STORE)
-                                  ? store[(int64_t)(v * 16 + 4 * r + c) * store_events + ev] : acc;
-              Lpb[4 * r + c] = accb;
-            }
-#pragma unroll
-          for (int r = 0; r < 4; r++)
-#pragma unroll
-            for (int c = 0; c < 4; c++) {
-              if ((r == 0 && c == 2) || (r == 1 && c == 0) || (r == 2 && c == 0) || (r == 3 && c == 2) ||
-                  c == 1 || c == 2) {
-                L1b[4 * r + c] = 0.0;
-                continue;
-              }
-              double acc = 0.0;
-#pragma unroll
-              for (int k = 0; k < 4; k++) acc += Lp[4 * k + r] * Lb[4 * k + c];
               L1b[4 * r + c] = acc;
             }
         } else {
