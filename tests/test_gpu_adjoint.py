@@ -263,3 +263,23 @@ def test_stored_matrix_form_against_finite_differences_and_recompute(torch):
     assert want <= held <= want + (2 << 20), (held, want)   # cudaMalloc's 2 MiB pages
     ps.set_adjoint_storage(ADJOINT_STORED)
     check_x_derivatives(torch, ps, proc, x, pbar, jbar, h, 0.9, "tt dx, stored-matrix form")
+
+
+@pytest.mark.parametrize("builder,E1,E2", [(P.ww, 250.0, 250.0), (P.ww, 300.0, 200.0),
+                                           (P.tt, 600.0, 400.0)])
+def test_adjoint_lab_boost_and_leaf_pairs_against_finite_differences(torch, builder, E1, E2):
+    """WW's root daughters each decay to two leaves (their frames are kept from the root's
+    in the forward pass, which is also the frame the root-daughter shortcuts assume), and
+    unequal beams (E1 = 1.2 E2) put the lab boost into the root's frame, where those
+    shortcuts do not apply; against finite differences as above."""
+    from gpu_phs_gb300.api import PhaseSpace
+    proc = builder()
+    proc.sqrts = 2.0 * np.sqrt(E1 * E2)        # the margins' upper bounds
+    n, h = 4000, 1e-6
+    x = torch.from_numpy(uniform_x(950 + proc.n_out + int(E1), n, proc.n_x)).cuda()
+    ps = PhaseSpace(proc, E1, E2)
+    g = torch.Generator(device="cuda").manual_seed(30 + proc.n_out)
+    pbar = torch.randn((n, proc.n_out, 4), generator=g, device="cuda", dtype=torch.float64)
+    jbar = torch.randn(n, generator=g, device="cuda", dtype=torch.float64)
+    check_x_derivatives(torch, ps, proc, x, pbar, jbar, h, 0.7,
+                        f"{proc.name} E1 {E1:g} E2 {E2:g} dx")
