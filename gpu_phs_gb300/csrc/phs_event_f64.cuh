@@ -502,16 +502,36 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
       }
     }
 
-    // leaf momenta: L_new * (E, 0, 0, +-p) (phs_cpu.cpp:286-291)
+    // leaf momenta: L_new * (E, 0, 0, +-p) (phs_cpu.cpp:286-291); the two leaves of a
+    // leaf-only visit share the products L_new[r][3] p
+    if (V.both_leaves) {
+      double t3[4];
 #pragma unroll
-    for (int j = 0; j < 2; j++) {
-      const PhsChild &C = V.child[j];
-      if (!C.internal && phs_in(C.out_index, ch.n_out, PHS_CHK_P)) {
-        double pj = j == 0 ? pc : -pc;
-        const double E = j == 0 ? ce0 : ce1;
-        double2 *o = reinterpret_cast<double2 *>(out + 4 * C.out_index);
-        o[0] = make_double2(Ln[0] * E + Ln[3] * pj, Ln[4] * E + Ln[7] * pj);
-        o[1] = make_double2(Ln[8] * E + Ln[11] * pj, Ln[12] * E + Ln[15] * pj);
+      for (int r = 0; r < 4; r++) t3[r] = Ln[4 * r + 3] * pc;
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        const PhsChild &C = V.child[j];
+        if (phs_in(C.out_index, ch.n_out, PHS_CHK_P)) {
+          const double E = j == 0 ? ce0 : ce1;
+          double q[4];
+#pragma unroll
+          for (int r = 0; r < 4; r++) q[r] = fma(Ln[4 * r], E, j == 0 ? t3[r] : -t3[r]);
+          double2 *o = reinterpret_cast<double2 *>(out + 4 * C.out_index);
+          o[0] = make_double2(q[0], q[1]);
+          o[1] = make_double2(q[2], q[3]);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        const PhsChild &C = V.child[j];
+        if (!C.internal && phs_in(C.out_index, ch.n_out, PHS_CHK_P)) {
+          double pj = j == 0 ? pc : -pc;
+          const double E = j == 0 ? ce0 : ce1;
+          double2 *o = reinterpret_cast<double2 *>(out + 4 * C.out_index);
+          o[0] = make_double2(Ln[0] * E + Ln[3] * pj, Ln[4] * E + Ln[7] * pj);
+          o[1] = make_double2(Ln[8] * E + Ln[11] * pj, Ln[12] * E + Ln[15] * pj);
+        }
       }
     }
 
