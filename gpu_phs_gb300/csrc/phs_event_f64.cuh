@@ -406,8 +406,16 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
     double ct, st, fct;
     map_ct(V.ct_class, xrow_at(xe, V.x_ct, seg.x_stride), b0, b1, ct, st, fct);
     if (V.ct_class == PHS_CT_COLLINEAR) factor *= fct;   // the uniform map's factor is 1
-    const double e01 = -bg * st, e03 = bg * ct, e11 = ct * cphi, e12 = -sphi, e13 = st * cphi;
-    const double e21 = ct * sphi, e22 = cphi, e23 = st * sphi, e31 = -ga * st, e33 = ga * ct;
+    const double e03 = bg * ct, e12 = -sphi, e13 = st * cphi;
+    const double e22 = cphi, e23 = st * sphi, e33 = ga * ct;
+    // the entries of L1 that only the frame's columns 1 and 2 read: formed in the branches
+    // that write those (a leaf-only visit writes columns 0 and 3 only)
+    const auto col12 = [&](double &e01, double &e11, double &e21, double &e31) {
+      e01 = -bg * st;
+      e11 = ct * cphi;
+      e21 = ct * sphi;
+      e31 = -ga * st;
+    };
 
     double Ln[16];
     if (V.friend_sign != 0) {
@@ -420,6 +428,8 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
       double Rf[9];
       rot_z_onto(-(L[1] - ff * L[13]), -(L[2] - ff * L[14]),
                  -bg * u0 - ga * (L[3] - ff * L[15]), Rf);
+      double e01, e11, e21, e31;
+      col12(e01, e11, e21, e31);
       const double A[9] = {e11, e12, e13, e21, e22, e23, -st, 0.0, ct};
       double Q[9];
 #pragma unroll
@@ -440,6 +450,8 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
       }
     } else if (V.self_root && !lab) {
       // parent frame is the identity: L0 * L1 = L1
+      double e01, e11, e21, e31;
+      col12(e01, e11, e21, e31);
       Ln[0] = ga;  Ln[1] = e01; Ln[2] = 0.0;  Ln[3] = e03;
       Ln[4] = 0.0; Ln[5] = e11; Ln[6] = e12;  Ln[7] = e13;
       Ln[8] = 0.0; Ln[9] = e21; Ln[10] = e22; Ln[11] = e23;
@@ -449,6 +461,8 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
       // keep the general product, which leaves their registers to the common case)
       // the parent frame is the lab boost B_z(lab_bg): rows 1 and 2 are unit rows, and the
       // root's bg is 0 and its gamma 1
+      double e01, e11, e21, e31;
+      col12(e01, e11, e21, e31);
       Ln[0] = L[0];   Ln[1] = L[3] * e31;  Ln[2] = 0.0;  Ln[3] = L[3] * e33;
       Ln[4] = 0.0;    Ln[5] = e11;         Ln[6] = e12;  Ln[7] = e13;
       Ln[8] = 0.0;    Ln[9] = e21;         Ln[10] = e22; Ln[11] = e23;
@@ -456,6 +470,8 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
     } else if (V.parent_root && !lab) {
       // the parent frame is the root's rotation (its bg is 0 and its gamma 1): row 0 is
       // (1, 0, 0, 0) and L[4], L[8], L[12], L[14] are 0, so half the products drop out
+      double e01 = 0.0, e11 = 0.0, e21 = 0.0, e31 = 0.0;
+      if (!V.both_leaves) col12(e01, e11, e21, e31);
       Ln[0] = ga;  Ln[1] = e01; Ln[2] = 0.0;  Ln[3] = e03;
 #pragma unroll
       for (int r = 1; r < 4; r++) {
@@ -472,6 +488,8 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
       }
     } else if (PER_EVENT && V.parent_root) {
       // the root's frame with the lab boost: entries (0,2), (1,0), (2,0), (3,2) are 0
+      double e01 = 0.0, e11 = 0.0, e21 = 0.0, e31 = 0.0;
+      if (!V.both_leaves) col12(e01, e11, e21, e31);
 #pragma unroll
       for (int r = 0; r < 4; r++) {
         const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
@@ -486,19 +504,26 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
           Ln[4 * r + 2] = 0.0;
         }
       }
-    } else {
+    } else if (V.both_leaves) {
+      // both daughters are leaves: their momenta read the frame's columns 0 and 3 only
 #pragma unroll
       for (int r = 0; r < 4; r++) {
         const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
         Ln[4 * r + 0] = l0 * ga + l3 * bg;
         Ln[4 * r + 3] = l0 * e03 + l1 * e13 + l2 * e23 + l3 * e33;
-        if (!V.both_leaves) {
-          Ln[4 * r + 1] = l0 * e01 + l1 * e11 + l2 * e21 + l3 * e31;
-          Ln[4 * r + 2] = l1 * e12 + l2 * e22;
-        } else {
-          Ln[4 * r + 1] = 0.0;
-          Ln[4 * r + 2] = 0.0;
-        }
+        Ln[4 * r + 1] = 0.0;
+        Ln[4 * r + 2] = 0.0;
+      }
+    } else {
+      double e01, e11, e21, e31;
+      col12(e01, e11, e21, e31);
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
+        Ln[4 * r + 0] = l0 * ga + l3 * bg;
+        Ln[4 * r + 3] = l0 * e03 + l1 * e13 + l2 * e23 + l3 * e33;
+        Ln[4 * r + 1] = l0 * e01 + l1 * e11 + l2 * e21 + l3 * e31;
+        Ln[4 * r + 2] = l1 * e12 + l2 * e22;
       }
     }
 
