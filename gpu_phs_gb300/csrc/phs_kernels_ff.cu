@@ -311,11 +311,20 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
       fct = one;
     }
     if (V.ct_class == PHS_CT_COLLINEAR) factor = ff_mul(factor, fct);   // uniform: 1
-    const ff e01 = ff_neg(ff_mul(bg, st)), e03 = ff_mul(bg, ct), e11 = ff_mul(ct, cphi);
-    const ff e12 = ff_neg(sphi), e13 = ff_mul(st, cphi), e21 = ff_mul(ct, sphi), e22 = cphi;
-    const ff e23 = ff_mul(st, sphi), e31 = ff_neg(ff_mul(ga, st)), e33 = ff_mul(ga, ct);
+    const ff e03 = ff_mul(bg, ct), e12 = ff_neg(sphi), e13 = ff_mul(st, cphi), e22 = cphi;
+    const ff e23 = ff_mul(st, sphi), e33 = ff_mul(ga, ct);
+    // the entries of L1 that only the frame's columns 1 and 2 read: formed in the branches
+    // that write those (a leaf-only visit writes columns 0 and 3 only)
+    const auto col12 = [&](ff &e01, ff &e11, ff &e21, ff &e31) {
+      e01 = ff_neg(ff_mul(bg, st));
+      e11 = ff_mul(ct, cphi);
+      e21 = ff_mul(ct, sphi);
+      e31 = ff_neg(ff_mul(ga, st));
+    };
 
     if (V.self_root && !lab) {
+      ff e01, e11, e21, e31;
+      col12(e01, e11, e21, e31);
       L[0] = ga;   L[1] = e01;  L[2] = zero;  L[3] = e03;
       L[4] = zero; L[5] = e11;  L[6] = e12;   L[7] = e13;
       L[8] = zero; L[9] = e21;  L[10] = e22;  L[11] = e23;
@@ -324,6 +333,8 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
       // (per-event beams, where nearly every event has a lab boost; the uniform-beam kernels
       // keep the general product, which leaves their registers to the common case)
       // the parent frame is the lab boost B_z(lab_bg): rows 1 and 2 are unit rows
+      ff e01, e11, e21, e31;
+      col12(e01, e11, e21, e31);
       const ff g0 = L[0], b0 = L[3];
       L[0] = ff_dot2(g0, ga, b0, bg);   L[1] = ff_dot2(g0, e01, b0, e31);
       L[2] = zero;                      L[3] = ff_dot2(g0, e03, b0, e33);
@@ -334,6 +345,8 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
     } else if (V.parent_root && !lab) {
       // the parent frame is the root's rotation (its bg is 0 and its gamma 1): row 0 is
       // (1, 0, 0, 0) and L[4], L[8], L[12], L[14] are 0, so half the products drop out
+      ff e01 = zero, e11 = zero, e21 = zero, e31 = zero;
+      if (!V.both_leaves) col12(e01, e11, e21, e31);
       L[0] = ga;   L[1] = e01;  L[2] = zero;  L[3] = e03;
 #pragma unroll
       for (int r = 1; r < 4; r++) {
@@ -347,6 +360,8 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
       }
     } else if (PER_EVENT && V.parent_root) {
       // the root's frame with the lab boost: entries (0,2), (1,0), (2,0), (3,2) are 0
+      ff e01 = zero, e11 = zero, e21 = zero, e31 = zero;
+      if (!V.both_leaves) col12(e01, e11, e21, e31);
 #pragma unroll
       for (int r = 0; r < 4; r++) {
         const ff l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
@@ -358,17 +373,25 @@ __device__ __forceinline__ bool phs_event_ff(const PhsLaunch &a, const PhsSegmen
           L[4 * r + 2] = edge ? ff_mul(l1, e12) : ff_dot2(l1, e12, l2, e22);
         }
       }
-    } else {
-      // row r of L L1 depends on row r of L only: update in place
+    } else if (V.both_leaves) {
+      // both daughters are leaves: their momenta read the frame's columns 0 and 3 only
 #pragma unroll
       for (int r = 0; r < 4; r++) {
         const ff l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
         L[4 * r + 0] = ff_dot2(l0, ga, l3, bg);
         L[4 * r + 3] = ff_dot4(l0, e03, l1, e13, l2, e23, l3, e33);
-        if (!V.both_leaves) {
-          L[4 * r + 1] = ff_dot4(l0, e01, l1, e11, l2, e21, l3, e31);
-          L[4 * r + 2] = ff_dot2(l1, e12, l2, e22);
-        }
+      }
+    } else {
+      // row r of L L1 depends on row r of L only: update in place
+      ff e01, e11, e21, e31;
+      col12(e01, e11, e21, e31);
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        const ff l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
+        L[4 * r + 0] = ff_dot2(l0, ga, l3, bg);
+        L[4 * r + 3] = ff_dot4(l0, e03, l1, e13, l2, e23, l3, e33);
+        L[4 * r + 1] = ff_dot4(l0, e01, l1, e11, l2, e21, l3, e31);
+        L[4 * r + 2] = ff_dot2(l1, e12, l2, e22);
       }
     }
 
