@@ -417,7 +417,7 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
       e31 = -ga * st;
     };
 
-    double Ln[16];
+    // the frame is updated in place: row r of L L1 depends on row r of L only
     if (V.friend_sign != 0) {
       // friend boost (phs.cu:853-910): the decay angles are measured from the friend
       // beam's direction in the branch's rest frame, B_z(-bg) L^-1 (1, 0, 0, ff) (only
@@ -446,16 +446,16 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
         const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
 #pragma unroll
         for (int c = 0; c < 4; c++)
-          Ln[4 * r + c] = l0 * E1r[c] + l1 * E2r[c] + l2 * E3r[c] + l3 * E4r[c];
+          L[4 * r + c] = l0 * E1r[c] + l1 * E2r[c] + l2 * E3r[c] + l3 * E4r[c];
       }
     } else if (V.self_root && !lab) {
       // parent frame is the identity: L0 * L1 = L1
       double e01, e11, e21, e31;
       col12(e01, e11, e21, e31);
-      Ln[0] = ga;  Ln[1] = e01; Ln[2] = 0.0;  Ln[3] = e03;
-      Ln[4] = 0.0; Ln[5] = e11; Ln[6] = e12;  Ln[7] = e13;
-      Ln[8] = 0.0; Ln[9] = e21; Ln[10] = e22; Ln[11] = e23;
-      Ln[12] = bg; Ln[13] = e31; Ln[14] = 0.0; Ln[15] = e33;
+      L[0] = ga;  L[1] = e01; L[2] = 0.0;  L[3] = e03;
+      L[4] = 0.0; L[5] = e11; L[6] = e12;  L[7] = e13;
+      L[8] = 0.0; L[9] = e21; L[10] = e22; L[11] = e23;
+      L[12] = bg; L[13] = e31; L[14] = 0.0; L[15] = e33;
     } else if (PER_EVENT && V.self_root) {
       // (per-event beams, where nearly every event has a lab boost; the uniform-beam kernels
       // keep the general product, which leaves their registers to the common case)
@@ -463,27 +463,28 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
       // root's bg is 0 and its gamma 1
       double e01, e11, e21, e31;
       col12(e01, e11, e21, e31);
-      Ln[0] = L[0];   Ln[1] = L[3] * e31;  Ln[2] = 0.0;  Ln[3] = L[3] * e33;
-      Ln[4] = 0.0;    Ln[5] = e11;         Ln[6] = e12;  Ln[7] = e13;
-      Ln[8] = 0.0;    Ln[9] = e21;         Ln[10] = e22; Ln[11] = e23;
-      Ln[12] = L[12]; Ln[13] = L[15] * e31; Ln[14] = 0.0; Ln[15] = L[15] * e33;
+      const double g0 = L[0], b0 = L[3], b3 = L[12], g3 = L[15];
+      L[0] = g0;     L[1] = b0 * e31;    L[2] = 0.0;  L[3] = b0 * e33;
+      L[4] = 0.0;    L[5] = e11;         L[6] = e12;  L[7] = e13;
+      L[8] = 0.0;    L[9] = e21;         L[10] = e22; L[11] = e23;
+      L[12] = b3;    L[13] = g3 * e31;   L[14] = 0.0; L[15] = g3 * e33;
     } else if (V.parent_root && !lab) {
       // the parent frame is the root's rotation (its bg is 0 and its gamma 1): row 0 is
       // (1, 0, 0, 0) and L[4], L[8], L[12], L[14] are 0, so half the products drop out
       double e01 = 0.0, e11 = 0.0, e21 = 0.0, e31 = 0.0;
       if (!V.both_leaves) col12(e01, e11, e21, e31);
-      Ln[0] = ga;  Ln[1] = e01; Ln[2] = 0.0;  Ln[3] = e03;
+      L[0] = ga;  L[1] = e01; L[2] = 0.0;  L[3] = e03;
 #pragma unroll
       for (int r = 1; r < 4; r++) {
         const double l1 = L[4 * r + 1], l2 = r < 3 ? L[4 * r + 2] : 0.0, l3 = L[4 * r + 3];
-        Ln[4 * r + 0] = l3 * bg;
-        Ln[4 * r + 3] = r < 3 ? l1 * e13 + l2 * e23 + l3 * e33 : l1 * e13 + l3 * e33;
+        L[4 * r + 0] = l3 * bg;
+        L[4 * r + 3] = r < 3 ? l1 * e13 + l2 * e23 + l3 * e33 : l1 * e13 + l3 * e33;
         if (!V.both_leaves) {
-          Ln[4 * r + 1] = r < 3 ? l1 * e11 + l2 * e21 + l3 * e31 : l1 * e11 + l3 * e31;
-          Ln[4 * r + 2] = r < 3 ? l1 * e12 + l2 * e22 : l1 * e12;
+          L[4 * r + 1] = r < 3 ? l1 * e11 + l2 * e21 + l3 * e31 : l1 * e11 + l3 * e31;
+          L[4 * r + 2] = r < 3 ? l1 * e12 + l2 * e22 : l1 * e12;
         } else {
-          Ln[4 * r + 1] = 0.0;
-          Ln[4 * r + 2] = 0.0;
+          L[4 * r + 1] = 0.0;
+          L[4 * r + 2] = 0.0;
         }
       }
     } else if (PER_EVENT && V.parent_root) {
@@ -494,14 +495,14 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
       for (int r = 0; r < 4; r++) {
         const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
         const bool edge = r == 0 || r == 3;   // l2 = 0; otherwise l0 = 0
-        Ln[4 * r + 0] = edge ? l0 * ga + l3 * bg : l3 * bg;
-        Ln[4 * r + 3] = edge ? l0 * e03 + l1 * e13 + l3 * e33 : l1 * e13 + l2 * e23 + l3 * e33;
+        L[4 * r + 0] = edge ? l0 * ga + l3 * bg : l3 * bg;
+        L[4 * r + 3] = edge ? l0 * e03 + l1 * e13 + l3 * e33 : l1 * e13 + l2 * e23 + l3 * e33;
         if (!V.both_leaves) {
-          Ln[4 * r + 1] = edge ? l0 * e01 + l1 * e11 + l3 * e31 : l1 * e11 + l2 * e21 + l3 * e31;
-          Ln[4 * r + 2] = edge ? l1 * e12 : l1 * e12 + l2 * e22;
+          L[4 * r + 1] = edge ? l0 * e01 + l1 * e11 + l3 * e31 : l1 * e11 + l2 * e21 + l3 * e31;
+          L[4 * r + 2] = edge ? l1 * e12 : l1 * e12 + l2 * e22;
         } else {
-          Ln[4 * r + 1] = 0.0;
-          Ln[4 * r + 2] = 0.0;
+          L[4 * r + 1] = 0.0;
+          L[4 * r + 2] = 0.0;
         }
       }
     } else if (V.both_leaves) {
@@ -509,10 +510,10 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
 #pragma unroll
       for (int r = 0; r < 4; r++) {
         const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
-        Ln[4 * r + 0] = l0 * ga + l3 * bg;
-        Ln[4 * r + 3] = l0 * e03 + l1 * e13 + l2 * e23 + l3 * e33;
-        Ln[4 * r + 1] = 0.0;
-        Ln[4 * r + 2] = 0.0;
+        L[4 * r + 0] = l0 * ga + l3 * bg;
+        L[4 * r + 3] = l0 * e03 + l1 * e13 + l2 * e23 + l3 * e33;
+        L[4 * r + 1] = 0.0;
+        L[4 * r + 2] = 0.0;
       }
     } else {
       double e01, e11, e21, e31;
@@ -520,10 +521,10 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
 #pragma unroll
       for (int r = 0; r < 4; r++) {
         const double l0 = L[4 * r], l1 = L[4 * r + 1], l2 = L[4 * r + 2], l3 = L[4 * r + 3];
-        Ln[4 * r + 0] = l0 * ga + l3 * bg;
-        Ln[4 * r + 3] = l0 * e03 + l1 * e13 + l2 * e23 + l3 * e33;
-        Ln[4 * r + 1] = l0 * e01 + l1 * e11 + l2 * e21 + l3 * e31;
-        Ln[4 * r + 2] = l1 * e12 + l2 * e22;
+        L[4 * r + 0] = l0 * ga + l3 * bg;
+        L[4 * r + 3] = l0 * e03 + l1 * e13 + l2 * e23 + l3 * e33;
+        L[4 * r + 1] = l0 * e01 + l1 * e11 + l2 * e21 + l3 * e31;
+        L[4 * r + 2] = l1 * e12 + l2 * e22;
       }
     }
 
@@ -532,7 +533,7 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
     if (V.both_leaves) {
       double t3[4];
 #pragma unroll
-      for (int r = 0; r < 4; r++) t3[r] = Ln[4 * r + 3] * pc;
+      for (int r = 0; r < 4; r++) t3[r] = L[4 * r + 3] * pc;
 #pragma unroll
       for (int j = 0; j < 2; j++) {
         const PhsChild &C = V.child[j];
@@ -540,7 +541,7 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
           const double E = j == 0 ? ce0 : ce1;
           double q[4];
 #pragma unroll
-          for (int r = 0; r < 4; r++) q[r] = fma(Ln[4 * r], E, j == 0 ? t3[r] : -t3[r]);
+          for (int r = 0; r < 4; r++) q[r] = fma(L[4 * r], E, j == 0 ? t3[r] : -t3[r]);
           double2 *o = reinterpret_cast<double2 *>(out + 4 * C.out_index);
           o[0] = make_double2(q[0], q[1]);
           o[1] = make_double2(q[2], q[3]);
@@ -554,8 +555,8 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
           double pj = j == 0 ? pc : -pc;
           const double E = j == 0 ? ce0 : ce1;
           double2 *o = reinterpret_cast<double2 *>(out + 4 * C.out_index);
-          o[0] = make_double2(Ln[0] * E + Ln[3] * pj, Ln[4] * E + Ln[7] * pj);
-          o[1] = make_double2(Ln[8] * E + Ln[11] * pj, Ln[12] * E + Ln[15] * pj);
+          o[0] = make_double2(L[0] * E + L[3] * pj, L[4] * E + L[7] * pj);
+          o[1] = make_double2(L[8] * E + L[11] * pj, L[12] * E + L[15] * pj);
         }
       }
     }
@@ -565,7 +566,7 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
     if (V.push >= 0 && phs_in(sp, a.stack_depth, PHS_CHK_STACK)) {
       const bool j0 = V.push == 0;
 #pragma unroll
-      for (int i = 0; i < 16; i++) stack_store<BLOCK>(smem, sp, i, Ln[i]);
+      for (int i = 0; i < 16; i++) stack_store<BLOCK>(smem, sp, i, L[i]);
       stack_store<BLOCK>(smem, sp, 16, j0 ? cmsq[0] : cmsq[1]);
       stack_store<BLOCK>(smem, sp, 17, j0 ? cm[0] : cm[1]);
       stack_store<BLOCK>(smem, sp, 18, j0 ? pc : -pc);
@@ -575,8 +576,6 @@ __device__ __forceinline__ void phs_event_f64(const PhsLaunch &a, const PhsSegme
     }
     if (V.carry >= 0) {
       const bool j0 = V.carry == 0;
-#pragma unroll
-      for (int i = 0; i < 16; i++) L[i] = Ln[i];
       msq_b = j0 ? cmsq[0] : cmsq[1];
       m_b = j0 ? cm[0] : cm[1];
       p_b = j0 ? pc : -pc;
