@@ -1074,10 +1074,13 @@ extern "C" int phs_generate_host(phs_process_t h, int64_t n_events, const int64_
       CUDA_TRY(cudaMemcpyAsync(p + e0 * 4 * n_out, h->bp[s].ptr, n * 4 * n_out * sizeof(double),
                                cudaMemcpyDeviceToHost, st));
       CUDA_TRY(cudaMemcpyAsync(f + e0, h->bf[s].ptr, n * sizeof(double), cudaMemcpyDeviceToHost, st));
-      CUDA_TRY(cudaMemcpyAsync(v + e0, h->bv[s].ptr, n * sizeof(double), cudaMemcpyDeviceToHost, st));
       CUDA_TRY(cudaMemcpyAsync(ok + e0, h->bo[s].ptr, n, cudaMemcpyDeviceToHost, st));
       e0 += n;
     }
+    // The volume of an event is its channel's (uniform beams: the kernels write the compiled
+    // PhsChannel::volume), so the host writes it while the copies run instead of copying
+    // 8 bytes per event back: the call is bound by the host link.
+    for (int c = 0; c < nch; c++) std::fill(v + prefix[c], v + prefix[c + 1], h->prog[c].volume);
     for (int s = 0; s < phs_process::kStreams; s++) CUDA_TRY(cudaStreamSynchronize(h->streams[s]));
     return PHS_OK;
   });

@@ -220,6 +220,25 @@ def test_host_path_matches_device(torch):
     assert torch.equal(h.factor, d.factor.cpu()) and torch.equal(h.volume, d.volume.cpu())
 
 
+def test_host_path_matches_device_many_channels(torch):
+    """40 channels with uneven counts through the pipelined host call (the volumes are
+    written on the host per channel, the rest copied back per chunk): the device path's bits."""
+    from gpu_phs_gb300.api import PhaseSpace
+    rng = np.random.default_rng(21)
+    proc = P.random_process(rng, 6, 40, 1000.0)
+    counts = rng.integers(0, 60_000, proc.n_channels).astype(np.int64)
+    counts[::9] = 0
+    n = int(counts.sum())
+    x = uniform_x(23, n, proc.n_x)
+    ps = PhaseSpace(proc, 500.0, 500.0)
+    xh = torch.from_numpy(x).pin_memory()
+    h = ps.generate_host(xh, counts)
+    d = ps.generate(xh.cuda(), counts)
+    torch.cuda.synchronize()
+    assert torch.equal(h.p, d.p.cpu()) and torch.equal(h.ok, d.ok.cpu())
+    assert torch.equal(h.factor, d.factor.cpu()) and torch.equal(h.volume, d.volume.cpu())
+
+
 @pytest.mark.parametrize("beams", ["uniform", "asymmetric", "random"])
 def test_per_event_beams(torch, beams):
     from gpu_phs_gb300.api import PhaseSpace
