@@ -383,7 +383,7 @@ cudaError_t phs_launch_philox(double *x, int64_t n_events, int32_t n_x, uint64_t
 // and drivers that would otherwise synchronise the device inside their hot loop.  The
 // channel programs and the segment table, which the regular entry points keep in buffers
 // the library allocates, live here in one file-scope device array instead.  Every GPU
-// that loads the library holds this array (sizeof(PhsNoAllocScratch), about 0.8 MB) until
+// that loads the library holds this array (sizeof(PhsNoAllocScratch), about 1 MB) until
 // the process exits.  All calls share it and it keeps the last call's contents; each call
 // overwrites everything it reads, so nothing needs clearing, but calls that overlap on
 // the GPU (different streams or host threads) race on it.
