@@ -857,8 +857,8 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-PROFILE_CASES = ("f64_tt", "ff_tt", "f64_batched", "f64_split_batched", "ff_batched", "inverse_bwbw",
-                 "adjoint_tt", "adjoint_tt_stored")
+PROFILE_CASES = ("f64_tt", "ff_tt", "f64_tt_beams", "ff_tt_beams", "f64_batched", "f64_split_batched",
+                 "ff_batched", "inverse_bwbw", "adjoint_tt", "adjoint_tt_stored")
 
 
 def run_case(name: str) -> None:
@@ -881,6 +881,22 @@ def run_case(name: str) -> None:
         o = ps.alloc(n)
         for _ in range(2):
             ps.generate(x, out=o)
+    elif name in ("f64_tt_beams", "ff_tt_beams"):   # 2^21 tt events, per-event beam energies
+        proc = P.tt()
+        n = 1 << 21
+        ps = PhaseSpace(proc)
+        if name == "ff_tt_beams":
+            ps.set_precision(1)
+            ps.set_variants(1, -1)
+        else:
+            ps.set_variants(-1, 0)
+        x = philox_x(n, proc.n_x, SEED)
+        g = torch.Generator(device="cuda").manual_seed(SEED)
+        E1 = proc.sqrts * (0.3 + 0.4 * torch.rand(n, generator=g, device="cuda", dtype=torch.float64))
+        E2 = proc.sqrts * (0.3 + 0.4 * torch.rand(n, generator=g, device="cuda", dtype=torch.float64))
+        o = ps.alloc(n)
+        for _ in range(2):
+            ps.generate_beams(x, E1, E2, out=o)
     elif name in ("f64_batched", "f64_split_batched", "ff_batched"):   # 2^22 batched events
         procs, counts = P.batched(seed=2024, n_channels=64, total_events=1 << 22)
         b = Batch([PhaseSpace(p, 500.0, 500.0) for p in procs])
