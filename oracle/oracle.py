@@ -89,6 +89,7 @@ class Oracle:
                                                 _pd, _pd, _pd, _pd, _pd, _pu8, C.c_int]
             L.oracle_generate_cond.argtypes = [C.c_void_p, C.c_long, C.c_int, _pd, C.c_void_p,
                                                _pd, _pd, _pd, _pu8, _pd, C.c_int]
+            L.oracle_set_nudge.argtypes = [C.c_void_p, C.c_int]
             L.oracle_set_friends.restype = C.c_int
             L.oracle_set_friends.argtypes = [C.c_void_p, _pi]
             L.oracle_inverse.restype = C.c_int
@@ -129,9 +130,12 @@ class Oracle:
 
     def generate(self, x: np.ndarray, channels: Optional[np.ndarray] = None,
                  threads: int = 0, E1: Optional[np.ndarray] = None,
-                 E2: Optional[np.ndarray] = None, condition: bool = False) -> Result:
+                 E2: Optional[np.ndarray] = None, condition: bool = False,
+                 nudge: int = 0) -> Result:
         """condition=True (uniform beams) also returns r.kappa, the per-event condition of
-        the Kallen functions (oracle_generate_cond in phs_oracle.c)."""
+        the Kallen functions (oracle_generate_cond in phs_oracle.c).  nudge != 0 (per-event
+        beams): every per-event constant that a transcendental function returns moved by
+        that many ulps (oracle_set_nudge), a sensitivity probe for tests."""
         x = np.ascontiguousarray(x, np.float64)
         n, n_x = x.shape
         r = Result(n, self.proc.n_out)
@@ -140,6 +144,8 @@ class Oracle:
             channels = np.ascontiguousarray(channels, np.int32)
             chp = channels.ctypes.data_as(C.c_void_p)
         threads = threads or os.cpu_count() or 1
+        if nudge and E1 is None:
+            raise ValueError("nudge moves per-event constants: give E1 and E2")
         if condition:
             if E1 is not None:
                 raise ValueError("condition numbers are computed for uniform beams")
@@ -152,8 +158,13 @@ class Oracle:
         else:
             E1 = np.ascontiguousarray(np.broadcast_to(E1, (n,)), np.float64)
             E2 = np.ascontiguousarray(np.broadcast_to(E2, (n,)), np.float64)
-            self.lib().oracle_generate_beams(self.h, n, n_x, x.reshape(-1), chp, E1, E2,
-                                             r.p.reshape(-1), r.factor, r.volume, r.ok, threads)
+            self.lib().oracle_set_nudge(self.h, int(nudge))
+            try:
+                self.lib().oracle_generate_beams(self.h, n, n_x, x.reshape(-1), chp, E1, E2,
+                                                 r.p.reshape(-1), r.factor, r.volume, r.ok,
+                                                 threads)
+            finally:
+                self.lib().oracle_set_nudge(self.h, 0)
         return r
 
     def inverse(self, p: np.ndarray, channels: Optional[np.ndarray] = None,

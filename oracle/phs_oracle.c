@@ -78,6 +78,7 @@ typedef struct {
   double *flv_masses;     /* n_in + n_out */
   int *friend_sign;       /* [c*stride + code]: 0, or the beam direction +-1 of a friend */
   double sqrts;           /* sqrts the constants were computed for */
+  int nudge;              /* per-event constants moved by this many ulps (see below) */
 } oracle_t;
 
 static int map_id_known(int t) {
@@ -101,8 +102,23 @@ static double mass_sum_rec(const oracle_t *o, int c, int code) {
   return o->mass_sum[i];
 }
 
-/* phs_cpu.cpp:452-531, for one channel and one sqrts, into a/b. */
-static void constants_for(const oracle_t *o, int c, double sqrts, double *a_out, double *b_out) {
+/* x moved by k ulps (k > 0 up, k < 0 down). */
+static double ulps_moved(double x, int k) {
+  for (; k > 0; k--) x = nextafter(x, INFINITY);
+  for (; k < 0; k++) x = nextafter(x, -INFINITY);
+  return x;
+}
+
+/* phs_cpu.cpp:452-531, for one channel and one sqrts, into a/b.  nudge != 0 (a test's
+ * sensitivity probe, never the reference's arithmetic) moves every constant that a
+ * transcendental function returns -- the Breit-Wigner bound a1 = atan(.), the logarithms
+ * of the exponential maps and of the cos(theta) map, the step maps' exp/log/sqrt
+ * constants -- by nudge ulps where it is formed, so that the constants computed from it
+ * (a2 = (a1 - a0) m w / s) follow: a device evaluating them per event with its own
+ * library (or its own series) is within a few ulps of these, and far in a Breit-Wigner
+ * tail one ulp of a1 moves the mapped mass by m w (1 + u^2) ulp(a1). */
+static void constants_for(const oracle_t *o, int c, double sqrts, double *a_out, double *b_out,
+                          int nudge) {
   double m_tot = o->mass_sum[c * o->stride + o->n_codes];
   for (int code = 1; code <= o->n_codes; code++) {
     int i = c * o->stride + code;
@@ -124,7 +140,7 @@ static void constants_for(const oracle_t *o, int c, double sqrts, double *a_out,
       case OR_MAP_SCHANNEL:
         msq0 = m * m;
         a[0] = atan((msq_min - msq0) / (m * w));
-        a[1] = atan((msq_max - msq0) / (m * w));
+        a[1] = ulps_moved(atan((msq_max - msq0) / (m * w)), nudge);
         a[2] = (a[1] - a[0]) * (m * w) / s;
         break;
       case OR_MAP_RADIATION:
@@ -132,28 +148,28 @@ static void constants_for(const oracle_t *o, int c, double sqrts, double *a_out,
       case OR_MAP_INFRARED:
         msq0 = (t == OR_MAP_RADIATION) ? w * w : m * m;
         a[0] = msq0;
-        a[1] = log((msq_max - msq_min) / msq0 + 1);
+        a[1] = ulps_moved(log((msq_max - msq_min) / msq0 + 1), nudge);
         a[2] = a[1] / s;
         break;
       case OR_MAP_TCHANNEL:
       case OR_MAP_UCHANNEL:
         msq0 = m * m;
         a[0] = msq0;
-        a[1] = 2 * log((msq_max - msq_min) / (2 * msq0) + 1);
+        a[1] = ulps_moved(2 * log((msq_max - msq_min) / (2 * msq0) + 1), nudge);
         a[2] = a[1] / s;
         break;
       case OR_MAP_STEP_E: {
         double r = 2 * m * w / (msq_max - msq_min);
         a[2] = r > 0.01 ? r : 0.01;
-        a[1] = exp(-(m * m - msq_min) / (msq_max - msq_min) / a[2]);
-        a[0] = 1 - a[2] * log((1 + a[1] * exp(1 / a[2])) / (1 + a[1]));
+        a[1] = ulps_moved(exp(-(m * m - msq_min) / (msq_max - msq_min) / a[2]), nudge);
+        a[0] = ulps_moved(1 - a[2] * log((1 + a[1] * exp(1 / a[2])) / (1 + a[1])), nudge);
         break;
       }
       case OR_MAP_STEP_H: {
         a[2] = (m * m - msq_min) / (msq_max - msq_min);
         double r = pow(2 * m * w / (msq_max - msq_min), 2) / a[2];
         a[1] = r > 0.000001 ? r : 0.000001;
-        a[0] = (1 + sqrt(1 + 4 * a[1] / (1 - a[2]))) / 2;
+        a[0] = ulps_moved((1 + sqrt(1 + 4 * a[1] / (1 - a[2]))) / 2, nudge);
         break;
       }
     }
@@ -162,7 +178,7 @@ static void constants_for(const oracle_t *o, int c, double sqrts, double *a_out,
       case OR_MAP_UCHANNEL:
       case OR_MAP_COLLINEAR:
         b[0] = m * m / s;
-        b[1] = log((b[0] + 1) / b[0]);
+        b[1] = ulps_moved(log((b[0] + 1) / b[0]), nudge);
         b[2] = 0;
         break;
       default:
@@ -173,7 +189,7 @@ static void constants_for(const oracle_t *o, int c, double sqrts, double *a_out,
 
 /* phs_cpu.cpp:12-61 */
 static void msq_from_x(int t, double x, double s, double m, double w, double msq_min, double msq_max,
-                       const double *a, double *msq, double *factor) {
+                       const double *a, double *msq, double *factor, int nudge) {
   double msq1, tmp, z;
   switch (t) {
     case OR_MAP_NO:
@@ -183,7 +199,7 @@ static void msq_from_x(int t, double x, double s, double m, double w, double msq
     case OR_MAP_SCHANNEL:
       z = (1 - x) * a[0] + x * a[1];
       if (-OR_PI / 2 < z && z < OR_PI / 2) {
-        tmp = tan(z);
+        tmp = ulps_moved(tan(z), nudge);
         *msq = m * (m + w * tmp);
         *factor = a[2] * (1 + tmp * tmp);
       } else {
@@ -194,17 +210,17 @@ static void msq_from_x(int t, double x, double s, double m, double w, double msq
     case OR_MAP_COLLINEAR:
     case OR_MAP_INFRARED:
     case OR_MAP_RADIATION:
-      msq1 = a[0] * exp(x * a[1]);
+      msq1 = a[0] * ulps_moved(exp(x * a[1]), nudge);
       *msq = msq1 - a[0] + msq_min;
       *factor = a[2] * msq1;
       break;
     case OR_MAP_TCHANNEL:
     case OR_MAP_UCHANNEL:
       if (x < 0.5) {
-        msq1 = a[0] * exp(x * a[1]);
+        msq1 = a[0] * ulps_moved(exp(x * a[1]), nudge);
         *msq = msq1 - a[0] + msq_min;
       } else {
-        msq1 = a[0] * exp((1 - x) * a[1]);
+        msq1 = a[0] * ulps_moved(exp((1 - x) * a[1]), nudge);
         *msq = -(msq1 - a[0]) + msq_max;
       }
       *factor = a[2] * msq1;
@@ -215,8 +231,8 @@ static void msq_from_x(int t, double x, double s, double m, double w, double msq
       *factor = (a[1] / ((a[0] - x) * (a[0] - x)) + a[2]) * (msq_max - msq_min) / s;
       break;
     case OR_MAP_STEP_E:
-      tmp = exp(-x * a[0] / a[2]) * (1 + a[1]);
-      z = -a[2] * log(tmp - a[1]);
+      tmp = ulps_moved(exp(-x * a[0] / a[2]), nudge) * (1 + a[1]);
+      z = -a[2] * ulps_moved(log(tmp - a[1]), nudge);
       *msq = z * msq_max + (1 - z) * msq_min;
       *factor = a[0] / (1 - a[1] / tmp) * (msq_max - msq_min) / s;
       break;
@@ -224,17 +240,18 @@ static void msq_from_x(int t, double x, double s, double m, double w, double msq
 }
 
 /* phs_cpu.cpp:112-146 */
-static void ct_from_x(int t, double x, const double *b, double *ct, double *st, double *factor) {
+static void ct_from_x(int t, double x, const double *b, double *ct, double *st, double *factor,
+                      int nudge) {
   double tmp;
   switch (t) {
     case OR_MAP_COLLINEAR:
     case OR_MAP_TCHANNEL:
     case OR_MAP_UCHANNEL:
       if (x < 0.5) {
-        tmp = b[0] * exp(2 * x * b[1]);
+        tmp = b[0] * ulps_moved(exp(2 * x * b[1]), nudge);
         *ct = tmp - b[0] - 1;
       } else {
-        tmp = b[0] * exp(2 * (1 - x) * b[1]);
+        tmp = b[0] * ulps_moved(exp(2 * (1 - x) * b[1]), nudge);
         *ct = -(tmp - b[0]) + 1;
       }
       if (*ct >= -1 && *ct <= 1) {
@@ -314,7 +331,7 @@ static void set_msq(ev_t *e, int code, double *factor, double *volume) {
     double m_min = o->mass_sum[i];
     m_max = sqrts - e->m_tot + m_min;
     msq_from_x(o->map_id[i], e->x[e->id_x], sqrts * sqrts, o->m[i], o->w[i], m_min * m_min,
-               m_max * m_max, e->a + 3 * code, &e->p2[code], factor);
+               m_max * m_max, e->a + 3 * code, &e->p2[code], factor, o->nudge);
     e->id_x++;
     *factor *= f1 * f2;
     *volume = v1 * v2 * sqrts * sqrts / (4 * OR_TWOPI2);
@@ -357,7 +374,7 @@ static void set_angles(ev_t *e, int code, double *factor, double L0[4][4]) {
   double xx = e->x[e->id_x];
   e->id_x++;
   double ct, st, f;
-  ct_from_x(o->map_id[i], xx, e->b + 3 * code, &ct, &st, &f);
+  ct_from_x(o->map_id[i], xx, e->b + 3 * code, &ct, &st, &f, o->nudge);
   *factor *= f;
   double L1[4][4] = {
       {gamma, -bg * st, 0, bg * ct},
@@ -471,8 +488,14 @@ oracle_t *oracle_create(int n_in, int n_out, int n_channels, const int *d1, cons
 void oracle_set_sqrts(oracle_t *o, double sqrts) {
   o->sqrts = sqrts;
   for (int c = 0; c < o->n_channels; c++)
-    constants_for(o, c, sqrts, o->a + (size_t)c * o->stride * 3, o->b + (size_t)c * o->stride * 3);
+    constants_for(o, c, sqrts, o->a + (size_t)c * o->stride * 3, o->b + (size_t)c * o->stride * 3, 0);
 }
+
+/* A test's sensitivity probe, never the reference's arithmetic: with per-event beams, every
+ * value a transcendental function returns on the mapping path -- the per-event constants
+ * (constants_for) and the maps' own tan, exp and log -- moved by `ulps` ulps from here on;
+ * 0 restores the reference's arithmetic.  The uniform-beam constants are never moved. */
+void oracle_set_nudge(oracle_t *o, int ulps) { o->nudge = ulps; }
 
 /* Constants for channel c at sqrts, [3*(2^n_out)] each, for inspection by tests. */
 void oracle_get_constants(const oracle_t *o, int c, double *a, double *b) {
@@ -512,7 +535,7 @@ static void *run_job(void *arg) {
     if (j->E1) {
       double E1 = j->E1[ev], E2 = j->E2[ev];
       e.sqrts = 2 * sqrt(E1 * E2);
-      constants_for(o, c, e.sqrts, a_ev, b_ev);
+      constants_for(o, c, e.sqrts, a_ev, b_ev, o->nudge);
       e.a = a_ev; e.b = b_ev;
       if (E1 != E2) { /* phs.cu:1286-1301 */
         lab = 1;
@@ -873,7 +896,7 @@ static void *run_inv_job(void *arg) {
       e.o = o; e.c = c; e.sqrts = sqrts; e.x = xr; e.id_x = 0;
       e.msq = msq; e.pd = pd; e.p = pp; e.factor = 1;
       if (j->E1) {
-        constants_for(o, c, sqrts, a_ev, b_ev);
+        constants_for(o, c, sqrts, a_ev, b_ev, o->nudge);
         e.a = a_ev; e.b = b_ev;
       } else {
         e.a = o->a + (size_t)c * o->stride * 3;

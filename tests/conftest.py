@@ -51,5 +51,71 @@ def momentum_rel_err(p, q, sqrts=None):
     return (np.abs(p - q).max(axis=-1) / e)
 
 
+def wide_beams(n, sqrts, seed):
+    """Beam energies log-uniform in [1e-4, 0.7] sqrt(s) each: collision energies from far
+    below the resonances' masses (negative Breit-Wigner ranges) up to where the range in
+    widths passes 1024 (the three-term atan series), lab boosts up to gamma ~ 40, tiny s."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.log(1e-4), np.log(0.7)
+    return (sqrts * np.exp(rng.uniform(lo, hi, n)), sqrts * np.exp(rng.uniform(lo, hi, n)))
+
+
+def oracle_sensitivity(o, x, r, sq, E1=None, E2=None, trials=2, seed=2, nudge=2):
+    """The oracle's own change under perturbations of the size a device's rounding makes:
+    one-ulp perturbations of its x inputs (each entry times 1 +- 2^-52, `trials` draws)
+    and, with per-event beams, every value a transcendental function returns on the
+    mapping path moved by +-`nudge` ulps (Oracle.generate(nudge=...): the per-event
+    constants such as the Breit-Wigner bound a1 = atan(u), and the maps' own tan, exp and
+    log, which a device evaluates with its own library within a few ulps of glibc's).  The
+    reference's Breit-Wigner map is ill-conditioned in both far below its pole: one ulp of
+    a1 moves z and tan(z) by (1 + u^2) ulps, and msq = m (m + w tan z) cancels.  Per event
+    the largest momentum change (the measure of momentum_rel_err against the event's
+    sqrt(s) `sq`) and relative factor change; infinite where the ok flag moved.  Near a
+    kinematic threshold the Kallen function amplifies all of these."""
+    rng = np.random.default_rng(seed)
+    n = x.shape[0]
+    sp = np.zeros(n)
+    sf = np.zeros(n)
+    flips = np.zeros(n, bool)
+    runs = [dict(x=x * (1 + rng.choice([-1.0, 1.0], x.shape) * 2.0 ** -52))
+            for _ in range(trials)]
+    if E1 is not None and nudge:
+        runs += [dict(x=x, nudge=nudge), dict(x=x, nudge=-nudge)]
+    for kw in runs:
+        q = o.generate(kw.pop("x"), E1=E1, E2=E2, **kw)
+        flips |= q.ok != r.ok
+        both = (q.ok == 1) & (r.ok == 1)
+        sp[both] = np.maximum(sp[both], momentum_rel_err(q.p[both], r.p[both],
+                                                         sq[both][:, None]).max(axis=1))
+        sf[both] = np.maximum(sf[both], np.abs(q.factor[both] - r.factor[both]) /
+                              np.abs(r.factor[both]))
+    sp[flips] = np.inf
+    sf[flips] = np.inf
+    return sp, sf
+
+
+def assert_within_conditioning(p, f, ok, o, x, r, sq, E1, E2, bar, ulps):
+    """ok flags bit-exact with the oracle; per event, momenta (against the event's own
+    sqrt(s)) and factors within max(bar, ulps x the oracle's own change under perturbations
+    of the device's rounding size, oracle_sensitivity); zero momenta and factor where
+    ok = 0."""
+    assert int(np.count_nonzero(ok != r.ok)) == 0
+    sel = r.ok == 1
+    n = ok.shape[0]
+    assert 0 < sel.sum() < n
+    sp, sf = oracle_sensitivity(o, x, r, sq, E1, E2)
+    ep = momentum_rel_err(p[sel], r.p[sel], sq[sel][:, None]).max(axis=1)
+    ef = np.abs(f[sel] - r.factor[sel]) / np.abs(r.factor[sel])
+    tp = np.maximum(bar, ulps * sp[sel])
+    tf = np.maximum(bar, ulps * sf[sel])
+    wide = (ep > bar) | (ef > bar)
+    print(f"max momentum error {ep.max():.3g}, factor {ef.max():.3g}; {int(wide.sum())} of "
+          f"{int(sel.sum())} ok events above {bar:g}; worst error / bound: momentum "
+          f"{np.max(ep / tp):.3g}, factor {np.max(ef / tf):.3g}")
+    assert np.all(ep <= tp), f"momentum: {np.max(ep / tp):.3g} x the bound"
+    assert np.all(ef <= tf), f"factor: {np.max(ef / tf):.3g} x the bound"
+    assert np.all(p[~sel] == 0) and np.all(f[~sel] == 0)
+
+
 def counts_of(channels, n_channels):
     return np.bincount(channels, minlength=n_channels).astype(np.int64)

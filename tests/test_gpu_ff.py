@@ -6,7 +6,8 @@ recomputed in FP64 -- and that exact fallback itself."""
 import numpy as np
 import pytest
 
-from conftest import REFCPU_FIXTURES, counts_of, golden, load_process, momentum_rel_err
+from conftest import (REFCPU_FIXTURES, assert_within_conditioning, counts_of, golden, load_process,
+                      momentum_rel_err, wide_beams)
 from gpu_phs_gb300 import processes as P
 from gpu_phs_gb300.philox import uniform_x
 from oracle import oracle
@@ -182,8 +183,9 @@ def test_ff_matches_f64_kernel_tt_full_size(torch):
 @pytest.mark.parametrize("beams", ["asymmetric", "random"])
 @pytest.mark.parametrize("builder", [P.tt, P.precision])
 def test_ff_per_event_beams(torch, builder, beams):
-    """Per-event beam energies in FP32-pair arithmetic: the constants that depend on sqrt(s)
-    per event in FP64, the walk in float-float; against the oracle at the same bar."""
+    """Per-event beam energies in FP32-pair arithmetic: the beams and the uniform and
+    Breit-Wigner constants in float-float (the others, sqrt(s) and the volume in FP64), the
+    walk in float-float; against the oracle at the same bar."""
     from gpu_phs_gb300.api import PhaseSpace
     proc = builder()
     n = 50_000
@@ -202,6 +204,34 @@ def test_ff_per_event_beams(torch, builder, beams):
     torch.cuda.synchronize()
     got = (ev.p.cpu().numpy(), ev.factor.cpu().numpy(), ev.volume.cpu().numpy(), ev.ok.cpu().numpy())
     check(got, r.p, r.factor, r.volume, r.ok, sq)
+
+
+@pytest.mark.parametrize("builder", [P.ww, P.tt, P.precision])
+def test_ff_per_event_beams_wide_energy_range(torch, builder):
+    """FP32 pairs with beam energies log-uniform in [1e-4, 0.7] sqrt(s) each (wide_beams:
+    negative Breit-Wigner ranges, the float-float series and its FP64 fallback, tiny s).
+    Bar: ok flags bit-exact with the oracle; momenta (against the event's own sqrt(s)) and
+    factors within 1e-7, or 1024 times the oracle's own change under perturbations of the
+    FP64 rounding size (oracle_sensitivity; float-float carries about 2^-48, 16 FP64 ulps,
+    times the FP64 test's 64) on the events near a threshold that the walk decides in
+    float-float (margins above 1e-5)."""
+    from gpu_phs_gb300.api import PhaseSpace
+    proc = builder()
+    n = 50_000
+    x = uniform_x(15, n, proc.n_x)
+    E1, E2 = wide_beams(n, proc.sqrts, 5)
+    sq = 2.0 * np.sqrt(E1 * E2)
+    o = oracle.Oracle(proc, proc.sqrts)
+    r = o.generate(x, E1=E1, E2=E2)
+    ps = PhaseSpace(proc)
+    ps.set_precision(1)
+    ev = ps.generate_beams(torch.from_numpy(x).cuda(), torch.from_numpy(E1).cuda(),
+                           torch.from_numpy(E2).cuda())
+    torch.cuda.synchronize()
+    p, f, v, ok = (ev.p.cpu().numpy(), ev.factor.cpu().numpy(), ev.volume.cpu().numpy(),
+                   ev.ok.cpu().numpy())
+    assert_within_conditioning(p, f, ok, o, x, r, sq, E1, E2, TOL, 1024)
+    assert np.allclose(v, r.volume, rtol=1e-15, atol=0)
 
 
 def test_ff_per_event_beams_exact_path(torch):

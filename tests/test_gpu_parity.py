@@ -13,7 +13,8 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from conftest import REFCPU_FIXTURES, counts_of, golden, load_process, momentum_rel_err
+from conftest import (REFCPU_FIXTURES, assert_within_conditioning, counts_of, golden, load_process,
+                      momentum_rel_err, wide_beams)
 from gpu_phs_gb300 import processes as P
 from gpu_phs_gb300.philox import uniform_x
 from oracle import oracle
@@ -220,9 +221,11 @@ def test_host_path_matches_device(torch):
     assert torch.equal(h.factor, d.factor.cpu()) and torch.equal(h.volume, d.volume.cpu())
 
 
-def test_host_path_matches_device_many_channels(torch):
+@pytest.mark.parametrize("precision", [0, 1])
+def test_host_path_matches_device_many_channels(torch, precision):
     """40 channels with uneven counts through the pipelined host call (the volumes are
-    written on the host per channel, the rest copied back per chunk): the device path's bits."""
+    written on the host per channel, the rest copied back per chunk): the device path's bits,
+    in FP64 and in FP32 pairs."""
     from gpu_phs_gb300.api import PhaseSpace
     rng = np.random.default_rng(21)
     proc = P.random_process(rng, 6, 40, 1000.0)
@@ -231,6 +234,7 @@ def test_host_path_matches_device_many_channels(torch):
     n = int(counts.sum())
     x = uniform_x(23, n, proc.n_x)
     ps = PhaseSpace(proc, 500.0, 500.0)
+    ps.set_precision(precision)
     xh = torch.from_numpy(x).pin_memory()
     h = ps.generate_host(xh, counts)
     d = ps.generate(xh.cuda(), counts)
@@ -268,6 +272,35 @@ def test_per_event_beams(torch, beams):
         tot = p[sel].sum(axis=1)
         assert np.allclose(tot[:, 0], (E1 + E2)[sel], rtol=1e-12)
         assert np.allclose(tot[:, 3], (E1 - E2)[sel], atol=1e-8)
+
+
+@pytest.mark.parametrize("builder", [P.ww, P.tt, P.precision])
+def test_per_event_beams_wide_energy_range(torch, builder):
+    """Per-event beams over four decades of energy (wide_beams).  The device evaluates the
+    constants that depend on sqrt(s), and the maps' tan/exp/log, within a few ulps of the
+    oracle's (CUDA's library against glibc's, the Breit-Wigner bound's series, products
+    with 1/s).  Far below a resonance the reference's Breit-Wigner map is ill-conditioned
+    in exactly these values (one ulp of a1 moves tan(z) by (1 + u^2) ulps, and
+    msq = m (m + w tan z) cancels), and many events sit near a threshold, where the Kallen
+    function amplifies that into momenta: the oracle itself moves by up to 1e-7 when they
+    move by two ulps.  Bar: ok flags bit-exact; momenta and factors within 1e-11, or 64
+    times the oracle's own change under such perturbations (assert_within_conditioning,
+    oracle_sensitivity); volumes within 1e-15."""
+    from gpu_phs_gb300.api import PhaseSpace
+    proc = builder()
+    n = 50_000
+    x = uniform_x(14, n, proc.n_x)
+    E1, E2 = wide_beams(n, proc.sqrts, 4)
+    sq = 2.0 * np.sqrt(E1 * E2)
+    o = oracle.Oracle(proc, proc.sqrts)
+    r = o.generate(x, E1=E1, E2=E2)
+    ps = PhaseSpace(proc)
+    ev = ps.generate_beams(torch.from_numpy(x).cuda(), torch.from_numpy(E1).cuda(),
+                           torch.from_numpy(E2).cuda())
+    p, f, v, ok = (ev.p.cpu().numpy(), ev.factor.cpu().numpy(), ev.volume.cpu().numpy(),
+                   ev.ok.cpu().numpy())
+    assert_within_conditioning(p, f, ok, o, x, r, sq, E1, E2, 1e-11, 64)
+    assert (np.abs(v - r.volume) / r.volume).max() < 1e-15
 
 
 def test_batch_matches_single_process_runs(torch):

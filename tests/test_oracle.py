@@ -173,3 +173,29 @@ def test_oracle_condition_output_leaves_results_unchanged():
     k = b.kappa[b.ok == 1]
     assert (k >= 1.0).all() and np.isfinite(k).all()
     assert (b.kappa[b.ok == 0] >= 0).all()
+
+
+def test_oracle_nudge_moves_only_the_per_event_constants():
+    """generate(nudge=k) (a sensitivity probe) moves the per-event transcendental constants
+    by k ulps: nudge=0 is the reference's arithmetic bit for bit, a nudge changes some
+    momenta by a little and is reset after the call, and uniform beams refuse it."""
+    proc = P.ww()
+    n = 20_000
+    x = uniform_x(78, n, proc.n_x)
+    rng = np.random.default_rng(9)
+    E1, E2 = rng.uniform(100, 350, n), rng.uniform(100, 350, n)
+    o = oracle.Oracle(proc, proc.sqrts)
+    a = o.generate(x, E1=E1, E2=E2)
+    b = o.generate(x, E1=E1, E2=E2, nudge=0)
+    for f in ("p", "factor", "volume", "ok"):
+        assert np.array_equal(getattr(a, f), getattr(b, f))
+    c = o.generate(x, E1=E1, E2=E2, nudge=2)
+    sel = (a.ok == 1) & (c.ok == 1)
+    sq = 2.0 * np.sqrt(E1 * E2)
+    d = momentum_rel_err(c.p[sel], a.p[sel], sq[sel][:, None]).max(axis=1)
+    assert d.max() > 0 and np.median(d) < 1e-13
+    assert np.array_equal(a.volume, c.volume)
+    again = o.generate(x, E1=E1, E2=E2)
+    assert np.array_equal(again.p, a.p)
+    with pytest.raises(ValueError):
+        o.generate(x, nudge=1)
