@@ -112,11 +112,12 @@ static double ulps_moved(double x, int k) {
 /* phs_cpu.cpp:452-531, for one channel and one sqrts, into a/b.  nudge != 0 (a test's
  * sensitivity probe, never the reference's arithmetic) moves every constant that a
  * transcendental function returns -- the Breit-Wigner bound a1 = atan(.), the logarithms
- * of the exponential maps and of the cos(theta) map, the step maps' exp/log/sqrt
+ * of the exponential maps and of the cos(theta) map, each exp and log of the STEP_E
  * constants -- by nudge ulps where it is formed, so that the constants computed from it
- * (a2 = (a1 - a0) m w / s) follow: a device evaluating them per event with its own
- * library (or its own series) is within a few ulps of these, and far in a Breit-Wigner
- * tail one ulp of a1 moves the mapped mass by m w (1 + u^2) ulp(a1). */
+ * (a2 = (a1 - a0) m w / s, STEP_E's a0 = 1 - a2 log(...)) follow (STEP_H's constants are
+ * correctly rounded operations, the same bits everywhere): a device evaluating them per
+ * event with its own library (or its own series) is within a few ulps of these, and far
+ * in a Breit-Wigner tail one ulp of a1 moves the mapped mass by m w (1 + u^2) ulp(a1). */
 static void constants_for(const oracle_t *o, int c, double sqrts, double *a_out, double *b_out,
                           int nudge) {
   double m_tot = o->mass_sum[c * o->stride + o->n_codes];
@@ -162,14 +163,15 @@ static void constants_for(const oracle_t *o, int c, double sqrts, double *a_out,
         double r = 2 * m * w / (msq_max - msq_min);
         a[2] = r > 0.01 ? r : 0.01;
         a[1] = ulps_moved(exp(-(m * m - msq_min) / (msq_max - msq_min) / a[2]), nudge);
-        a[0] = ulps_moved(1 - a[2] * log((1 + a[1] * exp(1 / a[2])) / (1 + a[1])), nudge);
+        a[0] = 1 - a[2] * ulps_moved(log((1 + a[1] * ulps_moved(exp(1 / a[2]), nudge)) / (1 + a[1])),
+                                     nudge);
         break;
       }
       case OR_MAP_STEP_H: {
         a[2] = (m * m - msq_min) / (msq_max - msq_min);
         double r = pow(2 * m * w / (msq_max - msq_min), 2) / a[2];
         a[1] = r > 0.000001 ? r : 0.000001;
-        a[0] = ulps_moved((1 + sqrt(1 + 4 * a[1] / (1 - a[2]))) / 2, nudge);
+        a[0] = (1 + sqrt(1 + 4 * a[1] / (1 - a[2]))) / 2;
         break;
       }
     }

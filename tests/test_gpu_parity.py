@@ -303,6 +303,62 @@ def test_per_event_beams_wide_energy_range(torch, builder):
     assert (np.abs(v - r.volume) / r.volume).max() < 1e-15
 
 
+def all_maps_process(seed, n_out, n_channels):
+    """random_process trees with some of their mappings swapped for the kinds it does not
+    draw: Breit-Wigner -> STEP_E or STEP_H, collinear -> RADIATION, t- -> u-channel, so
+    that every mapping's per-event constants run (n_out >= 4 draws all nine kinds)."""
+    rng = np.random.default_rng(seed)
+    proc = P.random_process(rng, n_out, n_channels, 1000.0)
+    ids = proc.map_ids.copy()
+    for c in range(ids.shape[0]):
+        for j in range(ids.shape[1]):
+            t = ids[c, j]
+            if t == P.MAP_SCHANNEL and rng.random() < 0.5:
+                ids[c, j] = P.MAP_STEP_E if rng.random() < 0.5 else P.MAP_STEP_H
+            elif t == P.MAP_COLLINEAR and rng.random() < 0.5:
+                ids[c, j] = P.MAP_RADIATION
+            elif t == P.MAP_TCHANNEL and rng.random() < 0.5:
+                ids[c, j] = P.MAP_UCHANNEL
+    proc.map_ids = ids
+    return proc
+
+
+@pytest.mark.parametrize("beams", ["mid", "wide"])
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("n_out", [3, 4, 5, 6, 7, 8])
+def test_per_event_beams_every_mapping(torch, n_out, precision, beams):
+    """Per-event beams on 8 random channels of n_out particles with every mapping kind
+    (all_maps_process), beam energies uniform in [0.3, 0.7] sqrt(s) ("mid") or over four
+    decades (wide_beams), FP64 and FP32 pairs (whose step-map channels take the exact
+    path per event).  Bar as test_per_event_beams_wide_energy_range: ok flags bit-exact,
+    momenta and factors within 1e-11 (FP32 pairs 1e-7) or 64 (1024) times the oracle's own
+    change under perturbations of the device's rounding size, volumes within 1e-15."""
+    from gpu_phs_gb300.api import PhaseSpace
+    proc = all_maps_process(100 + n_out, n_out, 8)
+    n = 20_000
+    counts = np.full(8, n // 8, np.int64)
+    ch = np.repeat(np.arange(8), counts).astype(np.int32)
+    x = uniform_x(200 + n_out, n, proc.n_x)
+    if beams == "wide":
+        E1, E2 = wide_beams(n, 1000.0, 7)
+    else:
+        rng = np.random.default_rng(n_out)
+        E1, E2 = rng.uniform(300.0, 700.0, n), rng.uniform(300.0, 700.0, n)
+    sq = 2.0 * np.sqrt(E1 * E2)
+    o = oracle.Oracle(proc, 1000.0)
+    r = o.generate(x, ch, E1=E1, E2=E2)
+    ps = PhaseSpace(proc)
+    ps.set_precision(precision)
+    ev = ps.generate_beams(torch.from_numpy(x).cuda(), torch.from_numpy(E1).cuda(),
+                           torch.from_numpy(E2).cuda(), counts)
+    torch.cuda.synchronize()
+    p, f, v, ok = (ev.p.cpu().numpy(), ev.factor.cpu().numpy(), ev.volume.cpu().numpy(),
+                   ev.ok.cpu().numpy())
+    bar, ulps = (1e-11, 64) if precision == 0 else (1e-7, 1024)
+    assert_within_conditioning(p, f, ok, o, x, r, sq, E1, E2, bar, ulps, channels=ch)
+    assert (np.abs(v - r.volume) / r.volume).max() < 1e-15
+
+
 def test_batch_matches_single_process_runs(torch):
     from gpu_phs_gb300.api import Batch, PhaseSpace
     rng = np.random.default_rng(21)
