@@ -171,10 +171,12 @@ class Oracle:
                 ok: Optional[np.ndarray] = None, x_own: Optional[np.ndarray] = None,
                 factor_own: Optional[np.ndarray] = None, n_x: Optional[int] = None,
                 E1: Optional[np.ndarray] = None, E2: Optional[np.ndarray] = None,
-                threads: int = 0):
+                threads: int = 0, nudge: int = 0):
         """All-channel factors [n, n_channels] and x [n_channels, n, n_x] of events with
         lab momenta p [n, n_out, 4] (phs.cu:1499-1554).  With x_own/factor_own the
-        generating channel's row is copied, otherwise inverted like the others."""
+        generating channel's row is copied, otherwise inverted like the others.  nudge != 0
+        (per-event beams): the sensitivity probe of generate(nudge=...), on the inverse
+        maps' atan, exp and log too."""
         p = np.ascontiguousarray(p, np.float64)
         n = p.shape[0]
         n_x = n_x or (x_own.shape[1] if x_own is not None else self.proc.n_x)
@@ -193,10 +195,16 @@ class Oracle:
         fac = np.zeros((n, self.proc.n_channels))
         xo = np.zeros((self.proc.n_channels, n, n_x))
         threads = threads or os.cpu_count() or 1
-        self.lib().oracle_inverse(self.h, n, n_x, p.reshape(-1), vp(channels, np.int32),
-                                  vp(ok, np.uint8), vp(E1, np.float64), vp(E2, np.float64),
-                                  vp(x_own, np.float64), vp(factor_own, np.float64),
-                                  fac.reshape(-1), xo.reshape(-1), threads)
+        if nudge and E1 is None:
+            raise ValueError("nudge moves per-event constants: give E1 and E2")
+        self.lib().oracle_set_nudge(self.h, int(nudge))
+        try:
+            self.lib().oracle_inverse(self.h, n, n_x, p.reshape(-1), vp(channels, np.int32),
+                                      vp(ok, np.uint8), vp(E1, np.float64), vp(E2, np.float64),
+                                      vp(x_own, np.float64), vp(factor_own, np.float64),
+                                      fac.reshape(-1), xo.reshape(-1), threads)
+        finally:
+            self.lib().oracle_set_nudge(self.h, 0)
         return fac, xo
 
 

@@ -495,8 +495,9 @@ void oracle_set_sqrts(oracle_t *o, double sqrts) {
 
 /* A test's sensitivity probe, never the reference's arithmetic: with per-event beams, every
  * value a transcendental function returns on the mapping path -- the per-event constants
- * (constants_for) and the maps' own tan, exp and log -- moved by `ulps` ulps from here on;
- * 0 restores the reference's arithmetic.  The uniform-beam constants are never moved. */
+ * (constants_for) and the forward and inverse maps' own tan, atan, exp and log -- moved by
+ * `ulps` ulps from here on; 0 restores the reference's arithmetic.  The uniform-beam
+ * constants are never moved. */
 void oracle_set_nudge(oracle_t *o, int ulps) { o->nudge = ulps; }
 
 /* Constants for channel c at sqrts, [3*(2^n_out)] each, for inspection by tests. */
@@ -665,7 +666,7 @@ int oracle_set_friends(oracle_t *o, const int *friends) {
 /* mappings_gpu.hpp:15-172 (mapping_x_from_msq_*), with the constants of
  * init_mapping_constants_cpu. */
 static void msq_to_x(int t, double msq, double s, double m, double w, double msq_min,
-                     double msq_max, const double *a, double *x, double *factor) {
+                     double msq_max, const double *a, double *x, double *factor, int nudge) {
   double z, z1, z2, z3;
   switch (t) {
     case OR_MAP_NO:
@@ -674,31 +675,31 @@ static void msq_to_x(int t, double msq, double s, double m, double w, double msq
       break;
     case OR_MAP_SCHANNEL:
       z = (msq - m * m) / (m * w);
-      *x = (atan(z) - a[0]) / (a[1] - a[0]);
+      *x = (ulps_moved(atan(z), nudge) - a[0]) / (a[1] - a[0]);
       *factor = a[2] * (1 + z * z);
       break;
     case OR_MAP_COLLINEAR:
     case OR_MAP_INFRARED:
     case OR_MAP_RADIATION:
       z = msq - msq_min + a[0];
-      *x = log(z / a[0]) / a[1];
+      *x = ulps_moved(log(z / a[0]), nudge) / a[1];
       *factor = a[2] * z;
       break;
     case OR_MAP_TCHANNEL:
     case OR_MAP_UCHANNEL:
       if (msq < (msq_max + msq_min) / 2) {
         z = msq - msq_min + a[0];
-        *x = log(z / a[0]) / a[1];
+        *x = ulps_moved(log(z / a[0]), nudge) / a[1];
       } else {
         z = msq_max - msq + a[0];
-        *x = 1 - log(z / a[0]) / a[1];
+        *x = 1 - ulps_moved(log(z / a[0]), nudge) / a[1];
       }
       *factor = a[2] * z;
       break;
     case OR_MAP_STEP_E:
       z1 = (msq - msq_min) / (msq_max - msq_min);
-      z2 = 1 + a[1] * exp(z1 / a[2]);
-      *x = (z1 - a[2] * log(z2 / (1 + a[1]))) / a[0];
+      z2 = 1 + a[1] * ulps_moved(exp(z1 / a[2]), nudge);
+      *x = (z1 - a[2] * ulps_moved(log(z2 / (1 + a[1])), nudge)) / a[0];
       *factor = a[0] * z2 * (msq_max - msq_min) / s;
       break;
     case OR_MAP_STEP_H:
@@ -714,7 +715,7 @@ static void msq_to_x(int t, double msq, double s, double m, double w, double msq
 }
 
 /* mappings_gpu.hpp:184-219 (mapping_x_from_ct_*) */
-static void ct_to_x(int t, double ct, const double *b, double *x, double *factor) {
+static void ct_to_x(int t, double ct, const double *b, double *x, double *factor, int nudge) {
   double ct1;
   switch (t) {
     case OR_MAP_COLLINEAR:
@@ -722,10 +723,10 @@ static void ct_to_x(int t, double ct, const double *b, double *x, double *factor
     case OR_MAP_UCHANNEL:
       if (ct < 0) {
         ct1 = ct + b[0] + 1;
-        *x = log(ct1 / b[0]) / (2 * b[1]);
+        *x = ulps_moved(log(ct1 / b[0]), nudge) / (2 * b[1]);
       } else {
         ct1 = -ct + b[0] + 1;
-        *x = 1 - log(ct1 / b[0]) / (2 * b[1]);
+        *x = 1 - ulps_moved(log(ct1 / b[0]), nudge) / (2 * b[1]);
       }
       *factor = ct1 * b[1];
       break;
@@ -784,7 +785,7 @@ static double inv_msq(inv_t *e, int code) {
     double m_tot = o->mass_sum[e->c * o->stride + o->n_codes];
     double m_min = o->mass_sum[i], m_max = e->sqrts - m_tot + m_min;
     msq_to_x(o->map_id[i], e->msq[code], e->sqrts * e->sqrts, o->m[i], o->w[i], m_min * m_min,
-             m_max * m_max, e->a + 3 * code, &e->x[e->id_x], &f);
+             m_max * m_max, e->a + 3 * code, &e->x[e->id_x], &f, o->nudge);
     e->id_x++;
     f *= f1 * f2;
   }
@@ -810,7 +811,7 @@ static void inv_angles(inv_t *e, int code, double G[4][4]) {
   e->x[e->id_x++] = phi / OR_TWOPI;
   double dn = sqrt(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
   double ct = q[3] / dn, st = sqrt(1 - ct * ct), f;
-  ct_to_x(o->map_id[i], ct, e->b + 3 * code, &e->x[e->id_x++], &f);
+  ct_to_x(o->map_id[i], ct, e->b + 3 * code, &e->x[e->id_x++], &f, o->nudge);
   e->factor *= f;
   double cp = cos(phi), sp = sin(phi);
   int kids[2] = {k1, k2};

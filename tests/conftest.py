@@ -122,5 +122,26 @@ def assert_within_conditioning(p, f, ok, o, x, r, sq, E1, E2, bar, ulps, channel
     assert np.all(p[~sel] == 0) and np.all(f[~sel] == 0)
 
 
+def all_maps_process(seed, n_out, n_channels):
+    """random_process trees with some of their mappings swapped for the kinds it does not
+    draw: Breit-Wigner -> STEP_E or STEP_H, collinear -> RADIATION, t- -> u-channel, so
+    that every mapping's per-event constants run (n_out >= 4 draws all nine kinds)."""
+    rng = np.random.default_rng(seed)
+    from gpu_phs_gb300 import processes as P
+    proc = P.random_process(rng, n_out, n_channels, 1000.0)
+    ids = proc.map_ids.copy()
+    for c in range(ids.shape[0]):
+        for j in range(ids.shape[1]):
+            t = ids[c, j]
+            if t == P.MAP_SCHANNEL and rng.random() < 0.5:
+                ids[c, j] = P.MAP_STEP_E if rng.random() < 0.5 else P.MAP_STEP_H
+            elif t == P.MAP_COLLINEAR and rng.random() < 0.5:
+                ids[c, j] = P.MAP_RADIATION
+            elif t == P.MAP_TCHANNEL and rng.random() < 0.5:
+                ids[c, j] = P.MAP_UCHANNEL
+    proc.map_ids = ids
+    return proc
+
+
 def counts_of(channels, n_channels):
     return np.bincount(channels, minlength=n_channels).astype(np.int64)

@@ -13,8 +13,8 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from conftest import (REFCPU_FIXTURES, assert_within_conditioning, counts_of, golden, load_process,
-                      momentum_rel_err, wide_beams)
+from conftest import (REFCPU_FIXTURES, all_maps_process, assert_within_conditioning, counts_of,
+                      golden, load_process, momentum_rel_err, wide_beams)
 from gpu_phs_gb300 import processes as P
 from gpu_phs_gb300.philox import uniform_x
 from oracle import oracle
@@ -301,26 +301,6 @@ def test_per_event_beams_wide_energy_range(torch, builder):
                    ev.ok.cpu().numpy())
     assert_within_conditioning(p, f, ok, o, x, r, sq, E1, E2, 1e-11, 64)
     assert (np.abs(v - r.volume) / r.volume).max() < 1e-15
-
-
-def all_maps_process(seed, n_out, n_channels):
-    """random_process trees with some of their mappings swapped for the kinds it does not
-    draw: Breit-Wigner -> STEP_E or STEP_H, collinear -> RADIATION, t- -> u-channel, so
-    that every mapping's per-event constants run (n_out >= 4 draws all nine kinds)."""
-    rng = np.random.default_rng(seed)
-    proc = P.random_process(rng, n_out, n_channels, 1000.0)
-    ids = proc.map_ids.copy()
-    for c in range(ids.shape[0]):
-        for j in range(ids.shape[1]):
-            t = ids[c, j]
-            if t == P.MAP_SCHANNEL and rng.random() < 0.5:
-                ids[c, j] = P.MAP_STEP_E if rng.random() < 0.5 else P.MAP_STEP_H
-            elif t == P.MAP_COLLINEAR and rng.random() < 0.5:
-                ids[c, j] = P.MAP_RADIATION
-            elif t == P.MAP_TCHANNEL and rng.random() < 0.5:
-                ids[c, j] = P.MAP_UCHANNEL
-    proc.map_ids = ids
-    return proc
 
 
 @pytest.mark.parametrize("beams", ["mid", "wide"])
