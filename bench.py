@@ -225,7 +225,23 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64, pin=
         "fp64_events_per_s": n / pe[0][0] * 1e3, "fp32_mixed_events_per_s": n / pe[1][0] * 1e3,
         "speedup": pe[0][0] / pe[1][0],
         "error_vs_fp64": _errors(torch, pe[0][1], pe[1][1], proc.sqrts)}
-    del pe, E1, E2
+    # the CPU path beside it on all n events with the same beams, checked event by event.
+    # The reference's phs_cpu.cpp takes one sqrt(s) per call, so its C restatement (which
+    # forms the constants per event as the reference's GPU path does) runs here.
+    from oracle import oracle as _oracle
+    threads = os.cpu_count() or 1
+    beams = (E1.cpu().numpy(), E2.cpu().numpy())
+    rate, passes, ref = cpu_time(_PerEventBeams(_oracle.Oracle(proc, proc.sqrts), *beams),
+                                 x_tt.cpu().numpy(), 2.0, threads)
+    rows = torch.full((n,), proc.n_out, dtype=torch.int64, device="cuda")
+    res["per_event_beams_tt"]["cpu_baseline"] = {
+        "value": rate, "unit": "events/s", "cores": threads, "kind": "port",
+        "sample": f"all {n} events (the GPU's x and beams), {passes} passes, all host threads"}
+    for prec, k in ((0, "fp64"), (1, "fp32_mixed")):
+        o = pe[prec][1]
+        res["per_event_beams_tt"][f"{k}_parity_vs_cpu"] = parity_vs_cpu(
+            torch, ref, o.p.view(-1), o.factor, o.volume, o.ok, rows, proc.sqrts)
+    del pe, E1, E2, ref, rows
 
     # Four forms per workload, three of them FP64 with identical output bits: the plain FP64
     # kernel (one pass: every event walked in full), FP64 compacting (an FP64 pass tests
@@ -475,7 +491,46 @@ def measure_variants(torch, steps: int, warmup: int, x_tt, out_tt, ms_tt64, pin=
         "algorithmic_bytes_per_step": wbytes + rbytes,
         "ok_fraction": ev.ok.double().mean().item(),
         "launch": "one persistent kernel: 64 events per block at a time, every channel per event"}
-    del fac, xo, ev, x, ps
+    # the CPU path beside it: the reference has no CPU inverse (its inverse is GPU code,
+    # phs.cu:1499-1554), so the oracle's restatement of that algorithm runs, on the first
+    # ns events (each channel's first ns / n_channels), checked element by element
+    from oracle import oracle as _oracle
+    threads = os.cpu_count() or 1
+    ns = 1 << 17
+    first = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    sel = np.concatenate([np.arange(first[c], first[c] + ns // proc.n_channels)
+                          for c in range(proc.n_channels)])
+    ch = np.repeat(np.arange(proc.n_channels, dtype=np.int32), ns // proc.n_channels)
+    idx = torch.from_numpy(sel).cuda()
+    ph, okh = ev.p[idx].cpu().numpy(), ev.ok[idx].cpu().numpy()
+    xh, fh = x[idx].cpu().numpy(), ev.factor[idx].cpu().numpy()
+    o_inv = _oracle.Oracle(proc, 1000.0)
+    t0, passes = time.perf_counter(), 0
+    while True:
+        rf, rx = o_inv.inverse(ph, ch, okh, x_own=xh, factor_own=fh, threads=threads)
+        passes += 1
+        if time.perf_counter() - t0 >= 2.0:
+            break
+    el = time.perf_counter() - t0
+    gf, gx = fac[idx].cpu().numpy(), xo[:, idx].cpu().numpy()
+    fin = np.isfinite(rf) & np.isfinite(gf) & (rf != 0)
+    finx = np.isfinite(rx) & np.isfinite(gx)
+    df = np.abs(gf[fin] - rf[fin]) / np.abs(rf[fin])
+    res["inverse_bwbw_61ch"]["cpu_baseline"] = {
+        "value": passes * sel.size * proc.n_channels / el, "unit": "channel inversions/s",
+        "cores": threads, "kind": "port",
+        "sample": f"{sel.size} events ({sel.size // proc.n_channels} of each channel) x "
+                  f"{proc.n_channels} channels, {passes} passes, all host threads"}
+    res["inverse_bwbw_61ch"]["parity_vs_cpu"] = {
+        "events": int(sel.size),
+        "non_finite_entries_differ": int((np.isfinite(gf) != np.isfinite(rf)).sum() +
+                                         (np.isfinite(gx) != np.isfinite(rx)).sum()),
+        "factor_max_rel_vs_cpu": float(df.max()),
+        "factor_median_rel_vs_cpu": float(np.median(df)),
+        "x_max_abs_vs_cpu": float(np.abs(gx[finx] - rx[finx]).max()),
+        "definition": "every (event, channel) factor and x against the CPU inverse of the "
+                      "GPU's momenta; relative factor error over finite non-zero entries"}
+    del fac, xo, ev, x, ps, idx, gf, gx, rf, rx, df
     res["whizard_abi_bwbw_61ch"] = whizard_abi_rate(proc, 1 << 17, max(2, min(steps, 5)))
     return res
 
@@ -560,6 +615,16 @@ def cpu_generator(proc, sqrts):
         except OSError:
             pass
     return oracle.Oracle(proc, sqrts), "port"
+
+
+class _PerEventBeams:
+    """An oracle generator with fixed per-event beam energies, for cpu_time."""
+
+    def __init__(self, gen, E1, E2):
+        self.gen, self.E1, self.E2 = gen, E1, E2
+
+    def generate(self, x, threads: int = 0):
+        return self.gen.generate(x, threads=threads, E1=self.E1, E2=self.E2)
 
 
 def cpu_time(gen, x, min_seconds: float, threads: int):
