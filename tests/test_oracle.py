@@ -199,3 +199,32 @@ def test_oracle_nudge_moves_only_the_per_event_constants():
     assert np.array_equal(again.p, a.p)
     with pytest.raises(ValueError):
         o.generate(x, nudge=1)
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference CPU path not built here")
+@pytest.mark.parametrize("case", ["ww", "tt", "precision", "all_maps_4", "all_maps_6"])
+def test_oracle_per_event_constants_bitexact_vs_live_reference(case):
+    """The oracle's per-event path (constants formed for each event's sqrt(s), as with
+    per-event beams) against the reference's phs_cpu.cpp set up at that sqrt(s), over three
+    decades of energy: bit for bit.  E1 = E2 = sqrt(s)/2 gives each event exactly that
+    sqrt(s) (sqrt of a correctly rounded square is the number itself)."""
+    from conftest import all_maps_process
+    if case.startswith("all_maps"):
+        proc = all_maps_process(500 + int(case[-1]), int(case[-1]), 4)
+    else:
+        proc = getattr(P, case)()
+    n = 4000
+    ch = np.repeat(np.arange(proc.n_channels, dtype=np.int32), n // proc.n_channels)
+    x = uniform_x(88, ch.size, proc.n_x)
+    o = oracle.Oracle(proc, proc.sqrts)
+    for f in (1e-3, 1e-2, 0.05, 0.2, 0.6, 1.0, 1.4):
+        sq = proc.sqrts * f
+        E = np.full(ch.size, sq / 2)
+        assert np.all(2.0 * np.sqrt(E * E) == sq)
+        r = o.generate(x, ch, E1=E, E2=E)
+        q = oracle.RefCPU(proc, sq).generate(x, ch)
+        assert np.array_equal(r.ok, q.ok), f"sqrt(s) = {sq}"
+        ok = r.ok == 1
+        assert np.array_equal(r.p[ok], q.p[ok]), f"sqrt(s) = {sq}"
+        assert np.array_equal(r.factor[ok], q.factor[ok]), f"sqrt(s) = {sq}"
+        assert np.array_equal(r.volume[ok], q.volume[ok]), f"sqrt(s) = {sq}"
