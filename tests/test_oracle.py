@@ -175,10 +175,11 @@ def test_oracle_condition_output_leaves_results_unchanged():
     assert (b.kappa[b.ok == 0] >= 0).all()
 
 
-def test_oracle_nudge_moves_only_the_per_event_constants():
-    """generate(nudge=k) (a sensitivity probe) moves the per-event transcendental constants
-    by k ulps: nudge=0 is the reference's arithmetic bit for bit, a nudge changes some
-    momenta by a little and is reset after the call, and uniform beams refuse it."""
+def test_oracle_nudge_is_a_probe_that_resets():
+    """generate(nudge=k) (a sensitivity probe) moves the transcendental values on the
+    per-event mapping path by k ulps: nudge=0 is the reference's arithmetic bit for bit, a
+    nudge changes some momenta by a little and is reset after the call, and uniform beams
+    refuse it."""
     proc = P.ww()
     n = 20_000
     x = uniform_x(78, n, proc.n_x)
