@@ -74,6 +74,28 @@ def test_oracle_bitexact_vs_reference_fixture(name):
 
 
 @pytest.mark.skipif(not oracle.ref_available(), reason="reference CPU path not built here")
+@pytest.mark.parametrize("case", ["nested_10", "nested_12", "all_maps_5", "all_maps_8"])
+def test_oracle_bitexact_vs_live_reference_largest_and_every_mapping(case):
+    """The API's largest trees (10 and 12 outgoing particles, nested resonances) and random
+    channels with every mapping kind (step, radiation and u-channel maps swapped in),
+    several channels per process: the oracle against the reference build, bit for bit."""
+    from conftest import all_maps_process
+    k = int(case.split("_")[-1])
+    proc = P.nested_resonances(k) if case.startswith("nested") else all_maps_process(k + 2, k, 6)
+    n = 6000
+    ch = np.repeat(np.arange(proc.n_channels, dtype=np.int32), n // proc.n_channels)
+    x = uniform_x(99, ch.size, proc.n_x)
+    r = oracle.Oracle(proc, 1000.0).generate(x, ch)
+    q = oracle.RefCPU(proc, 1000.0).generate(x, ch)
+    assert np.array_equal(r.ok, q.ok)
+    ok = r.ok == 1
+    assert ok.sum() > 200
+    assert np.array_equal(r.p[ok], q.p[ok])
+    assert np.array_equal(r.factor[ok], q.factor[ok])
+    assert np.array_equal(r.volume[ok], q.volume[ok])
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference CPU path not built here")
 @pytest.mark.parametrize("builder", [P.ww, P.tt, P.precision])
 def test_oracle_bitexact_vs_live_reference(builder):
     proc = builder()
