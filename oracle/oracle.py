@@ -133,9 +133,11 @@ class Oracle:
                  E2: Optional[np.ndarray] = None, condition: bool = False,
                  nudge: int = 0) -> Result:
         """condition=True (uniform beams) also returns r.kappa, the per-event condition of
-        the Kallen functions (oracle_generate_cond in phs_oracle.c).  nudge != 0 (per-event
-        beams): every per-event constant that a transcendental function returns moved by
-        that many ulps (oracle_set_nudge), a sensitivity probe for tests."""
+        the Kallen functions (oracle_generate_cond in phs_oracle.c).  nudge != 0: a
+        sensitivity probe for tests (oracle_set_nudge) -- every value a transcendental
+        function returns on the mapping path moved by that many ulps: the maps' tan, exp and
+        log, and with per-event beams the constants formed per event; the uniform-beam
+        constants stay the reference's."""
         x = np.ascontiguousarray(x, np.float64)
         n, n_x = x.shape
         r = Result(n, self.proc.n_out)
@@ -144,27 +146,26 @@ class Oracle:
             channels = np.ascontiguousarray(channels, np.int32)
             chp = channels.ctypes.data_as(C.c_void_p)
         threads = threads or os.cpu_count() or 1
-        if nudge and E1 is None:
-            raise ValueError("nudge moves per-event constants: give E1 and E2")
-        if condition:
-            if E1 is not None:
-                raise ValueError("condition numbers are computed for uniform beams")
-            r.kappa = np.zeros(n)
-            self.lib().oracle_generate_cond(self.h, n, n_x, x.reshape(-1), chp, r.p.reshape(-1),
-                                            r.factor, r.volume, r.ok, r.kappa, threads)
-        elif E1 is None:
-            self.lib().oracle_generate(self.h, n, n_x, x.reshape(-1), chp, r.p.reshape(-1),
-                                       r.factor, r.volume, r.ok, threads)
-        else:
-            E1 = np.ascontiguousarray(np.broadcast_to(E1, (n,)), np.float64)
-            E2 = np.ascontiguousarray(np.broadcast_to(E2, (n,)), np.float64)
-            self.lib().oracle_set_nudge(self.h, int(nudge))
-            try:
+        if condition and E1 is not None:
+            raise ValueError("condition numbers are computed for uniform beams")
+        self.lib().oracle_set_nudge(self.h, int(nudge))
+        try:
+            if condition:
+                r.kappa = np.zeros(n)
+                self.lib().oracle_generate_cond(self.h, n, n_x, x.reshape(-1), chp,
+                                                r.p.reshape(-1), r.factor, r.volume, r.ok,
+                                                r.kappa, threads)
+            elif E1 is None:
+                self.lib().oracle_generate(self.h, n, n_x, x.reshape(-1), chp, r.p.reshape(-1),
+                                           r.factor, r.volume, r.ok, threads)
+            else:
+                E1 = np.ascontiguousarray(np.broadcast_to(E1, (n,)), np.float64)
+                E2 = np.ascontiguousarray(np.broadcast_to(E2, (n,)), np.float64)
                 self.lib().oracle_generate_beams(self.h, n, n_x, x.reshape(-1), chp, E1, E2,
                                                  r.p.reshape(-1), r.factor, r.volume, r.ok,
                                                  threads)
-            finally:
-                self.lib().oracle_set_nudge(self.h, 0)
+        finally:
+            self.lib().oracle_set_nudge(self.h, 0)
         return r
 
     def inverse(self, p: np.ndarray, channels: Optional[np.ndarray] = None,
@@ -174,9 +175,9 @@ class Oracle:
                 threads: int = 0, nudge: int = 0):
         """All-channel factors [n, n_channels] and x [n_channels, n, n_x] of events with
         lab momenta p [n, n_out, 4] (phs.cu:1499-1554).  With x_own/factor_own the
-        generating channel's row is copied, otherwise inverted like the others.  nudge != 0
-        (per-event beams): the sensitivity probe of generate(nudge=...), on the inverse
-        maps' atan, exp and log too."""
+        generating channel's row is copied, otherwise inverted like the others.  nudge != 0:
+        the sensitivity probe of generate(nudge=...), on the inverse maps' atan, exp and
+        log too."""
         p = np.ascontiguousarray(p, np.float64)
         n = p.shape[0]
         n_x = n_x or (x_own.shape[1] if x_own is not None else self.proc.n_x)
@@ -195,8 +196,6 @@ class Oracle:
         fac = np.zeros((n, self.proc.n_channels))
         xo = np.zeros((self.proc.n_channels, n, n_x))
         threads = threads or os.cpu_count() or 1
-        if nudge and E1 is None:
-            raise ValueError("nudge moves per-event constants: give E1 and E2")
         self.lib().oracle_set_nudge(self.h, int(nudge))
         try:
             self.lib().oracle_inverse(self.h, n, n_x, p.reshape(-1), vp(channels, np.int32),

@@ -493,11 +493,12 @@ void oracle_set_sqrts(oracle_t *o, double sqrts) {
     constants_for(o, c, sqrts, o->a + (size_t)c * o->stride * 3, o->b + (size_t)c * o->stride * 3, 0);
 }
 
-/* A test's sensitivity probe, never the reference's arithmetic: with per-event beams, every
- * value a transcendental function returns on the mapping path -- the per-event constants
- * (constants_for) and the forward and inverse maps' own tan, atan, exp and log -- moved by
- * `ulps` ulps from here on; 0 restores the reference's arithmetic.  The uniform-beam
- * constants are never moved. */
+/* A test's sensitivity probe, never the reference's arithmetic: every value a
+ * transcendental function returns on the mapping path -- the forward and inverse maps' own
+ * tan, atan, exp and log and, with per-event beams, the constants formed per event
+ * (constants_for) -- moved by `ulps` ulps from here on; 0 restores the reference's
+ * arithmetic.  The uniform-beam constants (formed once, as the device takes them from the
+ * host) are never moved. */
 void oracle_set_nudge(oracle_t *o, int ulps) { o->nudge = ulps; }
 
 /* Constants for channel c at sqrts, [3*(2^n_out)] each, for inspection by tests. */

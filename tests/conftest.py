@@ -63,10 +63,11 @@ def wide_beams(n, sqrts, seed):
 def oracle_sensitivity(o, x, r, sq, E1=None, E2=None, trials=2, seed=2, nudge=2, channels=None):
     """The oracle's own change under perturbations of the size a device's rounding makes:
     one-ulp perturbations of its x inputs (each entry times 1 +- 2^-52, `trials` draws)
-    and, with per-event beams, every value a transcendental function returns on the
-    mapping path moved by +-1 ... +-`nudge` ulps (Oracle.generate(nudge=...): the per-event
-    constants such as the Breit-Wigner bound a1 = atan(u), and the maps' own tan, exp and
-    log, which a device evaluates with its own library within a few ulps of glibc's).  The
+    and every value a transcendental function returns on the mapping path moved by
+    +-1 ... +-`nudge` ulps (Oracle.generate(nudge=...): the maps' own tan, exp and log and,
+    with per-event beams, the constants formed per event such as the Breit-Wigner bound
+    a1 = atan(u), which a device evaluates with its own library within a few ulps of
+    glibc's).  The
     reference's Breit-Wigner map is ill-conditioned in both far below its pole: one ulp of
     a1 moves z and tan(z) by (1 + u^2) ulps, and msq = m (m + w tan z) cancels.  Per event
     the largest momentum change (the measure of momentum_rel_err against the event's
@@ -81,8 +82,7 @@ def oracle_sensitivity(o, x, r, sq, E1=None, E2=None, trials=2, seed=2, nudge=2,
     flips = np.zeros(n, bool)
     runs = [dict(x=x * (1 + rng.choice([-1.0, 1.0], x.shape) * 2.0 ** -52))
             for _ in range(trials)]
-    if E1 is not None:
-        runs += [dict(x=x, nudge=k * sign) for k in range(1, nudge + 1) for sign in (1, -1)]
+    runs += [dict(x=x, nudge=k * sign) for k in range(1, nudge + 1) for sign in (1, -1)]
     for kw in runs:
         q = o.generate(kw.pop("x"), channels, E1=E1, E2=E2, **kw)
         flips |= q.ok != r.ok

@@ -303,6 +303,31 @@ def test_per_event_beams_wide_energy_range(torch, builder):
     assert (np.abs(v - r.volume) / r.volume).max() < 1e-15
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("n_out", [3, 4, 5, 6, 7, 8])
+def test_every_mapping_uniform_beams(torch, n_out, precision):
+    """8 random channels of n_out particles with every mapping kind (all_maps_process) at
+    sqrt(s) = 1 TeV, FP64 and FP32 pairs: ok flags bit-exact with the oracle; momenta and
+    factors within 1e-12 (FP32 pairs 1e-7) or 64 (1024) times the oracle's own change when
+    x and the maps' tan/exp/log values move by an ulp or two (the constants are the host's
+    bits here; CUDA's and glibc's functions differ by an ulp, which a Breit-Wigner map
+    far below its pole, msq = m (m + w tan z), and the Kallen function near a threshold
+    amplify); volumes within 1e-15."""
+    from gpu_phs_gb300.api import PhaseSpace
+    proc = all_maps_process(100 + n_out, n_out, 8)
+    n = 20_000
+    counts = np.full(8, n // 8, np.int64)
+    ch = np.repeat(np.arange(8), counts).astype(np.int32)
+    x = uniform_x(700 + n_out, n, proc.n_x)
+    o = oracle.Oracle(proc, 1000.0)
+    r = o.generate(x, ch)
+    p, f, v, ok = run_gpu(torch, proc, x, 1000.0, counts, precision=precision)
+    bar, ulps = (1e-12, 64) if precision == 0 else (1e-7, 1024)
+    assert_within_conditioning(p, f, ok, o, x, r, np.full(n, 1000.0), None, None, bar, ulps,
+                               channels=ch)
+    assert (np.abs(v - r.volume) / r.volume).max() < 1e-15
+
+
 @pytest.mark.parametrize("beams", ["mid", "wide"])
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("n_out", [3, 4, 5, 6, 7, 8])
