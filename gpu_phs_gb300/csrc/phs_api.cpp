@@ -1079,7 +1079,7 @@ extern "C" int phs_generate_host(phs_process_t h, int64_t n_events, const int64_
     }
     // The volume of an event is its channel's (uniform beams: the kernels write the compiled
     // PhsChannel::volume), so the host writes it while the copies run instead of copying
-    // 8 bytes per event back: the call is bound by the host link.
+    // 8 bytes per event back across the host link, which the copies nearly fill.
     for (int c = 0; c < nch; c++) std::fill(v + prefix[c], v + prefix[c + 1], h->prog[c].volume);
     for (int s = 0; s < phs_process::kStreams; s++) CUDA_TRY(cudaStreamSynchronize(h->streams[s]));
     return PHS_OK;
